@@ -1,0 +1,169 @@
+/*
+ * cgfd3d_gpu.h -- C ABI of the GB300 (sm_103a) time-stepping library.
+ *
+ * This library replaces the time loop of CGFD3D:
+ *
+ *   void drv_rk_curv_col_allstep(fd_t*, gd_t*, gdcurv_metric_t*, md_t*,
+ *        src_t*, bdry_t*, wav_t*, mympi_t*, iorecv_t*, ioline_t*,
+ *        ioslice_t*, iosnap_t*, float dt, int nt_total, float t0, ...)
+ *   (reference: forward/drv_rk_curv_col.h:17-37, forward/drv_rk_curv_col.c:27-556)
+ *
+ * Two layers are exported:
+ *
+ *   1. the drop-in `drv_rk_curv_col_allstep` itself, built from
+ *      cgfd3d_gb300/csrc/dropin/drv_rk_curv_col_gpu.c against the reference's
+ *      own struct headers; it unpacks the reference
+ *      structs into a cgfd_problem_t and calls cgfd_allstep();
+ *   2. the flat C ABI below: plain pointers and sizes, no reference types,
+ *      so any FFI (ctypes, cgo, JNI) can bind it.
+ *
+ * Every array is a host array in the reference's layout: padded volume
+ * nx*ny*nz (ni+6, nj+6, nk+6), index i + j*nx + k*nx*ny, k upward with the
+ * free surface at k = nk2 (forward/gd_t.c:2856-2892); wavefield levels are
+ * nlevel x ncmp x volume with component order Vx,Vy,Vz,Txx,Tyy,Tzz,Tyz,Txz,Txy
+ * (forward/wav_t.c:93-136).  Errors are reported by return code (0 = ok) and
+ * cgfd_last_error(); nothing in this ABI calls exit().
+ */
+#ifndef CGFD3D_GPU_H
+#define CGFD3D_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGFD_ABI_VERSION 1
+
+/* medium types, same codes as forward/constants.h:24-29 */
+#define CGFD_MEDIUM_ELASTIC_ISO 2
+#define CGFD_MEDIUM_ELASTIC_VTI 3
+#define CGFD_MEDIUM_VISCOELASTIC_ISO 5
+#define CGFD_MAX_MAXWELL 8
+
+/* source spatial types, forward/constants.h:36-38 */
+#define CGFD_SRC_POINT 1
+#define CGFD_SRC_GAUSSIAN 2
+
+/* error codes */
+#define CGFD_OK 0
+#define CGFD_EINVAL 1      /* bad argument / unsupported configuration */
+#define CGFD_ECUDA 2       /* CUDA runtime error */
+#define CGFD_ENOMEM 3      /* device allocation failed */
+#define CGFD_ENONFINITE 4  /* NaN/Inf found by the finiteness check */
+
+/* One CFS-PML face: bdry_t.{ni1..nk2,A,B,D,auxvar}[idim][iside]
+ * (forward/bdry_t.h:86-108, forward/bdry_t.c:115-327). */
+typedef struct {
+  int enabled;                       /* is_sides_pml[idim][iside] */
+  int ni1, ni2, nj1, nj2, nk1, nk2;  /* face box, inclusive, padded indices */
+  const float *A, *B, *D;            /* length = box extent along the normal */
+  float *aux;  /* nlevel x ncmp x box volume, level order pre,tmp,rhs,end;
+                  only level 0 (pre) is read, the final state is written
+                  back to level 0 (nt_total even) or 3 (odd) like the
+                  reference's pointer swap */
+} cgfd_pml_face_t;
+
+/* Everything drv_rk_curv_col_allstep reads and writes, flattened. */
+typedef struct {
+  /* grid: gd_t (forward/gd_t.h:27-125) */
+  int ni, nj, nk, nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2;
+
+  /* metrics: gdcurv_metric_t (forward/gd_t.h:152-174), each nx*ny*nz */
+  const float *jac, *xi_x, *xi_y, *xi_z, *eta_x, *eta_y, *eta_z,
+              *zeta_x, *zeta_y, *zeta_z;
+
+  /* media: md_t (forward/md_t.h:11-73); slw is 1/rho
+   * (md_rho_to_slow, forward/md_t.c:601-623, applied before the call) */
+  int medium_type;
+  const float *slw, *lambda, *mu;                /* iso, visco */
+  const float *c11, *c13, *c33, *c55, *c66;       /* vti */
+  int nmaxwell;                                   /* visco GMB */
+  const float *wl;                                /* nmaxwell */
+  const float *Ylam[CGFD_MAX_MAXWELL], *Ymu[CGFD_MAX_MAXWELL];
+
+  /* boundaries: bdry_t (forward/bdry_t.h:66-151) */
+  int free_top;                      /* is_sides_free[2][1] */
+  cgfd_pml_face_t pml[3][2];         /* [idim][iside] */
+
+  /* sources: src_t (forward/src_t.h:21-128) */
+  int src_n, src_max_nt, src_max_stage;
+  int src_force, src_moment;         /* force_actived, moment_actived */
+  int src_spatial;                   /* itype_spatial_ext */
+  int src_ext_half;                  /* ext_half_npoint */
+  float src_ext_coef;                /* ext_func_coef (Gaussian width) */
+  int src_surface_strict;            /* is_surface_force_strict */
+  int src_n_surface_force;           /* total_number_surface_force (must be 0) */
+  const int *src_si, *src_sj, *src_sk, *src_it_begin, *src_it_end;
+  const float *src_si_inc, *src_sj_inc, *src_sk_inc;
+  const float *Fx, *Fy, *Fz;                     /* [is][it][istage] */
+  const float *Mxx, *Myy, *Mzz, *Mxz, *Myz, *Mxy;
+
+  /* station receivers: iorecv_t (forward/io_funcs.h:17-39) */
+  int recv_n, recv_max_nt, recv_ncmp;
+  const float *recv_dijk;            /* 3 per receiver: di, dj, dk */
+  const int *recv_indx1d;            /* 8 per receiver */
+  float *recv_seismo;                /* [n][ncmp][max_nt], written */
+
+  /* line receivers: ioline_t (forward/io_funcs.h:42-60), all lines
+   * concatenated */
+  int line_n, line_max_nt;
+  const int *line_iptr;              /* line_n */
+  float *line_seismo;                /* [line_n][ncmp][max_nt], written */
+
+  /* wavefield: wav_t.v5d (forward/wav_t.h:15-67) */
+  int ncmp, nlevel;
+  float *wav;  /* nlevel x ncmp x volume; level 0 read, final state written
+                  to level 0 or 3 as for the PML aux */
+
+  float dt, t0;
+  int nt_total;
+} cgfd_problem_t;
+
+/* Opaque device-resident solver. */
+typedef struct cgfd_solver cgfd_solver_t;
+
+/* Last error message of the calling thread ("" when none). */
+const char *cgfd_last_error(void);
+
+/* ABI version (CGFD_ABI_VERSION). */
+int cgfd_abi_version(void);
+
+/* Uploads every input of `p` into HBM, computes the free-surface conversion
+ * matrices on the device (forward/sv_curv_col_el_iso.c:1258-1375) and
+ * returns a solver positioned at step 0.  `p` must stay valid until
+ * cgfd_solver_destroy (host output arrays are written by cgfd_solver_fetch). */
+int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out);
+
+/* Advances `nsteps` RK4 steps on the device (no host traffic). */
+int cgfd_solver_run(cgfd_solver_t *s, int nsteps);
+
+/* Copies the current wavefield (into p->wav level 0 or 3, as the reference
+ * leaves it), PML aux and seismograms back into the host arrays of `p`. */
+int cgfd_solver_fetch(cgfd_solver_t *s);
+
+/* Current step index. */
+int cgfd_solver_step(const cgfd_solver_t *s);
+
+/* Checks the whole wavefield for NaN/Inf on the device.
+ * Returns CGFD_OK or CGFD_ENONFINITE. */
+int cgfd_solver_check_finite(cgfd_solver_t *s);
+
+/* Sum of CUDA-event time of the last cgfd_solver_run, per kernel family:
+ * out[0] = interior launches, out[1] = surface launches, out[2] = other;
+ * count[] the launches.  Units: milliseconds. */
+int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3]);
+
+void cgfd_solver_destroy(cgfd_solver_t *s);
+
+/* One-shot equivalent of drv_rk_curv_col_allstep on flat arrays:
+ * create + run(nt_total) + fetch + destroy. */
+int cgfd_allstep(const cgfd_problem_t *p);
+
+/* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
+size_t cgfd_device_bytes(const cgfd_problem_t *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,797 @@
+/*
+ * cgfd_oracle.c -- CPU restatement of the CGFD3D time-stepping hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU library is
+ * compared against: tests/, __graft_entry__.smoke() and the cpu_baseline leg
+ * of bench.py may load it; the product path never does.
+ *
+ * It restates, for the flat problem description of include/cgfd3d_gpu.h,
+ * what the reference's drv_rk_curv_col_allstep does for isotropic elastic
+ * media (the float arithmetic is ordered as in the reference so that the
+ * results are bit-identical to the reference's own CPU build, which is
+ * checked against the golden fixtures under tests/golden/):
+ *
+ *   time loop, pair/stage schedule, RK4 combine
+ *                        forward/drv_rk_curv_col.c:167-544, fd_t.c:36-49,182-289
+ *   operator tables      forward/fd_t.c:75-122 (MacCormack DRP + surface ops)
+ *   interior RHS         forward/sv_curv_col_el_iso.c:208-441
+ *   traction image       forward/sv_curv_col_el.c:30-305
+ *   velocity "vlow"      forward/sv_curv_col_el_iso.c:451-634
+ *   ADE CFS-PML          forward/sv_curv_col_el_iso.c:644-1146
+ *   source injection     forward/sv_curv_col_el.c:311-479, src_t.c:2111-2151
+ *   receivers / lines    forward/io_funcs.c:1584-1645
+ *   free-surface matrices forward/sv_curv_col_el_iso.c:1258-1375,
+ *                        lib/fdlib_math.c:8-48
+ *
+ * Multi-threaded with pthreads (one slab of k-planes per thread) so that it
+ * can serve as the host-core baseline.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "cgfd3d_gpu.h"
+
+/* ------------------------------------------------------------------------ */
+/* operator tables                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* bias 0: taps at -1..3; bias 1: taps at -3..1 (fd_t.c:75-122, layer 3) */
+static const int OP_SHIFT[2][5] = {{-1, 0, 1, 2, 3}, {-3, -2, -1, 0, 1}};
+static const float OP_COEF[2][5] = {
+  {-0.30874f, -0.6326f, 1.233f, -0.3334f, 0.04168f},
+  {-0.04168f, 0.3334f, -1.233f, 0.6326f, 0.30874f}};
+/* z operators of the two layers below the surface (fd_t.c:81-99):
+ * layer 1 (k = nk2-1) second order, layer 2 (k = nk2-2) fourth order */
+static const int OPZ1_SHIFT[2][2] = {{0, 1}, {-1, 0}};
+static const float OPZ1_COEF[2][2] = {{-1.0f, 1.0f}, {-1.0f, 1.0f}};
+static const int OPZ2_SHIFT[2][3] = {{0, 1, 2}, {-2, -1, 0}};
+static const float OPZ2_COEF[2][3] = {
+  {(float)(-7.0 / 6.0), (float)(8.0 / 6.0), (float)(-1.0 / 6.0)},
+  {(float)(1.0 / 6.0), (float)(-8.0 / 6.0), (float)(7.0 / 6.0)}};
+/* forward/backward flags of the 8 pairs (fd_t.c:185-195) */
+static const int PAIR_FLAGS[8][3] = {{0, 0, 0}, {1, 1, 0}, {1, 1, 1}, {0, 0, 1},
+                                     {0, 1, 0}, {1, 0, 0}, {1, 0, 1}, {0, 1, 1}};
+static const float RK_A[3] = {0.5f, 0.5f, 1.0f};
+static const float RK_B[4] = {(float)(1.0 / 6.0), (float)(1.0 / 3.0),
+                              (float)(1.0 / 3.0), (float)(1.0 / 6.0)};
+
+/* 5-tap derivative, evaluated left to right as in M_FD_SHIFT_PTR_MACDRP */
+static inline float d5(const float *p, const float *c, long s0, long s1,
+                       long s2, long s3, long s4)
+{
+  return c[0] * p[s0] + c[1] * p[s1] + c[2] * p[s2] + c[3] * p[s3] +
+         c[4] * p[s4];
+}
+
+typedef struct {
+  const float *c;
+  long s[5];
+} op5_t;
+
+static op5_t make_op(int bias, long stride)
+{
+  op5_t o;
+  o.c = OP_COEF[bias];
+  for (int n = 0; n < 5; n++) o.s[n] = OP_SHIFT[bias][n] * stride;
+  return o;
+}
+
+static inline float D5(const op5_t *o, const float *p)
+{
+  return d5(p, o->c, o->s[0], o->s[1], o->s[2], o->s[3], o->s[4]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* state                                                                    */
+/* ------------------------------------------------------------------------ */
+
+enum { VX, VY, VZ, TXX, TYY, TZZ, TYZ, TXZ, TXY };
+
+typedef struct {
+  const cgfd_problem_t *p;
+  size_t vol, sl, ln;        /* volume, slice, line strides */
+  float *lev[4];             /* pre, tmp, rhs, end (rotating pre/end) */
+  float *aux[3][2][4];
+  size_t aux_vol[3][2];
+  float *mVx, *mVy, *mF;     /* free-surface matrices, 9 per (i,j) */
+  float **ext;               /* per source Gaussian weights (or NULL) */
+  int nthreads;
+  int timg_mode;
+  pthread_barrier_t bar;
+} orc_t;
+
+typedef struct {
+  orc_t *o;
+  int tid;
+} thr_t;
+
+static inline float lam2mu_of(float lam, float mu)
+{
+  return (float)((double)lam + 2.0 * (double)mu);
+}
+
+/* ------------------------------------------------------------------------ */
+/* free-surface conversion matrices                                          */
+/* ------------------------------------------------------------------------ */
+
+static void inv3(float m[3][3])
+{
+  float v[3][3];
+  v[0][0] = m[1][1] * m[2][2] - m[2][1] * m[1][2];
+  v[0][1] = m[2][1] * m[0][2] - m[0][1] * m[2][2];
+  v[0][2] = m[0][1] * m[1][2] - m[0][2] * m[1][1];
+  v[1][0] = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+  v[1][1] = m[0][0] * m[2][2] - m[2][0] * m[0][2];
+  v[1][2] = m[1][0] * m[0][2] - m[0][0] * m[1][2];
+  v[2][0] = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+  v[2][1] = m[2][0] * m[0][1] - m[0][0] * m[2][1];
+  v[2][2] = m[0][0] * m[1][1] - m[0][1] * m[1][0];
+  float det = v[0][0] * m[0][0] + v[0][1] * m[1][0] + v[0][2] * m[2][0];
+  det = 1.0f / det;
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) m[a][b] = v[a][b] * det;
+}
+
+static void mul3(float A[3][3], float B[3][3], float C[3][3])
+{
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) {
+      C[a][b] = 0.0f;
+      for (int k = 0; k < 3; k++) C[a][b] += A[a][k] * B[k][b];
+    }
+}
+
+/* matVx2Vz = A^-1 B, matVy2Vz = A^-1 C, matF2Vz = A^-1 at k = nk2 */
+int oracle_dvh2dvz_iso(const cgfd_problem_t *p, float *mVx, float *mVy,
+                       float *mF)
+{
+  size_t ln = p->nx, sl = (size_t)p->nx * p->ny;
+  int k = p->nk2;
+  for (int j = p->nj1; j <= p->nj2; j++)
+    for (int i = p->ni1; i <= p->ni2; i++) {
+      size_t q = i + j * ln + k * sl;
+      float e11 = p->xi_x[q], e12 = p->xi_y[q], e13 = p->xi_z[q];
+      float e21 = p->eta_x[q], e22 = p->eta_y[q], e23 = p->eta_z[q];
+      float e31 = p->zeta_x[q], e32 = p->zeta_y[q], e33 = p->zeta_z[q];
+      float lam = p->lambda[q], mu = p->mu[q];
+      float l2m = lam + 2.0f * mu;
+      float A[3][3], B[3][3], C[3][3], AB[3][3], AC[3][3];
+      A[0][0] = l2m * e31 * e31 + mu * (e32 * e32 + e33 * e33);
+      A[0][1] = lam * e31 * e32 + mu * e32 * e31;
+      A[0][2] = lam * e31 * e33 + mu * e33 * e31;
+      A[1][0] = lam * e32 * e31 + mu * e31 * e32;
+      A[1][1] = l2m * e32 * e32 + mu * (e31 * e31 + e33 * e33);
+      A[1][2] = lam * e32 * e33 + mu * e33 * e32;
+      A[2][0] = lam * e33 * e31 + mu * e31 * e33;
+      A[2][1] = lam * e33 * e32 + mu * e32 * e33;
+      A[2][2] = l2m * e33 * e33 + mu * (e31 * e31 + e32 * e32);
+      inv3(A);
+      B[0][0] = -l2m * e31 * e11 - mu * (e32 * e12 + e33 * e13);
+      B[0][1] = -lam * e31 * e12 - mu * e32 * e11;
+      B[0][2] = -lam * e31 * e13 - mu * e33 * e11;
+      B[1][0] = -lam * e32 * e11 - mu * e31 * e12;
+      B[1][1] = -l2m * e32 * e12 - mu * (e31 * e11 + e33 * e13);
+      B[1][2] = -lam * e32 * e13 - mu * e33 * e12;
+      B[2][0] = -lam * e33 * e11 - mu * e31 * e13;
+      B[2][1] = -lam * e33 * e12 - mu * e32 * e13;
+      B[2][2] = -l2m * e33 * e13 - mu * (e31 * e11 + e32 * e12);
+      C[0][0] = -l2m * e31 * e21 - mu * (e32 * e22 + e33 * e23);
+      C[0][1] = -lam * e31 * e22 - mu * e32 * e21;
+      C[0][2] = -lam * e31 * e23 - mu * e33 * e21;
+      C[1][0] = -lam * e32 * e21 - mu * e31 * e22;
+      C[1][1] = -l2m * e32 * e22 - mu * (e31 * e21 + e33 * e23);
+      C[1][2] = -lam * e32 * e23 - mu * e33 * e22;
+      C[2][0] = -lam * e33 * e21 - mu * e31 * e23;
+      C[2][1] = -lam * e33 * e22 - mu * e32 * e23;
+      C[2][2] = -l2m * e33 * e23 - mu * (e31 * e21 + e32 * e22);
+      mul3(A, B, AB);
+      mul3(A, C, AC);
+      size_t ij = (j * ln + i) * 9;
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+          mVx[ij + r * 3 + c] = AB[r][c];
+          mVy[ij + r * 3 + c] = AC[r][c];
+          mF[ij + r * 3 + c] = A[r][c];
+        }
+    }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* RHS passes                                                               */
+/* ------------------------------------------------------------------------ */
+
+/* interior RHS of one k-plane (sv_curv_col_el_iso.c:304-440) */
+static void rhs_inner_plane(orc_t *o, const float *w, float *h, int k,
+                            const op5_t *ox, const op5_t *oy, const op5_t *oz)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t V = o->vol;
+  const float *Vx = w + VX * V, *Vy = w + VY * V, *Vz = w + VZ * V;
+  const float *Txx = w + TXX * V, *Tyy = w + TYY * V, *Tzz = w + TZZ * V;
+  const float *Tyz = w + TYZ * V, *Txz = w + TXZ * V, *Txy = w + TXY * V;
+  for (int j = p->nj1; j <= p->nj2; j++) {
+    size_t q = p->ni1 + j * o->ln + (size_t)k * o->sl;
+    for (int i = p->ni1; i <= p->ni2; i++, q++) {
+      float DxVx = D5(ox, Vx + q), DyVx = D5(oy, Vx + q), DzVx = D5(oz, Vx + q);
+      float DxVy = D5(ox, Vy + q), DyVy = D5(oy, Vy + q), DzVy = D5(oz, Vy + q);
+      float DxVz = D5(ox, Vz + q), DyVz = D5(oy, Vz + q), DzVz = D5(oz, Vz + q);
+      float DxTxx = D5(ox, Txx + q), DyTxx = D5(oy, Txx + q), DzTxx = D5(oz, Txx + q);
+      float DxTyy = D5(ox, Tyy + q), DyTyy = D5(oy, Tyy + q), DzTyy = D5(oz, Tyy + q);
+      float DxTzz = D5(ox, Tzz + q), DyTzz = D5(oy, Tzz + q), DzTzz = D5(oz, Tzz + q);
+      float DxTxz = D5(ox, Txz + q), DyTxz = D5(oy, Txz + q), DzTxz = D5(oz, Txz + q);
+      float DxTyz = D5(ox, Tyz + q), DyTyz = D5(oy, Tyz + q), DzTyz = D5(oz, Tyz + q);
+      float DxTxy = D5(ox, Txy + q), DyTxy = D5(oy, Txy + q), DzTxy = D5(oz, Txy + q);
+      float xix = p->xi_x[q], xiy = p->xi_y[q], xiz = p->xi_z[q];
+      float etx = p->eta_x[q], ety = p->eta_y[q], etz = p->eta_z[q];
+      float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
+      float lam = p->lambda[q], mu = p->mu[q], slw = p->slw[q];
+      float l2m = lam2mu_of(lam, mu);
+      h[VX * V + q] = slw * (xix * DxTxx + xiy * DxTxy + xiz * DxTxz +
+                             etx * DyTxx + ety * DyTxy + etz * DyTxz +
+                             ztx * DzTxx + zty * DzTxy + ztz * DzTxz);
+      h[VY * V + q] = slw * (xix * DxTxy + xiy * DxTyy + xiz * DxTyz +
+                             etx * DyTxy + ety * DyTyy + etz * DyTyz +
+                             ztx * DzTxy + zty * DzTyy + ztz * DzTyz);
+      h[VZ * V + q] = slw * (xix * DxTxz + xiy * DxTyz + xiz * DxTzz +
+                             etx * DyTxz + ety * DyTyz + etz * DyTzz +
+                             ztx * DzTxz + zty * DzTyz + ztz * DzTzz);
+      h[TXX * V + q] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
+                       lam * (xiy * DxVy + ety * DyVy + zty * DzVy +
+                              xiz * DxVz + etz * DyVz + ztz * DzVz);
+      h[TYY * V + q] = l2m * (xiy * DxVy + ety * DyVy + zty * DzVy) +
+                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
+                              xiz * DxVz + etz * DyVz + ztz * DzVz);
+      h[TZZ * V + q] = l2m * (xiz * DxVz + etz * DyVz + ztz * DzVz) +
+                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
+                              xiy * DxVy + ety * DyVy + zty * DzVy);
+      h[TXY * V + q] = mu * (xiy * DxVx + xix * DxVy + ety * DyVx +
+                             etx * DyVy + zty * DzVx + ztx * DzVy);
+      h[TXZ * V + q] = mu * (xiz * DxVx + xix * DxVz + etz * DyVx +
+                             etx * DyVz + ztz * DzVx + ztx * DzVz);
+      h[TYZ * V + q] = mu * (xiz * DxVy + xiy * DxVz + etz * DyVy +
+                             ety * DyVz + ztz * DzVy + zty * DzVz);
+    }
+  }
+}
+
+/* conservative traction term J * (m . T) at one point, for one momentum row */
+static inline float cons(const float *jac, const float *mx, const float *my,
+                         const float *mz, const float *Ta, const float *Tb,
+                         const float *Tc, size_t q)
+{
+  return jac[q] * (mx[q] * Ta[q] + my[q] * Tb[q] + mz[q] * Tc[q]);
+}
+
+/*
+ * Traction image for the top layers of row j (sv_curv_col_el.c:84-304).
+ * Above the surface the conservative z-flux is mirrored:
+ * vec[n] = 2 T_surf - vec[2 n_free - n].  At k = nk2 with the taps at -1..3
+ * the mirror needs n = -1, -2, i.e. values of the points k-2, k-3 that the
+ * reference never computes: it reads past the start of its local array.
+ * timg_mode chooses what stands there: 0 = zero (the value that array slot
+ * holds in the reference build this oracle is pinned against), 1 = the
+ * conservative value at k-2/k-3 (the mirror the formula intends).
+ */
+static void rhs_timg_row(orc_t *o, const float *w, float *h, int j, int zbias,
+                         const op5_t *ox, const op5_t *oy)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t V = o->vol, ln = o->ln, sl = o->sl;
+  const float *T[9];
+  for (int c = 0; c < 9; c++) T[c] = w + c * V;
+  const int *zs = OP_SHIFT[zbias];
+  const float *zc = OP_COEF[zbias];
+  int k_min = p->nk2 - zs[4];
+  /* momentum rows: (x-flux metric set) x (stress triplet) */
+  const int rowT[3][3] = {{TXX, TXY, TXZ}, {TXY, TYY, TYZ}, {TXZ, TYZ, TZZ}};
+  for (int k = k_min; k <= p->nk2; k++) {
+    int n_free = p->nk2 - k - zs[0];
+    size_t q = p->ni1 + j * ln + (size_t)k * sl;
+    for (int i = p->ni1; i <= p->ni2; i++, q++) {
+      float slwjac = p->slw[q] / p->jac[q];
+      for (int r = 0; r < 3; r++) {
+        const float *Ta = T[rowT[r][0]], *Tb = T[rowT[r][1]], *Tc = T[rowT[r][2]];
+        float vx[5], vy[5], vzb[7];
+        float *vz = vzb + 2; /* vz[-2], vz[-1] addressable */
+        for (int n = 0; n < 5; n++) {
+          vx[n] = cons(p->jac, p->xi_x, p->xi_y, p->xi_z, Ta, Tb, Tc, q + ox->s[n]);
+          vy[n] = cons(p->jac, p->eta_x, p->eta_y, p->eta_z, Ta, Tb, Tc, q + oy->s[n]);
+        }
+        for (int n = 0; n < n_free; n++)
+          vz[n] = cons(p->jac, p->zeta_x, p->zeta_y, p->zeta_z, Ta, Tb, Tc,
+                       q + zs[n] * (long)sl);
+        if (o->timg_mode == 1) {
+          for (int n = -2; n < 0; n++)
+            vz[n] = cons(p->jac, p->zeta_x, p->zeta_y, p->zeta_z, Ta, Tb, Tc,
+                         q + (zs[0] + n) * (long)sl);
+        } else {
+          vz[-2] = 0.0f;
+          vz[-1] = 0.0f;
+        }
+        float tsurf = 0.0f; /* TxSrc/TySrc/TzSrc: no surface force */
+        vz[n_free] = tsurf;
+        for (int n = n_free + 1; n < 5; n++)
+          vz[n] = (float)(2.0 * (double)tsurf - (double)vz[2 * n_free - n]);
+        float Dx = ox->c[0] * vx[0];
+        for (int n = 1; n < 5; n++) Dx += ox->c[n] * vx[n];
+        float Dy = oy->c[0] * vy[0];
+        for (int n = 1; n < 5; n++) Dy += oy->c[n] * vy[n];
+        float Dz = zc[0] * vz[0];
+        for (int n = 1; n < 5; n++) Dz += zc[n] * vz[n];
+        h[(VX + r) * V + q] = (Dx + Dy + Dz) * slwjac;
+      }
+    }
+  }
+}
+
+/* velocity-gradient conversion on the top three layers of row j
+ * (sv_curv_col_el_iso.c:501-633) */
+static void rhs_vlow_row(orc_t *o, const float *w, float *h, int j, int zbias,
+                         const op5_t *ox, const op5_t *oy)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t V = o->vol, ln = o->ln, sl = o->sl;
+  const float *Vx = w + VX * V, *Vy = w + VY * V, *Vz = w + VZ * V;
+  for (int n = 0; n < 3; n++) {
+    int k = p->nk2 - n;
+    size_t q = p->ni1 + j * ln + (size_t)k * sl;
+    for (int i = p->ni1; i <= p->ni2; i++, q++) {
+      float xix = p->xi_x[q], xiy = p->xi_y[q], xiz = p->xi_z[q];
+      float etx = p->eta_x[q], ety = p->eta_y[q], etz = p->eta_z[q];
+      float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
+      float lam = p->lambda[q], mu = p->mu[q];
+      float l2m = lam2mu_of(lam, mu);
+      float DxVx = D5(ox, Vx + q), DyVx = D5(oy, Vx + q);
+      float DxVy = D5(ox, Vy + q), DyVy = D5(oy, Vy + q);
+      float DxVz = D5(ox, Vz + q), DyVz = D5(oy, Vz + q);
+      float DzVx, DzVy, DzVz;
+      if (n == 0) {
+        size_t ij = (i + j * ln) * 9;
+        const float *a = o->mVx + ij, *b = o->mVy + ij;
+        DzVx = a[0] * DxVx + a[1] * DxVy + a[2] * DxVz + b[0] * DyVx +
+               b[1] * DyVy + b[2] * DyVz;
+        DzVy = a[3] * DxVx + a[4] * DxVy + a[5] * DxVz + b[3] * DyVx +
+               b[4] * DyVy + b[5] * DyVz;
+        DzVz = a[6] * DxVx + a[7] * DxVy + a[8] * DxVz + b[6] * DyVx +
+               b[7] * DyVy + b[8] * DyVz;
+        /* + matF2Vz * (VxSrc,VySrc,VzSrc): zero without surface forces */
+        const float *f = o->mF + ij;
+        DzVx += f[0] * 0.0f + f[1] * 0.0f + f[2] * 0.0f;
+        DzVy += f[3] * 0.0f + f[4] * 0.0f + f[5] * 0.0f;
+        DzVz += f[6] * 0.0f + f[7] * 0.0f + f[8] * 0.0f;
+      } else if (n == 1) {
+        long s0 = OPZ1_SHIFT[zbias][0] * (long)sl, s1 = OPZ1_SHIFT[zbias][1] * (long)sl;
+        const float *c = OPZ1_COEF[zbias];
+        DzVx = c[0] * Vx[q + s0]; DzVx += c[1] * Vx[q + s1];
+        DzVy = c[0] * Vy[q + s0]; DzVy += c[1] * Vy[q + s1];
+        DzVz = c[0] * Vz[q + s0]; DzVz += c[1] * Vz[q + s1];
+      } else {
+        long s0 = OPZ2_SHIFT[zbias][0] * (long)sl, s1 = OPZ2_SHIFT[zbias][1] * (long)sl,
+             s2 = OPZ2_SHIFT[zbias][2] * (long)sl;
+        const float *c = OPZ2_COEF[zbias];
+        DzVx = c[0] * Vx[q + s0]; DzVx += c[1] * Vx[q + s1]; DzVx += c[2] * Vx[q + s2];
+        DzVy = c[0] * Vy[q + s0]; DzVy += c[1] * Vy[q + s1]; DzVy += c[2] * Vy[q + s2];
+        DzVz = c[0] * Vz[q + s0]; DzVz += c[1] * Vz[q + s1]; DzVz += c[2] * Vz[q + s2];
+      }
+      h[TXX * V + q] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
+                       lam * (xiy * DxVy + ety * DyVy + zty * DzVy +
+                              xiz * DxVz + etz * DyVz + ztz * DzVz);
+      h[TYY * V + q] = l2m * (xiy * DxVy + ety * DyVy + zty * DzVy) +
+                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
+                              xiz * DxVz + etz * DyVz + ztz * DzVz);
+      h[TZZ * V + q] = l2m * (xiz * DxVz + etz * DyVz + ztz * DzVz) +
+                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
+                              xiy * DxVy + ety * DyVy + zty * DzVy);
+      h[TXY * V + q] = mu * (xiy * DxVx + xix * DxVy + ety * DyVx +
+                             etx * DyVy + zty * DzVx + ztx * DzVy);
+      h[TXZ * V + q] = mu * (xiz * DxVx + xix * DxVz + etz * DyVx +
+                             etx * DyVz + ztz * DzVx + ztx * DzVz);
+      h[TYZ * V + q] = mu * (xiz * DxVy + xiy * DxVz + etz * DyVy +
+                             ety * DyVz + ztz * DzVy + zty * DzVz);
+    }
+  }
+}
+
+/* CFS-PML corrections of one face for the points of plane k
+ * (sv_curv_col_el_iso.c:708-1143) */
+static void rhs_pml_face_plane(orc_t *o, const float *w, float *h, int idim,
+                               int iside, int k, const op5_t *op,
+                               const float *acur, float *arhs)
+{
+  const cgfd_problem_t *p = o->p;
+  const cgfd_pml_face_t *f = &p->pml[idim][iside];
+  size_t V = o->vol, ln = o->ln, sl = o->sl;
+  int nbx = f->ni2 - f->ni1 + 1, nby = f->nj2 - f->nj1 + 1;
+  size_t AV = o->aux_vol[idim][iside];
+  const float *m1, *m2, *m3;
+  if (idim == 0) { m1 = p->xi_x; m2 = p->xi_y; m3 = p->xi_z; }
+  else if (idim == 1) { m1 = p->eta_x; m2 = p->eta_y; m3 = p->eta_z; }
+  else { m1 = p->zeta_x; m2 = p->zeta_y; m3 = p->zeta_z; }
+  const float *W[9];
+  for (int c = 0; c < 9; c++) W[c] = w + c * V;
+  for (int j = f->nj1; j <= f->nj2; j++) {
+    for (int i = f->ni1; i <= f->ni2; i++) {
+      size_t q = i + j * ln + (size_t)k * sl;
+      size_t a = (size_t)(i - f->ni1) + (size_t)(j - f->nj1) * nbx +
+                 (size_t)(k - f->nk1) * nbx * nby;
+      int n = idim == 0 ? i - f->ni1 : (idim == 1 ? j - f->nj1 : k - f->nk1);
+      float cD = f->D[n], cA = f->A[n], cB = f->B[n];
+      float cB1 = (float)((double)cB - 1.0);
+      float e1 = m1[q], e2 = m2[q], e3 = m3[q];
+      float lam = p->lambda[q], mu = p->mu[q], slw = p->slw[q];
+      float l2m = lam2mu_of(lam, mu);
+      float DVx = D5(op, W[VX] + q), DVy = D5(op, W[VY] + q), DVz = D5(op, W[VZ] + q);
+      float DTxx = D5(op, W[TXX] + q), DTyy = D5(op, W[TYY] + q),
+            DTzz = D5(op, W[TZZ] + q), DTxz = D5(op, W[TXZ] + q),
+            DTyz = D5(op, W[TYZ] + q), DTxy = D5(op, W[TXY] + q);
+      float r[9];
+      r[VX] = slw * (e1 * DTxx + e2 * DTxy + e3 * DTxz);
+      r[VY] = slw * (e1 * DTxy + e2 * DTyy + e3 * DTyz);
+      r[VZ] = slw * (e1 * DTxz + e2 * DTyz + e3 * DTzz);
+      r[TXX] = l2m * e1 * DVx + lam * e2 * DVy + lam * e3 * DVz;
+      r[TYY] = lam * e1 * DVx + l2m * e2 * DVy + lam * e3 * DVz;
+      r[TZZ] = lam * e1 * DVx + lam * e2 * DVy + l2m * e3 * DVz;
+      r[TXY] = mu * (e2 * DVx + e1 * DVy);
+      r[TXZ] = mu * (e3 * DVx + e1 * DVz);
+      r[TYZ] = mu * (e3 * DVy + e2 * DVz);
+      /* same component order of updates as the reference */
+      static const int ord[9] = {VX, VY, VZ, TXX, TYY, TZZ, TXZ, TYZ, TXY};
+      for (int m = 0; m < 9; m++) {
+        int c = ord[m];
+        h[c * V + q] += cB1 * r[c] - cB * acur[c * AV + a];
+      }
+      for (int m = 0; m < 9; m++) {
+        int c = ord[m];
+        arhs[c * AV + a] = cD * r[c] - cA * acur[c * AV + a];
+      }
+      if (idim < 2 && p->free_top && k == p->nk2) {
+        size_t ij = (i + j * ln) * 9;
+        const float *M = (idim == 0 ? o->mVx : o->mVy) + ij;
+        float DzVx = M[0] * DVx + M[1] * DVy + M[2] * DVz;
+        float DzVy = M[3] * DVx + M[4] * DVy + M[5] * DVz;
+        float DzVz = M[6] * DVx + M[7] * DVy + M[8] * DVz;
+        float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
+        float s[9];
+        s[TXX] = l2m * (ztx * DzVx) + lam * (zty * DzVy + ztz * DzVz);
+        s[TYY] = l2m * (zty * DzVy) + lam * (ztx * DzVx + ztz * DzVz);
+        s[TZZ] = l2m * (ztz * DzVz) + lam * (ztx * DzVx + zty * DzVy);
+        s[TXY] = mu * (zty * DzVx + ztx * DzVy);
+        s[TXZ] = mu * (ztz * DzVx + ztx * DzVz);
+        s[TYZ] = mu * (ztz * DzVy + zty * DzVz);
+        static const int ordT[6] = {TXX, TYY, TZZ, TXZ, TYZ, TXY};
+        for (int m = 0; m < 6; m++) {
+          int c = ordT[m];
+          h[c * V + q] = (float)((double)h[c * V + q] +
+                                 ((double)cB - 1.0) * (double)s[c]);
+        }
+        for (int m = 0; m < 6; m++) {
+          int c = ordT[m];
+          arhs[c * AV + a] += cD * s[c];
+        }
+      }
+    }
+  }
+}
+
+/* Gaussian weights normalised over the points at or below the surface
+ * (src_t.c:2111-2151; fun_gauss src_t.c:2179) */
+static float gauss1(float t, float a)
+{
+  float tt = t - 0.0f;
+  float e = (-tt) * tt / (a * a);
+  float den = sqrtf((float)3.14159265358979323846) * a;
+  return (float)(exp((double)e) / (double)den);
+}
+
+static void src_weights(float *delt, float x0, float y0, float z0, float r,
+                        int half, int half_z2)
+{
+  int idx = 0;
+  for (int k = -half; k <= half; k++)
+    for (int j = -half; j <= half; j++)
+      for (int i = -half; i <= half; i++) {
+        float D1 = gauss1(i - x0, r), D2 = gauss1(j - y0, r), D3 = gauss1(k - z0, r);
+        delt[idx++] = D1 * D2 * D3;
+      }
+  float sum = 0.0f;
+  idx = 0;
+  for (int k = -half; k <= half_z2; k++)
+    for (int j = -half; j <= half; j++)
+      for (int i = -half; i <= half; i++) sum += delt[idx++];
+  int n1 = 2 * half + 1;
+  for (int m = 0; m < n1 * n1 * n1; m++) delt[m] /= sum;
+}
+
+/* source injection (sv_curv_col_el.c:350-476) */
+static void rhs_src(orc_t *o, float *h, int it, int istage)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t V = o->vol, ln = o->ln, sl = o->sl;
+  for (int is = 0; is < p->src_n; is++) {
+    if (it < p->src_it_begin[is] || it > p->src_it_end[is]) continue;
+    size_t t = (size_t)is * p->src_max_nt * p->src_max_stage +
+               (size_t)(it - p->src_it_begin[is]) * p->src_max_stage + istage;
+    float fx = 0, fy = 0, fz = 0, Mxx = 0, Myy = 0, Mzz = 0, Mxz = 0, Myz = 0, Mxy = 0;
+    if (p->src_force) { fx = p->Fx[t]; fy = p->Fy[t]; fz = p->Fz[t]; }
+    if (p->src_moment) {
+      Mxx = p->Mxx[t]; Myy = p->Myy[t]; Mzz = p->Mzz[t];
+      Mxz = p->Mxz[t]; Myz = p->Myz[t]; Mxy = p->Mxy[t];
+    }
+    int si = p->src_si[is], sj = p->src_sj[is], sk = p->src_sk[is];
+    if (p->src_spatial == CGFD_SRC_POINT) {
+      size_t q = si + sj * ln + (size_t)sk * sl;
+      if (p->src_force && (p->src_surface_strict == 0 || sk < p->nk2)) {
+        float Vf = p->slw[q] / p->jac[q];
+        h[VX * V + q] += fx * Vf;
+        h[VY * V + q] += fy * Vf;
+        h[VZ * V + q] += fz * Vf;
+      }
+      if (p->src_moment) {
+        float rjac = (float)(1.0 / (double)p->jac[q]);
+        h[TXX * V + q] -= Mxx * rjac;
+        h[TYY * V + q] -= Myy * rjac;
+        h[TZZ * V + q] -= Mzz * rjac;
+        h[TXZ * V + q] -= Mxz * rjac;
+        h[TYZ * V + q] -= Myz * rjac;
+        h[TXY * V + q] -= Mxy * rjac;
+      }
+    } else {
+      int half = p->src_ext_half;
+      int kz2 = (sk + half < p->nk2) ? half : p->nk2 - sk;
+      const float *wgt = o->ext[is];
+      int idx = 0;
+      for (int kk = -half; kk <= kz2; kk++)
+        for (int jj = -half; jj <= half; jj++)
+          for (int ii = -half; ii <= half; ii++, idx++) {
+            int i = si + ii, j = sj + jj, k = sk + kk;
+            if (i < p->ni1 || i > p->ni2 || j < p->nj1 || j > p->nj2 ||
+                k < p->nk1 || k > p->nk2)
+              continue;
+            size_t q = i + j * ln + (size_t)k * sl;
+            float c = wgt[idx];
+            if (p->src_force && (p->src_surface_strict == 0 || k < p->nk2)) {
+              float Vf = c * p->slw[q] / p->jac[q];
+              h[VX * V + q] += fx * Vf;
+              h[VY * V + q] += fy * Vf;
+              h[VZ * V + q] += fz * Vf;
+            }
+            if (p->src_moment) {
+              float rjac = c / p->jac[q];
+              h[TXX * V + q] -= Mxx * rjac;
+              h[TYY * V + q] -= Myy * rjac;
+              h[TZZ * V + q] -= Mzz * rjac;
+              h[TXZ * V + q] -= Mxz * rjac;
+              h[TYZ * V + q] -= Myz * rjac;
+              h[TXY * V + q] -= Mxy * rjac;
+            }
+          }
+    }
+  }
+}
+
+/* receivers (io_funcs.c:1584-1645), including the reference's use of
+ * corner 5 twice and corner 4 never */
+static void keep_recv(orc_t *o, const float *w, int it)
+{
+  const cgfd_problem_t *p = o->p;
+  for (int n = 0; n < p->recv_n; n++) {
+    const int *x = p->recv_indx1d + 8 * n;
+    float Lx2 = p->recv_dijk[3 * n], Ly2 = p->recv_dijk[3 * n + 1],
+          Lz2 = p->recv_dijk[3 * n + 2];
+    float Lx1 = (float)(1.0 - (double)Lx2), Ly1 = (float)(1.0 - (double)Ly2),
+          Lz1 = (float)(1.0 - (double)Lz2);
+    for (int c = 0; c < p->recv_ncmp; c++) {
+      const float *v = w + c * o->vol;
+      p->recv_seismo[((size_t)n * p->recv_ncmp + c) * p->recv_max_nt + it] =
+          v[x[0]] * Lx1 * Ly1 * Lz1 + v[x[1]] * Lx2 * Ly1 * Lz1 +
+          v[x[2]] * Lx1 * Ly2 * Lz1 + v[x[3]] * Lx2 * Ly2 * Lz1 +
+          v[x[5]] * Lx1 * Ly1 * Lz2 + v[x[5]] * Lx2 * Ly1 * Lz2 +
+          v[x[6]] * Lx1 * Ly2 * Lz2 + v[x[7]] * Lx2 * Ly2 * Lz2;
+    }
+  }
+  for (int n = 0; n < p->line_n; n++)
+    for (int c = 0; c < p->ncmp; c++)
+      p->line_seismo[((size_t)n * p->ncmp + c) * p->line_max_nt + it] =
+          w[c * o->vol + p->line_iptr[n]];
+}
+
+/* ------------------------------------------------------------------------ */
+/* time loop                                                                */
+/* ------------------------------------------------------------------------ */
+
+static void slab(const orc_t *o, int tid, long n0, long n1, long *a, long *b)
+{
+  long n = n1 - n0, T = o->nthreads;
+  *a = n0 + n * tid / T;
+  *b = n0 + n * (tid + 1) / T;
+}
+
+static void *worker(void *arg)
+{
+  thr_t *th = (thr_t *)arg;
+  orc_t *o = th->o;
+  const cgfd_problem_t *p = o->p;
+  int tid = th->tid;
+  size_t V = o->vol;
+  size_t L = V * p->ncmp;
+  float *pre = o->lev[0], *tmp = o->lev[1], *rhs = o->lev[2], *end = o->lev[3];
+  float *apre[3][2], *atmp[3][2], *arhs[3][2], *aend[3][2];
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      apre[d][s] = o->aux[d][s][0]; atmp[d][s] = o->aux[d][s][1];
+      arhs[d][s] = o->aux[d][s][2]; aend[d][s] = o->aux[d][s][3];
+    }
+  long k0, k1, e0, e1;
+  slab(o, tid, p->nk1, p->nk2 + 1, &k0, &k1);
+  slab(o, tid, 0, (long)L, &e0, &e1);
+
+  for (int it = 0; it < p->nt_total; it++) {
+    int ipair = it % 8;
+    for (int is = 0; is < 4; is++) {
+      const float *cur = (is == 0) ? pre : tmp;
+      int bx = (PAIR_FLAGS[ipair][0] + is) % 2;
+      int by = (PAIR_FLAGS[ipair][1] + is) % 2;
+      int bz = (PAIR_FLAGS[ipair][2] + is) % 2;
+      op5_t ox = make_op(bx, 1), oy = make_op(by, (long)o->ln),
+            oz = make_op(bz, (long)o->sl);
+      /* 1. interior RHS on all physical points */
+      for (long k = k0; k < k1; k++) rhs_inner_plane(o, cur, rhs, (int)k, &ox, &oy, &oz);
+      pthread_barrier_wait(&o->bar);
+      /* 2./3. free surface overwrites (rows split over threads) */
+      if (p->free_top) {
+        for (int j = p->nj1 + tid; j <= p->nj2; j += o->nthreads) {
+          rhs_timg_row(o, cur, rhs, j, bz, &ox, &oy);
+          rhs_vlow_row(o, cur, rhs, j, bz, &ox, &oy);
+        }
+      }
+      pthread_barrier_wait(&o->bar);
+      /* 4. PML corrections, faces in reference order, per point */
+      for (int d = 0; d < 3; d++)
+        for (int s = 0; s < 2; s++) {
+          const cgfd_pml_face_t *f = &p->pml[d][s];
+          if (!f->enabled) continue;
+          const op5_t *op = d == 0 ? &ox : (d == 1 ? &oy : &oz);
+          const float *acur = (is == 0) ? apre[d][s] : atmp[d][s];
+          for (long k = k0; k < k1; k++) {
+            if (k < f->nk1 || k > f->nk2) continue;
+            rhs_pml_face_plane(o, cur, rhs, d, s, (int)k, op, acur, arhs[d][s]);
+          }
+        }
+      pthread_barrier_wait(&o->bar);
+      /* 5. sources */
+      if (tid == 0 && p->src_n > 0) rhs_src(o, rhs, it, is);
+      pthread_barrier_wait(&o->bar);
+      /* RK combine over the whole padded volume (drv_rk_curv_col.c:292-446) */
+      if (is < 3) {
+        float ca = RK_A[is] * p->dt;
+        float cb = RK_B[is] * p->dt;
+        for (long e = e0; e < e1; e++) tmp[e] = pre[e] + ca * rhs[e];
+        for (int d = 0; d < 3; d++)
+          for (int s = 0; s < 2; s++) {
+            if (!p->pml[d][s].enabled) continue;
+            long a0, a1;
+            slab(o, tid, 0, (long)(o->aux_vol[d][s] * p->ncmp), &a0, &a1);
+            for (long e = a0; e < a1; e++)
+              atmp[d][s][e] = apre[d][s][e] + ca * arhs[d][s][e];
+          }
+        if (is == 0)
+          for (long e = e0; e < e1; e++) end[e] = pre[e] + cb * rhs[e];
+        else
+          for (long e = e0; e < e1; e++) end[e] += cb * rhs[e];
+        for (int d = 0; d < 3; d++)
+          for (int s = 0; s < 2; s++) {
+            if (!p->pml[d][s].enabled) continue;
+            long a0, a1;
+            slab(o, tid, 0, (long)(o->aux_vol[d][s] * p->ncmp), &a0, &a1);
+            if (is == 0)
+              for (long e = a0; e < a1; e++)
+                aend[d][s][e] = apre[d][s][e] + cb * arhs[d][s][e];
+            else
+              for (long e = a0; e < a1; e++) aend[d][s][e] += cb * arhs[d][s][e];
+          }
+      } else {
+        float cb = RK_B[is] * p->dt;
+        for (long e = e0; e < e1; e++) end[e] += cb * rhs[e];
+        for (int d = 0; d < 3; d++)
+          for (int s = 0; s < 2; s++) {
+            if (!p->pml[d][s].enabled) continue;
+            long a0, a1;
+            slab(o, tid, 0, (long)(o->aux_vol[d][s] * p->ncmp), &a0, &a1);
+            for (long e = a0; e < a1; e++) aend[d][s][e] += cb * arhs[d][s][e];
+          }
+      }
+      pthread_barrier_wait(&o->bar);
+    }
+    if (tid == 0) keep_recv(o, end, it);
+    /* swap pre and end (drv_rk_curv_col.c:530-542) */
+    float *t = pre; pre = end; end = t;
+    for (int d = 0; d < 3; d++)
+      for (int s = 0; s < 2; s++) {
+        float *u = apre[d][s]; apre[d][s] = aend[d][s]; aend[d][s] = u;
+      }
+    pthread_barrier_wait(&o->bar);
+  }
+  (void)V;
+  return NULL;
+}
+
+/*
+ * Runs the whole time loop on the host arrays of `p` (wav and PML aux are
+ * updated in place, level semantics as in the reference; seismograms
+ * written).  mVx/mVy/mF receive the free-surface matrices (nx*ny*9 each,
+ * may be NULL when there is no free surface).
+ */
+int oracle_allstep(const cgfd_problem_t *p, int timg_mode, int nthreads,
+                   float *mVx, float *mVy, float *mF)
+{
+  if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO) return CGFD_EINVAL;
+  if (p->src_n_surface_force > 0) return CGFD_EINVAL;
+  if (p->nlevel != 4 || p->ncmp != 9) return CGFD_EINVAL;
+  orc_t o;
+  memset(&o, 0, sizeof(o));
+  o.p = p;
+  o.ln = p->nx;
+  o.sl = (size_t)p->nx * p->ny;
+  o.vol = o.sl * p->nz;
+  o.timg_mode = timg_mode;
+  o.nthreads = nthreads < 1 ? 1 : nthreads;
+  for (int l = 0; l < 4; l++) o.lev[l] = p->wav + (size_t)l * o.vol * p->ncmp;
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      const cgfd_pml_face_t *f = &p->pml[d][s];
+      if (!f->enabled) continue;
+      size_t av = (size_t)(f->ni2 - f->ni1 + 1) * (f->nj2 - f->nj1 + 1) *
+                  (f->nk2 - f->nk1 + 1);
+      o.aux_vol[d][s] = av;
+      for (int l = 0; l < 4; l++) o.aux[d][s][l] = f->aux + (size_t)l * av * 9;
+    }
+  size_t n2 = o.sl * 9;
+  int own_m = 0;
+  if (p->free_top) {
+    if (!mVx) {
+      mVx = calloc(n2, sizeof(float));
+      mVy = calloc(n2, sizeof(float));
+      mF = calloc(n2, sizeof(float));
+      own_m = 1;
+    } else {
+      memset(mVx, 0, n2 * 4); memset(mVy, 0, n2 * 4); memset(mF, 0, n2 * 4);
+    }
+    oracle_dvh2dvz_iso(p, mVx, mVy, mF);
+  }
+  o.mVx = mVx; o.mVy = mVy; o.mF = mF;
+  if (p->src_n > 0 && p->src_spatial != CGFD_SRC_POINT) {
+    int n1 = 2 * p->src_ext_half + 1;
+    o.ext = calloc(p->src_n, sizeof(float *));
+    for (int is = 0; is < p->src_n; is++) {
+      o.ext[is] = calloc((size_t)n1 * n1 * n1, sizeof(float));
+      int sk = p->src_sk[is], half = p->src_ext_half;
+      int kz2 = (sk + half < p->nk2) ? half : p->nk2 - sk;
+      src_weights(o.ext[is], p->src_si_inc[is], p->src_sj_inc[is],
+                  p->src_sk_inc[is], p->src_ext_coef, half, kz2);
+    }
+  }
+  pthread_barrier_init(&o.bar, NULL, o.nthreads);
+  pthread_t *ths = calloc(o.nthreads, sizeof(pthread_t));
+  thr_t *ta = calloc(o.nthreads, sizeof(thr_t));
+  for (int t = 0; t < o.nthreads; t++) {
+    ta[t].o = &o;
+    ta[t].tid = t;
+    if (t > 0) pthread_create(&ths[t], NULL, worker, &ta[t]);
+  }
+  worker(&ta[0]);
+  for (int t = 1; t < o.nthreads; t++) pthread_join(ths[t], NULL);
+  pthread_barrier_destroy(&o.bar);
+  free(ths);
+  free(ta);
+  if (o.ext) {
+    for (int is = 0; is < p->src_n; is++) free(o.ext[is]);
+    free(o.ext);
+  }
+  if (own_m) { free(mVx); free(mVy); free(mF); }
+  return 0;
+}

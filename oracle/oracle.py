@@ -1,0 +1,62 @@
+"""Python binding of the C oracle (oracle/cgfd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+cpu_baseline leg of bench.py, never by the product package.
+"""
+
+import ctypes as C
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+LIB = os.path.join(HERE, "_build", "libcgfd_oracle.so")
+
+TIMG_ZERO = 0     # value the reference build reads beyond its local array
+TIMG_MIRROR = 1   # the mirror the traction-image formula intends
+
+
+def build(force=False):
+    """Compile the oracle with gcc (x86-64 and aarch64 alike)."""
+    src = os.path.join(HERE, "cgfd_oracle.c")
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    subprocess.run(["gcc", "-O3", "-ffp-contract=off", "-fPIC", "-shared",
+                    "-I" + os.path.join(REPO, "include"), "-o", LIB, src,
+                    "-lpthread", "-lm"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.oracle_allstep.restype = C.c_int
+        _lib.oracle_allstep.argtypes = [C.c_void_p, C.c_int, C.c_int,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.oracle_dvh2dvz_iso.restype = C.c_int
+        _lib.oracle_dvh2dvz_iso.argtypes = [C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]
+    return _lib
+
+
+def allstep(problem, timg_mode=TIMG_ZERO, nthreads=1, want_mats=False):
+    """Run the oracle on a cgfd3d_gb300.problem.Problem in place."""
+    import numpy as np
+    cs = problem.to_c()
+    mats = None
+    if problem.free_top:
+        n2 = problem.nx * problem.ny * 9
+        mats = [np.zeros(n2, np.float32) for _ in range(3)]
+        ptrs = [m.ctypes.data for m in mats]
+    else:
+        ptrs = [None, None, None]
+    rc = lib().oracle_allstep(C.addressof(cs), timg_mode, nthreads, *ptrs)
+    if rc != 0:
+        raise RuntimeError("oracle_allstep failed with code %d" % rc)
+    return mats if want_mats else None

@@ -1,0 +1,53 @@
+"""The C oracle against the reference's own outputs (golden fixtures).
+
+The fixtures under tests/golden/ were produced by the CGFD3D reference CPU
+build (oracle/Makefile, tests/golden/make_golden.py).  The oracle restates the
+reference's float arithmetic in the same order, so the comparison is exact.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from cgfd3d_gb300 import problem as P
+from conftest import GOLDEN, GOLDEN_CASES
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("nthreads", [1, 3])
+def test_oracle_matches_reference_bitwise(case, nthreads):
+    p, exp = P.from_golden(os.path.join(GOLDEN, case + ".npz"))
+    mats = oracle.allstep(p, oracle.TIMG_ZERO, nthreads, want_mats=True)
+    np.testing.assert_array_equal(p.level(p.final_level()), exp["wav"])
+    for key, val in exp.items():
+        if key.startswith("pml."):
+            d, s = int(key[4]), int(key[6])
+            np.testing.assert_array_equal(p.pml_final(d, s), val)
+    if "recv" in exp:
+        np.testing.assert_array_equal(p.recv["seismo"], exp["recv"])
+    if "line" in exp:
+        np.testing.assert_array_equal(p.line["seismo"], exp["line"])
+    if mats is not None:
+        for m, n in zip(mats, ["matVx2Vz2", "matVy2Vz2", "matF2Vz2"]):
+            np.testing.assert_array_equal(m, exp[n])
+
+
+def test_mirror_variant_differs_from_reference():
+    """The intended traction mirror is NOT what the reference computes."""
+    p, exp = P.from_golden(os.path.join(GOLDEN, "iso_flat_explosion.npz"))
+    oracle.allstep(p, oracle.TIMG_MIRROR, 2)
+    got = p.level(p.final_level())
+    assert np.abs(got - exp["wav"]).max() > 1e-3 * np.abs(exp["wav"]).max()
+
+
+def test_planted_error_is_detected():
+    """A one-ulp change of one input coefficient changes the result."""
+    p, exp = P.from_golden(os.path.join(GOLDEN, "iso_box_pml6.npz"))
+    q = (p.ni1 + p.ni // 2) + (p.nj1 + p.nj // 2) * p.nx + \
+        (p.nk1 + p.nk // 2) * p.nx * p.ny
+    p.media["mu"] = p.media["mu"].copy()
+    p.media["mu"][q] = np.nextafter(p.media["mu"][q], np.float32(np.inf))
+    oracle.allstep(p, oracle.TIMG_ZERO, 1)
+    assert not np.array_equal(p.level(p.final_level()), exp["wav"])
