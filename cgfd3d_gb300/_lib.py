@@ -1,0 +1,56 @@
+"""Loader of the in-tree CUDA library (cgfd3d_gb300/_build/libcgfd3d_gpu.so).
+
+The library is the only compute path: there is no CPU fallback, so a missing
+or unloadable library raises instead of degrading.
+"""
+
+import ctypes as C
+import os
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcgfd3d_gpu.so")
+
+_lib = None
+
+
+class CgfdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("cgfd error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            "CUDA library %s is missing: run `python -c \"import "
+            "__graft_entry__ as g; g.build()\"` (needs nvcc)" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.cgfd_last_error.restype = C.c_char_p
+    L.cgfd_abi_version.restype = C.c_int
+    L.cgfd_solver_create.argtypes = [vp, C.POINTER(vp)]
+    L.cgfd_solver_run.argtypes = [vp, C.c_int]
+    L.cgfd_solver_fetch.argtypes = [vp]
+    L.cgfd_solver_step.argtypes = [vp]
+    L.cgfd_solver_check_finite.argtypes = [vp]
+    L.cgfd_solver_kernel_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    L.cgfd_solver_destroy.argtypes = [vp]
+    L.cgfd_solver_destroy.restype = None
+    L.cgfd_allstep.argtypes = [vp]
+    L.cgfd_device_bytes.argtypes = [vp]
+    L.cgfd_device_bytes.restype = C.c_size_t
+    if L.cgfd_abi_version() != abi.CGFD_ABI_VERSION:
+        raise ImportError("libcgfd3d_gpu ABI version mismatch")
+    _lib = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        raise CgfdError(rc, lib().cgfd_last_error().decode())
+    return rc

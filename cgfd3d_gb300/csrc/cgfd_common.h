@@ -1,0 +1,85 @@
+/*
+ * Shared host/device definitions of the GB300 time-stepping library.
+ *
+ * Device layout in HBM (per solver):
+ *   wavefield  4 levels x 9 components x padded volume (nx*ny*nz), the
+ *              reference's layout (forward/wav_t.c:40-136) with the level
+ *              roles  pre | tmpA | tmpB | end.  The reference keeps a
+ *              separate rhs level; here the RHS lives only in registers and
+ *              the former rhs level is the second tmp buffer, so that the
+ *              stage that reads tmp with a +-3 stencil never writes the
+ *              buffer it reads.
+ *   metrics    10 x volume: jac, xi_x..zeta_z (forward/gd_t.c:142-180)
+ *   media      3 x volume: slw (=1/rho), lambda, mu
+ *   PML aux    per enabled face: 4 levels x 9 x face-box volume
+ *   surface    3 x (nx*ny*9) conversion matrices (k = nk2)
+ */
+#ifndef CGFD_COMMON_H
+#define CGFD_COMMON_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#define CGFD_NCMP 9
+#define CGFD_NFACE 6
+
+/* component order of the reference (forward/wav_t.c:93-136) */
+enum { C_VX = 0, C_VY, C_VZ, C_TXX, C_TYY, C_TZZ, C_TYZ, C_TXZ, C_TXY };
+
+struct DevGrid {
+  int ni, nj, nk, nx, ny, nz;
+  int ni1, ni2, nj1, nj2, nk1, nk2;
+  long long sl;   /* nx*ny */
+  long long vol;  /* nx*ny*nz */
+};
+
+struct DevFace {
+  int on;
+  int dim;                       /* 0 x, 1 y, 2 z */
+  int i1, i2, j1, j2, k1, k2;    /* box, inclusive */
+  int bx, by;                    /* box extents in i and j */
+  long long avol;                /* box volume */
+  const float *A, *B, *D;
+};
+
+/* one source contribution at one grid point (precomputed on the host) */
+struct SrcEntry {
+  int k;          /* plane */
+  int is;         /* source index */
+  float vf;       /* coef * slw / jac  (force weight) */
+  float rjac;     /* coef / jac        (moment weight) */
+  int force_on;   /* force applied at this point (strict surface rule) */
+  int pad;
+};
+
+struct StageArgs {
+  DevGrid g;
+  /* metrics and media */
+  const float *jac, *xix, *xiy, *xiz, *etx, *ety, *etz, *ztx, *zty, *ztz;
+  const float *slw, *lam, *mu;
+  /* wavefield levels for this stage */
+  const float *cur;   /* stencil input */
+  const float *pre;   /* level "pre" */
+  float *tmp_out;     /* next tmp (stages 0-2) */
+  float *end;         /* accumulator */
+  float ca, cb;       /* rk_a*dt, rk_b*dt */
+  /* PML */
+  DevFace face[CGFD_NFACE];
+  const float *acur[CGFD_NFACE];
+  const float *apre[CGFD_NFACE];
+  float *atmp_out[CGFD_NFACE];
+  float *aend[CGFD_NFACE];
+  /* free surface */
+  int free_top;
+  const float *mVx, *mVy, *mF;
+  /* sources */
+  int src_n, src_max_nt, src_max_stage, src_force, src_moment;
+  const int *src_col;          /* (ni*nj + 1) offsets into src_ent */
+  const SrcEntry *src_ent;
+  const int *src_it_begin, *src_it_end;
+  const float *Fx, *Fy, *Fz, *Mxx, *Myy, *Mzz, *Mxz, *Myz, *Mxy;
+  const int *d_it;             /* current step on the device */
+  int istage;
+};
+
+#endif

@@ -1,0 +1,797 @@
+/*
+ * cgfd_solver.cu -- device-resident RK4 time loop for CGFD3D, sm_103a.
+ *
+ * Implements the flat C ABI of include/cgfd3d_gpu.h.  One solver object
+ * owns every array the time loop touches in HBM; a step is four fused stage
+ * launches (cgfd_stage.cuh) plus one receiver-gather launch, and the
+ * 8-step pair cycle (forward/fd_t.c:182-236) can be captured once into a
+ * CUDA graph and replayed.
+ *
+ * Reference: forward/drv_rk_curv_col.c:27-556 (time loop),
+ * forward/sv_curv_col_el_iso.c:1258-1375 (free-surface matrices),
+ * forward/io_funcs.c:1584-1645 (receivers, lines).
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cgfd3d_gpu.h"
+#include "cgfd_common.h"
+#include "cgfd_stage.cuh"
+
+/* ------------------------------------------------------------------------ */
+/* errors                                                                    */
+/* ------------------------------------------------------------------------ */
+
+static thread_local std::string g_err;
+
+static int set_err(int code, const char *fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                              \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess)                                                    \
+      return set_err(CGFD_ECUDA, "%s failed: %s (%s:%d)", #call,              \
+                     cudaGetErrorString(e_), __FILE__, __LINE__);             \
+  } while (0)
+
+extern "C" const char *cgfd_last_error(void) { return g_err.c_str(); }
+extern "C" int cgfd_abi_version(void) { return CGFD_ABI_VERSION; }
+
+/* ------------------------------------------------------------------------ */
+/* kernels                                                                   */
+/* ------------------------------------------------------------------------ */
+
+#define TX 32
+#define TY 4
+#define KCHUNK 8
+
+template <int BX, int BY, int BZ, int KIND>
+__global__ void __launch_bounds__(TX *TY)
+    k_stage(const __grid_constant__ StageArgs a)
+{
+  int i = a.g.ni1 + blockIdx.x * TX + threadIdx.x;
+  int j = a.g.nj1 + blockIdx.y * TY + threadIdx.y;
+  if (i > a.g.ni2 || j > a.g.nj2) return;
+  int k0 = a.g.nk1 + blockIdx.z * KCHUNK;
+  int k1 = min(k0 + KCHUNK - 1, a.g.nk2);
+  for (int k = k0; k <= k1; k++) stage_point<BX, BY, BZ, KIND>(a, i, j, k);
+}
+
+/* free-surface conversion matrices A^-1 B, A^-1 C, A^-1 per surface point
+ * (forward/sv_curv_col_el_iso.c:1304-1372, inverse lib/fdlib_math.c:8-35) */
+__global__ void k_dvh2dvz_iso(DevGrid g, const float *__restrict__ xix,
+                              const float *__restrict__ xiy,
+                              const float *__restrict__ xiz,
+                              const float *__restrict__ etx,
+                              const float *__restrict__ ety,
+                              const float *__restrict__ etz,
+                              const float *__restrict__ ztx,
+                              const float *__restrict__ zty,
+                              const float *__restrict__ ztz,
+                              const float *__restrict__ lam3,
+                              const float *__restrict__ mu3, float *mVx,
+                              float *mVy, float *mF)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = i + (long long)j * g.nx + (long long)g.nk2 * g.sl;
+  float e11 = xix[q], e12 = xiy[q], e13 = xiz[q];
+  float e21 = etx[q], e22 = ety[q], e23 = etz[q];
+  float e31 = ztx[q], e32 = zty[q], e33 = ztz[q];
+  float lam = lam3[q], mu = mu3[q];
+  float l2m = lam + 2.0f * mu;
+  float A[3][3], B[3][3], C[3][3];
+  A[0][0] = l2m * e31 * e31 + mu * (e32 * e32 + e33 * e33);
+  A[0][1] = lam * e31 * e32 + mu * e32 * e31;
+  A[0][2] = lam * e31 * e33 + mu * e33 * e31;
+  A[1][0] = lam * e32 * e31 + mu * e31 * e32;
+  A[1][1] = l2m * e32 * e32 + mu * (e31 * e31 + e33 * e33);
+  A[1][2] = lam * e32 * e33 + mu * e33 * e32;
+  A[2][0] = lam * e33 * e31 + mu * e31 * e33;
+  A[2][1] = lam * e33 * e32 + mu * e32 * e33;
+  A[2][2] = l2m * e33 * e33 + mu * (e31 * e31 + e32 * e32);
+  /* adjugate / determinant */
+  float v[3][3];
+  v[0][0] = A[1][1] * A[2][2] - A[2][1] * A[1][2];
+  v[0][1] = A[2][1] * A[0][2] - A[0][1] * A[2][2];
+  v[0][2] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+  v[1][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+  v[1][1] = A[0][0] * A[2][2] - A[2][0] * A[0][2];
+  v[1][2] = A[1][0] * A[0][2] - A[0][0] * A[1][2];
+  v[2][0] = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+  v[2][1] = A[2][0] * A[0][1] - A[0][0] * A[2][1];
+  v[2][2] = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+  float det = v[0][0] * A[0][0] + v[0][1] * A[1][0] + v[0][2] * A[2][0];
+  det = 1.0f / det;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) A[r][c] = v[r][c] * det;
+  B[0][0] = -l2m * e31 * e11 - mu * (e32 * e12 + e33 * e13);
+  B[0][1] = -lam * e31 * e12 - mu * e32 * e11;
+  B[0][2] = -lam * e31 * e13 - mu * e33 * e11;
+  B[1][0] = -lam * e32 * e11 - mu * e31 * e12;
+  B[1][1] = -l2m * e32 * e12 - mu * (e31 * e11 + e33 * e13);
+  B[1][2] = -lam * e32 * e13 - mu * e33 * e12;
+  B[2][0] = -lam * e33 * e11 - mu * e31 * e13;
+  B[2][1] = -lam * e33 * e12 - mu * e32 * e13;
+  B[2][2] = -l2m * e33 * e13 - mu * (e31 * e11 + e32 * e12);
+  C[0][0] = -l2m * e31 * e21 - mu * (e32 * e22 + e33 * e23);
+  C[0][1] = -lam * e31 * e22 - mu * e32 * e21;
+  C[0][2] = -lam * e31 * e23 - mu * e33 * e21;
+  C[1][0] = -lam * e32 * e21 - mu * e31 * e22;
+  C[1][1] = -l2m * e32 * e22 - mu * (e31 * e21 + e33 * e23);
+  C[1][2] = -lam * e32 * e23 - mu * e33 * e22;
+  C[2][0] = -lam * e33 * e21 - mu * e31 * e23;
+  C[2][1] = -lam * e33 * e22 - mu * e32 * e23;
+  C[2][2] = -l2m * e33 * e23 - mu * (e31 * e21 + e32 * e22);
+  long long ij = (i + (long long)j * g.nx) * 9;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      float ab = 0.f, ac = 0.f;
+      for (int m = 0; m < 3; m++) {
+        ab += A[r][m] * B[m][c];
+        ac += A[r][m] * C[m][c];
+      }
+      mVx[ij + r * 3 + c] = ab;
+      mVy[ij + r * 3 + c] = ac;
+      mF[ij + r * 3 + c] = A[r][c];
+    }
+}
+
+/* receivers and lines after a step; one block; advances the step counter.
+ * Trilinear weights as forward/io_funcs.c:1595-1612, which uses corner 5
+ * twice and corner 4 never (harmless for receivers on a grid plane). */
+__global__ void k_recv(const float *__restrict__ w, long long vol, int ncmp,
+                       int nrecv, int recv_ncmp, int recv_max_nt,
+                       const float *__restrict__ dijk,
+                       const int *__restrict__ idx8, float *seismo,
+                       int nline, int line_max_nt,
+                       const int *__restrict__ line_iptr, float *line_seismo,
+                       int *d_it)
+{
+  int it = *d_it;
+  for (int t = threadIdx.x; t < nrecv * recv_ncmp; t += blockDim.x) {
+    int n = t / recv_ncmp, c = t % recv_ncmp;
+    const int *x = idx8 + 8 * n;
+    float Lx2 = dijk[3 * n], Ly2 = dijk[3 * n + 1], Lz2 = dijk[3 * n + 2];
+    float Lx1 = 1.0f - Lx2, Ly1 = 1.0f - Ly2, Lz1 = 1.0f - Lz2;
+    const float *v = w + c * vol;
+    seismo[((long long)n * recv_ncmp + c) * recv_max_nt + it] =
+        v[x[0]] * Lx1 * Ly1 * Lz1 + v[x[1]] * Lx2 * Ly1 * Lz1 +
+        v[x[2]] * Lx1 * Ly2 * Lz1 + v[x[3]] * Lx2 * Ly2 * Lz1 +
+        v[x[5]] * Lx1 * Ly1 * Lz2 + v[x[5]] * Lx2 * Ly1 * Lz2 +
+        v[x[6]] * Lx1 * Ly2 * Lz2 + v[x[7]] * Lx2 * Ly2 * Lz2;
+  }
+  for (int t = threadIdx.x; t < nline * ncmp; t += blockDim.x) {
+    int n = t / ncmp, c = t % ncmp;
+    line_seismo[((long long)n * ncmp + c) * line_max_nt + it] =
+        w[c * vol + line_iptr[n]];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *d_it = it + 1;
+}
+
+__global__ void k_nonfinite(const float *__restrict__ w, long long n, int *flag)
+{
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  long long stride = (long long)gridDim.x * blockDim.x;
+  int bad = 0;
+  for (; t < n; t += stride) bad |= !isfinite(w[t]);
+  if (bad) atomicOr(flag, 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* host-side source preprocessing                                            */
+/* ------------------------------------------------------------------------ */
+
+/* Gaussian weights normalised over the points at or below the surface
+ * (forward/src_t.c:2111-2151 with fun_gauss src_t.c:2179-2184), evaluated
+ * with the same float/double steps as the reference. */
+static float gauss1(float t, float a)
+{
+  float tt = t - 0.0f;
+  float e = (-tt) * tt / (a * a);
+  float den = sqrtf((float)3.14159265358979323846) * a;
+  return (float)(std::exp((double)e) / (double)den);
+}
+
+static void gauss_weights(std::vector<float> &delt, float x0, float y0,
+                          float z0, float r, int half, int half_z2)
+{
+  int n1 = 2 * half + 1;
+  delt.assign((size_t)n1 * n1 * n1, 0.f);
+  int idx = 0;
+  for (int k = -half; k <= half; k++)
+    for (int j = -half; j <= half; j++)
+      for (int i = -half; i <= half; i++)
+        delt[idx++] = gauss1(i - x0, r) * gauss1(j - y0, r) * gauss1(k - z0, r);
+  float sum = 0.f;
+  idx = 0;
+  for (int k = -half; k <= half_z2; k++)
+    for (int j = -half; j <= half; j++)
+      for (int i = -half; i <= half; i++) sum += delt[idx++];
+  for (size_t m = 0; m < delt.size(); m++) delt[m] /= sum;
+}
+
+struct HostEntry {
+  int col;
+  SrcEntry e;
+};
+
+/* Source contributions per (i,j) column, sorted by k then source index. */
+static int build_source_entries(const cgfd_problem_t *p, std::vector<int> &col,
+                                std::vector<SrcEntry> &ent)
+{
+  size_t ln = p->nx, sl = (size_t)p->nx * p->ny;
+  std::vector<HostEntry> all;
+  for (int is = 0; is < p->src_n; is++) {
+    int si = p->src_si[is], sj = p->src_sj[is], sk = p->src_sk[is];
+    if (p->src_spatial == CGFD_SRC_POINT) {
+      if (si < p->ni1 || si > p->ni2 || sj < p->nj1 || sj > p->nj2 ||
+          sk < p->nk1 || sk > p->nk2)
+        continue;
+      size_t q = si + sj * ln + (size_t)sk * sl;
+      HostEntry h;
+      h.col = (si - p->ni1) + (sj - p->nj1) * p->ni;
+      h.e.k = sk;
+      h.e.is = is;
+      h.e.vf = p->slw[q] / p->jac[q];
+      h.e.rjac = (float)(1.0 / (double)p->jac[q]);
+      h.e.force_on = (p->src_surface_strict == 0 || sk < p->nk2);
+      h.e.pad = 0;
+      all.push_back(h);
+    } else {
+      int half = p->src_ext_half;
+      int kz2 = (sk + half < p->nk2) ? half : p->nk2 - sk;
+      std::vector<float> w;
+      gauss_weights(w, p->src_si_inc[is], p->src_sj_inc[is],
+                    p->src_sk_inc[is], p->src_ext_coef, half, kz2);
+      int idx = 0;
+      for (int kk = -half; kk <= kz2; kk++)
+        for (int jj = -half; jj <= half; jj++)
+          for (int ii = -half; ii <= half; ii++, idx++) {
+            int i = si + ii, j = sj + jj, k = sk + kk;
+            if (i < p->ni1 || i > p->ni2 || j < p->nj1 || j > p->nj2 ||
+                k < p->nk1 || k > p->nk2)
+              continue;
+            size_t q = i + j * ln + (size_t)k * sl;
+            float c = w[idx];
+            HostEntry h;
+            h.col = (i - p->ni1) + (j - p->nj1) * p->ni;
+            h.e.k = k;
+            h.e.is = is;
+            h.e.vf = c * p->slw[q] / p->jac[q];
+            h.e.rjac = c / p->jac[q];
+            h.e.force_on = (p->src_surface_strict == 0 || k < p->nk2);
+            h.e.pad = 0;
+            all.push_back(h);
+          }
+    }
+  }
+  /* stable ordering: column, then k, then source index (the reference adds
+   * the sources in index order at every point) */
+  std::stable_sort(all.begin(), all.end(), [](const HostEntry &a, const HostEntry &b) {
+    if (a.col != b.col) return a.col < b.col;
+    if (a.e.k != b.e.k) return a.e.k < b.e.k;
+    return a.e.is < b.e.is;
+  });
+  size_t ncol = (size_t)p->ni * p->nj;
+  col.assign(ncol + 1, 0);
+  for (auto &h : all) col[h.col + 1]++;
+  for (size_t c = 0; c < ncol; c++) col[c + 1] += col[c];
+  ent.resize(all.size());
+  for (size_t n = 0; n < all.size(); n++) ent[n] = all[n].e;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* solver                                                                    */
+/* ------------------------------------------------------------------------ */
+
+struct cgfd_solver {
+  const cgfd_problem_t *p;
+  DevGrid g;
+  cudaStream_t stream;
+  float *wav;                   /* 4 levels */
+  float *metric;                /* 10 x vol */
+  float *media;                 /* 3 x vol */
+  float *mats;                  /* 3 x sl*9 */
+  float *aux[CGFD_NFACE];       /* 4 levels each */
+  DevFace face[CGFD_NFACE];
+  int face_src[CGFD_NFACE][2];  /* idim, iside */
+  int *src_col, *src_it_begin, *src_it_end;
+  SrcEntry *src_ent;
+  float *stf;                   /* 9 tables */
+  float *recv_dijk, *recv_seismo, *line_seismo;
+  int *recv_idx, *line_iptr;
+  int *d_it;
+  int *d_flag;
+  int step;
+  int pre_lev, end_lev;         /* level of pre/end in wav (0 or 3) */
+  int nsrc_ent;
+  size_t bytes;
+  cudaEvent_t ev0, ev1;
+  float t_stage_ms, t_other_ms;
+  int n_stage, n_other;
+  int timing;
+  cudaGraphExec_t graph8;
+  int graph_pre_lev;
+};
+
+static size_t level_floats(const DevGrid &g) { return (size_t)CGFD_NCMP * g.vol; }
+
+extern "C" size_t cgfd_device_bytes(const cgfd_problem_t *p)
+{
+  size_t vol = (size_t)p->nx * p->ny * p->nz;
+  size_t b = (4 * 9 + 10 + 3) * vol * sizeof(float);
+  if (p->free_top) b += 3 * (size_t)p->nx * p->ny * 9 * sizeof(float);
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      const cgfd_pml_face_t *f = &p->pml[d][s];
+      if (!f->enabled) continue;
+      size_t av = (size_t)(f->ni2 - f->ni1 + 1) * (f->nj2 - f->nj1 + 1) *
+                  (f->nk2 - f->nk1 + 1);
+      b += 4 * 9 * av * sizeof(float);
+    }
+  return b;
+}
+
+static int validate(const cgfd_problem_t *p)
+{
+  if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO)
+    return set_err(CGFD_EINVAL, "medium_type %d not supported by this build",
+                   p->medium_type);
+  if (p->ncmp != 9 || p->nlevel != 4)
+    return set_err(CGFD_EINVAL, "ncmp=%d nlevel=%d (need 9, 4)", p->ncmp, p->nlevel);
+  if (p->nx != p->ni + 6 || p->ny != p->nj + 6 || p->nz != p->nk + 6 ||
+      p->ni1 != 3 || p->nj1 != 3 || p->nk1 != 3 || p->ni2 != p->ni + 2 ||
+      p->nj2 != p->nj + 2 || p->nk2 != p->nk + 2)
+    return set_err(CGFD_EINVAL, "grid indices are not the 3-ghost layout");
+  if (p->ni < 8 || p->nj < 8 || p->nk < 8)
+    return set_err(CGFD_EINVAL, "grid too small (ni,nj,nk >= 8 required)");
+  if (p->src_n > 0 && p->src_n_surface_force > 0)
+    return set_err(CGFD_EINVAL, "surface force sources are not supported");
+  if (!p->jac || !p->xi_x || !p->slw || !p->lambda || !p->mu || !p->wav)
+    return set_err(CGFD_EINVAL, "missing input array");
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      const cgfd_pml_face_t *f = &p->pml[d][s];
+      if (!f->enabled) continue;
+      if (f->ni1 < p->ni1 || f->ni2 > p->ni2 || f->nj1 < p->nj1 ||
+          f->nj2 > p->nj2 || f->nk1 < p->nk1 || f->nk2 > p->nk2 ||
+          f->ni1 > f->ni2 || f->nj1 > f->nj2 || f->nk1 > f->nk2)
+        return set_err(CGFD_EINVAL, "PML face %d/%d box outside the grid", d, s);
+      if (!f->A || !f->B || !f->D || !f->aux)
+        return set_err(CGFD_EINVAL, "PML face %d/%d arrays missing", d, s);
+    }
+  if (p->recv_n > 0 && (!p->recv_dijk || !p->recv_indx1d || !p->recv_seismo))
+    return set_err(CGFD_EINVAL, "receiver arrays missing");
+  if (p->recv_n > 0 && p->recv_max_nt < p->nt_total)
+    return set_err(CGFD_EINVAL, "receiver max_nt < nt_total");
+  if (p->line_n > 0 && p->line_max_nt < p->nt_total)
+    return set_err(CGFD_EINVAL, "line max_nt < nt_total");
+  long long vol = (long long)p->nx * p->ny * p->nz;
+  for (int n = 0; n < 8 * p->recv_n; n++)
+    if (p->recv_indx1d[n] < 0 || p->recv_indx1d[n] >= vol)
+      return set_err(CGFD_EINVAL, "receiver index out of the volume");
+  if (p->line_n > 0 && (!p->line_iptr || !p->line_seismo))
+    return set_err(CGFD_EINVAL, "line arrays missing");
+  for (int n = 0; n < p->line_n; n++)
+    if (p->line_iptr[n] < 0 || p->line_iptr[n] >= vol)
+      return set_err(CGFD_EINVAL, "line receiver index out of the volume");
+  if (p->src_n > 0) {
+    if (!p->src_si || !p->src_sj || !p->src_sk || !p->src_it_begin ||
+        !p->src_it_end || p->src_max_nt < 1 || p->src_max_stage != 4)
+      return set_err(CGFD_EINVAL, "source description incomplete");
+    if (p->src_spatial != CGFD_SRC_POINT &&
+        (!p->src_si_inc || p->src_ext_half < 0 || p->src_ext_half > 8))
+      return set_err(CGFD_EINVAL, "Gaussian source description incomplete");
+    if ((p->src_force && (!p->Fx || !p->Fy || !p->Fz)) ||
+        (p->src_moment && (!p->Mxx || !p->Myy || !p->Mzz || !p->Mxz ||
+                           !p->Myz || !p->Mxy)))
+      return set_err(CGFD_EINVAL, "source time-function tables missing");
+    for (int is = 0; is < p->src_n; is++)
+      if (p->src_it_end[is] - p->src_it_begin[is] + 1 > p->src_max_nt)
+        return set_err(CGFD_EINVAL, "source %d time window exceeds max_nt", is);
+  }
+  return 0;
+}
+
+template <typename T>
+static int dalloc(cgfd_solver_t *s, T **ptr, size_t n)
+{
+  *ptr = nullptr;
+  if (n == 0) return 0;
+  cudaError_t e = cudaMalloc((void **)ptr, n * sizeof(T));
+  if (e != cudaSuccess)
+    return set_err(CGFD_ENOMEM, "cudaMalloc(%zu bytes): %s", n * sizeof(T),
+                   cudaGetErrorString(e));
+  s->bytes += n * sizeof(T);
+  return 0;
+}
+
+extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
+{
+  if (!s) return;
+  if (s->graph8) cudaGraphExecDestroy(s->graph8);
+  void *ptrs[] = {s->wav, s->metric, s->media, s->mats, s->src_col,
+                  s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
+                  s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
+                  s->line_iptr, s->d_it, s->d_flag};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  for (int f = 0; f < CGFD_NFACE; f++)
+    if (s->aux[f]) cudaFree(s->aux[f]);
+  for (int f = 0; f < CGFD_NFACE; f++) {
+    if (s->face[f].A) cudaFree((void *)s->face[f].A);
+  }
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
+{
+  *out = nullptr;
+  int rc = validate(p);
+  if (rc) return rc;
+  cgfd_solver_t *s = new cgfd_solver_t();
+  memset((void *)s, 0, sizeof(*s));
+  s->p = p;
+  DevGrid &g = s->g;
+  g.ni = p->ni; g.nj = p->nj; g.nk = p->nk;
+  g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
+  g.ni1 = p->ni1; g.ni2 = p->ni2; g.nj1 = p->nj1; g.nj2 = p->nj2;
+  g.nk1 = p->nk1; g.nk2 = p->nk2;
+  g.sl = (long long)p->nx * p->ny;
+  g.vol = g.sl * p->nz;
+#define TRY(x) do { int r_ = (x); if (r_) { cgfd_solver_destroy(s); return r_; } } while (0)
+#define TRYC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { set_err(CGFD_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); cgfd_solver_destroy(s); return CGFD_ECUDA; } } while (0)
+  TRYC(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  TRYC(cudaEventCreate(&s->ev0));
+  TRYC(cudaEventCreate(&s->ev1));
+  size_t vol = g.vol, L = level_floats(g);
+  cudaStream_t st = s->stream;
+  /* wavefield: level 0 of the input copied into all four levels, so that
+   * ghost values stay what the caller passed (they never change in the
+   * reference either: rhs ghosts are zero) */
+  TRY(dalloc(s, &s->wav, 4 * L));
+  for (int l = 0; l < 4; l++)
+    TRYC(cudaMemcpyAsync(s->wav + l * L, p->wav, L * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+  s->pre_lev = 0;
+  s->end_lev = 3;
+  TRY(dalloc(s, &s->metric, 10 * vol));
+  const float *mh[10] = {p->jac, p->xi_x, p->xi_y, p->xi_z, p->eta_x,
+                         p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
+  for (int m = 0; m < 10; m++)
+    TRYC(cudaMemcpyAsync(s->metric + m * vol, mh[m], vol * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+  TRY(dalloc(s, &s->media, 3 * vol));
+  const float *md[3] = {p->slw, p->lambda, p->mu};
+  for (int m = 0; m < 3; m++)
+    TRYC(cudaMemcpyAsync(s->media + m * vol, md[m], vol * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+  /* PML faces */
+  int nf = 0;
+  for (int d = 0; d < 3; d++)
+    for (int sd = 0; sd < 2; sd++) {
+      const cgfd_pml_face_t *f = &p->pml[d][sd];
+      int fi = d * 2 + sd;
+      DevFace &F = s->face[fi];
+      F.on = f->enabled ? 1 : 0;
+      F.dim = d;
+      if (!F.on) continue;
+      nf++;
+      F.i1 = f->ni1; F.i2 = f->ni2; F.j1 = f->nj1; F.j2 = f->nj2;
+      F.k1 = f->nk1; F.k2 = f->nk2;
+      F.bx = f->ni2 - f->ni1 + 1;
+      F.by = f->nj2 - f->nj1 + 1;
+      F.avol = (long long)F.bx * F.by * (f->nk2 - f->nk1 + 1);
+      int np = d == 0 ? F.bx : (d == 1 ? F.by : f->nk2 - f->nk1 + 1);
+      float *coef;
+      TRYC(cudaMalloc((void **)&coef, 3 * np * sizeof(float)));
+      s->bytes += 3 * np * sizeof(float);
+      TRYC(cudaMemcpyAsync(coef, f->A, np * 4, cudaMemcpyHostToDevice, st));
+      TRYC(cudaMemcpyAsync(coef + np, f->B, np * 4, cudaMemcpyHostToDevice, st));
+      TRYC(cudaMemcpyAsync(coef + 2 * np, f->D, np * 4, cudaMemcpyHostToDevice, st));
+      F.A = coef; F.B = coef + np; F.D = coef + 2 * np;
+      size_t al = 9 * (size_t)F.avol;
+      TRY(dalloc(s, &s->aux[fi], 4 * al));
+      for (int l = 0; l < 4; l++)
+        TRYC(cudaMemcpyAsync(s->aux[fi] + l * al, f->aux, al * sizeof(float),
+                             cudaMemcpyHostToDevice, st));
+    }
+  (void)nf;
+  /* free surface matrices, computed on the device */
+  if (p->free_top) {
+    size_t n2 = (size_t)g.sl * 9;
+    TRY(dalloc(s, &s->mats, 3 * n2));
+    TRYC(cudaMemsetAsync(s->mats, 0, 3 * n2 * sizeof(float), st));
+    dim3 b(32, 8), gr((g.ni + 31) / 32, (g.nj + 7) / 8);
+    const float *M = s->metric;
+    k_dvh2dvz_iso<<<gr, b, 0, st>>>(g, M + vol, M + 2 * vol, M + 3 * vol,
+                                    M + 4 * vol, M + 5 * vol, M + 6 * vol,
+                                    M + 7 * vol, M + 8 * vol, M + 9 * vol,
+                                    s->media + vol, s->media + 2 * vol,
+                                    s->mats, s->mats + n2, s->mats + 2 * n2);
+    TRYC(cudaGetLastError());
+  }
+  /* sources */
+  if (p->src_n > 0) {
+    std::vector<int> col;
+    std::vector<SrcEntry> ent;
+    build_source_entries(p, col, ent);
+    s->nsrc_ent = (int)ent.size();
+    TRY(dalloc(s, &s->src_col, col.size()));
+    TRYC(cudaMemcpyAsync(s->src_col, col.data(), col.size() * 4, cudaMemcpyHostToDevice, st));
+    TRY(dalloc(s, &s->src_ent, ent.size() > 0 ? ent.size() : 1));
+    if (!ent.empty())
+      TRYC(cudaMemcpyAsync(s->src_ent, ent.data(), ent.size() * sizeof(SrcEntry),
+                           cudaMemcpyHostToDevice, st));
+    TRY(dalloc(s, &s->src_it_begin, p->src_n));
+    TRY(dalloc(s, &s->src_it_end, p->src_n));
+    TRYC(cudaMemcpyAsync(s->src_it_begin, p->src_it_begin, p->src_n * 4, cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemcpyAsync(s->src_it_end, p->src_it_end, p->src_n * 4, cudaMemcpyHostToDevice, st));
+    size_t nstf = (size_t)p->src_n * p->src_max_nt * p->src_max_stage;
+    TRY(dalloc(s, &s->stf, 9 * nstf));
+    TRYC(cudaMemsetAsync(s->stf, 0, 9 * nstf * sizeof(float), st));
+    const float *tabs[9] = {p->Fx, p->Fy, p->Fz, p->Mxx, p->Myy, p->Mzz, p->Mxz, p->Myz, p->Mxy};
+    int use[9] = {p->src_force, p->src_force, p->src_force, p->src_moment, p->src_moment,
+                  p->src_moment, p->src_moment, p->src_moment, p->src_moment};
+    for (int t = 0; t < 9; t++)
+      if (use[t] && tabs[t])
+        TRYC(cudaMemcpyAsync(s->stf + t * nstf, tabs[t], nstf * 4, cudaMemcpyHostToDevice, st));
+  }
+  /* receivers and lines */
+  if (p->recv_n > 0) {
+    TRY(dalloc(s, &s->recv_dijk, 3 * (size_t)p->recv_n));
+    TRY(dalloc(s, &s->recv_idx, 8 * (size_t)p->recv_n));
+    size_t ns = (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt;
+    TRY(dalloc(s, &s->recv_seismo, ns));
+    TRYC(cudaMemcpyAsync(s->recv_dijk, p->recv_dijk, 3 * p->recv_n * 4, cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemcpyAsync(s->recv_idx, p->recv_indx1d, 8 * p->recv_n * 4, cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemsetAsync(s->recv_seismo, 0, ns * 4, st));
+  }
+  if (p->line_n > 0) {
+    TRY(dalloc(s, &s->line_iptr, p->line_n));
+    size_t ns = (size_t)p->line_n * p->ncmp * p->line_max_nt;
+    TRY(dalloc(s, &s->line_seismo, ns));
+    TRYC(cudaMemcpyAsync(s->line_iptr, p->line_iptr, p->line_n * 4, cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemsetAsync(s->line_seismo, 0, ns * 4, st));
+  }
+  TRY(dalloc(s, &s->d_it, 1));
+  TRYC(cudaMemsetAsync(s->d_it, 0, 4, st));
+  TRY(dalloc(s, &s->d_flag, 1));
+  TRYC(cudaStreamSynchronize(st));
+  *out = s;
+  return 0;
+#undef TRY
+#undef TRYC
+}
+
+/* level roles of the four device levels for one stage */
+static void stage_levels(cgfd_solver_t *s, int istage, float **cur, float **pre,
+                         float **tmp_out, float **end)
+{
+  size_t L = level_floats(s->g);
+  float *base = s->wav;
+  int tA = 1, tB = 2;
+  *pre = base + s->pre_lev * L;
+  *end = base + s->end_lev * L;
+  if (istage == 0) { *cur = *pre; *tmp_out = base + tA * L; }
+  else if (istage == 1) { *cur = base + tA * L; *tmp_out = base + tB * L; }
+  else if (istage == 2) { *cur = base + tB * L; *tmp_out = base + tA * L; }
+  else { *cur = base + tA * L; *tmp_out = nullptr; }
+}
+
+typedef void (*stage_fn)(const StageArgs);
+
+template <int BX, int BY, int BZ>
+static void launch_stage(int kind, dim3 gr, dim3 b, cudaStream_t st, const StageArgs &a)
+{
+  if (kind == 0) k_stage<BX, BY, BZ, 0><<<gr, b, 0, st>>>(a);
+  else if (kind == 1) k_stage<BX, BY, BZ, 1><<<gr, b, 0, st>>>(a);
+  else k_stage<BX, BY, BZ, 2><<<gr, b, 0, st>>>(a);
+}
+
+static const int PAIR_FLAGS[8][3] = {{0, 0, 0}, {1, 1, 0}, {1, 1, 1}, {0, 0, 1},
+                                     {0, 1, 0}, {1, 0, 0}, {1, 0, 1}, {0, 1, 1}};
+static const float RK_A[3] = {0.5f, 0.5f, 1.0f};
+static const float RK_B[4] = {(float)(1.0 / 6.0), (float)(1.0 / 3.0),
+                              (float)(1.0 / 3.0), (float)(1.0 / 6.0)};
+
+static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
+{
+  const cgfd_problem_t *p = s->p;
+  memset(&a, 0, sizeof(a));
+  a.g = s->g;
+  size_t vol = s->g.vol;
+  const float *M = s->metric;
+  a.jac = M; a.xix = M + vol; a.xiy = M + 2 * vol; a.xiz = M + 3 * vol;
+  a.etx = M + 4 * vol; a.ety = M + 5 * vol; a.etz = M + 6 * vol;
+  a.ztx = M + 7 * vol; a.zty = M + 8 * vol; a.ztz = M + 9 * vol;
+  a.slw = s->media; a.lam = s->media + vol; a.mu = s->media + 2 * vol;
+  float *cur, *pre, *tmp, *end;
+  stage_levels(s, istage, &cur, &pre, &tmp, &end);
+  a.cur = cur; a.pre = pre; a.tmp_out = tmp; a.end = end;
+  a.ca = istage < 3 ? RK_A[istage] * p->dt : 0.f;
+  a.cb = RK_B[istage] * p->dt;
+  for (int f = 0; f < CGFD_NFACE; f++) {
+    a.face[f] = s->face[f];
+    if (!s->face[f].on) continue;
+    size_t al = 9 * (size_t)s->face[f].avol;
+    float *b = s->aux[f];
+    float *apre = b + s->pre_lev * al, *aend = b + s->end_lev * al;
+    float *tA = b + 1 * al, *tB = b + 2 * al;
+    a.apre[f] = apre;
+    a.aend[f] = aend;
+    if (istage == 0) { a.acur[f] = apre; a.atmp_out[f] = tA; }
+    else if (istage == 1) { a.acur[f] = tA; a.atmp_out[f] = tB; }
+    else if (istage == 2) { a.acur[f] = tB; a.atmp_out[f] = tA; }
+    else { a.acur[f] = tA; a.atmp_out[f] = nullptr; }
+  }
+  a.free_top = p->free_top;
+  if (p->free_top) {
+    size_t n2 = (size_t)s->g.sl * 9;
+    a.mVx = s->mats; a.mVy = s->mats + n2; a.mF = s->mats + 2 * n2;
+  }
+  if (p->src_n > 0) {
+    a.src_n = p->src_n;
+    a.src_max_nt = p->src_max_nt;
+    a.src_max_stage = p->src_max_stage;
+    a.src_force = p->src_force;
+    a.src_moment = p->src_moment;
+    a.src_col = s->src_col;
+    a.src_ent = s->src_ent;
+    a.src_it_begin = s->src_it_begin;
+    a.src_it_end = s->src_it_end;
+    size_t nstf = (size_t)p->src_n * p->src_max_nt * p->src_max_stage;
+    a.Fx = s->stf; a.Fy = s->stf + nstf; a.Fz = s->stf + 2 * nstf;
+    a.Mxx = s->stf + 3 * nstf; a.Myy = s->stf + 4 * nstf; a.Mzz = s->stf + 5 * nstf;
+    a.Mxz = s->stf + 6 * nstf; a.Myz = s->stf + 7 * nstf; a.Mxy = s->stf + 8 * nstf;
+  }
+  a.d_it = s->d_it;
+  a.istage = istage;
+}
+
+/* enqueue one step (4 stages + receivers) for step index `it` */
+static int enqueue_step(cgfd_solver_t *s, int it, bool timed)
+{
+  const cgfd_problem_t *p = s->p;
+  cudaStream_t st = s->stream;
+  int ipair = it % 8;
+  dim3 b(TX, TY);
+  dim3 gr((s->g.ni + TX - 1) / TX, (s->g.nj + TY - 1) / TY,
+          (s->g.nk + KCHUNK - 1) / KCHUNK);
+  for (int is = 0; is < 4; is++) {
+    StageArgs a;
+    fill_args(s, a, is);
+    int bx = (PAIR_FLAGS[ipair][0] + is) % 2;
+    int by = (PAIR_FLAGS[ipair][1] + is) % 2;
+    int bz = (PAIR_FLAGS[ipair][2] + is) % 2;
+    int kind = is == 0 ? 0 : (is < 3 ? 1 : 2);
+    int code = bx * 4 + by * 2 + bz;
+    switch (code) {
+      case 0: launch_stage<0, 0, 0>(kind, gr, b, st, a); break;
+      case 1: launch_stage<0, 0, 1>(kind, gr, b, st, a); break;
+      case 2: launch_stage<0, 1, 0>(kind, gr, b, st, a); break;
+      case 3: launch_stage<0, 1, 1>(kind, gr, b, st, a); break;
+      case 4: launch_stage<1, 0, 0>(kind, gr, b, st, a); break;
+      case 5: launch_stage<1, 0, 1>(kind, gr, b, st, a); break;
+      case 6: launch_stage<1, 1, 0>(kind, gr, b, st, a); break;
+      default: launch_stage<1, 1, 1>(kind, gr, b, st, a); break;
+    }
+  }
+  size_t L = level_floats(s->g);
+  k_recv<<<1, 256, 0, st>>>(s->wav + s->end_lev * L, s->g.vol, p->ncmp,
+                            p->recv_n, p->recv_ncmp, p->recv_max_nt, s->recv_dijk,
+                            s->recv_idx, s->recv_seismo, p->line_n, p->line_max_nt,
+                            s->line_iptr, s->line_seismo, s->d_it);
+  (void)timed;
+  /* swap pre and end (forward/drv_rk_curv_col.c:530-542) */
+  int t = s->pre_lev; s->pre_lev = s->end_lev; s->end_lev = t;
+  return 0;
+}
+
+extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (nsteps < 0 || s->step + nsteps > s->p->nt_total)
+    return set_err(CGFD_EINVAL, "run(%d) past nt_total=%d (at step %d)", nsteps,
+                   s->p->nt_total, s->step);
+  CK(cudaEventRecord(s->ev0, s->stream));
+  for (int n = 0; n < nsteps; n++) {
+    enqueue_step(s, s->step, false);
+    s->step++;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(s->ev1, s->stream));
+  CK(cudaEventSynchronize(s->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+  s->t_stage_ms = ms;
+  s->n_stage = 4 * nsteps;
+  s->n_other = nsteps;
+  return 0;
+}
+
+extern "C" int cgfd_solver_step(const cgfd_solver_t *s) { return s ? s->step : -1; }
+
+extern "C" int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3])
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  out[0] = s->t_stage_ms; out[1] = 0.f; out[2] = s->t_other_ms;
+  count[0] = s->n_stage; count[1] = 0; count[2] = s->n_other;
+  return 0;
+}
+
+extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  const cgfd_problem_t *p = s->p;
+  size_t L = level_floats(s->g);
+  int host_lev = (s->step % 2 == 1) ? 3 : 0;
+  CK(cudaMemcpyAsync(p->wav + host_lev * L, s->wav + s->pre_lev * L,
+                     L * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  for (int d = 0; d < 3; d++)
+    for (int sd = 0; sd < 2; sd++) {
+      int f = d * 2 + sd;
+      if (!s->face[f].on) continue;
+      size_t al = 9 * (size_t)s->face[f].avol;
+      CK(cudaMemcpyAsync(p->pml[d][sd].aux + host_lev * al, s->aux[f] + s->pre_lev * al,
+                         al * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    }
+  if (p->recv_n > 0)
+    CK(cudaMemcpyAsync(p->recv_seismo, s->recv_seismo,
+                       (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt * 4,
+                       cudaMemcpyDeviceToHost, s->stream));
+  if (p->line_n > 0)
+    CK(cudaMemcpyAsync(p->line_seismo, s->line_seismo,
+                       (size_t)p->line_n * p->ncmp * p->line_max_nt * 4,
+                       cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+extern "C" int cgfd_solver_check_finite(cgfd_solver_t *s)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  size_t L = level_floats(s->g);
+  CK(cudaMemsetAsync(s->d_flag, 0, 4, s->stream));
+  k_nonfinite<<<152 * 4, 256, 0, s->stream>>>(s->wav + s->pre_lev * L, L, s->d_flag);
+  CK(cudaGetLastError());
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, s->d_flag, 4, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return h ? set_err(CGFD_ENONFINITE, "wavefield holds NaN/Inf at step %d", s->step) : 0;
+}
+
+extern "C" int cgfd_allstep(const cgfd_problem_t *p)
+{
+  cgfd_solver_t *s = nullptr;
+  int rc = cgfd_solver_create(p, &s);
+  if (rc) return rc;
+  rc = cgfd_solver_run(s, p->nt_total);
+  if (!rc) rc = cgfd_solver_fetch(s);
+  cgfd_solver_destroy(s);
+  return rc;
+}

@@ -524,6 +524,11 @@ static void rhs_src(orc_t *o, float *h, int it, int istage)
     }
     int si = p->src_si[is], sj = p->src_sj[is], sk = p->src_sk[is];
     if (p->src_spatial == CGFD_SRC_POINT) {
+      /* a point source outside the physical region is not located
+         (src_t.c:481-495 keeps only sources inside the domain) */
+      if (si < p->ni1 || si > p->ni2 || sj < p->nj1 || sj > p->nj2 ||
+          sk < p->nk1 || sk > p->nk2)
+        continue;
       size_t q = si + sj * ln + (size_t)sk * sl;
       if (p->src_force && (p->src_surface_strict == 0 || sk < p->nk2)) {
         float Vf = p->slw[q] / p->jac[q];

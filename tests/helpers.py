@@ -1,0 +1,28 @@
+"""Comparison helpers shared by the parity tests."""
+
+import numpy as np
+
+# tolerances of the parity bar: relative L2 and max-abs relative to the peak
+REL_L2 = 1e-5
+MAX_ABS_OF_PEAK = 1e-4
+
+
+def rel_l2(got, ref):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    n = np.linalg.norm(ref)
+    return float(np.linalg.norm(got - ref) / n) if n > 0 else float(np.linalg.norm(got))
+
+
+def max_abs_of_peak(got, ref):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    pk = np.abs(ref).max()
+    return float(np.abs(got - ref).max() / pk) if pk > 0 else float(np.abs(got).max())
+
+
+def assert_parity(got, ref, what=""):
+    r, m = rel_l2(got, ref), max_abs_of_peak(got, ref)
+    assert r <= REL_L2 and m <= MAX_ABS_OF_PEAK, \
+        "%s: rel_l2=%.3e max_abs/peak=%.3e" % (what, r, m)
+    return r, m
