@@ -1,0 +1,336 @@
+#!/usr/bin/env python
+"""Benchmark of the CGFD3D time-stepping hot path on GB300.
+
+Metric: grid-point RK-stage updates per second (N_phys * 4 * steps / time)
+on the curvilinear-topography isotropic workload (400 x 400 x 200 physical
+points, CFS-PML 12 layers on five faces, traction-image free surface, a
+double-couple source and 400 surface receivers), synthetic and seeded.
+
+One "step" is one RK4 time step (four stage kernels + the receiver gather)
+of the whole model, with every input resident in HBM (~7 GB, far larger than
+the 129 MB L2, so no flush is needed between steps).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU runs (torchrun, one rank per GPU) are independent replicas of the
+whole model: the single-domain path keeps the domain on one GPU, so ranks
+share nothing but the barrier and the max-over-ranks timing.
+"""
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "grid-pt RK-stage updates/s"
+UNIT = "pt-stage/s"
+BYTES_PER_PT_STAGE = 192       # algorithmic HBM bytes per point-stage (iso)
+WORKLOAD = dict(ni=400, nj=400, nk=200)
+SAMPLE_NK = 24                 # CPU sample: same model, 24 planes deep
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ni", type=int, default=WORKLOAD["ni"])
+    ap.add_argument("--nj", type=int, default=WORKLOAD["nj"])
+    ap.add_argument("--nk", type=int, default=WORKLOAD["nk"])
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak_hbm():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_point_stage():
+    """DRAM bytes per point-stage of the stage kernel from the committed ncu
+    summary (profiles/k_stage_topo_traffic.json), or None."""
+    path = os.path.join(REPO, "profiles", "k_stage_topo_traffic.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["dram_bytes_per_point_stage"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+def build_model(args, steps, nk=None):
+    from cgfd3d_gb300 import models
+    return models.topo_model(ni=args.ni, nj=args.nj, nk=nk or args.nk,
+                             steps=steps, dt=0.01, nrecv=400)
+
+
+def pin_problem(p):
+    """Move the large host arrays of a problem into pinned memory."""
+    import numpy as np
+    import torch
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float32, pin_memory=True)
+        out = t.numpy()
+        out[:] = a.ravel()
+        out._pin_owner = t  # noqa: keep the tensor alive
+        return out
+
+    holders = []
+    for k in list(p.metric):
+        p.metric[k] = pinned(p.metric[k])
+    for k in list(p.media):
+        p.media[k] = pinned(p.media[k])
+    p.wav = pinned(p.wav)
+    return holders
+
+
+def cpu_rate(args, steps, threads):
+    """Oracle (CPU port of the reference path) on a bounded sample."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.build()
+    p = build_model(args, steps - 1, nk=SAMPLE_NK)
+    t0 = time.perf_counter()
+    oracle.allstep(p, oracle.TIMG_ZERO, threads)
+    t = time.perf_counter() - t0
+    n = p.ni * p.nj * p.nk * 4 * p.nt_total
+    return n / t, t, p
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    # warm-up sample, then the timed samples (one RK4 step each)
+    cpu_rate(args, 1, threads)
+    rates, tot = [], 0.0
+    for _ in range(max(args.warmup, 0)):
+        cpu_rate(args, 1, threads)
+    for _ in range(args.steps):
+        r, t, p = cpu_rate(args, 1, threads)
+        rates.append(r)
+        tot += t
+    rate = args.steps / sum(1.0 / r for r in rates)
+    sample = ("one RK4 step of the %dx%dx%d topography model (same generator, "
+              "nk cut to %d), C oracle port, %d threads" %
+              (args.ni, args.nj, args.nk, SAMPLE_NK, threads))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": "topography iso %dx%dx%d (CPU sample nk=%d)" %
+                   (args.ni, args.nj, args.nk, SAMPLE_NK)},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from cgfd3d_gb300 import solver
+
+    K, W = args.steps, max(args.warmup, 0)
+    p = build_model(args, K + W)
+    n_phys = p.ni * p.nj * p.nk
+
+    # ---- device-resident timing ------------------------------------------
+    s = solver.Solver(p)
+    s.run(W)
+    s.set_timing(True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.6)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    s.run(K)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    (t_stage, t_total, _), (n_stage, n_all, _) = s.kernel_times()
+    s.check_finite()
+    s.close()
+    t = t_total * 1e-3
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * n_phys * 4 * K / t
+
+    # ---- roofline of the stage kernel -----------------------------------
+    peak, peak_kind = measured_peak_hbm()
+    avg_launch = t_stage * 1e-3 / n_stage
+    alg_bytes = n_phys * BYTES_PER_PT_STAGE
+    achieved = alg_bytes / avg_launch / 1e9
+    tpp = traffic_per_point_stage()
+
+    # ---- end to end through the C ABI with host (pinned) buffers ---------
+    q = build_model(args, K - 1)
+    pin_problem(q)
+    # one small call first so that module loading is not timed
+    from cgfd3d_gb300 import models
+    solver.drv_rk_curv_col_allstep(models.topo_model(ni=48, nj=48, nk=40, steps=1,
+                                                     dt=0.01, nrecv=4))
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    se = solver.Solver(q)
+    se.run(q.nt_total)
+    se.fetch()
+    h2d, d2h = se.transfer_bytes()
+    se.close()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([t_e2e], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = world * n_phys * 4 * q.nt_total / t_e2e
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": 1e3 * t / K,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": "topography iso %dx%dx%d, CFS-PML 12 on 5 faces, "
+                   "timg free surface, DC point source, 400 receivers" %
+                   (args.ni, args.nj, args.nk),
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs (%.1f GB resident) larger than L2, no flush"
+                         % (solver.device_bytes(p) / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind,
+                     "traffic": None if tpp is None else tpp * n_phys,
+                     "alg_bytes_per_launch": alg_bytes,
+                     "avg_launch_ms": avg_launch * 1e3},
+        "e2e": {"value": e2e, "unit": UNIT,
+                "h2d_bytes_per_step": h2d / q.nt_total,
+                "d2h_bytes_per_step": d2h / q.nt_total,
+                "steps": q.nt_total},
+        "gpu_launches": n_all,
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r, tcpu, _ = cpu_rate(args, 1, threads)
+        line["cpu_baseline"] = {
+            "value": r, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "one RK4 step of the same model cut to nk=%d, C oracle "
+                      "port, %d threads, %.1f s" % (SAMPLE_NK, threads, tcpu)}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -39,6 +39,8 @@ def lib():
     L.cgfd_solver_step.argtypes = [vp]
     L.cgfd_solver_check_finite.argtypes = [vp]
     L.cgfd_solver_kernel_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    L.cgfd_solver_set_timing.argtypes = [vp, C.c_int]
+    L.cgfd_solver_transfer_bytes.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     L.cgfd_solver_destroy.argtypes = [vp]
     L.cgfd_solver_destroy.restype = None
     L.cgfd_allstep.argtypes = [vp]

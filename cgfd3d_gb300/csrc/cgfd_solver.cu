@@ -327,8 +327,10 @@ struct cgfd_solver {
   int pre_lev, end_lev;         /* level of pre/end in wav (0 or 3) */
   int nsrc_ent;
   size_t bytes;
+  size_t h2d_bytes, d2h_bytes;
   cudaEvent_t ev0, ev1;
-  float t_stage_ms, t_other_ms;
+  std::vector<cudaEvent_t> kev;   /* per-launch timing events */
+  float t_stage_ms, t_other_ms, t_total_ms;
   int n_stage, n_other;
   int timing;
   cudaGraphExec_t graph8;
@@ -442,6 +444,7 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
   for (int f = 0; f < CGFD_NFACE; f++) {
     if (s->face[f].A) cudaFree((void *)s->face[f].A);
   }
+  for (cudaEvent_t e : s->kev) cudaEventDestroy(e);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -454,7 +457,6 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   int rc = validate(p);
   if (rc) return rc;
   cgfd_solver_t *s = new cgfd_solver_t();
-  memset((void *)s, 0, sizeof(*s));
   s->p = p;
   DevGrid &g = s->g;
   g.ni = p->ni; g.nj = p->nj; g.nk = p->nk;
@@ -474,9 +476,12 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
    * ghost values stay what the caller passed (they never change in the
    * reference either: rhs ghosts are zero) */
   TRY(dalloc(s, &s->wav, 4 * L));
-  for (int l = 0; l < 4; l++)
-    TRYC(cudaMemcpyAsync(s->wav + l * L, p->wav, L * sizeof(float),
-                         cudaMemcpyHostToDevice, st));
+  TRYC(cudaMemcpyAsync(s->wav, p->wav, L * sizeof(float),
+                       cudaMemcpyHostToDevice, st));
+  for (int l = 1; l < 4; l++)
+    TRYC(cudaMemcpyAsync(s->wav + l * L, s->wav, L * sizeof(float),
+                         cudaMemcpyDeviceToDevice, st));
+  s->h2d_bytes += L * sizeof(float);
   s->pre_lev = 0;
   s->end_lev = 3;
   TRY(dalloc(s, &s->metric, 10 * vol));
@@ -485,11 +490,13 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   for (int m = 0; m < 10; m++)
     TRYC(cudaMemcpyAsync(s->metric + m * vol, mh[m], vol * sizeof(float),
                          cudaMemcpyHostToDevice, st));
+  s->h2d_bytes += 10 * vol * sizeof(float);
   TRY(dalloc(s, &s->media, 3 * vol));
   const float *md[3] = {p->slw, p->lambda, p->mu};
   for (int m = 0; m < 3; m++)
     TRYC(cudaMemcpyAsync(s->media + m * vol, md[m], vol * sizeof(float),
                          cudaMemcpyHostToDevice, st));
+  s->h2d_bytes += 3 * vol * sizeof(float);
   /* PML faces */
   int nf = 0;
   for (int d = 0; d < 3; d++)
@@ -516,9 +523,12 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
       F.A = coef; F.B = coef + np; F.D = coef + 2 * np;
       size_t al = 9 * (size_t)F.avol;
       TRY(dalloc(s, &s->aux[fi], 4 * al));
-      for (int l = 0; l < 4; l++)
-        TRYC(cudaMemcpyAsync(s->aux[fi] + l * al, f->aux, al * sizeof(float),
-                             cudaMemcpyHostToDevice, st));
+      TRYC(cudaMemcpyAsync(s->aux[fi], f->aux, al * sizeof(float),
+                           cudaMemcpyHostToDevice, st));
+      for (int l = 1; l < 4; l++)
+        TRYC(cudaMemcpyAsync(s->aux[fi] + l * al, s->aux[fi], al * sizeof(float),
+                             cudaMemcpyDeviceToDevice, st));
+      s->h2d_bytes += al * sizeof(float) + 3 * np * sizeof(float);
     }
   (void)nf;
   /* free surface matrices, computed on the device */
@@ -674,7 +684,7 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
 }
 
 /* enqueue one step (4 stages + receivers) for step index `it` */
-static int enqueue_step(cgfd_solver_t *s, int it, bool timed)
+static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
 {
   const cgfd_problem_t *p = s->p;
   cudaStream_t st = s->stream;
@@ -690,6 +700,7 @@ static int enqueue_step(cgfd_solver_t *s, int it, bool timed)
     int bz = (PAIR_FLAGS[ipair][2] + is) % 2;
     int kind = is == 0 ? 0 : (is < 3 ? 1 : 2);
     int code = bx * 4 + by * 2 + bz;
+    if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
     switch (code) {
       case 0: launch_stage<0, 0, 0>(kind, gr, b, st, a); break;
       case 1: launch_stage<0, 0, 1>(kind, gr, b, st, a); break;
@@ -700,13 +711,13 @@ static int enqueue_step(cgfd_solver_t *s, int it, bool timed)
       case 6: launch_stage<1, 1, 0>(kind, gr, b, st, a); break;
       default: launch_stage<1, 1, 1>(kind, gr, b, st, a); break;
     }
+    if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
   size_t L = level_floats(s->g);
   k_recv<<<1, 256, 0, st>>>(s->wav + s->end_lev * L, s->g.vol, p->ncmp,
                             p->recv_n, p->recv_ncmp, p->recv_max_nt, s->recv_dijk,
                             s->recv_idx, s->recv_seismo, p->line_n, p->line_max_nt,
                             s->line_iptr, s->line_seismo, s->d_it);
-  (void)timed;
   /* swap pre and end (forward/drv_rk_curv_col.c:530-542) */
   int t = s->pre_lev; s->pre_lev = s->end_lev; s->end_lev = t;
   return 0;
@@ -718,9 +729,16 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   if (nsteps < 0 || s->step + nsteps > s->p->nt_total)
     return set_err(CGFD_EINVAL, "run(%d) past nt_total=%d (at step %d)", nsteps,
                    s->p->nt_total, s->step);
+  int nev = s->timing ? 8 * nsteps : 0;
+  while ((int)s->kev.size() < nev) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    s->kev.push_back(e);
+  }
+  int ev = 0;
   CK(cudaEventRecord(s->ev0, s->stream));
   for (int n = 0; n < nsteps; n++) {
-    enqueue_step(s, s->step, false);
+    enqueue_step(s, s->step, s->timing ? &ev : nullptr);
     s->step++;
   }
   CK(cudaGetLastError());
@@ -728,7 +746,16 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   CK(cudaEventSynchronize(s->ev1));
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
-  s->t_stage_ms = ms;
+  s->t_total_ms = ms;
+  s->t_stage_ms = 0.f;
+  if (s->timing) {
+    for (int e = 0; e < ev; e += 2) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, s->kev[e], s->kev[e + 1]));
+      s->t_stage_ms += t;
+    }
+  }
+  s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
   s->n_other = nsteps;
   return 0;
@@ -739,8 +766,23 @@ extern "C" int cgfd_solver_step(const cgfd_solver_t *s) { return s ? s->step : -
 extern "C" int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3])
 {
   if (!s) return set_err(CGFD_EINVAL, "null solver");
-  out[0] = s->t_stage_ms; out[1] = 0.f; out[2] = s->t_other_ms;
-  count[0] = s->n_stage; count[1] = 0; count[2] = s->n_other;
+  out[0] = s->t_stage_ms; out[1] = s->t_total_ms; out[2] = s->t_other_ms;
+  count[0] = s->n_stage; count[1] = s->n_stage + s->n_other; count[2] = s->n_other;
+  return 0;
+}
+
+extern "C" int cgfd_solver_set_timing(cgfd_solver_t *s, int on)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  s->timing = on ? 1 : 0;
+  return 0;
+}
+
+extern "C" int cgfd_solver_transfer_bytes(const cgfd_solver_t *s, size_t *h2d, size_t *d2h)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  *h2d = s->h2d_bytes;
+  *d2h = s->d2h_bytes;
   return 0;
 }
 
@@ -752,6 +794,7 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
   int host_lev = (s->step % 2 == 1) ? 3 : 0;
   CK(cudaMemcpyAsync(p->wav + host_lev * L, s->wav + s->pre_lev * L,
                      L * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  s->d2h_bytes += L * sizeof(float);
   for (int d = 0; d < 3; d++)
     for (int sd = 0; sd < 2; sd++) {
       int f = d * 2 + sd;
@@ -759,15 +802,20 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
       size_t al = 9 * (size_t)s->face[f].avol;
       CK(cudaMemcpyAsync(p->pml[d][sd].aux + host_lev * al, s->aux[f] + s->pre_lev * al,
                          al * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+      s->d2h_bytes += al * sizeof(float);
     }
-  if (p->recv_n > 0)
-    CK(cudaMemcpyAsync(p->recv_seismo, s->recv_seismo,
-                       (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt * 4,
+  if (p->recv_n > 0) {
+    size_t nb = (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt * 4;
+    CK(cudaMemcpyAsync(p->recv_seismo, s->recv_seismo, nb,
                        cudaMemcpyDeviceToHost, s->stream));
-  if (p->line_n > 0)
-    CK(cudaMemcpyAsync(p->line_seismo, s->line_seismo,
-                       (size_t)p->line_n * p->ncmp * p->line_max_nt * 4,
+    s->d2h_bytes += nb;
+  }
+  if (p->line_n > 0) {
+    size_t nb = (size_t)p->line_n * p->ncmp * p->line_max_nt * 4;
+    CK(cudaMemcpyAsync(p->line_seismo, s->line_seismo, nb,
                        cudaMemcpyDeviceToHost, s->stream));
+    s->d2h_bytes += nb;
+  }
   CK(cudaStreamSynchronize(s->stream));
   return 0;
 }

@@ -43,6 +43,14 @@ class Solver:
         _lib.check(_lib.lib().cgfd_solver_kernel_times(self._h, t, n))
         return list(t), list(n)
 
+    def set_timing(self, on=True):
+        _lib.check(_lib.lib().cgfd_solver_set_timing(self._h, int(bool(on))))
+
+    def transfer_bytes(self):
+        h, d = C.c_size_t(), C.c_size_t()
+        _lib.check(_lib.lib().cgfd_solver_transfer_bytes(self._h, C.byref(h), C.byref(d)))
+        return h.value, d.value
+
     def close(self):
         if self._h:
             _lib.lib().cgfd_solver_destroy(self._h)

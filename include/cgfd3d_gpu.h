@@ -149,10 +149,17 @@ int cgfd_solver_step(const cgfd_solver_t *s);
  * Returns CGFD_OK or CGFD_ENONFINITE. */
 int cgfd_solver_check_finite(cgfd_solver_t *s);
 
-/* Sum of CUDA-event time of the last cgfd_solver_run, per kernel family:
- * out[0] = interior launches, out[1] = surface launches, out[2] = other;
- * count[] the launches.  Units: milliseconds. */
+/* CUDA-event times of the last cgfd_solver_run, milliseconds:
+ * out[0] = sum over the stage-kernel launches (only with timing on),
+ * out[1] = the whole run, out[2] = the rest (receivers, bookkeeping);
+ * count[0] stage launches, count[1] all launches, count[2] the rest. */
 int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3]);
+
+/* Record a CUDA event pair around every stage launch of later runs. */
+int cgfd_solver_set_timing(cgfd_solver_t *s, int on);
+
+/* Host<->device bytes moved so far (uploads at create, fetches). */
+int cgfd_solver_transfer_bytes(const cgfd_solver_t *s, size_t *h2d, size_t *d2h);
 
 void cgfd_solver_destroy(cgfd_solver_t *s);
 
