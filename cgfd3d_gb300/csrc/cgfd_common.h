@@ -26,11 +26,17 @@
 /* component order of the reference (forward/wav_t.c:93-136) */
 enum { C_VX = 0, C_VY, C_VZ, C_TXX, C_TYY, C_TZZ, C_TYZ, C_TXZ, C_TXY };
 
+/* Device volumes are pitched: row pitch px >= nx + xoff (multiple of 32
+ * floats) and x offset xoff chosen so that the first physical column
+ * (i = 3) starts a 128-byte line; element (i,j,k) sits at
+ * (i + xoff) + j*px + k*px*ny.  This keeps every warp-wide row access and
+ * every TMA box aligned. */
 struct DevGrid {
   int ni, nj, nk, nx, ny, nz;
   int ni1, ni2, nj1, nj2, nk1, nk2;
-  long long sl;   /* nx*ny */
-  long long vol;  /* nx*ny*nz */
+  int px, xoff;
+  long long sl;   /* px*ny */
+  long long vol;  /* px*ny*nz */
 };
 
 struct DevFace {
@@ -80,6 +86,9 @@ struct StageArgs {
   const float *Fx, *Fy, *Fz, *Mxx, *Myy, *Mzz, *Mxz, *Myz, *Mxy;
   const int *d_it;             /* current step on the device */
   int istage;
+  int *err;                    /* device error word (bounded waits) */
+  int cur_level;               /* level index of `cur` (TMA coordinate) */
+  int kchunk;                  /* planes per CTA along k */
 };
 
 #endif

@@ -25,6 +25,7 @@
 #include "../../include/cgfd3d_gpu.h"
 #include "cgfd_common.h"
 #include "cgfd_stage.cuh"
+#include "cgfd_stage2.cuh"
 
 /* ------------------------------------------------------------------------ */
 /* errors                                                                    */
@@ -58,19 +59,19 @@ extern "C" int cgfd_abi_version(void) { return CGFD_ABI_VERSION; }
 /* kernels                                                                   */
 /* ------------------------------------------------------------------------ */
 
-#define TX 32
-#define TY 4
-#define KCHUNK 8
+#define V1_TX 32
+#define V1_TY 4
+#define V1_KCHUNK 8
 
 template <int BX, int BY, int BZ, int KIND>
-__global__ void __launch_bounds__(TX *TY)
+__global__ void __launch_bounds__(V1_TX *V1_TY)
     k_stage(const __grid_constant__ StageArgs a)
 {
-  int i = a.g.ni1 + blockIdx.x * TX + threadIdx.x;
-  int j = a.g.nj1 + blockIdx.y * TY + threadIdx.y;
+  int i = a.g.ni1 + blockIdx.x * V1_TX + threadIdx.x;
+  int j = a.g.nj1 + blockIdx.y * V1_TY + threadIdx.y;
   if (i > a.g.ni2 || j > a.g.nj2) return;
-  int k0 = a.g.nk1 + blockIdx.z * KCHUNK;
-  int k1 = min(k0 + KCHUNK - 1, a.g.nk2);
+  int k0 = a.g.nk1 + blockIdx.z * V1_KCHUNK;
+  int k1 = min(k0 + V1_KCHUNK - 1, a.g.nk2);
   for (int k = k0; k <= k1; k++) stage_point<BX, BY, BZ, KIND>(a, i, j, k);
 }
 
@@ -92,7 +93,7 @@ __global__ void k_dvh2dvz_iso(DevGrid g, const float *__restrict__ xix,
   int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
   int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
   if (i > g.ni2 || j > g.nj2) return;
-  long long q = i + (long long)j * g.nx + (long long)g.nk2 * g.sl;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
   float e11 = xix[q], e12 = xiy[q], e13 = xiz[q];
   float e21 = etx[q], e22 = ety[q], e23 = etz[q];
   float e31 = ztx[q], e32 = zty[q], e33 = ztz[q];
@@ -335,13 +336,20 @@ struct cgfd_solver {
   int timing;
   cudaGraphExec_t graph8;
   int graph_pre_lev;
+  int *d_err;
+  CUtensorMap tmap;             /* 5-D map over the four wavefield levels */
+  int kernel;                   /* 2: TMA z-marching (default), 1: direct */
+  int kchunk;
 };
 
 static size_t level_floats(const DevGrid &g) { return (size_t)CGFD_NCMP * g.vol; }
 
+static int pitch_for(int ni) { return 32 * ((ni + 31) / 32 + 2); }
+#define XOFF 29
+
 extern "C" size_t cgfd_device_bytes(const cgfd_problem_t *p)
 {
-  size_t vol = (size_t)p->nx * p->ny * p->nz;
+  size_t vol = (size_t)pitch_for(p->ni) * p->ny * p->nz;
   size_t b = (4 * 9 + 10 + 3) * vol * sizeof(float);
   if (p->free_top) b += 3 * (size_t)p->nx * p->ny * 9 * sizeof(float);
   for (int d = 0; d < 3; d++)
@@ -416,6 +424,16 @@ static int validate(const cgfd_problem_t *p)
   return 0;
 }
 
+/* host index of the reference layout -> device (pitched) index */
+static long long dev_index(const DevGrid &g, long long h)
+{
+  long long i = h % g.nx, j = (h / g.nx) % g.ny, k = h / ((long long)g.nx * g.ny);
+  return (i + g.xoff) + j * g.px + k * g.sl;
+}
+
+static cudaError_t upload_volume(cgfd_solver_t *s, float *dst, const float *src);
+static int make_tmap(cgfd_solver_t *s);
+
 template <typename T>
 static int dalloc(cgfd_solver_t *s, T **ptr, size_t n)
 {
@@ -429,6 +447,56 @@ static int dalloc(cgfd_solver_t *s, T **ptr, size_t n)
   return 0;
 }
 
+static cudaError_t upload_volume(cgfd_solver_t *s, float *dst, const float *src)
+{
+  const DevGrid &g = s->g;
+  s->h2d_bytes += (size_t)g.nx * g.ny * g.nz * sizeof(float);
+  return cudaMemcpy2DAsync(dst + g.xoff, (size_t)g.px * sizeof(float), src,
+                           (size_t)g.nx * sizeof(float), (size_t)g.nx * sizeof(float),
+                           (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, s->stream);
+}
+
+static cudaError_t download_volume(cgfd_solver_t *s, float *dst, const float *src)
+{
+  const DevGrid &g = s->g;
+  s->d2h_bytes += (size_t)g.nx * g.ny * g.nz * sizeof(float);
+  return cudaMemcpy2DAsync(dst, (size_t)g.nx * sizeof(float), src + g.xoff,
+                           (size_t)g.px * sizeof(float), (size_t)g.nx * sizeof(float),
+                           (size_t)g.ny * g.nz, cudaMemcpyDeviceToHost, s->stream);
+}
+
+typedef CUresult (*encode_tiled_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
+                                    void *, const cuuint64_t *, const cuuint64_t *,
+                                    const cuuint32_t *, const cuuint32_t *,
+                                    CUtensorMapInterleave, CUtensorMapSwizzle,
+                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+/* 5-D tensor map (x, y, z, component, level) over the wavefield block */
+static int make_tmap(cgfd_solver_t *s)
+{
+  static encode_tiled_fn fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr,
+                                                     12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !ptr)
+      return set_err(CGFD_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = (encode_tiled_fn)ptr;
+  }
+  const DevGrid &g = s->g;
+  cuuint64_t dims[5] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 9, 4};
+  cuuint64_t strides[4] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4,
+                           (cuuint64_t)g.vol * 4, (cuuint64_t)g.vol * 9 * 4};
+  cuuint32_t box[5] = {s2::BW, s2::BH, 1, 9, 1};
+  cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(&s->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return 0;
+}
+
 extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
 {
   if (!s) return;
@@ -436,7 +504,7 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
   void *ptrs[] = {s->wav, s->metric, s->media, s->mats, s->src_col,
                   s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
                   s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
-                  s->line_iptr, s->d_it, s->d_flag};
+                  s->line_iptr, s->d_it, s->d_flag, s->d_err};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (int f = 0; f < CGFD_NFACE; f++)
@@ -463,7 +531,9 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
   g.ni1 = p->ni1; g.ni2 = p->ni2; g.nj1 = p->nj1; g.nj2 = p->nj2;
   g.nk1 = p->nk1; g.nk2 = p->nk2;
-  g.sl = (long long)p->nx * p->ny;
+  g.xoff = XOFF;
+  g.px = pitch_for(p->ni);
+  g.sl = (long long)g.px * p->ny;
   g.vol = g.sl * p->nz;
 #define TRY(x) do { int r_ = (x); if (r_) { cgfd_solver_destroy(s); return r_; } } while (0)
 #define TRYC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { set_err(CGFD_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); cgfd_solver_destroy(s); return CGFD_ECUDA; } } while (0)
@@ -471,32 +541,32 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   TRYC(cudaEventCreate(&s->ev0));
   TRYC(cudaEventCreate(&s->ev1));
   size_t vol = g.vol, L = level_floats(g);
+  size_t hvol = (size_t)p->nx * p->ny * p->nz;
   cudaStream_t st = s->stream;
   /* wavefield: level 0 of the input copied into all four levels, so that
    * ghost values stay what the caller passed (they never change in the
    * reference either: rhs ghosts are zero) */
   TRY(dalloc(s, &s->wav, 4 * L));
-  TRYC(cudaMemcpyAsync(s->wav, p->wav, L * sizeof(float),
-                       cudaMemcpyHostToDevice, st));
+  TRYC(cudaMemsetAsync(s->wav, 0, L * sizeof(float), st));
+  for (int c = 0; c < 9; c++)
+    TRYC(upload_volume(s, s->wav + c * vol, p->wav + (size_t)c * hvol));
   for (int l = 1; l < 4; l++)
     TRYC(cudaMemcpyAsync(s->wav + l * L, s->wav, L * sizeof(float),
                          cudaMemcpyDeviceToDevice, st));
-  s->h2d_bytes += L * sizeof(float);
+
   s->pre_lev = 0;
   s->end_lev = 3;
   TRY(dalloc(s, &s->metric, 10 * vol));
+  TRYC(cudaMemsetAsync(s->metric, 0, 10 * vol * sizeof(float), st));
   const float *mh[10] = {p->jac, p->xi_x, p->xi_y, p->xi_z, p->eta_x,
                          p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
   for (int m = 0; m < 10; m++)
-    TRYC(cudaMemcpyAsync(s->metric + m * vol, mh[m], vol * sizeof(float),
-                         cudaMemcpyHostToDevice, st));
-  s->h2d_bytes += 10 * vol * sizeof(float);
+    TRYC(upload_volume(s, s->metric + m * vol, mh[m]));
   TRY(dalloc(s, &s->media, 3 * vol));
+  TRYC(cudaMemsetAsync(s->media, 0, 3 * vol * sizeof(float), st));
   const float *md[3] = {p->slw, p->lambda, p->mu};
   for (int m = 0; m < 3; m++)
-    TRYC(cudaMemcpyAsync(s->media + m * vol, md[m], vol * sizeof(float),
-                         cudaMemcpyHostToDevice, st));
-  s->h2d_bytes += 3 * vol * sizeof(float);
+    TRYC(upload_volume(s, s->media + m * vol, md[m]));
   /* PML faces */
   int nf = 0;
   for (int d = 0; d < 3; d++)
@@ -578,19 +648,35 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     size_t ns = (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt;
     TRY(dalloc(s, &s->recv_seismo, ns));
     TRYC(cudaMemcpyAsync(s->recv_dijk, p->recv_dijk, 3 * p->recv_n * 4, cudaMemcpyHostToDevice, st));
-    TRYC(cudaMemcpyAsync(s->recv_idx, p->recv_indx1d, 8 * p->recv_n * 4, cudaMemcpyHostToDevice, st));
+    std::vector<int> di(8 * (size_t)p->recv_n);
+    for (size_t n = 0; n < di.size(); n++) di[n] = (int)dev_index(g, p->recv_indx1d[n]);
+    TRYC(cudaMemcpy(s->recv_idx, di.data(), di.size() * 4, cudaMemcpyHostToDevice));
     TRYC(cudaMemsetAsync(s->recv_seismo, 0, ns * 4, st));
   }
   if (p->line_n > 0) {
     TRY(dalloc(s, &s->line_iptr, p->line_n));
     size_t ns = (size_t)p->line_n * p->ncmp * p->line_max_nt;
     TRY(dalloc(s, &s->line_seismo, ns));
-    TRYC(cudaMemcpyAsync(s->line_iptr, p->line_iptr, p->line_n * 4, cudaMemcpyHostToDevice, st));
+    std::vector<int> di(p->line_n);
+    for (int n = 0; n < p->line_n; n++) di[n] = (int)dev_index(g, p->line_iptr[n]);
+    TRYC(cudaMemcpy(s->line_iptr, di.data(), di.size() * 4, cudaMemcpyHostToDevice));
     TRYC(cudaMemsetAsync(s->line_seismo, 0, ns * 4, st));
   }
   TRY(dalloc(s, &s->d_it, 1));
   TRYC(cudaMemsetAsync(s->d_it, 0, 4, st));
   TRY(dalloc(s, &s->d_flag, 1));
+  TRY(dalloc(s, &s->d_err, 1));
+  TRYC(cudaMemsetAsync(s->d_err, 0, 4, st));
+  s->kernel = 2;
+  if (const char *e = getenv("CGFD_STAGE_KERNEL")) s->kernel = atoi(e) == 1 ? 1 : 2;
+  {
+    int tiles = ((g.ni + s2::TX - 1) / s2::TX) * ((g.nj + s2::TY - 1) / s2::TY);
+    int want = 4 * 2 * 152;                 /* about four waves of CTAs */
+    int nch = std::max(1, std::min(g.nk / 16, (want + tiles - 1) / tiles));
+    s->kchunk = (g.nk + nch - 1) / nch;
+    if (const char *e = getenv("CGFD_KCHUNK")) s->kchunk = std::max(4, atoi(e));
+  }
+  TRY(make_tmap(s));
   TRYC(cudaStreamSynchronize(st));
   *out = s;
   return 0;
@@ -615,12 +701,34 @@ static void stage_levels(cgfd_solver_t *s, int istage, float **cur, float **pre,
 
 typedef void (*stage_fn)(const StageArgs);
 
-template <int BX, int BY, int BZ>
-static void launch_stage(int kind, dim3 gr, dim3 b, cudaStream_t st, const StageArgs &a)
+template <int BX, int BY, int BZ, int KIND>
+static void launch_one(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
 {
-  if (kind == 0) k_stage<BX, BY, BZ, 0><<<gr, b, 0, st>>>(a);
-  else if (kind == 1) k_stage<BX, BY, BZ, 1><<<gr, b, 0, st>>>(a);
-  else k_stage<BX, BY, BZ, 2><<<gr, b, 0, st>>>(a);
+  if (s->kernel == 1) {
+    dim3 b(V1_TX, V1_TY);
+    dim3 gr((s->g.ni + V1_TX - 1) / V1_TX, (s->g.nj + V1_TY - 1) / V1_TY,
+            (s->g.nk + V1_KCHUNK - 1) / V1_KCHUNK);
+    k_stage<BX, BY, BZ, KIND><<<gr, b, 0, st>>>(a);
+  } else {
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(s2::k_stage2<BX, BY, BZ, KIND>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, s2::SMEM_BYTES);
+      attr_set = true;
+    }
+    dim3 b(s2::TX, s2::TY);
+    dim3 gr((s->g.ni + s2::TX - 1) / s2::TX, (s->g.nj + s2::TY - 1) / s2::TY,
+            (s->g.nk + s->kchunk - 1) / s->kchunk);
+    s2::k_stage2<BX, BY, BZ, KIND><<<gr, b, s2::SMEM_BYTES, st>>>(a, s->tmap);
+  }
+}
+
+template <int BX, int BY, int BZ>
+static void launch_stage(cgfd_solver_t *s, int kind, cudaStream_t st, const StageArgs &a)
+{
+  if (kind == 0) launch_one<BX, BY, BZ, 0>(s, st, a);
+  else if (kind == 1) launch_one<BX, BY, BZ, 1>(s, st, a);
+  else launch_one<BX, BY, BZ, 2>(s, st, a);
 }
 
 static const int PAIR_FLAGS[8][3] = {{0, 0, 0}, {1, 1, 0}, {1, 1, 1}, {0, 0, 1},
@@ -681,6 +789,10 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   }
   a.d_it = s->d_it;
   a.istage = istage;
+  a.err = s->d_err;
+  a.kchunk = s->kchunk;
+  size_t L = level_floats(s->g);
+  a.cur_level = (int)((cur - s->wav) / (long long)L);
 }
 
 /* enqueue one step (4 stages + receivers) for step index `it` */
@@ -689,9 +801,6 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
   const cgfd_problem_t *p = s->p;
   cudaStream_t st = s->stream;
   int ipair = it % 8;
-  dim3 b(TX, TY);
-  dim3 gr((s->g.ni + TX - 1) / TX, (s->g.nj + TY - 1) / TY,
-          (s->g.nk + KCHUNK - 1) / KCHUNK);
   for (int is = 0; is < 4; is++) {
     StageArgs a;
     fill_args(s, a, is);
@@ -702,14 +811,14 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
     int code = bx * 4 + by * 2 + bz;
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
     switch (code) {
-      case 0: launch_stage<0, 0, 0>(kind, gr, b, st, a); break;
-      case 1: launch_stage<0, 0, 1>(kind, gr, b, st, a); break;
-      case 2: launch_stage<0, 1, 0>(kind, gr, b, st, a); break;
-      case 3: launch_stage<0, 1, 1>(kind, gr, b, st, a); break;
-      case 4: launch_stage<1, 0, 0>(kind, gr, b, st, a); break;
-      case 5: launch_stage<1, 0, 1>(kind, gr, b, st, a); break;
-      case 6: launch_stage<1, 1, 0>(kind, gr, b, st, a); break;
-      default: launch_stage<1, 1, 1>(kind, gr, b, st, a); break;
+      case 0: launch_stage<0, 0, 0>(s, kind, st, a); break;
+      case 1: launch_stage<0, 0, 1>(s, kind, st, a); break;
+      case 2: launch_stage<0, 1, 0>(s, kind, st, a); break;
+      case 3: launch_stage<0, 1, 1>(s, kind, st, a); break;
+      case 4: launch_stage<1, 0, 0>(s, kind, st, a); break;
+      case 5: launch_stage<1, 0, 1>(s, kind, st, a); break;
+      case 6: launch_stage<1, 1, 0>(s, kind, st, a); break;
+      default: launch_stage<1, 1, 1>(s, kind, st, a); break;
     }
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
@@ -758,6 +867,9 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
   s->n_other = nsteps;
+  int herr = 0;
+  CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));
+  if (herr) return set_err(CGFD_ECUDA, "device wait timed out (code %d)", herr);
   return 0;
 }
 
@@ -792,9 +904,10 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
   const cgfd_problem_t *p = s->p;
   size_t L = level_floats(s->g);
   int host_lev = (s->step % 2 == 1) ? 3 : 0;
-  CK(cudaMemcpyAsync(p->wav + host_lev * L, s->wav + s->pre_lev * L,
-                     L * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
-  s->d2h_bytes += L * sizeof(float);
+  size_t hvol = (size_t)p->nx * p->ny * p->nz;
+  for (int c = 0; c < 9; c++)
+    CK(download_volume(s, p->wav + (size_t)host_lev * 9 * hvol + c * hvol,
+                       s->wav + s->pre_lev * L + c * s->g.vol));
   for (int d = 0; d < 3; d++)
     for (int sd = 0; sd < 2; sd++) {
       int f = d * 2 + sd;

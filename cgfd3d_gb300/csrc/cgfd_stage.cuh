@@ -99,7 +99,7 @@ __device__ __forceinline__ float cons_flux(const float *__restrict__ jac,
 template <int BX, int BY, int BZ>
 __device__ float timg_row(const StageArgs &a, long long q, int k, int r)
 {
-  const long long vol = a.g.vol, nx = a.g.nx, sl = a.g.sl;
+  const long long vol = a.g.vol, nx = a.g.px, sl = a.g.sl;
   const float *w = a.cur;
   const float *Ta, *Tb, *Tc;
   if (r == 0) { Ta = w + C_TXX * vol; Tb = w + C_TXY * vol; Tc = w + C_TXZ * vol; }
@@ -240,8 +240,8 @@ __device__ __forceinline__ void stage_point(const StageArgs &a, int i, int j,
                                             int k)
 {
   const DevGrid &g = a.g;
-  const long long vol = g.vol, nx = g.nx, sl = g.sl;
-  const long long q = (long long)i + (long long)j * nx + (long long)k * sl;
+  const long long vol = g.vol, nx = g.px, sl = g.sl;
+  const long long q = (long long)(i + g.xoff) + (long long)j * nx + (long long)k * sl;
   const float *w = a.cur;
 
   Deriv9 dx, dy, dz;
@@ -271,7 +271,7 @@ __device__ __forceinline__ void stage_point(const StageArgs &a, int i, int j,
     /* vlow: z-derivatives of V replaced near the surface */
     float DzVx, DzVy, DzVz;
     if (k == nk2) {
-      long long ij = ((long long)i + (long long)j * nx) * 9;
+      long long ij = ((long long)i + (long long)j * g.nx) * 9;
       const float *A = a.mVx + ij, *Bm = a.mVy + ij;
       DzVx = LDG(A + 0) * dx.Vx + LDG(A + 1) * dx.Vy + LDG(A + 2) * dx.Vz +
              LDG(Bm + 0) * dy.Vx + LDG(Bm + 1) * dy.Vy + LDG(Bm + 2) * dy.Vz;
