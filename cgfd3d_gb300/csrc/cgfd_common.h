@@ -88,6 +88,7 @@ struct StageArgs {
   int istage;
   int *err;                    /* device error word (bounded waits) */
   int cur_level;               /* level index of `cur` (TMA coordinate) */
+  int pre_level, end_level;    /* level indices of `pre` and `end` */
   int kchunk;                  /* planes per CTA along k */
 };
 

@@ -25,7 +25,7 @@
 #include "../../include/cgfd3d_gpu.h"
 #include "cgfd_common.h"
 #include "cgfd_stage.cuh"
-#include "cgfd_stage2.cuh"
+#include "cgfd_stage3.cuh"
 
 /* ------------------------------------------------------------------------ */
 /* errors                                                                    */
@@ -338,6 +338,9 @@ struct cgfd_solver {
   int graph_pre_lev;
   int *d_err;
   CUtensorMap tmap;             /* 5-D map over the four wavefield levels */
+  CUtensorMap tmap_met;         /* 4-D maps of the per-point streams */
+  CUtensorMap tmap_med;
+  CUtensorMap tmap_pt;
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
   int kchunk;
 };
@@ -494,6 +497,25 @@ static int make_tmap(cgfd_solver_t *s)
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  /* per-point tiles (no halo) for L2 prefetch of the streams */
+  cuuint32_t boxp[5] = {s2::TX, s2::TY, 1, 9, 1};
+  r = fn(&s->tmap_pt, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
+         boxp, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (points) failed (%d)", (int)r);
+  cuuint64_t dm[4] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 10};
+  cuuint64_t sm_[3] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4, (cuuint64_t)g.vol * 4};
+  cuuint32_t bm[4] = {s2::TX, s2::TY, 1, 10};
+  r = fn(&s->tmap_met, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->metric, dm, sm_, bm, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (metrics) failed (%d)", (int)r);
+  dm[3] = 3;
+  bm[3] = 3;
+  r = fn(&s->tmap_med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->media, dm, sm_, bm, estr,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (media) failed (%d)", (int)r);
   return 0;
 }
 
@@ -671,7 +693,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   if (const char *e = getenv("CGFD_STAGE_KERNEL")) s->kernel = atoi(e) == 1 ? 1 : 2;
   {
     int tiles = ((g.ni + s2::TX - 1) / s2::TX) * ((g.nj + s2::TY - 1) / s2::TY);
-    int want = 4 * 2 * 152;                 /* about four waves of CTAs */
+    int want = 8 * 152;                     /* about eight waves of CTAs */
     int nch = std::max(1, std::min(g.nk / 16, (want + tiles - 1) / tiles));
     s->kchunk = (g.nk + nch - 1) / nch;
     if (const char *e = getenv("CGFD_KCHUNK")) s->kchunk = std::max(4, atoi(e));
@@ -712,14 +734,15 @@ static void launch_one(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
   } else {
     static bool attr_set = false;
     if (!attr_set) {
-      cudaFuncSetAttribute(s2::k_stage2<BX, BY, BZ, KIND>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, s2::SMEM_BYTES);
+      cudaFuncSetAttribute(s3::k_stage3<BX, BY, BZ, KIND>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, s3::SMEM_BYTES);
       attr_set = true;
     }
-    dim3 b(s2::TX, s2::TY);
+    dim3 b(s3::NTHREADS);
     dim3 gr((s->g.ni + s2::TX - 1) / s2::TX, (s->g.nj + s2::TY - 1) / s2::TY,
             (s->g.nk + s->kchunk - 1) / s->kchunk);
-    s2::k_stage2<BX, BY, BZ, KIND><<<gr, b, s2::SMEM_BYTES, st>>>(a, s->tmap);
+    s3::k_stage3<BX, BY, BZ, KIND><<<gr, b, s3::SMEM_BYTES, st>>>(
+        a, s->tmap, s->tmap_met, s->tmap_med, s->tmap_pt);
   }
 }
 
@@ -793,6 +816,8 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   a.kchunk = s->kchunk;
   size_t L = level_floats(s->g);
   a.cur_level = (int)((cur - s->wav) / (long long)L);
+  a.pre_level = (int)((pre - s->wav) / (long long)L);
+  a.end_level = (int)((end - s->wav) / (long long)L);
 }
 
 /* enqueue one step (4 stages + receivers) for step index `it` */

@@ -1,0 +1,328 @@
+/*
+ * Stage kernel: warp-specialised, TMA-fed, z-marching (sm_103a).
+ *
+ * Work split.  A CTA owns a 32 x 8 column tile of the (i, j) plane and a run
+ * of `kchunk` k planes.  Warp 8 is the producer: its lane 0 issues every
+ * load of the CTA as bulk tensor copies (cp.async.bulk.tensor) into shared
+ * memory; warps 0-7 are consumers, one tile row each, and never touch global
+ * memory for the regular stencil path.
+ *
+ * Shared memory (167 KB, one CTA per SM):
+ *   wavefield ring  NB = 6 plane tiles (9 components with x/y halo, see
+ *                   cgfd_stage2.cuh) -- the 5 planes of the z operator's
+ *                   window plus one in flight;
+ *   stream ring     NS = 2 slots of the per-point streams of one plane:
+ *                   metrics (jac + 9), media (slw, lambda, mu) and, as the
+ *                   stage needs them, the `pre` and `end` levels.
+ *
+ * Synchronisation uses only mbarriers: `full` barriers complete when a
+ * copy's bytes land (expect_tx / complete_tx), `empty` barriers complete
+ * when all eight consumer warps have released a buffer.  With no CTA-wide
+ * barrier in the loop, consumer warps drift freely and the producer runs
+ * as far ahead as the rings allow.  Every wait is bounded: on timeout the
+ * waiting thread records device error 1 (a.err) and goes on, so the kernel
+ * always terminates and the host reports the failure.
+ *
+ * Per point the consumer computes exactly what cgfd_stage.cuh computes
+ * (reference: forward/sv_curv_col_el_iso.c:208-1146,
+ * forward/sv_curv_col_el.c:30-479, forward/drv_rk_curv_col.c:292-446).
+ */
+#ifndef CGFD_STAGE3_CUH
+#define CGFD_STAGE3_CUH
+
+#include "cgfd_stage2.cuh"
+
+namespace s3 {
+
+using namespace s2;
+
+constexpr int NB = 6;                 /* wavefield ring */
+constexpr int NS = 2;                 /* stream ring */
+constexpr int NCW = TY;               /* consumer warps (one per tile row) */
+constexpr int NTHREADS = (NCW + 1) * 32;
+constexpr int PTS = TX * TY;
+constexpr int S_MET = 0;              /* 10 components */
+constexpr int S_MED = 10 * PTS;       /* 3 */
+constexpr int S_PRE = 13 * PTS;       /* 9 */
+constexpr int S_END = 22 * PTS;       /* 9 */
+constexpr int SLOT = 31 * PTS;        /* floats per stream slot */
+constexpr int SMEM_BYTES = (NB * PLANE + NS * SLOT) * 4;
+
+/* bounded wait; `err` records a timeout */
+__device__ __forceinline__ void wait_full(uint64_t *bar, uint32_t parity, int *err)
+{
+  mbar_wait(bar, parity, err);
+}
+
+template <int BX, int BY, int BZ, int KIND>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_stage3(const __grid_constant__ StageArgs a,
+             const __grid_constant__ CUtensorMap tmap,
+             const __grid_constant__ CUtensorMap tmap_met,
+             const __grid_constant__ CUtensorMap tmap_med,
+             const __grid_constant__ CUtensorMap tmap_pt)
+{
+  extern __shared__ __align__(128) float sm[];
+  __shared__ __align__(8) uint64_t full_w[NB], empty_w[NB], full_s[NS], empty_s[NS];
+  float *ring = sm;
+  float *slots = sm + NB * PLANE;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const DevGrid &g = a.g;
+  const int i0 = g.ni1 + blockIdx.x * TX;
+  const int j0 = g.nj1 + blockIdx.y * TY;
+  const int kbeg = g.nk1 + blockIdx.z * a.kchunk;
+  const int kend = min(kbeg + a.kchunk - 1, g.nk2);
+  const int niter = kend - kbeg + 1;
+  constexpr int ZS0 = BZ == 0 ? -1 : -3;
+  constexpr int YL = BY == 0 ? 1 : 3;
+  constexpr int ZC = BZ == 0 ? 1 : 3;
+  const int pbase = kbeg + ZS0;       /* plane of ring index 0 */
+
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < NB; b++) { mbar_init(&full_w[b], 1); mbar_init(&empty_w[b], NCW); }
+    for (int b = 0; b < NS; b++) { mbar_init(&full_s[b], 1); mbar_init(&empty_s[b], NCW); }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  /* ------------------------------------------------------------------ */
+  /* producer                                                             */
+  /* ------------------------------------------------------------------ */
+  if (warp == NCW) {
+    if (lane != 0) return;
+    const int bx0 = i0 + g.xoff - XL;  /* 16-byte aligned box origin */
+    const int by0 = j0 - YL;
+    const int xs = i0 + g.xoff;        /* stream tiles: no halo */
+    constexpr uint32_t slot_bytes =
+        (13 + (KIND == 1 ? 9 : 0) + (KIND >= 1 ? 9 : 0)) * PTS * 4;
+    auto issue_wav = [&](int rel) {
+      int b = rel % NB;
+      if (rel >= NB) {
+        mbar_wait(&empty_w[b], ((rel / NB) - 1) & 1, a.err);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      }
+      mbar_expect_tx(&full_w[b], PLANE * 4);
+      tma_load_5d(ring + b * PLANE, &tmap, bx0, by0, pbase + rel, 0, a.cur_level,
+                  &full_w[b]);
+    };
+    auto issue_slot = [&](int it) {
+      int b = it % NS;
+      if (it >= NS) {
+        mbar_wait(&empty_s[b], ((it / NS) - 1) & 1, a.err);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      }
+      float *dst = slots + b * SLOT;
+      int k = kbeg + it;
+      mbar_expect_tx(&full_s[b], slot_bytes);
+      tma_load_4d(dst + S_MET, &tmap_met, xs, j0, k, 0, &full_s[b]);
+      tma_load_4d(dst + S_MED, &tmap_med, xs, j0, k, 0, &full_s[b]);
+      if (KIND == 1) tma_load_5d(dst + S_PRE, &tmap_pt, xs, j0, k, 0, a.pre_level, &full_s[b]);
+      if (KIND >= 1) tma_load_5d(dst + S_END, &tmap_pt, xs, j0, k, 0, a.end_level, &full_s[b]);
+    };
+    for (int rel = 0; rel < 5; rel++) issue_wav(rel);
+    for (int it = 0; it < niter; it++) {
+      issue_slot(it);
+      if (it + 5 < niter + 4) issue_wav(it + 5);
+    }
+    return;
+  }
+
+  /* ------------------------------------------------------------------ */
+  /* consumers                                                            */
+  /* ------------------------------------------------------------------ */
+  const int tx = lane, ty = warp;
+  const int i = i0 + tx, j = j0 + ty;
+  const bool valid = (i <= g.ni2) && (j <= g.nj2);
+  const int row = ty + YL, col = tx + XL;
+  const long long px = g.px, sl = g.sl, vol = g.vol;
+  const int sp = ty * TX + tx;        /* point index inside a stream slot */
+
+  /* per-thread constants of the k loop */
+  int pml_mask = 0;
+  for (int f = 0; f < CGFD_NFACE; f++) {
+    const DevFace &F = a.face[f];
+    if (F.on && i >= F.i1 && i <= F.i2 && j >= F.j1 && j <= F.j2) pml_mask |= 1 << f;
+  }
+  int src_e0 = 0, src_e1 = 0;
+  if (a.src_n > 0 && valid) {
+    long long colidx = (long long)(i - g.ni1) + (long long)(j - g.nj1) * g.ni;
+    src_e0 = a.src_col[colidx];
+    src_e1 = a.src_col[colidx + 1];
+  }
+
+  for (int it = 0; it < niter; it++) {
+    const int k = kbeg + it;
+    const int rtop = it + 4;
+#pragma unroll
+    for (int n = 0; n < 5; n++) {
+      int rel = rtop - 4 + n;
+      wait_full(&full_w[rel % NB], (rel / NB) & 1, a.err);
+    }
+    wait_full(&full_s[it % NS], (it / NS) & 1, a.err);
+    Win w;
+    {
+      int b = (rtop - 4) % NB;
+      w.p0 = ring + b * PLANE; b = b + 1 == NB ? 0 : b + 1;
+      w.p1 = ring + b * PLANE; b = b + 1 == NB ? 0 : b + 1;
+      w.p2 = ring + b * PLANE; b = b + 1 == NB ? 0 : b + 1;
+      w.p3 = ring + b * PLANE; b = b + 1 == NB ? 0 : b + 1;
+      w.p4 = ring + b * PLANE;
+    }
+    const float *cen = w.at(ZC);
+    const float *st = slots + (it % NS) * SLOT;
+
+    if (valid) {
+      const long long q = (long long)(i + g.xoff) + (long long)j * px +
+                          (long long)k * sl;
+      const float *ms = st + S_MET + sp;
+      float xix = ms[1 * PTS], xiy = ms[2 * PTS], xiz = ms[3 * PTS];
+      float etx = ms[4 * PTS], ety = ms[5 * PTS], etz = ms[6 * PTS];
+      float ztx = ms[7 * PTS], zty = ms[8 * PTS], ztz = ms[9 * PTS];
+      const float *md = st + S_MED + sp;
+      float slw = md[0], lam = md[PTS], mu = md[2 * PTS];
+      float l2m = lam + 2.0f * mu;
+      float r[9];
+#define DX(c) sdop<BX>(cen + soff(c, row, col), 1)
+#define DY(c) sdop<BY>(cen + soff(c, row, col), BW)
+#define DZ(c) zdop<BZ>(w, soff(c, row, col))
+      {
+        float DxTxx = DX(C_TXX), DyTxx = DY(C_TXX), DzTxx = DZ(C_TXX);
+        float DxTxy = DX(C_TXY), DyTxy = DY(C_TXY), DzTxy = DZ(C_TXY);
+        float DxTxz = DX(C_TXZ), DyTxz = DY(C_TXZ), DzTxz = DZ(C_TXZ);
+        r[C_VX] = slw * (xix * DxTxx + xiy * DxTxy + xiz * DxTxz +
+                         etx * DyTxx + ety * DyTxy + etz * DyTxz +
+                         ztx * DzTxx + zty * DzTxy + ztz * DzTxz);
+        float DxTyy = DX(C_TYY), DyTyy = DY(C_TYY), DzTyy = DZ(C_TYY);
+        float DxTyz = DX(C_TYZ), DyTyz = DY(C_TYZ), DzTyz = DZ(C_TYZ);
+        r[C_VY] = slw * (xix * DxTxy + xiy * DxTyy + xiz * DxTyz +
+                         etx * DyTxy + ety * DyTyy + etz * DyTyz +
+                         ztx * DzTxy + zty * DzTyy + ztz * DzTyz);
+        float DxTzz = DX(C_TZZ), DyTzz = DY(C_TZZ), DzTzz = DZ(C_TZZ);
+        r[C_VZ] = slw * (xix * DxTxz + xiy * DxTyz + xiz * DxTzz +
+                         etx * DyTxz + ety * DyTyz + etz * DyTzz +
+                         ztx * DzTxz + zty * DzTyz + ztz * DzTzz);
+      }
+      {
+        float DxVx = DX(C_VX), DyVx = DY(C_VX);
+        float DxVy = DX(C_VY), DyVy = DY(C_VY);
+        float DxVz = DX(C_VZ), DyVz = DY(C_VZ);
+        float DzVx, DzVy, DzVz;
+        const int nk2 = g.nk2;
+        if (a.free_top && k >= nk2 - 2) {
+          if (k == nk2) {
+            long long ij = ((long long)i + (long long)j * g.nx) * 9;
+            const float *A = a.mVx + ij, *Bm = a.mVy + ij;
+            DzVx = LDG(A + 0) * DxVx + LDG(A + 1) * DxVy + LDG(A + 2) * DxVz +
+                   LDG(Bm + 0) * DyVx + LDG(Bm + 1) * DyVy + LDG(Bm + 2) * DyVz;
+            DzVy = LDG(A + 3) * DxVx + LDG(A + 4) * DxVy + LDG(A + 5) * DxVz +
+                   LDG(Bm + 3) * DyVx + LDG(Bm + 4) * DyVy + LDG(Bm + 5) * DyVz;
+            DzVz = LDG(A + 6) * DxVx + LDG(A + 7) * DxVy + LDG(A + 8) * DxVz +
+                   LDG(Bm + 6) * DyVx + LDG(Bm + 7) * DyVy + LDG(Bm + 8) * DyVz;
+          } else if (k == nk2 - 1) {
+            const float *lo = BZ == 0 ? w.at(ZC) : w.at(ZC - 1);
+            const float *hi = BZ == 0 ? w.at(ZC + 1) : w.at(ZC);
+            int ox = soff(C_VX, row, col), oy = soff(C_VY, row, col),
+                oz = soff(C_VZ, row, col);
+            DzVx = -lo[ox] + hi[ox];
+            DzVy = -lo[oy] + hi[oy];
+            DzVz = -lo[oz] + hi[oz];
+          } else {
+            const float c0 = BZ == 0 ? (float)(-7.0 / 6.0) : (float)(1.0 / 6.0);
+            const float c1 = BZ == 0 ? (float)(8.0 / 6.0) : (float)(-8.0 / 6.0);
+            const float c2 = BZ == 0 ? (float)(-1.0 / 6.0) : (float)(7.0 / 6.0);
+            const float *p0 = BZ == 0 ? w.at(ZC) : w.at(ZC - 2);
+            const float *p1 = BZ == 0 ? w.at(ZC + 1) : w.at(ZC - 1);
+            const float *p2 = BZ == 0 ? w.at(ZC + 2) : w.at(ZC);
+            int ox = soff(C_VX, row, col), oy = soff(C_VY, row, col),
+                oz = soff(C_VZ, row, col);
+            DzVx = c0 * p0[ox] + c1 * p1[ox] + c2 * p2[ox];
+            DzVy = c0 * p0[oy] + c1 * p1[oy] + c2 * p2[oy];
+            DzVz = c0 * p0[oz] + c1 * p1[oz] + c2 * p2[oz];
+          }
+        } else {
+          DzVx = DZ(C_VX);
+          DzVy = DZ(C_VY);
+          DzVz = DZ(C_VZ);
+        }
+        hooke_iso(lam, mu, l2m, xix, xiy, xiz, etx, ety, etz, ztx, zty, ztz,
+                  DxVx, DxVy, DxVz, DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, r);
+      }
+#undef DX
+#undef DY
+#undef DZ
+      if (a.free_top && k >= g.nk2 - (BZ == 0 ? 3 : 1)) {
+        r[C_VX] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 0);
+        r[C_VY] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 1);
+        r[C_VZ] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 2);
+      }
+
+      if (pml_mask) {
+#pragma unroll 1
+        for (int f = 0; f < CGFD_NFACE; f++) {
+          const DevFace &F = a.face[f];
+          if (!((pml_mask >> f) & 1) || k < F.k1 || k > F.k2) continue;
+          Deriv9 d;
+          sderiv9<BX, BY, BZ>(cen, w, row, col, F.dim, d);
+          if (F.dim == 0)
+            pml_face<KIND>(a, f, i, j, k, q, d, xix, xiy, xiz, lam, mu, l2m, slw, r);
+          else if (F.dim == 1)
+            pml_face<KIND>(a, f, i, j, k, q, d, etx, ety, etz, lam, mu, l2m, slw, r);
+          else
+            pml_face<KIND>(a, f, i, j, k, q, d, ztx, zty, ztz, lam, mu, l2m, slw, r);
+        }
+      }
+
+      if (src_e0 < src_e1) {
+        int itg = *a.d_it;
+        for (int e = src_e0; e < src_e1; e++) {
+          SrcEntry s = a.src_ent[e];
+          if (s.k != k) continue;
+          if (itg < a.src_it_begin[s.is] || itg > a.src_it_end[s.is]) continue;
+          long long t = ((long long)s.is * a.src_max_nt +
+                         (itg - a.src_it_begin[s.is])) * a.src_max_stage + a.istage;
+          if (a.src_force && s.force_on) {
+            r[C_VX] += a.Fx[t] * s.vf;
+            r[C_VY] += a.Fy[t] * s.vf;
+            r[C_VZ] += a.Fz[t] * s.vf;
+          }
+          if (a.src_moment) {
+            r[C_TXX] -= a.Mxx[t] * s.rjac;
+            r[C_TYY] -= a.Myy[t] * s.rjac;
+            r[C_TZZ] -= a.Mzz[t] * s.rjac;
+            r[C_TXZ] -= a.Mxz[t] * s.rjac;
+            r[C_TYZ] -= a.Myz[t] * s.rjac;
+            r[C_TXY] -= a.Mxy[t] * s.rjac;
+          }
+        }
+      }
+
+      /* RK combine */
+#pragma unroll
+      for (int c = 0; c < 9; c++) {
+        long long x = c * vol + q;
+        if (KIND == 0) {
+          float p = cen[soff(c, row, col)];
+          a.tmp_out[x] = p + a.ca * r[c];
+          a.end[x] = p + a.cb * r[c];
+        } else if (KIND == 1) {
+          a.tmp_out[x] = st[S_PRE + c * PTS + sp] + a.ca * r[c];
+          a.end[x] = st[S_END + c * PTS + sp] + a.cb * r[c];
+        } else {
+          a.end[x] = st[S_END + c * PTS + sp] + a.cb * r[c];
+        }
+      }
+    }
+
+    /* release the oldest window plane and this plane's stream slot */
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(&empty_w[(rtop - 4) % NB]);
+      mbar_arrive(&empty_s[it % NS]);
+    }
+  }
+}
+
+}  // namespace s3
+
+#endif
