@@ -26,6 +26,7 @@
 #include "cgfd_common.h"
 #include "cgfd_stage.cuh"
 #include "cgfd_stage3.cuh"
+#include "cgfd_pml.cuh"
 
 /* ------------------------------------------------------------------------ */
 /* errors                                                                    */
@@ -331,7 +332,8 @@ struct cgfd_solver {
   size_t h2d_bytes, d2h_bytes;
   cudaEvent_t ev0, ev1;
   std::vector<cudaEvent_t> kev;   /* per-launch timing events */
-  float t_stage_ms, t_other_ms, t_total_ms;
+  float t_stage_ms, t_other_ms, t_total_ms, t_pml_ms;
+  int n_pml;
   int n_stage, n_other;
   int timing;
   cudaGraphExec_t graph8;
@@ -746,6 +748,29 @@ static void launch_one(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
   }
 }
 
+template <int DIM, int B>
+static void launch_pml(int kind, int f, long long n, cudaStream_t st, const StageArgs &a)
+{
+  dim3 b(256), gr((unsigned)((n + 255) / 256));
+  if (kind == 0) k_pml_face<DIM, B, 0><<<gr, b, 0, st>>>(a, f);
+  else if (kind == 1) k_pml_face<DIM, B, 1><<<gr, b, 0, st>>>(a, f);
+  else k_pml_face<DIM, B, 2><<<gr, b, 0, st>>>(a, f);
+}
+
+/* CFS-PML corrections, faces in the reference order (after the stage kernel) */
+static void launch_pml_faces(cgfd_solver_t *s, int kind, int bx, int by, int bz,
+                             cudaStream_t st, const StageArgs &a)
+{
+  for (int f = 0; f < CGFD_NFACE; f++) {
+    const DevFace &F = s->face[f];
+    if (!F.on) continue;
+    int dim = F.dim, b = dim == 0 ? bx : (dim == 1 ? by : bz);
+    if (dim == 0) { if (b) launch_pml<0, 1>(kind, f, F.avol, st, a); else launch_pml<0, 0>(kind, f, F.avol, st, a); }
+    else if (dim == 1) { if (b) launch_pml<1, 1>(kind, f, F.avol, st, a); else launch_pml<1, 0>(kind, f, F.avol, st, a); }
+    else { if (b) launch_pml<2, 1>(kind, f, F.avol, st, a); else launch_pml<2, 0>(kind, f, F.avol, st, a); }
+  }
+}
+
 template <int BX, int BY, int BZ>
 static void launch_stage(cgfd_solver_t *s, int kind, cudaStream_t st, const StageArgs &a)
 {
@@ -846,6 +871,8 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
       default: launch_stage<1, 1, 1>(s, kind, st, a); break;
     }
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
+    if (s->kernel == 2) launch_pml_faces(s, kind, bx, by, bz, st, a);
+    if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
   size_t L = level_floats(s->g);
   k_recv<<<1, 256, 0, st>>>(s->wav + s->end_lev * L, s->g.vol, p->ncmp,
@@ -863,7 +890,7 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   if (nsteps < 0 || s->step + nsteps > s->p->nt_total)
     return set_err(CGFD_EINVAL, "run(%d) past nt_total=%d (at step %d)", nsteps,
                    s->p->nt_total, s->step);
-  int nev = s->timing ? 8 * nsteps : 0;
+  int nev = s->timing ? 12 * nsteps : 0;
   while ((int)s->kev.size() < nev) {
     cudaEvent_t e;
     CK(cudaEventCreate(&e));
@@ -882,15 +909,21 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   CK(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
   s->t_total_ms = ms;
   s->t_stage_ms = 0.f;
+  s->t_pml_ms = 0.f;
   if (s->timing) {
-    for (int e = 0; e < ev; e += 2) {
-      float t = 0.f;
+    for (int e = 0; e < ev; e += 3) {
+      float t = 0.f, t2 = 0.f;
       CK(cudaEventElapsedTime(&t, s->kev[e], s->kev[e + 1]));
+      CK(cudaEventElapsedTime(&t2, s->kev[e + 1], s->kev[e + 2]));
       s->t_stage_ms += t;
+      s->t_pml_ms += t2;
     }
   }
+  int nfaces = 0;
+  for (int f = 0; f < CGFD_NFACE; f++) nfaces += s->face[f].on;
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
+  s->n_pml = s->kernel == 2 ? 4 * nfaces * nsteps : 0;
   s->n_other = nsteps;
   int herr = 0;
   CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));
@@ -903,8 +936,9 @@ extern "C" int cgfd_solver_step(const cgfd_solver_t *s) { return s ? s->step : -
 extern "C" int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3])
 {
   if (!s) return set_err(CGFD_EINVAL, "null solver");
-  out[0] = s->t_stage_ms; out[1] = s->t_total_ms; out[2] = s->t_other_ms;
-  count[0] = s->n_stage; count[1] = s->n_stage + s->n_other; count[2] = s->n_other;
+  out[0] = s->t_stage_ms; out[1] = s->t_total_ms; out[2] = s->t_pml_ms;
+  count[0] = s->n_stage; count[1] = s->n_stage + s->n_pml + s->n_other;
+  count[2] = s->n_pml;
   return 0;
 }
 

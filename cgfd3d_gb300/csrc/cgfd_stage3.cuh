@@ -23,8 +23,9 @@
  * waiting thread records device error 1 (a.err) and goes on, so the kernel
  * always terminates and the host reports the failure.
  *
- * Per point the consumer computes exactly what cgfd_stage.cuh computes
- * (reference: forward/sv_curv_col_el_iso.c:208-1146,
+ * Per point the consumer computes what cgfd_stage.cuh computes except the
+ * CFS-PML terms, which the face kernels of cgfd_pml.cuh add afterwards
+ * (reference: forward/sv_curv_col_el_iso.c:208-634,
  * forward/sv_curv_col_el.c:30-479, forward/drv_rk_curv_col.c:292-446).
  */
 #ifndef CGFD_STAGE3_CUH
@@ -139,11 +140,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int sp = ty * TX + tx;        /* point index inside a stream slot */
 
   /* per-thread constants of the k loop */
-  int pml_mask = 0;
-  for (int f = 0; f < CGFD_NFACE; f++) {
-    const DevFace &F = a.face[f];
-    if (F.on && i >= F.i1 && i <= F.i2 && j >= F.j1 && j <= F.j2) pml_mask |= 1 << f;
-  }
   int src_e0 = 0, src_e1 = 0;
   if (a.src_n > 0 && valid) {
     long long colidx = (long long)(i - g.ni1) + (long long)(j - g.nj1) * g.ni;
@@ -255,22 +251,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         r[C_VX] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 0);
         r[C_VY] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 1);
         r[C_VZ] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 2);
-      }
-
-      if (pml_mask) {
-#pragma unroll 1
-        for (int f = 0; f < CGFD_NFACE; f++) {
-          const DevFace &F = a.face[f];
-          if (!((pml_mask >> f) & 1) || k < F.k1 || k > F.k2) continue;
-          Deriv9 d;
-          sderiv9<BX, BY, BZ>(cen, w, row, col, F.dim, d);
-          if (F.dim == 0)
-            pml_face<KIND>(a, f, i, j, k, q, d, xix, xiy, xiz, lam, mu, l2m, slw, r);
-          else if (F.dim == 1)
-            pml_face<KIND>(a, f, i, j, k, q, d, etx, ety, etz, lam, mu, l2m, slw, r);
-          else
-            pml_face<KIND>(a, f, i, j, k, q, d, ztx, zty, ztz, lam, mu, l2m, slw, r);
-        }
       }
 
       if (src_e0 < src_e1) {

@@ -150,9 +150,9 @@ int cgfd_solver_step(const cgfd_solver_t *s);
 int cgfd_solver_check_finite(cgfd_solver_t *s);
 
 /* CUDA-event times of the last cgfd_solver_run, milliseconds:
- * out[0] = sum over the stage-kernel launches (only with timing on),
- * out[1] = the whole run, out[2] = the rest (receivers, bookkeeping);
- * count[0] stage launches, count[1] all launches, count[2] the rest. */
+ * out[0] = sum over the interior stage-kernel launches (timing on only),
+ * out[1] = the whole run, out[2] = sum over the CFS-PML face launches;
+ * count[0] stage launches, count[1] all launches, count[2] face launches. */
 int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3]);
 
 /* Record a CUDA event pair around every stage launch of later runs. */
