@@ -58,13 +58,6 @@ struct SrcEntry {
   int pad;
 };
 
-/* disjoint boxes whose union is the set of points inside some PML face */
-struct DevBox {
-  int i1, i2, j1, j2, k1, k2;
-  long long n;      /* points */
-  long long start;  /* prefix sum over the boxes */
-};
-
 struct StageArgs {
   DevGrid g;
   /* metrics and media */
@@ -97,9 +90,6 @@ struct StageArgs {
   int cur_level;               /* level index of `cur` (TMA coordinate) */
   int pre_level, end_level;    /* level indices of `pre` and `end` */
   int kchunk;                  /* planes per CTA along k */
-  int nreg;                    /* PML region boxes */
-  DevBox reg[6];
-  int skip_pml;                /* interior kernel leaves PML points alone */
 };
 
 #endif

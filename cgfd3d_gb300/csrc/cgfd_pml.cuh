@@ -1,19 +1,24 @@
 /*
- * CFS-PML region kernel.
+ * CFS-PML face kernel (ADE, unsplit), one launch per enabled face per stage.
  *
- * The points inside the CFS-PML faces (about a fifth of a 400 x 400 x 200
- * model with 12-layer faces) take their whole stage update here: interior
- * RHS, free-surface overwrites, the PML corrections of every face containing
- * the point in the reference order x1, x2, y1, y2, z1, z2, sources and the
- * RK combine -- the per-point function of cgfd_stage.cuh, i.e. exactly the
- * reference's sequence (forward/sv_curv_col_el_iso.c:22-1146,
- * forward/drv_rk_curv_col.c:292-446).  The TMA interior kernel skips these
- * points, so both kernels write disjoint points and run concurrently on two
- * streams.
+ * The interior stage kernel (cgfd_stage3.cuh) writes tmp = pre + a*dt*r and
+ * end (+)= b*dt*r with r the RHS without PML terms.  The PML terms of the
+ * reference (forward/sv_curv_col_el_iso.c:708-1143) are linear additions to
+ * r, so this kernel adds them afterwards:
  *
- * The union of the face boxes is split on the host into disjoint boxes
- * (x faces; y faces without the x columns; z faces without both), one
- * thread per point, i fastest.
+ *   corr = (B-1) * r_d - B * aux_cur        (+ the free-surface term of
+ *                                             x/y faces at k = nk2)
+ *   aux_rhs = D * r_d - A * aux_cur
+ *   tmp += a*dt*corr ;  end += b*dt*corr ;  aux levels advanced by RK4
+ *
+ * where r_d is the part of the RHS made of derivatives along the face normal.
+ * Faces are launched in the reference order x1, x2, y1, y2, z1, z2, so a
+ * corner point receives its corrections in the same order.  Rounding differs
+ * from the reference only by the association (pre + a r) + a corr versus
+ * pre + a (r + corr).
+ *
+ * One thread per point of the face box, linear index with i fastest, plain
+ * coalesced loads (the face boxes are thin; their operands are read once).
  */
 #ifndef CGFD_PML_CUH
 #define CGFD_PML_CUH
@@ -21,21 +26,100 @@
 #include "cgfd_common.h"
 #include "cgfd_stage.cuh"
 
-template <int BX, int BY, int BZ, int KIND>
-__global__ void __launch_bounds__(128)
-    k_pml_region(const __grid_constant__ StageArgs a, long long total)
+template <int DIM, int B, int KIND>
+__global__ void __launch_bounds__(256)
+    k_pml_face(const __grid_constant__ StageArgs a, int f)
 {
-  long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (n >= total) return;
-  int r = 0;
-  while (r + 1 < a.nreg && n >= a.reg[r + 1].start) r++;
-  const DevBox &B = a.reg[r];
-  long long m = n - B.start;
-  int bx = B.i2 - B.i1 + 1, by = B.j2 - B.j1 + 1;
-  int i = B.i1 + (int)(m % bx);
-  int j = B.j1 + (int)((m / bx) % by);
-  int k = B.k1 + (int)(m / ((long long)bx * by));
-  stage_point<BX, BY, BZ, KIND>(a, i, j, k);
+  const DevFace &F = a.face[f];
+  const long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (n >= F.avol) return;
+  const int bxy = F.bx * F.by;
+  const int ii = (int)(n % F.bx);
+  const int jj = (int)((n / F.bx) % F.by);
+  const int kk = (int)(n / bxy);
+  const int i = F.i1 + ii, j = F.j1 + jj, k = F.k1 + kk;
+  const DevGrid &g = a.g;
+  const long long vol = g.vol;
+  const long long q = (long long)(i + g.xoff) + (long long)j * g.px + (long long)k * g.sl;
+  const long long s = DIM == 0 ? 1 : (DIM == 1 ? (long long)g.px : g.sl);
+
+  const float *e1p = DIM == 0 ? a.xix : (DIM == 1 ? a.etx : a.ztx);
+  const float *e2p = DIM == 0 ? a.xiy : (DIM == 1 ? a.ety : a.zty);
+  const float *e3p = DIM == 0 ? a.xiz : (DIM == 1 ? a.etz : a.ztz);
+  float e1 = LDG(e1p + q), e2 = LDG(e2p + q), e3 = LDG(e3p + q);
+  float lam = LDG(a.lam + q), mu = LDG(a.mu + q), slw = LDG(a.slw + q);
+  float l2m = lam + 2.0f * mu;
+
+  Deriv9 d;
+  deriv9<B>(a.cur, q, vol, s, d);
+
+  const int nidx = DIM == 0 ? ii : (DIM == 1 ? jj : kk);
+  float cD = LDG(F.D + nidx), cA = LDG(F.A + nidx), cB = LDG(F.B + nidx);
+  float cB1 = cB - 1.0f;
+  float sv[9];
+  sv[C_VX] = slw * (e1 * d.Txx + e2 * d.Txy + e3 * d.Txz);
+  sv[C_VY] = slw * (e1 * d.Txy + e2 * d.Tyy + e3 * d.Tyz);
+  sv[C_VZ] = slw * (e1 * d.Txz + e2 * d.Tyz + e3 * d.Tzz);
+  sv[C_TXX] = l2m * e1 * d.Vx + lam * e2 * d.Vy + lam * e3 * d.Vz;
+  sv[C_TYY] = lam * e1 * d.Vx + l2m * e2 * d.Vy + lam * e3 * d.Vz;
+  sv[C_TZZ] = lam * e1 * d.Vx + lam * e2 * d.Vy + l2m * e3 * d.Vz;
+  sv[C_TXY] = mu * (e2 * d.Vx + e1 * d.Vy);
+  sv[C_TXZ] = mu * (e3 * d.Vx + e1 * d.Vz);
+  sv[C_TYZ] = mu * (e3 * d.Vy + e2 * d.Vz);
+
+  const long long av = F.avol;
+  const float *acur = a.acur[f];
+  float corr[9], arhs[9];
+#pragma unroll
+  for (int c = 0; c < 9; c++) {
+    float ac = LDG(acur + c * av + n);
+    corr[c] = cB1 * sv[c] - cB * ac;
+    arhs[c] = cD * sv[c] - cA * ac;
+  }
+  if (DIM < 2 && a.free_top && k == g.nk2) {
+    long long ij = ((long long)i + (long long)j * g.nx) * 9;
+    const float *M = (DIM == 0 ? a.mVx : a.mVy) + ij;
+    float DzVx = LDG(M + 0) * d.Vx + LDG(M + 1) * d.Vy + LDG(M + 2) * d.Vz;
+    float DzVy = LDG(M + 3) * d.Vx + LDG(M + 4) * d.Vy + LDG(M + 5) * d.Vz;
+    float DzVz = LDG(M + 6) * d.Vx + LDG(M + 7) * d.Vy + LDG(M + 8) * d.Vz;
+    float ztx = LDG(a.ztx + q), zty = LDG(a.zty + q), ztz = LDG(a.ztz + q);
+    float t[9];
+    t[C_TXX] = l2m * (ztx * DzVx) + lam * (zty * DzVy + ztz * DzVz);
+    t[C_TYY] = l2m * (zty * DzVy) + lam * (ztx * DzVx + ztz * DzVz);
+    t[C_TZZ] = l2m * (ztz * DzVz) + lam * (ztx * DzVx + zty * DzVy);
+    t[C_TXY] = mu * (zty * DzVx + ztx * DzVy);
+    t[C_TXZ] = mu * (ztz * DzVx + ztx * DzVz);
+    t[C_TYZ] = mu * (ztz * DzVy + zty * DzVz);
+#pragma unroll
+    for (int c = C_TXX; c <= C_TXY; c++) {
+      corr[c] += cB1 * t[c];
+      arhs[c] += cD * t[c];
+    }
+  }
+
+  /* auxiliary RK combine and the corrections of tmp / end */
+  const float *apre = a.apre[f];
+  float *aend = a.aend[f];
+#pragma unroll
+  for (int c = 0; c < 9; c++) {
+    long long xa = c * av + n;
+    long long x = c * vol + q;
+    if (KIND == 0) {
+      float p = LDG(apre + xa);
+      a.atmp_out[f][xa] = p + a.ca * arhs[c];
+      aend[xa] = p + a.cb * arhs[c];
+      a.tmp_out[x] += a.ca * corr[c];
+      a.end[x] += a.cb * corr[c];
+    } else if (KIND == 1) {
+      a.atmp_out[f][xa] = LDG(apre + xa) + a.ca * arhs[c];
+      aend[xa] = aend[xa] + a.cb * arhs[c];
+      a.tmp_out[x] += a.ca * corr[c];
+      a.end[x] += a.cb * corr[c];
+    } else {
+      aend[xa] = aend[xa] + a.cb * arhs[c];
+      a.end[x] += a.cb * corr[c];
+    }
+  }
 }
 
 #endif

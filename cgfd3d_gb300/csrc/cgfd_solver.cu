@@ -336,11 +336,6 @@ struct cgfd_solver {
   int n_pml;
   int n_stage, n_other;
   int timing;
-  cudaStream_t stream2;         /* PML region kernel */
-  cudaEvent_t ev_fork, ev_join;
-  long long pml_total;          /* points in the PML region boxes */
-  DevBox reg[6];
-  int nreg;
   cudaGraphExec_t graph8;
   int graph_pre_lev;
   int *d_err;
@@ -443,7 +438,6 @@ static long long dev_index(const DevGrid &g, long long h)
 
 static cudaError_t upload_volume(cgfd_solver_t *s, float *dst, const float *src);
 static int make_tmap(cgfd_solver_t *s);
-static void build_pml_regions(cgfd_solver_t *s);
 
 template <typename T>
 static int dalloc(cgfd_solver_t *s, T **ptr, size_t n)
@@ -527,35 +521,6 @@ static int make_tmap(cgfd_solver_t *s)
   return 0;
 }
 
-/* Disjoint boxes covering the union of the PML face boxes: the x faces,
- * the y faces without the x-face columns, the z faces without both. */
-static void build_pml_regions(cgfd_solver_t *s)
-{
-  const DevGrid &g = s->g;
-  s->nreg = 0;
-  s->pml_total = 0;
-  int xlo = g.ni1, xhi = g.ni2, ylo = g.nj1, yhi = g.nj2;
-  const DevFace *F = s->face;
-  if (F[0].on) xlo = F[0].i2 + 1;
-  if (F[1].on) xhi = F[1].i1 - 1;
-  if (F[2].on) ylo = F[2].j2 + 1;
-  if (F[3].on) yhi = F[3].j1 - 1;
-  auto add = [&](int i1, int i2, int j1, int j2, int k1, int k2) {
-    if (i1 > i2 || j1 > j2 || k1 > k2) return;
-    DevBox &b = s->reg[s->nreg++];
-    b.i1 = i1; b.i2 = i2; b.j1 = j1; b.j2 = j2; b.k1 = k1; b.k2 = k2;
-    b.n = (long long)(i2 - i1 + 1) * (j2 - j1 + 1) * (k2 - k1 + 1);
-    b.start = s->pml_total;
-    s->pml_total += b.n;
-  };
-  for (int f = 0; f < 2; f++)
-    if (F[f].on) add(F[f].i1, F[f].i2, F[f].j1, F[f].j2, F[f].k1, F[f].k2);
-  for (int f = 2; f < 4; f++)
-    if (F[f].on) add(xlo, xhi, F[f].j1, F[f].j2, F[f].k1, F[f].k2);
-  for (int f = 4; f < 6; f++)
-    if (F[f].on) add(xlo, xhi, ylo, yhi, F[f].k1, F[f].k2);
-}
-
 extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
 {
   if (!s) return;
@@ -572,9 +537,6 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
     if (s->face[f].A) cudaFree((void *)s->face[f].A);
   }
   for (cudaEvent_t e : s->kev) cudaEventDestroy(e);
-  if (s->ev_fork) cudaEventDestroy(s->ev_fork);
-  if (s->ev_join) cudaEventDestroy(s->ev_join);
-  if (s->stream2) cudaStreamDestroy(s->stream2);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -601,9 +563,6 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
 #define TRYC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { set_err(CGFD_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); cgfd_solver_destroy(s); return CGFD_ECUDA; } } while (0)
   TRYC(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   TRYC(cudaEventCreate(&s->ev0));
-  TRYC(cudaStreamCreateWithFlags(&s->stream2, cudaStreamNonBlocking));
-  TRYC(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
-  TRYC(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
   TRYC(cudaEventCreate(&s->ev1));
   size_t vol = g.vol, L = level_floats(g);
   size_t hvol = (size_t)p->nx * p->ny * p->nz;
@@ -742,7 +701,6 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     if (const char *e = getenv("CGFD_KCHUNK")) s->kchunk = std::max(4, atoi(e));
   }
   TRY(make_tmap(s));
-  build_pml_regions(s);
   TRYC(cudaStreamSynchronize(st));
   *out = s;
   return 0;
@@ -768,23 +726,8 @@ static void stage_levels(cgfd_solver_t *s, int istage, float **cur, float **pre,
 typedef void (*stage_fn)(const StageArgs);
 
 template <int BX, int BY, int BZ, int KIND>
-static void launch_pml_region(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
-{
-  if (s->pml_total == 0) return;
-  dim3 b(128), gr((unsigned)((s->pml_total + 127) / 128));
-  k_pml_region<BX, BY, BZ, KIND><<<gr, b, 0, st>>>(a, s->pml_total);
-}
-
-template <int BX, int BY, int BZ, int KIND>
 static void launch_one(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
 {
-  if (s->kernel == 2 && s->pml_total > 0) {
-    /* PML points on the side stream, concurrently with the interior */
-    cudaEventRecord(s->ev_fork, st);
-    cudaStreamWaitEvent(s->stream2, s->ev_fork, 0);
-    launch_pml_region<BX, BY, BZ, KIND>(s, s->stream2, a);
-    cudaEventRecord(s->ev_join, s->stream2);
-  }
   if (s->kernel == 1) {
     dim3 b(V1_TX, V1_TY);
     dim3 gr((s->g.ni + V1_TX - 1) / V1_TX, (s->g.nj + V1_TY - 1) / V1_TY,
@@ -802,7 +745,29 @@ static void launch_one(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
             (s->g.nk + s->kchunk - 1) / s->kchunk);
     s3::k_stage3<BX, BY, BZ, KIND><<<gr, b, s3::SMEM_BYTES, st>>>(
         a, s->tmap, s->tmap_met, s->tmap_med, s->tmap_pt);
-    if (s->pml_total > 0) cudaStreamWaitEvent(st, s->ev_join, 0);
+  }
+}
+
+template <int DIM, int B>
+static void launch_pml(int kind, int f, long long n, cudaStream_t st, const StageArgs &a)
+{
+  dim3 b(256), gr((unsigned)((n + 255) / 256));
+  if (kind == 0) k_pml_face<DIM, B, 0><<<gr, b, 0, st>>>(a, f);
+  else if (kind == 1) k_pml_face<DIM, B, 1><<<gr, b, 0, st>>>(a, f);
+  else k_pml_face<DIM, B, 2><<<gr, b, 0, st>>>(a, f);
+}
+
+/* CFS-PML corrections, faces in the reference order (after the stage kernel) */
+static void launch_pml_faces(cgfd_solver_t *s, int kind, int bx, int by, int bz,
+                             cudaStream_t st, const StageArgs &a)
+{
+  for (int f = 0; f < CGFD_NFACE; f++) {
+    const DevFace &F = s->face[f];
+    if (!F.on) continue;
+    int dim = F.dim, b = dim == 0 ? bx : (dim == 1 ? by : bz);
+    if (dim == 0) { if (b) launch_pml<0, 1>(kind, f, F.avol, st, a); else launch_pml<0, 0>(kind, f, F.avol, st, a); }
+    else if (dim == 1) { if (b) launch_pml<1, 1>(kind, f, F.avol, st, a); else launch_pml<1, 0>(kind, f, F.avol, st, a); }
+    else { if (b) launch_pml<2, 1>(kind, f, F.avol, st, a); else launch_pml<2, 0>(kind, f, F.avol, st, a); }
   }
 }
 
@@ -876,9 +841,6 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   a.kchunk = s->kchunk;
   size_t L = level_floats(s->g);
   a.cur_level = (int)((cur - s->wav) / (long long)L);
-  a.nreg = s->nreg;
-  for (int r = 0; r < s->nreg; r++) a.reg[r] = s->reg[r];
-  a.skip_pml = (s->kernel == 2 && s->pml_total > 0) ? 1 : 0;
   a.pre_level = (int)((pre - s->wav) / (long long)L);
   a.end_level = (int)((end - s->wav) / (long long)L);
 }
@@ -909,6 +871,7 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
       default: launch_stage<1, 1, 1>(s, kind, st, a); break;
     }
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
+    if (s->kernel == 2) launch_pml_faces(s, kind, bx, by, bz, st, a);
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
   size_t L = level_floats(s->g);
@@ -960,8 +923,7 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   for (int f = 0; f < CGFD_NFACE; f++) nfaces += s->face[f].on;
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
-  s->n_pml = (s->kernel == 2 && s->pml_total > 0) ? 4 * nsteps : 0;
-  (void)nfaces;
+  s->n_pml = s->kernel == 2 ? 4 * nfaces * nsteps : 0;
   s->n_other = nsteps;
   int herr = 0;
   CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));

@@ -23,10 +23,10 @@
  * waiting thread records device error 1 (a.err) and goes on, so the kernel
  * always terminates and the host reports the failure.
  *
- * Per point the consumer computes what cgfd_stage.cuh computes (reference:
- * forward/sv_curv_col_el_iso.c:208-634, forward/sv_curv_col_el.c:30-479,
- * forward/drv_rk_curv_col.c:292-446) for every point outside the CFS-PML
- * faces; the points inside them are updated by cgfd_pml.cuh, concurrently.
+ * Per point the consumer computes what cgfd_stage.cuh computes except the
+ * CFS-PML terms, which the face kernels of cgfd_pml.cuh add afterwards
+ * (reference: forward/sv_curv_col_el_iso.c:208-634,
+ * forward/sv_curv_col_el.c:30-479, forward/drv_rk_curv_col.c:292-446).
  */
 #ifndef CGFD_STAGE3_CUH
 #define CGFD_STAGE3_CUH
@@ -139,14 +139,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const long long px = g.px, sl = g.sl, vol = g.vol;
   const int sp = ty * TX + tx;        /* point index inside a stream slot */
 
-  /* per-thread constants of the k loop: PML faces this column crosses
-     (those points belong to the PML region kernel) */
-  int pml_mask = 0;
-  if (a.skip_pml)
-    for (int f = 0; f < CGFD_NFACE; f++) {
-      const DevFace &F = a.face[f];
-      if (F.on && i >= F.i1 && i <= F.i2 && j >= F.j1 && j <= F.j2) pml_mask |= 1 << f;
-    }
+  /* per-thread constants of the k loop */
   int src_e0 = 0, src_e1 = 0;
   if (a.src_n > 0 && valid) {
     long long colidx = (long long)(i - g.ni1) + (long long)(j - g.nj1) * g.ni;
@@ -174,13 +167,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     const float *cen = w.at(ZC);
     const float *st = slots + (it % NS) * SLOT;
-    bool in_pml = false;
-    if (pml_mask)
-#pragma unroll
-      for (int f = 0; f < CGFD_NFACE; f++)
-        if (((pml_mask >> f) & 1) && k >= a.face[f].k1 && k <= a.face[f].k2) in_pml = true;
 
-    if (valid && !in_pml) {
+    if (valid) {
       const long long q = (long long)(i + g.xoff) + (long long)j * px +
                           (long long)k * sl;
       const float *ms = st + S_MET + sp;
