@@ -305,7 +305,9 @@ def run_ours(args):
                      "peak_kind": peak_kind,
                      "traffic": None if tpp is None else tpp * n_phys,
                      "alg_bytes_per_launch": alg_bytes,
-                     "avg_launch_ms": avg_launch * 1e3},
+                     "avg_launch_ms": avg_launch * 1e3,
+                     "kernel": "k_stage3 (interior stage)",
+                     "whole_step_frac": value / world * BYTES_PER_PT_STAGE / 1e9 / peak},
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": h2d / q.nt_total,
                 "d2h_bytes_per_step": d2h / q.nt_total,
