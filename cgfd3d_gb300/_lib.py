@@ -46,6 +46,8 @@ def lib():
     L.cgfd_allstep.argtypes = [vp]
     L.cgfd_device_bytes.argtypes = [vp]
     L.cgfd_device_bytes.restype = C.c_size_t
+    L.cgfd_check_finite_noalloc.argtypes = [C.c_void_p, C.c_size_t, C.POINTER(C.c_int)]
+    L.cgfd_check_finite_noalloc.restype = C.c_int
     if L.cgfd_abi_version() != abi.CGFD_ABI_VERSION:
         raise ImportError("libcgfd3d_gpu ABI version mismatch")
     _lib = L

@@ -54,6 +54,12 @@ static int set_err(int code, const char *fmt, ...)
   } while (0)
 
 extern "C" const char *cgfd_last_error(void) { return g_err.c_str(); }
+
+__attribute__((visibility("hidden"))) int cgfd_set_error_msg(int code, const char *msg)
+{
+  g_err = msg;
+  return code;
+}
 extern "C" int cgfd_abi_version(void) { return CGFD_ABI_VERSION; }
 
 /* ------------------------------------------------------------------------ */

@@ -170,6 +170,23 @@ int cgfd_allstep(const cgfd_problem_t *p);
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);
 
+/* No counterpart in the reference.  NaN/Inf test of a device array the
+ * caller owns that allocates no device memory, for callers that cannot call
+ * cudaMalloc (a process whose device memory belongs to another framework's
+ * pool or sits under a hard cap, or a check issued between the launches of
+ * a time loop where an allocation would synchronise the device).  Same test
+ * as cgfd_solver_check_finite(); *nonfinite = 1 when any of the n floats at
+ * d_data is NaN or Inf, else 0.  Scratch: a file-scope __device__ array of
+ * CGFD_NOALLOC_MAX_BLOCKS + 1 ints that every GPU loading this library keeps
+ * until exit; n above CGFD_NOALLOC_MAX_FLOATS is rejected (CGFD_EINVAL).
+ * The first call on a device looks the scratch address up and should come
+ * before any stream capture; calls that overlap on the GPU race on the
+ * shared scratch.  Runs on the legacy default stream and returns after the
+ * result is on the host. */
+#define CGFD_NOALLOC_MAX_BLOCKS 65536
+#define CGFD_NOALLOC_MAX_FLOATS (65536ull * 256ull * 64ull)
+int cgfd_check_finite_noalloc(const float *d_data, size_t n, int *nonfinite);
+
 #ifdef __cplusplus
 }
 #endif
