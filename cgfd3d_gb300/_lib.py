@@ -41,6 +41,9 @@ def lib():
     L.cgfd_solver_kernel_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
     L.cgfd_solver_set_timing.argtypes = [vp, C.c_int]
     L.cgfd_solver_transfer_bytes.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+    L.cgfd_solver_fetch_pg.argtypes = [vp, vp]
+    L.cgfd_solver_fetch_state.argtypes = [vp, vp]
+    L.cgfd_solver_fetch_surface_matrices.argtypes = [vp, vp, vp, vp]
     L.cgfd_solver_destroy.argtypes = [vp]
     L.cgfd_solver_destroy.restype = None
     L.cgfd_allstep.argtypes = [vp]
@@ -52,6 +55,26 @@ def lib():
         raise ImportError("libcgfd3d_gpu ABI version mismatch")
     _lib = L
     return L
+
+
+DROPIN_PATH = os.path.join(HERE, "_build", "libcgfd3d_dropin.so")
+_dropin = None
+
+
+def dropin():
+    """The drop-in library exporting drv_rk_curv_col_allstep."""
+    global _dropin
+    if _dropin is None:
+        lib()
+        if not os.path.exists(DROPIN_PATH):
+            raise ImportError("drop-in library %s is missing: run build()" % DROPIN_PATH)
+        D = C.CDLL(DROPIN_PATH)
+        D.drv_rk_curv_col_allstep.restype = None
+        D.drv_rk_curv_col_allstep.argtypes = [C.c_void_p] * 12 + [
+            C.c_float, C.c_int, C.c_float, C.c_char_p, C.c_char_p, C.c_int,
+            C.c_int, C.c_int]
+        _dropin = D
+    return _dropin
 
 
 def check(rc):

@@ -196,6 +196,42 @@ __global__ void k_recv(const float *__restrict__ w, long long vol, int ncmp,
   if (threadIdx.x == 0) *d_it = it + 1;
 }
 
+/* surface peak ground motion after a step (forward/wav_t.c:379-455):
+ * running maxima of |V|, |A| = |dV/dt| and |D| (D integrated with the
+ * trapezoid rule), 15 maps of nx*ny in the order PGV, PGVh, PGVx, PGVy,
+ * PGVz, PGA, PGAh, PGAx..z, PGD, PGDh, PGDx..z; Dis holds Dx, Dy, Dz */
+__global__ void k_pg(DevGrid g, const float *__restrict__ w1,
+                     const float *__restrict__ w0, float *PG, float *Dis, float dt)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
+  long long s2 = (long long)g.nx * g.ny;
+  long long q2 = i + (long long)j * g.nx;
+  float vx1 = w1[q], vy1 = w1[g.vol + q], vz1 = w1[2 * g.vol + q];
+  float vx0 = w0[q], vy0 = w0[g.vol + q], vz0 = w0[2 * g.vol + q];
+  float Ax = fabsf((vx1 - vx0) / dt), Ay = fabsf((vy1 - vy0) / dt),
+        Az = fabsf((vz1 - vz0) / dt);
+  float Dx = Dis[q2] + 0.5f * (vx1 + vx0) * dt;
+  float Dy = Dis[s2 + q2] + 0.5f * (vy1 + vy0) * dt;
+  float Dz = Dis[2 * s2 + q2] + 0.5f * (vz1 + vz0) * dt;
+  Dis[q2] = Dx; Dis[s2 + q2] = Dy; Dis[2 * s2 + q2] = Dz;
+  float V = sqrtf(vx1 * vx1 + vy1 * vy1 + vz1 * vz1);
+  float Vh = sqrtf(vx1 * vx1 + vy1 * vy1);
+  float A = sqrtf(Ax * Ax + Ay * Ay + Az * Az);
+  float Ah = sqrtf(Ax * Ax + Ay * Ay);
+  float D = sqrtf(Dx * Dx + Dy * Dy + Dz * Dz);
+  float Dh = sqrtf(Dx * Dx + Dy * Dy);
+  float v[15] = {V, Vh, fabsf(vx1), fabsf(vy1), fabsf(vz1), A, Ah, Ax, Ay, Az,
+                 D, Dh, fabsf(Dx), fabsf(Dy), fabsf(Dz)};
+#pragma unroll
+  for (int m = 0; m < 15; m++) {
+    float *p = PG + m * s2 + q2;
+    if (*p < v[m]) *p = v[m];
+  }
+}
+
 __global__ void k_nonfinite(const float *__restrict__ w, long long n, int *flag)
 {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -345,6 +381,7 @@ struct cgfd_solver {
   cudaGraphExec_t graph8;
   int graph_pre_lev;
   int *d_err;
+  float *pg, *dis;              /* surface peak-motion maps (free top) */
   CUtensorMap tmap;             /* 5-D map over the four wavefield levels */
   CUtensorMap tmap_met;         /* 4-D maps of the per-point streams */
   CUtensorMap tmap_med;
@@ -534,7 +571,7 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
   void *ptrs[] = {s->wav, s->metric, s->media, s->mats, s->src_col,
                   s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
                   s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
-                  s->line_iptr, s->d_it, s->d_flag, s->d_err};
+                  s->line_iptr, s->d_it, s->d_flag, s->d_err, s->pg, s->dis};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (int f = 0; f < CGFD_NFACE; f++)
@@ -633,7 +670,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   (void)nf;
   /* free surface matrices, computed on the device */
   if (p->free_top) {
-    size_t n2 = (size_t)g.sl * 9;
+    size_t n2 = (size_t)g.nx * g.ny * 9;
     TRY(dalloc(s, &s->mats, 3 * n2));
     TRYC(cudaMemsetAsync(s->mats, 0, 3 * n2 * sizeof(float), st));
     dim3 b(32, 8), gr((g.ni + 31) / 32, (g.nj + 7) / 8);
@@ -691,6 +728,13 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     for (int n = 0; n < p->line_n; n++) di[n] = (int)dev_index(g, p->line_iptr[n]);
     TRYC(cudaMemcpy(s->line_iptr, di.data(), di.size() * 4, cudaMemcpyHostToDevice));
     TRYC(cudaMemsetAsync(s->line_seismo, 0, ns * 4, st));
+  }
+  if (p->free_top) {
+    size_t s2 = (size_t)p->nx * p->ny;
+    TRY(dalloc(s, &s->pg, 15 * s2));
+    TRY(dalloc(s, &s->dis, 3 * s2));
+    TRYC(cudaMemsetAsync(s->pg, 0, 15 * s2 * 4, st));
+    TRYC(cudaMemsetAsync(s->dis, 0, 3 * s2 * 4, st));
   }
   TRY(dalloc(s, &s->d_it, 1));
   TRYC(cudaMemsetAsync(s->d_it, 0, 4, st));
@@ -823,7 +867,7 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   }
   a.free_top = p->free_top;
   if (p->free_top) {
-    size_t n2 = (size_t)s->g.sl * 9;
+    size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
     a.mVx = s->mats; a.mVy = s->mats + n2; a.mF = s->mats + 2 * n2;
   }
   if (p->src_n > 0) {
@@ -881,6 +925,11 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
   size_t L = level_floats(s->g);
+  if (s->pg) {
+    dim3 b(32, 8), gr((s->g.ni + 31) / 32, (s->g.nj + 7) / 8);
+    k_pg<<<gr, b, 0, st>>>(s->g, s->wav + s->end_lev * L, s->wav + s->pre_lev * L,
+                           s->pg, s->dis, p->dt);
+  }
   k_recv<<<1, 256, 0, st>>>(s->wav + s->end_lev * L, s->g.vol, p->ncmp,
                             p->recv_n, p->recv_ncmp, p->recv_max_nt, s->recv_dijk,
                             s->recv_idx, s->recv_seismo, p->line_n, p->line_max_nt,
@@ -930,7 +979,7 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
   s->n_pml = s->kernel == 2 ? 4 * nfaces * nsteps : 0;
-  s->n_other = nsteps;
+  s->n_other = nsteps * (s->pg ? 2 : 1);
   int herr = 0;
   CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));
   if (herr) return set_err(CGFD_ECUDA, "device wait timed out (code %d)", herr);
@@ -994,6 +1043,39 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
                        cudaMemcpyDeviceToHost, s->stream));
     s->d2h_bytes += nb;
   }
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
+extern "C" int cgfd_solver_fetch_surface_matrices(cgfd_solver_t *s, float *mVx,
+                                                  float *mVy, float *mF)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (!s->mats) return set_err(CGFD_EINVAL, "no free surface");
+  size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
+  float *dst[3] = {mVx, mVy, mF};
+  for (int m = 0; m < 3; m++)
+    if (dst[m]) CK(cudaMemcpy(dst[m], s->mats + m * n2, n2 * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int cgfd_solver_fetch_pg(cgfd_solver_t *s, float *pg)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (!s->pg) return set_err(CGFD_EINVAL, "no free surface, no peak-motion maps");
+  size_t n = 15 * (size_t)s->g.nx * s->g.ny;
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(pg, s->pg, n * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  size_t hvol = (size_t)s->g.nx * s->g.ny * s->g.nz;
+  size_t L = level_floats(s->g);
+  for (int c = 0; c < 9; c++)
+    CK(download_volume(s, w + c * hvol, s->wav + s->pre_lev * L + c * s->g.vol));
   CK(cudaStreamSynchronize(s->stream));
   return 0;
 }

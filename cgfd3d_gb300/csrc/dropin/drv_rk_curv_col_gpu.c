@@ -1,0 +1,265 @@
+/*
+ * drv_rk_curv_col_gpu.c -- drop-in replacement of CGFD3D's time loop.
+ *
+ * Exports drv_rk_curv_col_allstep() with the reference prototype
+ * (forward/drv_rk_curv_col.h:17-37), reading the reference's structs
+ * unchanged, and runs the whole loop through the flat C ABI of
+ * include/cgfd3d_gpu.h on the GPU.  Link it instead of
+ * forward/drv_rk_curv_col.o; see INTEGRATION.md.
+ *
+ * What the reference's loop leaves behind is left behind here too:
+ *   wav->v5d         final state in level 0 (nt_total even) or 3 (odd)
+ *   bdry->auxvar[][].var   final PML auxiliaries, same level rule
+ *   bdry->matVx2Vz2/matVy2Vz2/matF2Vz2   free-surface matrices
+ *   iorecv->recvone[r].seismo, ioline->recv_seismo[l]   seismograms
+ *   PGV/PGA/PGD surface maps (forward/wav_t.c:379-455), computed on the
+ *   device every step and, inside the reference binary, written by its
+ *   PG_slice_output() (forward/drv_rk_curv_col.c:547-550)
+ * Slices and snapshots (NetCDF, forward/io_funcs.c:780-1268) are written by
+ * the reference's own writers when this file is built inside the reference
+ * tree (CGFD_DROPIN_REFERENCE_HEADERS); the loop then advances step by step
+ * and hands them a host copy of the state at each step that writes.  Built
+ * without the reference (tests, other hosts) there are no NetCDF writers and
+ * requested slices/snapshots are reported and skipped.
+ *
+ * Errors print the library's message and call MPI_Abort when MPI is linked
+ * (exit(1) otherwise), as the reference does.  Unsupported configurations
+ * (surface force sources, dd sources, ablexp, media other than isotropic
+ * elastic) are reported the same way instead of being ignored.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../../include/cgfd3d_gpu.h"
+
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+#include "drv_rk_curv_col.h"
+#else
+#include "../../../include/cgfd3d_ref_abi.h"
+#endif
+
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+#define CGFD_ABORT() MPI_Abort(MPI_COMM_WORLD, 1)
+#else
+#define CGFD_ABORT() exit(1)
+#endif
+
+static void fail(const char *what)
+{
+  fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s: %s\n", what,
+          cgfd_last_error());
+  fflush(stderr);
+  CGFD_ABORT();
+}
+
+static void unsupported(const char *what)
+{
+  fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s is not supported\n", what);
+  fflush(stderr);
+  CGFD_ABORT();
+}
+
+void drv_rk_curv_col_allstep(
+    fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md, src_t *src,
+    bdry_t *bdry, wav_t *wav, mympi_t *mympi, iorecv_t *iorecv,
+    ioline_t *ioline, ioslice_t *ioslice, iosnap_t *iosnap, float dt,
+    int nt_total, float t0, char *output_fname_part, char *output_dir,
+    int qc_check_nan_num_of_step, const int output_all, const int verbose)
+{
+  (void)mympi; (void)output_fname_part; (void)output_dir; (void)output_all;
+
+  if (fd->num_rk_stages != 4 || fd->num_of_pairs != 8)
+    unsupported("an operator set other than MacCormack DRP with RK4");
+  if (md->medium_type != CGFD_MEDIUM_ELASTIC_ISO)
+    unsupported("this medium type");
+  if (src->dd_is_valid == 1) unsupported("a distributed (dd) source");
+  if (src->total_number > 0 && src->total_number_surface_force > 0)
+    unsupported("a surface force source");
+  if (bdry->is_enable_ablexp == 1) unsupported("the ablexp sponge boundary");
+
+  cgfd_problem_t p;
+  memset(&p, 0, sizeof(p));
+  p.ni = gd->ni; p.nj = gd->nj; p.nk = gd->nk;
+  p.nx = gd->nx; p.ny = gd->ny; p.nz = gd->nz;
+  p.ni1 = gd->ni1; p.ni2 = gd->ni2; p.nj1 = gd->nj1;
+  p.nj2 = gd->nj2; p.nk1 = gd->nk1; p.nk2 = gd->nk2;
+  p.jac = metric->jac;
+  p.xi_x = metric->xi_x; p.xi_y = metric->xi_y; p.xi_z = metric->xi_z;
+  p.eta_x = metric->eta_x; p.eta_y = metric->eta_y; p.eta_z = metric->eta_z;
+  p.zeta_x = metric->zeta_x; p.zeta_y = metric->zeta_y; p.zeta_z = metric->zeta_z;
+  p.medium_type = md->medium_type;
+  p.slw = md->rho; /* md_rho_to_slow ran before the call */
+  p.lambda = md->lambda;
+  p.mu = md->mu;
+  p.free_top = bdry->is_sides_free[2][1] == 1;
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      cgfd_pml_face_t *f = &p.pml[d][s];
+      f->enabled = bdry->is_enable_pml == 1 && bdry->is_sides_pml[d][s] == 1;
+      if (!f->enabled) continue;
+      f->ni1 = bdry->ni1[d][s]; f->ni2 = bdry->ni2[d][s];
+      f->nj1 = bdry->nj1[d][s]; f->nj2 = bdry->nj2[d][s];
+      f->nk1 = bdry->nk1[d][s]; f->nk2 = bdry->nk2[d][s];
+      f->A = bdry->A[d][s]; f->B = bdry->B[d][s]; f->D = bdry->D[d][s];
+      f->aux = bdry->auxvar[d][s].var;
+    }
+
+  if (src->total_number > 0) {
+    p.src_n = src->total_number;
+    p.src_max_nt = src->max_nt;
+    p.src_max_stage = src->max_stage;
+    p.src_force = src->force_actived;
+    p.src_moment = src->moment_actived;
+    p.src_spatial = src->itype_spatial_ext;
+    p.src_ext_half = src->ext_half_npoint;
+    p.src_ext_coef = src->ext_func_coef;
+    p.src_surface_strict = src->is_surface_force_strict;
+    p.src_n_surface_force = src->total_number_surface_force;
+    p.src_si = src->si; p.src_sj = src->sj; p.src_sk = src->sk;
+    p.src_si_inc = src->si_inc; p.src_sj_inc = src->sj_inc; p.src_sk_inc = src->sk_inc;
+    p.src_it_begin = src->it_begin; p.src_it_end = src->it_end;
+    p.Fx = src->Fx; p.Fy = src->Fy; p.Fz = src->Fz;
+    p.Mxx = src->Mxx; p.Myy = src->Myy; p.Mzz = src->Mzz;
+    p.Mxz = src->Mxz; p.Myz = src->Myz; p.Mxy = src->Mxy;
+  }
+
+  /* receivers: gather the per-station interpolation data, packed output */
+  int nr = iorecv->total_number;
+  float *rdijk = NULL, *rseis = NULL;
+  int *ridx = NULL;
+  if (nr > 0) {
+    rdijk = (float *)malloc(sizeof(float) * 3 * nr);
+    ridx = (int *)malloc(sizeof(int) * 8 * nr);
+    rseis = (float *)calloc((size_t)nr * iorecv->ncmp * iorecv->max_nt, sizeof(float));
+    if (!rdijk || !ridx || !rseis) unsupported("host memory for receivers");
+    for (int r = 0; r < nr; r++) {
+      iorecv_one_t *o = iorecv->recvone + r;
+      rdijk[3 * r] = o->di; rdijk[3 * r + 1] = o->dj; rdijk[3 * r + 2] = o->dk;
+      memcpy(ridx + 8 * r, o->indx1d, 8 * sizeof(int));
+    }
+    p.recv_n = nr;
+    p.recv_max_nt = iorecv->max_nt;
+    p.recv_ncmp = iorecv->ncmp;
+    p.recv_dijk = rdijk;
+    p.recv_indx1d = ridx;
+    p.recv_seismo = rseis;
+  }
+  /* lines: concatenated */
+  int nline = 0;
+  for (int l = 0; l < ioline->num_of_lines; l++) nline += ioline->line_nr[l];
+  int *liptr = NULL;
+  float *lseis = NULL;
+  if (nline > 0) {
+    liptr = (int *)malloc(sizeof(int) * nline);
+    lseis = (float *)calloc((size_t)nline * wav->ncmp * ioline->max_nt, sizeof(float));
+    if (!liptr || !lseis) unsupported("host memory for receiver lines");
+    int n = 0;
+    for (int l = 0; l < ioline->num_of_lines; l++)
+      for (int r = 0; r < ioline->line_nr[l]; r++) liptr[n++] = ioline->recv_iptr[l][r];
+    p.line_n = nline;
+    p.line_max_nt = ioline->max_nt;
+    p.line_iptr = liptr;
+    p.line_seismo = lseis;
+  }
+
+  p.ncmp = wav->ncmp;
+  p.nlevel = wav->nlevel;
+  p.wav = wav->v5d;
+  p.dt = dt;
+  p.t0 = t0;
+  p.nt_total = nt_total;
+
+  /* slice / snapshot writers of the reference */
+  int nslice = ioslice->num_of_slice_x + ioslice->num_of_slice_y +
+               ioslice->num_of_slice_z;
+  int nsnap = iosnap->num_of_snap;
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+  ioslice_nc_t ioslice_nc;
+  iosnap_nc_t iosnap_nc;
+  io_slice_nc_create(ioslice, wav->ncmp, wav->visco_type, wav->cmp_name, gd->ni,
+                     gd->nj, gd->nk, mympi->topoid, &ioslice_nc);
+  io_snap_nc_create(iosnap, &iosnap_nc, mympi->topoid);
+#else
+  if (nslice + nsnap > 0) {
+    fprintf(stderr, "drv_rk_curv_col_allstep (GPU): built without the reference's "
+                    "NetCDF writers, %d slices and %d snapshots skipped\n",
+            nslice, nsnap);
+    nslice = nsnap = 0;
+  }
+#endif
+  const int step_wise = nslice + nsnap > 0;
+  float *w_host = NULL, *w_buff = NULL;
+  if (step_wise) {
+    size_t L = (size_t)wav->ncmp * gd->nx * gd->ny * gd->nz;
+    w_host = (float *)malloc(L * sizeof(float));
+    w_buff = (float *)calloc(L, sizeof(float));
+    if (!w_host || !w_buff) unsupported("host memory for slice/snapshot output");
+  }
+
+  if (verbose > 0) fprintf(stdout, "GPU time loop: %d steps ...\n", nt_total);
+  cgfd_solver_t *s = NULL;
+  if (cgfd_solver_create(&p, &s) != 0) fail("solver setup");
+  int chunk = step_wise ? 1
+            : (qc_check_nan_num_of_step > 0 ? qc_check_nan_num_of_step : nt_total);
+  for (int done = 0; done < nt_total;) {
+    int n = nt_total - done < chunk ? nt_total - done : chunk;
+    if (cgfd_solver_run(s, n) != 0) fail("time loop");
+    done += n;
+    if (qc_check_nan_num_of_step > 0 && done % qc_check_nan_num_of_step == 0 &&
+        cgfd_solver_check_finite(s) != 0)
+      fail("wavefield check");
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+    if (step_wise) {
+      int it = done - 1;
+      float t_end = it * dt + t0 + dt;
+      int due = nslice > 0;
+      for (int m = 0; m < nsnap && !due; m++) {
+        int d = it - iosnap->it1[m];
+        due = d >= 0 && d % iosnap->dit[m] == 0 &&
+              d / iosnap->dit[m] <= (nt_total - iosnap->it1[m]) / iosnap->dit[m];
+      }
+      if (due) {
+        if (cgfd_solver_fetch_state(s, w_host) != 0) fail("state for output");
+        io_slice_nc_put(ioslice, &ioslice_nc, gd, w_host, w_buff, it, t_end, 0,
+                        wav->ncmp - 1, wav->visco_type);
+        io_snap_nc_put(iosnap, &iosnap_nc, gd, md, wav, w_host, w_buff, nt_total,
+                       it, t_end, 1, 1, 1);
+      }
+    }
+#endif
+  }
+  if (cgfd_solver_fetch(s) != 0) fail("fetch");
+  if (p.free_top && bdry->matVx2Vz2 &&
+      cgfd_solver_fetch_surface_matrices(s, bdry->matVx2Vz2, bdry->matVy2Vz2,
+                                          bdry->matF2Vz2) != 0)
+    fail("free-surface matrices");
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+  if (p.free_top) {
+    float *PG = (float *)calloc((size_t)15 * gd->nx * gd->ny, sizeof(float));
+    if (!PG) unsupported("host memory for the peak-motion maps");
+    if (cgfd_solver_fetch_pg(s, PG) != 0) fail("peak-motion maps");
+    PG_slice_output(PG, gd, output_dir, output_fname_part, mympi->topoid);
+    free(PG);
+  }
+  io_slice_nc_close(&ioslice_nc);
+  io_snap_nc_close(&iosnap_nc);
+#endif
+  cgfd_solver_destroy(s);
+  free(w_host);
+  free(w_buff);
+
+  /* scatter seismograms back into the reference's buffers */
+  for (int r = 0; r < nr; r++) {
+    size_t len = (size_t)iorecv->ncmp * iorecv->max_nt;
+    memcpy(iorecv->recvone[r].seismo, rseis + r * len, len * sizeof(float));
+  }
+  int n = 0;
+  for (int l = 0; l < ioline->num_of_lines; l++) {
+    size_t len = (size_t)ioline->line_nr[l] * wav->ncmp * ioline->max_nt;
+    memcpy(ioline->recv_seismo[l], lseis + (size_t)n * wav->ncmp * ioline->max_nt,
+           len * sizeof(float));
+    n += ioline->line_nr[l];
+  }
+  free(rdijk); free(ridx); free(rseis); free(liptr); free(lseis);
+}

@@ -43,6 +43,22 @@ class Solver:
         _lib.check(_lib.lib().cgfd_solver_kernel_times(self._h, t, n))
         return list(t), list(n)
 
+    def fetch_pg(self):
+        """Surface peak-motion maps (15 x ny x nx)."""
+        import numpy as np
+        p = self.problem
+        out = np.zeros(15 * p.nx * p.ny, np.float32)
+        _lib.check(_lib.lib().cgfd_solver_fetch_pg(self._h, out.ctypes.data))
+        return out.reshape(15, p.ny, p.nx)
+
+    def fetch_surface_matrices(self):
+        import numpy as np
+        p = self.problem
+        mats = [np.zeros(p.nx * p.ny * 9, np.float32) for _ in range(3)]
+        _lib.check(_lib.lib().cgfd_solver_fetch_surface_matrices(
+            self._h, *[m.ctypes.data for m in mats]))
+        return mats
+
     def set_timing(self, on=True):
         _lib.check(_lib.lib().cgfd_solver_set_timing(self._h, int(bool(on))))
 
@@ -74,6 +90,17 @@ def drv_rk_curv_col_allstep(problem):
     c = problem.to_c()
     _lib.check(_lib.lib().cgfd_allstep(C.addressof(c)))
     return problem
+
+
+def drv_rk_curv_col_allstep_structs(structs, dt, nt_total, t0=0.0,
+                                    qc_check_nan_num_of_step=0, verbose=0):
+    """Call the drop-in entry point with reference structs (refabi)."""
+    order = ["fd", "gd", "metric", "md", "src", "bdry", "wav", "mympi",
+             "iorecv", "ioline", "ioslice", "iosnap"]
+    args = [C.addressof(structs[n]) for n in order]
+    _lib.dropin().drv_rk_curv_col_allstep(*args, float(dt), int(nt_total), float(t0),
+                                          b"", b"", int(qc_check_nan_num_of_step),
+                                          0, int(verbose))
 
 
 def device_bytes(problem):

@@ -145,6 +145,21 @@ int cgfd_solver_fetch(cgfd_solver_t *s);
 /* Current step index. */
 int cgfd_solver_step(const cgfd_solver_t *s);
 
+/* Copies the free-surface conversion matrices (3 x nx*ny*9, layout of
+ * bdry_t.matVx2Vz2/matVy2Vz2/matF2Vz2, forward/bdry_t.c:86-109) to the host
+ * arrays given (NULL skips one). */
+int cgfd_solver_fetch_surface_matrices(cgfd_solver_t *s, float *mVx, float *mVy,
+                                       float *mF);
+
+/* Copies the surface peak-motion maps accumulated so far (15 x nx*ny, the
+ * PG array of forward/drv_rk_curv_col.c:123-130, filled as PG_calcu does,
+ * forward/wav_t.c:379-455).  Only with a free surface. */
+int cgfd_solver_fetch_pg(cgfd_solver_t *s, float *pg);
+
+/* Copies the current state (9 x nx*ny*nz, reference layout) to w without
+ * touching the problem's arrays. */
+int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w);
+
 /* Checks the whole wavefield for NaN/Inf on the device.
  * Returns CGFD_OK or CGFD_ENONFINITE. */
 int cgfd_solver_check_finite(cgfd_solver_t *s);

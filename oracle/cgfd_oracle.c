@@ -101,6 +101,7 @@ typedef struct {
   float **ext;               /* per source Gaussian weights (or NULL) */
   int nthreads;
   int timg_mode;
+  float *pg, *dis;           /* peak-motion maps (NULL: not computed) */
   pthread_barrier_t bar;
 } orc_t;
 
@@ -605,6 +606,39 @@ static void keep_recv(orc_t *o, const float *w, int it)
           w[c * o->vol + p->line_iptr[n]];
 }
 
+/* surface peak ground motion after a step (forward/wav_t.c:379-455) */
+static void pg_calcu(orc_t *o, const float *w1, const float *w0, float *PG,
+                     float *Dis)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t s2 = o->sl, V = o->vol;
+  float dt = p->dt;
+  for (int j = p->nj1; j <= p->nj2; j++)
+    for (int i = p->ni1; i <= p->ni2; i++) {
+      size_t q = i + j * o->ln + (size_t)p->nk2 * s2, q1 = i + j * o->ln;
+      float vx1 = w1[q], vy1 = w1[V + q], vz1 = w1[2 * V + q];
+      float vx0 = w0[q], vy0 = w0[V + q], vz0 = w0[2 * V + q];
+      float Ax = fabsf((vx1 - vx0) / dt), Ay = fabsf((vy1 - vy0) / dt),
+            Az = fabsf((vz1 - vz0) / dt);
+      float *Dx = Dis + q1, *Dy = Dis + s2 + q1, *Dz = Dis + 2 * s2 + q1;
+      *Dx = (float)(*Dx + 0.5 * (vx1 + vx0) * dt);
+      *Dy = (float)(*Dy + 0.5 * (vy1 + vy0) * dt);
+      *Dz = (float)(*Dz + 0.5 * (vz1 + vz0) * dt);
+      float v[15];
+      v[0] = (float)sqrt(vx1 * vx1 + vy1 * vy1 + vz1 * vz1);
+      v[1] = (float)sqrt(vx1 * vx1 + vy1 * vy1);
+      v[2] = fabsf(vx1); v[3] = fabsf(vy1); v[4] = fabsf(vz1);
+      v[5] = (float)sqrt(Ax * Ax + Ay * Ay + Az * Az);
+      v[6] = (float)sqrt(Ax * Ax + Ay * Ay);
+      v[7] = Ax; v[8] = Ay; v[9] = Az;
+      v[10] = (float)sqrt(*Dx * *Dx + *Dy * *Dy + *Dz * *Dz);
+      v[11] = (float)sqrt(*Dx * *Dx + *Dy * *Dy);
+      v[12] = fabsf(*Dx); v[13] = fabsf(*Dy); v[14] = fabsf(*Dz);
+      for (int m = 0; m < 15; m++)
+        if (PG[m * s2 + q1] < v[m]) PG[m * s2 + q1] = v[m];
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* time loop                                                                */
 /* ------------------------------------------------------------------------ */
@@ -712,7 +746,10 @@ static void *worker(void *arg)
       }
       pthread_barrier_wait(&o->bar);
     }
-    if (tid == 0) keep_recv(o, end, it);
+    if (tid == 0) {
+      if (o->pg) pg_calcu(o, end, pre, o->pg, o->dis);
+      keep_recv(o, end, it);
+    }
     /* swap pre and end (drv_rk_curv_col.c:530-542) */
     float *t = pre; pre = end; end = t;
     for (int d = 0; d < 3; d++)
@@ -731,8 +768,19 @@ static void *worker(void *arg)
  * written).  mVx/mVy/mF receive the free-surface matrices (nx*ny*9 each,
  * may be NULL when there is no free surface).
  */
+int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
+                      float *mVx, float *mVy, float *mF, float *pg);
+
 int oracle_allstep(const cgfd_problem_t *p, int timg_mode, int nthreads,
                    float *mVx, float *mVy, float *mF)
+{
+  return oracle_allstep_pg(p, timg_mode, nthreads, mVx, mVy, mF, NULL);
+}
+
+/* as oracle_allstep; pg (15 x nx*ny, zero on entry) receives the surface
+ * peak-motion maps when non-NULL and the top is free */
+int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
+                      float *mVx, float *mVy, float *mF, float *pg)
 {
   if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO) return CGFD_EINVAL;
   if (p->src_n_surface_force > 0) return CGFD_EINVAL;
@@ -780,6 +828,10 @@ int oracle_allstep(const cgfd_problem_t *p, int timg_mode, int nthreads,
                   p->src_sk_inc[is], p->src_ext_coef, half, kz2);
     }
   }
+  if (pg && p->free_top) {
+    o.pg = pg;
+    o.dis = calloc(3 * o.sl, sizeof(float));
+  }
   pthread_barrier_init(&o.bar, NULL, o.nthreads);
   pthread_t *ths = calloc(o.nthreads, sizeof(pthread_t));
   thr_t *ta = calloc(o.nthreads, sizeof(thr_t));
@@ -798,5 +850,6 @@ int oracle_allstep(const cgfd_problem_t *p, int timg_mode, int nthreads,
     free(o.ext);
   }
   if (own_m) { free(mVx); free(mVy); free(mF); }
+  free(o.dis);
   return 0;
 }

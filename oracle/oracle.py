@@ -39,14 +39,22 @@ def lib():
         _lib.oracle_allstep.restype = C.c_int
         _lib.oracle_allstep.argtypes = [C.c_void_p, C.c_int, C.c_int,
                                         C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.oracle_allstep_pg.restype = C.c_int
+        _lib.oracle_allstep_pg.argtypes = [C.c_void_p, C.c_int, C.c_int,
+                                           C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p]
         _lib.oracle_dvh2dvz_iso.restype = C.c_int
         _lib.oracle_dvh2dvz_iso.argtypes = [C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p]
     return _lib
 
 
-def allstep(problem, timg_mode=TIMG_ZERO, nthreads=1, want_mats=False):
-    """Run the oracle on a cgfd3d_gb300.problem.Problem in place."""
+def allstep(problem, timg_mode=TIMG_ZERO, nthreads=1, want_mats=False,
+            want_pg=False):
+    """Run the oracle on a cgfd3d_gb300.problem.Problem in place.
+
+    Returns the free-surface matrices (want_mats) and/or the 15 peak-motion
+    maps (want_pg) when asked for."""
     import numpy as np
     cs = problem.to_c()
     mats = None
@@ -56,7 +64,15 @@ def allstep(problem, timg_mode=TIMG_ZERO, nthreads=1, want_mats=False):
         ptrs = [m.ctypes.data for m in mats]
     else:
         ptrs = [None, None, None]
-    rc = lib().oracle_allstep(C.addressof(cs), timg_mode, nthreads, *ptrs)
+    pg = None
+    if want_pg and problem.free_top:
+        pg = np.zeros(15 * problem.nx * problem.ny, np.float32)
+    rc = lib().oracle_allstep_pg(C.addressof(cs), timg_mode, nthreads, *ptrs,
+                                 None if pg is None else pg.ctypes.data)
     if rc != 0:
         raise RuntimeError("oracle_allstep failed with code %d" % rc)
+    if want_mats and want_pg:
+        return mats, pg
+    if want_pg:
+        return pg
     return mats if want_mats else None
