@@ -44,6 +44,7 @@ def lib():
     L.cgfd_solver_fetch_pg.argtypes = [vp, vp]
     L.cgfd_solver_fetch_state.argtypes = [vp, vp]
     L.cgfd_solver_fetch_surface_matrices.argtypes = [vp, vp, vp, vp]
+    L.cgfd_solver_fetch_surface_rotation.argtypes = [vp, vp]
     L.cgfd_solver_destroy.argtypes = [vp]
     L.cgfd_solver_destroy.restype = None
     L.cgfd_allstep.argtypes = [vp]

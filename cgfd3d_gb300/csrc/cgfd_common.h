@@ -2,7 +2,7 @@
  * Shared host/device definitions of the GB300 time-stepping library.
  *
  * Device layout in HBM (per solver):
- *   wavefield  4 levels x 9 components x padded volume (nx*ny*nz), the
+ *   wavefield  4 levels x ncmp components x padded volume, the
  *              reference's layout (forward/wav_t.c:40-136) with the level
  *              roles  pre | tmpA | tmpB | end.  The reference keeps a
  *              separate rhs level; here the RHS lives only in registers and
@@ -10,7 +10,8 @@
  *              stage that reads tmp with a +-3 stencil never writes the
  *              buffer it reads.
  *   metrics    10 x volume: jac, xi_x..zeta_z (forward/gd_t.c:142-180)
- *   media      3 x volume: slw (=1/rho), lambda, mu
+ *   media      slw (=1/rho) and the medium's constants, one volume each
+ *              (cgfd_media.cuh)
  *   PML aux    per enabled face: 4 levels x 9 x face-box volume
  *   surface    3 x (nx*ny*9) conversion matrices (k = nk2)
  */
@@ -58,11 +59,18 @@ struct SrcEntry {
   int pad;
 };
 
+/* Maxwell bodies the fused visco-elastic path holds in shared memory */
+#define CGFD_VIS_NMW_MAX 3
+
 struct StageArgs {
   DevGrid g;
   /* metrics and media */
   const float *jac, *xix, *xiy, *xiz, *etx, *ety, *etz, *ztx, *zty, *ztz;
   const float *slw, *lam, *mu;
+  const float *med;   /* media block (cgfd_media.cuh), component stride g.vol */
+  int ncmp;           /* wavefield components per level (9 + 6 nmw) */
+  int nmw;            /* Maxwell bodies (visco-elastic), else 0 */
+  float wl[CGFD_VIS_NMW_MAX];   /* relaxation angular frequencies */
   /* wavefield levels for this stage */
   const float *cur;   /* stencil input */
   const float *pre;   /* level "pre" */
@@ -77,7 +85,7 @@ struct StageArgs {
   float *aend[CGFD_NFACE];
   /* free surface */
   int free_top;
-  const float *mVx, *mVy, *mF;
+  const float *mVx, *mVy, *mF, *mD;
   /* sources */
   int src_n, src_max_nt, src_max_stage, src_force, src_moment;
   const int *src_col;          /* (ni*nj + 1) offsets into src_ent */

@@ -1,0 +1,43 @@
+/*
+ * Launchers of the per-stage kernels, one set per medium.  Each medium's
+ * kernels live in their own translation unit (cgfd_launch_{iso,vti,vis}.cu,
+ * all expanding cgfd_launch.cuh) so that the library's build compiles them
+ * in parallel; cgfd_solver.cu only sees these declarations.
+ */
+#ifndef CGFD_LAUNCH_H
+#define CGFD_LAUNCH_H
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "cgfd_common.h"
+
+/* tensor maps of one solver (cgfd_stage3.cuh) */
+struct StageMaps {
+  CUtensorMap wav;   /* 5-D (x, y, z, component, level), 9-component planes */
+  CUtensorMap met;   /* 4-D metrics, TX x TY tiles */
+  CUtensorMap med;   /* 4-D media, TX x TY tiles */
+  CUtensorMap pt;    /* 5-D wavefield, TX x TY x 9 tiles (pre / end) */
+  CUtensorMap j;     /* 5-D wavefield, TX x TY x 6 nmw tiles (memory variables) */
+};
+
+/* fused interior stage kernel: bias code bx*4 + by*2 + bz, kind 0/1/2 */
+void cgfd_launch_stage_iso(int code, int kind, dim3 grid, cudaStream_t st,
+                           const StageArgs &a, const StageMaps &m);
+void cgfd_launch_stage_vti(int code, int kind, dim3 grid, cudaStream_t st,
+                           const StageArgs &a, const StageMaps &m);
+void cgfd_launch_stage_vis(int code, int kind, dim3 grid, cudaStream_t st,
+                           const StageArgs &a, const StageMaps &m);
+
+/* CFS-PML face kernel of face f (normal dim, operator bias b), n points */
+void cgfd_launch_pml_iso(int dim, int b, int kind, int f, long long n,
+                         cudaStream_t st, const StageArgs &a);
+void cgfd_launch_pml_vti(int dim, int b, int kind, int f, long long n,
+                         cudaStream_t st, const StageArgs &a);
+void cgfd_launch_pml_vis(int dim, int b, int kind, int f, long long n,
+                         cudaStream_t st, const StageArgs &a);
+
+/* dynamic shared memory of the stage kernel of a medium (0 iso, 1 vti, 2 vis) */
+int cgfd_stage_smem_bytes(int med);
+
+#endif

@@ -19,14 +19,21 @@
  *
  * One thread per point of the face box, linear index with i fastest, plain
  * coalesced loads (the face boxes are thin; their operands are read once).
+ *
+ * MED selects Hooke's law (cgfd_media.cuh; VTI: forward/sv_curv_col_el_vti.c:
+ * 592-1075).  For the GMB visco-elastic medium the reference's attenuation
+ * pass reads hT after the PML corrections (forward/sv_curv_col_vis_iso.c:
+ * 200-232); its memory-variable rates are linear in hT, so this kernel also
+ * adds wl_n EV(corr) to the memory variables' tmp/end.
  */
 #ifndef CGFD_PML_CUH
 #define CGFD_PML_CUH
 
 #include "cgfd_common.h"
+#include "cgfd_media.cuh"
 #include "cgfd_stage.cuh"
 
-template <int DIM, int B, int KIND>
+template <int DIM, int B, int KIND, int MED>
 __global__ void __launch_bounds__(256)
     k_pml_face(const __grid_constant__ StageArgs a, int f)
 {
@@ -47,8 +54,8 @@ __global__ void __launch_bounds__(256)
   const float *e2p = DIM == 0 ? a.xiy : (DIM == 1 ? a.ety : a.zty);
   const float *e3p = DIM == 0 ? a.xiz : (DIM == 1 ? a.etz : a.ztz);
   float e1 = LDG(e1p + q), e2 = LDG(e2p + q), e3 = LDG(e3p + q);
-  float lam = LDG(a.lam + q), mu = LDG(a.mu + q), slw = LDG(a.slw + q);
-  float l2m = lam + 2.0f * mu;
+  const MedPt m = med_from<MED, true>(a.med + q, vol);
+  const float slw = m.slw;
 
   Deriv9 d;
   deriv9<B>(a.cur, q, vol, s, d);
@@ -60,12 +67,7 @@ __global__ void __launch_bounds__(256)
   sv[C_VX] = slw * (e1 * d.Txx + e2 * d.Txy + e3 * d.Txz);
   sv[C_VY] = slw * (e1 * d.Txy + e2 * d.Tyy + e3 * d.Tyz);
   sv[C_VZ] = slw * (e1 * d.Txz + e2 * d.Tyz + e3 * d.Tzz);
-  sv[C_TXX] = l2m * e1 * d.Vx + lam * e2 * d.Vy + lam * e3 * d.Vz;
-  sv[C_TYY] = lam * e1 * d.Vx + l2m * e2 * d.Vy + lam * e3 * d.Vz;
-  sv[C_TZZ] = lam * e1 * d.Vx + lam * e2 * d.Vy + l2m * e3 * d.Vz;
-  sv[C_TXY] = mu * (e2 * d.Vx + e1 * d.Vy);
-  sv[C_TXZ] = mu * (e3 * d.Vx + e1 * d.Vz);
-  sv[C_TYZ] = mu * (e3 * d.Vy + e2 * d.Vz);
+  hooke1<MED>(m, e1, e2, e3, d.Vx, d.Vy, d.Vz, sv);
 
   const long long av = F.avol;
   const float *acur = a.acur[f];
@@ -84,12 +86,7 @@ __global__ void __launch_bounds__(256)
     float DzVz = LDG(M + 6) * d.Vx + LDG(M + 7) * d.Vy + LDG(M + 8) * d.Vz;
     float ztx = LDG(a.ztx + q), zty = LDG(a.zty + q), ztz = LDG(a.ztz + q);
     float t[9];
-    t[C_TXX] = l2m * (ztx * DzVx) + lam * (zty * DzVy + ztz * DzVz);
-    t[C_TYY] = l2m * (zty * DzVy) + lam * (ztx * DzVx + ztz * DzVz);
-    t[C_TZZ] = l2m * (ztz * DzVz) + lam * (ztx * DzVx + zty * DzVy);
-    t[C_TXY] = mu * (zty * DzVx + ztx * DzVy);
-    t[C_TXZ] = mu * (ztz * DzVx + ztx * DzVz);
-    t[C_TYZ] = mu * (ztz * DzVy + zty * DzVz);
+    hooke1<MED>(m, ztx, zty, ztz, DzVx, DzVy, DzVz, t);
 #pragma unroll
     for (int c = C_TXX; c <= C_TXY; c++) {
       corr[c] += cB1 * t[c];
@@ -118,6 +115,22 @@ __global__ void __launch_bounds__(256)
     } else {
       aend[xa] = aend[xa] + a.cb * arhs[c];
       a.end[x] += a.cb * corr[c];
+    }
+  }
+  if (MED == MED_VIS) {
+    /* memory-variable rates of the correction: wl_n EV(corr) */
+    float ev[6];
+    vis_strain_rate(m.lam, m.mu, corr, ev);
+#pragma unroll
+    for (int n = 0; n < CGFD_VIS_NMW_MAX; n++) {
+      if (n >= a.nmw) break;
+#pragma unroll
+      for (int c = 0; c < 6; c++) {
+        long long x = (long long)(9 + 6 * n + c) * vol + q;
+        float h = a.wl[n] * ev[c];
+        if (KIND <= 1) a.tmp_out[x] += a.ca * h;
+        a.end[x] += a.cb * h;
+      }
     }
   }
 }

@@ -2,13 +2,16 @@
  * cgfd_solver.cu -- device-resident RK4 time loop for CGFD3D, sm_103a.
  *
  * Implements the flat C ABI of include/cgfd3d_gpu.h.  One solver object
- * owns every array the time loop touches in HBM; a step is four fused stage
- * launches (cgfd_stage.cuh) plus one receiver-gather launch, and the
- * 8-step pair cycle (forward/fd_t.c:182-236) can be captured once into a
- * CUDA graph and replayed.
+ * owns every array the time loop touches in HBM; a step is, per RK stage,
+ * one fused interior stage launch (cgfd_stage3.cuh) and one CFS-PML launch
+ * per enabled face (cgfd_pml.cuh), then the surface and receiver launches.
+ * Media: isotropic elastic, VTI elastic and GMB visco-elastic isotropic
+ * (cgfd_media.cuh); their kernels are compiled in cgfd_launch_*.cu.
  *
  * Reference: forward/drv_rk_curv_col.c:27-556 (time loop),
- * forward/sv_curv_col_el_iso.c:1258-1375 (free-surface matrices),
+ * forward/sv_curv_col_el_iso.c:1258-1375, forward/sv_curv_col_el_vti.c:
+ * 1085-1206, forward/sv_curv_col_vis_iso.c:353-507 (free-surface matrices),
+ * forward/sv_curv_col_vis_iso.c:509-623 (visco surface stress rotation),
  * forward/io_funcs.c:1584-1645 (receivers, lines).
  */
 #include <cuda_runtime.h>
@@ -24,9 +27,9 @@
 
 #include "../../include/cgfd3d_gpu.h"
 #include "cgfd_common.h"
-#include "cgfd_stage.cuh"
-#include "cgfd_stage3.cuh"
-#include "cgfd_pml.cuh"
+#include "cgfd_launch.h"
+#include "cgfd_media.cuh"
+#include "cgfd_stage2.cuh"
 
 /* ------------------------------------------------------------------------ */
 /* errors                                                                    */
@@ -161,6 +164,190 @@ __global__ void k_dvh2dvz_iso(DevGrid g, const float *__restrict__ xix,
       mVy[ij + r * 3 + c] = ac;
       mF[ij + r * 3 + c] = A[r][c];
     }
+}
+
+/* 3x3 inverse by adjugate / determinant, as lib/fdlib_math.c:8-35 */
+__device__ __forceinline__ void inv3_dev(float A[3][3])
+{
+  float v[3][3];
+  v[0][0] = A[1][1] * A[2][2] - A[2][1] * A[1][2];
+  v[0][1] = A[2][1] * A[0][2] - A[0][1] * A[2][2];
+  v[0][2] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+  v[1][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+  v[1][1] = A[0][0] * A[2][2] - A[2][0] * A[0][2];
+  v[1][2] = A[1][0] * A[0][2] - A[0][0] * A[1][2];
+  v[2][0] = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+  v[2][1] = A[2][0] * A[0][1] - A[0][0] * A[2][1];
+  v[2][2] = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+  float det = 1.0f / (v[0][0] * A[0][0] + v[0][1] * A[1][0] + v[0][2] * A[2][0]);
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) A[r][c] = v[r][c] * det;
+}
+
+/* VTI free-surface matrices -A^-1 B, -A^-1 C per surface point
+ * (forward/sv_curv_col_el_vti.c:1149-1203): A, B, C are the zeta-zeta,
+ * zeta-xi and zeta-eta contractions of the VTI stiffness */
+__global__ void k_dvh2dvz_vti(DevGrid g, const float *__restrict__ M,
+                              const float *__restrict__ med, float *mVx,
+                              float *mVy)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
+  const long long v = g.vol;
+  float xi[3] = {M[v + q], M[2 * v + q], M[3 * v + q]};
+  float et[3] = {M[4 * v + q], M[5 * v + q], M[6 * v + q]};
+  float zt[3] = {M[7 * v + q], M[8 * v + q], M[9 * v + q]};
+  MedPt m = med_from<MED_VTI, true>(med + q, v);
+  /* K(a, b)[r][c]: row r of the traction on the plane of normal a produced
+   * by the velocity gradient along direction b, component c (VTI stiffness) */
+  auto K = [&](const float *a, const float *b, float out[3][3]) {
+    out[0][0] = m.c11 * b[0] * a[0] + m.c66 * b[1] * a[1] + m.c55 * b[2] * a[2];
+    out[0][1] = m.c12 * b[1] * a[0] + m.c66 * b[0] * a[1];
+    out[0][2] = m.c13 * b[2] * a[0] + m.c55 * b[0] * a[2];
+    out[1][0] = m.c66 * b[1] * a[0] + m.c12 * b[0] * a[1];
+    out[1][1] = m.c66 * b[0] * a[0] + m.c11 * b[1] * a[1] + m.c55 * b[2] * a[2];
+    out[1][2] = m.c13 * b[2] * a[1] + m.c55 * b[1] * a[2];
+    out[2][0] = m.c55 * b[2] * a[0] + m.c13 * b[0] * a[2];
+    out[2][1] = m.c55 * b[2] * a[1] + m.c13 * b[1] * a[2];
+    out[2][2] = m.c55 * b[0] * a[0] + m.c55 * b[1] * a[1] + m.c33 * b[2] * a[2];
+  };
+  float A[3][3], B[3][3], C[3][3];
+  K(zt, zt, A);
+  K(zt, xi, B);
+  K(zt, et, C);
+  inv3_dev(A);
+  long long ij = (i + (long long)j * g.nx) * 9;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      float ab = 0.f, ac = 0.f;
+      for (int k = 0; k < 3; k++) {
+        ab += A[r][k] * B[k][c];
+        ac += A[r][k] * C[k][c];
+      }
+      mVx[ij + r * 3 + c] = -ab;
+      mVy[ij + r * 3 + c] = -ac;
+    }
+}
+
+/* visco-elastic free-surface matrices (forward/sv_curv_col_vis_iso.c:
+ * 416-503): the isotropic A^-1 B, A^-1 C and the rotation matrix D of the
+ * local surface frame (rows: the in-plane direction normal to the eta
+ * tangent, the eta tangent, the zeta normal), from the grid's eta tangent
+ * (centred 7-point operator along j on the coordinates of the surface
+ * plane, forward/fd_t.c:152-176) */
+__global__ void k_dvh2dvz_vis(DevGrid g, const float *__restrict__ M,
+                              const float *__restrict__ med,
+                              const float *__restrict__ x2,
+                              const float *__restrict__ y2,
+                              const float *__restrict__ z2, float *mVx,
+                              float *mVy, float *mD)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
+  const long long v = g.vol;
+  const float e11 = M[v + q], e12 = M[2 * v + q], e13 = M[3 * v + q];
+  const float e21 = M[4 * v + q], e22 = M[5 * v + q], e23 = M[6 * v + q];
+  const float e31 = M[7 * v + q], e32 = M[8 * v + q], e33 = M[9 * v + q];
+  const float lam = med[v + q], mu = med[2 * v + q];
+  const float l2m = lam + 2.0f * mu;
+  const float fc[7] = {-0.02084f, 0.1667f, -0.7709f, 0.0f, 0.7709f, -0.1667f, 0.02084f};
+  float xet = 0.f, yet = 0.f, zet = 0.f;
+  for (int n = 0; n < 7; n++) {
+    long long p2 = i + (long long)(j + n - 3) * g.nx;
+    xet += fc[n] * x2[p2];
+    yet += fc[n] * y2[p2];
+    zet += fc[n] * z2[p2];
+  }
+  float e_n = 1.0f / sqrtf(xet * xet + yet * yet + zet * zet);
+  float e_m = 1.0f / sqrtf(e31 * e31 + e32 * e32 + e33 * e33);
+  float e_nm = e_n * e_m;
+  float A[3][3], B[3][3], C[3][3];
+  A[0][0] = l2m * e31 * e31 + mu * (e32 * e32 + e33 * e33);
+  A[0][1] = lam * e31 * e32 + mu * e32 * e31;
+  A[0][2] = lam * e31 * e33 + mu * e33 * e31;
+  A[1][0] = lam * e32 * e31 + mu * e31 * e32;
+  A[1][1] = l2m * e32 * e32 + mu * (e31 * e31 + e33 * e33);
+  A[1][2] = lam * e32 * e33 + mu * e33 * e32;
+  A[2][0] = lam * e33 * e31 + mu * e31 * e33;
+  A[2][1] = lam * e33 * e32 + mu * e32 * e33;
+  A[2][2] = l2m * e33 * e33 + mu * (e31 * e31 + e32 * e32);
+  inv3_dev(A);
+  B[0][0] = -l2m * e31 * e11 - mu * (e32 * e12 + e33 * e13);
+  B[0][1] = -lam * e31 * e12 - mu * e32 * e11;
+  B[0][2] = -lam * e31 * e13 - mu * e33 * e11;
+  B[1][0] = -lam * e32 * e11 - mu * e31 * e12;
+  B[1][1] = -l2m * e32 * e12 - mu * (e31 * e11 + e33 * e13);
+  B[1][2] = -lam * e32 * e13 - mu * e33 * e12;
+  B[2][0] = -lam * e33 * e11 - mu * e31 * e13;
+  B[2][1] = -lam * e33 * e12 - mu * e32 * e13;
+  B[2][2] = -l2m * e33 * e13 - mu * (e31 * e11 + e32 * e12);
+  C[0][0] = -l2m * e31 * e21 - mu * (e32 * e22 + e33 * e23);
+  C[0][1] = -lam * e31 * e22 - mu * e32 * e21;
+  C[0][2] = -lam * e31 * e23 - mu * e33 * e21;
+  C[1][0] = -lam * e32 * e21 - mu * e31 * e22;
+  C[1][1] = -l2m * e32 * e22 - mu * (e31 * e21 + e33 * e23);
+  C[1][2] = -lam * e32 * e23 - mu * e33 * e22;
+  C[2][0] = -lam * e33 * e21 - mu * e31 * e23;
+  C[2][1] = -lam * e33 * e22 - mu * e32 * e23;
+  C[2][2] = -l2m * e33 * e23 - mu * (e31 * e21 + e32 * e22);
+  float D[3][3] = {{(yet * e33 - zet * e32) * e_nm, (zet * e31 - xet * e33) * e_nm,
+                    (xet * e32 - yet * e31) * e_nm},
+                   {xet * e_n, yet * e_n, zet * e_n},
+                   {e31 * e_m, e32 * e_m, e33 * e_m}};
+  long long ij = (i + (long long)j * g.nx) * 9;
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      float ab = 0.f, ac = 0.f;
+      for (int k = 0; k < 3; k++) {
+        ab += A[r][k] * B[k][c];
+        ac += A[r][k] * C[k][c];
+      }
+      mVx[ij + r * 3 + c] = ab;
+      mVy[ij + r * 3 + c] = ac;
+      mD[ij + r * 3 + c] = D[r][c];
+    }
+}
+
+/* visco-elastic free surface after the last stage: the surface stress is
+ * rotated into the local frame D, its components on the surface normal are
+ * dropped and it is rotated back, T <- D^T P(D T D^T) D
+ * (forward/sv_curv_col_vis_iso.c:509-623); surface plane of the end level */
+__global__ void k_vis_free(DevGrid g, float *w, const float *__restrict__ mD)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
+  const long long v = g.vol;
+  const float *D = mD + (i + (long long)j * g.nx) * 9;
+  float d11 = D[0], d12 = D[1], d13 = D[2], d21 = D[3], d22 = D[4], d23 = D[5];
+  float Txx = w[C_TXX * v + q], Tyy = w[C_TYY * v + q], Tzz = w[C_TZZ * v + q];
+  float Txy = w[C_TXY * v + q], Txz = w[C_TXZ * v + q], Tyz = w[C_TYZ * v + q];
+  float l00 = d11 * d11 * Txx + d12 * d12 * Tyy + d13 * d13 * Tzz +
+              2.0f * (d11 * d12 * Txy + d11 * d13 * Txz + d12 * d13 * Tyz);
+  float l01 = d11 * d21 * Txx + d12 * d22 * Tyy + d13 * d23 * Tzz +
+              (d11 * d22 + d12 * d21) * Txy + (d11 * d23 + d21 * d13) * Txz +
+              (d12 * d23 + d22 * d13) * Tyz;
+  float l11 = d21 * d21 * Txx + d22 * d22 * Tyy + d23 * d23 * Tzz +
+              2.0f * (d21 * d22 * Txy + d21 * d23 * Txz + d22 * d23 * Tyz);
+  /* Tg = D^T Tl D with Tl = [[l00, l01, 0], [l01, l11, 0], [0, 0, 0]] */
+  float Tg[3][3];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      float dr0 = D[0 * 3 + r], dr1 = D[1 * 3 + r];
+      float dc0 = D[0 * 3 + c], dc1 = D[1 * 3 + c];
+      Tg[r][c] = (dr0 * l00 + dr1 * l01) * dc0 + (dr0 * l01 + dr1 * l11) * dc1;
+    }
+  w[C_TXX * v + q] = Tg[0][0];
+  w[C_TYY * v + q] = Tg[1][1];
+  w[C_TZZ * v + q] = Tg[2][2];
+  w[C_TXY * v + q] = Tg[0][1];
+  w[C_TXZ * v + q] = Tg[0][2];
+  w[C_TYZ * v + q] = Tg[1][2];
 }
 
 /* receivers and lines after a step; one block; advances the step counter.
@@ -353,10 +540,13 @@ struct cgfd_solver {
   const cgfd_problem_t *p;
   DevGrid g;
   cudaStream_t stream;
-  float *wav;                   /* 4 levels */
+  int med;                      /* MED_ISO / MED_VTI / MED_VIS */
+  int ncmp;                     /* wavefield components per level */
+  int nmed;                     /* media components */
+  float *wav;                   /* 4 levels x ncmp x vol */
   float *metric;                /* 10 x vol */
-  float *media;                 /* 3 x vol */
-  float *mats;                  /* 3 x sl*9 */
+  float *media;                 /* nmed x vol (cgfd_media.cuh) */
+  float *mats;                  /* 3 (4 for visco) x nx*ny*9 */
   float *aux[CGFD_NFACE];       /* 4 levels each */
   DevFace face[CGFD_NFACE];
   int face_src[CGFD_NFACE][2];  /* idim, iside */
@@ -382,15 +572,18 @@ struct cgfd_solver {
   int graph_pre_lev;
   int *d_err;
   float *pg, *dis;              /* surface peak-motion maps (free top) */
-  CUtensorMap tmap;             /* 5-D map over the four wavefield levels */
-  CUtensorMap tmap_met;         /* 4-D maps of the per-point streams */
-  CUtensorMap tmap_med;
-  CUtensorMap tmap_pt;
+  StageMaps maps;               /* tensor maps of the stage kernel */
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
   int kchunk;
 };
 
-static size_t level_floats(const DevGrid &g) { return (size_t)CGFD_NCMP * g.vol; }
+static size_t level_floats(const cgfd_solver_t *s) { return (size_t)s->ncmp * s->g.vol; }
+
+static int medium_of(int medium_type)
+{
+  return medium_type == CGFD_MEDIUM_ELASTIC_VTI ? MED_VTI
+       : medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO ? MED_VIS : MED_ISO;
+}
 
 static int pitch_for(int ni) { return 32 * ((ni + 31) / 32 + 2); }
 #define XOFF 29
@@ -398,8 +591,10 @@ static int pitch_for(int ni) { return 32 * ((ni + 31) / 32 + 2); }
 extern "C" size_t cgfd_device_bytes(const cgfd_problem_t *p)
 {
   size_t vol = (size_t)pitch_for(p->ni) * p->ny * p->nz;
-  size_t b = (4 * 9 + 10 + 3) * vol * sizeof(float);
-  if (p->free_top) b += 3 * (size_t)p->nx * p->ny * 9 * sizeof(float);
+  int med = medium_of(p->medium_type);
+  int nmw = med == MED_VIS ? p->nmaxwell : 0;
+  size_t b = (size_t)(4 * (9 + 6 * nmw) + 10 + med_ncomp(med, nmw)) * vol * sizeof(float);
+  if (p->free_top) b += (med == MED_VIS ? 4 : 3) * (size_t)p->nx * p->ny * 9 * sizeof(float);
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {
       const cgfd_pml_face_t *f = &p->pml[d][s];
@@ -413,11 +608,31 @@ extern "C" size_t cgfd_device_bytes(const cgfd_problem_t *p)
 
 static int validate(const cgfd_problem_t *p)
 {
-  if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO)
-    return set_err(CGFD_EINVAL, "medium_type %d not supported by this build",
-                   p->medium_type);
-  if (p->ncmp != 9 || p->nlevel != 4)
-    return set_err(CGFD_EINVAL, "ncmp=%d nlevel=%d (need 9, 4)", p->ncmp, p->nlevel);
+  if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO &&
+      p->medium_type != CGFD_MEDIUM_ELASTIC_VTI &&
+      p->medium_type != CGFD_MEDIUM_VISCOELASTIC_ISO)
+    return set_err(CGFD_EINVAL, "medium_type %d not supported (elastic_iso 2, "
+                   "elastic_vti 3, viscoelastic_iso 5)", p->medium_type);
+  int ncmp_want = 9;
+  if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO) {
+    if (p->nmaxwell < 1 || p->nmaxwell > CGFD_VIS_NMW_MAX)
+      return set_err(CGFD_EINVAL, "nmaxwell=%d: the GPU visco-elastic path holds "
+                     "1..%d Maxwell bodies", p->nmaxwell, CGFD_VIS_NMW_MAX);
+    if (!p->wl || !p->lambda || !p->mu)
+      return set_err(CGFD_EINVAL, "visco-elastic medium arrays missing");
+    for (int n = 0; n < p->nmaxwell; n++)
+      if (!p->Ylam[n] || !p->Ymu[n])
+        return set_err(CGFD_EINVAL, "Ylam/Ymu[%d] missing", n);
+    if (p->free_top && (!p->x3d || !p->y3d || !p->z3d))
+      return set_err(CGFD_EINVAL, "visco-elastic free surface needs x3d/y3d/z3d");
+    ncmp_want += 6 * p->nmaxwell;
+  }
+  if (p->medium_type == CGFD_MEDIUM_ELASTIC_VTI &&
+      (!p->c11 || !p->c13 || !p->c33 || !p->c55 || !p->c66))
+    return set_err(CGFD_EINVAL, "VTI medium arrays missing");
+  if (p->ncmp != ncmp_want || p->nlevel != 4)
+    return set_err(CGFD_EINVAL, "ncmp=%d nlevel=%d (need %d, 4)", p->ncmp,
+                   p->nlevel, ncmp_want);
   if (p->nx != p->ni + 6 || p->ny != p->nj + 6 || p->nz != p->nk + 6 ||
       p->ni1 != 3 || p->nj1 != 3 || p->nk1 != 3 || p->ni2 != p->ni + 2 ||
       p->nj2 != p->nj + 2 || p->nk2 != p->nk + 2)
@@ -426,8 +641,10 @@ static int validate(const cgfd_problem_t *p)
     return set_err(CGFD_EINVAL, "grid too small (ni,nj,nk >= 8 required)");
   if (p->src_n > 0 && p->src_n_surface_force > 0)
     return set_err(CGFD_EINVAL, "surface force sources are not supported");
-  if (!p->jac || !p->xi_x || !p->slw || !p->lambda || !p->mu || !p->wav)
+  if (!p->jac || !p->xi_x || !p->slw || !p->wav)
     return set_err(CGFD_EINVAL, "missing input array");
+  if (p->medium_type != CGFD_MEDIUM_ELASTIC_VTI && (!p->lambda || !p->mu))
+    return set_err(CGFD_EINVAL, "missing lambda/mu");
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {
       const cgfd_pml_face_t *f = &p->pml[d][s];
@@ -533,34 +750,48 @@ static int make_tmap(cgfd_solver_t *s)
     fn = (encode_tiled_fn)ptr;
   }
   const DevGrid &g = s->g;
+  StageMaps &M = s->maps;
+  /* components 0..8 of every level; the level stride spans all ncmp */
   cuuint64_t dims[5] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 9, 4};
   cuuint64_t strides[4] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4,
-                           (cuuint64_t)g.vol * 4, (cuuint64_t)g.vol * 9 * 4};
+                           (cuuint64_t)g.vol * 4, (cuuint64_t)g.vol * s->ncmp * 4};
   cuuint32_t box[5] = {s2::BW, s2::BH, 1, 9, 1};
   cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-  CUresult r = fn(&s->tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
+  CUresult r = fn(&M.wav, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   /* per-point tiles (no halo) for L2 prefetch of the streams */
   cuuint32_t boxp[5] = {s2::TX, s2::TY, 1, 9, 1};
-  r = fn(&s->tmap_pt, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
+  r = fn(&M.pt, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
          boxp, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (points) failed (%d)", (int)r);
   cuuint64_t dm[4] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 10};
   cuuint64_t sm_[3] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4, (cuuint64_t)g.vol * 4};
   cuuint32_t bm[4] = {s2::TX, s2::TY, 1, 10};
-  r = fn(&s->tmap_met, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->metric, dm, sm_, bm, estr,
+  r = fn(&M.met, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->metric, dm, sm_, bm, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (metrics) failed (%d)", (int)r);
-  dm[3] = 3;
-  bm[3] = 3;
-  r = fn(&s->tmap_med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->media, dm, sm_, bm, estr,
+  dm[3] = (cuuint64_t)s->nmed;
+  bm[3] = (cuuint32_t)s->nmed;
+  r = fn(&M.med, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->media, dm, sm_, bm, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (media) failed (%d)", (int)r);
+  /* memory variables (components 9 .. ncmp-1) of the visco-elastic medium */
+  M.j = M.pt;
+  if (s->ncmp > 9) {
+    cuuint64_t dj[5] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz,
+                        (cuuint64_t)s->ncmp, 4};
+    cuuint32_t bj[5] = {s2::TX, s2::TY, 1, (cuuint32_t)(s->ncmp - 9), 1};
+    r = fn(&M.j, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dj, strides, bj, estr,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+      return set_err(CGFD_ECUDA, "tensor map (memory variables) failed (%d)", (int)r);
+  }
   return 0;
 }
 
@@ -593,6 +824,9 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   if (rc) return rc;
   cgfd_solver_t *s = new cgfd_solver_t();
   s->p = p;
+  s->med = medium_of(p->medium_type);
+  s->ncmp = p->ncmp;
+  s->nmed = med_ncomp(s->med, s->med == MED_VIS ? p->nmaxwell : 0);
   DevGrid &g = s->g;
   g.ni = p->ni; g.nj = p->nj; g.nk = p->nk;
   g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
@@ -607,7 +841,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   TRYC(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   TRYC(cudaEventCreate(&s->ev0));
   TRYC(cudaEventCreate(&s->ev1));
-  size_t vol = g.vol, L = level_floats(g);
+  size_t vol = g.vol, L = level_floats(s);
   size_t hvol = (size_t)p->nx * p->ny * p->nz;
   cudaStream_t st = s->stream;
   /* wavefield: level 0 of the input copied into all four levels, so that
@@ -615,7 +849,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
    * reference either: rhs ghosts are zero) */
   TRY(dalloc(s, &s->wav, 4 * L));
   TRYC(cudaMemsetAsync(s->wav, 0, L * sizeof(float), st));
-  for (int c = 0; c < 9; c++)
+  for (int c = 0; c < s->ncmp; c++)
     TRYC(upload_volume(s, s->wav + c * vol, p->wav + (size_t)c * hvol));
   for (int l = 1; l < 4; l++)
     TRYC(cudaMemcpyAsync(s->wav + l * L, s->wav, L * sizeof(float),
@@ -629,11 +863,25 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
                          p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
   for (int m = 0; m < 10; m++)
     TRYC(upload_volume(s, s->metric + m * vol, mh[m]));
-  TRY(dalloc(s, &s->media, 3 * vol));
-  TRYC(cudaMemsetAsync(s->media, 0, 3 * vol * sizeof(float), st));
-  const float *md[3] = {p->slw, p->lambda, p->mu};
-  for (int m = 0; m < 3; m++)
-    TRYC(upload_volume(s, s->media + m * vol, md[m]));
+  TRY(dalloc(s, &s->media, (size_t)s->nmed * vol));
+  TRYC(cudaMemsetAsync(s->media, 0, (size_t)s->nmed * vol * sizeof(float), st));
+  {
+    const float *md[3 + 2 * CGFD_VIS_NMW_MAX];
+    int nm = 0;
+    md[nm++] = p->slw;
+    if (s->med == MED_VTI) {
+      md[nm++] = p->c11; md[nm++] = p->c13; md[nm++] = p->c33;
+      md[nm++] = p->c55; md[nm++] = p->c66;
+    } else {
+      md[nm++] = p->lambda; md[nm++] = p->mu;
+      if (s->med == MED_VIS) {
+        for (int n = 0; n < p->nmaxwell; n++) md[nm++] = p->Ylam[n];
+        for (int n = 0; n < p->nmaxwell; n++) md[nm++] = p->Ymu[n];
+      }
+    }
+    for (int m = 0; m < nm; m++)
+      TRYC(upload_volume(s, s->media + m * vol, md[m]));
+  }
   /* PML faces */
   int nf = 0;
   for (int d = 0; d < 3; d++)
@@ -658,6 +906,9 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
       TRYC(cudaMemcpyAsync(coef + np, f->B, np * 4, cudaMemcpyHostToDevice, st));
       TRYC(cudaMemcpyAsync(coef + 2 * np, f->D, np * 4, cudaMemcpyHostToDevice, st));
       F.A = coef; F.B = coef + np; F.D = coef + 2 * np;
+      /* device: the 9 components the PML updates; the host layout holds
+       * ncmp per level (forward/bdry_t.c:300-306), its memory-variable
+       * components never change */
       size_t al = 9 * (size_t)F.avol;
       TRY(dalloc(s, &s->aux[fi], 4 * al));
       TRYC(cudaMemcpyAsync(s->aux[fi], f->aux, al * sizeof(float),
@@ -671,15 +922,36 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   /* free surface matrices, computed on the device */
   if (p->free_top) {
     size_t n2 = (size_t)g.nx * g.ny * 9;
-    TRY(dalloc(s, &s->mats, 3 * n2));
-    TRYC(cudaMemsetAsync(s->mats, 0, 3 * n2 * sizeof(float), st));
+    int nmat = s->med == MED_VIS ? 4 : 3;
+    TRY(dalloc(s, &s->mats, nmat * n2));
+    TRYC(cudaMemsetAsync(s->mats, 0, nmat * n2 * sizeof(float), st));
     dim3 b(32, 8), gr((g.ni + 31) / 32, (g.nj + 7) / 8);
     const float *M = s->metric;
-    k_dvh2dvz_iso<<<gr, b, 0, st>>>(g, M + vol, M + 2 * vol, M + 3 * vol,
-                                    M + 4 * vol, M + 5 * vol, M + 6 * vol,
-                                    M + 7 * vol, M + 8 * vol, M + 9 * vol,
-                                    s->media + vol, s->media + 2 * vol,
-                                    s->mats, s->mats + n2, s->mats + 2 * n2);
+    if (s->med == MED_ISO) {
+      k_dvh2dvz_iso<<<gr, b, 0, st>>>(g, M + vol, M + 2 * vol, M + 3 * vol,
+                                      M + 4 * vol, M + 5 * vol, M + 6 * vol,
+                                      M + 7 * vol, M + 8 * vol, M + 9 * vol,
+                                      s->media + vol, s->media + 2 * vol,
+                                      s->mats, s->mats + n2, s->mats + 2 * n2);
+    } else if (s->med == MED_VTI) {
+      k_dvh2dvz_vti<<<gr, b, 0, st>>>(g, M, s->media, s->mats, s->mats + n2);
+    } else {
+      /* the surface plane of the grid coordinates (rows j-3..j+3 are read) */
+      size_t s2n = (size_t)g.nx * g.ny;
+      size_t off = (size_t)p->nk2 * s2n;
+      float *xyz = nullptr;
+      TRYC(cudaMalloc((void **)&xyz, 3 * s2n * sizeof(float)));
+      cudaError_t e1 = cudaMemcpyAsync(xyz, p->x3d + off, s2n * 4, cudaMemcpyHostToDevice, st);
+      cudaError_t e2 = cudaMemcpyAsync(xyz + s2n, p->y3d + off, s2n * 4, cudaMemcpyHostToDevice, st);
+      cudaError_t e3 = cudaMemcpyAsync(xyz + 2 * s2n, p->z3d + off, s2n * 4, cudaMemcpyHostToDevice, st);
+      if (e1 == cudaSuccess && e2 == cudaSuccess && e3 == cudaSuccess)
+        k_dvh2dvz_vis<<<gr, b, 0, st>>>(g, M, s->media, xyz, xyz + s2n, xyz + 2 * s2n,
+                                        s->mats, s->mats + n2, s->mats + 3 * n2);
+      cudaError_t e4 = cudaStreamSynchronize(st);
+      cudaFree(xyz);
+      s->h2d_bytes += 3 * s2n * 4;
+      TRYC(e1); TRYC(e2); TRYC(e3); TRYC(e4);
+    }
     TRYC(cudaGetLastError());
   }
   /* sources */
@@ -742,7 +1014,9 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   TRY(dalloc(s, &s->d_err, 1));
   TRYC(cudaMemsetAsync(s->d_err, 0, 4, st));
   s->kernel = 2;
-  if (const char *e = getenv("CGFD_STAGE_KERNEL")) s->kernel = atoi(e) == 1 ? 1 : 2;
+  /* the direct-load A/B kernel (cgfd_stage.cuh) covers isotropic media only */
+  if (const char *e = getenv("CGFD_STAGE_KERNEL"))
+    s->kernel = (atoi(e) == 1 && s->med == MED_ISO) ? 1 : 2;
   {
     int tiles = ((g.ni + s2::TX - 1) / s2::TX) * ((g.nj + s2::TY - 1) / s2::TY);
     int want = 8 * 152;                     /* about eight waves of CTAs */
@@ -762,7 +1036,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
 static void stage_levels(cgfd_solver_t *s, int istage, float **cur, float **pre,
                          float **tmp_out, float **end)
 {
-  size_t L = level_floats(s->g);
+  size_t L = level_floats(s);
   float *base = s->wav;
   int tA = 1, tB = 2;
   *pre = base + s->pre_lev * L;
@@ -773,38 +1047,39 @@ static void stage_levels(cgfd_solver_t *s, int istage, float **cur, float **pre,
   else { *cur = base + tA * L; *tmp_out = nullptr; }
 }
 
-typedef void (*stage_fn)(const StageArgs);
-
-template <int BX, int BY, int BZ, int KIND>
-static void launch_one(cgfd_solver_t *s, cudaStream_t st, const StageArgs &a)
+/* direct-load A/B kernel (isotropic media only) */
+template <int BX, int BY, int BZ>
+static void launch_v1(cgfd_solver_t *s, int kind, cudaStream_t st, const StageArgs &a)
 {
-  if (s->kernel == 1) {
-    dim3 b(V1_TX, V1_TY);
-    dim3 gr((s->g.ni + V1_TX - 1) / V1_TX, (s->g.nj + V1_TY - 1) / V1_TY,
-            (s->g.nk + V1_KCHUNK - 1) / V1_KCHUNK);
-    k_stage<BX, BY, BZ, KIND><<<gr, b, 0, st>>>(a);
-  } else {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(s3::k_stage3<BX, BY, BZ, KIND>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, s3::SMEM_BYTES);
-      attr_set = true;
-    }
-    dim3 b(s3::NTHREADS);
-    dim3 gr((s->g.ni + s2::TX - 1) / s2::TX, (s->g.nj + s2::TY - 1) / s2::TY,
-            (s->g.nk + s->kchunk - 1) / s->kchunk);
-    s3::k_stage3<BX, BY, BZ, KIND><<<gr, b, s3::SMEM_BYTES, st>>>(
-        a, s->tmap, s->tmap_met, s->tmap_med, s->tmap_pt);
-  }
+  dim3 b(V1_TX, V1_TY);
+  dim3 gr((s->g.ni + V1_TX - 1) / V1_TX, (s->g.nj + V1_TY - 1) / V1_TY,
+          (s->g.nk + V1_KCHUNK - 1) / V1_KCHUNK);
+  if (kind == 0) k_stage<BX, BY, BZ, 0><<<gr, b, 0, st>>>(a);
+  else if (kind == 1) k_stage<BX, BY, BZ, 1><<<gr, b, 0, st>>>(a);
+  else k_stage<BX, BY, BZ, 2><<<gr, b, 0, st>>>(a);
 }
 
-template <int DIM, int B>
-static void launch_pml(int kind, int f, long long n, cudaStream_t st, const StageArgs &a)
+static void launch_stage(cgfd_solver_t *s, int code, int kind, cudaStream_t st,
+                         const StageArgs &a)
 {
-  dim3 b(256), gr((unsigned)((n + 255) / 256));
-  if (kind == 0) k_pml_face<DIM, B, 0><<<gr, b, 0, st>>>(a, f);
-  else if (kind == 1) k_pml_face<DIM, B, 1><<<gr, b, 0, st>>>(a, f);
-  else k_pml_face<DIM, B, 2><<<gr, b, 0, st>>>(a, f);
+  if (s->kernel == 1) {
+    switch (code) {
+      case 0: launch_v1<0, 0, 0>(s, kind, st, a); break;
+      case 1: launch_v1<0, 0, 1>(s, kind, st, a); break;
+      case 2: launch_v1<0, 1, 0>(s, kind, st, a); break;
+      case 3: launch_v1<0, 1, 1>(s, kind, st, a); break;
+      case 4: launch_v1<1, 0, 0>(s, kind, st, a); break;
+      case 5: launch_v1<1, 0, 1>(s, kind, st, a); break;
+      case 6: launch_v1<1, 1, 0>(s, kind, st, a); break;
+      default: launch_v1<1, 1, 1>(s, kind, st, a); break;
+    }
+    return;
+  }
+  dim3 gr((s->g.ni + s2::TX - 1) / s2::TX, (s->g.nj + s2::TY - 1) / s2::TY,
+          (s->g.nk + s->kchunk - 1) / s->kchunk);
+  if (s->med == MED_VTI) cgfd_launch_stage_vti(code, kind, gr, st, a, s->maps);
+  else if (s->med == MED_VIS) cgfd_launch_stage_vis(code, kind, gr, st, a, s->maps);
+  else cgfd_launch_stage_iso(code, kind, gr, st, a, s->maps);
 }
 
 /* CFS-PML corrections, faces in the reference order (after the stage kernel) */
@@ -815,18 +1090,10 @@ static void launch_pml_faces(cgfd_solver_t *s, int kind, int bx, int by, int bz,
     const DevFace &F = s->face[f];
     if (!F.on) continue;
     int dim = F.dim, b = dim == 0 ? bx : (dim == 1 ? by : bz);
-    if (dim == 0) { if (b) launch_pml<0, 1>(kind, f, F.avol, st, a); else launch_pml<0, 0>(kind, f, F.avol, st, a); }
-    else if (dim == 1) { if (b) launch_pml<1, 1>(kind, f, F.avol, st, a); else launch_pml<1, 0>(kind, f, F.avol, st, a); }
-    else { if (b) launch_pml<2, 1>(kind, f, F.avol, st, a); else launch_pml<2, 0>(kind, f, F.avol, st, a); }
+    if (s->med == MED_VTI) cgfd_launch_pml_vti(dim, b, kind, f, F.avol, st, a);
+    else if (s->med == MED_VIS) cgfd_launch_pml_vis(dim, b, kind, f, F.avol, st, a);
+    else cgfd_launch_pml_iso(dim, b, kind, f, F.avol, st, a);
   }
-}
-
-template <int BX, int BY, int BZ>
-static void launch_stage(cgfd_solver_t *s, int kind, cudaStream_t st, const StageArgs &a)
-{
-  if (kind == 0) launch_one<BX, BY, BZ, 0>(s, st, a);
-  else if (kind == 1) launch_one<BX, BY, BZ, 1>(s, st, a);
-  else launch_one<BX, BY, BZ, 2>(s, st, a);
 }
 
 static const int PAIR_FLAGS[8][3] = {{0, 0, 0}, {1, 1, 0}, {1, 1, 1}, {0, 0, 1},
@@ -846,6 +1113,10 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   a.etx = M + 4 * vol; a.ety = M + 5 * vol; a.etz = M + 6 * vol;
   a.ztx = M + 7 * vol; a.zty = M + 8 * vol; a.ztz = M + 9 * vol;
   a.slw = s->media; a.lam = s->media + vol; a.mu = s->media + 2 * vol;
+  a.med = s->media;
+  a.ncmp = s->ncmp;
+  a.nmw = s->med == MED_VIS ? p->nmaxwell : 0;
+  for (int n = 0; n < a.nmw; n++) a.wl[n] = p->wl[n];
   float *cur, *pre, *tmp, *end;
   stage_levels(s, istage, &cur, &pre, &tmp, &end);
   a.cur = cur; a.pre = pre; a.tmp_out = tmp; a.end = end;
@@ -869,6 +1140,7 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   if (p->free_top) {
     size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
     a.mVx = s->mats; a.mVy = s->mats + n2; a.mF = s->mats + 2 * n2;
+    a.mD = s->med == MED_VIS ? s->mats + 3 * n2 : nullptr;
   }
   if (p->src_n > 0) {
     a.src_n = p->src_n;
@@ -889,7 +1161,7 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   a.istage = istage;
   a.err = s->d_err;
   a.kchunk = s->kchunk;
-  size_t L = level_floats(s->g);
+  size_t L = level_floats(s);
   a.cur_level = (int)((cur - s->wav) / (long long)L);
   a.pre_level = (int)((pre - s->wav) / (long long)L);
   a.end_level = (int)((end - s->wav) / (long long)L);
@@ -910,27 +1182,24 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
     int kind = is == 0 ? 0 : (is < 3 ? 1 : 2);
     int code = bx * 4 + by * 2 + bz;
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
-    switch (code) {
-      case 0: launch_stage<0, 0, 0>(s, kind, st, a); break;
-      case 1: launch_stage<0, 0, 1>(s, kind, st, a); break;
-      case 2: launch_stage<0, 1, 0>(s, kind, st, a); break;
-      case 3: launch_stage<0, 1, 1>(s, kind, st, a); break;
-      case 4: launch_stage<1, 0, 0>(s, kind, st, a); break;
-      case 5: launch_stage<1, 0, 1>(s, kind, st, a); break;
-      case 6: launch_stage<1, 1, 0>(s, kind, st, a); break;
-      default: launch_stage<1, 1, 1>(s, kind, st, a); break;
-    }
+    launch_stage(s, code, kind, st, a);
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
     if (s->kernel == 2) launch_pml_faces(s, kind, bx, by, bz, st, a);
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
-  size_t L = level_floats(s->g);
+  size_t L = level_floats(s);
+  if (s->med == MED_VIS && p->free_top) {
+    /* surface stress rotation after the last stage (drv_rk_curv_col.c:440-445) */
+    dim3 b(32, 8), gr((s->g.ni + 31) / 32, (s->g.nj + 7) / 8);
+    size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
+    k_vis_free<<<gr, b, 0, st>>>(s->g, s->wav + s->end_lev * L, s->mats + 3 * n2);
+  }
   if (s->pg) {
     dim3 b(32, 8), gr((s->g.ni + 31) / 32, (s->g.nj + 7) / 8);
     k_pg<<<gr, b, 0, st>>>(s->g, s->wav + s->end_lev * L, s->wav + s->pre_lev * L,
                            s->pg, s->dis, p->dt);
   }
-  k_recv<<<1, 256, 0, st>>>(s->wav + s->end_lev * L, s->g.vol, p->ncmp,
+  k_recv<<<1, 256, 0, st>>>(s->wav + s->end_lev * L, s->g.vol, s->ncmp,
                             p->recv_n, p->recv_ncmp, p->recv_max_nt, s->recv_dijk,
                             s->recv_idx, s->recv_seismo, p->line_n, p->line_max_nt,
                             s->line_iptr, s->line_seismo, s->d_it);
@@ -979,7 +1248,7 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
   s->n_pml = s->kernel == 2 ? 4 * nfaces * nsteps : 0;
-  s->n_other = nsteps * (s->pg ? 2 : 1);
+  s->n_other = nsteps * (1 + (s->pg ? 1 : 0) + (s->med == MED_VIS && s->p->free_top ? 1 : 0));
   int herr = 0;
   CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));
   if (herr) return set_err(CGFD_ECUDA, "device wait timed out (code %d)", herr);
@@ -1016,20 +1285,26 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
 {
   if (!s) return set_err(CGFD_EINVAL, "null solver");
   const cgfd_problem_t *p = s->p;
-  size_t L = level_floats(s->g);
+  size_t L = level_floats(s);
   int host_lev = (s->step % 2 == 1) ? 3 : 0;
   size_t hvol = (size_t)p->nx * p->ny * p->nz;
-  for (int c = 0; c < 9; c++)
-    CK(download_volume(s, p->wav + (size_t)host_lev * 9 * hvol + c * hvol,
+  for (int c = 0; c < s->ncmp; c++)
+    CK(download_volume(s, p->wav + (size_t)host_lev * s->ncmp * hvol + c * hvol,
                        s->wav + s->pre_lev * L + c * s->g.vol));
   for (int d = 0; d < 3; d++)
     for (int sd = 0; sd < 2; sd++) {
       int f = d * 2 + sd;
       if (!s->face[f].on) continue;
-      size_t al = 9 * (size_t)s->face[f].avol;
-      CK(cudaMemcpyAsync(p->pml[d][sd].aux + host_lev * al, s->aux[f] + s->pre_lev * al,
-                         al * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+      size_t av = (size_t)s->face[f].avol;
+      size_t al = 9 * av;
+      float *hl = p->pml[d][sd].aux + (size_t)host_lev * s->ncmp * av;
+      CK(cudaMemcpyAsync(hl, s->aux[f] + s->pre_lev * al, al * sizeof(float),
+                         cudaMemcpyDeviceToHost, s->stream));
       s->d2h_bytes += al * sizeof(float);
+      /* memory-variable components of the aux: never updated by the PML,
+       * every level keeps the input values (rhs stays 0 in the reference) */
+      if (s->ncmp > 9 && host_lev != 0)
+        memcpy(hl + al, p->pml[d][sd].aux + al, (size_t)(s->ncmp - 9) * av * sizeof(float));
     }
   if (p->recv_n > 0) {
     size_t nb = (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt * 4;
@@ -1059,6 +1334,16 @@ extern "C" int cgfd_solver_fetch_surface_matrices(cgfd_solver_t *s, float *mVx,
   return 0;
 }
 
+extern "C" int cgfd_solver_fetch_surface_rotation(cgfd_solver_t *s, float *mD)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (!s->mats || s->med != MED_VIS)
+    return set_err(CGFD_EINVAL, "no visco-elastic free surface");
+  size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
+  CK(cudaMemcpy(mD, s->mats + 3 * n2, n2 * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 extern "C" int cgfd_solver_fetch_pg(cgfd_solver_t *s, float *pg)
 {
   if (!s) return set_err(CGFD_EINVAL, "null solver");
@@ -1073,8 +1358,8 @@ extern "C" int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w)
 {
   if (!s) return set_err(CGFD_EINVAL, "null solver");
   size_t hvol = (size_t)s->g.nx * s->g.ny * s->g.nz;
-  size_t L = level_floats(s->g);
-  for (int c = 0; c < 9; c++)
+  size_t L = level_floats(s);
+  for (int c = 0; c < s->ncmp; c++)
     CK(download_volume(s, w + c * hvol, s->wav + s->pre_lev * L + c * s->g.vol));
   CK(cudaStreamSynchronize(s->stream));
   return 0;
@@ -1083,7 +1368,7 @@ extern "C" int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w)
 extern "C" int cgfd_solver_check_finite(cgfd_solver_t *s)
 {
   if (!s) return set_err(CGFD_EINVAL, "null solver");
-  size_t L = level_floats(s->g);
+  size_t L = level_floats(s);
   CK(cudaMemsetAsync(s->d_flag, 0, 4, s->stream));
   k_nonfinite<<<152 * 4, 256, 0, s->stream>>>(s->wav + s->pre_lev * L, L, s->d_flag);
   CK(cudaGetLastError());

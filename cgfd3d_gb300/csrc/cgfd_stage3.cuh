@@ -27,10 +27,20 @@
  * CFS-PML terms, which the face kernels of cgfd_pml.cuh add afterwards
  * (reference: forward/sv_curv_col_el_iso.c:208-634,
  * forward/sv_curv_col_el.c:30-479, forward/drv_rk_curv_col.c:292-446).
+ *
+ * MED selects the medium (cgfd_media.cuh).  VTI changes Hooke's law only
+ * (forward/sv_curv_col_el_vti.c:200-590).  The GMB visco-elastic medium
+ * (forward/sv_curv_col_vis_iso.c:165-347) adds, per point, the memory
+ * variables J (6 per Maxwell body): their current values and the
+ * coefficients Ylam/Ymu arrive through the stream slot, and the stage
+ *   hJ_n = wl_n (EV(hT) - J_n),  hT -= lam sum Ylam_n tr(J_n) + 2 mu sum Ymu_n J_n
+ * is applied before the sources, as in the reference (EV: strain rates
+ * implied by hT).  J's RK combine reads pre/end directly (coalesced rows).
  */
 #ifndef CGFD_STAGE3_CUH
 #define CGFD_STAGE3_CUH
 
+#include "cgfd_media.cuh"
 #include "cgfd_stage2.cuh"
 
 namespace s3 {
@@ -42,12 +52,22 @@ constexpr int NS = 2;                 /* stream ring */
 constexpr int NCW = TY;               /* consumer warps (one per tile row) */
 constexpr int NTHREADS = (NCW + 1) * 32;
 constexpr int PTS = TX * TY;
-constexpr int S_MET = 0;              /* 10 components */
-constexpr int S_MED = 10 * PTS;       /* 3 */
-constexpr int S_PRE = 13 * PTS;       /* 9 */
-constexpr int S_END = 22 * PTS;       /* 9 */
-constexpr int SLOT = 31 * PTS;        /* floats per stream slot */
-constexpr int SMEM_BYTES = (NB * PLANE + NS * SLOT) * 4;
+
+/* stream-slot layout (floats) for a medium: metrics (jac + 9), media,
+ * current memory variables (visco), pre, end */
+template <int MED>
+struct Slot {
+  static constexpr int NMED = MED == MED_VTI ? 6
+                            : (MED == MED_VIS ? 3 + 2 * CGFD_VIS_NMW_MAX : 3);
+  static constexpr int NJ = MED == MED_VIS ? 6 * CGFD_VIS_NMW_MAX : 0;
+  static constexpr int S_MET = 0;
+  static constexpr int S_MED = 10 * PTS;
+  static constexpr int S_JC = S_MED + NMED * PTS;
+  static constexpr int S_PRE = S_JC + NJ * PTS;
+  static constexpr int S_END = S_PRE + 9 * PTS;
+  static constexpr int SLOT = S_END + 9 * PTS;
+  static constexpr int SMEM_BYTES = (NB * PLANE + NS * SLOT) * 4;
+};
 
 /* bounded wait; `err` records a timeout */
 __device__ __forceinline__ void wait_full(uint64_t *bar, uint32_t parity, int *err)
@@ -55,14 +75,18 @@ __device__ __forceinline__ void wait_full(uint64_t *bar, uint32_t parity, int *e
   mbar_wait(bar, parity, err);
 }
 
-template <int BX, int BY, int BZ, int KIND>
+template <int BX, int BY, int BZ, int KIND, int MED>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_stage3(const __grid_constant__ StageArgs a,
              const __grid_constant__ CUtensorMap tmap,
              const __grid_constant__ CUtensorMap tmap_met,
              const __grid_constant__ CUtensorMap tmap_med,
-             const __grid_constant__ CUtensorMap tmap_pt)
+             const __grid_constant__ CUtensorMap tmap_pt,
+             const __grid_constant__ CUtensorMap tmap_j)
 {
+  using L = Slot<MED>;
+  constexpr int S_MET = L::S_MET, S_MED = L::S_MED, S_JC = L::S_JC,
+                S_PRE = L::S_PRE, S_END = L::S_END, SLOT = L::SLOT;
   extern __shared__ __align__(128) float sm[];
   __shared__ __align__(8) uint64_t full_w[NB], empty_w[NB], full_s[NS], empty_s[NS];
   float *ring = sm;
@@ -95,8 +119,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int bx0 = i0 + g.xoff - XL;  /* 16-byte aligned box origin */
     const int by0 = j0 - YL;
     const int xs = i0 + g.xoff;        /* stream tiles: no halo */
-    constexpr uint32_t slot_bytes =
-        (13 + (KIND == 1 ? 9 : 0) + (KIND >= 1 ? 9 : 0)) * PTS * 4;
+    const int nmed = med_ncomp(MED, a.nmw);
+    const uint32_t slot_bytes =
+        (10 + nmed + (MED == MED_VIS ? 6 * a.nmw : 0) + (KIND == 1 ? 9 : 0) +
+         (KIND >= 1 ? 9 : 0)) * PTS * 4;
     auto issue_wav = [&](int rel) {
       int b = rel % NB;
       if (rel >= NB) {
@@ -118,6 +144,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_expect_tx(&full_s[b], slot_bytes);
       tma_load_4d(dst + S_MET, &tmap_met, xs, j0, k, 0, &full_s[b]);
       tma_load_4d(dst + S_MED, &tmap_med, xs, j0, k, 0, &full_s[b]);
+      if (MED == MED_VIS)
+        tma_load_5d(dst + S_JC, &tmap_j, xs, j0, k, 9, a.cur_level, &full_s[b]);
       if (KIND == 1) tma_load_5d(dst + S_PRE, &tmap_pt, xs, j0, k, 0, a.pre_level, &full_s[b]);
       if (KIND >= 1) tma_load_5d(dst + S_END, &tmap_pt, xs, j0, k, 0, a.end_level, &full_s[b]);
     };
@@ -175,9 +203,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       float xix = ms[1 * PTS], xiy = ms[2 * PTS], xiz = ms[3 * PTS];
       float etx = ms[4 * PTS], ety = ms[5 * PTS], etz = ms[6 * PTS];
       float ztx = ms[7 * PTS], zty = ms[8 * PTS], ztz = ms[9 * PTS];
-      const float *md = st + S_MED + sp;
-      float slw = md[0], lam = md[PTS], mu = md[2 * PTS];
-      float l2m = lam + 2.0f * mu;
+      const MedPt m = med_from<MED, false>(st + S_MED + sp, PTS);
+      const float slw = m.slw;
       float r[9];
 #define DX(c) sdop<BX>(cen + soff(c, row, col), 1)
 #define DY(c) sdop<BY>(cen + soff(c, row, col), BW)
@@ -241,8 +268,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           DzVy = DZ(C_VY);
           DzVz = DZ(C_VZ);
         }
-        hooke_iso(lam, mu, l2m, xix, xiy, xiz, etx, ety, etz, ztx, zty, ztz,
-                  DxVx, DxVy, DxVz, DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, r);
+        hooke9<MED>(m, xix, xiy, xiz, etx, ety, etz, ztx, zty, ztz, DxVx, DxVy,
+                    DxVz, DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, r);
       }
 #undef DX
 #undef DY
@@ -251,6 +278,38 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         r[C_VX] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 0);
         r[C_VY] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 1);
         r[C_VZ] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 2);
+      }
+
+      /* GMB attenuation (forward/sv_curv_col_vis_iso.c:250-347) */
+      float hJ[MED == MED_VIS ? 6 * CGFD_VIS_NMW_MAX : 1];
+      if (MED == MED_VIS) {
+        float ev[6];
+        vis_strain_rate(m.lam, m.mu, r, ev);
+        float sl_ = 0.f, sm_[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const int nyl = 3, nym = 3 + a.nmw;
+#pragma unroll
+        for (int n = 0; n < CGFD_VIS_NMW_MAX; n++) {
+          if (n < a.nmw) {
+            const float *jc = st + S_JC + 6 * n * PTS + sp;
+            const float yl = st[S_MED + (nyl + n) * PTS + sp];
+            const float ym = st[S_MED + (nym + n) * PTS + sp];
+            float J[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+              J[c] = jc[c * PTS];
+              hJ[6 * n + c] = a.wl[n] * (ev[c] - J[c]);
+              sm_[c] += ym * J[c];
+            }
+            sl_ += yl * (J[0] + J[1] + J[2]);
+          }
+        }
+        const float lsl = m.lam * sl_, mu2 = 2.0f * m.mu;
+        r[C_TXX] -= lsl + mu2 * sm_[0];
+        r[C_TYY] -= lsl + mu2 * sm_[1];
+        r[C_TZZ] -= lsl + mu2 * sm_[2];
+        r[C_TYZ] -= mu2 * sm_[3];
+        r[C_TXZ] -= mu2 * sm_[4];
+        r[C_TXY] -= mu2 * sm_[5];
       }
 
       if (src_e0 < src_e1) {
@@ -290,6 +349,36 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           a.end[x] = st[S_END + c * PTS + sp] + a.cb * r[c];
         } else {
           a.end[x] = st[S_END + c * PTS + sp] + a.cb * r[c];
+        }
+      }
+      if (MED == MED_VIS) {
+        /* memory variables: RK combine (pre/end read directly) */
+#pragma unroll
+        for (int n = 0; n < CGFD_VIS_NMW_MAX; n++) {
+          if (n < a.nmw) {
+            float pv[6], ev[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+              long long x = (long long)(9 + 6 * n + c) * vol + q;
+              if (KIND == 0) pv[c] = st[S_JC + (6 * n + c) * PTS + sp];
+              else if (KIND == 1) pv[c] = __ldg(a.pre + x);
+              if (KIND >= 1) ev[c] = a.end[x];
+            }
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+              long long x = (long long)(9 + 6 * n + c) * vol + q;
+              float h = hJ[6 * n + c];
+              if (KIND == 0) {
+                a.tmp_out[x] = pv[c] + a.ca * h;
+                a.end[x] = pv[c] + a.cb * h;
+              } else if (KIND == 1) {
+                a.tmp_out[x] = pv[c] + a.ca * h;
+                a.end[x] = ev[c] + a.cb * h;
+              } else {
+                a.end[x] = ev[c] + a.cb * h;
+              }
+            }
+          }
         }
       }
     }

@@ -24,8 +24,8 @@
  *
  * Errors print the library's message and call MPI_Abort when MPI is linked
  * (exit(1) otherwise), as the reference does.  Unsupported configurations
- * (surface force sources, dd sources, ablexp, media other than isotropic
- * elastic) are reported the same way instead of being ignored.
+ * (surface force sources, dd sources, ablexp, full anisotropy, Graves Q)
+ * are reported the same way instead of being ignored.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -35,6 +35,7 @@
 
 #ifdef CGFD_DROPIN_REFERENCE_HEADERS
 #include "drv_rk_curv_col.h"
+#define CGFD_REF_VISCO_GMB CONST_VISCO_GMB
 #else
 #include "../../../include/cgfd3d_ref_abi.h"
 #endif
@@ -71,8 +72,13 @@ void drv_rk_curv_col_allstep(
 
   if (fd->num_rk_stages != 4 || fd->num_of_pairs != 8)
     unsupported("an operator set other than MacCormack DRP with RK4");
-  if (md->medium_type != CGFD_MEDIUM_ELASTIC_ISO)
+  if (md->medium_type != CGFD_MEDIUM_ELASTIC_ISO &&
+      md->medium_type != CGFD_MEDIUM_ELASTIC_VTI &&
+      md->medium_type != CGFD_MEDIUM_VISCOELASTIC_ISO)
     unsupported("this medium type");
+  if (md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO &&
+      md->visco_type != CGFD_REF_VISCO_GMB)
+    unsupported("a visco-elastic model other than GMB");
   if (src->dd_is_valid == 1) unsupported("a distributed (dd) source");
   if (src->total_number > 0 && src->total_number_surface_force > 0)
     unsupported("a surface force source");
@@ -92,6 +98,18 @@ void drv_rk_curv_col_allstep(
   p.slw = md->rho; /* md_rho_to_slow ran before the call */
   p.lambda = md->lambda;
   p.mu = md->mu;
+  p.c11 = md->c11; p.c13 = md->c13; p.c33 = md->c33;
+  p.c55 = md->c55; p.c66 = md->c66;
+  if (md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO) {
+    if (md->nmaxwell > CGFD_MAX_MAXWELL) unsupported("more than 8 Maxwell bodies");
+    p.nmaxwell = md->nmaxwell;
+    p.wl = md->wl;
+    for (int n = 0; n < md->nmaxwell; n++) {
+      p.Ylam[n] = md->Ylam[n];
+      p.Ymu[n] = md->Ymu[n];
+    }
+    p.x3d = gd->x3d; p.y3d = gd->y3d; p.z3d = gd->z3d;
+  }
   p.free_top = bdry->is_sides_free[2][1] == 1;
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {

@@ -348,3 +348,153 @@ def topo_model(ni=400, nj=400, nk=200, steps=2000, dt=None, npml=12, seed=2024,
               for a in range(side) for b in range(side)][:nrecv]
     add_surface_receivers(p, [(int(x), int(y)) for x, y in coords])
     return p
+
+
+# ---------------------------------------------------------------------------
+# anisotropic and attenuating media on the topography (300 x 300 x 150)
+# ---------------------------------------------------------------------------
+
+def gaussian_field_3d(shape, dh, corr, seed):
+    """Unit-variance Gaussian random field with Gaussian correlation of
+    length `corr` (metres) on a grid of spacing dh, shape (nz, ny, nx)."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape).astype(np.float32)
+    ks = [np.fft.fftfreq(n, d=dh).astype(np.float32) for n in shape]
+    filt = np.ones((1, 1, 1), np.float32)
+    for ax, k in enumerate(ks):
+        sh = [1, 1, 1]
+        sh[ax] = k.size
+        filt = filt * np.exp(-(np.pi * corr * k) ** 2 / 2.0).reshape(sh)
+    f = np.fft.ifftn(np.fft.fftn(w) * filt).real.astype(np.float32)
+    f -= f.mean()
+    f /= max(float(f.std()), 1e-30)
+    return f
+
+
+def normal_cdf(x):
+    from math import sqrt
+    from scipy.special import erf
+    return 0.5 * (1.0 + erf(np.asarray(x, np.float64) / sqrt(2.0)))
+
+
+def thomsen_to_vti(vp, vs, rho, eps, delta, gamma):
+    """Thomsen (1986) parameters -> c11, c13, c33, c55, c66 (the relations of
+    the reference's converter, media/media_utility.hpp:424)."""
+    vp, vs, rho = [np.asarray(a, np.float64) for a in (vp, vs, rho)]
+    c33 = rho * vp * vp
+    c55 = rho * vs * vs
+    c11 = c33 * (1.0 + 2.0 * eps)
+    c66 = c55 * (1.0 + 2.0 * gamma)
+    c13 = np.sqrt(2.0 * delta * c33 * (c33 - c55) + (c33 - c55) ** 2) - c55
+    return [np.ascontiguousarray(c.astype(np.float32)).ravel()
+            for c in (c11, c13, c33, c55, c66)]
+
+
+def gmb_coefficients(Qp, Qs, nmaxwell, fmin, fmax, fr):
+    """GMB relaxation frequencies and weights for constant Qp, Qs, and the
+    relaxed-to-unrelaxed modulus factors, restating the least-squares fit of
+    forward/md_t.c:642-792 (2n-1 log-spaced frequencies between fmin and
+    fmax, weights by the normal equations, moduli referred to fr).
+
+    Returns wl (nmaxwell), YP, YS (nmaxwell), fac_p, fac_s with
+    lam+2mu unrelaxed = (lam+2mu) fac_p and mu unrelaxed = mu fac_s."""
+    kmax = 2 * nmaxwell - 1
+    wr, wmin, wmax = 2 * math.pi * fr, 2 * math.pi * fmin, 2 * math.pi * fmax
+    wk = wmin * (wmax / wmin) ** (np.arange(kmax) / float(kmax - 1))
+    wl = wk[0::2][:nmaxwell]
+
+    def fit(Q):
+        q1 = 1.0 / round(Q)
+        G = (wl[None, :] * wk[:, None] + wl[None, :] ** 2 * q1) / \
+            (wl[None, :] ** 2 + wk[:, None] ** 2)
+        Y = np.linalg.solve(G.T @ G, G.T @ np.full(kmax, q1))
+        th1 = 1.0 - np.sum(Y / (1.0 + (wr / wl) ** 2))
+        th2 = np.sum(Y * wr / wl / (1.0 + (wr / wl) ** 2))
+        R = math.sqrt(th1 ** 2 + th2 ** 2)
+        return Y, (R + th1) / (2.0 * R * R)
+
+    YP, fac_p = fit(Qp)
+    YS, fac_s = fit(Qs)
+    return wl.astype(np.float32), YP, YS, fac_p, fac_s
+
+
+def topo_media_model(kind, ni=300, nj=300, nk=150, steps=1500, dt=None,
+                     npml=12, seed=2025, nrecv=400, nmaxwell=3):
+    """The topography model with a VTI (kind "vti") or GMB visco-elastic
+    (kind "visco") medium.
+
+    vti:   the three layers perturbed by 5 % with a seeded Gaussian random
+           field of 2 km correlation; Thomsen epsilon, delta ~ U[0, 0.2] and
+           gamma ~ U[0, 0.1] per point (independent seeded fields mapped
+           through the normal CDF); converted to c11, c13, c33, c55, c66.
+    visco: the three layers, Qp = 200, Qs = 100, `nmaxwell` Maxwell bodies
+           fitted over 0.5-5 Hz with reference frequency 1.58 Hz.
+    """
+    p = topo_model(ni=ni, nj=nj, nk=nk, steps=steps, dt=dt, npml=npml,
+                   seed=seed, nrecv=0)
+    rho = (1.0 / p.media["slw"].astype(np.float64))
+    mu = p.media["mu"].astype(np.float64)
+    lam = p.media["lambda"].astype(np.float64)
+    vs = np.sqrt(mu / rho)
+    vp = np.sqrt((lam + 2 * mu) / rho)
+    shape = (p.nz, p.ny, p.nx)
+    if kind == "vti":
+        pert = 1.0 + 0.05 * gaussian_field_3d(shape, 100.0, 2000.0, seed + 1).ravel()
+        vp, vs, rho = vp * pert, vs * pert, rho * pert
+        u = [normal_cdf(gaussian_field_3d(shape, 100.0, 2000.0, seed + s).ravel())
+             for s in (2, 3, 4)]
+        eps, delta, gamma = 0.2 * u[0], 0.2 * u[1], 0.1 * u[2]
+        c11, c13, c33, c55, c66 = thomsen_to_vti(vp, vs, rho, eps, delta, gamma)
+        p.medium_type = abi.CGFD_MEDIUM_ELASTIC_VTI
+        p.media = {"slw": np.ascontiguousarray((1.0 / rho).astype(np.float32)),
+                   "c11": c11, "c13": c13, "c33": c33, "c55": c55, "c66": c66}
+    elif kind == "visco":
+        wl, YP, YS, fac_p, fac_s = gmb_coefficients(200.0, 100.0, nmaxwell,
+                                                    0.5, 5.0, 1.58)
+        mu_u = mu * fac_s
+        lam_u = (lam + 2 * mu) * fac_p - 2 * mu_u
+        p.medium_type = abi.CGFD_MEDIUM_VISCOELASTIC_ISO
+        p.media["lambda"] = lam_u.astype(np.float32)
+        p.media["mu"] = mu_u.astype(np.float32)
+        p.nmaxwell = nmaxwell
+        p.wl = wl
+        r = (2.0 * mu_u / lam_u)
+        p.Ylam = [((1.0 + r) * YP[n] - r * YS[n]).astype(np.float32)
+                  for n in range(nmaxwell)]
+        p.Ymu = [np.full(p.vol, YS[n], np.float32) for n in range(nmaxwell)]
+        # memory variables: 6 per Maxwell body after the 9 components
+        ncmp = 9 + 6 * nmaxwell
+        wav = np.zeros(NLEVEL * ncmp * p.vol, np.float32)
+        p.ncmp = ncmp
+        p.wav = wav
+        for row in p.pml:
+            for f in row:
+                if f is not None:
+                    n9 = f["aux"].size // (NLEVEL * 9)
+                    f["aux"] = np.zeros(NLEVEL * ncmp * n9, np.float32)
+        X, Y, Z = _coords_of(p, seed)
+        p.coords = {"x3d": X, "y3d": Y, "z3d": Z}
+    else:
+        raise ValueError(kind)
+    side = int(round(math.sqrt(nrecv)))
+    if nrecv > 0:
+        coords = [(npml + 2 + (ni - 2 * npml - 4) * a / max(side - 1, 1),
+                   npml + 2 + (nj - 2 * npml - 4) * b / max(side - 1, 1))
+                  for a in range(side) for b in range(side)][:nrecv]
+        add_surface_receivers(p, [(int(x), int(y)) for x, y in coords])
+    return p
+
+
+def _coords_of(p, seed):
+    """Grid coordinates of topo_model's grid (flattened float32)."""
+    dh = 100.0
+    ni, nj, nk = p.ni, p.nj, p.nk
+    Lx, Ly = (ni - 1) * dh, (nj - 1) * dh
+    rough = gaussian_roughness(ni + 6, nj + 6, dh, 100.0, 1000.0, seed)
+
+    def surface(X, Y):
+        r2 = (X - Lx / 2) ** 2 + (Y - Ly / 2) ** 2
+        return 2000.0 * np.exp(-r2 / 5000.0 ** 2) + rough
+
+    X, Y, Z = grid_coords(ni, nj, nk, dh, surface, -(nk - 1) * dh)
+    return [np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (X, Y, Z)]

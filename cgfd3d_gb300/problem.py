@@ -47,6 +47,7 @@ class Problem:
         self.dt, self.t0, self.nt_total = float(dt), float(t0), int(nt_total)
         self.ncmp, self.nlevel = int(ncmp), NLEVEL
         self.metric = {}
+        self.coords = {}          # x3d, y3d, z3d (visco free surface only)
         self.medium_type = abi.CGFD_MEDIUM_ELASTIC_ISO
         self.media = {}
         self.nmaxwell = 0
@@ -164,6 +165,8 @@ class Problem:
         s.ncmp, s.nlevel = self.ncmp, self.nlevel
         s.wav = P(self.wav)
         s.dt, s.t0, s.nt_total = self.dt, self.t0, self.nt_total
+        for n in ("x3d", "y3d", "z3d"):
+            setattr(s, n, P(self.coords.get(n)))
         s._keep = keep
         return s
 
@@ -194,6 +197,9 @@ def from_golden(path_or_npz):
     assert tuple(int(v) for v in g) == p.grid_dims
     for n in abi.METRIC_NAMES:
         p.metric[n] = _f32(d["metric." + n])
+    for n in ("x3d", "y3d", "z3d"):
+        if "gd." + n in d:
+            p.coords[n] = _f32(d["gd." + n])
     p.medium_type = int(d["md.medium_type"][0])
     p.media["slw"] = _f32(d["md.slw"])
     for n in ("lambda", "mu", "c11", "c13", "c33", "c55", "c66"):
@@ -263,6 +269,8 @@ def from_golden(path_or_npz):
         expected["matVx2Vz2"] = d["out.matVx2Vz2"]
         expected["matVy2Vz2"] = d["out.matVy2Vz2"]
         expected["matF2Vz2"] = d["out.matF2Vz2"]
+    if "out.matD" in d:
+        expected["matD"] = d["out.matD"]
     if "case.json" in d:
         expected["case"] = json.loads(bytes(d["case.json"]).decode())
     return p, expected

@@ -59,6 +59,15 @@ class Solver:
             self._h, *[m.ctypes.data for m in mats]))
         return mats
 
+    def fetch_surface_rotation(self):
+        """Visco-elastic surface rotation matrices (nx*ny*9)."""
+        import numpy as np
+        p = self.problem
+        out = np.zeros(p.nx * p.ny * 9, np.float32)
+        _lib.check(_lib.lib().cgfd_solver_fetch_surface_rotation(
+            self._h, out.ctypes.data))
+        return out
+
     def set_timing(self, on=True):
         _lib.check(_lib.lib().cgfd_solver_set_timing(self._h, int(bool(on))))
 

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define CGFD_ABI_VERSION 1
+#define CGFD_ABI_VERSION 2
 
 /* medium types, same codes as forward/constants.h:24-29 */
 #define CGFD_MEDIUM_ELASTIC_ISO 2
@@ -118,6 +118,12 @@ typedef struct {
 
   float dt, t0;
   int nt_total;
+
+  /* grid coordinates gd_t.x3d/y3d/z3d (forward/gd_t.h:62-67), each
+   * nx*ny*nz; read only for the visco-elastic free surface, whose stress
+   * rotation needs the grid's eta tangent at k = nk2
+   * (forward/sv_curv_col_vis_iso.c:353-507).  May be NULL otherwise. */
+  const float *x3d, *y3d, *z3d;
 } cgfd_problem_t;
 
 /* Opaque device-resident solver. */
@@ -130,8 +136,11 @@ const char *cgfd_last_error(void);
 int cgfd_abi_version(void);
 
 /* Uploads every input of `p` into HBM, computes the free-surface conversion
- * matrices on the device (forward/sv_curv_col_el_iso.c:1258-1375) and
- * returns a solver positioned at step 0.  `p` must stay valid until
+ * matrices of the medium on the device (forward/sv_curv_col_el_iso.c:
+ * 1258-1375, forward/sv_curv_col_el_vti.c:1085-1206,
+ * forward/sv_curv_col_vis_iso.c:353-507) and returns a solver positioned at
+ * step 0.  Media: elastic_iso, elastic_vti, viscoelastic_iso (GMB, 1 to 3
+ * Maxwell bodies).  `p` must stay valid until
  * cgfd_solver_destroy (host output arrays are written by cgfd_solver_fetch). */
 int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out);
 
@@ -151,12 +160,17 @@ int cgfd_solver_step(const cgfd_solver_t *s);
 int cgfd_solver_fetch_surface_matrices(cgfd_solver_t *s, float *mVx, float *mVy,
                                        float *mF);
 
+/* Copies the visco-elastic surface rotation matrices (nx*ny*9, layout of
+ * bdry_t.matD, forward/sv_curv_col_vis_iso.c:487-501) to mD.  Only for a
+ * visco-elastic medium with a free surface. */
+int cgfd_solver_fetch_surface_rotation(cgfd_solver_t *s, float *mD);
+
 /* Copies the surface peak-motion maps accumulated so far (15 x nx*ny, the
  * PG array of forward/drv_rk_curv_col.c:123-130, filled as PG_calcu does,
  * forward/wav_t.c:379-455).  Only with a free surface. */
 int cgfd_solver_fetch_pg(cgfd_solver_t *s, float *pg);
 
-/* Copies the current state (9 x nx*ny*nz, reference layout) to w without
+/* Copies the current state (ncmp x nx*ny*nz, reference layout) to w without
  * touching the problem's arrays. */
 int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w);
 

@@ -34,6 +34,7 @@
 #define CGFD_REF_2_NDIM 8
 #define CGFD_REF_MAX_STRLEN 1024
 #define CGFD_REF_GD_TILE 4
+#define CGFD_REF_VISCO_GMB 2 /* CONST_VISCO_GMB, forward/constants.h:30 */
 
 typedef struct {
   int total_len;

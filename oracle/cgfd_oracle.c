@@ -6,10 +6,11 @@
  * of bench.py may load it; the product path never does.
  *
  * It restates, for the flat problem description of include/cgfd3d_gpu.h,
- * what the reference's drv_rk_curv_col_allstep does for isotropic elastic
- * media (the float arithmetic is ordered as in the reference so that the
- * results are bit-identical to the reference's own CPU build, which is
- * checked against the golden fixtures under tests/golden/):
+ * what the reference's drv_rk_curv_col_allstep does for isotropic elastic,
+ * VTI elastic and GMB visco-elastic isotropic media (the float arithmetic
+ * is ordered as in the reference so that the results are bit-identical to
+ * the reference's own CPU build, which is checked against the golden
+ * fixtures under tests/golden/):
  *
  *   time loop, pair/stage schedule, RK4 combine
  *                        forward/drv_rk_curv_col.c:167-544, fd_t.c:36-49,182-289
@@ -22,6 +23,13 @@
  *   receivers / lines    forward/io_funcs.c:1584-1645
  *   free-surface matrices forward/sv_curv_col_el_iso.c:1258-1375,
  *                        lib/fdlib_math.c:8-48
+ *   VTI media            forward/sv_curv_col_el_vti.c:200-397 (interior),
+ *                        :407-590 (vlow), :592-1075 (CFS-PML),
+ *                        :1085-1206 (free-surface matrices)
+ *   GMB visco-elastic    forward/sv_curv_col_vis_iso.c:22-245 (stage order),
+ *                        :250-347 (attenuation), :353-507 (free-surface
+ *                        matrices), :509-623 (surface stress rotation, after
+ *                        the last stage: forward/drv_rk_curv_col.c:440-445)
  *
  * Multi-threaded with pthreads (one slab of k-planes per thread) so that it
  * can serve as the host-core baseline.
@@ -98,6 +106,8 @@ typedef struct {
   float *aux[3][2][4];
   size_t aux_vol[3][2];
   float *mVx, *mVy, *mF;     /* free-surface matrices, 9 per (i,j) */
+  float *mD;                 /* visco: surface rotation matrix, 9 per (i,j) */
+  int med;                   /* medium_type */
   float **ext;               /* per source Gaussian weights (or NULL) */
   int nthreads;
   int timg_mode;
@@ -113,6 +123,133 @@ typedef struct {
 static inline float lam2mu_of(float lam, float mu)
 {
   return (float)((double)lam + 2.0 * (double)mu);
+}
+
+/* ------------------------------------------------------------------------ */
+/* media                                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* elastic constants of one point: isotropic (lam, mu, l2m) or VTI (c11,
+ * c12 = c11 - 2 c66 evaluated in double as the reference's `2.0 *` does,
+ * c13, c33, c55, c66; forward/sv_curv_col_el_vti.c:345-351) */
+typedef struct {
+  int vti;
+  float lam, mu, l2m;
+  float c11, c12, c13, c33, c55, c66;
+} med_t;
+
+static inline void med_at(const cgfd_problem_t *p, size_t q, med_t *m)
+{
+  memset(m, 0, sizeof(*m));
+  if (p->medium_type == CGFD_MEDIUM_ELASTIC_VTI) {
+    m->vti = 1;
+    m->c11 = p->c11[q]; m->c13 = p->c13[q]; m->c33 = p->c33[q];
+    m->c55 = p->c55[q]; m->c66 = p->c66[q];
+    m->c12 = (float)((double)m->c11 - 2.0 * (double)m->c66);
+  } else {
+    m->vti = 0;
+    m->lam = p->lambda[q];
+    m->mu = p->mu[q];
+    m->l2m = (float)((double)m->lam + 2.0 * (double)m->mu);
+  }
+}
+
+/* Hooke's law with all nine velocity gradients (interior and vlow):
+ * isotropic forward/sv_curv_col_el_iso.c:409-435, VTI
+ * forward/sv_curv_col_el_vti.c:366-389 (same expression order) */
+static inline void hooke9(const med_t *m, float xix, float xiy, float xiz,
+                          float etx, float ety, float etz, float ztx,
+                          float zty, float ztz, float DxVx, float DxVy,
+                          float DxVz, float DyVx, float DyVy, float DyVz,
+                          float DzVx, float DzVy, float DzVz, float *h,
+                          size_t V, size_t q)
+{
+  if (!m->vti) {
+    float lam = m->lam, mu = m->mu, l2m = m->l2m;
+    h[TXX * V + q] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
+                     lam * (xiy * DxVy + ety * DyVy + zty * DzVy +
+                            xiz * DxVz + etz * DyVz + ztz * DzVz);
+    h[TYY * V + q] = l2m * (xiy * DxVy + ety * DyVy + zty * DzVy) +
+                     lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
+                            xiz * DxVz + etz * DyVz + ztz * DzVz);
+    h[TZZ * V + q] = l2m * (xiz * DxVz + etz * DyVz + ztz * DzVz) +
+                     lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
+                            xiy * DxVy + ety * DyVy + zty * DzVy);
+    h[TXY * V + q] = mu * (xiy * DxVx + xix * DxVy + ety * DyVx +
+                           etx * DyVy + zty * DzVx + ztx * DzVy);
+    h[TXZ * V + q] = mu * (xiz * DxVx + xix * DxVz + etz * DyVx +
+                           etx * DyVz + ztz * DzVx + ztx * DzVz);
+    h[TYZ * V + q] = mu * (xiz * DxVy + xiy * DxVz + etz * DyVy +
+                           ety * DyVz + ztz * DzVy + zty * DzVz);
+    return;
+  }
+  float c11 = m->c11, c12 = m->c12, c13 = m->c13, c33 = m->c33,
+        c55 = m->c55, c66 = m->c66;
+  h[TXX * V + q] = (c11 * xix) * DxVx + (c12 * xiy) * DxVy + (c13 * xiz) * DxVz +
+                   (c11 * etx) * DyVx + (c12 * ety) * DyVy + (c13 * etz) * DyVz +
+                   (c11 * ztx) * DzVx + (c12 * zty) * DzVy + (c13 * ztz) * DzVz;
+  h[TYY * V + q] = (c12 * xix) * DxVx + (c11 * xiy) * DxVy + (c13 * xiz) * DxVz +
+                   (c12 * etx) * DyVx + (c11 * ety) * DyVy + (c13 * etz) * DyVz +
+                   (c12 * ztx) * DzVx + (c11 * zty) * DzVy + (c13 * ztz) * DzVz;
+  h[TZZ * V + q] = (c13 * xix) * DxVx + (c13 * xiy) * DxVy + (c33 * xiz) * DxVz +
+                   (c13 * etx) * DyVx + (c13 * ety) * DyVy + (c33 * etz) * DyVz +
+                   (c13 * ztx) * DzVx + (c13 * zty) * DzVy + (c33 * ztz) * DzVz;
+  h[TYZ * V + q] = (c55 * xiz) * DxVy + (c55 * xiy) * DxVz +
+                   (c55 * etz) * DyVy + (c55 * ety) * DyVz +
+                   (c55 * ztz) * DzVy + (c55 * zty) * DzVz;
+  h[TXZ * V + q] = (c55 * xiz) * DxVx + (c55 * xix) * DxVz +
+                   (c55 * etz) * DyVx + (c55 * etx) * DyVz +
+                   (c55 * ztz) * DzVx + (c55 * ztx) * DzVz;
+  h[TXY * V + q] = (c66 * xiy) * DxVx + (c66 * xix) * DxVy +
+                   (c66 * ety) * DyVx + (c66 * etx) * DyVy +
+                   (c66 * zty) * DzVx + (c66 * ztx) * DzVy;
+}
+
+/* Hooke's law with the gradients along one direction only (CFS-PML terms;
+ * e1..e3 the metric of that direction): isotropic
+ * forward/sv_curv_col_el_iso.c:806-811, VTI forward/sv_curv_col_el_vti.c:
+ * 760-765 */
+static inline void hooke1(const med_t *m, float e1, float e2, float e3,
+                          float DVx, float DVy, float DVz, float *r)
+{
+  if (!m->vti) {
+    float lam = m->lam, mu = m->mu, l2m = m->l2m;
+    r[TXX] = l2m * e1 * DVx + lam * e2 * DVy + lam * e3 * DVz;
+    r[TYY] = lam * e1 * DVx + l2m * e2 * DVy + lam * e3 * DVz;
+    r[TZZ] = lam * e1 * DVx + lam * e2 * DVy + l2m * e3 * DVz;
+    r[TXY] = mu * (e2 * DVx + e1 * DVy);
+    r[TXZ] = mu * (e3 * DVx + e1 * DVz);
+    r[TYZ] = mu * (e3 * DVy + e2 * DVz);
+    return;
+  }
+  float c11 = m->c11, c12 = m->c12, c13 = m->c13, c33 = m->c33,
+        c55 = m->c55, c66 = m->c66;
+  r[TXX] = (c11 * e1) * DVx + (c12 * e2) * DVy + (c13 * e3) * DVz;
+  r[TYY] = (c12 * e1) * DVx + (c11 * e2) * DVy + (c13 * e3) * DVz;
+  r[TZZ] = (c13 * e1) * DVx + (c13 * e2) * DVy + (c33 * e3) * DVz;
+  r[TYZ] = (c55 * e3) * DVy + (c55 * e2) * DVz;
+  r[TXZ] = (c55 * e3) * DVx + (c55 * e1) * DVz;
+  r[TXY] = (c66 * e2) * DVx + (c66 * e1) * DVy;
+}
+
+/* free-surface part of the x/y-face PML terms at k = nk2: zeta-metric
+ * Hooke's law applied to the converted z gradients (isotropic
+ * forward/sv_curv_col_el_iso.c:863-877, VTI forward/sv_curv_col_el_vti.c:
+ * 817-822) */
+static inline void hooke_surf(const med_t *m, float ztx, float zty, float ztz,
+                              float DzVx, float DzVy, float DzVz, float *s)
+{
+  if (!m->vti) {
+    float lam = m->lam, mu = m->mu, l2m = m->l2m;
+    s[TXX] = l2m * (ztx * DzVx) + lam * (zty * DzVy + ztz * DzVz);
+    s[TYY] = l2m * (zty * DzVy) + lam * (ztx * DzVx + ztz * DzVz);
+    s[TZZ] = l2m * (ztz * DzVz) + lam * (ztx * DzVx + zty * DzVy);
+    s[TXY] = mu * (zty * DzVx + ztx * DzVy);
+    s[TXZ] = mu * (ztz * DzVx + ztx * DzVz);
+    s[TYZ] = mu * (ztz * DzVy + zty * DzVz);
+    return;
+  }
+  hooke1(m, ztx, zty, ztz, DzVx, DzVy, DzVz, s);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -202,6 +339,154 @@ int oracle_dvh2dvz_iso(const cgfd_problem_t *p, float *mVx, float *mVy,
   return 0;
 }
 
+/* VTI: matVx2Vz = -A^-1 B, matVy2Vz = -A^-1 C at k = nk2
+ * (forward/sv_curv_col_el_vti.c:1085-1206); matF2Vz is left untouched */
+int oracle_dvh2dvz_vti(const cgfd_problem_t *p, float *mVx, float *mVy)
+{
+  size_t ln = p->nx, sl = (size_t)p->nx * p->ny;
+  int k = p->nk2;
+  for (int j = p->nj1; j <= p->nj2; j++)
+    for (int i = p->ni1; i <= p->ni2; i++) {
+      size_t q = i + j * ln + k * sl;
+      float xix = p->xi_x[q], xiy = p->xi_y[q], xiz = p->xi_z[q];
+      float etx = p->eta_x[q], ety = p->eta_y[q], etz = p->eta_z[q];
+      float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
+      med_t m;
+      med_at(p, q, &m);
+      float c11 = m.c11, c12 = m.c12, c13 = m.c13, c33 = m.c33, c55 = m.c55,
+            c66 = m.c66;
+      float A[3][3], B[3][3], C[3][3], AB[3][3], AC[3][3];
+      A[0][0] = (c11 * ztx) * ztx + (c66 * zty) * zty + (c55 * ztz) * ztz;
+      A[0][1] = (c12 * zty) * ztx + (c66 * ztx) * zty;
+      A[0][2] = (c13 * ztz) * ztx + (c55 * ztx) * ztz;
+      A[1][0] = (c66 * zty) * ztx + (c12 * ztx) * zty;
+      A[1][1] = (c66 * ztx) * ztx + (c11 * zty) * zty + (c55 * ztz) * ztz;
+      A[1][2] = (c13 * ztz) * zty + (c55 * zty) * ztz;
+      A[2][0] = (c55 * ztz) * ztx + (c13 * ztx) * ztz;
+      A[2][1] = (c55 * ztz) * zty + (c13 * zty) * ztz;
+      A[2][2] = (c55 * ztx) * ztx + (c55 * zty) * zty + (c33 * ztz) * ztz;
+      inv3(A);
+      B[0][0] = (c11 * xix) * ztx + (c66 * xiy) * zty + (c55 * xiz) * ztz;
+      B[0][1] = (c12 * xiy) * ztx + (c66 * xix) * zty;
+      B[0][2] = (c13 * xiz) * ztx + (c55 * xix) * ztz;
+      B[1][0] = (c66 * xiy) * ztx + (c12 * xix) * zty;
+      B[1][1] = (c66 * xix) * ztx + (c11 * xiy) * zty + (c55 * xiz) * ztz;
+      B[1][2] = (c13 * xiz) * zty + (c55 * xiy) * ztz;
+      B[2][0] = (c55 * xiz) * ztx + (c13 * xix) * ztz;
+      B[2][1] = (c55 * xiz) * zty + (c13 * xiy) * ztz;
+      B[2][2] = (c55 * xix) * ztx + (c55 * xiy) * zty + (c33 * xiz) * ztz;
+      C[0][0] = (c11 * etx) * ztx + (c66 * ety) * zty + (c55 * etz) * ztz;
+      C[0][1] = (c12 * ety) * ztx + (c66 * etx) * zty;
+      C[0][2] = (c13 * etz) * ztx + (c55 * etx) * ztz;
+      C[1][0] = (c66 * ety) * ztx + (c12 * etx) * zty;
+      C[1][1] = (c66 * etx) * ztx + (c11 * ety) * zty + (c55 * etz) * ztz;
+      C[1][2] = (c13 * etz) * zty + (c55 * ety) * ztz;
+      C[2][0] = (c55 * etz) * ztx + (c13 * etx) * ztz;
+      C[2][1] = (c55 * etz) * zty + (c13 * ety) * ztz;
+      C[2][2] = (c55 * etx) * ztx + (c55 * ety) * zty + (c33 * etz) * ztz;
+      mul3(A, B, AB);
+      mul3(A, C, AC);
+      size_t ij = (j * ln + i) * 9;
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+          mVx[ij + r * 3 + c] = -1.0f * AB[r][c];
+          mVy[ij + r * 3 + c] = -1.0f * AC[r][c];
+        }
+    }
+  return 0;
+}
+
+/* centred 7-point operator of the metric calculation (fd_t.c:152-176,
+ * layer 3), used along j on the grid coordinates */
+static const float FDC_COEF[7] = {-0.02084f, 0.1667f, -0.7709f, 0.0f,
+                                  0.7709f, -0.1667f, 0.02084f};
+
+/* visco-elastic (GMB): matVx2Vz = A^-1 B, matVy2Vz = A^-1 C and the
+ * rotation matrix matD of the local surface frame at k = nk2
+ * (forward/sv_curv_col_vis_iso.c:353-507); matF2Vz is left untouched */
+int oracle_dvh2dvz_vis(const cgfd_problem_t *p, float *mVx, float *mVy,
+                       float *mD)
+{
+  size_t ln = p->nx, sl = (size_t)p->nx * p->ny;
+  int k = p->nk2;
+  for (int j = p->nj1; j <= p->nj2; j++)
+    for (int i = p->ni1; i <= p->ni2; i++) {
+      size_t q = i + j * ln + k * sl;
+      float xix = p->xi_x[q], xiy = p->xi_y[q], xiz = p->xi_z[q];
+      float etx = p->eta_x[q], ety = p->eta_y[q], etz = p->eta_z[q];
+      float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
+      float xet, yet, zet;
+      xet = FDC_COEF[0] * p->x3d[q - 3 * ln];
+      yet = FDC_COEF[0] * p->y3d[q - 3 * ln];
+      zet = FDC_COEF[0] * p->z3d[q - 3 * ln];
+      for (int n = 1; n < 7; n++) {
+        long s = (long)(n - 3) * (long)ln;
+        xet += FDC_COEF[n] * p->x3d[q + s];
+      }
+      for (int n = 1; n < 7; n++) {
+        long s = (long)(n - 3) * (long)ln;
+        yet += FDC_COEF[n] * p->y3d[q + s];
+      }
+      for (int n = 1; n < 7; n++) {
+        long s = (long)(n - 3) * (long)ln;
+        zet += FDC_COEF[n] * p->z3d[q + s];
+      }
+      float e_n = (float)(1.0 / sqrt((double)(xet * xet + yet * yet + zet * zet)));
+      float e_m = (float)(1.0 / sqrt((double)(ztx * ztx + zty * zty + ztz * ztz)));
+      float e_nm = e_n * e_m;
+      float lam = p->lambda[q], mu = p->mu[q];
+      float l2m = lam + 2.0f * mu;
+      float A[3][3], B[3][3], C[3][3], D[3][3], AB[3][3], AC[3][3];
+      A[0][0] = l2m * ztx * ztx + mu * (zty * zty + ztz * ztz);
+      A[0][1] = lam * ztx * zty + mu * zty * ztx;
+      A[0][2] = lam * ztx * ztz + mu * ztz * ztx;
+      A[1][0] = lam * zty * ztx + mu * ztx * zty;
+      A[1][1] = l2m * zty * zty + mu * (ztx * ztx + ztz * ztz);
+      A[1][2] = lam * zty * ztz + mu * ztz * zty;
+      A[2][0] = lam * ztz * ztx + mu * ztx * ztz;
+      A[2][1] = lam * ztz * zty + mu * zty * ztz;
+      A[2][2] = l2m * ztz * ztz + mu * (ztx * ztx + zty * zty);
+      inv3(A);
+      B[0][0] = -l2m * ztx * xix - mu * (zty * xiy + ztz * xiz);
+      B[0][1] = -lam * ztx * xiy - mu * zty * xix;
+      B[0][2] = -lam * ztx * xiz - mu * ztz * xix;
+      B[1][0] = -lam * zty * xix - mu * ztx * xiy;
+      B[1][1] = -l2m * zty * xiy - mu * (ztx * xix + ztz * xiz);
+      B[1][2] = -lam * zty * xiz - mu * ztz * xiy;
+      B[2][0] = -lam * ztz * xix - mu * ztx * xiz;
+      B[2][1] = -lam * ztz * xiy - mu * zty * xiz;
+      B[2][2] = -l2m * ztz * xiz - mu * (ztx * xix + zty * xiy);
+      C[0][0] = -l2m * ztx * etx - mu * (zty * ety + ztz * etz);
+      C[0][1] = -lam * ztx * ety - mu * zty * etx;
+      C[0][2] = -lam * ztx * etz - mu * ztz * etx;
+      C[1][0] = -lam * zty * etx - mu * ztx * ety;
+      C[1][1] = -l2m * zty * ety - mu * (ztx * etx + ztz * etz);
+      C[1][2] = -lam * zty * etz - mu * ztz * ety;
+      C[2][0] = -lam * ztz * etx - mu * ztx * etz;
+      C[2][1] = -lam * ztz * ety - mu * zty * etz;
+      C[2][2] = -l2m * ztz * etz - mu * (ztx * etx + zty * ety);
+      mul3(A, B, AB);
+      mul3(A, C, AC);
+      D[0][0] = (yet * ztz - zet * zty) * e_nm;
+      D[0][1] = (zet * ztx - xet * ztz) * e_nm;
+      D[0][2] = (xet * zty - yet * ztx) * e_nm;
+      D[1][0] = xet * e_n;
+      D[1][1] = yet * e_n;
+      D[1][2] = zet * e_n;
+      D[2][0] = ztx * e_m;
+      D[2][1] = zty * e_m;
+      D[2][2] = ztz * e_m;
+      size_t ij = (j * ln + i) * 9;
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+          mVx[ij + r * 3 + c] = AB[r][c];
+          mVy[ij + r * 3 + c] = AC[r][c];
+          mD[ij + r * 3 + c] = D[r][c];
+        }
+    }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* RHS passes                                                               */
 /* ------------------------------------------------------------------------ */
@@ -230,8 +515,9 @@ static void rhs_inner_plane(orc_t *o, const float *w, float *h, int k,
       float xix = p->xi_x[q], xiy = p->xi_y[q], xiz = p->xi_z[q];
       float etx = p->eta_x[q], ety = p->eta_y[q], etz = p->eta_z[q];
       float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
-      float lam = p->lambda[q], mu = p->mu[q], slw = p->slw[q];
-      float l2m = lam2mu_of(lam, mu);
+      float slw = p->slw[q];
+      med_t m;
+      med_at(p, q, &m);
       h[VX * V + q] = slw * (xix * DxTxx + xiy * DxTxy + xiz * DxTxz +
                              etx * DyTxx + ety * DyTxy + etz * DyTxz +
                              ztx * DzTxx + zty * DzTxy + ztz * DzTxz);
@@ -241,21 +527,8 @@ static void rhs_inner_plane(orc_t *o, const float *w, float *h, int k,
       h[VZ * V + q] = slw * (xix * DxTxz + xiy * DxTyz + xiz * DxTzz +
                              etx * DyTxz + ety * DyTyz + etz * DyTzz +
                              ztx * DzTxz + zty * DzTyz + ztz * DzTzz);
-      h[TXX * V + q] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
-                       lam * (xiy * DxVy + ety * DyVy + zty * DzVy +
-                              xiz * DxVz + etz * DyVz + ztz * DzVz);
-      h[TYY * V + q] = l2m * (xiy * DxVy + ety * DyVy + zty * DzVy) +
-                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
-                              xiz * DxVz + etz * DyVz + ztz * DzVz);
-      h[TZZ * V + q] = l2m * (xiz * DxVz + etz * DyVz + ztz * DzVz) +
-                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
-                              xiy * DxVy + ety * DyVy + zty * DzVy);
-      h[TXY * V + q] = mu * (xiy * DxVx + xix * DxVy + ety * DyVx +
-                             etx * DyVy + zty * DzVx + ztx * DzVy);
-      h[TXZ * V + q] = mu * (xiz * DxVx + xix * DxVz + etz * DyVx +
-                             etx * DyVz + ztz * DzVx + ztx * DzVz);
-      h[TYZ * V + q] = mu * (xiz * DxVy + xiy * DxVz + etz * DyVy +
-                             ety * DyVz + ztz * DzVy + zty * DzVz);
+      hooke9(&m, xix, xiy, xiz, etx, ety, etz, ztx, zty, ztz, DxVx, DxVy, DxVz,
+             DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, h, V, q);
     }
   }
 }
@@ -345,8 +618,8 @@ static void rhs_vlow_row(orc_t *o, const float *w, float *h, int j, int zbias,
       float xix = p->xi_x[q], xiy = p->xi_y[q], xiz = p->xi_z[q];
       float etx = p->eta_x[q], ety = p->eta_y[q], etz = p->eta_z[q];
       float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
-      float lam = p->lambda[q], mu = p->mu[q];
-      float l2m = lam2mu_of(lam, mu);
+      med_t m;
+      med_at(p, q, &m);
       float DxVx = D5(ox, Vx + q), DyVx = D5(oy, Vx + q);
       float DxVy = D5(ox, Vy + q), DyVy = D5(oy, Vy + q);
       float DxVz = D5(ox, Vz + q), DyVz = D5(oy, Vz + q);
@@ -360,11 +633,14 @@ static void rhs_vlow_row(orc_t *o, const float *w, float *h, int j, int zbias,
                b[4] * DyVy + b[5] * DyVz;
         DzVz = a[6] * DxVx + a[7] * DxVy + a[8] * DxVz + b[6] * DyVx +
                b[7] * DyVy + b[8] * DyVz;
-        /* + matF2Vz * (VxSrc,VySrc,VzSrc): zero without surface forces */
-        const float *f = o->mF + ij;
-        DzVx += f[0] * 0.0f + f[1] * 0.0f + f[2] * 0.0f;
-        DzVy += f[3] * 0.0f + f[4] * 0.0f + f[5] * 0.0f;
-        DzVz += f[6] * 0.0f + f[7] * 0.0f + f[8] * 0.0f;
+        /* + matF2Vz * (VxSrc,VySrc,VzSrc): zero without surface forces;
+           the VTI routine has no such term (sv_curv_col_el_vti.c:525-547) */
+        if (!m.vti) {
+          const float *f = o->mF + ij;
+          DzVx += f[0] * 0.0f + f[1] * 0.0f + f[2] * 0.0f;
+          DzVy += f[3] * 0.0f + f[4] * 0.0f + f[5] * 0.0f;
+          DzVz += f[6] * 0.0f + f[7] * 0.0f + f[8] * 0.0f;
+        }
       } else if (n == 1) {
         long s0 = OPZ1_SHIFT[zbias][0] * (long)sl, s1 = OPZ1_SHIFT[zbias][1] * (long)sl;
         const float *c = OPZ1_COEF[zbias];
@@ -379,21 +655,8 @@ static void rhs_vlow_row(orc_t *o, const float *w, float *h, int j, int zbias,
         DzVy = c[0] * Vy[q + s0]; DzVy += c[1] * Vy[q + s1]; DzVy += c[2] * Vy[q + s2];
         DzVz = c[0] * Vz[q + s0]; DzVz += c[1] * Vz[q + s1]; DzVz += c[2] * Vz[q + s2];
       }
-      h[TXX * V + q] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
-                       lam * (xiy * DxVy + ety * DyVy + zty * DzVy +
-                              xiz * DxVz + etz * DyVz + ztz * DzVz);
-      h[TYY * V + q] = l2m * (xiy * DxVy + ety * DyVy + zty * DzVy) +
-                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
-                              xiz * DxVz + etz * DyVz + ztz * DzVz);
-      h[TZZ * V + q] = l2m * (xiz * DxVz + etz * DyVz + ztz * DzVz) +
-                       lam * (xix * DxVx + etx * DyVx + ztx * DzVx +
-                              xiy * DxVy + ety * DyVy + zty * DzVy);
-      h[TXY * V + q] = mu * (xiy * DxVx + xix * DxVy + ety * DyVx +
-                             etx * DyVy + zty * DzVx + ztx * DzVy);
-      h[TXZ * V + q] = mu * (xiz * DxVx + xix * DxVz + etz * DyVx +
-                             etx * DyVz + ztz * DzVx + ztx * DzVz);
-      h[TYZ * V + q] = mu * (xiz * DxVy + xiy * DxVz + etz * DyVy +
-                             ety * DyVz + ztz * DzVy + zty * DzVz);
+      hooke9(&m, xix, xiy, xiz, etx, ety, etz, ztx, zty, ztz, DxVx, DxVy, DxVz,
+             DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, h, V, q);
     }
   }
 }
@@ -424,8 +687,9 @@ static void rhs_pml_face_plane(orc_t *o, const float *w, float *h, int idim,
       float cD = f->D[n], cA = f->A[n], cB = f->B[n];
       float cB1 = (float)((double)cB - 1.0);
       float e1 = m1[q], e2 = m2[q], e3 = m3[q];
-      float lam = p->lambda[q], mu = p->mu[q], slw = p->slw[q];
-      float l2m = lam2mu_of(lam, mu);
+      float slw = p->slw[q];
+      med_t m;
+      med_at(p, q, &m);
       float DVx = D5(op, W[VX] + q), DVy = D5(op, W[VY] + q), DVz = D5(op, W[VZ] + q);
       float DTxx = D5(op, W[TXX] + q), DTyy = D5(op, W[TYY] + q),
             DTzz = D5(op, W[TZZ] + q), DTxz = D5(op, W[TXZ] + q),
@@ -434,12 +698,7 @@ static void rhs_pml_face_plane(orc_t *o, const float *w, float *h, int idim,
       r[VX] = slw * (e1 * DTxx + e2 * DTxy + e3 * DTxz);
       r[VY] = slw * (e1 * DTxy + e2 * DTyy + e3 * DTyz);
       r[VZ] = slw * (e1 * DTxz + e2 * DTyz + e3 * DTzz);
-      r[TXX] = l2m * e1 * DVx + lam * e2 * DVy + lam * e3 * DVz;
-      r[TYY] = lam * e1 * DVx + l2m * e2 * DVy + lam * e3 * DVz;
-      r[TZZ] = lam * e1 * DVx + lam * e2 * DVy + l2m * e3 * DVz;
-      r[TXY] = mu * (e2 * DVx + e1 * DVy);
-      r[TXZ] = mu * (e3 * DVx + e1 * DVz);
-      r[TYZ] = mu * (e3 * DVy + e2 * DVz);
+      hooke1(&m, e1, e2, e3, DVx, DVy, DVz, r);
       /* same component order of updates as the reference */
       static const int ord[9] = {VX, VY, VZ, TXX, TYY, TZZ, TXZ, TYZ, TXY};
       for (int m = 0; m < 9; m++) {
@@ -458,12 +717,7 @@ static void rhs_pml_face_plane(orc_t *o, const float *w, float *h, int idim,
         float DzVz = M[6] * DVx + M[7] * DVy + M[8] * DVz;
         float ztx = p->zeta_x[q], zty = p->zeta_y[q], ztz = p->zeta_z[q];
         float s[9];
-        s[TXX] = l2m * (ztx * DzVx) + lam * (zty * DzVy + ztz * DzVz);
-        s[TYY] = l2m * (zty * DzVy) + lam * (ztx * DzVx + ztz * DzVz);
-        s[TZZ] = l2m * (ztz * DzVz) + lam * (ztx * DzVx + zty * DzVy);
-        s[TXY] = mu * (zty * DzVx + ztx * DzVy);
-        s[TXZ] = mu * (ztz * DzVx + ztx * DzVz);
-        s[TYZ] = mu * (ztz * DzVy + zty * DzVz);
+        hooke_surf(&m, ztx, zty, ztz, DzVx, DzVy, DzVz, s);
         static const int ordT[6] = {TXX, TYY, TZZ, TXZ, TYZ, TXY};
         for (int m = 0; m < 6; m++) {
           int c = ordT[m];
@@ -476,6 +730,112 @@ static void rhs_pml_face_plane(orc_t *o, const float *w, float *h, int idim,
         }
       }
     }
+  }
+}
+
+/* GMB attenuation of one k plane (forward/sv_curv_col_vis_iso.c:250-347):
+ * memory-variable rates from the strain rates implied by hT, and the
+ * memory-stress correction of hT.  Runs after the PML pass and before the
+ * sources, as in sv_curv_col_vis_iso_onestage (:165-232). */
+static void rhs_atten_plane(orc_t *o, const float *w, float *h, int k)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t V = o->vol;
+  int nm = p->nmaxwell;
+  for (int j = p->nj1; j <= p->nj2; j++) {
+    size_t q = p->ni1 + j * o->ln + (size_t)k * o->sl;
+    for (int i = p->ni1; i <= p->ni2; i++, q++) {
+      float lam = p->lambda[q], mu = p->mu[q];
+      float hxx = h[TXX * V + q], hyy = h[TYY * V + q], hzz = h[TZZ * V + q];
+      float hxy = h[TXY * V + q], hxz = h[TXZ * V + q], hyz = h[TYZ * V + q];
+      float sum_hxyz = (hxx + hyy + hzz) / (3 * lam + 2 * mu);
+      double mu2 = (double)(2 * mu);
+      float EVxx = (float)(((2.0 * hxx - hyy - hzz) / mu2 + sum_hxyz) / 3);
+      float EVyy = (float)(((2.0 * hyy - hxx - hzz) / mu2 + sum_hxyz) / 3);
+      float EVzz = (float)(((2.0 * hzz - hxx - hyy) / mu2 + sum_hxyz) / 3);
+      float EVxy = (float)(hxy / mu * 0.5);
+      float EVxz = (float)(hxz / mu * 0.5);
+      float EVyz = (float)(hyz / mu * 0.5);
+      for (int n = 0; n < nm; n++) {
+        size_t b = (size_t)(9 + 6 * n) * V + q;
+        float wl = p->wl[n];
+        h[b + 0 * V] = wl * (EVxx - w[b + 0 * V]);
+        h[b + 1 * V] = wl * (EVyy - w[b + 1 * V]);
+        h[b + 2 * V] = wl * (EVzz - w[b + 2 * V]);
+        h[b + 5 * V] = wl * (EVxy - w[b + 5 * V]);
+        h[b + 4 * V] = wl * (EVxz - w[b + 4 * V]);
+        h[b + 3 * V] = wl * (EVyz - w[b + 3 * V]);
+      }
+      float sxyz = 0.0f, sxx = 0.0f, syy = 0.0f, szz = 0.0f, sxy = 0.0f,
+            sxz = 0.0f, syz = 0.0f;
+      for (int n = 0; n < nm; n++) {
+        size_t b = (size_t)(9 + 6 * n) * V + q;
+        float yl = p->Ylam[n][q], ym = p->Ymu[n][q];
+        float Jxx = w[b], Jyy = w[b + V], Jzz = w[b + 2 * V];
+        float Jyz = w[b + 3 * V], Jxz = w[b + 4 * V], Jxy = w[b + 5 * V];
+        sxyz += yl * (Jxx + Jyy + Jzz);
+        sxx += ym * Jxx;
+        syy += ym * Jyy;
+        szz += ym * Jzz;
+        sxy += ym * Jxy;
+        sxz += ym * Jxz;
+        syz += ym * Jyz;
+      }
+      double mu2d = 2.0 * (double)mu;
+      float mxx = (float)((double)(lam * sxyz) + mu2d * (double)sxx);
+      float myy = (float)((double)(lam * sxyz) + mu2d * (double)syy);
+      float mzz = (float)((double)(lam * sxyz) + mu2d * (double)szz);
+      float mxy = (float)(mu2d * (double)sxy);
+      float mxz = (float)(mu2d * (double)sxz);
+      float myz = (float)(mu2d * (double)syz);
+      h[TXX * V + q] = hxx - mxx;
+      h[TYY * V + q] = hyy - myy;
+      h[TZZ * V + q] = hzz - mzz;
+      h[TXY * V + q] = hxy - mxy;
+      h[TXZ * V + q] = hxz - mxz;
+      h[TYZ * V + q] = hyz - myz;
+    }
+  }
+}
+
+/* visco-elastic free surface after the last stage: rotate the surface
+ * stress into the local frame, drop the traction components, rotate back
+ * (forward/sv_curv_col_vis_iso.c:509-623) */
+static void vis_free_row(orc_t *o, float *w, int j)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t V = o->vol, ln = o->ln;
+  size_t q = p->ni1 + j * ln + (size_t)p->nk2 * o->sl;
+  for (int i = p->ni1; i <= p->ni2; i++, q++) {
+    const float *M = o->mD + (i + j * ln) * 9;
+    float D[3][3], DT[3][3], Tl[3][3], DTl[3][3], Tg[3][3];
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) {
+        D[r][c] = M[r * 3 + c];
+        DT[c][r] = M[r * 3 + c];
+      }
+    float d11 = D[0][0], d12 = D[0][1], d13 = D[0][2];
+    float d21 = D[1][0], d22 = D[1][1], d23 = D[1][2];
+    float Txx = w[TXX * V + q], Tyy = w[TYY * V + q], Tzz = w[TZZ * V + q];
+    float Txy = w[TXY * V + q], Txz = w[TXZ * V + q], Tyz = w[TYZ * V + q];
+    Tl[0][0] = d11 * d11 * Txx + d12 * d12 * Tyy + d13 * d13 * Tzz +
+               2 * (d11 * d12 * Txy + d11 * d13 * Txz + d12 * d13 * Tyz);
+    Tl[0][1] = d11 * d21 * Txx + d12 * d22 * Tyy + d13 * d23 * Tzz +
+               (d11 * d22 + d12 * d21) * Txy + (d11 * d23 + d21 * d13) * Txz +
+               (d12 * d23 + d22 * d13) * Tyz;
+    Tl[1][1] = d21 * d21 * Txx + d22 * d22 * Tyy + d23 * d23 * Tzz +
+               2 * (d21 * d22 * Txy + d21 * d23 * Txz + d22 * d23 * Tyz);
+    Tl[1][0] = Tl[0][1];
+    Tl[0][2] = 0.0f; Tl[1][2] = 0.0f; Tl[2][0] = 0.0f; Tl[2][1] = 0.0f;
+    Tl[2][2] = 0.0f;
+    mul3(DT, Tl, DTl);
+    mul3(DTl, D, Tg);
+    w[TXX * V + q] = Tg[0][0];
+    w[TYY * V + q] = Tg[1][1];
+    w[TZZ * V + q] = Tg[2][2];
+    w[TXY * V + q] = Tg[0][1];
+    w[TXZ * V + q] = Tg[0][2];
+    w[TYZ * V + q] = Tg[1][2];
   }
 }
 
@@ -702,6 +1062,11 @@ static void *worker(void *arg)
           }
         }
       pthread_barrier_wait(&o->bar);
+      /* 4b. GMB attenuation (visco-elastic media) */
+      if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO) {
+        for (long k = k0; k < k1; k++) rhs_atten_plane(o, cur, rhs, (int)k);
+        pthread_barrier_wait(&o->bar);
+      }
       /* 5. sources */
       if (tid == 0 && p->src_n > 0) rhs_src(o, rhs, it, is);
       pthread_barrier_wait(&o->bar);
@@ -743,6 +1108,12 @@ static void *worker(void *arg)
             slab(o, tid, 0, (long)(o->aux_vol[d][s] * p->ncmp), &a0, &a1);
             for (long e = a0; e < a1; e++) aend[d][s][e] += cb * arhs[d][s][e];
           }
+        /* visco-elastic free surface (drv_rk_curv_col.c:440-445) */
+        if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO && p->free_top) {
+          pthread_barrier_wait(&o->bar);
+          for (int j = p->nj1 + tid; j <= p->nj2; j += o->nthreads)
+            vis_free_row(o, end, j);
+        }
       }
       pthread_barrier_wait(&o->bar);
     }
@@ -782,9 +1153,18 @@ int oracle_allstep(const cgfd_problem_t *p, int timg_mode, int nthreads,
 int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
                       float *mVx, float *mVy, float *mF, float *pg)
 {
-  if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO) return CGFD_EINVAL;
+  int med = p->medium_type;
+  if (med != CGFD_MEDIUM_ELASTIC_ISO && med != CGFD_MEDIUM_ELASTIC_VTI &&
+      med != CGFD_MEDIUM_VISCOELASTIC_ISO)
+    return CGFD_EINVAL;
   if (p->src_n_surface_force > 0) return CGFD_EINVAL;
-  if (p->nlevel != 4 || p->ncmp != 9) return CGFD_EINVAL;
+  int ncmp_want = 9;
+  if (med == CGFD_MEDIUM_VISCOELASTIC_ISO) {
+    if (p->nmaxwell < 1 || p->nmaxwell > CGFD_MAX_MAXWELL || !p->wl) return CGFD_EINVAL;
+    if (p->free_top && (!p->x3d || !p->y3d || !p->z3d)) return CGFD_EINVAL;
+    ncmp_want += 6 * p->nmaxwell;
+  }
+  if (p->nlevel != 4 || p->ncmp != ncmp_want) return CGFD_EINVAL;
   orc_t o;
   memset(&o, 0, sizeof(o));
   o.p = p;
@@ -801,7 +1181,7 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
       size_t av = (size_t)(f->ni2 - f->ni1 + 1) * (f->nj2 - f->nj1 + 1) *
                   (f->nk2 - f->nk1 + 1);
       o.aux_vol[d][s] = av;
-      for (int l = 0; l < 4; l++) o.aux[d][s][l] = f->aux + (size_t)l * av * 9;
+      for (int l = 0; l < 4; l++) o.aux[d][s][l] = f->aux + (size_t)l * av * p->ncmp;
     }
   size_t n2 = o.sl * 9;
   int own_m = 0;
@@ -814,9 +1194,17 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
     } else {
       memset(mVx, 0, n2 * 4); memset(mVy, 0, n2 * 4); memset(mF, 0, n2 * 4);
     }
-    oracle_dvh2dvz_iso(p, mVx, mVy, mF);
+    if (med == CGFD_MEDIUM_ELASTIC_VTI) {
+      oracle_dvh2dvz_vti(p, mVx, mVy);
+    } else if (med == CGFD_MEDIUM_VISCOELASTIC_ISO) {
+      o.mD = calloc(n2, sizeof(float));
+      oracle_dvh2dvz_vis(p, mVx, mVy, o.mD);
+    } else {
+      oracle_dvh2dvz_iso(p, mVx, mVy, mF);
+    }
   }
   o.mVx = mVx; o.mVy = mVy; o.mF = mF;
+  o.med = med;
   if (p->src_n > 0 && p->src_spatial != CGFD_SRC_POINT) {
     int n1 = 2 * p->src_ext_half + 1;
     o.ext = calloc(p->src_n, sizeof(float *));
@@ -850,6 +1238,7 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
     free(o.ext);
   }
   if (own_m) { free(mVx); free(mVy); free(mF); }
+  free(o.mD);
   free(o.dis);
   return 0;
 }

@@ -46,6 +46,11 @@ def lib():
         _lib.oracle_dvh2dvz_iso.restype = C.c_int
         _lib.oracle_dvh2dvz_iso.argtypes = [C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_void_p]
+        _lib.oracle_dvh2dvz_vti.restype = C.c_int
+        _lib.oracle_dvh2dvz_vti.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.oracle_dvh2dvz_vis.restype = C.c_int
+        _lib.oracle_dvh2dvz_vis.argtypes = [C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -76,3 +81,25 @@ def allstep(problem, timg_mode=TIMG_ZERO, nthreads=1, want_mats=False,
     if want_pg:
         return pg
     return mats if want_mats else None
+
+
+def surface_matrices(problem):
+    """Free-surface matrices of the problem's medium, as the oracle computes
+    them before the time loop: dict of matVx2Vz2, matVy2Vz2, matF2Vz2 and,
+    for visco-elastic media, matD (each nx*ny*9)."""
+    import numpy as np
+    cs = problem.to_c()
+    n2 = problem.nx * problem.ny * 9
+    out = {k: np.zeros(n2, np.float32)
+           for k in ("matVx2Vz2", "matVy2Vz2", "matF2Vz2")}
+    ptr = {k: v.ctypes.data for k, v in out.items()}
+    if problem.medium_type == 3:
+        lib().oracle_dvh2dvz_vti(C.addressof(cs), ptr["matVx2Vz2"], ptr["matVy2Vz2"])
+    elif problem.medium_type == 5:
+        out["matD"] = np.zeros(n2, np.float32)
+        lib().oracle_dvh2dvz_vis(C.addressof(cs), ptr["matVx2Vz2"],
+                                 ptr["matVy2Vz2"], out["matD"].ctypes.data)
+    else:
+        lib().oracle_dvh2dvz_iso(C.addressof(cs), ptr["matVx2Vz2"],
+                                 ptr["matVy2Vz2"], ptr["matF2Vz2"])
+    return out

@@ -168,6 +168,12 @@ static void dump_inputs(fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md,
   put("metric.zeta_x", 'f', metric->zeta_x, n);
   put("metric.zeta_y", 'f', metric->zeta_y, n);
   put("metric.zeta_z", 'f', metric->zeta_z, n);
+  /* grid coordinates: read by the visco-elastic free surface only */
+  if (md->medium_type == CONST_MEDIUM_VISCOELASTIC_ISO && gd->x3d) {
+    put("gd.x3d", 'f', gd->x3d, n);
+    put("gd.y3d", 'f', gd->y3d, n);
+    put("gd.z3d", 'f', gd->z3d, n);
+  }
 
   put_i("md.medium_type", md->medium_type);
   put_i("md.visco_type", md->visco_type);
@@ -303,6 +309,7 @@ static void dump_outputs(gd_t *gd, bdry_t *bdry, wav_t *wav,
     put("out.matVx2Vz2", 'f', bdry->matVx2Vz2, n2);
     put("out.matVy2Vz2", 'f', bdry->matVy2Vz2, n2);
     put("out.matF2Vz2", 'f', bdry->matF2Vz2, n2);
+    if (bdry->matD) put("out.matD", 'f', bdry->matD, n2);
   }
   for (int r = 0; r < iorecv->total_number; r++) {
     char nm[48];

@@ -63,6 +63,33 @@ CASES = {
         stations=[(5.0 + 2 * n, 14.0, 0.0, 1) for n in range(10)],
         lines=[dict(start=(0, 14, 23), incre=(3, 0, 0), count=10)],
     ),
+    # VTI medium (the reference's built-in VTI test medium, perturbed +-10 %
+    # per point by the seed) on the same curvilinear topography
+    "vti_topo_noise": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_vti",
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        free=True, seed=4242, steps=9, dt=0.004,
+        src=dict(kind="force+moment", loc=(8.3, 7.6, 4.0), spatial="gauss",
+                 f=(1e15, -2e15, 3e15), m=(1e16, 2e16, -1e16, 0.5e16, -0.3e16, 0.2e16),
+                 fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1), (12.0, 6.0, 3.4, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
+    # GMB visco-elastic isotropic medium with three Maxwell bodies (the
+    # reference's built-in test medium: Qp 80, Qs 40), seeded noise state
+    # including the memory variables
+    "visco_topo_noise": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="viscoelastic_iso",
+        visco=dict(type="gmb", number_of_maxwell=3, min_freq=0.5, max_freq=5.0,
+                   refer_freq=1.58),
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        free=True, seed=9191, steps=9, dt=0.004,
+        src=dict(kind="force+moment", loc=(8.3, 7.6, 4.0), spatial="gauss",
+                 f=(1e15, -2e15, 3e15), m=(1e16, 2e16, -1e16, 0.5e16, -0.3e16, 0.2e16),
+                 fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1), (12.0, 6.0, 3.4, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
     # no free surface: PML on all six faces (z2 face included), noise state
     "iso_box_pml6": dict(
         ni=16, nj=14, nk=12, dh=100.0, topo=False, medium="elastic_iso",
@@ -139,6 +166,7 @@ def write_par(path, c, work):
         "is_export_metric": 0,
         "medium": {"type": c["medium"], "input_way": "code", "code": "x",
                    "equivalent_medium_method": "loc"},
+        **({"visco_config": c["visco"]} if "visco" in c else {}),
         "is_export_media": 0,
         "media_export_dir": work,
         "in_source_file": os.path.join(work, "case.src"),

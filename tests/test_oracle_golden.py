@@ -51,3 +51,32 @@ def test_planted_error_is_detected():
     p.media["mu"][q] = np.nextafter(p.media["mu"][q], np.float32(np.inf))
     oracle.allstep(p, oracle.TIMG_ZERO, 1)
     assert not np.array_equal(p.level(p.final_level()), exp["wav"])
+
+
+@pytest.mark.parametrize("case", [c for c in GOLDEN_CASES
+                                  if c.startswith(("vti", "visco", "iso_topo"))])
+def test_surface_matrices_match_reference(case):
+    """Free-surface conversion matrices (and the visco rotation matrix)."""
+    p, exp = P.from_golden(os.path.join(GOLDEN, case + ".npz"))
+    got = oracle.surface_matrices(p)
+    for k, v in got.items():
+        np.testing.assert_array_equal(v, exp[k], err_msg=k)
+
+
+def test_visco_attenuation_is_exercised():
+    """Zeroing the relaxation frequencies changes the visco result, so the
+    fixture checks the memory-variable terms."""
+    p, exp = P.from_golden(os.path.join(GOLDEN, "visco_topo_noise.npz"))
+    p.wl = np.zeros_like(p.wl)
+    oracle.allstep(p, oracle.TIMG_ZERO, 2)
+    got = p.level(p.final_level())
+    assert np.abs(got - exp["wav"]).max() > 1e-6 * np.abs(exp["wav"]).max()
+
+
+def test_vti_differs_from_iso_formulas():
+    """A planted error in one VTI constant (c13 scaled by 1.0001) is
+    detected by the fixture."""
+    p, exp = P.from_golden(os.path.join(GOLDEN, "vti_topo_noise.npz"))
+    p.media["c13"] = p.media["c13"] * np.float32(1.0001)
+    oracle.allstep(p, oracle.TIMG_ZERO, 2)
+    assert not np.array_equal(p.level(p.final_level()), exp["wav"])
