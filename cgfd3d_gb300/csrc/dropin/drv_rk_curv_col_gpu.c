@@ -11,6 +11,7 @@
  *   wav->v5d         final state in level 0 (nt_total even) or 3 (odd)
  *   bdry->auxvar[][].var   final PML auxiliaries, same level rule
  *   bdry->matVx2Vz2/matVy2Vz2/matF2Vz2   free-surface matrices
+ *   bdry->matD       visco-elastic surface rotation matrices
  *   iorecv->recvone[r].seismo, ioline->recv_seismo[l]   seismograms
  *   PGV/PGA/PGD surface maps (forward/wav_t.c:379-455), computed on the
  *   device every step and, inside the reference binary, written by its
@@ -252,6 +253,9 @@ void drv_rk_curv_col_allstep(
       cgfd_solver_fetch_surface_matrices(s, bdry->matVx2Vz2, bdry->matVy2Vz2,
                                           bdry->matF2Vz2) != 0)
     fail("free-surface matrices");
+  if (p.free_top && md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO && bdry->matD &&
+      cgfd_solver_fetch_surface_rotation(s, bdry->matD) != 0)
+    fail("free-surface rotation matrices");
 #ifdef CGFD_DROPIN_REFERENCE_HEADERS
   if (p.free_top) {
     float *PG = (float *)calloc((size_t)15 * gd->nx * gd->ny, sizeof(float));

@@ -241,14 +241,30 @@ def build_reference_structs(p):
     gd.siz_iy = gd.siz_line = p.nx
     gd.siz_iz = gd.siz_slice = p.nx * p.ny
     gd.siz_icmp = gd.siz_volume = p.vol
+    for n in ("x3d", "y3d", "z3d"):
+        if n in p.coords:
+            setattr(gd, n, _fp(p.coords[n]))
     met = Metric()
     for n, v in p.metric.items():
         setattr(met, n, _fp(v))
     md = Md()
     md.medium_type = p.medium_type
     md.rho = _fp(p.media["slw"])
-    md.lambda_ = _fp(p.media["lambda"])
-    md.mu = _fp(p.media["mu"])
+    if "lambda" in p.media:
+        md.lambda_ = _fp(p.media["lambda"])
+        md.mu = _fp(p.media["mu"])
+    for n in ("c11", "c13", "c33", "c55", "c66"):
+        if n in p.media:
+            setattr(md, n, _fp(p.media[n]))
+    if p.nmaxwell > 0:
+        md.nmaxwell = p.nmaxwell
+        md.visco_type = 2                     # CONST_VISCO_GMB
+        md.wl = _fp(p.wl)
+        yl = (PF * p.nmaxwell)(*[_fp(a) for a in p.Ylam])
+        ym = (PF * p.nmaxwell)(*[_fp(a) for a in p.Ymu])
+        keep["Y"] = (yl, ym)
+        md.Ylam = C.cast(yl, PPF)
+        md.Ymu = C.cast(ym, PPF)
     src = Src()
     s = p.src
     if s is not None and s["n"] > 0:
@@ -268,9 +284,9 @@ def build_reference_structs(p):
     bd.is_sides_free[2][1] = int(p.free_top)
     bd.is_enable_free = int(p.free_top)
     n2 = p.nx * p.ny * 9
-    mats = [np.zeros(n2, np.float32) for _ in range(3)]
+    mats = [np.zeros(n2, np.float32) for _ in range(4)]
     keep["mats"] = mats
-    bd.matVx2Vz2, bd.matVy2Vz2, bd.matF2Vz2 = [_fp(m) for m in mats]
+    bd.matVx2Vz2, bd.matVy2Vz2, bd.matF2Vz2, bd.matD = [_fp(m) for m in mats]
     for d in range(3):
         for sd in range(2):
             f = p.pml[d][sd]

@@ -39,7 +39,10 @@ def test_dropin_matches_reference(case):
     if "line" in exp:
         assert_parity(keep["line"][2], exp["line"], case + " lines")
     if "matVx2Vz2" in exp:
-        for m, n in zip(keep["mats"], ["matVx2Vz2", "matVy2Vz2", "matF2Vz2"]):
+        names = ["matVx2Vz2", "matVy2Vz2", "matF2Vz2"]
+        if p.nmaxwell > 0:
+            names.append("matD")
+        for m, n in zip(keep["mats"], names):
             # the free-surface matrices are computed once: tighter bound
             np.testing.assert_allclose(m, exp[n], rtol=2e-5,
                                        atol=2e-6 * np.abs(exp[n]).max())
