@@ -1,16 +1,21 @@
 #!/usr/bin/env python
 """Benchmark of the CGFD3D time-stepping hot path on GB300.
 
-Metric: grid-point RK-stage updates per second (N_phys * 4 * steps / time)
-on the curvilinear-topography isotropic workload (400 x 400 x 200 physical
-points, CFS-PML 12 layers on five faces, traction-image free surface, a
-double-couple source and 400 surface receivers), synthetic and seeded.
+Metric: grid-point RK-stage updates per second (N_phys * 4 * steps / time).
+Default workload: the curvilinear-topography isotropic model (400 x 400 x
+200 physical points, CFS-PML 12 layers on five faces, traction-image free
+surface, a double-couple source and 400 surface receivers), synthetic and
+seeded.  --workload vti / visco run the same topography at 300 x 300 x 150
+with a VTI or a GMB visco-elastic (3 Maxwell bodies) medium; --workload flat
+the 100 x 100 x 60 flat model.
 
-One "step" is one RK4 time step (four stage kernels + the receiver gather)
-of the whole model, with every input resident in HBM (~7 GB, far larger than
-the 129 MB L2, so no flush is needed between steps).
+One "step" is one RK4 time step (four stage kernels, the CFS-PML face
+kernels, the surface and receiver kernels) of the whole model, with every
+input resident in HBM (several GB, far larger than the 129 MB L2, so no
+flush is needed between steps).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload topo|vti|visco|flat]
 
 Multi-GPU runs (torchrun, one rank per GPU) are independent replicas of the
 whole model: the single-domain path keeps the domain on one GPU, so ranks
@@ -32,9 +37,17 @@ sys.path.insert(0, REPO)
 
 METRIC = "grid-pt RK-stage updates/s"
 UNIT = "pt-stage/s"
-BYTES_PER_PT_STAGE = 192       # algorithmic HBM bytes per point-stage (iso)
-WORKLOAD = dict(ni=400, nj=400, nk=200)
+# algorithmic HBM bytes per point-stage, RK-stage average: wavefield
+# components (stage 0: pre r, tmp w, end w; stages 1-2: cur, pre, end r, tmp,
+# end w; stage 3: cur, end r, end w) plus the per-point coefficients (9
+# metrics + media), float32.  iso 36+12, vti 36+15, visco 108+18 floats.
+BYTES_PER_PT_STAGE = {"topo": 192, "flat": 192, "vti": 204, "visco": 504}
+WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
+             "vti": dict(ni=300, nj=300, nk=150),
+             "visco": dict(ni=300, nj=300, nk=150),
+             "flat": dict(ni=100, nj=100, nk=60)}
 SAMPLE_NK = 24                 # CPU sample: same model, 24 planes deep
+CPU_SAMPLE_S = 12.0            # target seconds of CPU work per baseline sample
 
 
 def parse():
@@ -44,10 +57,15 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ni", type=int, default=WORKLOAD["ni"])
-    ap.add_argument("--nj", type=int, default=WORKLOAD["nj"])
-    ap.add_argument("--nk", type=int, default=WORKLOAD["nk"])
-    return ap.parse_args()
+    ap.add_argument("--workload", default="topo", choices=sorted(WORKLOADS))
+    ap.add_argument("--ni", type=int, default=None)
+    ap.add_argument("--nj", type=int, default=None)
+    ap.add_argument("--nk", type=int, default=None)
+    a = ap.parse_args()
+    for k in ("ni", "nj", "nk"):
+        if getattr(a, k) is None:
+            setattr(a, k, WORKLOADS[a.workload][k])
+    return a
 
 
 def dist_env():
@@ -128,10 +146,11 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_per_point_stage():
+def traffic_per_point_stage(workload):
     """DRAM bytes per point-stage of the stage kernel from the committed ncu
-    summary (profiles/k_stage_topo_traffic.json), or None."""
-    path = os.path.join(REPO, "profiles", "k_stage_topo_traffic.json")
+    summary (profiles/k_stage_<workload>_traffic.json), or None."""
+    name = "topo" if workload in ("topo", "flat") else workload
+    path = os.path.join(REPO, "profiles", "k_stage_%s_traffic.json" % name)
     try:
         with open(path) as f:
             return float(json.load(f)["dram_bytes_per_point_stage"])
@@ -145,8 +164,25 @@ def traffic_per_point_stage():
 
 def build_model(args, steps, nk=None):
     from cgfd3d_gb300 import models
-    return models.topo_model(ni=args.ni, nj=args.nj, nk=nk or args.nk,
-                             steps=steps, dt=0.01, nrecv=400)
+    nk = nk or args.nk
+    if args.workload == "flat":
+        return models.flat_model(ni=args.ni, nj=args.nj, nk=nk, steps=steps)
+    if args.workload in ("vti", "visco"):
+        return models.topo_media_model(args.workload, ni=args.ni, nj=args.nj,
+                                       nk=nk, steps=steps, dt=0.005, nrecv=400)
+    return models.topo_model(ni=args.ni, nj=args.nj, nk=nk, steps=steps,
+                             dt=0.01, nrecv=400)
+
+
+def workload_name(args):
+    return {"topo": "topography iso %dx%dx%d, CFS-PML 12 on 5 faces, timg free "
+                    "surface, DC point source, 400 receivers",
+            "vti": "topography VTI %dx%dx%d (Thomsen eps,delta,gamma, 5%% GRF), "
+                   "CFS-PML 12, timg free surface, DC source, 400 receivers",
+            "visco": "topography visco-elastic GMB 3 bodies %dx%dx%d (Qp 200, Qs "
+                     "100), CFS-PML 12, timg free surface, DC source, 400 receivers",
+            "flat": "flat iso %dx%dx%d, CFS-PML 10, timg free surface, explosive "
+                    "source, 20 receivers"}[args.workload] % (args.ni, args.nj, args.nk)
 
 
 def pin_problem(p):
@@ -167,21 +203,33 @@ def pin_problem(p):
         p.metric[k] = pinned(p.metric[k])
     for k in list(p.media):
         p.media[k] = pinned(p.media[k])
+    p.Ylam = [pinned(a) for a in p.Ylam]
+    p.Ymu = [pinned(a) for a in p.Ymu]
     p.wav = pinned(p.wav)
     return holders
 
 
 def cpu_rate(args, steps, threads):
-    """Oracle (CPU port of the reference path) on a bounded sample."""
+    """Oracle (CPU port of the reference path) on a bounded sample: `steps`
+    RK4 steps of the workload's model cut to SAMPLE_NK planes."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     oracle.build()
-    p = build_model(args, steps - 1, nk=SAMPLE_NK)
+    p = build_model(args, steps - 1, nk=min(SAMPLE_NK, args.nk))
     t0 = time.perf_counter()
     oracle.allstep(p, oracle.TIMG_ZERO, threads)
     t = time.perf_counter() - t0
     n = p.ni * p.nj * p.nk * 4 * p.nt_total
     return n / t, t, p
+
+
+def cpu_sample(args, threads):
+    """CPU baseline sized to about CPU_SAMPLE_S seconds: one step to gauge
+    the rate, then as many steps as fit.  Returns (rate, seconds, steps)."""
+    r1, t1, _ = cpu_rate(args, 1, threads)
+    steps = max(1, min(400, int(math.ceil(CPU_SAMPLE_S / max(t1, 1e-3)))))
+    r, t, _ = cpu_rate(args, steps, threads)
+    return r, t, steps
 
 
 def run_reference(args):
@@ -199,17 +247,17 @@ def run_reference(args):
         rates.append(r)
         tot += t
     rate = args.steps / sum(1.0 / r for r in rates)
-    sample = ("one RK4 step of the %dx%dx%d topography model (same generator, "
+    sample = ("one RK4 step per timed step of the %s model (same generator, "
               "nk cut to %d), C oracle port, %d threads" %
-              (args.ni, args.nj, args.nk, SAMPLE_NK, threads))
+              (args.workload, min(SAMPLE_NK, args.nk), threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": "topography iso %dx%dx%d (CPU sample nk=%d)" %
-                   (args.ni, args.nj, args.nk, SAMPLE_NK)},
+        "config": {"workload": workload_name(args) + " (CPU sample nk=%d)" %
+                   min(SAMPLE_NK, args.nk)},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -261,9 +309,10 @@ def run_ours(args):
     # ---- roofline of the stage kernel -----------------------------------
     peak, peak_kind = measured_peak_hbm()
     avg_launch = t_stage * 1e-3 / n_stage
-    alg_bytes = n_phys * BYTES_PER_PT_STAGE
+    bpps = BYTES_PER_PT_STAGE[args.workload]
+    alg_bytes = n_phys * bpps
     achieved = alg_bytes / avg_launch / 1e9
-    tpp = traffic_per_point_stage()
+    tpp = traffic_per_point_stage(args.workload)
 
     # ---- end to end through the C ABI with host (pinned) buffers ---------
     q = build_model(args, K - 1)
@@ -294,9 +343,7 @@ def run_ours(args):
         "steps": K, "warmup": W, "ms_per_step": 1e3 * t / K,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": "topography iso %dx%dx%d, CFS-PML 12 on 5 faces, "
-                   "timg free surface, DC point source, 400 receivers" %
-                   (args.ni, args.nj, args.nk),
+        "config": {"workload": workload_name(args),
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs (%.1f GB resident) larger than L2, no flush"
                          % (solver.device_bytes(p) / 1e9)},
@@ -307,7 +354,7 @@ def run_ours(args):
                      "alg_bytes_per_launch": alg_bytes,
                      "avg_launch_ms": avg_launch * 1e3,
                      "kernel": "k_stage3 (interior stage)",
-                     "whole_step_frac": value / world * BYTES_PER_PT_STAGE / 1e9 / peak},
+                     "whole_step_frac": value / world * bpps / 1e9 / peak},
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": h2d / q.nt_total,
                 "d2h_bytes_per_step": d2h / q.nt_total,
@@ -317,11 +364,12 @@ def run_ours(args):
     }
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        r, tcpu, _ = cpu_rate(args, 1, threads)
+        r, tcpu, nst = cpu_sample(args, threads)
         line["cpu_baseline"] = {
             "value": r, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "one RK4 step of the same model cut to nk=%d, C oracle "
-                      "port, %d threads, %.1f s" % (SAMPLE_NK, threads, tcpu)}
+            "sample": "%d RK4 steps of the same model cut to nk=%d, C oracle "
+                      "port, %d threads, %.1f s" % (nst, min(SAMPLE_NK, args.nk),
+                                                    threads, tcpu)}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

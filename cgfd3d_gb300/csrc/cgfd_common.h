@@ -95,6 +95,7 @@ struct StageArgs {
   const int *d_it;             /* current step on the device */
   int istage;
   int *err;                    /* device error word (bounded waits) */
+  int pml_fused;               /* CFS-PML inside the stage kernel (else face kernels) */
   int cur_level;               /* level index of `cur` (TMA coordinate) */
   int pre_level, end_level;    /* level indices of `pre` and `end` */
   int kchunk;                  /* planes per CTA along k */

@@ -574,6 +574,7 @@ struct cgfd_solver {
   float *pg, *dis;              /* surface peak-motion maps (free top) */
   StageMaps maps;               /* tensor maps of the stage kernel */
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
+  int pml_fused;                /* 1: CFS-PML inside the stage kernel */
   int kchunk;
 };
 
@@ -1017,6 +1018,14 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   /* the direct-load A/B kernel (cgfd_stage.cuh) covers isotropic media only */
   if (const char *e = getenv("CGFD_STAGE_KERNEL"))
     s->kernel = (atoi(e) == 1 && s->med == MED_ISO) ? 1 : 2;
+  /* CFS-PML inside the stage kernel or by the per-face kernels after it.
+   * Measured on GB300 (topography model, 12 layers): isotropic media are
+   * faster split (the fused PML lengthens the latency-bound consumer warps
+   * more than the face kernels cost), VTI and visco-elastic media fused
+   * (their face kernels re-read more per point).  CGFD_PML_SPLIT=1 / 0
+   * forces either form. */
+  s->pml_fused = s->med != MED_ISO;
+  if (const char *e = getenv("CGFD_PML_SPLIT")) s->pml_fused = atoi(e) == 1 ? 0 : 1;
   {
     int tiles = ((g.ni + s2::TX - 1) / s2::TX) * ((g.nj + s2::TY - 1) / s2::TY);
     int want = 8 * 152;                     /* about eight waves of CTAs */
@@ -1161,6 +1170,7 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   a.istage = istage;
   a.err = s->d_err;
   a.kchunk = s->kchunk;
+  a.pml_fused = s->pml_fused;
   size_t L = level_floats(s);
   a.cur_level = (int)((cur - s->wav) / (long long)L);
   a.pre_level = (int)((pre - s->wav) / (long long)L);
@@ -1184,7 +1194,7 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
     launch_stage(s, code, kind, st, a);
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
-    if (s->kernel == 2) launch_pml_faces(s, kind, bx, by, bz, st, a);
+    if (s->kernel == 2 && !s->pml_fused) launch_pml_faces(s, kind, bx, by, bz, st, a);
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
   }
   size_t L = level_floats(s);
@@ -1247,7 +1257,7 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   for (int f = 0; f < CGFD_NFACE; f++) nfaces += s->face[f].on;
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
-  s->n_pml = s->kernel == 2 ? 4 * nfaces * nsteps : 0;
+  s->n_pml = (s->kernel == 2 && !s->pml_fused) ? 4 * nfaces * nsteps : 0;
   s->n_other = nsteps * (1 + (s->pg ? 1 : 0) + (s->med == MED_VIS && s->p->free_top ? 1 : 0));
   int herr = 0;
   CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));

@@ -23,10 +23,17 @@
  * waiting thread records device error 1 (a.err) and goes on, so the kernel
  * always terminates and the host reports the failure.
  *
- * Per point the consumer computes what cgfd_stage.cuh computes except the
- * CFS-PML terms, which the face kernels of cgfd_pml.cuh add afterwards
- * (reference: forward/sv_curv_col_el_iso.c:208-634,
+ * Per point the consumer computes the interior RHS, the traction image and
+ * vlow overwrites at the top layers, the CFS-PML terms of every face that
+ * contains the point (in the reference's face order, with the face's
+ * auxiliary variables advanced in the same pass), the sources and the RK
+ * combine (reference: forward/sv_curv_col_el_iso.c:208-1146,
  * forward/sv_curv_col_el.c:30-479, forward/drv_rk_curv_col.c:292-446).
+ * The auxiliary variables are the only operands read straight from global
+ * memory: they are pointwise (no stencil), and each consumer thread
+ * prefetches its next plane's auxiliaries into L2 one plane ahead so that
+ * the loads of the PML points hit L2.  With a.pml_fused = 0 the PML terms
+ * are left to the face kernels of cgfd_pml.cuh instead.
  *
  * MED selects the medium (cgfd_media.cuh).  VTI changes Hooke's law only
  * (forward/sv_curv_col_el_vti.c:200-590).  The GMB visco-elastic medium
@@ -73,6 +80,126 @@ struct Slot {
 __device__ __forceinline__ void wait_full(uint64_t *bar, uint32_t parity, int *err)
 {
   mbar_wait(bar, parity, err);
+}
+
+/* L2 prefetch of one global address (no register, no completion) */
+__device__ __forceinline__ void prefetch_l2(const float *p)
+{
+  asm volatile("prefetch.global.L2::evict_last [%0];" ::"l"(p));
+}
+
+__device__ __forceinline__ bool in_face(const DevFace &F, int i, int j, int k)
+{
+  return F.on && i >= F.i1 && i <= F.i2 && j >= F.j1 && j <= F.j2 &&
+         k >= F.k1 && k <= F.k2;
+}
+
+/* L2 prefetch of the auxiliary variables a stage reads at (i, j, k) */
+template <int KIND>
+__device__ __forceinline__ void prefetch_aux(const StageArgs &a, int i, int j, int k)
+{
+#pragma unroll 1
+  for (int f = 0; f < CGFD_NFACE; f++) {
+    const DevFace &F = a.face[f];
+    if (!in_face(F, i, j, k)) continue;
+    const long long av = F.avol;
+    const long long ai = (long long)(i - F.i1) + (long long)(j - F.j1) * F.bx +
+                         (long long)(k - F.k1) * F.bx * F.by;
+#pragma unroll
+    for (int c = 0; c < 9; c++) {
+      prefetch_l2(a.acur[f] + c * av + ai);
+      if (KIND == 1) prefetch_l2(a.apre[f] + c * av + ai);
+      if (KIND >= 1) prefetch_l2(a.aend[f] + c * av + ai);
+    }
+  }
+}
+
+/* CFS-PML terms of face f at one point (forward/sv_curv_col_el_iso.c:
+ * 708-1143, VTI forward/sv_curv_col_el_vti.c:592-1075): corrections added
+ * to r, the face's auxiliary variables advanced by the RK stage.  d holds
+ * the nine derivatives along the face normal, e1..e3 that direction's
+ * metric. */
+template <int KIND>
+struct AuxPt {
+  float ac[9], ap[KIND == 1 ? 9 : 1], ae[KIND >= 1 ? 9 : 1];
+};
+
+template <int KIND>
+__device__ __forceinline__ long long aux_index(const DevFace &F, int i, int j, int k)
+{
+  return (long long)(i - F.i1) + (long long)(j - F.j1) * F.bx +
+         (long long)(k - F.k1) * F.bx * F.by;
+}
+
+/* the auxiliary values one stage reads at a face point */
+template <int KIND>
+__device__ __forceinline__ void load_aux(const StageArgs &a, int f, long long ai,
+                                         AuxPt<KIND> &x)
+{
+  const long long av = a.face[f].avol;
+#pragma unroll
+  for (int c = 0; c < 9; c++) {
+    x.ac[c] = __ldg(a.acur[f] + c * av + ai);
+    if (KIND == 1) x.ap[c] = __ldg(a.apre[f] + c * av + ai);
+    if (KIND >= 1) x.ae[c] = a.aend[f][c * av + ai];
+  }
+}
+
+template <int KIND, int MED>
+__device__ __forceinline__ void spml_face(const StageArgs &a, int f, int i,
+                                          int j, int k, long long q,
+                                          const float *d, float e1, float e2,
+                                          float e3, float ztx, float zty,
+                                          float ztz, const MedPt &m,
+                                          const AuxPt<KIND> &x, float *r)
+{
+  const DevFace &F = a.face[f];
+  const long long av = F.avol;
+  const long long ai = aux_index<KIND>(F, i, j, k);
+  const float *ac = x.ac, *ap = x.ap, *ae = x.ae;
+  const int n = F.dim == 0 ? i - F.i1 : (F.dim == 1 ? j - F.j1 : k - F.k1);
+  const float cD = __ldg(F.D + n), cA = __ldg(F.A + n), cB = __ldg(F.B + n);
+  const float cB1 = cB - 1.0f;
+  float sv[9];
+  sv[C_VX] = m.slw * (e1 * d[C_TXX] + e2 * d[C_TXY] + e3 * d[C_TXZ]);
+  sv[C_VY] = m.slw * (e1 * d[C_TXY] + e2 * d[C_TYY] + e3 * d[C_TYZ]);
+  sv[C_VZ] = m.slw * (e1 * d[C_TXZ] + e2 * d[C_TYZ] + e3 * d[C_TZZ]);
+  hooke1<MED>(m, e1, e2, e3, d[C_VX], d[C_VY], d[C_VZ], sv);
+  float arhs[9];
+#pragma unroll
+  for (int c = 0; c < 9; c++) {
+    r[c] += cB1 * sv[c] - cB * ac[c];
+    arhs[c] = cD * sv[c] - cA * ac[c];
+  }
+  if (F.dim < 2 && a.free_top && k == a.g.nk2) {
+    /* free-surface part: the z gradients converted from this direction's
+     * (forward/sv_curv_col_el_iso.c:841-901) */
+    const long long ij = ((long long)i + (long long)j * a.g.nx) * 9;
+    const float *M = (F.dim == 0 ? a.mVx : a.mVy) + ij;
+    float DzVx = __ldg(M + 0) * d[C_VX] + __ldg(M + 1) * d[C_VY] + __ldg(M + 2) * d[C_VZ];
+    float DzVy = __ldg(M + 3) * d[C_VX] + __ldg(M + 4) * d[C_VY] + __ldg(M + 5) * d[C_VZ];
+    float DzVz = __ldg(M + 6) * d[C_VX] + __ldg(M + 7) * d[C_VY] + __ldg(M + 8) * d[C_VZ];
+    float t[9];
+    hooke1<MED>(m, ztx, zty, ztz, DzVx, DzVy, DzVz, t);
+#pragma unroll
+    for (int c = C_TXX; c <= C_TXY; c++) {
+      r[c] += cB1 * t[c];
+      arhs[c] += cD * t[c];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 9; c++) {
+    const long long x = c * av + ai;
+    if (KIND == 0) {
+      a.atmp_out[f][x] = ac[c] + a.ca * arhs[c];
+      a.aend[f][x] = ac[c] + a.cb * arhs[c];
+    } else if (KIND == 1) {
+      a.atmp_out[f][x] = ap[c] + a.ca * arhs[c];
+      a.aend[f][x] = ae[c] + a.cb * arhs[c];
+    } else {
+      a.aend[f][x] = ae[c] + a.cb * arhs[c];
+    }
+  }
 }
 
 template <int BX, int BY, int BZ, int KIND, int MED>
@@ -175,9 +302,30 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     src_e1 = a.src_col[colidx + 1];
   }
 
+  /* faces whose (i, j) range holds this column (x/y faces), and the k
+   * ranges of the z faces, so that points outside every face skip the PML
+   * logic with register tests only */
+  int fmask_xy = 0, kz1_top = -1, kz2_bot = 1 << 30;
+  if (a.pml_fused && valid) {
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+      const DevFace &F = a.face[f];
+      if (F.on && i >= F.i1 && i <= F.i2 && j >= F.j1 && j <= F.j2) fmask_xy |= 1 << f;
+    }
+    if (a.face[4].on) kz1_top = a.face[4].k2;
+    if (a.face[5].on) kz2_bot = a.face[5].k1;
+  }
+  auto in_pml = [&](int kk) {
+    return fmask_xy != 0 || kk <= kz1_top || kk >= kz2_bot;
+  };
+  if (a.pml_fused && valid && in_pml(kbeg)) prefetch_aux<KIND>(a, i, j, kbeg);
+
   for (int it = 0; it < niter; it++) {
     const int k = kbeg + it;
     const int rtop = it + 4;
+    const bool pml_here = a.pml_fused && valid && in_pml(k);
+    if (a.pml_fused && valid && it + 1 < niter && in_pml(k + 1))
+      prefetch_aux<KIND>(a, i, j, k + 1);
 #pragma unroll
     for (int n = 0; n < 5; n++) {
       int rel = rtop - 4 + n;
@@ -271,14 +419,39 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         hooke9<MED>(m, xix, xiy, xiz, etx, ety, etz, ztx, zty, ztz, DxVx, DxVy,
                     DxVz, DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, r);
       }
-#undef DX
-#undef DY
-#undef DZ
       if (a.free_top && k >= g.nk2 - (BZ == 0 ? 3 : 1)) {
         r[C_VX] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 0);
         r[C_VY] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 1);
         r[C_VZ] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 2);
       }
+
+      /* CFS-PML, faces in the reference order x1, x2, y1, y2, z1, z2 */
+      if (pml_here) {
+#pragma unroll 1
+        for (int f = 0; f < CGFD_NFACE; f++) {
+          const DevFace &F = a.face[f];
+          if (!in_face(F, i, j, k)) continue;
+          AuxPt<KIND> pax;
+          load_aux<KIND>(a, f, aux_index<KIND>(F, i, j, k), pax);
+          float d[9];
+          if (F.dim == 0) {
+#pragma unroll
+            for (int c = 0; c < 9; c++) d[c] = DX(c);
+            spml_face<KIND, MED>(a, f, i, j, k, q, d, xix, xiy, xiz, ztx, zty, ztz, m, pax, r);
+          } else if (F.dim == 1) {
+#pragma unroll
+            for (int c = 0; c < 9; c++) d[c] = DY(c);
+            spml_face<KIND, MED>(a, f, i, j, k, q, d, etx, ety, etz, ztx, zty, ztz, m, pax, r);
+          } else {
+#pragma unroll
+            for (int c = 0; c < 9; c++) d[c] = DZ(c);
+            spml_face<KIND, MED>(a, f, i, j, k, q, d, ztx, zty, ztz, ztx, zty, ztz, m, pax, r);
+          }
+        }
+      }
+#undef DX
+#undef DY
+#undef DZ
 
       /* GMB attenuation (forward/sv_curv_col_vis_iso.c:250-347) */
       float hJ[MED == MED_VIS ? 6 * CGFD_VIS_NMW_MAX : 1];

@@ -1,4 +1,4 @@
-"""GPU against the oracle for the VTI and GMB visco-elastic media.
+"""GPU against the oracle for the isotropic, VTI and GMB visco-elastic media.
 
 The oracle is pinned bit-for-bit to the reference for both media
 (test_oracle_golden.py, fixtures vti_topo_noise and visco_topo_noise).  Here
@@ -6,7 +6,8 @@ the GPU library and the oracle run the same synthetic topography model with
 a VTI or a visco-elastic (three Maxwell bodies) medium from a seeded noise
 state -- wavefield, memory variables and PML auxiliaries -- so that every
 operator tap, every boundary branch and the attenuation terms act from the
-first step.  Tolerance: relative L2 <= 1e-5 and max-abs <= 1e-4 of the peak
+first step, with the CFS-PML terms inside the stage kernel and by the face
+kernels.  Tolerance: relative L2 <= 1e-5 and max-abs <= 1e-4 of the peak
 (tests/helpers.py).
 """
 
@@ -53,13 +54,27 @@ def _compare(p_gpu, p_cpu, what):
         assert_parity(p_gpu.recv["seismo"], p_cpu.recv["seismo"], what + " receivers")
 
 
-@pytest.mark.parametrize("kind", ["vti", "visco"])
+@pytest.fixture(params=["default", "fused", "split"])
+def pml_mode(request, monkeypatch):
+    """CFS-PML inside the stage kernel or by the face kernels (both forms
+    must give the same result for every medium)."""
+    if request.param == "fused":
+        monkeypatch.setenv("CGFD_PML_SPLIT", "0")
+    elif request.param == "split":
+        monkeypatch.setenv("CGFD_PML_SPLIT", "1")
+    return request.param
+
+
+@pytest.mark.parametrize("kind", ["iso", "vti", "visco"])
 @pytest.mark.parametrize("shape", [(96, 80, 48), (70, 45, 37)])
-def test_media_model_noise_state(kind, shape):
+def test_media_model_noise_state(kind, shape, pml_mode):
     from cgfd3d_gb300 import models, solver
     ni, nj, nk = shape
-    p = models.topo_media_model(kind, ni=ni, nj=nj, nk=nk, steps=9, dt=0.005,
-                                nrecv=16)
+    if kind == "iso":
+        p = models.topo_model(ni=ni, nj=nj, nk=nk, steps=9, dt=0.005, nrecv=16)
+    else:
+        p = models.topo_media_model(kind, ni=ni, nj=nj, nk=nk, steps=9,
+                                    dt=0.005, nrecv=16)
     _noise(p, 5)
     q = p.copy()
     solver.drv_rk_curv_col_allstep(p)
