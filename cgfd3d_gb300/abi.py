@@ -6,7 +6,7 @@ tests/test_abi.py checks sizes and offsets against a compiled probe.
 
 import ctypes as C
 
-CGFD_ABI_VERSION = 2
+CGFD_ABI_VERSION = 3
 CGFD_MEDIUM_ELASTIC_ISO = 2
 CGFD_MEDIUM_ELASTIC_VTI = 3
 CGFD_MEDIUM_VISCOELASTIC_ISO = 5
@@ -71,7 +71,9 @@ class Problem(C.Structure):
            ("wav", PF),
            ("dt", C.c_float), ("t0", C.c_float),
            ("nt_total", C.c_int),
-           ("x3d", PF), ("y3d", PF), ("z3d", PF)]
+           ("x3d", PF), ("y3d", PF), ("z3d", PF),
+           ("src_force_rate_indx", PI),
+           ("Fx_rate", PF), ("Fy_rate", PF), ("Fz_rate", PF)]
     )
 
 

@@ -49,6 +49,16 @@ struct DevFace {
   const float *A, *B, *D;
 };
 
+/* one surface force source (forward/src_t.c:202-311) */
+struct SurfForce {
+  int is;          /* source index (time window, force table) */
+  int n;           /* surface-force index (rate table) */
+  int si, sj, sk;  /* grid indices */
+  int half;        /* Gaussian half width, 0 for a point force */
+  int w0;          /* offset of its (2 half + 1)^2 surface weights */
+  int pad;
+};
+
 /* one source contribution at one grid point (precomputed on the host) */
 struct SrcEntry {
   int k;          /* plane */
@@ -86,6 +96,9 @@ struct StageArgs {
   /* free surface */
   int free_top;
   const float *mVx, *mVy, *mF, *mD;
+  /* surface force layers of the stage (TxSrc,TySrc,TzSrc / VxSrc,VySrc,
+   * VzSrc, 3 x nx*ny each, forward/src_t.c:153-314), or null */
+  const float *TS, *VS;
   /* sources */
   int src_n, src_max_nt, src_max_stage, src_force, src_moment;
   const int *src_col;          /* (ni*nj + 1) offsets into src_ent */

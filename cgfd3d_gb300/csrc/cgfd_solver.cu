@@ -350,6 +350,47 @@ __global__ void k_vis_free(DevGrid g, float *w, const float *__restrict__ mD)
   w[C_TYZ * v + q] = Tg[1][2];
 }
 
+/* surface force layers of one stage (forward/src_t.c:153-314): per surface
+ * column (i, j) the traction TxSrc..TzSrc and velocity-rate VxSrc..VzSrc
+ * sums over the surface forces active at step *d_it, in source order.  A
+ * point force adds its value at its column (rate over the Jacobian at the
+ * source point), a Gaussian one the surface layer of its weights. */
+__global__ void k_surf_layer(DevGrid g, int nsf, const SurfForce *__restrict__ sf,
+                             const float *__restrict__ wsurf,
+                             const float *__restrict__ jac,
+                             const int *__restrict__ it_begin,
+                             const int *__restrict__ it_end,
+                             const float *__restrict__ Fx, const float *__restrict__ Fy,
+                             const float *__restrict__ Fz, const float *__restrict__ Rx,
+                             const float *__restrict__ Ry, const float *__restrict__ Rz,
+                             int max_nt, int max_stage, int istage,
+                             const int *__restrict__ d_it, float *TS, float *VS)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  const int it = *d_it;
+  const long long n2 = (long long)g.nx * g.ny, i2 = i + (long long)j * g.nx;
+  float t[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+  for (int n = 0; n < nsf; n++) {
+    const SurfForce f = sf[n];
+    if (it < it_begin[f.is] || it > it_end[f.is]) continue;
+    const int di = i - f.si, dj = j - f.sj;
+    if (di < -f.half || di > f.half || dj < -f.half || dj > f.half) continue;
+    const long long tt = ((long long)f.is * max_nt + (it - it_begin[f.is])) * max_stage + istage;
+    const long long tr = ((long long)f.n * max_nt + (it - it_begin[f.is])) * max_stage + istage;
+    const int k = f.half == 0 ? f.sk : g.nk2;
+    const float rj = 1.0f / jac[(i + g.xoff) + (long long)j * g.px + (long long)k * g.sl];
+    const float c = f.half == 0 ? 1.0f : wsurf[f.w0 + (dj + f.half) * (2 * f.half + 1) + di + f.half];
+    t[0] += Fx[tt] * c; t[1] += Fy[tt] * c; t[2] += Fz[tt] * c;
+    v[0] += Rx[tr] * c * rj; v[1] += Ry[tr] * c * rj; v[2] += Rz[tr] * c * rj;
+  }
+  for (int m = 0; m < 3; m++) {
+    TS[m * n2 + i2] = t[m];
+    VS[m * n2 + i2] = v[m];
+  }
+}
+
 /* receivers and lines after a step; one block; advances the step counter.
  * Trilinear weights as forward/io_funcs.c:1595-1612, which uses corner 5
  * twice and corner 4 never (harmless for receivers on a grid plane). */
@@ -553,6 +594,11 @@ struct cgfd_solver {
   int *src_col, *src_it_begin, *src_it_end;
   SrcEntry *src_ent;
   float *stf;                   /* 9 tables */
+  int nsf;                      /* surface force sources */
+  SurfForce *sf;                /* their descriptors */
+  float *sf_w;                  /* their surface-layer Gaussian weights */
+  float *frate;                 /* 3 force-rate tables */
+  float *surf;                  /* 6 x nx*ny: TxSrc..TzSrc, VxSrc..VzSrc */
   float *recv_dijk, *recv_seismo, *line_seismo;
   int *recv_idx, *line_iptr;
   int *d_it;
@@ -640,8 +686,17 @@ static int validate(const cgfd_problem_t *p)
     return set_err(CGFD_EINVAL, "grid indices are not the 3-ghost layout");
   if (p->ni < 8 || p->nj < 8 || p->nk < 8)
     return set_err(CGFD_EINVAL, "grid too small (ni,nj,nk >= 8 required)");
-  if (p->src_n > 0 && p->src_n_surface_force > 0)
-    return set_err(CGFD_EINVAL, "surface force sources are not supported");
+  if (p->src_n > 0 && p->src_n_surface_force > 0) {
+    if (!p->src_force || !p->src_force_rate_indx || !p->Fx_rate || !p->Fy_rate ||
+        !p->Fz_rate)
+      return set_err(CGFD_EINVAL, "surface force sources need the force and "
+                     "force-rate tables");
+    if (!p->free_top)
+      return set_err(CGFD_EINVAL, "surface force sources need a free surface");
+    for (int n = 0; n < p->src_n_surface_force; n++)
+      if (p->src_force_rate_indx[n] < 0 || p->src_force_rate_indx[n] >= p->src_n)
+        return set_err(CGFD_EINVAL, "surface force %d: bad source index", n);
+  }
   if (!p->jac || !p->xi_x || !p->slw || !p->wav)
     return set_err(CGFD_EINVAL, "missing input array");
   if (p->medium_type != CGFD_MEDIUM_ELASTIC_VTI && (!p->lambda || !p->mu))
@@ -803,7 +858,8 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
   void *ptrs[] = {s->wav, s->metric, s->media, s->mats, s->src_col,
                   s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
                   s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
-                  s->line_iptr, s->d_it, s->d_flag, s->d_err, s->pg, s->dis};
+                  s->line_iptr, s->d_it, s->d_flag, s->d_err, s->pg, s->dis,
+                  s->sf, s->sf_w, s->frate, s->surf};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (int f = 0; f < CGFD_NFACE; f++)
@@ -980,6 +1036,49 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     for (int t = 0; t < 9; t++)
       if (use[t] && tabs[t])
         TRYC(cudaMemcpyAsync(s->stf + t * nstf, tabs[t], nstf * 4, cudaMemcpyHostToDevice, st));
+    if (p->src_n_surface_force > 0) {
+      /* surface forces: descriptors, surface-layer weights, rate tables */
+      int nsf = p->src_n_surface_force;
+      std::vector<SurfForce> sfv(nsf);
+      std::vector<float> wv;
+      for (int n = 0; n < nsf; n++) {
+        int is = p->src_force_rate_indx[n];
+        SurfForce &f = sfv[n];
+        f.is = is; f.n = n;
+        f.si = p->src_si[is]; f.sj = p->src_sj[is]; f.sk = p->src_sk[is];
+        f.half = p->src_spatial == CGFD_SRC_POINT ? 0 : p->src_ext_half;
+        f.w0 = (int)wv.size();
+        f.pad = 0;
+        if (f.half > 0) {
+          int half = f.half, len = 2 * half + 1;
+          int kx = p->nk2 - f.sk;
+          std::vector<float> w3;
+          gauss_weights(w3, p->src_si_inc[is], p->src_sj_inc[is], p->src_sk_inc[is],
+                        p->src_ext_coef, half, kx);
+          size_t off = (size_t)(kx + half) * len * len;
+          if (kx < -half || kx > half) {
+            set_err(CGFD_EINVAL, "surface force %d does not reach the surface", n);
+            cgfd_solver_destroy(s);
+            return CGFD_EINVAL;
+          }
+          wv.insert(wv.end(), w3.begin() + off, w3.begin() + off + len * len);
+        }
+      }
+      s->nsf = nsf;
+      TRY(dalloc(s, &s->sf, nsf));
+      TRYC(cudaMemcpyAsync(s->sf, sfv.data(), nsf * sizeof(SurfForce), cudaMemcpyHostToDevice, st));
+      TRY(dalloc(s, &s->sf_w, wv.empty() ? 1 : wv.size()));
+      if (!wv.empty())
+        TRYC(cudaMemcpyAsync(s->sf_w, wv.data(), wv.size() * 4, cudaMemcpyHostToDevice, st));
+      size_t nr = (size_t)nsf * p->src_max_nt * p->src_max_stage;
+      TRY(dalloc(s, &s->frate, 3 * nr));
+      const float *rt[3] = {p->Fx_rate, p->Fy_rate, p->Fz_rate};
+      for (int m = 0; m < 3; m++)
+        TRYC(cudaMemcpyAsync(s->frate + m * nr, rt[m], nr * 4, cudaMemcpyHostToDevice, st));
+      TRY(dalloc(s, &s->surf, 6 * (size_t)g.nx * g.ny));
+      TRYC(cudaMemsetAsync(s->surf, 0, 6 * (size_t)g.nx * g.ny * sizeof(float), st));
+      cudaStreamSynchronize(st);       /* host vectors go out of scope */
+    }
   }
   /* receivers and lines */
   if (p->recv_n > 0) {
@@ -1017,7 +1116,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   s->kernel = 2;
   /* the direct-load A/B kernel (cgfd_stage.cuh) covers isotropic media only */
   if (const char *e = getenv("CGFD_STAGE_KERNEL"))
-    s->kernel = (atoi(e) == 1 && s->med == MED_ISO) ? 1 : 2;
+    s->kernel = (atoi(e) == 1 && s->med == MED_ISO && s->nsf == 0) ? 1 : 2;
   /* CFS-PML inside the stage kernel or by the per-face kernels after it.
    * Measured on GB300 (topography model, 12 layers): isotropic media are
    * faster split (the fused PML lengthens the latency-bound consumer warps
@@ -1150,6 +1249,11 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
     size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
     a.mVx = s->mats; a.mVy = s->mats + n2; a.mF = s->mats + 2 * n2;
     a.mD = s->med == MED_VIS ? s->mats + 3 * n2 : nullptr;
+    if (s->surf) {
+      size_t s2n = (size_t)s->g.nx * s->g.ny;
+      a.TS = s->surf;
+      a.VS = s->surf + 3 * s2n;
+    }
   }
   if (p->src_n > 0) {
     a.src_n = p->src_n;
@@ -1191,6 +1295,19 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
     int bz = (PAIR_FLAGS[ipair][2] + is) % 2;
     int kind = is == 0 ? 0 : (is < 3 ? 1 : 2);
     int code = bx * 4 + by * 2 + bz;
+    if (s->nsf > 0) {
+      /* surface force layers of this stage (drv_rk_curv_col.c:230) */
+      dim3 b2(32, 8), g2((s->g.ni + 31) / 32, (s->g.nj + 7) / 8);
+      size_t nstf = (size_t)p->src_n * p->src_max_nt * p->src_max_stage;
+      size_t nr = (size_t)s->nsf * p->src_max_nt * p->src_max_stage;
+      size_t s2n = (size_t)s->g.nx * s->g.ny;
+      k_surf_layer<<<g2, b2, 0, st>>>(s->g, s->nsf, s->sf, s->sf_w, s->metric,
+                                      s->src_it_begin, s->src_it_end, s->stf,
+                                      s->stf + nstf, s->stf + 2 * nstf, s->frate,
+                                      s->frate + nr, s->frate + 2 * nr,
+                                      p->src_max_nt, p->src_max_stage, is, s->d_it,
+                                      s->surf, s->surf + 3 * s2n);
+    }
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
     launch_stage(s, code, kind, st, a);
     if (ev_next) cudaEventRecord(s->kev[(*ev_next)++], st);
@@ -1258,7 +1375,8 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   s->t_other_ms = s->timing ? ms - s->t_stage_ms : 0.f;
   s->n_stage = 4 * nsteps;
   s->n_pml = (s->kernel == 2 && !s->pml_fused) ? 4 * nfaces * nsteps : 0;
-  s->n_other = nsteps * (1 + (s->pg ? 1 : 0) + (s->med == MED_VIS && s->p->free_top ? 1 : 0));
+  s->n_other = nsteps * (1 + (s->pg ? 1 : 0) + (s->med == MED_VIS && s->p->free_top ? 1 : 0) +
+                         (s->nsf > 0 ? 4 : 0));
   int herr = 0;
   CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));
   if (herr) return set_err(CGFD_ECUDA, "device wait timed out (code %d)", herr);

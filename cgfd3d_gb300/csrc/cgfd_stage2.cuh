@@ -192,7 +192,7 @@ __device__ __forceinline__ float scons(const StageArgs &a, const float *P,
 template <int BX, int BY, int BZ>
 __device__ float stimg_row(const StageArgs &a, const Win &w,
                            const float *cen, int row, int col, long long q,
-                           int k, int r)
+                           int k, int r, float ts)
 {
   const long long px = a.g.px, sl = a.g.sl;
   int ca, cb, cc;
@@ -218,14 +218,15 @@ __device__ float stimg_row(const StageArgs &a, const Win &w,
       v = scons(a, w.at(n), ca, cb, cc, row, col, q + (long long)(kk - k) * sl,
                 a.ztx, a.zty, a.ztz);
     } else if (kk == nk2) {
-      v = 0.f;
+      v = ts;                     /* surface traction (TxSrc/TySrc/TzSrc) */
     } else {
       int km = 2 * nk2 - kk;
-      /* image point km lies inside the 5-plane window whenever km >= klow */
-      v = (km >= klow)
-              ? -scons(a, w.at(km - klow), ca, cb, cc, row, col,
-                       q + (long long)(km - k) * sl, a.ztx, a.zty, a.ztz)
-              : 0.f;
+      /* mirror 2 ts - flux(km); the image point km lies inside the 5-plane
+       * window whenever km >= klow (else the reference reads zeros) */
+      v = 2.0f * ts -
+          ((km >= klow) ? scons(a, w.at(km - klow), ca, cb, cc, row, col,
+                                q + (long long)(km - k) * sl, a.ztx, a.zty, a.ztz)
+                        : 0.f);
     }
     Dz += tap_coef<BZ>(n) * v;
   }

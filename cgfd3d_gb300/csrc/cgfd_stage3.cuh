@@ -390,6 +390,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                    LDG(Bm + 3) * DyVx + LDG(Bm + 4) * DyVy + LDG(Bm + 5) * DyVz;
             DzVz = LDG(A + 6) * DxVx + LDG(A + 7) * DxVy + LDG(A + 8) * DxVz +
                    LDG(Bm + 6) * DyVx + LDG(Bm + 7) * DyVy + LDG(Bm + 8) * DyVz;
+            if (MED != MED_VTI && a.VS) {
+              /* surface force: matF2Vz (VxSrc, VySrc, VzSrc)
+               * (forward/sv_curv_col_el_iso.c:583-592) */
+              const long long n2 = (long long)g.nx * g.ny, i2 = i + (long long)j * g.nx;
+              const float vx = a.VS[i2], vy = a.VS[n2 + i2], vz = a.VS[2 * n2 + i2];
+              const float *F = a.mF + ij;
+              DzVx += LDG(F + 0) * vx + LDG(F + 1) * vy + LDG(F + 2) * vz;
+              DzVy += LDG(F + 3) * vx + LDG(F + 4) * vy + LDG(F + 5) * vz;
+              DzVz += LDG(F + 6) * vx + LDG(F + 7) * vy + LDG(F + 8) * vz;
+            }
           } else if (k == nk2 - 1) {
             const float *lo = BZ == 0 ? w.at(ZC) : w.at(ZC - 1);
             const float *hi = BZ == 0 ? w.at(ZC + 1) : w.at(ZC);
@@ -420,9 +430,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                     DxVz, DyVx, DyVy, DyVz, DzVx, DzVy, DzVz, r);
       }
       if (a.free_top && k >= g.nk2 - (BZ == 0 ? 3 : 1)) {
-        r[C_VX] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 0);
-        r[C_VY] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 1);
-        r[C_VZ] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 2);
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        if (a.TS) {
+          const long long n2 = (long long)g.nx * g.ny, i2 = i + (long long)j * g.nx;
+          tx = a.TS[i2]; ty = a.TS[n2 + i2]; tz = a.TS[2 * n2 + i2];
+        }
+        r[C_VX] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 0, tx);
+        r[C_VY] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 1, ty);
+        r[C_VZ] = stimg_row<BX, BY, BZ>(a, w, cen, row, col, q, k, 2, tz);
       }
 
       /* CFS-PML, faces in the reference order x1, x2, y1, y2, z1, z2 */

@@ -25,7 +25,7 @@
  *
  * Errors print the library's message and call MPI_Abort when MPI is linked
  * (exit(1) otherwise), as the reference does.  Unsupported configurations
- * (surface force sources, dd sources, ablexp, full anisotropy, Graves Q)
+ * (dd sources, ablexp, full anisotropy, Graves Q)
  * are reported the same way instead of being ignored.
  */
 #include <stdio.h>
@@ -81,8 +81,6 @@ void drv_rk_curv_col_allstep(
       md->visco_type != CGFD_REF_VISCO_GMB)
     unsupported("a visco-elastic model other than GMB");
   if (src->dd_is_valid == 1) unsupported("a distributed (dd) source");
-  if (src->total_number > 0 && src->total_number_surface_force > 0)
-    unsupported("a surface force source");
   if (bdry->is_enable_ablexp == 1) unsupported("the ablexp sponge boundary");
 
   cgfd_problem_t p;
@@ -141,6 +139,10 @@ void drv_rk_curv_col_allstep(
     p.Fx = src->Fx; p.Fy = src->Fy; p.Fz = src->Fz;
     p.Mxx = src->Mxx; p.Myy = src->Myy; p.Mzz = src->Mzz;
     p.Mxz = src->Mxz; p.Myz = src->Myz; p.Mxy = src->Mxy;
+    if (src->total_number_surface_force > 0) {
+      p.src_force_rate_indx = src->force_rate_indx;
+      p.Fx_rate = src->Fx_rate; p.Fy_rate = src->Fy_rate; p.Fz_rate = src->Fz_rate;
+    }
   }
 
   /* receivers: gather the per-station interpolation data, packed output */

@@ -151,6 +151,10 @@ class Problem:
                 setattr(s, "src_" + n, P(src[n]))
             for n in ("Fx", "Fy", "Fz", "Mxx", "Myy", "Mzz", "Mxz", "Myz", "Mxy"):
                 setattr(s, n, P(src.get(n)))
+            if src.get("n_surface_force", 0) > 0:
+                s.src_force_rate_indx = P(src["force_rate_indx"], C.c_int)
+                for n in ("Fx_rate", "Fy_rate", "Fz_rate"):
+                    setattr(s, n, P(src[n]))
         r = self.recv
         if r is not None and r["n"] > 0:
             s.recv_n, s.recv_max_nt, s.recv_ncmp = r["n"], r["max_nt"], r["ncmp"]
@@ -243,6 +247,10 @@ def from_golden(path_or_npz):
             src[n] = _f32(d["src." + n])
         for n in ("Fx", "Fy", "Fz", "Mxx", "Myy", "Mzz", "Mxz", "Myz", "Mxy"):
             if "src." + n in d:
+                src[n] = _f32(d["src." + n])
+        if src["n_surface_force"] > 0:
+            src["force_rate_indx"] = _i32(d["src.force_rate_indx"])
+            for n in ("Fx_rate", "Fy_rate", "Fz_rate"):
                 src[n] = _f32(d["src." + n])
         p.src = src
     nr = int(d["recv.total_number"][0])

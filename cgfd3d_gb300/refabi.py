@@ -277,9 +277,11 @@ def build_reference_structs(p):
         for n in ("si", "sj", "sk", "it_begin", "it_end"):
             setattr(src, n, s[n].ctypes.data_as(PI))
         for n in ("si_inc", "sj_inc", "sk_inc", "Fx", "Fy", "Fz", "Mxx", "Myy", "Mzz",
-                  "Mxz", "Myz", "Mxy"):
+                  "Mxz", "Myz", "Mxy", "Fx_rate", "Fy_rate", "Fz_rate"):
             if s.get(n) is not None:
                 setattr(src, n, _fp(s[n]))
+        if s.get("force_rate_indx") is not None:
+            src.force_rate_indx = s["force_rate_indx"].ctypes.data_as(PI)
     bd = Bdry()
     bd.is_sides_free[2][1] = int(p.free_top)
     bd.is_enable_free = int(p.free_top)

@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define CGFD_ABI_VERSION 2
+#define CGFD_ABI_VERSION 3
 
 /* medium types, same codes as forward/constants.h:24-29 */
 #define CGFD_MEDIUM_ELASTIC_ISO 2
@@ -93,7 +93,9 @@ typedef struct {
   int src_ext_half;                  /* ext_half_npoint */
   float src_ext_coef;                /* ext_func_coef (Gaussian width) */
   int src_surface_strict;            /* is_surface_force_strict */
-  int src_n_surface_force;           /* total_number_surface_force (must be 0) */
+  int src_n_surface_force;           /* total_number_surface_force: force
+                                        sources whose spread reaches the free
+                                        surface (their rate tables below) */
   const int *src_si, *src_sj, *src_sk, *src_it_begin, *src_it_end;
   const float *src_si_inc, *src_sj_inc, *src_sk_inc;
   const float *Fx, *Fy, *Fz;                     /* [is][it][istage] */
@@ -124,6 +126,14 @@ typedef struct {
    * rotation needs the grid's eta tangent at k = nk2
    * (forward/sv_curv_col_vis_iso.c:353-507).  May be NULL otherwise. */
   const float *x3d, *y3d, *z3d;
+
+  /* surface force sources (forward/src_t.c:1021-1028, :1084-1090):
+   * src_force_rate_indx[n] is the source index of the n-th surface force,
+   * F*_rate its force-rate table [n][max_nt][max_stage].  Each stage they
+   * give the surface traction and velocity-rate layers
+   * (forward/src_t.c:153-314) used by the traction image and vlow. */
+  const int *src_force_rate_indx;
+  const float *Fx_rate, *Fy_rate, *Fz_rate;
 } cgfd_problem_t;
 
 /* Opaque device-resident solver. */

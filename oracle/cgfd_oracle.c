@@ -20,6 +20,9 @@
  *   velocity "vlow"      forward/sv_curv_col_el_iso.c:451-634
  *   ADE CFS-PML          forward/sv_curv_col_el_iso.c:644-1146
  *   source injection     forward/sv_curv_col_el.c:311-479, src_t.c:2111-2151
+ *   surface force layers forward/src_t.c:153-314 (traction and velocity-rate
+ *                        layers of the forces whose spread reaches the
+ *                        surface, used by the traction image and vlow)
  *   receivers / lines    forward/io_funcs.c:1584-1645
  *   free-surface matrices forward/sv_curv_col_el_iso.c:1258-1375,
  *                        lib/fdlib_math.c:8-48
@@ -109,6 +112,8 @@ typedef struct {
   float *mD;                 /* visco: surface rotation matrix, 9 per (i,j) */
   int med;                   /* medium_type */
   float **ext;               /* per source Gaussian weights (or NULL) */
+  float *TS, *VS;            /* surface force layers: Tx,Ty,Tz / Vx,Vy,Vz Src,
+                                3 x nx*ny each (NULL without surface forces) */
   int nthreads;
   int timg_mode;
   float *pg, *dis;           /* peak-motion maps (NULL: not computed) */
@@ -587,7 +592,7 @@ static void rhs_timg_row(orc_t *o, const float *w, float *h, int j, int zbias,
           vz[-2] = 0.0f;
           vz[-1] = 0.0f;
         }
-        float tsurf = 0.0f; /* TxSrc/TySrc/TzSrc: no surface force */
+        float tsurf = o->TS ? o->TS[r * sl + i + j * ln] : 0.0f; /* TxSrc.. */
         vz[n_free] = tsurf;
         for (int n = n_free + 1; n < 5; n++)
           vz[n] = (float)(2.0 * (double)tsurf - (double)vz[2 * n_free - n]);
@@ -637,9 +642,12 @@ static void rhs_vlow_row(orc_t *o, const float *w, float *h, int j, int zbias,
            the VTI routine has no such term (sv_curv_col_el_vti.c:525-547) */
         if (!m.vti) {
           const float *f = o->mF + ij;
-          DzVx += f[0] * 0.0f + f[1] * 0.0f + f[2] * 0.0f;
-          DzVy += f[3] * 0.0f + f[4] * 0.0f + f[5] * 0.0f;
-          DzVz += f[6] * 0.0f + f[7] * 0.0f + f[8] * 0.0f;
+          size_t i2 = i + j * ln;
+          float vx = 0.0f, vy = 0.0f, vz = 0.0f;
+          if (o->VS) { vx = o->VS[i2]; vy = o->VS[sl + i2]; vz = o->VS[2 * sl + i2]; }
+          DzVx += f[0] * vx + f[1] * vy + f[2] * vz;
+          DzVy += f[3] * vx + f[4] * vy + f[5] * vz;
+          DzVz += f[6] * vx + f[7] * vy + f[8] * vz;
         }
       } else if (n == 1) {
         long s0 = OPZ1_SHIFT[zbias][0] * (long)sl, s1 = OPZ1_SHIFT[zbias][1] * (long)sl;
@@ -868,6 +876,52 @@ static void src_weights(float *delt, float x0, float y0, float z0, float r,
   for (int m = 0; m < n1 * n1 * n1; m++) delt[m] /= sum;
 }
 
+/* surface traction (TxSrc..) and velocity-rate (VxSrc..) layers of the
+ * surface forces at (it, istage) (forward/src_t.c:153-314): a point force
+ * adds its value at its column, a spread one the surface layer of its
+ * Gaussian weights (the same weights as its volume injection). */
+static void surf_layer(orc_t *o, int it, int istage)
+{
+  const cgfd_problem_t *p = o->p;
+  size_t s2 = o->sl, ln = o->ln;
+  memset(o->TS, 0, 3 * s2 * sizeof(float));
+  memset(o->VS, 0, 3 * s2 * sizeof(float));
+  for (int n = 0; n < p->src_n_surface_force; n++) {
+    int is = p->src_force_rate_indx[n];
+    if (it < p->src_it_begin[is] || it > p->src_it_end[is]) continue;
+    int si = p->src_si[is], sj = p->src_sj[is], sk = p->src_sk[is];
+    size_t t = (size_t)is * p->src_max_nt * p->src_max_stage +
+               (size_t)(it - p->src_it_begin[is]) * p->src_max_stage + istage;
+    size_t tr = (size_t)n * p->src_max_nt * p->src_max_stage +
+                (size_t)(it - p->src_it_begin[is]) * p->src_max_stage + istage;
+    float fx = p->Fx[t], fy = p->Fy[t], fz = p->Fz[t];
+    float rx = p->Fx_rate[tr], ry = p->Fy_rate[tr], rz = p->Fz_rate[tr];
+    if (p->src_spatial == CGFD_SRC_POINT) {
+      size_t q = si + sj * ln + (size_t)sk * s2, i2 = si + sj * ln;
+      o->TS[i2] += fx; o->TS[s2 + i2] += fy; o->TS[2 * s2 + i2] += fz;
+      o->VS[i2] += rx / p->jac[q];
+      o->VS[s2 + i2] += ry / p->jac[q];
+      o->VS[2 * s2 + i2] += rz / p->jac[q];
+    } else {
+      int half = p->src_ext_half, len = 2 * half + 1;
+      int kx = p->nk2 - sk;                     /* k_ext of the surface */
+      const float *wgt = o->ext[is] + (size_t)(kx + half) * len * len;
+      int k = sk + kx;
+      for (int jj = -half; jj <= half; jj++)
+        for (int ii = -half; ii <= half; ii++) {
+          float c = *wgt++;
+          int i = si + ii, j = sj + jj;
+          if (i < 0 || i >= p->nx || j < 0 || j >= p->ny) continue;
+          size_t q = i + j * ln + (size_t)k * s2, i2 = i + j * ln;
+          o->TS[i2] += fx * c; o->TS[s2 + i2] += fy * c; o->TS[2 * s2 + i2] += fz * c;
+          o->VS[i2] += rx * c / p->jac[q];
+          o->VS[s2 + i2] += ry * c / p->jac[q];
+          o->VS[2 * s2 + i2] += rz * c / p->jac[q];
+        }
+    }
+  }
+}
+
 /* source injection (sv_curv_col_el.c:350-476) */
 static void rhs_src(orc_t *o, float *h, int it, int istage)
 {
@@ -1038,6 +1092,11 @@ static void *worker(void *arg)
       int bz = (PAIR_FLAGS[ipair][2] + is) % 2;
       op5_t ox = make_op(bx, 1), oy = make_op(by, (long)o->ln),
             oz = make_op(bz, (long)o->sl);
+      /* 0. surface force layers of this stage (drv_rk_curv_col.c:230) */
+      if (o->TS) {
+        if (tid == 0) surf_layer(o, it, is);
+        pthread_barrier_wait(&o->bar);
+      }
       /* 1. interior RHS on all physical points */
       for (long k = k0; k < k1; k++) rhs_inner_plane(o, cur, rhs, (int)k, &ox, &oy, &oz);
       pthread_barrier_wait(&o->bar);
@@ -1157,7 +1216,10 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
   if (med != CGFD_MEDIUM_ELASTIC_ISO && med != CGFD_MEDIUM_ELASTIC_VTI &&
       med != CGFD_MEDIUM_VISCOELASTIC_ISO)
     return CGFD_EINVAL;
-  if (p->src_n_surface_force > 0) return CGFD_EINVAL;
+  if (p->src_n_surface_force > 0 &&
+      (!p->src_force || !p->src_force_rate_indx || !p->Fx_rate || !p->Fy_rate ||
+       !p->Fz_rate || !p->free_top))
+    return CGFD_EINVAL;
   int ncmp_want = 9;
   if (med == CGFD_MEDIUM_VISCOELASTIC_ISO) {
     if (p->nmaxwell < 1 || p->nmaxwell > CGFD_MAX_MAXWELL || !p->wl) return CGFD_EINVAL;
@@ -1216,6 +1278,10 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
                   p->src_sk_inc[is], p->src_ext_coef, half, kz2);
     }
   }
+  if (p->src_n > 0 && p->src_n_surface_force > 0) {
+    o.TS = calloc(3 * o.sl, sizeof(float));
+    o.VS = calloc(3 * o.sl, sizeof(float));
+  }
   if (pg && p->free_top) {
     o.pg = pg;
     o.dis = calloc(3 * o.sl, sizeof(float));
@@ -1239,6 +1305,8 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
   }
   if (own_m) { free(mVx); free(mVy); free(mF); }
   free(o.mD);
+  free(o.TS);
+  free(o.VS);
   free(o.dis);
   return 0;
 }

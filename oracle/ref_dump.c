@@ -250,6 +250,14 @@ static void dump_inputs(fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md,
       put("src.Fy", 'f', src->Fy, nstf);
       put("src.Fz", 'f', src->Fz, nstf);
     }
+    if (src->total_number_surface_force > 0) {
+      int nsf = src->total_number_surface_force;
+      size_t nr = (size_t)nsf * src->max_nt * src->max_stage;
+      put("src.force_rate_indx", 'i', src->force_rate_indx, nsf);
+      put("src.Fx_rate", 'f', src->Fx_rate, nr);
+      put("src.Fy_rate", 'f', src->Fy_rate, nr);
+      put("src.Fz_rate", 'f', src->Fz_rate, nr);
+    }
     if (src->moment_actived == 1) {
       put("src.Mxx", 'f', src->Mxx, nstf);
       put("src.Myy", 'f', src->Myy, nstf);

@@ -90,6 +90,38 @@ CASES = {
         stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1), (12.0, 6.0, 3.4, 1)],
         lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
     ),
+    # force sources whose spread reaches the free surface (the reference
+    # then injects them through the traction image and vlow layers,
+    # forward/src_t.c:153-314): a Gaussian force one cell below the
+    # topography, and a point force at the flat surface
+    "iso_surface_force": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_iso",
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        free=True, seed=2468, steps=9, dt=0.004,
+        src=dict(kind="force", loc=(8.4, 7.3, 1.0), spatial="gauss",
+                 f=(2e15, -1e15, 3e15), fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
+    "iso_surface_point_force": dict(
+        ni=24, nj=20, nk=16, dh=100.0, topo=False, medium="elastic_iso",
+        media_override=(6000.0, 3464.0, 2700.0),
+        pml=dict(x_left=5, x_right=5, y_front=5, y_back=5, z_bottom=5),
+        free=True, seed=None, steps=30, dt=0.005,
+        src=dict(kind="force", loc=(12.0, 10.0, 0.0), spatial="point",
+                 f=(0.0, 0.0, 1e15), fc=10.0, t0=0.12),
+        stations=[(4.0 + 2 * n, 10.0, 0.0, 1) for n in range(8)],
+        lines=[],
+    ),
+    "vti_surface_force": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_vti",
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        free=True, seed=1357, steps=9, dt=0.004,
+        src=dict(kind="force", loc=(8.4, 7.3, 2.0), spatial="gauss",
+                 f=(2e15, -1e15, 3e15), fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
     # no free surface: PML on all six faces (z2 face included), noise state
     "iso_box_pml6": dict(
         ni=16, nj=14, nk=12, dh=100.0, topo=False, medium="elastic_iso",

@@ -80,3 +80,14 @@ def test_vti_differs_from_iso_formulas():
     p.media["c13"] = p.media["c13"] * np.float32(1.0001)
     oracle.allstep(p, oracle.TIMG_ZERO, 2)
     assert not np.array_equal(p.level(p.final_level()), exp["wav"])
+
+
+def test_surface_force_layers_are_exercised():
+    """Without its surface layers (traction image, vlow) the point force at
+    the flat surface would inject nothing: dropping them changes the run."""
+    p, exp = P.from_golden(os.path.join(GOLDEN, "iso_surface_point_force.npz"))
+    p.src = dict(p.src, Fz_rate=np.zeros_like(p.src["Fz_rate"]),
+                 Fz=np.zeros_like(p.src["Fz"]))
+    oracle.allstep(p, oracle.TIMG_ZERO, 2)
+    assert not np.array_equal(p.level(p.final_level()), exp["wav"])
+    assert np.abs(exp["wav"]).max() > 0
