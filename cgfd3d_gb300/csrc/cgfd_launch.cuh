@@ -79,6 +79,13 @@ void CGFD_CAT(cgfd_launch_stage_, CGFD_MED_NAME)(int code, int kind, dim3 grid,
   launch_stage_med<CGFD_MED>(code, kind, grid, st, a, m);
 }
 
+int CGFD_CAT(cgfd_stage_rows_, CGFD_MED_NAME)(void) { return s2::TY; }
+
+int CGFD_CAT(cgfd_stage_smem_, CGFD_MED_NAME)(void)
+{
+  return s3::Slot<CGFD_MED>::SMEM_BYTES;
+}
+
 void CGFD_CAT(cgfd_launch_pml_, CGFD_MED_NAME)(int dim, int b, int kind, int f,
                                                long long n, cudaStream_t st,
                                                const StageArgs &a)

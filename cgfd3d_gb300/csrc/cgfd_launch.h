@@ -37,7 +37,13 @@ void cgfd_launch_pml_vti(int dim, int b, int kind, int f, long long n,
 void cgfd_launch_pml_vis(int dim, int b, int kind, int f, long long n,
                          cudaStream_t st, const StageArgs &a);
 
-/* dynamic shared memory of the stage kernel of a medium (0 iso, 1 vti, 2 vis) */
-int cgfd_stage_smem_bytes(int med);
+/* tile rows (consumer warps) and dynamic shared memory of each medium's
+ * stage kernel */
+int cgfd_stage_rows_iso(void);
+int cgfd_stage_rows_vti(void);
+int cgfd_stage_rows_vis(void);
+int cgfd_stage_smem_iso(void);
+int cgfd_stage_smem_vti(void);
+int cgfd_stage_smem_vis(void);
 
 #endif

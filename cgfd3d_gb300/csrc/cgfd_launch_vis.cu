@@ -1,4 +1,5 @@
 /* Stage and CFS-PML kernels of the vis medium (see cgfd_launch.cuh). */
+#define CGFD_TILE_ROWS 8
 #include "cgfd_media.cuh"
 #define CGFD_MED MED_VIS
 #define CGFD_MED_NAME vis

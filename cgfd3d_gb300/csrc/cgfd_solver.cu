@@ -620,6 +620,7 @@ struct cgfd_solver {
   float *pg, *dis;              /* surface peak-motion maps (free top) */
   StageMaps maps;               /* tensor maps of the stage kernel */
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
+  int ty;                       /* tile rows of the medium's stage kernel */
   int pml_fused;                /* 1: CFS-PML inside the stage kernel */
   int kchunk;
 };
@@ -811,21 +812,21 @@ static int make_tmap(cgfd_solver_t *s)
   cuuint64_t dims[5] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 9, 4};
   cuuint64_t strides[4] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4,
                            (cuuint64_t)g.vol * 4, (cuuint64_t)g.vol * s->ncmp * 4};
-  cuuint32_t box[5] = {s2::BW, s2::BH, 1, 9, 1};
+  cuuint32_t box[5] = {s2::BW, (cuuint32_t)(s->ty + 4), 1, 9, 1};
   cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   CUresult r = fn(&M.wav, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   /* per-point tiles (no halo) for L2 prefetch of the streams */
-  cuuint32_t boxp[5] = {s2::TX, s2::TY, 1, 9, 1};
+  cuuint32_t boxp[5] = {s2::TX, (cuuint32_t)s->ty, 1, 9, 1};
   r = fn(&M.pt, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dims, strides,
          boxp, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (points) failed (%d)", (int)r);
   cuuint64_t dm[4] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 10};
   cuuint64_t sm_[3] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4, (cuuint64_t)g.vol * 4};
-  cuuint32_t bm[4] = {s2::TX, s2::TY, 1, 10};
+  cuuint32_t bm[4] = {s2::TX, (cuuint32_t)s->ty, 1, 10};
   r = fn(&M.met, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->metric, dm, sm_, bm, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -841,7 +842,7 @@ static int make_tmap(cgfd_solver_t *s)
   if (s->ncmp > 9) {
     cuuint64_t dj[5] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz,
                         (cuuint64_t)s->ncmp, 4};
-    cuuint32_t bj[5] = {s2::TX, s2::TY, 1, (cuuint32_t)(s->ncmp - 9), 1};
+    cuuint32_t bj[5] = {s2::TX, (cuuint32_t)s->ty, 1, (cuuint32_t)(s->ncmp - 9), 1};
     r = fn(&M.j, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, s->wav, dj, strides, bj, estr,
            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -884,6 +885,8 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   s->med = medium_of(p->medium_type);
   s->ncmp = p->ncmp;
   s->nmed = med_ncomp(s->med, s->med == MED_VIS ? p->nmaxwell : 0);
+  s->ty = s->med == MED_VTI ? cgfd_stage_rows_vti()
+        : s->med == MED_VIS ? cgfd_stage_rows_vis() : cgfd_stage_rows_iso();
   DevGrid &g = s->g;
   g.ni = p->ni; g.nj = p->nj; g.nk = p->nk;
   g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
@@ -1117,16 +1120,14 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   /* the direct-load A/B kernel (cgfd_stage.cuh) covers isotropic media only */
   if (const char *e = getenv("CGFD_STAGE_KERNEL"))
     s->kernel = (atoi(e) == 1 && s->med == MED_ISO && s->nsf == 0) ? 1 : 2;
-  /* CFS-PML inside the stage kernel or by the per-face kernels after it.
-   * Measured on GB300 (topography model, 12 layers): isotropic media are
-   * faster split (the fused PML lengthens the latency-bound consumer warps
-   * more than the face kernels cost), VTI and visco-elastic media fused
-   * (their face kernels re-read more per point).  CGFD_PML_SPLIT=1 / 0
-   * forces either form. */
-  s->pml_fused = s->med != MED_ISO;
+  /* CFS-PML inside the stage kernel (default: measured faster on GB300 for
+   * every medium, the face kernels re-read the wavefield, metrics and media
+   * and read-modify-write tmp/end) or by the per-face kernels after it.
+   * CGFD_PML_SPLIT=1 / 0 forces either form. */
+  s->pml_fused = 1;
   if (const char *e = getenv("CGFD_PML_SPLIT")) s->pml_fused = atoi(e) == 1 ? 0 : 1;
   {
-    int tiles = ((g.ni + s2::TX - 1) / s2::TX) * ((g.nj + s2::TY - 1) / s2::TY);
+    int tiles = ((g.ni + s2::TX - 1) / s2::TX) * ((g.nj + s->ty - 1) / s->ty);
     int want = 8 * 152;                     /* about eight waves of CTAs */
     int nch = std::max(1, std::min(g.nk / 16, (want + tiles - 1) / tiles));
     s->kchunk = (g.nk + nch - 1) / nch;
@@ -1183,7 +1184,7 @@ static void launch_stage(cgfd_solver_t *s, int code, int kind, cudaStream_t st,
     }
     return;
   }
-  dim3 gr((s->g.ni + s2::TX - 1) / s2::TX, (s->g.nj + s2::TY - 1) / s2::TY,
+  dim3 gr((s->g.ni + s2::TX - 1) / s2::TX, (s->g.nj + s->ty - 1) / s->ty,
           (s->g.nk + s->kchunk - 1) / s->kchunk);
   if (s->med == MED_VTI) cgfd_launch_stage_vti(code, kind, gr, st, a, s->maps);
   else if (s->med == MED_VIS) cgfd_launch_stage_vis(code, kind, gr, st, a, s->maps);

@@ -21,11 +21,20 @@
 namespace s2 {
 
 constexpr int TX = 32;
-constexpr int TY = 8;
+/* tile rows (one consumer warp each); set per translation unit: more rows
+ * give more warps per SM to hide latency where the shared memory allows */
+#ifndef CGFD_TILE_ROWS
+#define CGFD_TILE_ROWS 8
+#endif
+constexpr int TY = CGFD_TILE_ROWS;
 constexpr int BW = 40;               /* box width (x), multiple of 4 */
 constexpr int BH = TY + 4;           /* box height (y) */
 constexpr int XL = 4;                /* smem column of the tile's first i */
-constexpr int PLANE = 9 * BH * BW;   /* floats per plane buffer */
+constexpr int PLANE_DATA = 9 * BH * BW;  /* floats one plane copy lands */
+/* plane buffer stride: every bulk tensor copy must land on a 128-byte
+ * aligned shared-memory address, so the ring stride is rounded up */
+constexpr int PLANE = (PLANE_DATA + 31) / 32 * 32;
+static_assert(PLANE % 32 == 0, "plane buffers must stay 128-byte aligned");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {

@@ -74,6 +74,10 @@ struct Slot {
   static constexpr int S_END = S_PRE + 9 * PTS;
   static constexpr int SLOT = S_END + 9 * PTS;
   static constexpr int SMEM_BYTES = (NB * PLANE + NS * SLOT) * 4;
+  /* every bulk tensor copy lands on a 128-byte aligned shared address */
+  static_assert(PTS % 32 == 0 && (NB * PLANE) % 32 == 0 && SLOT % 32 == 0,
+                "stream-slot regions must stay 128-byte aligned");
+  static_assert(SMEM_BYTES <= 232448, "more shared memory than one CTA gets");
 };
 
 /* bounded wait; `err` records a timeout */
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         mbar_wait(&empty_w[b], ((rel / NB) - 1) & 1, a.err);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
-      mbar_expect_tx(&full_w[b], PLANE * 4);
+      mbar_expect_tx(&full_w[b], PLANE_DATA * 4);
       tma_load_5d(ring + b * PLANE, &tmap, bx0, by0, pbase + rel, 0, a.cur_level,
                   &full_w[b]);
     };
