@@ -109,6 +109,7 @@ struct StageArgs {
   int istage;
   int *err;                    /* device error word (bounded waits) */
   int pml_fused;               /* CFS-PML inside the stage kernel (else face kernels) */
+  int l2_ahead;                /* planes of L2 prefetch beyond the smem rings */
   int cur_level;               /* level index of `cur` (TMA coordinate) */
   int pre_level, end_level;    /* level indices of `pre` and `end` */
   int kchunk;                  /* planes per CTA along k */

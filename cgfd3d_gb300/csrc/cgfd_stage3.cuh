@@ -280,8 +280,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (KIND == 1) tma_load_5d(dst + S_PRE, &tmap_pt, xs, j0, k, 0, a.pre_level, &full_s[b]);
       if (KIND >= 1) tma_load_5d(dst + S_END, &tmap_pt, xs, j0, k, 0, a.end_level, &full_s[b]);
     };
+    /* L2 prefetch of the tiles a.l2_ahead planes beyond what the rings
+     * hold: more bytes in flight per SM than the shared memory allows */
+    const int L2_AHEAD = a.l2_ahead;
+    auto prefetch_ahead = [&](int it) {
+      const int ip = it + L2_AHEAD;
+      if (ip < niter) {
+        const int k = kbeg + ip;
+        tma_prefetch_4d(&tmap_met, xs, j0, k, 0);
+        tma_prefetch_4d(&tmap_med, xs, j0, k, 0);
+        if (MED == MED_VIS) tma_prefetch_5d(&tmap_j, xs, j0, k, 9, a.cur_level);
+        if (KIND == 1) tma_prefetch_5d(&tmap_pt, xs, j0, k, 0, a.pre_level);
+        if (KIND >= 1) tma_prefetch_5d(&tmap_pt, xs, j0, k, 0, a.end_level);
+      }
+      const int rp = it + 5 + L2_AHEAD;
+      if (rp < niter + 4) tma_prefetch_5d(&tmap, bx0, by0, pbase + rp, 0, a.cur_level);
+    };
     for (int rel = 0; rel < 5; rel++) issue_wav(rel);
     for (int it = 0; it < niter; it++) {
+      if (L2_AHEAD > 0) prefetch_ahead(it);
       issue_slot(it);
       if (it + 5 < niter + 4) issue_wav(it + 5);
     }
