@@ -50,6 +50,18 @@ def lib():
     L.cgfd_allstep.argtypes = [vp]
     L.cgfd_device_bytes.argtypes = [vp]
     L.cgfd_device_bytes.restype = C.c_size_t
+    L.cgfd_batch_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
+    L.cgfd_batch_run.argtypes = [vp, C.c_int]
+    L.cgfd_batch_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    L.cgfd_batch_fetch.argtypes = [vp]
+    L.cgfd_batch_reset.argtypes = [vp]
+    L.cgfd_batch_set_kchunk.argtypes = [vp, C.c_int]
+    L.cgfd_batch_autotune.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.c_int,
+                                      C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    L.cgfd_batch_shot.argtypes = [vp, C.c_int]
+    L.cgfd_batch_shot.restype = vp
+    L.cgfd_batch_destroy.argtypes = [vp]
+    L.cgfd_batch_destroy.restype = None
     L.cgfd_check_finite_noalloc.argtypes = [C.c_void_p, C.c_size_t, C.POINTER(C.c_int)]
     L.cgfd_check_finite_noalloc.restype = C.c_int
     if L.cgfd_abi_version() != abi.CGFD_ABI_VERSION:

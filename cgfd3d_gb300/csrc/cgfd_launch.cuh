@@ -5,11 +5,18 @@
 #ifndef CGFD_LAUNCH_CUH
 #define CGFD_LAUNCH_CUH
 
+/* CGFD_SINGLE: the single-problem stage/PML launchers; CGFD_BATCH: the
+ * batched stage launchers.  A translation unit may hold either or both. */
+#ifndef CGFD_SINGLE
+#define CGFD_SINGLE 1
+#endif
+
 #include "cgfd_launch.h"
 #include "cgfd_media.cuh"
 #include "cgfd_pml.cuh"
 #include "cgfd_stage3.cuh"
 
+#if CGFD_SINGLE
 template <int BX, int BY, int BZ, int KIND, int MED>
 static void launch_stage_t(dim3 grid, cudaStream_t st, const StageArgs &a,
                            const StageMaps &m)
@@ -50,6 +57,50 @@ static void launch_stage_med(int code, int kind, dim3 grid, cudaStream_t st,
   }
 }
 
+#endif
+
+#if CGFD_BATCH
+template <int BX, int BY, int BZ, int KIND, int MED>
+static void launch_batch_t(int nctas, cudaStream_t st, const StageArgs *args,
+                           const s3::ShotGeo *geo, int nshot)
+{
+  constexpr int smem = s3::Slot<MED>::SMEM_BYTES;
+  if (nctas <= 0) {   /* preparation only: set the shared-memory attribute */
+    cudaFuncSetAttribute(s3::k_stage3_batch<BX, BY, BZ, KIND, MED>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return;
+  }
+  s3::k_stage3_batch<BX, BY, BZ, KIND, MED><<<nctas, s3::NTHREADS, smem, st>>>(
+      args, geo, nshot);
+}
+
+template <int BX, int BY, int BZ, int MED>
+static void launch_batch_k(int kind, int nctas, cudaStream_t st, const StageArgs *args,
+                           const s3::ShotGeo *geo, int nshot)
+{
+  if (kind == 0) launch_batch_t<BX, BY, BZ, 0, MED>(nctas, st, args, geo, nshot);
+  else if (kind == 1) launch_batch_t<BX, BY, BZ, 1, MED>(nctas, st, args, geo, nshot);
+  else launch_batch_t<BX, BY, BZ, 2, MED>(nctas, st, args, geo, nshot);
+}
+
+template <int MED>
+static void launch_batch_med(int code, int kind, int nctas, cudaStream_t st,
+                             const StageArgs *args, const s3::ShotGeo *geo, int nshot)
+{
+  switch (code) {
+    case 0: launch_batch_k<0, 0, 0, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 1: launch_batch_k<0, 0, 1, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 2: launch_batch_k<0, 1, 0, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 3: launch_batch_k<0, 1, 1, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 4: launch_batch_k<1, 0, 0, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 5: launch_batch_k<1, 0, 1, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 6: launch_batch_k<1, 1, 0, MED>(kind, nctas, st, args, geo, nshot); break;
+    default: launch_batch_k<1, 1, 1, MED>(kind, nctas, st, args, geo, nshot); break;
+  }
+}
+#endif
+
+#if CGFD_SINGLE
 template <int DIM, int B, int MED>
 static void launch_pml_t(int kind, int f, long long n, cudaStream_t st,
                          const StageArgs &a)
@@ -69,9 +120,12 @@ static void launch_pml_med(int dim, int b, int kind, int f, long long n,
   else { if (b) launch_pml_t<2, 1, MED>(kind, f, n, st, a); else launch_pml_t<2, 0, MED>(kind, f, n, st, a); }
 }
 
+#endif
+
 #define CGFD_CAT2(a, b) a##b
 #define CGFD_CAT(a, b) CGFD_CAT2(a, b)
 
+#if CGFD_SINGLE
 void CGFD_CAT(cgfd_launch_stage_, CGFD_MED_NAME)(int code, int kind, dim3 grid,
                                                  cudaStream_t st, const StageArgs &a,
                                                  const StageMaps &m)
@@ -79,6 +133,19 @@ void CGFD_CAT(cgfd_launch_stage_, CGFD_MED_NAME)(int code, int kind, dim3 grid,
   launch_stage_med<CGFD_MED>(code, kind, grid, st, a, m);
 }
 
+#endif
+
+#if CGFD_BATCH
+void CGFD_CAT(cgfd_launch_stage_batch_, CGFD_MED_NAME)(int code, int kind, int nctas,
+                                                       cudaStream_t st,
+                                                       const StageArgs *args,
+                                                       const s3::ShotGeo *geo, int nshot)
+{
+  launch_batch_med<CGFD_MED>(code, kind, nctas, st, args, geo, nshot);
+}
+#endif
+
+#if CGFD_SINGLE
 int CGFD_CAT(cgfd_stage_rows_, CGFD_MED_NAME)(void) { return s2::TY; }
 
 int CGFD_CAT(cgfd_stage_smem_, CGFD_MED_NAME)(void)
@@ -92,5 +159,6 @@ void CGFD_CAT(cgfd_launch_pml_, CGFD_MED_NAME)(int dim, int b, int kind, int f,
 {
   launch_pml_med<CGFD_MED>(dim, b, kind, f, n, st, a);
 }
+#endif
 
 #endif

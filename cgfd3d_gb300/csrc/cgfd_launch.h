@@ -12,6 +12,10 @@
 
 #include "cgfd_common.h"
 
+namespace s3 {
+struct ShotGeo;
+}
+
 /* tensor maps of one solver (cgfd_stage3.cuh) */
 struct StageMaps {
   CUtensorMap wav;   /* 5-D (x, y, z, component, level), 9-component planes */
@@ -28,6 +32,17 @@ void cgfd_launch_stage_vti(int code, int kind, dim3 grid, cudaStream_t st,
                            const StageArgs &a, const StageMaps &m);
 void cgfd_launch_stage_vis(int code, int kind, dim3 grid, cudaStream_t st,
                            const StageArgs &a, const StageMaps &m);
+
+/* the stage of a batch of shots in one launch of `nctas` CTAs (per-shot
+ * arguments and tensor maps in device memory); isotropic and VTI media.
+ * nctas <= 0 only sets the kernel's shared-memory attribute (done for every
+ * form before a CUDA graph is captured). */
+void cgfd_launch_stage_batch_iso(int code, int kind, int nctas, cudaStream_t st,
+                                 const StageArgs *args, const s3::ShotGeo *geo,
+                                 int nshot);
+void cgfd_launch_stage_batch_vti(int code, int kind, int nctas, cudaStream_t st,
+                                 const StageArgs *args, const s3::ShotGeo *geo,
+                                 int nshot);
 
 /* CFS-PML face kernel of face f (normal dim, operator bias b), n points */
 void cgfd_launch_pml_iso(int dim, int b, int kind, int f, long long n,

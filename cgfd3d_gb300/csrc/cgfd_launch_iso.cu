@@ -3,5 +3,6 @@
 #include "cgfd_media.cuh"
 #define CGFD_MED MED_ISO
 #define CGFD_MED_NAME iso
+#define CGFD_BATCH 0
 #include "cgfd_launch.cuh"
 

@@ -3,4 +3,5 @@
 #include "cgfd_media.cuh"
 #define CGFD_MED MED_VIS
 #define CGFD_MED_NAME vis
+#define CGFD_BATCH 0
 #include "cgfd_launch.cuh"

@@ -30,6 +30,7 @@
 #include "cgfd_launch.h"
 #include "cgfd_media.cuh"
 #include "cgfd_stage2.cuh"
+#include "cgfd_stage3.cuh"
 
 /* ------------------------------------------------------------------------ */
 /* errors                                                                    */
@@ -1523,4 +1524,441 @@ extern "C" int cgfd_allstep(const cgfd_problem_t *p)
   if (!rc) rc = cgfd_solver_fetch(s);
   cgfd_solver_destroy(s);
   return rc;
+}
+
+/* ------------------------------------------------------------------------ */
+/* reset (used by the batch autotuner)                                       */
+/* ------------------------------------------------------------------------ */
+
+/* Puts a solver back at step 0 with the problem's host inputs: wavefield
+ * level 0 and PML auxiliary level 0 into all four levels, seismograms,
+ * peak-motion maps and the step counter zeroed. */
+static int solver_reset(cgfd_solver_t *s)
+{
+  const cgfd_problem_t *p = s->p;
+  const DevGrid &g = s->g;
+  cudaStream_t st = s->stream;
+  size_t vol = g.vol, L = level_floats(s);
+  size_t hvol = (size_t)p->nx * p->ny * p->nz;
+  for (int c = 0; c < s->ncmp; c++) CK(upload_volume(s, s->wav + c * vol, p->wav + c * hvol));
+  for (int l = 1; l < 4; l++)
+    CK(cudaMemcpyAsync(s->wav + l * L, s->wav, L * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  for (int d = 0; d < 3; d++)
+    for (int sd = 0; sd < 2; sd++) {
+      int f = d * 2 + sd;
+      if (!s->face[f].on) continue;
+      size_t al = 9 * (size_t)s->face[f].avol;
+      CK(cudaMemcpyAsync(s->aux[f], p->pml[d][sd].aux, al * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+      for (int l = 1; l < 4; l++)
+        CK(cudaMemcpyAsync(s->aux[f] + l * al, s->aux[f], al * sizeof(float),
+                           cudaMemcpyDeviceToDevice, st));
+    }
+  if (s->recv_seismo)
+    CK(cudaMemsetAsync(s->recv_seismo, 0,
+                       (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt * 4, st));
+  if (s->line_seismo)
+    CK(cudaMemsetAsync(s->line_seismo, 0, (size_t)p->line_n * p->ncmp * p->line_max_nt * 4, st));
+  if (s->pg) {
+    size_t s2n = (size_t)p->nx * p->ny;
+    CK(cudaMemsetAsync(s->pg, 0, 15 * s2n * 4, st));
+    CK(cudaMemsetAsync(s->dis, 0, 3 * s2n * 4, st));
+  }
+  CK(cudaMemsetAsync(s->d_it, 0, 4, st));
+  CK(cudaStreamSynchronize(st));
+  s->step = 0;
+  s->pre_lev = 0;
+  s->end_lev = 3;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* batched shots                                                             */
+/* ------------------------------------------------------------------------ */
+
+/* receivers / lines of one shot after a step (arguments of k_recv) */
+struct RecvJob {
+  const float *w;
+  long long vol;
+  int ncmp, nrecv, recv_ncmp, recv_max_nt;
+  const float *dijk;
+  const int *idx8;
+  float *seismo;
+  int nline, line_max_nt;
+  const int *line_iptr;
+  float *line_seismo;
+  int *d_it;
+};
+
+/* peak-motion maps of one shot after a step (arguments of k_pg) */
+struct PgJob {
+  DevGrid g;
+  const float *w1, *w0;
+  float *pg, *dis;
+  float dt;
+  int on;
+};
+
+/* k_recv for every shot of a batch: one block per shot */
+__global__ void k_recv_batch(const RecvJob *__restrict__ jobs)
+{
+  const RecvJob &J = jobs[blockIdx.x];
+  const int it = *J.d_it;
+  for (int t = threadIdx.x; t < J.nrecv * J.recv_ncmp; t += blockDim.x) {
+    int n = t / J.recv_ncmp, c = t % J.recv_ncmp;
+    const int *x = J.idx8 + 8 * n;
+    float Lx2 = J.dijk[3 * n], Ly2 = J.dijk[3 * n + 1], Lz2 = J.dijk[3 * n + 2];
+    float Lx1 = 1.0f - Lx2, Ly1 = 1.0f - Ly2, Lz1 = 1.0f - Lz2;
+    const float *v = J.w + c * J.vol;
+    J.seismo[((long long)n * J.recv_ncmp + c) * J.recv_max_nt + it] =
+        v[x[0]] * Lx1 * Ly1 * Lz1 + v[x[1]] * Lx2 * Ly1 * Lz1 +
+        v[x[2]] * Lx1 * Ly2 * Lz1 + v[x[3]] * Lx2 * Ly2 * Lz1 +
+        v[x[5]] * Lx1 * Ly1 * Lz2 + v[x[5]] * Lx2 * Ly1 * Lz2 +
+        v[x[6]] * Lx1 * Ly2 * Lz2 + v[x[7]] * Lx2 * Ly2 * Lz2;
+  }
+  for (int t = threadIdx.x; t < J.nline * J.ncmp; t += blockDim.x) {
+    int n = t / J.ncmp, c = t % J.ncmp;
+    J.line_seismo[((long long)n * J.ncmp + c) * J.line_max_nt + it] =
+        J.w[c * J.vol + J.line_iptr[n]];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *J.d_it = it + 1;
+}
+
+/* k_pg for every shot of a batch: blockIdx.z is the shot */
+__global__ void k_pg_batch(const PgJob *__restrict__ jobs)
+{
+  const PgJob &J = jobs[blockIdx.z];
+  if (!J.on) return;
+  const DevGrid &g = J.g;
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
+  long long s2 = (long long)g.nx * g.ny;
+  long long q2 = i + (long long)j * g.nx;
+  const float dt = J.dt;
+  float vx1 = J.w1[q], vy1 = J.w1[g.vol + q], vz1 = J.w1[2 * g.vol + q];
+  float vx0 = J.w0[q], vy0 = J.w0[g.vol + q], vz0 = J.w0[2 * g.vol + q];
+  float Ax = fabsf((vx1 - vx0) / dt), Ay = fabsf((vy1 - vy0) / dt),
+        Az = fabsf((vz1 - vz0) / dt);
+  float Dx = J.dis[q2] + 0.5f * (vx1 + vx0) * dt;
+  float Dy = J.dis[s2 + q2] + 0.5f * (vy1 + vy0) * dt;
+  float Dz = J.dis[2 * s2 + q2] + 0.5f * (vz1 + vz0) * dt;
+  J.dis[q2] = Dx; J.dis[s2 + q2] = Dy; J.dis[2 * s2 + q2] = Dz;
+  float v[15] = {sqrtf(vx1 * vx1 + vy1 * vy1 + vz1 * vz1), sqrtf(vx1 * vx1 + vy1 * vy1),
+                 fabsf(vx1), fabsf(vy1), fabsf(vz1),
+                 sqrtf(Ax * Ax + Ay * Ay + Az * Az), sqrtf(Ax * Ax + Ay * Ay), Ax, Ay, Az,
+                 sqrtf(Dx * Dx + Dy * Dy + Dz * Dz), sqrtf(Dx * Dx + Dy * Dy),
+                 fabsf(Dx), fabsf(Dy), fabsf(Dz)};
+#pragma unroll
+  for (int m = 0; m < 15; m++) {
+    float *p = J.pg + m * s2 + q2;
+    if (*p < v[m]) *p = v[m];
+  }
+}
+
+struct cgfd_batch {
+  std::vector<cgfd_solver_t *> sv;
+  int n = 0;
+  int med = MED_ISO;
+  int kchunk = 16;
+  int step = 0;
+  int par = 0;                    /* level parity: 0 pre=0/end=3, 1 swapped */
+  int nt_total = 0;
+  cudaStream_t stream = nullptr;
+  StageArgs *d_args = nullptr;    /* [parity][stage][shot] */
+  s3::ShotGeo *d_geo = nullptr;   /* [shot] */
+  RecvJob *d_recv = nullptr;      /* [parity][shot] */
+  PgJob *d_pg = nullptr;          /* [parity][shot] */
+  int nctas = 0, pg_any = 0, max_ni = 0, max_nj = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_par = -1;
+  int use_graph = 1;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float t_ms = 0.f;
+  int launches = 0;
+};
+
+static void batch_free_tables(cgfd_batch_t *b)
+{
+  void *ptrs[] = {b->d_args, b->d_geo, b->d_recv, b->d_pg};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  b->d_args = nullptr; b->d_geo = nullptr; b->d_recv = nullptr; b->d_pg = nullptr;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_par = -1;
+}
+
+/* device tables of the batch for its current kchunk */
+static int batch_tables(cgfd_batch_t *b)
+{
+  batch_free_tables(b);
+  const int n = b->n;
+  std::vector<StageArgs> args((size_t)8 * n);
+  std::vector<s3::ShotGeo> geo(n);
+  std::vector<RecvJob> rj((size_t)2 * n);
+  std::vector<PgJob> pj((size_t)2 * n);
+  int cta = 0;
+  b->pg_any = 0; b->max_ni = 0; b->max_nj = 0;
+  for (int k = 0; k < n; k++) {
+    cgfd_solver_t *s = b->sv[k];
+    s->kchunk = b->kchunk;
+    const int pre0 = s->pre_lev, end0 = s->end_lev;
+    for (int par = 0; par < 2; par++) {
+      s->pre_lev = par == 0 ? 0 : 3;
+      s->end_lev = par == 0 ? 3 : 0;
+      for (int is = 0; is < 4; is++) fill_args(s, args[(size_t)(par * 4 + is) * n + k], is);
+      size_t L = level_floats(s);
+      RecvJob &r = rj[(size_t)par * n + k];
+      const cgfd_problem_t *p = s->p;
+      r.w = s->wav + s->end_lev * L; r.vol = s->g.vol; r.ncmp = s->ncmp;
+      r.nrecv = p->recv_n; r.recv_ncmp = p->recv_ncmp; r.recv_max_nt = p->recv_max_nt;
+      r.dijk = s->recv_dijk; r.idx8 = s->recv_idx; r.seismo = s->recv_seismo;
+      r.nline = p->line_n; r.line_max_nt = p->line_max_nt; r.line_iptr = s->line_iptr;
+      r.line_seismo = s->line_seismo; r.d_it = s->d_it;
+      PgJob &g = pj[(size_t)par * n + k];
+      g.g = s->g; g.w1 = s->wav + s->end_lev * L; g.w0 = s->wav + s->pre_lev * L;
+      g.pg = s->pg; g.dis = s->dis; g.dt = p->dt; g.on = s->pg != nullptr;
+    }
+    s->pre_lev = pre0; s->end_lev = end0;
+    s3::ShotGeo &G = geo[k];
+    memset(&G, 0, sizeof(G));
+    G.wav = s->maps.wav; G.met = s->maps.met; G.med = s->maps.med;
+    G.pt = s->maps.pt; G.j = s->maps.j;
+    G.tiles_x = (s->g.ni + s2::TX - 1) / s2::TX;
+    G.tiles_y = (s->g.nj + s->ty - 1) / s->ty;
+    G.nchunk = (s->g.nk + b->kchunk - 1) / b->kchunk;
+    G.cta0 = cta;
+    cta += G.tiles_x * G.tiles_y * G.nchunk;
+    b->pg_any |= s->pg != nullptr;
+    b->max_ni = std::max(b->max_ni, s->g.ni);
+    b->max_nj = std::max(b->max_nj, s->g.nj);
+  }
+  b->nctas = cta;
+  CK(cudaMalloc((void **)&b->d_args, args.size() * sizeof(StageArgs)));
+  CK(cudaMalloc((void **)&b->d_geo, geo.size() * sizeof(s3::ShotGeo)));
+  CK(cudaMalloc((void **)&b->d_recv, rj.size() * sizeof(RecvJob)));
+  CK(cudaMalloc((void **)&b->d_pg, pj.size() * sizeof(PgJob)));
+  CK(cudaMemcpy(b->d_args, args.data(), args.size() * sizeof(StageArgs), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_geo, geo.data(), geo.size() * sizeof(s3::ShotGeo), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_recv, rj.data(), rj.size() * sizeof(RecvJob), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(b->d_pg, pj.data(), pj.size() * sizeof(PgJob), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+extern "C" void cgfd_batch_destroy(cgfd_batch_t *b)
+{
+  if (!b) return;
+  batch_free_tables(b);
+  for (cgfd_solver_t *s : b->sv) cgfd_solver_destroy(s);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
+                                 int kchunk, cgfd_batch_t **out)
+{
+  *out = nullptr;
+  if (!shots || nshot < 1) return set_err(CGFD_EINVAL, "empty batch");
+  for (int k = 0; k < nshot; k++) {
+    const cgfd_problem_t *p = shots[k];
+    if (!p) return set_err(CGFD_EINVAL, "shot %d: null problem", k);
+    if (p->medium_type != shots[0]->medium_type)
+      return set_err(CGFD_EINVAL, "shot %d: every shot of a batch has the same medium", k);
+    if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO)
+      return set_err(CGFD_EINVAL, "batched shots: elastic media (iso, VTI) only");
+    if (p->src_n > 0 && p->src_n_surface_force > 0)
+      return set_err(CGFD_EINVAL, "shot %d: surface force sources are not batched", k);
+    if (p->nt_total != shots[0]->nt_total || p->dt != shots[0]->dt)
+      return set_err(CGFD_EINVAL, "shot %d: every shot steps with the same dt and nt_total", k);
+  }
+  cgfd_batch_t *b = new cgfd_batch_t();
+  b->n = nshot;
+  b->nt_total = shots[0]->nt_total;
+  b->med = medium_of(shots[0]->medium_type);
+  b->kchunk = kchunk > 0 ? kchunk : 16;
+  if (const char *e = getenv("CGFD_BATCH_GRAPH")) b->use_graph = atoi(e) != 0;
+#define BTRY(x) do { int r_ = (x); if (r_) { cgfd_batch_destroy(b); return r_; } } while (0)
+#define BTRYC(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { set_err(CGFD_ECUDA, "%s: %s", #x, cudaGetErrorString(e_)); cgfd_batch_destroy(b); return CGFD_ECUDA; } } while (0)
+  BTRYC(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BTRYC(cudaEventCreate(&b->ev0));
+  BTRYC(cudaEventCreate(&b->ev1));
+  for (int k = 0; k < nshot; k++) {
+    cgfd_solver_t *s = nullptr;
+    int rc = cgfd_solver_create(shots[k], &s);
+    if (rc) {
+      std::string m = g_err;
+      cgfd_batch_destroy(b);
+      return set_err(rc, "shot %d: %s", k, m.c_str());
+    }
+    s->pml_fused = 1;
+    s->kernel = 2;
+    b->sv.push_back(s);
+  }
+  /* shared-memory attribute of every batched stage form (graph capture
+   * must not be the first use) */
+  for (int code = 0; code < 8; code++)
+    for (int kind = 0; kind < 3; kind++) {
+      if (b->med == MED_VTI) cgfd_launch_stage_batch_vti(code, kind, 0, b->stream, nullptr, nullptr, 0);
+      else cgfd_launch_stage_batch_iso(code, kind, 0, b->stream, nullptr, nullptr, 0);
+    }
+  BTRY(batch_tables(b));
+  *out = b;
+  return 0;
+#undef BTRY
+#undef BTRYC
+}
+
+static void batch_enqueue_step(cgfd_batch_t *b, int it)
+{
+  const int n = b->n, ipair = it % 8, par = b->par;
+  for (int is = 0; is < 4; is++) {
+    int bx = (PAIR_FLAGS[ipair][0] + is) % 2;
+    int by = (PAIR_FLAGS[ipair][1] + is) % 2;
+    int bz = (PAIR_FLAGS[ipair][2] + is) % 2;
+    int kind = is == 0 ? 0 : (is < 3 ? 1 : 2);
+    int code = bx * 4 + by * 2 + bz;
+    const StageArgs *args = b->d_args + (size_t)(par * 4 + is) * n;
+    if (b->med == MED_VTI)
+      cgfd_launch_stage_batch_vti(code, kind, b->nctas, b->stream, args, b->d_geo, n);
+    else
+      cgfd_launch_stage_batch_iso(code, kind, b->nctas, b->stream, args, b->d_geo, n);
+  }
+  if (b->pg_any) {
+    dim3 bl(32, 8), gr((b->max_ni + 31) / 32, (b->max_nj + 7) / 8, n);
+    k_pg_batch<<<gr, bl, 0, b->stream>>>(b->d_pg + (size_t)par * n);
+  }
+  k_recv_batch<<<n, 256, 0, b->stream>>>(b->d_recv + (size_t)par * n);
+  b->par ^= 1;
+}
+
+/* advance the per-shot bookkeeping of the solvers by nsteps */
+static void batch_sync_solvers(cgfd_batch_t *b, int nsteps)
+{
+  for (cgfd_solver_t *s : b->sv) {
+    s->step += nsteps;
+    if (nsteps % 2) std::swap(s->pre_lev, s->end_lev);
+  }
+}
+
+extern "C" int cgfd_batch_run(cgfd_batch_t *b, int nsteps)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  if (nsteps < 0 || b->step + nsteps > b->nt_total)
+    return set_err(CGFD_EINVAL, "run(%d) past nt_total=%d (at step %d)", nsteps,
+                   b->nt_total, b->step);
+  CK(cudaEventRecord(b->ev0, b->stream));
+  int it = b->step, end = b->step + nsteps;
+  int launches = 0;
+  const int per_step = 4 + (b->pg_any ? 1 : 0) + 1;
+  /* whole 8-step pair cycles (starting at a multiple of 8) are replayed
+   * from one CUDA graph; the steps before and after run eagerly */
+  while (it < end) {
+    if (!(b->use_graph && it % 8 == 0 && end - it >= 8)) {
+      batch_enqueue_step(b, it++);
+      launches += per_step;
+      continue;
+    }
+    if (!b->graph || b->graph_par != b->par) {
+      if (b->graph) cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+      const int par0 = b->par;
+      cudaGraph_t gph = nullptr;
+      CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      for (int m = 0; m < 8; m++) batch_enqueue_step(b, m);
+      CK(cudaStreamEndCapture(b->stream, &gph));
+      cudaError_t e = cudaGraphInstantiate(&b->graph, gph, 0);
+      cudaGraphDestroy(gph);
+      CK(e);
+      b->graph_par = par0;
+      b->par = par0;              /* capture recorded, nothing ran */
+    }
+    CK(cudaGraphLaunch(b->graph, b->stream));
+    it += 8;
+    launches += 8 * per_step;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(b->ev1, b->stream));
+  CK(cudaEventSynchronize(b->ev1));
+  CK(cudaEventElapsedTime(&b->t_ms, b->ev0, b->ev1));
+  b->launches = launches;
+  batch_sync_solvers(b, nsteps);
+  b->step = end;
+  for (cgfd_solver_t *s : b->sv) {
+    int herr = 0;
+    CK(cudaMemcpy(&herr, s->d_err, 4, cudaMemcpyDeviceToHost));
+    if (herr) return set_err(CGFD_ECUDA, "device wait timed out (code %d)", herr);
+  }
+  return 0;
+}
+
+extern "C" int cgfd_batch_times(const cgfd_batch_t *b, float *ms, int *launches)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  *ms = b->t_ms;
+  *launches = b->launches;
+  return 0;
+}
+
+extern "C" int cgfd_batch_fetch(cgfd_batch_t *b)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  for (cgfd_solver_t *s : b->sv) {
+    int rc = cgfd_solver_fetch(s);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+extern "C" int cgfd_batch_reset(cgfd_batch_t *b)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  for (cgfd_solver_t *s : b->sv) {
+    int rc = solver_reset(s);
+    if (rc) return rc;
+  }
+  b->step = 0;
+  b->par = 0;
+  return 0;
+}
+
+extern "C" int cgfd_batch_set_kchunk(cgfd_batch_t *b, int kchunk)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  if (kchunk < 4 || kchunk > 4096) return set_err(CGFD_EINVAL, "kchunk %d out of 4..4096", kchunk);
+  b->kchunk = kchunk;
+  return batch_tables(b);
+}
+
+extern "C" int cgfd_batch_autotune(cgfd_batch_t *b, const int *cand, int ncand, int steps,
+                                   float *ms_out, int *best)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  if (!cand || ncand < 1 || steps < 1 || steps > b->nt_total)
+    return set_err(CGFD_EINVAL, "autotune: bad candidates or steps");
+  float tbest = 0.f;
+  int kbest = b->kchunk;
+  for (int c = 0; c < ncand; c++) {
+    int rc = cgfd_batch_set_kchunk(b, cand[c]);
+    if (!rc) rc = cgfd_batch_run(b, 1);         /* warm-up step */
+    if (!rc) rc = cgfd_batch_run(b, steps < b->nt_total ? steps : b->nt_total - 1);
+    if (rc) return rc;
+    float t = b->t_ms;
+    if (ms_out) ms_out[c] = t;
+    if (c == 0 || t < tbest) { tbest = t; kbest = cand[c]; }
+    rc = cgfd_batch_reset(b);
+    if (rc) return rc;
+  }
+  *best = kbest;
+  return cgfd_batch_set_kchunk(b, kbest);
+}
+
+extern "C" cgfd_solver_t *cgfd_batch_shot(cgfd_batch_t *b, int k)
+{
+  if (!b || k < 0 || k >= b->n) return nullptr;
+  return b->sv[k];
 }

@@ -206,14 +206,23 @@ __device__ __forceinline__ void spml_face(const StageArgs &a, int f, int i,
   }
 }
 
+/* tensor maps and CTA grid of one shot of a batch (global memory; the
+ * tensor maps keep their 64-byte alignment) */
+struct ShotGeo {
+  CUtensorMap wav, met, med, pt, j;
+  int tiles_x, tiles_y, nchunk, cta0;   /* CTA grid of the shot, first CTA */
+  int pad[12];
+};
+
+/* One CTA of the stage: tile (bx, by) of the (i, j) plane, k chunk bz. */
 template <int BX, int BY, int BZ, int KIND, int MED>
-__global__ void __launch_bounds__(NTHREADS, 1)
-    k_stage3(const __grid_constant__ StageArgs a,
-             const __grid_constant__ CUtensorMap tmap,
-             const __grid_constant__ CUtensorMap tmap_met,
-             const __grid_constant__ CUtensorMap tmap_med,
-             const __grid_constant__ CUtensorMap tmap_pt,
-             const __grid_constant__ CUtensorMap tmap_j)
+__device__ __forceinline__ void stage3_body(const StageArgs &a,
+                                            const CUtensorMap &tmap,
+                                            const CUtensorMap &tmap_met,
+                                            const CUtensorMap &tmap_med,
+                                            const CUtensorMap &tmap_pt,
+                                            const CUtensorMap &tmap_j,
+                                            int bx, int by, int bz, bool gmem_maps)
 {
   using L = Slot<MED>;
   constexpr int S_MET = L::S_MET, S_MED = L::S_MED, S_JC = L::S_JC,
@@ -225,9 +234,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const DevGrid &g = a.g;
-  const int i0 = g.ni1 + blockIdx.x * TX;
-  const int j0 = g.nj1 + blockIdx.y * TY;
-  const int kbeg = g.nk1 + blockIdx.z * a.kchunk;
+  const int i0 = g.ni1 + bx * TX;
+  const int j0 = g.nj1 + by * TY;
+  const int kbeg = g.nk1 + bz * a.kchunk;
   const int kend = min(kbeg + a.kchunk - 1, g.nk2);
   const int niter = kend - kbeg + 1;
   constexpr int ZS0 = BZ == 0 ? -1 : -3;
@@ -247,6 +256,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   /* ------------------------------------------------------------------ */
   if (warp == NCW) {
     if (lane != 0) return;
+    if (gmem_maps) {
+      /* tensor maps read from global memory: order the writes that put them
+       * there before the bulk copies read them */
+      const CUtensorMap *maps[5] = {&tmap, &tmap_met, &tmap_med, &tmap_pt, &tmap_j};
+#pragma unroll
+      for (int m = 0; m < 5; m++)
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(
+                         reinterpret_cast<uint64_t>(maps[m]))
+                     : "memory");
+    }
     const int bx0 = i0 + g.xoff - XL;  /* 16-byte aligned box origin */
     const int by0 = j0 - YL;
     const int xs = i0 + g.xoff;        /* stream tiles: no halo */
@@ -599,6 +618,45 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_arrive(&empty_s[it % NS]);
     }
   }
+}
+
+/* the stage of one problem: grid (tiles_x, tiles_y, k chunks) */
+template <int BX, int BY, int BZ, int KIND, int MED>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_stage3(const __grid_constant__ StageArgs a,
+             const __grid_constant__ CUtensorMap tmap,
+             const __grid_constant__ CUtensorMap tmap_met,
+             const __grid_constant__ CUtensorMap tmap_med,
+             const __grid_constant__ CUtensorMap tmap_pt,
+             const __grid_constant__ CUtensorMap tmap_j)
+{
+  stage3_body<BX, BY, BZ, KIND, MED>(a, tmap, tmap_met, tmap_med, tmap_pt, tmap_j,
+                                     blockIdx.x, blockIdx.y, blockIdx.z, false);
+}
+
+/* The same stage for a batch of independent shots in one launch: a 1-D
+ * grid over every shot's CTAs, shot s owning [geo[s].cta0, geo[s+1].cta0);
+ * each CTA reads its shot's arguments and tensor maps from global memory.
+ * All shots share the step's operator biases and RK stage. */
+template <int BX, int BY, int BZ, int KIND, int MED>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_stage3_batch(const StageArgs *__restrict__ args,
+                   const ShotGeo *__restrict__ geo, int nshot)
+{
+  int lo = 0, hi = nshot - 1;
+  const int cta = (int)blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (geo[mid].cta0 <= cta) lo = mid; else hi = mid - 1;
+  }
+  const ShotGeo &G = geo[lo];
+  int c = cta - G.cta0;
+  const int bx = c % G.tiles_x;
+  c /= G.tiles_x;
+  const int by = c % G.tiles_y;
+  const int bz = c / G.tiles_y;
+  stage3_body<BX, BY, BZ, KIND, MED>(args[lo], G.wav, G.met, G.med, G.pt, G.j,
+                                     bx, by, bz, true);
 }
 
 }  // namespace s3

@@ -498,3 +498,83 @@ def _coords_of(p, seed):
 
     X, Y, Z = grid_coords(ni, nj, nk, dh, surface, -(nk - 1) * dh)
     return [np.ascontiguousarray(a, dtype=np.float32).ravel() for a in (X, Y, Z)]
+
+
+# ---------------------------------------------------------------------------
+# batched shots: windows of the topography model (config 3)
+# ---------------------------------------------------------------------------
+
+def _topo_base(ni, nj, nk, seed):
+    """Grid, metrics and layered media of the topography model (padded
+    (nz, ny, nx) arrays)."""
+    dh = 100.0
+    Lx, Ly = (ni - 1) * dh, (nj - 1) * dh
+    rough = gaussian_roughness(ni + 6, nj + 6, dh, 100.0, 1000.0, seed)
+
+    def surface(X, Y):
+        r2 = (X - Lx / 2) ** 2 + (Y - Ly / 2) ** 2
+        return 2000.0 * np.exp(-r2 / 5000.0 ** 2) + rough
+
+    X, Y, Z = grid_coords(ni, nj, nk, dh, surface, -(nk - 1) * dh)
+    met = {k: v.reshape(nk + 6, nj + 6, ni + 6) for k, v in metrics(X, Y, Z).items()}
+    vp, vs, rho = layered(Z, Z[-4], [(3000.0, 4000.0, 2310.0, 2400.0),
+                                     (10000.0, 5500.0, 3175.0, 2650.0),
+                                     (None, 6500.0, 3750.0, 2900.0)])
+    return X, Y, Z, met, vp, vs, rho
+
+
+def moment_random(rng, m0=1e16):
+    """Six i.i.d. N(0,1) components, Frobenius-normalised, times m0:
+    (Mxx, Myy, Mzz, Myz, Mxz, Mxy)."""
+    m = rng.standard_normal(6)
+    fro = math.sqrt(m[0] ** 2 + m[1] ** 2 + m[2] ** 2 + 2 * (m[3] ** 2 + m[4] ** 2 + m[5] ** 2))
+    return tuple(float(m0 * v / fro) for v in m)
+
+
+def window_shots(nshot, base=(400, 400, 200), wmin=(128, 128, 96),
+                 wmax=(256, 256, 160), steps=1000, dt=0.005, npml=12,
+                 seed=2026, nrecv=64, base_model=None):
+    """`nshot` shots, each on its own window of the topography model: window
+    sizes uniform in [wmin, wmax] (seeded), placed inside the base model with
+    the free surface at the top; per shot a source at depth 1-8 km (inside
+    the window, at least PML + 3 cells from its sides), a random moment
+    tensor (six i.i.d. N(0,1) components, Frobenius-normalised), Ricker
+    2 Hz, and `nrecv` surface receivers on a regular grid.  Metrics and
+    media are cropped from the base model (ghost layers are the base
+    model's neighbouring values)."""
+    rng = np.random.default_rng(seed)
+    bni, bnj, bnk = base
+    if base_model is None:
+        base_model = _topo_base(bni, bnj, bnk, seed)
+    X, Y, Z, met, vp, vs, rho = base_model
+    shots = []
+    for s in range(nshot):
+        wi = int(rng.integers(wmin[0], wmax[0] + 1))
+        wj = int(rng.integers(wmin[1], wmax[1] + 1))
+        wk = int(rng.integers(wmin[2], wmax[2] + 1))
+        wi, wj, wk = min(wi, bni), min(wj, bnj), min(wk, bnk)
+        i0 = int(rng.integers(0, bni - wi + 1))
+        j0 = int(rng.integers(0, bnj - wj + 1))
+        k0 = bnk - wk                       # window top = base surface
+        sl = (slice(k0, k0 + wk + 6), slice(j0, j0 + wj + 6), slice(i0, i0 + wi + 6))
+        p = Problem(wi, wj, wk, dt, steps + 1)
+        p.metric = {k: np.ascontiguousarray(v[sl]).ravel() for k, v in met.items()}
+        set_iso_media(p, vp[sl], vs[sl], rho[sl])
+        p.free_top = 1
+        add_pml(p, X[sl], Y[sl], Z[sl], npml, [(0, 0), (0, 1), (1, 0), (1, 1), (2, 0)],
+                vref=6500.0, alpha_max=math.pi * 2.0)
+        margin = npml + 3
+        depth = rng.uniform(1000.0, min(8000.0, (wk - margin - 2) * 100.0))
+        si = p.ni1 + int(rng.integers(margin, wi - margin))
+        sj = p.nj1 + int(rng.integers(margin, wj - margin))
+        sk = p.nk2 - int(round(depth / 100.0))
+        add_moment_source(p, si, sj, sk, moment_random(rng), fc=2.0, t0=0.6,
+                          stf_len=min(steps + 1, 400) * dt)
+        side = int(round(math.sqrt(nrecv)))
+        coords = [(npml + 2 + (wi - 2 * npml - 4) * a / max(side - 1, 1),
+                   npml + 2 + (wj - 2 * npml - 4) * b / max(side - 1, 1))
+                  for a in range(side) for b in range(side)][:nrecv]
+        add_surface_receivers(p, [(int(x), int(y)) for x, y in coords])
+        p.window = dict(i0=i0, j0=j0, k0=k0)
+        shots.append(p)
+    return shots

@@ -115,3 +115,95 @@ def drv_rk_curv_col_allstep_structs(structs, dt, nt_total, t0=0.0,
 def device_bytes(problem):
     c = problem.to_c()
     return _lib.lib().cgfd_device_bytes(C.addressof(c))
+
+
+class Batch:
+    """Independent shots stepped together (cgfd_batch_* of the C ABI): one
+    stage launch per RK stage over every shot's tiles, one CUDA graph per
+    8-step operator cycle.  Results per shot equal a single-shot run."""
+
+    def __init__(self, problems, kchunk=0):
+        self.problems = list(problems)
+        self._c = [p.to_c() for p in self.problems]
+        arr = (C.c_void_p * len(self._c))(*[C.addressof(c) for c in self._c])
+        self._arr = arr
+        self._h = C.c_void_p()
+        _lib.check(_lib.lib().cgfd_batch_create(arr, len(self._c), int(kchunk),
+                                                 C.byref(self._h)))
+
+    def run(self, nsteps):
+        _lib.check(_lib.lib().cgfd_batch_run(self._h, int(nsteps)))
+
+    def times(self):
+        ms, n = C.c_float(), C.c_int()
+        _lib.check(_lib.lib().cgfd_batch_times(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def fetch(self):
+        _lib.check(_lib.lib().cgfd_batch_fetch(self._h))
+
+    def reset(self):
+        _lib.check(_lib.lib().cgfd_batch_reset(self._h))
+
+    def set_kchunk(self, kchunk):
+        _lib.check(_lib.lib().cgfd_batch_set_kchunk(self._h, int(kchunk)))
+
+    def autotune(self, candidates=(8, 12, 16, 24, 32), steps=2, cache=None, key=None):
+        """Pick k planes per CTA by timing `steps` steps per candidate; with
+        `cache` (a JSON file path) and `key`, reuse or record the choice."""
+        import json
+        import os
+        if cache and key and os.path.exists(cache):
+            try:
+                with open(cache) as f:
+                    got = json.load(f).get(key)
+                if got:
+                    self.set_kchunk(got["kchunk"])
+                    return got
+            except (OSError, ValueError):
+                pass
+        cand = (C.c_int * len(candidates))(*candidates)
+        ms = (C.c_float * len(candidates))()
+        best = C.c_int()
+        _lib.check(_lib.lib().cgfd_batch_autotune(self._h, cand, len(candidates),
+                                                   int(steps), ms, C.byref(best)))
+        res = {"kchunk": best.value, "candidates": list(candidates),
+               "ms": [float(v) for v in ms], "steps": int(steps)}
+        if cache and key:
+            data = {}
+            try:
+                with open(cache) as f:
+                    data = json.load(f)
+            except (OSError, ValueError):
+                pass
+            data[key] = res
+            os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+            with open(cache, "w") as f:
+                json.dump(data, f, indent=1)
+        return res
+
+    def shot_pg(self, k):
+        """Peak-motion maps of shot k (15 x ny x nx)."""
+        import numpy as np
+        p = self.problems[k]
+        h = _lib.lib().cgfd_batch_shot(self._h, int(k))
+        out = np.zeros(15 * p.nx * p.ny, np.float32)
+        _lib.check(_lib.lib().cgfd_solver_fetch_pg(h, out.ctypes.data))
+        return out.reshape(15, p.ny, p.nx)
+
+    def close(self):
+        if self._h:
+            _lib.lib().cgfd_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -209,6 +209,48 @@ int cgfd_allstep(const cgfd_problem_t *p);
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);
 
+/* ------------------------------------------------------------------------
+ * Batched shots.  No counterpart in the reference (it runs one shot per
+ * process).  Independent problems that share the medium type (isotropic or
+ * VTI elastic), dt and nt_total step together: every RK stage of every shot
+ * is one kernel launch over all shots' tiles, the receivers and peak-motion
+ * maps one launch each, and whole 8-step cycles of the operator schedule
+ * replay from one CUDA graph.  Each shot keeps the semantics of
+ * cgfd_solver_* (its results equal a single-shot run of its problem).
+ * ---------------------------------------------------------------------- */
+typedef struct cgfd_batch cgfd_batch_t;
+
+/* Uploads every shot (each as cgfd_solver_create) and builds the batch;
+ * kchunk = k planes per CTA (<= 0: default 16). */
+int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot, int kchunk,
+                      cgfd_batch_t **out);
+
+/* Advances every shot by nsteps RK4 steps. */
+int cgfd_batch_run(cgfd_batch_t *b, int nsteps);
+
+/* Device time (CUDA events) and kernel launches of the last cgfd_batch_run. */
+int cgfd_batch_times(const cgfd_batch_t *b, float *ms, int *launches);
+
+/* cgfd_solver_fetch for every shot (results into each shot's problem). */
+int cgfd_batch_fetch(cgfd_batch_t *b);
+
+/* Every shot back at step 0 with its problem's host inputs. */
+int cgfd_batch_reset(cgfd_batch_t *b);
+
+/* k planes per CTA of the batched stage kernel. */
+int cgfd_batch_set_kchunk(cgfd_batch_t *b, int kchunk);
+
+/* Times `steps` steps for each candidate kchunk (after one warm-up step),
+ * resetting the shots after each, and keeps the fastest: ms[c] receives the
+ * times, *best the kchunk chosen.  The shots are at step 0 afterwards. */
+int cgfd_batch_autotune(cgfd_batch_t *b, const int *cand, int ncand, int steps,
+                        float *ms, int *best);
+
+/* The solver of shot k (for cgfd_solver_fetch_* on one shot), or NULL. */
+cgfd_solver_t *cgfd_batch_shot(cgfd_batch_t *b, int k);
+
+void cgfd_batch_destroy(cgfd_batch_t *b);
+
 /* No counterpart in the reference.  NaN/Inf test of a device array the
  * caller owns that allocates no device memory, for callers that cannot call
  * cudaMalloc (a process whose device memory belongs to another framework's
