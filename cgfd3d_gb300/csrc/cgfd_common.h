@@ -115,4 +115,8 @@ struct StageArgs {
   int kchunk;                  /* planes per CTA along k */
 };
 
+/* StageArgs is copied word by word into shared memory by the batched stage
+ * kernel */
+static_assert(sizeof(StageArgs) % 4 == 0, "StageArgs size");
+
 #endif

@@ -1806,6 +1806,7 @@ extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
       if (b->med == MED_VTI) cgfd_launch_stage_batch_vti(code, kind, 0, b->stream, nullptr, nullptr, 0);
       else cgfd_launch_stage_batch_iso(code, kind, 0, b->stream, nullptr, nullptr, 0);
     }
+  BTRYC(cudaGetLastError());
   BTRY(batch_tables(b));
   *out = b;
   return 0;

@@ -655,8 +655,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   c /= G.tiles_x;
   const int by = c % G.tiles_y;
   const int bz = c / G.tiles_y;
-  stage3_body<BX, BY, BZ, KIND, MED>(args[lo], G.wav, G.met, G.med, G.pt, G.j,
-                                     bx, by, bz, true);
+  /* the shot's arguments in shared memory where the CTA's 227 KB allow
+   * it: the stage reads them all through its loops, and shared loads are
+   * cheaper than re-reading global memory.  The body reads the tile
+   * geometry from them before its own first barrier, so the copy
+   * completes here. */
+  constexpr bool kArgsInSmem =
+      Slot<MED>::SMEM_BYTES + (int)sizeof(StageArgs) + 256 <= 232448;
+  if constexpr (kArgsInSmem) {
+    __shared__ __align__(16) StageArgs sa;
+    const int n4 = (int)(sizeof(StageArgs) / 4);
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(args + lo);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
+    for (int t = threadIdx.x; t < n4; t += blockDim.x) dst[t] = src[t];
+    __syncthreads();
+    stage3_body<BX, BY, BZ, KIND, MED>(sa, G.wav, G.met, G.med, G.pt, G.j, bx, by,
+                                       bz, true);
+  } else {
+    stage3_body<BX, BY, BZ, KIND, MED>(args[lo], G.wav, G.met, G.med, G.pt, G.j,
+                                       bx, by, bz, true);
+  }
 }
 
 }  // namespace s3
