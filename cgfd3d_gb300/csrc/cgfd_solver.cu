@@ -714,6 +714,19 @@ static int validate(const cgfd_problem_t *p)
         return set_err(CGFD_EINVAL, "PML face %d/%d box outside the grid", d, s);
       if (!f->A || !f->B || !f->D || !f->aux)
         return set_err(CGFD_EINVAL, "PML face %d/%d arrays missing", d, s);
+      /* a face box is the physical box cut down along its normal only
+       * (forward/bdry_t.c:160-186); the stage kernel relies on it */
+      int lo[3] = {f->ni1, f->nj1, f->nk1}, hi[3] = {f->ni2, f->nj2, f->nk2};
+      int glo[3] = {p->ni1, p->nj1, p->nk1}, ghi[3] = {p->ni2, p->nj2, p->nk2};
+      for (int e = 0; e < 3; e++) {
+        if (e == d) {
+          if ((s == 0 && lo[e] != glo[e]) || (s == 1 && hi[e] != ghi[e]))
+            return set_err(CGFD_EINVAL, "PML face %d/%d does not start at its side", d, s);
+        } else if (lo[e] != glo[e] || hi[e] != ghi[e]) {
+          return set_err(CGFD_EINVAL, "PML face %d/%d does not span the grid across "
+                         "its normal", d, s);
+        }
+      }
     }
   if (p->recv_n > 0 && (!p->recv_dijk || !p->recv_indx1d || !p->recv_seismo))
     return set_err(CGFD_EINVAL, "receiver arrays missing");

@@ -98,14 +98,16 @@ __device__ __forceinline__ bool in_face(const DevFace &F, int i, int j, int k)
          k >= F.k1 && k <= F.k2;
 }
 
-/* L2 prefetch of the auxiliary variables a stage reads at (i, j, k) */
+/* L2 prefetch of the auxiliary variables a stage reads at (i, j, k) of the
+ * faces in `mask` (bit f: face f holds the point) */
 template <int KIND>
-__device__ __forceinline__ void prefetch_aux(const StageArgs &a, int i, int j, int k)
+__device__ __forceinline__ void prefetch_aux(const StageArgs &a, int i, int j, int k,
+                                             int mask)
 {
-#pragma unroll 1
+#pragma unroll
   for (int f = 0; f < CGFD_NFACE; f++) {
+    if (!(mask & (1 << f))) continue;
     const DevFace &F = a.face[f];
-    if (!in_face(F, i, j, k)) continue;
     const long long av = F.avol;
     const long long ai = (long long)(i - F.i1) + (long long)(j - F.j1) * F.bx +
                          (long long)(k - F.k1) * F.bx * F.by;
@@ -355,17 +357,20 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
     if (a.face[4].on) kz1_top = a.face[4].k2;
     if (a.face[5].on) kz2_bot = a.face[5].k1;
   }
-  auto in_pml = [&](int kk) {
-    return fmask_xy != 0 || kk <= kz1_top || kk >= kz2_bot;
+  /* faces holding the point at plane kk: x/y faces span every k, z faces
+   * every (i, j) (forward/bdry_t.c:168-186) */
+  auto pml_mask = [&](int kk) {
+    return fmask_xy | (kk <= kz1_top ? 16 : 0) | (kk >= kz2_bot ? 32 : 0);
   };
-  if (a.pml_fused && valid && in_pml(kbeg)) prefetch_aux<KIND>(a, i, j, kbeg);
+  if (a.pml_fused && valid && pml_mask(kbeg))
+    prefetch_aux<KIND>(a, i, j, kbeg, pml_mask(kbeg));
 
   for (int it = 0; it < niter; it++) {
     const int k = kbeg + it;
     const int rtop = it + 4;
-    const bool pml_here = a.pml_fused && valid && in_pml(k);
-    if (a.pml_fused && valid && it + 1 < niter && in_pml(k + 1))
-      prefetch_aux<KIND>(a, i, j, k + 1);
+    const int pmask = (a.pml_fused && valid) ? pml_mask(k) : 0;
+    if (a.pml_fused && valid && it + 1 < niter && pml_mask(k + 1))
+      prefetch_aux<KIND>(a, i, j, k + 1, pml_mask(k + 1));
 #pragma unroll
     for (int n = 0; n < 5; n++) {
       int rel = rtop - 4 + n;
@@ -481,19 +486,21 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       }
 
       /* CFS-PML, faces in the reference order x1, x2, y1, y2, z1, z2 */
-      if (pml_here) {
-#pragma unroll 1
+      if (pmask) {
+        /* unrolled over the faces: every face parameter is a static
+         * operand of the kernel's parameter space */
+#pragma unroll
         for (int f = 0; f < CGFD_NFACE; f++) {
+          if (!(pmask & (1 << f))) continue;
           const DevFace &F = a.face[f];
-          if (!in_face(F, i, j, k)) continue;
           AuxPt<KIND> pax;
           load_aux<KIND>(a, f, aux_index<KIND>(F, i, j, k), pax);
           float d[9];
-          if (F.dim == 0) {
+          if (f < 2) {
 #pragma unroll
             for (int c = 0; c < 9; c++) d[c] = DX(c);
             spml_face<KIND, MED>(a, f, i, j, k, q, d, xix, xiy, xiz, ztx, zty, ztz, m, pax, r);
-          } else if (F.dim == 1) {
+          } else if (f < 4) {
 #pragma unroll
             for (int c = 0; c < 9; c++) d[c] = DY(c);
             spml_face<KIND, MED>(a, f, i, j, k, q, d, etx, ety, etz, ztx, zty, ztz, m, pax, r);
