@@ -373,8 +373,10 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       prefetch_aux<KIND>(a, i, j, k + 1, pml_mask(k + 1));
 #pragma unroll
     for (int n = 0; n < 5; n++) {
+      /* the window's older planes were waited for in earlier iterations:
+       * only the first iteration waits for all five */
       int rel = rtop - 4 + n;
-      wait_full(&full_w[rel % NB], (rel / NB) & 1, a.err);
+      if (it == 0 || n == 4) wait_full(&full_w[rel % NB], (rel / NB) & 1, a.err);
     }
     wait_full(&full_s[it % NS], (it / NS) & 1, a.err);
     Win w;
