@@ -48,7 +48,7 @@ WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "visco": dict(ni=300, nj=300, nk=150),
              "flat": dict(ni=100, nj=100, nk=60)}
 SAMPLE_NK = 24                 # CPU sample: same model, 24 planes deep
-CPU_SAMPLE_S = 12.0            # target seconds of CPU work per baseline sample
+CPU_SAMPLE_S = 24.0            # target seconds of CPU work per baseline sample
 
 
 def parse():
@@ -226,6 +226,10 @@ def pin_problem(p):
     p.Ylam = [pinned(a) for a in p.Ylam]
     p.Ymu = [pinned(a) for a in p.Ymu]
     p.wav = pinned(p.wav)
+    for row in p.pml:
+        for f in row:
+            if f is not None:
+                f["aux"] = pinned(f["aux"])
     return holders
 
 

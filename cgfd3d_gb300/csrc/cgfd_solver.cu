@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <string>
 #include <vector>
 
@@ -48,6 +49,35 @@ static int set_err(int code, const char *fmt, ...)
   g_err = buf;
   return code;
 }
+
+/* CGFD_TRACE=1: phase timings of the solver set-up on stderr (the device
+ * work of each phase is waited for, so the trace changes the timing) */
+struct SetupTrace {
+  bool on = false;
+  cudaStream_t st = nullptr;
+  double t0 = 0.0;
+  static double now()
+  {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return ts.tv_sec + 1e-9 * ts.tv_nsec;
+  }
+  void start(cudaStream_t s)
+  {
+    const char *e = getenv("CGFD_TRACE");
+    on = e && atoi(e) != 0;
+    st = s;
+    t0 = now();
+  }
+  void mark(const char *what)
+  {
+    if (!on) return;
+    cudaStreamSynchronize(st);
+    double t = now();
+    fprintf(stderr, "cgfd setup: %-28s %8.2f ms\n", what, 1e3 * (t - t0));
+    t0 = t;
+  }
+};
 
 #define CK(call)                                                              \
   do {                                                                        \
@@ -619,6 +649,7 @@ struct cgfd_solver {
   int graph_pre_lev;
   int *d_err;
   float *pg, *dis;              /* surface peak-motion maps (free top) */
+  float *staging;               /* upload staging volume (set-up only) */
   StageMaps maps;               /* tensor maps of the stage kernel */
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
   int ty;                       /* tile rows of the medium's stage kernel */
@@ -784,13 +815,45 @@ static int dalloc(cgfd_solver_t *s, T **ptr, size_t n)
   return 0;
 }
 
+/* reference layout (nx*ny*nz, contiguous) -> pitched device layout */
+__global__ void k_repitch(DevGrid g, const float *__restrict__ src, float *dst)
+{
+  const int rows = g.ny * g.nz;                 /* row r = j + k*ny */
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const float *a = src + (long long)r * g.nx;
+    float *b = dst + g.xoff + (long long)r * g.px;
+    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) b[i] = a[i];
+  }
+}
+
+/* One host volume into the pitched device layout: a contiguous copy into a
+ * device staging buffer, then a re-pitch kernel (a strided host-to-device
+ * copy with rows of nx floats measured ~35 GB/s on GB300; the contiguous
+ * copy runs at the link's rate).  The staging buffer lives until
+ * release_staging(). */
 static cudaError_t upload_volume(cgfd_solver_t *s, float *dst, const float *src)
 {
   const DevGrid &g = s->g;
-  s->h2d_bytes += (size_t)g.nx * g.ny * g.nz * sizeof(float);
-  return cudaMemcpy2DAsync(dst + g.xoff, (size_t)g.px * sizeof(float), src,
-                           (size_t)g.nx * sizeof(float), (size_t)g.nx * sizeof(float),
-                           (size_t)g.ny * g.nz, cudaMemcpyHostToDevice, s->stream);
+  const size_t n = (size_t)g.nx * g.ny * g.nz;
+  s->h2d_bytes += n * sizeof(float);
+  if (!s->staging) {
+    cudaError_t e = cudaMalloc((void **)&s->staging, n * sizeof(float));
+    if (e != cudaSuccess) return e;
+  }
+  cudaError_t e = cudaMemcpyAsync(s->staging, src, n * sizeof(float),
+                                  cudaMemcpyHostToDevice, s->stream);
+  if (e != cudaSuccess) return e;
+  k_repitch<<<152 * 8, 256, 0, s->stream>>>(g, s->staging, dst);
+  return cudaGetLastError();
+}
+
+static void release_staging(cgfd_solver_t *s)
+{
+  if (s->staging) {
+    cudaStreamSynchronize(s->stream);
+    cudaFree(s->staging);
+    s->staging = nullptr;
+  }
 }
 
 static cudaError_t download_volume(cgfd_solver_t *s, float *dst, const float *src)
@@ -875,7 +938,7 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
                   s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
                   s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
                   s->line_iptr, s->d_it, s->d_flag, s->d_err, s->pg, s->dis,
-                  s->sf, s->sf_w, s->frate, s->surf};
+                  s->sf, s->sf_w, s->frate, s->surf, s->staging};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (int f = 0; f < CGFD_NFACE; f++)
@@ -922,7 +985,10 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   /* wavefield: level 0 of the input copied into all four levels, so that
    * ghost values stay what the caller passed (they never change in the
    * reference either: rhs ghosts are zero) */
+  SetupTrace tr;
+  tr.start(st);
   TRY(dalloc(s, &s->wav, 4 * L));
+  tr.mark("allocate wavefield");
   TRYC(cudaMemsetAsync(s->wav, 0, L * sizeof(float), st));
   for (int c = 0; c < s->ncmp; c++)
     TRYC(upload_volume(s, s->wav + c * vol, p->wav + (size_t)c * hvol));
@@ -932,12 +998,14 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
 
   s->pre_lev = 0;
   s->end_lev = 3;
+  tr.mark("upload wavefield");
   TRY(dalloc(s, &s->metric, 10 * vol));
   TRYC(cudaMemsetAsync(s->metric, 0, 10 * vol * sizeof(float), st));
   const float *mh[10] = {p->jac, p->xi_x, p->xi_y, p->xi_z, p->eta_x,
                          p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
   for (int m = 0; m < 10; m++)
     TRYC(upload_volume(s, s->metric + m * vol, mh[m]));
+  tr.mark("metrics");
   TRY(dalloc(s, &s->media, (size_t)s->nmed * vol));
   TRYC(cudaMemsetAsync(s->media, 0, (size_t)s->nmed * vol * sizeof(float), st));
   {
@@ -957,6 +1025,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     for (int m = 0; m < nm; m++)
       TRYC(upload_volume(s, s->media + m * vol, md[m]));
   }
+  tr.mark("media");
   /* PML faces */
   int nf = 0;
   for (int d = 0; d < 3; d++)
@@ -994,6 +1063,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
       s->h2d_bytes += al * sizeof(float) + 3 * np * sizeof(float);
     }
   (void)nf;
+  tr.mark("PML faces");
   /* free surface matrices, computed on the device */
   if (p->free_top) {
     size_t n2 = (size_t)g.nx * g.ny * 9;
@@ -1029,6 +1099,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     }
     TRYC(cudaGetLastError());
   }
+  tr.mark("surface matrices");
   /* sources */
   if (p->src_n > 0) {
     std::vector<int> col;
@@ -1098,6 +1169,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
       cudaStreamSynchronize(st);       /* host vectors go out of scope */
     }
   }
+  tr.mark("sources");
   /* receivers and lines */
   if (p->recv_n > 0) {
     TRY(dalloc(s, &s->recv_dijk, 3 * (size_t)p->recv_n));
@@ -1159,8 +1231,11 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     s->kchunk = (g.nk + nch - 1) / nch;
     if (const char *e = getenv("CGFD_KCHUNK")) s->kchunk = std::max(4, atoi(e));
   }
+  tr.mark("receivers, counters");
   TRY(make_tmap(s));
   TRYC(cudaStreamSynchronize(st));
+  release_staging(s);
+  tr.mark("tensor maps");
   *out = s;
   return 0;
 #undef TRY
@@ -1585,6 +1660,7 @@ static int solver_reset(cgfd_solver_t *s)
   }
   CK(cudaMemsetAsync(s->d_it, 0, 4, st));
   CK(cudaStreamSynchronize(st));
+  release_staging(s);
   s->step = 0;
   s->pre_lev = 0;
   s->end_lev = 3;
