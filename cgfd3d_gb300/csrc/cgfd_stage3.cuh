@@ -296,8 +296,13 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       mbar_expect_tx(&full_s[b], slot_bytes);
       tma_load_4d(dst + S_MET, &tmap_met, xs, j0, k, 0, &full_s[b]);
       tma_load_4d(dst + S_MED, &tmap_med, xs, j0, k, 0, &full_s[b]);
-      if (MED == MED_VIS)
+      if (MED == MED_VIS) {
         tma_load_5d(dst + S_JC, &tmap_j, xs, j0, k, 9, a.cur_level, &full_s[b]);
+        /* the memory variables' pre/end values are read directly by the
+         * consumers (no shared memory left): bring them into L2 now */
+        if (KIND == 1) tma_prefetch_5d(&tmap_j, xs, j0, k, 9, a.pre_level);
+        if (KIND >= 1) tma_prefetch_5d(&tmap_j, xs, j0, k, 9, a.end_level);
+      }
       if (KIND == 1) tma_load_5d(dst + S_PRE, &tmap_pt, xs, j0, k, 0, a.pre_level, &full_s[b]);
       if (KIND >= 1) tma_load_5d(dst + S_END, &tmap_pt, xs, j0, k, 0, a.end_level, &full_s[b]);
     };
