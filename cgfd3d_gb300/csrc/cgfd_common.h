@@ -66,7 +66,8 @@ struct SrcEntry {
   float vf;       /* coef * slw / jac  (force weight) */
   float rjac;     /* coef / jac        (moment weight) */
   int force_on;   /* force applied at this point (strict surface rule) */
-  int pad;
+  float coef;     /* spatial weight (1 for a point source) */
+  long long q;    /* device index of the point (weights filled on the device) */
 };
 
 /* Maxwell bodies the fused visco-elastic path holds in shared memory */

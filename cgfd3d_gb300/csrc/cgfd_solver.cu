@@ -422,6 +422,83 @@ __global__ void k_surf_layer(DevGrid g, int nsf, const SurfForce *__restrict__ s
   }
 }
 
+/* grid metrics of the physical points from the node coordinates
+ * (forward/gd_t.c:238-290): centred 7-point derivatives along i, j, k
+ * (forward/fd_t.c:152-176), the Jacobian (x_xi x x_et) . x_zt, and the
+ * contravariant metrics as cross products over it.  Grid (ni/32, nj/8, nk). */
+__global__ void k_metric(DevGrid g, const float *__restrict__ x,
+                         const float *__restrict__ y, const float *__restrict__ z,
+                         float *m)
+{
+  const int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = g.nk1 + blockIdx.z;
+  if (i > g.ni2 || j > g.nj2) return;
+  const long long q = (i + g.xoff) + (long long)j * g.px + (long long)k * g.sl;
+  const float fc[7] = {-0.02084f, 0.1667f, -0.7709f, 0.0f, 0.7709f, -0.1667f, 0.02084f};
+  const float *X[3] = {x, y, z};
+  const long long st[3] = {1, g.px, g.sl};
+  float d[3][3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float v = 0.f;
+#pragma unroll
+      for (int n = 0; n < 7; n++) v += fc[n] * X[c][q + (n - 3) * st[ax]];
+      d[ax][c] = v;
+    }
+  auto cross = [](const float *A, const float *B, float *C) {
+    C[0] = A[1] * B[2] - A[2] * B[1];
+    C[1] = A[2] * B[0] - A[0] * B[2];
+    C[2] = A[0] * B[1] - A[1] * B[0];
+  };
+  float gv[3];
+  cross(d[0], d[1], gv);
+  const float jac = gv[0] * d[2][0] + gv[1] * d[2][1] + gv[2] * d[2][2];
+  const long long v = g.vol;
+  m[q] = jac;
+  const int pa[3] = {1, 2, 0}, pb[3] = {2, 0, 1};
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    cross(d[pa[r]], d[pb[r]], gv);
+#pragma unroll
+    for (int c = 0; c < 3; c++) m[(1 + 3 * r + c) * v + q] = gv[c] / jac;
+  }
+}
+
+/* ghost layers of the metrics: mirrored about the physical boundary along
+ * x, then y, then z (forward/gd_t.c:291-401) -- a ghost point takes the
+ * value of the physical point whose index is mirrored in every direction */
+__global__ void k_metric_ghost(DevGrid g, float *m)
+{
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nx), j = (int)((t / g.nx) % g.ny), k = (int)(t / ((long long)g.nx * g.ny));
+    const int mi = i < g.ni1 ? 2 * g.ni1 - 1 - i : (i > g.ni2 ? 2 * g.ni2 + 1 - i : i);
+    const int mj = j < g.nj1 ? 2 * g.nj1 - 1 - j : (j > g.nj2 ? 2 * g.nj2 + 1 - j : j);
+    const int mk = k < g.nk1 ? 2 * g.nk1 - 1 - k : (k > g.nk2 ? 2 * g.nk2 + 1 - k : k);
+    if (mi == i && mj == j && mk == k) continue;
+    const long long q = (i + g.xoff) + (long long)j * g.px + (long long)k * g.sl;
+    const long long s = (mi + g.xoff) + (long long)mj * g.px + (long long)mk * g.sl;
+    for (int c = 0; c < 10; c++) m[c * g.vol + q] = m[c * g.vol + s];
+  }
+}
+
+/* source weights at their points: force coef*slw/jac, moment coef/jac
+ * (forward/sv_curv_col_el.c:381-470) from the device media and metrics */
+__global__ void k_src_weights(DevGrid g, SrcEntry *ent, int n,
+                              const float *__restrict__ slw,
+                              const float *__restrict__ jac)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const float j = jac[ent[e].q], c = ent[e].coef;
+  ent[e].vf = c * slw[ent[e].q] / j;
+  ent[e].rjac = c / j;
+}
+
 /* receivers and lines after a step; one block; advances the step counter.
  * Trilinear weights as forward/io_funcs.c:1595-1612, which uses corner 5
  * twice and corner 4 never (harmless for receivers on a grid plane). */
@@ -555,10 +632,11 @@ static int build_source_entries(const cgfd_problem_t *p, std::vector<int> &col,
       h.col = (si - p->ni1) + (sj - p->nj1) * p->ni;
       h.e.k = sk;
       h.e.is = is;
-      h.e.vf = p->slw[q] / p->jac[q];
-      h.e.rjac = (float)(1.0 / (double)p->jac[q]);
+      h.e.coef = 1.0f;
+      h.e.q = q;                   /* host index; vf, rjac on the device */
+      h.e.vf = 0.f;
+      h.e.rjac = 0.f;
       h.e.force_on = (p->src_surface_strict == 0 || sk < p->nk2);
-      h.e.pad = 0;
       all.push_back(h);
     } else {
       int half = p->src_ext_half;
@@ -580,10 +658,11 @@ static int build_source_entries(const cgfd_problem_t *p, std::vector<int> &col,
             h.col = (i - p->ni1) + (j - p->nj1) * p->ni;
             h.e.k = k;
             h.e.is = is;
-            h.e.vf = c * p->slw[q] / p->jac[q];
-            h.e.rjac = c / p->jac[q];
+            h.e.coef = c;
+            h.e.q = q;
+            h.e.vf = 0.f;
+            h.e.rjac = 0.f;
             h.e.force_on = (p->src_surface_strict == 0 || k < p->nk2);
-            h.e.pad = 0;
             all.push_back(h);
           }
     }
@@ -731,8 +810,15 @@ static int validate(const cgfd_problem_t *p)
       if (p->src_force_rate_indx[n] < 0 || p->src_force_rate_indx[n] >= p->src_n)
         return set_err(CGFD_EINVAL, "surface force %d: bad source index", n);
   }
-  if (!p->jac || !p->xi_x || !p->slw || !p->wav)
-    return set_err(CGFD_EINVAL, "missing input array");
+  if (!p->slw || !p->wav) return set_err(CGFD_EINVAL, "missing input array");
+  if (p->jac) {
+    const float *mh[10] = {p->jac, p->xi_x, p->xi_y, p->xi_z, p->eta_x,
+                           p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
+    for (int m = 0; m < 10; m++)
+      if (!mh[m]) return set_err(CGFD_EINVAL, "metric array %d missing", m);
+  } else if (!p->x3d || !p->y3d || !p->z3d) {
+    return set_err(CGFD_EINVAL, "neither metrics nor grid coordinates given");
+  }
   if (p->medium_type != CGFD_MEDIUM_ELASTIC_VTI && (!p->lambda || !p->mu))
     return set_err(CGFD_EINVAL, "missing lambda/mu");
   for (int d = 0; d < 3; d++)
@@ -845,6 +931,30 @@ static cudaError_t upload_volume(cgfd_solver_t *s, float *dst, const float *src)
   if (e != cudaSuccess) return e;
   k_repitch<<<152 * 8, 256, 0, s->stream>>>(g, s->staging, dst);
   return cudaGetLastError();
+}
+
+/* metrics (10 volumes, device layout) from host grid coordinates */
+static int device_metrics(cgfd_solver_t *s, const float *x3d, const float *y3d,
+                          const float *z3d, float *metric)
+{
+  const DevGrid &g = s->g;
+  float *xyz = nullptr;
+  CK(cudaMalloc((void **)&xyz, 3 * (size_t)g.vol * sizeof(float)));
+  cudaError_t e = cudaMemsetAsync(xyz, 0, 3 * (size_t)g.vol * sizeof(float), s->stream);
+  const float *src[3] = {x3d, y3d, z3d};
+  for (int c = 0; c < 3 && e == cudaSuccess; c++)
+    e = upload_volume(s, xyz + c * g.vol, src[c]);
+  if (e == cudaSuccess) {
+    dim3 b(32, 8), gr((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk);
+    k_metric<<<gr, b, 0, s->stream>>>(g, xyz, xyz + g.vol, xyz + 2 * g.vol, metric);
+    k_metric_ghost<<<152 * 8, 256, 0, s->stream>>>(g, metric);
+    e = cudaGetLastError();
+  }
+  cudaError_t e2 = cudaStreamSynchronize(s->stream);
+  cudaFree(xyz);
+  CK(e);
+  CK(e2);
+  return 0;
 }
 
 static void release_staging(cgfd_solver_t *s)
@@ -1001,10 +1111,15 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   tr.mark("upload wavefield");
   TRY(dalloc(s, &s->metric, 10 * vol));
   TRYC(cudaMemsetAsync(s->metric, 0, 10 * vol * sizeof(float), st));
-  const float *mh[10] = {p->jac, p->xi_x, p->xi_y, p->xi_z, p->eta_x,
-                         p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
-  for (int m = 0; m < 10; m++)
-    TRYC(upload_volume(s, s->metric + m * vol, mh[m]));
+  if (p->jac) {
+    const float *mh[10] = {p->jac, p->xi_x, p->xi_y, p->xi_z, p->eta_x,
+                           p->eta_y, p->eta_z, p->zeta_x, p->zeta_y, p->zeta_z};
+    for (int m = 0; m < 10; m++)
+      TRYC(upload_volume(s, s->metric + m * vol, mh[m]));
+  } else {
+    /* no metrics given: computed here from the grid coordinates */
+    TRY(device_metrics(s, p->x3d, p->y3d, p->z3d, s->metric));
+  }
   tr.mark("metrics");
   TRY(dalloc(s, &s->media, (size_t)s->nmed * vol));
   TRYC(cudaMemsetAsync(s->media, 0, (size_t)s->nmed * vol * sizeof(float), st));
@@ -1105,6 +1220,7 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     std::vector<int> col;
     std::vector<SrcEntry> ent;
     build_source_entries(p, col, ent);
+    for (SrcEntry &e : ent) e.q = dev_index(g, e.q);
     s->nsrc_ent = (int)ent.size();
     TRY(dalloc(s, &s->src_col, col.size()));
     TRYC(cudaMemcpyAsync(s->src_col, col.data(), col.size() * 4, cudaMemcpyHostToDevice, st));
@@ -1112,6 +1228,12 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     if (!ent.empty())
       TRYC(cudaMemcpyAsync(s->src_ent, ent.data(), ent.size() * sizeof(SrcEntry),
                            cudaMemcpyHostToDevice, st));
+    if (!ent.empty()) {
+      /* weights coef*slw/jac and coef/jac from the device media and metrics */
+      k_src_weights<<<(unsigned)((ent.size() + 127) / 128), 128, 0, st>>>(
+          g, s->src_ent, (int)ent.size(), s->media, s->metric);
+      TRYC(cudaGetLastError());
+    }
     TRY(dalloc(s, &s->src_it_begin, p->src_n));
     TRY(dalloc(s, &s->src_it_end, p->src_n));
     TRYC(cudaMemcpyAsync(s->src_it_begin, p->src_it_begin, p->src_n * 4, cudaMemcpyHostToDevice, st));
@@ -2057,4 +2179,51 @@ extern "C" cgfd_solver_t *cgfd_batch_shot(cgfd_batch_t *b, int k)
 {
   if (!b || k < 0 || k >= b->n) return nullptr;
   return b->sv[k];
+}
+
+/* ------------------------------------------------------------------------ */
+/* grid metrics on the device (forward/gd_t.c:190-402)                       */
+/* ------------------------------------------------------------------------ */
+
+extern "C" int cgfd_metric_calc(int nx, int ny, int nz, int ni1, int ni2, int nj1,
+                                int nj2, int nk1, int nk2, const float *x3d,
+                                const float *y3d, const float *z3d, float *metric)
+{
+  if (!x3d || !y3d || !z3d || !metric) return set_err(CGFD_EINVAL, "null array");
+  if (ni1 != 3 || nj1 != 3 || nk1 != 3 || nx != ni2 + 4 || ny != nj2 + 4 ||
+      nz != nk2 + 4 || ni2 < ni1 || nj2 < nj1 || nk2 < nk1)
+    return set_err(CGFD_EINVAL, "grid indices are not the 3-ghost layout");
+  cgfd_solver_t tmp{};
+  cgfd_solver_t *s = &tmp;
+  DevGrid &g = s->g;
+  g.nx = nx; g.ny = ny; g.nz = nz;
+  g.ni = ni2 - ni1 + 1; g.nj = nj2 - nj1 + 1; g.nk = nk2 - nk1 + 1;
+  g.ni1 = ni1; g.ni2 = ni2; g.nj1 = nj1; g.nj2 = nj2; g.nk1 = nk1; g.nk2 = nk2;
+  g.xoff = XOFF;
+  g.px = pitch_for(g.ni);
+  g.sl = (long long)g.px * ny;
+  g.vol = g.sl * nz;
+  CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  float *m = nullptr;
+  int rc = 0;
+  cudaError_t e = cudaMalloc((void **)&m, 10 * (size_t)g.vol * sizeof(float));
+  if (e != cudaSuccess) rc = set_err(CGFD_ENOMEM, "cudaMalloc: %s", cudaGetErrorString(e));
+  if (!rc) {
+    e = cudaMemsetAsync(m, 0, 10 * (size_t)g.vol * sizeof(float), s->stream);
+    if (e != cudaSuccess) rc = set_err(CGFD_ECUDA, "memset: %s", cudaGetErrorString(e));
+  }
+  if (!rc) rc = device_metrics(s, x3d, y3d, z3d, m);
+  const size_t hvol = (size_t)nx * ny * nz;
+  for (int c = 0; c < 10 && !rc; c++) {
+    e = download_volume(s, metric + c * hvol, m + c * g.vol);
+    if (e != cudaSuccess) rc = set_err(CGFD_ECUDA, "download: %s", cudaGetErrorString(e));
+  }
+  if (!rc) {
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) rc = set_err(CGFD_ECUDA, "sync: %s", cudaGetErrorString(e));
+  }
+  release_staging(s);
+  if (m) cudaFree(m);
+  cudaStreamDestroy(s->stream);
+  return rc;
 }

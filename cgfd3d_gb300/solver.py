@@ -207,3 +207,19 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def metric_calc(dims, x3d, y3d, z3d):
+    """Grid metrics on the GPU from node coordinates (cgfd_metric_calc):
+    dims = (ni, nj, nk, nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2); returns a
+    dict jac, xi_x, ..., zeta_z of flat float32 arrays (reference layout)."""
+    import numpy as np
+    from . import abi
+    ni, nj, nk, nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2 = [int(v) for v in dims]
+    x, y, z = [np.ascontiguousarray(a, np.float32).ravel() for a in (x3d, y3d, z3d)]
+    out = np.zeros(10 * nx * ny * nz, np.float32)
+    _lib.check(_lib.lib().cgfd_metric_calc(nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2,
+                                            x.ctypes.data, y.ctypes.data,
+                                            z.ctypes.data, out.ctypes.data))
+    v = nx * ny * nz
+    return {n: out[c * v:(c + 1) * v] for c, n in enumerate(abi.METRIC_NAMES)}

@@ -206,6 +206,17 @@ void cgfd_solver_destroy(cgfd_solver_t *s);
  * create + run(nt_total) + fetch + destroy. */
 int cgfd_allstep(const cgfd_problem_t *p);
 
+/* Grid metrics on the device, as the reference's gd_curv_metric_cal
+ * (forward/gd_t.c:190-402): from the node coordinates x3d/y3d/z3d
+ * (nx*ny*nz each, ghosts included, 3-ghost layout) into `metric` =
+ * 10 x nx*ny*nz host floats in the order jac, xi_x, xi_y, xi_z, eta_x,
+ * eta_y, eta_z, zeta_x, zeta_y, zeta_z, ghost layers mirrored.  A problem
+ * whose jac is NULL but whose x3d/y3d/z3d are set gets its metrics computed
+ * this way inside cgfd_solver_create. */
+int cgfd_metric_calc(int nx, int ny, int nz, int ni1, int ni2, int nj1, int nj2,
+                     int nk1, int nk2, const float *x3d, const float *y3d,
+                     const float *z3d, float *metric);
+
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);
 

@@ -26,6 +26,8 @@
  *   receivers / lines    forward/io_funcs.c:1584-1645
  *   free-surface matrices forward/sv_curv_col_el_iso.c:1258-1375,
  *                        lib/fdlib_math.c:8-48
+ *   grid metrics         forward/gd_t.c:190-402 (set-up, restated for the
+ *                        device metric calculation's parity)
  *   VTI media            forward/sv_curv_col_el_vti.c:200-397 (interior),
  *                        :407-590 (vlow), :592-1075 (CFS-PML),
  *                        :1085-1206 (free-surface matrices)
@@ -1308,5 +1310,80 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
   free(o.TS);
   free(o.VS);
   free(o.dis);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* grid metrics (forward/gd_t.c:190-402)                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Restatement of gd_curv_metric_cal: centred 7-point derivatives of the
+ * node coordinates along i, j, k (all seven taps, the zero centre
+ * included, left to right), the Jacobian as (x_xi x x_et) . x_zt and the
+ * contravariant metrics as cross products over it, then the ghost layers
+ * mirrored x, y, z in turn.  out: 10 x nx*ny*nz (jac, xi_x..zeta_z). */
+int oracle_metric_calc(int nx, int ny, int nz, int ni1, int ni2, int nj1,
+                       int nj2, int nk1, int nk2, const float *x3d,
+                       const float *y3d, const float *z3d, float *out)
+{
+  size_t ln = nx, sl = (size_t)nx * ny, V = sl * nz;
+  float *m[10];
+  for (int c = 0; c < 10; c++) m[c] = out + c * V;
+  long sx[7], sy[7], sz[7];
+  for (int n = 0; n < 7; n++) {
+    sx[n] = n - 3;
+    sy[n] = (long)(n - 3) * (long)ln;
+    sz[n] = (long)(n - 3) * (long)sl;
+  }
+  for (int k = nk1; k <= nk2; k++)
+    for (int j = nj1; j <= nj2; j++)
+      for (int i = ni1; i <= ni2; i++) {
+        size_t q = i + j * ln + (size_t)k * sl;
+        const float *cx[3] = {x3d, y3d, z3d};
+        float d[3][3];                 /* d[axis][coord] */
+        const long *sh[3] = {sx, sy, sz};
+        for (int ax = 0; ax < 3; ax++)
+          for (int c = 0; c < 3; c++) {
+            float v = FDC_COEF[0] * cx[c][q + sh[ax][0]];
+            for (int n = 1; n < 7; n++) v += FDC_COEF[n] * cx[c][q + sh[ax][n]];
+            d[ax][c] = v;
+          }
+        const float *v1 = d[0], *v2 = d[1], *v3 = d[2];
+        float g[3];
+        g[0] = v1[1] * v2[2] - v1[2] * v2[1];
+        g[1] = v1[2] * v2[0] - v1[0] * v2[2];
+        g[2] = v1[0] * v2[1] - v1[1] * v2[0];
+        float jac = 0.0f;
+        for (int c = 0; c < 3; c++) jac += g[c] * v3[c];
+        m[0][q] = jac;
+        const float *pa[3] = {v2, v3, v1}, *pb[3] = {v3, v1, v2};
+        for (int r = 0; r < 3; r++) {
+          const float *A = pa[r], *B = pb[r];
+          g[0] = A[1] * B[2] - A[2] * B[1];
+          g[1] = A[2] * B[0] - A[0] * B[2];
+          g[2] = A[0] * B[1] - A[1] * B[0];
+          for (int c = 0; c < 3; c++) m[1 + 3 * r + c][q] = g[c] / jac;
+        }
+      }
+  /* ghosts: mirrored about the physical boundary, x then y then z */
+  for (int c = 0; c < 10; c++) {
+    float *a = m[c];
+    for (int k = 0; k < nz; k++)
+      for (int j = 0; j < ny; j++) {
+        size_t r = j * ln + (size_t)k * sl;
+        for (int i = 0; i < ni1; i++) a[r + i] = a[r + 2 * ni1 - 1 - i];
+        for (int i = ni2 + 1; i < nx; i++) a[r + i] = a[r + 2 * ni2 + 1 - i];
+      }
+    for (int k = 0; k < nz; k++)
+      for (int j = 0; j < ny; j++) {
+        size_t r = j * ln + (size_t)k * sl;
+        if (j < nj1) memcpy(a + r, a + (2 * nj1 - 1 - j) * ln + (size_t)k * sl, ln * 4);
+        if (j > nj2) memcpy(a + r, a + (2 * nj2 + 1 - j) * ln + (size_t)k * sl, ln * 4);
+      }
+    for (int k = 0; k < nz; k++) {
+      if (k < nk1) memcpy(a + (size_t)k * sl, a + (size_t)(2 * nk1 - 1 - k) * sl, sl * 4);
+      if (k > nk2) memcpy(a + (size_t)k * sl, a + (size_t)(2 * nk2 + 1 - k) * sl, sl * 4);
+    }
+  }
   return 0;
 }

@@ -103,3 +103,17 @@ def surface_matrices(problem):
         lib().oracle_dvh2dvz_iso(C.addressof(cs), ptr["matVx2Vz2"],
                                  ptr["matVy2Vz2"], ptr["matF2Vz2"])
     return out
+
+
+def metric_calc(nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2, x3d, y3d, z3d):
+    """Grid metrics as the reference computes them (jac, xi_x..zeta_z;
+    10 x nx*ny*nz float32)."""
+    import numpy as np
+    L = lib()
+    L.oracle_metric_calc.restype = C.c_int
+    L.oracle_metric_calc.argtypes = [C.c_int] * 9 + [C.c_void_p] * 4
+    x, y, z = [np.ascontiguousarray(a, np.float32).ravel() for a in (x3d, y3d, z3d)]
+    out = np.zeros(10 * nx * ny * nz, np.float32)
+    L.oracle_metric_calc(nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2, x.ctypes.data,
+                         y.ctypes.data, z.ctypes.data, out.ctypes.data)
+    return out.reshape(10, -1)

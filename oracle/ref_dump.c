@@ -168,8 +168,9 @@ static void dump_inputs(fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md,
   put("metric.zeta_x", 'f', metric->zeta_x, n);
   put("metric.zeta_y", 'f', metric->zeta_y, n);
   put("metric.zeta_z", 'f', metric->zeta_z, n);
-  /* grid coordinates: read by the visco-elastic free surface only */
-  if (md->medium_type == CONST_MEDIUM_VISCOELASTIC_ISO && gd->x3d) {
+  /* grid coordinates: read by the visco-elastic free surface, and the
+   * input of the metric calculation (checked on its own) */
+  if (gd->x3d) {
     put("gd.x3d", 'f', gd->x3d, n);
     put("gd.y3d", 'f', gd->y3d, n);
     put("gd.z3d", 'f', gd->z3d, n);
