@@ -1014,7 +1014,7 @@ static int make_tmap(cgfd_solver_t *s)
   if (r != CUDA_SUCCESS) return set_err(CGFD_ECUDA, "tensor map (points) failed (%d)", (int)r);
   cuuint64_t dm[4] = {(cuuint64_t)g.px, (cuuint64_t)g.ny, (cuuint64_t)g.nz, 10};
   cuuint64_t sm_[3] = {(cuuint64_t)g.px * 4, (cuuint64_t)g.sl * 4, (cuuint64_t)g.vol * 4};
-  cuuint32_t bm[4] = {s2::TX, (cuuint32_t)s->ty, 1, 10};
+  cuuint32_t bm[4] = {s2::TX, (cuuint32_t)s->ty, 1, 9};   /* xi_x..zeta_z */
   r = fn(&M.met, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->metric, dm, sm_, bm, estr,
          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);

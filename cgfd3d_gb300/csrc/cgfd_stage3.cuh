@@ -12,7 +12,7 @@
  *                   cgfd_stage2.cuh) -- the 5 planes of the z operator's
  *                   window plus one in flight;
  *   stream ring     NS = 2 slots of the per-point streams of one plane:
- *                   metrics (jac + 9), media (slw, lambda, mu) and, as the
+ *                   the 9 metrics, media (slw, lambda, mu) and, as the
  *                   stage needs them, the `pre` and `end` levels.
  *
  * Synchronisation uses only mbarriers: `full` barriers complete when a
@@ -60,7 +60,8 @@ constexpr int NCW = TY;               /* consumer warps (one per tile row) */
 constexpr int NTHREADS = (NCW + 1) * 32;
 constexpr int PTS = TX * TY;
 
-/* stream-slot layout (floats) for a medium: metrics (jac + 9), media,
+/* stream-slot layout (floats) for a medium: metrics (the 9 of xi, eta,
+ * zeta; jac is read from global memory at the top layers only), media,
  * current memory variables (visco), pre, end */
 template <int MED>
 struct Slot {
@@ -68,7 +69,7 @@ struct Slot {
                             : (MED == MED_VIS ? 3 + 2 * CGFD_VIS_NMW_MAX : 3);
   static constexpr int NJ = MED == MED_VIS ? 6 * CGFD_VIS_NMW_MAX : 0;
   static constexpr int S_MET = 0;
-  static constexpr int S_MED = 10 * PTS;
+  static constexpr int S_MED = 9 * PTS;
   static constexpr int S_JC = S_MED + NMED * PTS;
   static constexpr int S_PRE = S_JC + NJ * PTS;
   static constexpr int S_END = S_PRE + 9 * PTS;
@@ -273,7 +274,7 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
     const int xs = i0 + g.xoff;        /* stream tiles: no halo */
     const int nmed = med_ncomp(MED, a.nmw);
     const uint32_t slot_bytes =
-        (10 + nmed + (MED == MED_VIS ? 6 * a.nmw : 0) + (KIND == 1 ? 9 : 0) +
+        (9 + nmed + (MED == MED_VIS ? 6 * a.nmw : 0) + (KIND == 1 ? 9 : 0) +
          (KIND >= 1 ? 9 : 0)) * PTS * 4;
     auto issue_wav = [&](int rel) {
       int b = rel % NB;
@@ -294,7 +295,7 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       float *dst = slots + b * SLOT;
       int k = kbeg + it;
       mbar_expect_tx(&full_s[b], slot_bytes);
-      tma_load_4d(dst + S_MET, &tmap_met, xs, j0, k, 0, &full_s[b]);
+      tma_load_4d(dst + S_MET, &tmap_met, xs, j0, k, 1, &full_s[b]);
       tma_load_4d(dst + S_MED, &tmap_med, xs, j0, k, 0, &full_s[b]);
       if (MED == MED_VIS) {
         tma_load_5d(dst + S_JC, &tmap_j, xs, j0, k, 9, a.cur_level, &full_s[b]);
@@ -313,7 +314,7 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       const int ip = it + L2_AHEAD;
       if (ip < niter) {
         const int k = kbeg + ip;
-        tma_prefetch_4d(&tmap_met, xs, j0, k, 0);
+        tma_prefetch_4d(&tmap_met, xs, j0, k, 1);
         tma_prefetch_4d(&tmap_med, xs, j0, k, 0);
         if (MED == MED_VIS) tma_prefetch_5d(&tmap_j, xs, j0, k, 9, a.cur_level);
         if (KIND == 1) tma_prefetch_5d(&tmap_pt, xs, j0, k, 0, a.pre_level);
@@ -400,9 +401,9 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       const long long q = (long long)(i + g.xoff) + (long long)j * px +
                           (long long)k * sl;
       const float *ms = st + S_MET + sp;
-      float xix = ms[1 * PTS], xiy = ms[2 * PTS], xiz = ms[3 * PTS];
-      float etx = ms[4 * PTS], ety = ms[5 * PTS], etz = ms[6 * PTS];
-      float ztx = ms[7 * PTS], zty = ms[8 * PTS], ztz = ms[9 * PTS];
+      float xix = ms[0 * PTS], xiy = ms[1 * PTS], xiz = ms[2 * PTS];
+      float etx = ms[3 * PTS], ety = ms[4 * PTS], etz = ms[5 * PTS];
+      float ztx = ms[6 * PTS], zty = ms[7 * PTS], ztz = ms[8 * PTS];
       const MedPt m = med_from<MED, false>(st + S_MED + sp, PTS);
       const float slw = m.slw;
       float r[9];
