@@ -43,6 +43,7 @@ UNIT = "pt-stage/s"
 # metrics + media), float32.  iso 36+12, vti 36+15, visco 108+18 floats.
 BYTES_PER_PT_STAGE = {"topo": 192, "flat": 192, "vti": 204, "visco": 504}
 WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
+             "slices": dict(ni=400, nj=400, nk=200),
              "batch": dict(ni=400, nj=400, nk=200),
              "vti": dict(ni=300, nj=300, nk=150),
              "visco": dict(ni=300, nj=300, nk=150),
@@ -202,7 +203,9 @@ def workload_name(args):
             "visco": "topography visco-elastic GMB 3 bodies %dx%dx%d (Qp 200, Qs "
                      "100), CFS-PML 12, timg free surface, DC source, 400 receivers",
             "flat": "flat iso %dx%dx%d, CFS-PML 10, timg free surface, explosive "
-                    "source, 20 receivers"}[args.workload] % (args.ni, args.nj, args.nk)
+                    "source, 20 receivers"}[
+                "topo" if args.workload == "slices" else args.workload] % (
+                args.ni, args.nj, args.nk)
 
 
 def pin_problem(p):
@@ -557,12 +560,104 @@ def run_batch(args):
     return 0
 
 
+def run_slices(args):
+    """Time loop with slice output every step, as a run with slices in its
+    parameter file does: three slices (x and y through the middle, z at the
+    free surface) of the 9 components copied to a host state buffer after
+    every step, packed on the device and handed out while the device runs
+    the next step: as arrays in the writers' order (the headline), scattered
+    into a host state buffer (what the drop-in hands the reference's
+    writers); against the scatter without overlap, against copying the whole
+    state, and against stepping with no output."""
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    from cgfd3d_gb300 import output, solver
+    K, W = args.steps, max(args.warmup, 0)
+    p = build_model(args, 5 * (K + W))
+    n_phys = p.ni * p.nj * p.nk
+    boxes = output.slice_boxes(p, x=[(p.ni1 + p.ni2) // 2], y=[(p.nj1 + p.nj2) // 2],
+                               z=[p.nk2])
+    nfl = sum((b.c2 - b.c1 + 1) * b.ni * b.nj * b.nk for b in boxes)
+    w = np.zeros((p.ncmp, p.nz, p.ny, p.nx), np.float32)
+    s = solver.Solver(p)
+
+    def loop(mode, n):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if mode.startswith("overlap"):   # step n+1 runs while step n is handed out
+            dst = w if mode == "overlap_scatter" else None
+            slot = 0
+            for it in range(n):
+                s.run_async(1)
+                s.pack_boxes_async(boxes, slot)
+                if it > 0:
+                    s.collect_boxes(slot ^ 1, dst)
+                slot ^= 1
+            if n > 0:
+                s.collect_boxes(slot ^ 1, dst)
+            s.run(0)
+        for _ in range(0 if mode.startswith("overlap") else n):
+            s.run(1)
+            if mode == "packed":
+                s.fetch_boxes(boxes, w)
+            elif mode == "whole":
+                s.fetch_state(w)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    sampler = ClockSampler(local)
+    res = {}
+    for mode in ("overlap_arrays", "overlap_scatter", "packed", "whole", "none"):
+        loop(mode, W)
+        if mode == "overlap_arrays":
+            sampler.start()
+            time.sleep(0.6)
+        res[mode] = loop(mode, K) / K
+        if mode == "overlap_arrays":
+            clocks = sampler.stop()
+    s.check_finite()
+    h2d, d2h = s.transfer_bytes()
+    s.close()
+    value = n_phys * 4 / res["overlap_arrays"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": K,
+        "warmup": W, "ms_per_step": 1e3 * res["overlap_arrays"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": {"workload": workload_name(args) + "; 3 slices (x, y, z) of 9 "
+                   "components to the host every step",
+                   "parallelism": "single",
+                   "l2": "inputs larger than L2, no flush"},
+        "output": {"floats_per_step": nfl,
+                   "ms_per_step_overlapped_arrays": 1e3 * res["overlap_arrays"],
+                   "ms_per_step_overlapped_scatter": 1e3 * res["overlap_scatter"],
+                   "ms_per_step_blocking_scatter": 1e3 * res["packed"],
+                   "ms_per_step_whole_state": 1e3 * res["whole"],
+                   "ms_per_step_no_output": 1e3 * res["none"],
+                   "whole_state_bytes": 4 * p.ncmp * p.nx * p.ny * p.nz},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 4 * nfl},
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "slices":
+        return run_slices(args)
     return run_ours(args)
 
 

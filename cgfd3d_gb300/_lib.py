@@ -43,6 +43,13 @@ def lib():
     L.cgfd_solver_transfer_bytes.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     L.cgfd_solver_fetch_pg.argtypes = [vp, vp]
     L.cgfd_solver_fetch_state.argtypes = [vp, vp]
+    L.cgfd_box_floats.argtypes = [vp, C.c_int]
+    L.cgfd_box_floats.restype = C.c_size_t
+    L.cgfd_solver_pack_boxes.argtypes = [vp, vp, C.c_int, vp]
+    L.cgfd_solver_fetch_boxes.argtypes = [vp, vp, C.c_int, vp]
+    L.cgfd_solver_run_async.argtypes = [vp, C.c_int]
+    L.cgfd_solver_pack_boxes_async.argtypes = [vp, vp, C.c_int, C.c_int]
+    L.cgfd_solver_collect_boxes.argtypes = [vp, C.c_int, vp, vp]
     L.cgfd_solver_fetch_surface_matrices.argtypes = [vp, vp, vp, vp]
     L.cgfd_solver_fetch_surface_rotation.argtypes = [vp, vp]
     L.cgfd_solver_destroy.argtypes = [vp]

@@ -77,5 +77,12 @@ class Problem(C.Structure):
     )
 
 
+class Box(C.Structure):
+    """cgfd_box_t: components c1..c2, points (i1 + a*di, j1 + b*dj, k1 + c*dk)
+    in padded-array indices."""
+    _fields_ = [(n, C.c_int) for n in
+                ("c1", "c2", "i1", "ni", "di", "j1", "nj", "dj", "k1", "nk", "dk")]
+
+
 def field_offsets(struct):
     return {name: getattr(struct, name).offset for name, _ in struct._fields_}

@@ -24,6 +24,7 @@
 #include <cstring>
 #include <ctime>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/cgfd3d_gpu.h"
@@ -577,6 +578,35 @@ __global__ void k_nonfinite(const float *__restrict__ w, long long n, int *flag)
   if (bad) atomicOr(flag, 1);
 }
 
+/* Gathers output boxes of one wavefield level into a packed buffer: box
+ * after box, component, k, j, i (i fastest).  off[] holds each box's first
+ * packed index (ascending), total the packed length. */
+__global__ void k_pack_boxes(const float *__restrict__ w, long long cvol, DevGrid g,
+                             const cgfd_box_t *__restrict__ box,
+                             const long long *__restrict__ off, int nbox,
+                             long long total, float *__restrict__ out)
+{
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (; t < total; t += stride) {
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const cgfd_box_t b = box[lo];
+    long long r = t - off[lo];
+    const int a = (int)(r % b.ni); r /= b.ni;
+    const int bj = (int)(r % b.nj); r /= b.nj;
+    const int ck = (int)(r % b.nk);
+    const int c = b.c1 + (int)(r / b.nk);
+    const long long i = b.i1 + (long long)a * b.di + g.xoff;
+    const long long j = b.j1 + (long long)bj * b.dj;
+    const long long k = b.k1 + (long long)ck * b.dk;
+    out[t] = w[c * cvol + i + j * g.px + k * g.sl];
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* host-side source preprocessing                                            */
 /* ------------------------------------------------------------------------ */
@@ -687,6 +717,20 @@ static int build_source_entries(const cgfd_problem_t *p, std::vector<int> &col,
 /* solver                                                                    */
 /* ------------------------------------------------------------------------ */
 
+/* One output slot: a set of boxes (slices, snapshots) packed on the device
+ * and copied to pinned host memory behind the queued steps. */
+struct OutSlot {
+  std::vector<cgfd_box_t> boxes;
+  cgfd_box_t *d_box, *h_box;    /* box table, device / pinned host */
+  long long *d_off, *h_off;     /* each box's first packed index */
+  int cap;
+  float *d_pack, *h_pack;       /* packed floats, device / pinned host */
+  size_t pack_cap, n;
+  int *h_err;                   /* pinned copy of the device error flag */
+  cudaEvent_t ev;
+  int pending;
+};
+
 struct cgfd_solver {
   const cgfd_problem_t *p;
   DevGrid g;
@@ -729,6 +773,7 @@ struct cgfd_solver {
   int *d_err;
   float *pg, *dis;              /* surface peak-motion maps (free top) */
   float *staging;               /* upload staging volume (set-up only) */
+  OutSlot out[CGFD_OUT_SLOTS + 1];   /* output boxes; the last: blocking calls */
   StageMaps maps;               /* tensor maps of the stage kernel */
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
   int ty;                       /* tile rows of the medium's stage kernel */
@@ -1051,6 +1096,16 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
                   s->sf, s->sf_w, s->frate, s->surf, s->staging};
   for (void *q : ptrs)
     if (q) cudaFree(q);
+  for (OutSlot &o : s->out) {
+    if (o.d_box) cudaFree(o.d_box);
+    if (o.d_off) cudaFree(o.d_off);
+    if (o.h_box) cudaFreeHost(o.h_box);
+    if (o.h_off) cudaFreeHost(o.h_off);
+    if (o.d_pack) cudaFree(o.d_pack);
+    if (o.h_pack) cudaFreeHost(o.h_pack);
+    if (o.h_err) cudaFreeHost(o.h_err);
+    if (o.ev) cudaEventDestroy(o.ev);
+  }
   for (int f = 0; f < CGFD_NFACE; f++)
     if (s->aux[f]) cudaFree(s->aux[f]);
   for (int f = 0; f < CGFD_NFACE; f++) {
@@ -1608,6 +1663,20 @@ extern "C" int cgfd_solver_run(cgfd_solver_t *s, int nsteps)
   return 0;
 }
 
+extern "C" int cgfd_solver_run_async(cgfd_solver_t *s, int nsteps)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (nsteps < 0 || s->step + nsteps > s->p->nt_total)
+    return set_err(CGFD_EINVAL, "run(%d) past nt_total=%d (at step %d)", nsteps,
+                   s->p->nt_total, s->step);
+  for (int n = 0; n < nsteps; n++) {
+    enqueue_step(s, s->step, nullptr);
+    s->step++;
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
 extern "C" int cgfd_solver_step(const cgfd_solver_t *s) { return s ? s->step : -1; }
 
 extern "C" int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3])
@@ -1716,6 +1785,195 @@ extern "C" int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w)
     CK(download_volume(s, w + c * hvol, s->wav + s->pre_lev * L + c * s->g.vol));
   CK(cudaStreamSynchronize(s->stream));
   return 0;
+}
+
+static size_t box_floats(const cgfd_box_t &b)
+{
+  if (b.c2 < b.c1 || b.ni < 1 || b.nj < 1 || b.nk < 1 || b.di < 1 || b.dj < 1 ||
+      b.dk < 1)
+    return 0;
+  return (size_t)(b.c2 - b.c1 + 1) * b.ni * b.nj * b.nk;
+}
+
+extern "C" size_t cgfd_box_floats(const cgfd_box_t *box, int nbox)
+{
+  if (!box || nbox < 1) return 0;
+  size_t n = 0;
+  for (int m = 0; m < nbox; m++) {
+    size_t f = box_floats(box[m]);
+    if (!f) return 0;
+    n += f;
+  }
+  return n;
+}
+
+/* Writes packed boxes into w (ncmp x nx*ny*nz) at their positions.  One
+ * task per (box, component); an x slice scatters one float per grid row,
+ * bound by cache and TLB misses rather than bandwidth, so large sets are
+ * split over a few host threads. */
+static void scatter_boxes(const DevGrid &g, const std::vector<cgfd_box_t> &boxes,
+                          const float *packed, float *w)
+{
+  struct Task { const cgfd_box_t *b; int c; const float *src; };
+  std::vector<Task> task;
+  const float *q = packed;
+  size_t total = 0;
+  for (const cgfd_box_t &b : boxes) {
+    const size_t per = (size_t)b.ni * b.nj * b.nk;
+    for (int c = b.c1; c <= b.c2; c++, q += per) task.push_back({&b, c, q});
+    total += per * (b.c2 - b.c1 + 1);
+  }
+  const size_t nx = g.nx, sl = nx * g.ny, hvol = sl * g.nz;
+  auto run = [&](size_t t0, size_t step) {
+    for (size_t t = t0; t < task.size(); t += step) {
+      const cgfd_box_t &b = *task[t].b;
+      const float *src = task[t].src;
+      for (int kk = 0; kk < b.nk; kk++)
+        for (int jj = 0; jj < b.nj; jj++) {
+          float *row = w + task[t].c * hvol + (size_t)(b.k1 + kk * b.dk) * sl +
+                       (size_t)(b.j1 + jj * b.dj) * nx + b.i1;
+          if (b.di == 1) {
+            memcpy(row, src, b.ni * sizeof(float));
+            src += b.ni;
+          } else {
+            for (int ii = 0; ii < b.ni; ii++) row[(size_t)ii * b.di] = *src++;
+          }
+        }
+    }
+  };
+  unsigned hw = std::thread::hardware_concurrency();
+  size_t nth = total < (1u << 18) ? 1 : std::min<size_t>({task.size(), 8, hw ? hw : 1});
+  if (nth <= 1) {
+    run(0, 1);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (size_t t = 1; t < nth; t++) th.emplace_back(run, t, nth);
+  run(0, nth);
+  for (std::thread &t : th) t.join();
+}
+
+/* Queues the packing of boxes of the current state into slot o: box table
+ * upload, gather kernel, copy to pinned host memory and the device error
+ * flag behind it, then the slot's event.  Returns without waiting. */
+static int pack_enqueue(cgfd_solver_t *s, OutSlot &o, const cgfd_box_t *box, int nbox)
+{
+  if (!box || nbox < 1) return set_err(CGFD_EINVAL, "no output boxes");
+  if (o.pending) return set_err(CGFD_EINVAL, "output slot still holds uncollected boxes");
+  const DevGrid &g = s->g;
+  std::vector<long long> off(nbox);
+  size_t total = 0;
+  for (int m = 0; m < nbox; m++) {
+    const cgfd_box_t &b = box[m];
+    size_t f = box_floats(b);
+    if (!f) return set_err(CGFD_EINVAL, "output box %d: empty count, stride or component range", m);
+    if (b.c1 < 0 || b.c2 >= s->ncmp)
+      return set_err(CGFD_EINVAL, "output box %d: components %d..%d outside 0..%d", m,
+                     b.c1, b.c2, s->ncmp - 1);
+    if (b.i1 < 0 || b.j1 < 0 || b.k1 < 0 ||
+        b.i1 + (long long)(b.ni - 1) * b.di >= g.nx ||
+        b.j1 + (long long)(b.nj - 1) * b.dj >= g.ny ||
+        b.k1 + (long long)(b.nk - 1) * b.dk >= g.nz)
+      return set_err(CGFD_EINVAL, "output box %d outside the padded grid", m);
+    off[m] = (long long)total;
+    total += f;
+  }
+  if (!o.ev) {
+    CK(cudaEventCreateWithFlags(&o.ev, cudaEventDisableTiming));
+    CK(cudaMallocHost((void **)&o.h_err, sizeof(int)));
+  }
+  if (nbox > o.cap) {
+    if (o.d_box) cudaFree(o.d_box);
+    if (o.d_off) cudaFree(o.d_off);
+    if (o.h_box) cudaFreeHost(o.h_box);
+    if (o.h_off) cudaFreeHost(o.h_off);
+    o.d_box = nullptr; o.d_off = nullptr; o.h_box = nullptr; o.h_off = nullptr;
+    o.cap = 0;
+    CK(cudaMalloc((void **)&o.d_box, nbox * sizeof(cgfd_box_t)));
+    CK(cudaMalloc((void **)&o.d_off, nbox * sizeof(long long)));
+    CK(cudaMallocHost((void **)&o.h_box, nbox * sizeof(cgfd_box_t)));
+    CK(cudaMallocHost((void **)&o.h_off, nbox * sizeof(long long)));
+    o.cap = nbox;
+  }
+  if (total > o.pack_cap) {
+    if (o.d_pack) cudaFree(o.d_pack);
+    if (o.h_pack) cudaFreeHost(o.h_pack);
+    o.d_pack = nullptr; o.h_pack = nullptr; o.pack_cap = 0;
+    CK(cudaMalloc((void **)&o.d_pack, total * sizeof(float)));
+    CK(cudaMallocHost((void **)&o.h_pack, total * sizeof(float)));
+    o.pack_cap = total;
+  }
+  /* the table goes through the slot's pinned copy: a copy from pageable
+   * memory may wait for the stream, which would end the overlap */
+  memcpy(o.h_box, box, nbox * sizeof(cgfd_box_t));
+  memcpy(o.h_off, off.data(), nbox * sizeof(long long));
+  CK(cudaMemcpyAsync(o.d_box, o.h_box, nbox * sizeof(cgfd_box_t), cudaMemcpyHostToDevice,
+                     s->stream));
+  CK(cudaMemcpyAsync(o.d_off, o.h_off, nbox * sizeof(long long), cudaMemcpyHostToDevice,
+                     s->stream));
+  long long nblk = ((long long)total + 255) / 256;
+  if (nblk > 152 * 8) nblk = 152 * 8;
+  k_pack_boxes<<<(int)nblk, 256, 0, s->stream>>>(s->wav + s->pre_lev * level_floats(s),
+                                                  g.vol, g, o.d_box, o.d_off, nbox,
+                                                  (long long)total, o.d_pack);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(o.h_pack, o.d_pack, total * sizeof(float), cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaMemcpyAsync(o.h_err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaEventRecord(o.ev, s->stream));
+  s->d2h_bytes += total * sizeof(float);
+  o.boxes.assign(box, box + nbox);
+  o.n = total;
+  o.pending = 1;
+  return 0;
+}
+
+/* Waits for slot o and hands its boxes out: scattered into w (reference
+ * layout) and/or packed into out; either may be null. */
+static int pack_collect(cgfd_solver_t *s, OutSlot &o, float *w, float *out)
+{
+  if (!o.pending) return set_err(CGFD_EINVAL, "output slot holds no boxes");
+  o.pending = 0;
+  CK(cudaEventSynchronize(o.ev));
+  if (*o.h_err) return set_err(CGFD_ECUDA, "device wait timed out (code %d)", *o.h_err);
+  if (out) memcpy(out, o.h_pack, o.n * sizeof(float));
+  if (w) scatter_boxes(s->g, o.boxes, o.h_pack, w);
+  return 0;
+}
+
+extern "C" int cgfd_solver_pack_boxes(cgfd_solver_t *s, const cgfd_box_t *box, int nbox,
+                                      float *out)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  OutSlot &o = s->out[CGFD_OUT_SLOTS];
+  int rc = pack_enqueue(s, o, box, nbox);
+  return rc ? rc : pack_collect(s, o, nullptr, out);
+}
+
+extern "C" int cgfd_solver_fetch_boxes(cgfd_solver_t *s, const cgfd_box_t *box, int nbox,
+                                       float *w)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  OutSlot &o = s->out[CGFD_OUT_SLOTS];
+  int rc = pack_enqueue(s, o, box, nbox);
+  return rc ? rc : pack_collect(s, o, w, nullptr);
+}
+
+extern "C" int cgfd_solver_pack_boxes_async(cgfd_solver_t *s, const cgfd_box_t *box,
+                                            int nbox, int slot)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (slot < 0 || slot >= CGFD_OUT_SLOTS)
+    return set_err(CGFD_EINVAL, "output slot %d outside 0..%d", slot, CGFD_OUT_SLOTS - 1);
+  return pack_enqueue(s, s->out[slot], box, nbox);
+}
+
+extern "C" int cgfd_solver_collect_boxes(cgfd_solver_t *s, int slot, float *w, float *out)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (slot < 0 || slot >= CGFD_OUT_SLOTS)
+    return set_err(CGFD_EINVAL, "output slot %d outside 0..%d", slot, CGFD_OUT_SLOTS - 1);
+  return pack_collect(s, s->out[slot], w, out);
 }
 
 extern "C" int cgfd_solver_check_finite(cgfd_solver_t *s)

@@ -18,10 +18,13 @@
  *   PG_slice_output() (forward/drv_rk_curv_col.c:547-550)
  * Slices and snapshots (NetCDF, forward/io_funcs.c:780-1268) are written by
  * the reference's own writers when this file is built inside the reference
- * tree (CGFD_DROPIN_REFERENCE_HEADERS); the loop then advances step by step
- * and hands them a host copy of the state at each step that writes.  Built
- * without the reference (tests, other hosts) there are no NetCDF writers and
- * requested slices/snapshots are reported and skipped.
+ * tree (CGFD_DROPIN_REFERENCE_HEADERS).  The loop then runs up to each step
+ * that writes and copies to the host only the points those writers read: the
+ * slice planes and the due snapshot boxes, packed on the device
+ * (cgfd_solver_fetch_boxes); output_all (a NetCDF volume of the whole state
+ * every step, forward/drv_rk_curv_col.c:511-526) copies the whole state.
+ * Built without the reference (tests, other hosts) there are no NetCDF
+ * writers and requested slices/snapshots are reported and skipped.
  *
  * Errors print the library's message and call MPI_Abort when MPI is linked
  * (exit(1) otherwise), as the reference does.  Unsupported configurations
@@ -55,6 +58,101 @@ static void fail(const char *what)
   CGFD_ABORT();
 }
 
+/* Boxes of the slices io_slice_nc_put writes (forward/io_funcs.c:992-1111):
+ * components 0..ncmp-1 (0..8 for GMB media), x slices over (k, j), y slices
+ * over (k, i), z slices over (j, i) of the physical points. */
+static int slice_boxes(const gd_t *gd, const ioslice_t *sl, const wav_t *wav,
+                       cgfd_box_t *box)
+{
+  const int c2 = wav->visco_type == CGFD_REF_VISCO_GMB ? 8 : wav->ncmp - 1;
+  int n = 0;
+  for (int m = 0; m < sl->num_of_slice_x; m++, n++) {
+    cgfd_box_t b = {0, c2, sl->slice_x_indx[m], 1, 1, gd->nj1, gd->nj, 1,
+                    gd->nk1, gd->nk, 1};
+    box[n] = b;
+  }
+  for (int m = 0; m < sl->num_of_slice_y; m++, n++) {
+    cgfd_box_t b = {0, c2, gd->ni1, gd->ni, 1, sl->slice_y_indx[m], 1, 1,
+                    gd->nk1, gd->nk, 1};
+    box[n] = b;
+  }
+  for (int m = 0; m < sl->num_of_slice_z; m++, n++) {
+    cgfd_box_t b = {0, c2, gd->ni1, gd->ni, 1, gd->nj1, gd->nj, 1,
+                    sl->slice_z_indx[m], 1, 1};
+    box[n] = b;
+  }
+  return n;
+}
+
+/* The rule of io_snap_nc_put (forward/io_funcs.c:1147-1153) for snapshot m
+ * at step it. */
+static int snapshot_due(const iosnap_t *sn, int m, int nt_total, int it)
+{
+  const int it1 = sn->it1[m], dit = sn->dit[m];
+  return it >= it1 && (it - it1) / dit <= (nt_total - it1) / dit &&
+         (it - it1) % dit == 0;
+}
+
+/* First step >= from at which a snapshot is due; nt_total when none is. */
+static int next_snapshot(const iosnap_t *sn, int nt_total, int from)
+{
+  int best = nt_total;
+  for (int m = 0; m < sn->num_of_snap; m++) {
+    const int it1 = sn->it1[m], dit = sn->dit[m];
+    int it = from <= it1 ? it1 : it1 + (from - it1 + dit - 1) / dit * dit;
+    if (it < best && snapshot_due(sn, m, nt_total, it)) best = it;
+  }
+  return best;
+}
+
+/* Box of snapshot m: velocity (components 0..2) and/or stress (3..8, also
+ * read for strain).  Returns the boxes added (0 or 1). */
+static int snapshot_box(const iosnap_t *sn, int m, cgfd_box_t *b)
+{
+  const int v = sn->out_vel[m] == 1;
+  const int t = sn->out_stress[m] == 1 || sn->out_strain[m] == 1;
+  if (!v && !t) return 0;
+  cgfd_box_t q = {v ? 0 : 3, t ? 8 : 2, sn->i1[m], sn->ni[m], sn->di[m],
+                  sn->j1[m], sn->nj[m], sn->dj[m], sn->k1[m], sn->nk[m], sn->dk[m]};
+  *b = q;
+  return 1;
+}
+
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+/* What the reference's writers need at an output step. */
+typedef struct {
+  ioslice_t *ioslice;
+  ioslice_nc_t *slice_nc;
+  iosnap_t *iosnap;
+  iosnap_nc_t *snap_nc;
+  gd_t *gd;
+  md_t *md;
+  wav_t *wav;
+  float *w_host, *w_buff;
+  int nt_total, output_every;
+  float dt, t0;
+  char *output_dir;
+  int *topoid;
+} out_ctx_t;
+
+/* The reference's writers for step it, handed the host state w_host, in the
+ * order of forward/drv_rk_curv_col.c:501-526. */
+static void write_step(const out_ctx_t *o, int it)
+{
+  const float t_end = it * o->dt + o->t0 + o->dt;
+  io_slice_nc_put(o->ioslice, o->slice_nc, o->gd, o->w_host, o->w_buff, it, t_end, 0,
+                  o->wav->ncmp - 1, o->wav->visco_type);
+  io_snap_nc_put(o->iosnap, o->snap_nc, o->gd, o->md, o->wav, o->w_host, o->w_buff,
+                 o->nt_total, it, t_end, 1, 1, 1);
+  if (o->output_every) {
+    char ou_file[CONST_MAX_STRLEN];
+    io_build_fname_time(o->output_dir, "w3d", ".nc", o->topoid, it, ou_file);
+    io_var3d_export_nc(ou_file, o->w_host, o->wav->cmp_pos, o->wav->cmp_name,
+                       o->wav->ncmp, o->gd->index_name, o->gd->nx, o->gd->ny, o->gd->nz);
+  }
+}
+#endif
+
 static void unsupported(const char *what)
 {
   fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s is not supported\n", what);
@@ -69,7 +167,7 @@ void drv_rk_curv_col_allstep(
     int nt_total, float t0, char *output_fname_part, char *output_dir,
     int qc_check_nan_num_of_step, const int output_all, const int verbose)
 {
-  (void)mympi; (void)output_fname_part; (void)output_dir; (void)output_all;
+  (void)mympi; (void)output_fname_part; (void)output_dir;
 
   if (fd->num_rk_stages != 4 || fd->num_of_pairs != 8)
     unsupported("an operator set other than MacCormack DRP with RK4");
@@ -209,47 +307,84 @@ void drv_rk_curv_col_allstep(
     nslice = nsnap = 0;
   }
 #endif
-  const int step_wise = nslice + nsnap > 0;
+#ifndef CGFD_DROPIN_REFERENCE_HEADERS
+  const int output_every = 0;
+  (void)output_all;
+#else
+  const int output_every = output_all == 1;
+#endif
+  const int step_wise = nslice + nsnap > 0 || output_every;
   float *w_host = NULL, *w_buff = NULL;
+  cgfd_box_t *box = NULL;
   if (step_wise) {
     size_t L = (size_t)wav->ncmp * gd->nx * gd->ny * gd->nz;
-    w_host = (float *)malloc(L * sizeof(float));
+    w_host = (float *)calloc(L, sizeof(float));
     w_buff = (float *)calloc(L, sizeof(float));
-    if (!w_host || !w_buff) unsupported("host memory for slice/snapshot output");
+    box = (cgfd_box_t *)malloc((size_t)(nslice + nsnap + 1) * sizeof(cgfd_box_t));
+    if (!w_host || !w_buff || !box) unsupported("host memory for slice/snapshot output");
   }
+  const int nslice_box = nslice > 0 ? slice_boxes(gd, ioslice, wav, box) : 0;
 
+#ifdef CGFD_DROPIN_REFERENCE_HEADERS
+  const out_ctx_t octx = {ioslice, &ioslice_nc, iosnap, &iosnap_nc, gd, md, wav,
+                          w_host, w_buff, nt_total, output_every, dt, t0,
+                          output_dir, mympi->topoid};
+#define write_output(it_) write_step(&octx, (it_))
+#else
+#define write_output(it_) ((void)(it_))
+#endif
   if (verbose > 0) fprintf(stdout, "GPU time loop: %d steps ...\n", nt_total);
   cgfd_solver_t *s = NULL;
   if (cgfd_solver_create(&p, &s) != 0) fail("solver setup");
-  int chunk = step_wise ? 1
-            : (qc_check_nan_num_of_step > 0 ? qc_check_nan_num_of_step : nt_total);
+  /* Steps are queued without waiting; the boxes of a step that writes are
+   * packed behind it into one of two output slots, and written while the
+   * device runs the next step. */
+  int pend_it = -1, pend_slot = 0, slot = 0;
   for (int done = 0; done < nt_total;) {
-    int n = nt_total - done < chunk ? nt_total - done : chunk;
-    if (cgfd_solver_run(s, n) != 0) fail("time loop");
+    int n = nt_total - done;
+    if (qc_check_nan_num_of_step > 0) {
+      int to_qc = qc_check_nan_num_of_step - done % qc_check_nan_num_of_step;
+      if (to_qc < n) n = to_qc;
+    }
+    if (step_wise) {   /* run through the next step that writes */
+      int next = nslice > 0 || output_every ? done : next_snapshot(iosnap, nt_total, done);
+      if (next - done + 1 < n) n = next - done + 1;
+    }
+    if (cgfd_solver_run_async(s, n) != 0) fail("time loop");
     done += n;
+    const int it = done - 1;
+    int nbox = 0, due = 0;
+    if (step_wise) {
+      nbox = nslice_box;
+      for (int m = 0; m < nsnap; m++)
+        if (snapshot_due(iosnap, m, nt_total, it)) nbox += snapshot_box(iosnap, m, box + nbox);
+      due = nbox > 0 || output_every;
+    }
+    if (due && !output_every &&
+        cgfd_solver_pack_boxes_async(s, box, nbox, slot) != 0)
+      fail("slices/snapshots");
+    if (pend_it >= 0) {
+      if (cgfd_solver_collect_boxes(s, pend_slot, w_host, NULL) != 0) fail("slices/snapshots");
+      write_output(pend_it);
+      pend_it = -1;
+    }
+    if (due && output_every) {
+      if (cgfd_solver_fetch_state(s, w_host) != 0) fail("state for output");
+      write_output(it);
+    } else if (due) {
+      pend_it = it;
+      pend_slot = slot;
+      slot ^= 1;
+    }
     if (qc_check_nan_num_of_step > 0 && done % qc_check_nan_num_of_step == 0 &&
         cgfd_solver_check_finite(s) != 0)
       fail("wavefield check");
-#ifdef CGFD_DROPIN_REFERENCE_HEADERS
-    if (step_wise) {
-      int it = done - 1;
-      float t_end = it * dt + t0 + dt;
-      int due = nslice > 0;
-      for (int m = 0; m < nsnap && !due; m++) {
-        int d = it - iosnap->it1[m];
-        due = d >= 0 && d % iosnap->dit[m] == 0 &&
-              d / iosnap->dit[m] <= (nt_total - iosnap->it1[m]) / iosnap->dit[m];
-      }
-      if (due) {
-        if (cgfd_solver_fetch_state(s, w_host) != 0) fail("state for output");
-        io_slice_nc_put(ioslice, &ioslice_nc, gd, w_host, w_buff, it, t_end, 0,
-                        wav->ncmp - 1, wav->visco_type);
-        io_snap_nc_put(iosnap, &iosnap_nc, gd, md, wav, w_host, w_buff, nt_total,
-                       it, t_end, 1, 1, 1);
-      }
-    }
-#endif
   }
+  if (pend_it >= 0) {
+    if (cgfd_solver_collect_boxes(s, pend_slot, w_host, NULL) != 0) fail("slices/snapshots");
+    write_output(pend_it);
+  }
+  if (cgfd_solver_run(s, 0) != 0) fail("time loop");   /* waits, reads device errors */
   if (cgfd_solver_fetch(s) != 0) fail("fetch");
   if (p.free_top && bdry->matVx2Vz2 &&
       cgfd_solver_fetch_surface_matrices(s, bdry->matVx2Vz2, bdry->matVy2Vz2,
@@ -272,6 +407,7 @@ void drv_rk_curv_col_allstep(
   cgfd_solver_destroy(s);
   free(w_host);
   free(w_buff);
+  free(box);
 
   /* scatter seismograms back into the reference's buffers */
   for (int r = 0; r < nr; r++) {

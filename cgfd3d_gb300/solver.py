@@ -13,7 +13,21 @@ that step, inspect and continue.
 
 import ctypes as C
 
-from . import _lib
+from . import _lib, abi
+
+
+def _box_array(boxes):
+    """ctypes array of cgfd_box_t from Box structs, dicts or 11-tuples
+    (c1, c2, i1, ni, di, j1, nj, dj, k1, nk, dk)."""
+    out = (abi.Box * len(boxes))()
+    for m, b in enumerate(boxes):
+        if isinstance(b, abi.Box):
+            out[m] = b
+        elif isinstance(b, dict):
+            out[m] = abi.Box(**b)
+        else:
+            out[m] = abi.Box(*[int(v) for v in b])
+    return out
 
 
 class Solver:
@@ -30,6 +44,11 @@ class Solver:
 
     def run(self, nsteps):
         _lib.check(_lib.lib().cgfd_solver_run(self._h, int(nsteps)))
+
+    def run_async(self, nsteps):
+        """Queue nsteps steps and return; errors surface at the next
+        collect or blocking call."""
+        _lib.check(_lib.lib().cgfd_solver_run_async(self._h, int(nsteps)))
 
     def fetch(self):
         _lib.check(_lib.lib().cgfd_solver_fetch(self._h))
@@ -70,6 +89,94 @@ class Solver:
 
     def set_timing(self, on=True):
         _lib.check(_lib.lib().cgfd_solver_set_timing(self._h, int(bool(on))))
+
+    def fetch_state(self, out=None):
+        """The current state as (ncmp, nz, ny, nx), reference layout (into
+        ``out`` when given: C-contiguous float32 of that shape)."""
+        import numpy as np
+        p = self.problem
+        shape = (p.ncmp, p.nz, p.ny, p.nx)
+        if out is None:
+            out = np.empty(shape, np.float32)
+        elif out.shape != shape or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("out must be C-contiguous float32 %r" % (shape,))
+        _lib.check(_lib.lib().cgfd_solver_fetch_state(self._h, out.ctypes.data))
+        return out
+
+    def pack_boxes(self, boxes):
+        """Output boxes of the current state, packed on the device: one array
+        (ncomp, nk, nj, ni) per box, the order of the reference's slice and
+        snapshot writers."""
+        import numpy as np
+        arr = _box_array(boxes)
+        n = _lib.lib().cgfd_box_floats(arr, len(arr))
+        if n == 0:
+            raise ValueError("empty or malformed output box")
+        flat = np.empty(n, np.float32)
+        _lib.check(_lib.lib().cgfd_solver_pack_boxes(self._h, arr, len(arr),
+                                                      flat.ctypes.data))
+        out, q = [], 0
+        for b in arr:
+            shape = (b.c2 - b.c1 + 1, b.nk, b.nj, b.ni)
+            cnt = shape[0] * shape[1] * shape[2] * shape[3]
+            out.append(flat[q:q + cnt].reshape(shape))
+            q += cnt
+        return out
+
+    def pack_boxes_async(self, boxes, slot):
+        """Queue the packing of boxes of the state after the queued steps into
+        output slot 0 or 1; collect_boxes(slot) hands them out."""
+        arr = _box_array(boxes)
+        if _lib.lib().cgfd_box_floats(arr, len(arr)) == 0:
+            raise ValueError("empty or malformed output box")
+        self._slot_boxes = getattr(self, "_slot_boxes", {})
+        self._slot_boxes[slot] = arr
+        _lib.check(_lib.lib().cgfd_solver_pack_boxes_async(self._h, arr, len(arr),
+                                                            int(slot)))
+
+    def collect_boxes(self, slot, w=None):
+        """Wait for output slot `slot`.  With w: scatter the boxes into it (as
+        fetch_boxes) and return None; without: return them as arrays (as
+        pack_boxes)."""
+        import numpy as np
+        arr = self._slot_boxes.get(slot) if hasattr(self, "_slot_boxes") else None
+        if arr is None:
+            raise ValueError("output slot %r holds no boxes" % (slot,))
+        flat = None
+        if w is None:
+            flat = np.empty(_lib.lib().cgfd_box_floats(arr, len(arr)), np.float32)
+        wp = None
+        if w is not None:
+            p = self.problem
+            if (w.dtype != np.float32 or not w.flags.c_contiguous or
+                    w.size != p.ncmp * p.nx * p.ny * p.nz):
+                raise ValueError("w must be a C-contiguous float32 array of the state's size")
+            wp = w.ctypes.data
+        del self._slot_boxes[slot]
+        _lib.check(_lib.lib().cgfd_solver_collect_boxes(
+            self._h, int(slot), wp, None if flat is None else flat.ctypes.data))
+        if flat is None:
+            return None
+        out, q = [], 0
+        for b in arr:
+            shape = (b.c2 - b.c1 + 1, b.nk, b.nj, b.ni)
+            cnt = shape[0] * shape[1] * shape[2] * shape[3]
+            out.append(flat[q:q + cnt].reshape(shape))
+            q += cnt
+        return out
+
+    def fetch_boxes(self, boxes, w):
+        """Write the boxes of the current state into w (ncmp x nz x ny x nx,
+        float32, C order) at their own positions; other points untouched."""
+        import numpy as np
+        p = self.problem
+        if (not isinstance(w, np.ndarray) or w.dtype != np.float32 or
+                not w.flags.c_contiguous or w.size != p.ncmp * p.nx * p.ny * p.nz):
+            raise ValueError("w must be a C-contiguous float32 array of the state's size")
+        arr = _box_array(boxes)
+        _lib.check(_lib.lib().cgfd_solver_fetch_boxes(self._h, arr, len(arr),
+                                                       w.ctypes.data))
+        return w
 
     def transfer_bytes(self):
         h, d = C.c_size_t(), C.c_size_t()

@@ -184,6 +184,54 @@ int cgfd_solver_fetch_pg(cgfd_solver_t *s, float *pg);
  * touching the problem's arrays. */
 int cgfd_solver_fetch_state(cgfd_solver_t *s, float *w);
 
+/* A box of wavefield points for slice and snapshot output: components
+ * c1..c2 and the points (i1 + a*di, j1 + b*dj, k1 + c*dk), a < ni, b < nj,
+ * c < nk, in padded-array indices (ghosts included), as the reference's
+ * ioslice_t / iosnap_t hold them (forward/io_funcs.h).  An x slice at i is
+ * {i1 = i, ni = 1, j over nj1..nj2, k over nk1..nk2}; a snapshot is
+ * {i1, ni, di, j1, nj, dj, k1, nk, dk} of iosnap_t. */
+typedef struct {
+  int c1, c2;
+  int i1, ni, di;
+  int j1, nj, dj;
+  int k1, nk, dk;
+} cgfd_box_t;
+
+/* Floats that nbox boxes hold; 0 when a box has a count or stride below 1 or
+ * c2 < c1. */
+size_t cgfd_box_floats(const cgfd_box_t *box, int nbox);
+
+/* Packs the boxes of the current state (the level cgfd_solver_fetch_state
+ * copies) on the device and copies only them to the host: box after box,
+ * component after component, then k, j, i (i fastest) -- the order in which
+ * io_slice_nc_put and io_snap_pack_buff (forward/io_funcs.c:992-1111,
+ * 1525-1557) pack slices and snapshots.  out holds cgfd_box_floats() floats.
+ * A box outside the padded grid or the solver's components is CGFD_EINVAL. */
+int cgfd_solver_pack_boxes(cgfd_solver_t *s, const cgfd_box_t *box, int nbox,
+                           float *out);
+
+/* The same boxes written into w (ncmp x nx*ny*nz, reference layout) at their
+ * own positions; the other points of w are left untouched.  Replaces the
+ * whole-state copy in front of the reference's slice/snapshot writers, which
+ * read only these points (forward/drv_rk_curv_col.c:501-506). */
+int cgfd_solver_fetch_boxes(cgfd_solver_t *s, const cgfd_box_t *box, int nbox,
+                            float *w);
+
+/* Output overlapped with the time loop.  cgfd_solver_run_async queues steps
+ * and returns; cgfd_solver_pack_boxes_async queues the packing of boxes of
+ * the state after the queued steps into output slot `slot`
+ * (0..CGFD_OUT_SLOTS-1) and returns; cgfd_solver_collect_boxes waits for that
+ * slot and hands the boxes out as cgfd_solver_fetch_boxes (into w) and/or
+ * cgfd_solver_pack_boxes (into out) do -- either pointer may be NULL.  With
+ * two slots a caller writes step n's slices while the device runs step n+1.
+ * A slot must be collected before it is packed again.  Errors of queued work
+ * surface at the next collect or blocking call. */
+#define CGFD_OUT_SLOTS 2
+int cgfd_solver_run_async(cgfd_solver_t *s, int nsteps);
+int cgfd_solver_pack_boxes_async(cgfd_solver_t *s, const cgfd_box_t *box, int nbox,
+                                 int slot);
+int cgfd_solver_collect_boxes(cgfd_solver_t *s, int slot, float *w, float *out);
+
 /* Checks the whole wavefield for NaN/Inf on the device.
  * Returns CGFD_OK or CGFD_ENONFINITE. */
 int cgfd_solver_check_finite(cgfd_solver_t *s);
