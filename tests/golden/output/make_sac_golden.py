@@ -1,4 +1,4 @@
-"""Generate tests/golden/sac_output.npz from the reference's SAC output.
+"""Generate tests/golden/output/sac_output.npz from the reference's SAC output.
 
 Runs ``oracle/_ref/ref_probe sac`` (the reference's io_recv_output_sac,
 io_recv_output_sac_el_iso_strain and io_line_output_sac over lib/sacLib.c,
@@ -8,7 +8,7 @@ stores the inputs together with the bytes of every file it writes.
 This script needs the reference build and runs only where it exists; the
 fixture it writes is committed and is all the tests need elsewhere.
 
-    python tests/golden/make_sac_golden.py
+    python tests/golden/output/make_sac_golden.py
 """
 
 import os
@@ -19,7 +19,7 @@ import tempfile
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REPO = os.path.dirname(os.path.dirname(HERE))
+REPO = os.path.dirname(os.path.dirname(os.path.dirname(HERE)))
 PROBE = os.path.join(REPO, "oracle", "_ref", "ref_probe")
 
 

@@ -76,7 +76,7 @@ def test_sac_files_match_reference(tmp_path):
     """Station, station-strain and line SAC files equal, byte for byte, the
     files the reference's own writers made from the same seismograms."""
     import numpy as np
-    z = np.load(os.path.join(REPO, "tests", "golden", "sac_output.npz"))
+    z = np.load(os.path.join(REPO, "tests", "golden", "output", "sac_output.npz"))
     d = {k: z[k] for k in z.files if not k.startswith("file:")}
     names = [str(n) for n in d["names"]]
     evt, dt = str(d["evtnm"]), float(d["dt"])
