@@ -44,6 +44,7 @@ UNIT = "pt-stage/s"
 BYTES_PER_PT_STAGE = {"topo": 192, "flat": 192, "vti": 204, "visco": 504}
 WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "slices": dict(ni=400, nj=400, nk=200),
+             "locate": dict(ni=400, nj=400, nk=200),
              "batch": dict(ni=400, nj=400, nk=200),
              "vti": dict(ni=300, nj=300, nk=150),
              "visco": dict(ni=300, nj=300, nk=150),
@@ -302,6 +303,8 @@ def run_reference(args):
         return 0
     if args.workload == "batch":
         return run_reference_batch(args)
+    if args.workload == "locate":
+        return run_locate(args, reference=True)
     threads = os.cpu_count() or 1
     # warm-up sample, then the timed samples (one RK4 step each)
     cpu_rate(args, 1, threads)
@@ -650,6 +653,90 @@ def run_slices(args):
     return 0
 
 
+def locate_points(X, Y, Z, nsta=400, nsrc=64, seed=9):
+    """Stations on a regular 20 x 20 surface grid given by depth 0 and
+    sources at depth 1-8 km given by depth, over the physical area."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    xs, ys = X[3, 3:-3, 3:-3], Y[3, 3:-3, 3:-3]
+    x0, x1, y0, y1 = float(xs.min()), float(xs.max()), float(ys.min()), float(ys.max())
+    m = int(round(nsta ** 0.5))
+    gx, gy = np.meshgrid(np.linspace(x0, x1, m + 2)[1:-1], np.linspace(y0, y1, m + 2)[1:-1])
+    sta = np.stack([gx.ravel(), gy.ravel(), np.zeros(m * m)], 1)
+    src = np.stack([rng.uniform(x0, x1, nsrc), rng.uniform(y0, y1, nsrc),
+                    rng.uniform(1000.0, 8000.0, nsrc)], 1)
+    pts = np.concatenate([sta, src]).astype(np.float32)
+    return pts, np.ones(len(pts), np.int32)
+
+
+def run_locate(args, reference=False):
+    """Set-up of stations and sources given by coordinates: 400 stations and
+    64 sources located on the topography grid (depth converted to z, cell
+    search, shift sampling), points per second."""
+    import numpy as np
+    from types import SimpleNamespace
+    from cgfd3d_gb300 import models
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    X, Y, Z = [a.reshape(args.nk + 6, args.nj + 6, args.ni + 6) for a in
+               models._coords_of(SimpleNamespace(ni=args.ni, nj=args.nj, nk=args.nk), 2024)]
+    pts, dep = locate_points(X, Y, Z)
+    name = ("point location: %d stations (depth 0) + %d sources (depth 1-8 km) on the "
+            "topography grid %dx%dx%d" % (400, len(pts) - 400, args.ni, args.nj, args.nk))
+    sample_n = 6
+    line = {"metric": "points located/s", "unit": "points/s", "n_gpus": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": name, "parallelism": "single"}}
+    if reference or not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+        sub = np.linspace(0, len(pts) - 1, sample_n).astype(int)
+        t0 = time.perf_counter()
+        oracle.locate(X, Y, Z, pts[:0], dep[:0])          # grid bounds only
+        t1 = time.perf_counter()
+        oracle.locate(X, Y, Z, pts[sub], dep[sub])
+        t2 = time.perf_counter()
+        t_cpu = max((t2 - t1) - (t1 - t0), 1e-9)
+        cpu = {"value": sample_n / t_cpu, "unit": "points/s", "cores": 1, "kind": "port",
+               "sample": "%d of the points, C oracle port, 1 thread, %.2f s after the "
+                         "grid bounds (%.2f s, once per grid)" % (sample_n, t_cpu, t1 - t0)}
+    if reference:
+        line.update({"impl": "reference", "value": cpu["value"], "steps": 1, "warmup": 0,
+                     "ms_per_step": 1e3 * sample_n / cpu["value"], "cpu_baseline": cpu,
+                     "e2e": {"value": cpu["value"], "unit": "points/s",
+                             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        print(json.dumps(line), flush=True)
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    from cgfd3d_gb300 import locate
+    K, W = args.steps, max(args.warmup, 0)
+    t0 = time.perf_counter()
+    L = locate.Locator(X, Y, Z)
+    t_setup = time.perf_counter() - t0
+    for _ in range(W):
+        L.locate(pts, dep)
+    times = []
+    for _ in range(K):
+        t0 = time.perf_counter()
+        L.locate(pts, dep)
+        times.append(time.perf_counter() - t0)
+    L.close()
+    t = sum(times) / len(times)
+    line.update({"value": len(pts) / t, "steps": K, "warmup": W, "ms_per_step": 1e3 * t,
+                 "setup_ms": 1e3 * t_setup,
+                 "e2e": {"value": len(pts) / (t + t_setup / K), "unit": "points/s",
+                         "h2d_bytes_per_step": int(3 * X.size * 4 / K + pts.nbytes),
+                         "d2h_bytes_per_step": int(len(pts) * 32)},
+                 "gpu_launches": None})
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -658,6 +745,8 @@ def main():
         return run_batch(args)
     if args.workload == "slices":
         return run_slices(args)
+    if args.workload == "locate":
+        return run_locate(args)
     return run_ours(args)
 
 

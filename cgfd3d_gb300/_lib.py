@@ -58,6 +58,10 @@ def lib():
     L.cgfd_device_bytes.argtypes = [vp]
     L.cgfd_device_bytes.restype = C.c_size_t
     L.cgfd_metric_calc.argtypes = [C.c_int] * 9 + [vp] * 4
+    L.cgfd_locator_create.argtypes = [C.c_int] * 3 + [vp] * 3 + [C.POINTER(vp)]
+    L.cgfd_locator_locate.argtypes = [vp, C.c_int] + [vp] * 8
+    L.cgfd_locator_destroy.argtypes = [vp]
+    L.cgfd_locator_destroy.restype = None
     L.cgfd_batch_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
     L.cgfd_batch_run.argtypes = [vp, C.c_int]
     L.cgfd_batch_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]

@@ -265,6 +265,34 @@ int cgfd_metric_calc(int nx, int ny, int nz, int ni1, int ni2, int nj1, int nj2,
                      int nk1, int nk2, const float *x3d, const float *y3d,
                      const float *z3d, float *metric);
 
+/* ------------------------------------------------------------------------
+ * Point location: stations and sources given by coordinates, located on a
+ * curvilinear grid as the reference locates them
+ * (gd_curv_coord_to_glob_indx, forward/gd_t.c:1917-1995, after
+ * gd_curv_depth_to_axis, :2179-2297, for points given by depth), with the
+ * same indices and shifts bit for bit.  The grid has 3 ghost layers per side
+ * (ni = nx - 6, ...).
+ * ------------------------------------------------------------------------ */
+typedef struct cgfd_locator cgfd_locator_t;
+
+/* Copies the padded coordinates (nx*ny*nz floats each) to the device and
+ * computes the bounds the search uses (gd_curv_set_minmax,
+ * forward/gd_t.c:1708-1880). */
+int cgfd_locator_create(int nx, int ny, int nz, const float *x3d, const float *y3d,
+                        const float *z3d, cgfd_locator_t **out);
+
+/* Locates n points.  is_depth[q] != 0 (is_depth may be NULL): z[q] is a
+ * depth below the surface, converted to z first.  Per point: found[q] (1 or
+ * 0), index[3q..3q+2] the global physical indices (i, j, k counted from the
+ * first physical point; -1000 when not found), shift[3q..3q+2] the offsets
+ * inside the cell (what the reference returns in sx_inc, sy_inc, sz_inc) and
+ * z_located[q] (may be NULL) the z that was located. */
+int cgfd_locator_locate(cgfd_locator_t *loc, int n, const float *x, const float *y,
+                        const float *z, const int *is_depth, int *found, int *index,
+                        float *shift, float *z_located);
+
+void cgfd_locator_destroy(cgfd_locator_t *loc);
+
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);
 

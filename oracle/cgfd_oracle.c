@@ -1387,3 +1387,308 @@ int oracle_metric_calc(int nx, int ny, int nz, int ni1, int ni2, int nj1,
   }
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* point location on a curvilinear grid: stations and sources given by      */
+/* coordinates (set-up beside the time loop)                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Restates, for a grid with 3 ghost layers on one rank:
+ *   gd_curv_set_minmax            forward/gd_t.c:1708-1880 (global bounds,
+ *                                 cell and 4x4x4 tile boxes)
+ *   gd_curv_depth_to_axis         forward/gd_t.c:2179-2297
+ *   gd_curv_coord_to_local_indx   forward/gd_t.c:1998-2171
+ *   gd_curv_coord2shift_sample    forward/gd_t.c:2304-2370
+ *   isPointInHexahedron           media/media_geometry3d.cpp:150-265
+ *   fdlib_math_isPoint2InTri, _Point2InWhichTri, _computeZfromTri
+ *                                 lib/fdlib_math.c:246-338
+ * in float arithmetic ordered as there (-ffp-contract=off). */
+
+#define LOC_TILES 4
+#define LOC_SAMPLES 100
+
+typedef struct { float x, y, z; } v3_t;
+
+static v3_t v3_sub(v3_t a, v3_t b)
+{
+  v3_t r = {a.x - b.x, a.y - b.y, a.z - b.z};
+  return r;
+}
+static float v3_dot(v3_t a, v3_t b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static v3_t v3_cross(v3_t a, v3_t b)
+{
+  v3_t r = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+  return r;
+}
+static float v3_len(v3_t a) { return sqrtf(v3_dot(a, a)); }
+static float tri_area2(v3_t a, v3_t b, v3_t c)
+{
+  return v3_len(v3_cross(v3_sub(b, a), v3_sub(c, a)));
+}
+
+/* a point on a triangle: the three sub-areas add up to its area */
+static int on_tri(v3_t p, v3_t a, v3_t b, v3_t c)
+{
+  float s = tri_area2(p, a, b) + tri_area2(p, b, c) + tri_area2(p, c, a) -
+            tri_area2(a, b, c);
+  return fabs(s) < 1e-6;
+}
+
+/* the ten tetrahedra (two cuts into five) of a hexahedron with corners
+ * numbered i + 2 j + 4 k, each as four faces */
+static const unsigned char TETRA_FACES[10][4][3] = {
+    {{0, 4, 2}, {2, 4, 1}, {1, 4, 0}, {0, 2, 1}},
+    {{4, 6, 2}, {2, 6, 7}, {7, 6, 4}, {4, 2, 7}},
+    {{2, 7, 3}, {3, 7, 1}, {1, 2, 3}, {1, 7, 2}},
+    {{7, 4, 5}, {1, 7, 5}, {5, 4, 1}, {1, 4, 7}},
+    {{2, 4, 7}, {7, 4, 1}, {2, 7, 1}, {4, 2, 1}},
+    {{4, 5, 6}, {4, 6, 0}, {4, 0, 5}, {6, 5, 0}},
+    {{6, 2, 0}, {6, 3, 2}, {0, 2, 3}, {3, 6, 0}},
+    {{6, 5, 7}, {3, 6, 7}, {7, 5, 3}, {5, 6, 3}},
+    {{5, 0, 1}, {3, 5, 1}, {0, 3, 1}, {0, 5, 3}},
+    {{5, 6, 0}, {5, 0, 3}, {0, 6, 3}, {3, 6, 5}}};
+
+static int in_hexahedron(v3_t p, const v3_t *v)
+{
+  for (int t = 0; t < 10; t++) {
+    int inside = 1;
+    for (int f = 0; f < 4 && inside; f++) {
+      v3_t a = v[TETRA_FACES[t][f][0]], b = v[TETRA_FACES[t][f][1]];
+      v3_t c = v[TETRA_FACES[t][f][2]];
+      if (on_tri(p, a, b, c)) break;          /* on a face: inside */
+      v3_t p2f = v3_sub(a, p);
+      v3_t n = v3_cross(v3_sub(b, a), v3_sub(c, a));
+      float d = v3_len(n);
+      n.x = n.x / d; n.y = n.y / d; n.z = n.z / d;
+      float sign = v3_dot(p2f, n);
+      sign /= v3_len(p2f);
+      if (sign <= -1.0e-6f) inside = 0;
+    }
+    if (inside) return 1;
+  }
+  return 0;
+}
+
+/* shift of p inside a cell: the closest of 101^3 trilinear samples, the
+ * first in (k, j, i) order on ties */
+static void cell_shift(v3_t p, const v3_t *v, float *si, float *sj, float *sk)
+{
+  float min_dist = sqrtf((p.x - v[0].x) * (p.x - v[0].x) + (p.y - v[0].y) * (p.y - v[0].y) +
+                         (p.z - v[0].z) * (p.z - v[0].z));
+  int bi = 0, bj = 0, bk = 0;
+  for (int n3 = 0; n3 <= LOC_SAMPLES; n3++) {
+    float lz[2];
+    lz[1] = (float)n3 / (float)LOC_SAMPLES;
+    lz[0] = 1.0 - lz[1];
+    for (int n2 = 0; n2 <= LOC_SAMPLES; n2++) {
+      float ly[2];
+      ly[1] = (float)n2 / (float)LOC_SAMPLES;
+      ly[0] = 1.0 - ly[1];
+      for (int n1 = 0; n1 <= LOC_SAMPLES; n1++) {
+        float lx[2];
+        lx[1] = (float)n1 / (float)LOC_SAMPLES;
+        lx[0] = 1.0 - lx[1];
+        float x = 0, y = 0, z = 0;
+        for (int c = 0; c < 8; c++) {
+          float w = lx[c & 1] * ly[(c >> 1) & 1] * lz[c >> 2];
+          x += w * v[c].x;
+          y += w * v[c].y;
+          z += w * v[c].z;
+        }
+        float d = sqrtf((p.x - x) * (p.x - x) + (p.y - y) * (p.y - y) + (p.z - z) * (p.z - z));
+        if (min_dist > d) {
+          min_dist = d;
+          bi = n1; bj = n2; bk = n3;
+        }
+      }
+    }
+  }
+  *si = (float)bi / (float)LOC_SAMPLES;
+  *sj = (float)bj / (float)LOC_SAMPLES;
+  *sk = (float)bk / (float)LOC_SAMPLES;
+}
+
+static int in_tri2(float px, float py, const float *vx, const float *vy)
+{
+  for (int i = 0; i < 3; i++) {
+    float ex = i == 2 ? vx[0] - vx[2] : vx[i + 1] - vx[i];
+    float ey = i == 2 ? vy[0] - vy[2] : vy[i + 1] - vy[i];
+    float tx = px - vx[i], ty = py - vy[i];
+    float sign = ex * ty - ey * tx;
+    sign /= sqrt(ex * ex + ey * ey);
+    if (sign < 0) return 0;
+  }
+  return 1;
+}
+
+static float z_on_tri(float x, float y, v3_t p1, v3_t p2, v3_t p3)
+{
+  float v1x = p2.x - p1.x, v1y = p2.y - p1.y, v1z = p2.z - p1.z;
+  float v2x = p3.x - p1.x, v2y = p3.y - p1.y, v2z = p3.z - p1.z;
+  float a = v1y * v2z - v1z * v2y;
+  float b = v1z * v2x - v1x * v2z;
+  float c = v1x * v2y - v1y * v2x;
+  float d = -(a * p1.x + b * p1.y + c * p1.z);
+  return -(a * x + b * y + d) / c;
+}
+
+typedef struct {
+  int nx, ny, nz;
+  size_t sl;
+  const float *x, *y, *z;
+  float xmin, xmax, ymin, ymax, zmin, zmax;
+  int ts[3][LOC_TILES], te[3][LOC_TILES];
+  float tb[LOC_TILES][LOC_TILES][LOC_TILES][6];   /* [kt][jt][it]: x0 x1 y0 y1 z0 z1 */
+} loc_grid_t;
+
+static v3_t grid_pt(const loc_grid_t *g, int i, int j, int k)
+{
+  size_t q = (size_t)i + (size_t)j * g->nx + (size_t)k * g->sl;
+  v3_t r = {g->x[q], g->y[q], g->z[q]};
+  return r;
+}
+
+static void cell_box(const loc_grid_t *g, int i, int j, int k, float *b)
+{
+  v3_t p = grid_pt(g, i, j, k);
+  b[0] = b[1] = p.x; b[2] = b[3] = p.y; b[4] = b[5] = p.z;
+  for (int c = 1; c < 8; c++) {
+    v3_t q = grid_pt(g, i + (c & 1), j + ((c >> 1) & 1), k + (c >> 2));
+    b[0] = b[0] < q.x ? b[0] : q.x; b[1] = b[1] > q.x ? b[1] : q.x;
+    b[2] = b[2] < q.y ? b[2] : q.y; b[3] = b[3] > q.y ? b[3] : q.y;
+    b[4] = b[4] < q.z ? b[4] : q.z; b[5] = b[5] > q.z ? b[5] : q.z;
+  }
+}
+
+static void loc_grid_init(loc_grid_t *g, int nx, int ny, int nz, const float *x,
+                          const float *y, const float *z)
+{
+  g->nx = nx; g->ny = ny; g->nz = nz;
+  g->sl = (size_t)nx * ny;
+  g->x = x; g->y = y; g->z = z;
+  size_t vol = g->sl * nz;
+  g->xmin = g->xmax = x[0]; g->ymin = g->ymax = y[0]; g->zmin = g->zmax = z[0];
+  for (size_t q = 0; q < vol; q++) {
+    g->xmin = g->xmin < x[q] ? g->xmin : x[q]; g->xmax = g->xmax > x[q] ? g->xmax : x[q];
+    g->ymin = g->ymin < y[q] ? g->ymin : y[q]; g->ymax = g->ymax > y[q] ? g->ymax : y[q];
+    g->zmin = g->zmin < z[q] ? g->zmin : z[q]; g->zmax = g->zmax > z[q] ? g->zmax : z[q];
+  }
+  const int n[3] = {nx - 6, ny - 6, nz - 6};
+  for (int d = 0; d < 3; d++) {
+    int avg = n[d] / LOC_TILES, left = n[d] % LOC_TILES;
+    for (int t = 0; t < LOC_TILES; t++) {
+      g->ts[d][t] = t == 0 ? 3 : g->te[d][t - 1] + 1;
+      g->te[d][t] = g->ts[d][t] + avg - 1 + (t < left ? 1 : 0);
+    }
+  }
+  for (int kt = 0; kt < LOC_TILES; kt++)
+    for (int jt = 0; jt < LOC_TILES; jt++)
+      for (int it = 0; it < LOC_TILES; it++) {
+        float *tb = g->tb[kt][jt][it];
+        tb[0] = tb[2] = tb[4] = 1.0e26f;
+        tb[1] = tb[3] = tb[5] = -1.0e26f;
+        for (int k = g->ts[2][kt]; k <= g->te[2][kt]; k++)
+          for (int j = g->ts[1][jt]; j <= g->te[1][jt]; j++)
+            for (int i = g->ts[0][it]; i <= g->te[0][it]; i++) {
+              float b[6];
+              cell_box(g, i, j, k, b);
+              for (int e = 0; e < 6; e += 2) {
+                tb[e] = tb[e] < b[e] ? tb[e] : b[e];
+                tb[e + 1] = tb[e + 1] > b[e + 1] ? tb[e + 1] : b[e + 1];
+              }
+            }
+      }
+}
+
+static void depth_to_axis(const loc_grid_t *g, float sx, float sy, float *sz)
+{
+  if (sx < g->xmin || sx > g->xmax || sy < g->ymin || sy > g->ymax) return;
+  const int kt = LOC_TILES - 1, k = g->te[2][kt];
+  for (int jt = 0; jt < LOC_TILES; jt++)
+    for (int it = 0; it < LOC_TILES; it++) {
+      const float *tb = g->tb[kt][jt][it];
+      if (sx < tb[0] || sx > tb[1] || sy < tb[2] || sy > tb[3]) continue;
+      for (int j = g->ts[1][jt]; j <= g->te[1][jt]; j++)
+        for (int i = g->ts[0][it]; i <= g->te[0][it]; i++) {
+          float b[6];
+          cell_box(g, i, j, k, b);
+          if (sx < b[0] || sx > b[1] || sy < b[2] || sy > b[3]) continue;
+          v3_t p[4];
+          float vx[5], vy[5];
+          for (int c = 0; c < 4; c++) p[c] = grid_pt(g, i + (c & 1), j + (c >> 1), k);
+          /* corners 0, 1, 3, 2 around the quadrilateral */
+          vx[0] = p[0].x; vx[1] = p[1].x; vx[2] = p[3].x; vx[3] = p[2].x; vx[4] = p[0].x;
+          vy[0] = p[0].y; vy[1] = p[1].y; vy[2] = p[3].y; vy[3] = p[2].y; vy[4] = p[0].y;
+          if (in_tri2(sx, sy, vx + 2, vy + 2)) {
+            *sz = z_on_tri(sx, sy, p[3], p[2], p[0]) - *sz;
+            return;
+          }
+          if (in_tri2(sx, sy, vx, vy)) {
+            *sz = z_on_tri(sx, sy, p[0], p[1], p[3]) - *sz;
+            return;
+          }
+        }
+    }
+}
+
+static int locate_one(const loc_grid_t *g, float sx, float sy, float sz, int *gi,
+                      float *shift)
+{
+  gi[0] = gi[1] = gi[2] = -1000;
+  shift[0] = shift[1] = shift[2] = 0.0f;
+  if (sx < g->xmin || sx > g->xmax || sy < g->ymin || sy > g->ymax || sz < g->zmin ||
+      sz > g->zmax)
+    return 0;
+  const v3_t p = {sx, sy, sz};
+  for (int kt = 0; kt < LOC_TILES; kt++)
+    for (int jt = 0; jt < LOC_TILES; jt++)
+      for (int it = 0; it < LOC_TILES; it++) {
+        const float *tb = g->tb[kt][jt][it];
+        if (sx < tb[0] || sx > tb[1] || sy < tb[2] || sy > tb[3] || sz < tb[4] ||
+            sz > tb[5])
+          continue;
+        for (int k = g->ts[2][kt]; k <= g->te[2][kt]; k++)
+          for (int j = g->ts[1][jt]; j <= g->te[1][jt]; j++)
+            for (int i = g->ts[0][it]; i <= g->te[0][it]; i++) {
+              float b[6];
+              cell_box(g, i, j, k, b);
+              if (sx < b[0] || sx > b[1] || sy < b[2] || sy > b[3] || sz < b[4] ||
+                  sz > b[5])
+                continue;
+              v3_t v[8];
+              for (int c = 0; c < 8; c++)
+                v[c] = grid_pt(g, i + (c & 1), j + ((c >> 1) & 1), k + (c >> 2));
+              if (!in_hexahedron(p, v)) continue;
+              int li[3] = {i, j, k};
+              cell_shift(p, v, &shift[0], &shift[1], &shift[2]);
+              for (int d = 0; d < 3; d++) {
+                if (shift[d] > 0.5) {
+                  li[d] += 1;
+                  shift[d] -= 1.0;
+                }
+                gi[d] = li[d] - 3;      /* local with ghosts -> global physical */
+              }
+              return 1;
+            }
+      }
+  return 0;
+}
+
+/* Locates n points (is_depth[q]: pz[q] is a depth below the surface, first
+ * converted to z).  Per point: found, global physical indices (-1000 when
+ * not found), shifts in the cell, and the z that was located. */
+int oracle_locate(int nx, int ny, int nz, const float *x3d, const float *y3d,
+                  const float *z3d, int n, const float *px, const float *py,
+                  const float *pz, const int *is_depth, int *found, int *idx,
+                  float *shift, float *zout)
+{
+  loc_grid_t g;
+  loc_grid_init(&g, nx, ny, nz, x3d, y3d, z3d);
+  for (int q = 0; q < n; q++) {
+    float sz = pz[q];
+    if (is_depth && is_depth[q]) depth_to_axis(&g, px[q], py[q], &sz);
+    found[q] = locate_one(&g, px[q], py[q], sz, idx + 3 * q, shift + 3 * q);
+    zout[q] = sz;
+  }
+  return 0;
+}

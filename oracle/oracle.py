@@ -117,3 +117,28 @@ def metric_calc(nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2, x3d, y3d, z3d):
     L.oracle_metric_calc(nx, ny, nz, ni1, ni2, nj1, nj2, nk1, nk2, x.ctypes.data,
                          y.ctypes.data, z.ctypes.data, out.ctypes.data)
     return out.reshape(10, -1)
+
+
+def locate(x3d, y3d, z3d, points, is_depth=None):
+    """Points located on a curvilinear grid (padded (nz, ny, nx) coordinates,
+    3 ghost layers) as the reference locates stations and sources given by
+    coordinates.  Returns found (n,), global physical indices (n, 3), shifts
+    (n, 3) and the located z (n,) (depths converted)."""
+    import numpy as np
+    L = lib()
+    L.oracle_locate.restype = C.c_int
+    L.oracle_locate.argtypes = [C.c_int] * 3 + [C.c_void_p] * 3 + [C.c_int] + [C.c_void_p] * 8
+    nz, ny, nx = np.shape(x3d)
+    x, y, z = [np.ascontiguousarray(a, np.float32).ravel() for a in (x3d, y3d, z3d)]
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    n = len(pts)
+    px, py, pz = [np.ascontiguousarray(pts[:, d]) for d in range(3)]
+    dep = np.zeros(n, np.int32) if is_depth is None else np.ascontiguousarray(is_depth, np.int32)
+    found = np.zeros(n, np.int32)
+    idx = np.zeros((n, 3), np.int32)
+    shift = np.zeros((n, 3), np.float32)
+    zout = np.zeros(n, np.float32)
+    L.oracle_locate(nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data, n,
+                    px.ctypes.data, py.ctypes.data, pz.ctypes.data, dep.ctypes.data,
+                    found.ctypes.data, idx.ctypes.data, shift.ctypes.data, zout.ctypes.data)
+    return found, idx, shift, zout

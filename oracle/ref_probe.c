@@ -16,6 +16,16 @@
  *         char line_name[16];
  *         nl x { int seq; float x, y, z; }
  *         float line_seismo[nl][ncmp][nt];
+ *
+ *   ref_probe locate <input> <output>
+ *       points of a curvilinear grid located as the reference locates
+ *       stations and sources given by coordinates: gd_curv_set_minmax, then
+ *       per point gd_curv_depth_to_axis when the point's z is a depth and
+ *       gd_curv_coord_to_glob_indx (forward/gd_t.c:1708-2171, 2179-2297).
+ *       <input>:  int nx, ny, nz, n; float x3d, y3d, z3d [nz][ny][nx];
+ *                 n x { float x, y, z; int is_depth; }
+ *       <output>: n x { int is_here, si, sj, sk; float sx_inc, sy_inc,
+ *                       sz_inc, z; }   (z after the depth conversion)
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -109,9 +119,69 @@ static int probe_sac(const char *in, char *out_dir)
   return 0;
 }
 
+static int probe_locate(const char *in, const char *out)
+{
+  FILE *fp = fopen(in, "rb");
+  if (!fp) return 2;
+  int hdr[4];
+  rd(hdr, sizeof hdr, fp);
+  gd_t gd;
+  memset(&gd, 0, sizeof gd);
+  gd.type = GD_TYPE_CURV;
+  gd.nx = hdr[0]; gd.ny = hdr[1]; gd.nz = hdr[2];
+  const int n = hdr[3];
+  gd.npoint_ghosts = 3;
+  gd.ni = gd.nx - 6; gd.nj = gd.ny - 6; gd.nk = gd.nz - 6;
+  gd.ni1 = 3; gd.ni2 = gd.ni1 + gd.ni - 1;
+  gd.nj1 = 3; gd.nj2 = gd.nj1 + gd.nj - 1;
+  gd.nk1 = 3; gd.nk2 = gd.nk1 + gd.nk - 1;
+  gd.ni1_to_glob_phys0 = 0; gd.ni2_to_glob_phys0 = gd.ni - 1;
+  gd.nj1_to_glob_phys0 = 0; gd.nj2_to_glob_phys0 = gd.nj - 1;
+  gd.nk1_to_glob_phys0 = 0; gd.nk2_to_glob_phys0 = gd.nk - 1;
+  gd.gni1 = 0; gd.gnj1 = 0; gd.gnk1 = 0;
+  gd.gni2 = gd.ni - 1; gd.gnj2 = gd.nj - 1; gd.gnk2 = gd.nk - 1;
+  gd.siz_iy = gd.siz_line = gd.nx;
+  gd.siz_iz = gd.siz_slice = (size_t)gd.nx * gd.ny;
+  gd.siz_icmp = gd.siz_volume = gd.siz_slice * gd.nz;
+  size_t vol = gd.siz_icmp;
+  gd.x3d = malloc(vol * sizeof(float));
+  gd.y3d = malloc(vol * sizeof(float));
+  gd.z3d = malloc(vol * sizeof(float));
+  rd(gd.x3d, vol * sizeof(float), fp);
+  rd(gd.y3d, vol * sizeof(float), fp);
+  rd(gd.z3d, vol * sizeof(float), fp);
+  float **cells[6] = {&gd.cell_xmin, &gd.cell_xmax, &gd.cell_ymin, &gd.cell_ymax,
+                      &gd.cell_zmin, &gd.cell_zmax};
+  for (int c = 0; c < 6; c++) *cells[c] = calloc(vol, sizeof(float));
+  gd_curv_set_minmax(&gd);
+
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  for (int q = 0; q < n; q++) {
+    float v[3];
+    int is_depth;
+    rd(v, sizeof v, fp);
+    rd(&is_depth, sizeof is_depth, fp);
+    float sz = v[2];
+    if (is_depth) gd_curv_depth_to_axis(&gd, v[0], v[1], &sz, MPI_COMM_WORLD, 0);
+    int idx[4];
+    float inc[4];
+    idx[0] = gd_curv_coord_to_glob_indx(&gd, v[0], v[1], sz, MPI_COMM_WORLD, 0,
+                                        &idx[1], &idx[2], &idx[3], &inc[0], &inc[1],
+                                        &inc[2]);
+    inc[3] = sz;
+    fwrite(idx, sizeof idx, 1, fo);
+    fwrite(inc, sizeof inc, 1, fo);
+  }
+  fclose(fo);
+  fclose(fp);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
-  fprintf(stderr, "usage: ref_probe sac <input> <out_dir>\n");
+  if (argc == 4 && strcmp(argv[1], "locate") == 0) return probe_locate(argv[2], argv[3]);
+  fprintf(stderr, "usage: ref_probe sac|locate <input> <output>\n");
   return 2;
 }
