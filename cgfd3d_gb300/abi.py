@@ -6,7 +6,7 @@ tests/test_abi.py checks sizes and offsets against a compiled probe.
 
 import ctypes as C
 
-CGFD_ABI_VERSION = 3
+CGFD_ABI_VERSION = 4
 CGFD_MEDIUM_ELASTIC_ISO = 2
 CGFD_MEDIUM_ELASTIC_VTI = 3
 CGFD_MEDIUM_VISCOELASTIC_ISO = 5
@@ -73,7 +73,11 @@ class Problem(C.Structure):
            ("nt_total", C.c_int),
            ("x3d", PF), ("y3d", PF), ("z3d", PF),
            ("src_force_rate_indx", PI),
-           ("Fx_rate", PF), ("Fy_rate", PF), ("Fz_rate", PF)]
+           ("Fx_rate", PF), ("Fy_rate", PF), ("Fz_rate", PF),
+           ("graves_qs", C.c_int), ("qs_freq", C.c_float), ("Qs", PF),
+           ("ablexp", C.c_int),
+           ("ablexp_Ex", PF), ("ablexp_Ey", PF), ("ablexp_Ez", PF),
+           ("ablexp_blk", (C.c_int * 7) * 6)]
     )
 
 

@@ -114,6 +114,9 @@ struct StageArgs {
   int cur_level;               /* level index of `cur` (TMA coordinate) */
   int pre_level, end_level;    /* level indices of `pre` and `end` */
   int kchunk;                  /* planes per CTA along k */
+  /* Graves Q attenuation factors expf(-PI f dt / Qs) per point (pitched
+   * volume), applied to `end` by the last stage; null when off */
+  const float *qatt;
 };
 
 /* StageArgs is copied word by word into shared memory by the batched stage

@@ -717,6 +717,46 @@ static int build_source_entries(const cgfd_problem_t *p, std::vector<int> &col,
 /* solver                                                                    */
 /* ------------------------------------------------------------------------ */
 
+/* The enabled blocks of the exponential sponge and their point counts. */
+struct AblexpBlocks {
+  int n;
+  int box[6][6];                /* ni1, ni2, nj1, nj2, nk1, nk2 */
+  long long first[7];           /* prefix sums of the blocks' point counts */
+};
+
+/* Exponential sponge after a step (forward/bdry_t.c:841-890): the points of
+ * the blocks times min(Ex[i], Ey[j], Ez[k]), every component. */
+__global__ void k_ablexp(DevGrid g, float *w, int ncmp, AblexpBlocks B,
+                         const float *__restrict__ Ex, const float *__restrict__ Ey,
+                         const float *__restrict__ Ez)
+{
+  const long long total = B.first[B.n];
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int b = 0;
+    while (b + 1 < B.n && t >= B.first[b + 1]) b++;
+    const int *x = B.box[b];
+    const int ni = x[1] - x[0] + 1, nj = x[3] - x[2] + 1;
+    long long r = t - B.first[b];
+    const int i = x[0] + (int)(r % ni);
+    r /= ni;
+    const int j = x[2] + (int)(r % nj);
+    const int k = x[4] + (int)(r / nj);
+    float mask = Ex[i] < Ey[j] ? Ex[i] : Ey[j];
+    if (mask > Ez[k]) mask = Ez[k];
+    const long long q = (long long)(i + g.xoff) + (long long)j * g.px + (long long)k * g.sl;
+    for (int c = 0; c < ncmp; c++) w[c * g.vol + q] *= mask;
+  }
+}
+
+/* Graves Q factors in place over a pitched volume holding Qs */
+__global__ void k_qatt(float *v, long long n, float coef)
+{
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    v[t] = expf(coef / v[t]);
+}
+
 /* One output slot: a set of boxes (slices, snapshots) packed on the device
  * and copied to pinned host memory behind the queued steps. */
 struct OutSlot {
@@ -774,6 +814,9 @@ struct cgfd_solver {
   float *pg, *dis;              /* surface peak-motion maps (free top) */
   float *staging;               /* upload staging volume (set-up only) */
   OutSlot out[CGFD_OUT_SLOTS + 1];   /* output boxes; the last: blocking calls */
+  float *qatt;                  /* Graves Q factors (pitched volume), or null */
+  float *abl;                   /* sponge masks Ex | Ey | Ez, or null */
+  AblexpBlocks abx;             /* sponge blocks */
   StageMaps maps;               /* tensor maps of the stage kernel */
   int kernel;                   /* 2: TMA z-marching (default), 1: direct */
   int ty;                       /* tile rows of the medium's stage kernel */
@@ -798,7 +841,8 @@ extern "C" size_t cgfd_device_bytes(const cgfd_problem_t *p)
   size_t vol = (size_t)pitch_for(p->ni) * p->ny * p->nz;
   int med = medium_of(p->medium_type);
   int nmw = med == MED_VIS ? p->nmaxwell : 0;
-  size_t b = (size_t)(4 * (9 + 6 * nmw) + 10 + med_ncomp(med, nmw)) * vol * sizeof(float);
+  size_t b = (size_t)(4 * (9 + 6 * nmw) + 10 + med_ncomp(med, nmw) + (p->graves_qs ? 1 : 0)) *
+             vol * sizeof(float);
   if (p->free_top) b += (med == MED_VIS ? 4 : 3) * (size_t)p->nx * p->ny * 9 * sizeof(float);
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {
@@ -890,6 +934,22 @@ static int validate(const cgfd_problem_t *p)
         }
       }
     }
+  if (p->graves_qs) {
+    if (!p->Qs) return set_err(CGFD_EINVAL, "Graves Q: Qs missing");
+    if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO)
+      return set_err(CGFD_EINVAL, "Graves Q and GMB attenuation are exclusive");
+  }
+  if (p->ablexp) {
+    if (!p->ablexp_Ex || !p->ablexp_Ey || !p->ablexp_Ez)
+      return set_err(CGFD_EINVAL, "sponge masks missing");
+    for (int n = 0; n < 6; n++) {
+      const int *b = p->ablexp_blk[n];
+      if (b[0] != 1) continue;
+      if (b[1] < 0 || b[2] >= p->nx || b[3] < 0 || b[4] >= p->ny || b[5] < 0 ||
+          b[6] >= p->nz || b[2] < b[1] || b[4] < b[3] || b[6] < b[5])
+        return set_err(CGFD_EINVAL, "sponge block %d outside the grid", n);
+    }
+  }
   if (p->recv_n > 0 && (!p->recv_dijk || !p->recv_indx1d || !p->recv_seismo))
     return set_err(CGFD_EINVAL, "receiver arrays missing");
   if (p->recv_n > 0 && p->recv_max_nt < p->nt_total)
@@ -1093,7 +1153,7 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
                   s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
                   s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
                   s->line_iptr, s->d_it, s->d_flag, s->d_err, s->pg, s->dis,
-                  s->sf, s->sf_w, s->frate, s->surf, s->staging};
+                  s->sf, s->sf_w, s->frate, s->surf, s->staging, s->qatt, s->abl};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (OutSlot &o : s->out) {
@@ -1194,6 +1254,39 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
     }
     for (int m = 0; m < nm; m++)
       TRYC(upload_volume(s, s->media + m * vol, md[m]));
+  }
+  if (p->graves_qs) {
+    /* Graves Q factors, forward/sv_curv_col_el.c:642 and :656:
+     * coef = -PI * freq * dt evaluated in double, stored as float */
+    TRY(dalloc(s, &s->qatt, vol));
+    TRYC(cudaMemsetAsync(s->qatt, 0, vol * sizeof(float), st));
+    TRYC(upload_volume(s, s->qatt, p->Qs));
+    const float coef = (float)(-3.14159265358979323846 * (double)p->qs_freq * (double)p->dt);
+    k_qatt<<<152 * 8, 256, 0, st>>>(s->qatt, (long long)vol, coef);
+    TRYC(cudaGetLastError());
+  }
+  if (p->ablexp) {
+    TRY(dalloc(s, &s->abl, (size_t)p->nx + p->ny + p->nz));
+    TRYC(cudaMemcpyAsync(s->abl, p->ablexp_Ex, p->nx * sizeof(float), cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemcpyAsync(s->abl + p->nx, p->ablexp_Ey, p->ny * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemcpyAsync(s->abl + p->nx + p->ny, p->ablexp_Ez, p->nz * sizeof(float),
+                         cudaMemcpyHostToDevice, st));
+    s->abx.n = 0;
+    s->abx.first[0] = 0;
+    for (int n = 0; n < 6; n++) {
+      const int *b = p->ablexp_blk[n];
+      if (b[0] != 1) continue;
+      int *x = s->abx.box[s->abx.n];
+      for (int e = 0; e < 6; e++) x[e] = b[1 + e];
+      s->abx.first[s->abx.n + 1] = s->abx.first[s->abx.n] +
+          (long long)(x[1] - x[0] + 1) * (x[3] - x[2] + 1) * (x[5] - x[4] + 1);
+      s->abx.n++;
+    }
+    if (s->abx.n == 0) {      /* no enabled block: nothing to apply */
+      cudaFree(s->abl);
+      s->abl = nullptr;
+    }
   }
   tr.mark("media");
   /* PML faces */
@@ -1523,6 +1616,7 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
     else if (istage == 2) { a.acur[f] = tB; a.atmp_out[f] = tA; }
     else { a.acur[f] = tA; a.atmp_out[f] = nullptr; }
   }
+  a.qatt = s->qatt;
   a.free_top = p->free_top;
   if (p->free_top) {
     size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
@@ -1600,6 +1694,13 @@ static int enqueue_step(cgfd_solver_t *s, int it, int *ev_next)
     dim3 b(32, 8), gr((s->g.ni + 31) / 32, (s->g.nj + 7) / 8);
     size_t n2 = (size_t)s->g.nx * s->g.ny * 9;
     k_vis_free<<<gr, b, 0, st>>>(s->g, s->wav + s->end_lev * L, s->mats + 3 * n2);
+  }
+  if (s->abl) {
+    /* exponential sponge (forward/drv_rk_curv_col.c:484-486) */
+    long long nb = (s->abx.first[s->abx.n] + 255) / 256;
+    k_ablexp<<<(int)(nb < 152 * 8 ? nb : 152 * 8), 256, 0, st>>>(
+        s->g, s->wav + s->end_lev * L, s->ncmp, s->abx, s->abl, s->abl + s->g.nx,
+        s->abl + s->g.nx + s->g.ny);
   }
   if (s->pg) {
     dim3 b(32, 8), gr((s->g.ni + 31) / 32, (s->g.nj + 7) / 8);
@@ -2248,6 +2349,9 @@ extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
       return set_err(CGFD_EINVAL, "batched shots: elastic media (iso, VTI) only");
     if (p->src_n > 0 && p->src_n_surface_force > 0)
       return set_err(CGFD_EINVAL, "shot %d: surface force sources are not batched", k);
+    if (p->ablexp)
+      return set_err(CGFD_EINVAL, "shot %d: the exponential sponge is not batched "
+                     "(CFS-PML is)", k);
     if (p->nt_total != shots[0]->nt_total || p->dt != shots[0]->dt)
       return set_err(CGFD_EINVAL, "shot %d: every shot steps with the same dt and nt_total", k);
   }

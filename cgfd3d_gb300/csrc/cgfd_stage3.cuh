@@ -579,7 +579,11 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
         }
       }
 
-      /* RK combine */
+      /* RK combine; the last stage also applies the Graves Q factor
+       * (forward/drv_rk_curv_col.c:408-416: end += b dt rhs, then end *= Qatt) */
+      float qa = 1.0f;
+      const bool graves = KIND == 2 && a.qatt != nullptr;
+      if (graves) qa = __ldg(a.qatt + q);
 #pragma unroll
       for (int c = 0; c < 9; c++) {
         long long x = c * vol + q;
@@ -591,7 +595,8 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
           a.tmp_out[x] = st[S_PRE + c * PTS + sp] + a.ca * r[c];
           a.end[x] = st[S_END + c * PTS + sp] + a.cb * r[c];
         } else {
-          a.end[x] = st[S_END + c * PTS + sp] + a.cb * r[c];
+          float v = st[S_END + c * PTS + sp] + a.cb * r[c];
+          a.end[x] = graves ? v * qa : v;
         }
       }
       if (MED == MED_VIS) {

@@ -28,7 +28,7 @@
  *
  * Errors print the library's message and call MPI_Abort when MPI is linked
  * (exit(1) otherwise), as the reference does.  Unsupported configurations
- * (dd sources, ablexp, full anisotropy, Graves Q)
+ * (dd sources, full anisotropy)
  * are reported the same way instead of being ignored.
  */
 #include <stdio.h>
@@ -40,6 +40,7 @@
 #ifdef CGFD_DROPIN_REFERENCE_HEADERS
 #include "drv_rk_curv_col.h"
 #define CGFD_REF_VISCO_GMB CONST_VISCO_GMB
+#define CGFD_REF_VISCO_GRAVES_QS CONST_VISCO_GRAVES_QS
 #else
 #include "../../../include/cgfd3d_ref_abi.h"
 #endif
@@ -179,7 +180,6 @@ void drv_rk_curv_col_allstep(
       md->visco_type != CGFD_REF_VISCO_GMB)
     unsupported("a visco-elastic model other than GMB");
   if (src->dd_is_valid == 1) unsupported("a distributed (dd) source");
-  if (bdry->is_enable_ablexp == 1) unsupported("the ablexp sponge boundary");
 
   cgfd_problem_t p;
   memset(&p, 0, sizeof(p));
@@ -206,6 +206,24 @@ void drv_rk_curv_col_allstep(
       p.Ymu[n] = md->Ymu[n];
     }
     p.x3d = gd->x3d; p.y3d = gd->y3d; p.z3d = gd->z3d;
+  }
+  if (md->visco_type == CGFD_REF_VISCO_GRAVES_QS) {
+    /* Graves Q (forward/drv_rk_curv_col.c:414-416) */
+    p.graves_qs = 1;
+    p.qs_freq = md->visco_Qs_freq;
+    p.Qs = md->Qs;
+  }
+  if (bdry->is_enable_ablexp == 1) {
+    /* exponential sponge (forward/drv_rk_curv_col.c:484-486) */
+    p.ablexp = 1;
+    p.ablexp_Ex = bdry->ablexp_Ex;
+    p.ablexp_Ey = bdry->ablexp_Ey;
+    p.ablexp_Ez = bdry->ablexp_Ez;
+    for (int n = 0; n < 6; n++) {
+      const bdry_block_t *D = &bdry->bdry_blk[n];
+      int v[7] = {D->enable, D->ni1, D->ni2, D->nj1, D->nj2, D->nk1, D->nk2};
+      memcpy(p.ablexp_blk[n], v, sizeof v);
+    }
   }
   p.free_top = bdry->is_sides_free[2][1] == 1;
   for (int d = 0; d < 3; d++)

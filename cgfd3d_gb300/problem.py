@@ -54,6 +54,8 @@ class Problem:
         self.wl = None
         self.Ylam, self.Ymu = [], []
         self.free_top = 0
+        self.graves_qs = None     # dict(Qs=volume, freq=Hz): Graves Q attenuation
+        self.ablexp = None        # dict(Ex, Ey, Ez, blk (6, 7)): exponential sponge
         self.pml = [[None, None] for _ in range(3)]
         self.src = None
         self.recv = None
@@ -171,6 +173,17 @@ class Problem:
         s.dt, s.t0, s.nt_total = self.dt, self.t0, self.nt_total
         for n in ("x3d", "y3d", "z3d"):
             setattr(s, n, P(self.coords.get(n)))
+        if self.graves_qs is not None:
+            s.graves_qs = 1
+            s.qs_freq = float(self.graves_qs["freq"])
+            s.Qs = P(self.graves_qs["Qs"])
+        if self.ablexp is not None:
+            s.ablexp = 1
+            s.ablexp_Ex, s.ablexp_Ey, s.ablexp_Ez = [P(self.ablexp[k]) for k in ("Ex", "Ey", "Ez")]
+            blk = np.asarray(self.ablexp["blk"], np.int32).reshape(6, 7)
+            for n in range(6):
+                for m in range(7):
+                    s.ablexp_blk[n][m] = int(blk[n, m])
         s._keep = keep
         return s
 
@@ -216,6 +229,11 @@ def from_golden(path_or_npz):
         p.Ymu = [_f32(d["md.Ymu.%d" % m]) for m in range(p.nmaxwell)]
     free = d["bdry.is_sides_free"].reshape(3, 2)
     p.free_top = int(free[2, 1])
+    if "md.Qs" in d:
+        p.graves_qs = dict(Qs=_f32(d["md.Qs"]), freq=float(d["md.visco_Qs_freq"][0]))
+    if "bdry.ablexp_Ex" in d:
+        p.ablexp = dict(Ex=_f32(d["bdry.ablexp_Ex"]), Ey=_f32(d["bdry.ablexp_Ey"]),
+                        Ez=_f32(d["bdry.ablexp_Ez"]), blk=_i32(d["bdry.ablexp_blk"]))
     pml = d["bdry.is_sides_pml"].reshape(3, 2)
     expected = {"wav": d["out.wav.final"]}
     for dd in range(3):

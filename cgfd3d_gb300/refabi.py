@@ -265,6 +265,10 @@ def build_reference_structs(p):
         keep["Y"] = (yl, ym)
         md.Ylam = C.cast(yl, PPF)
         md.Ymu = C.cast(ym, PPF)
+    if p.graves_qs is not None:
+        md.visco_type = 1                     # CONST_VISCO_GRAVES_QS
+        md.visco_Qs_freq = float(p.graves_qs["freq"])
+        md.Qs = _fp(p.graves_qs["Qs"])
     src = Src()
     s = p.src
     if s is not None and s["n"] > 0:
@@ -301,6 +305,13 @@ def build_reference_structs(p):
             bd.nj2[d][sd], bd.nk1[d][sd], bd.nk2[d][sd] = b[3], b[4], b[5]
             bd.A[d][sd], bd.B[d][sd], bd.D[d][sd] = _fp(f["A"]), _fp(f["B"]), _fp(f["D"])
             bd.auxvar[d][sd].var = _fp(f["aux"])
+    if p.ablexp is not None:
+        bd.is_enable_ablexp = 1
+        bd.ablexp_Ex, bd.ablexp_Ey, bd.ablexp_Ez = [_fp(p.ablexp[k]) for k in ("Ex", "Ey", "Ez")]
+        blk = np.asarray(p.ablexp["blk"]).reshape(6, 7)
+        for n in range(6):
+            b = bd.bdry_blk[n]
+            b.enable, b.ni1, b.ni2, b.nj1, b.nj2, b.nk1, b.nk2 = [int(v) for v in blk[n]]
     wav = Wav()
     wav.v5d = _fp(p.wav)
     wav.ncmp, wav.nlevel = p.ncmp, p.nlevel

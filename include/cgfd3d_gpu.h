@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define CGFD_ABI_VERSION 3
+#define CGFD_ABI_VERSION 4
 
 /* medium types, same codes as forward/constants.h:24-29 */
 #define CGFD_MEDIUM_ELASTIC_ISO 2
@@ -134,6 +134,23 @@ typedef struct {
    * (forward/src_t.c:153-314) used by the traction image and vlow. */
   const int *src_force_rate_indx;
   const float *Fx_rate, *Fy_rate, *Fz_rate;
+
+  /* Graves Q attenuation of an elastic medium (visco_type graves_Qs,
+   * forward/sv_curv_col_el.c:638-666, applied at drv_rk_curv_col.c:414-416):
+   * after each step's last stage every component of every physical point is
+   * multiplied by expf(-PI * qs_freq * dt / Qs).  Qs: nx*ny*nz. */
+  int graves_qs;
+  float qs_freq;
+  const float *Qs;
+
+  /* exponential sponge (ablexp, forward/bdry_t.c:513-890, applied after each
+   * step at drv_rk_curv_col.c:484-486): every component of the points of the
+   * enabled blocks is multiplied by min(Ex[i], Ey[j], Ez[k]).
+   * ablexp_blk[n] = {enable, ni1, ni2, nj1, nj2, nk1, nk2} of
+   * bdry_t.bdry_blk[n]; Ex/Ey/Ez: nx, ny, nz floats. */
+  int ablexp;
+  const float *ablexp_Ex, *ablexp_Ey, *ablexp_Ez;
+  int ablexp_blk[6][7];
 } cgfd_problem_t;
 
 /* Opaque device-resident solver. */

@@ -35,6 +35,7 @@
 #define CGFD_REF_MAX_STRLEN 1024
 #define CGFD_REF_GD_TILE 4
 #define CGFD_REF_VISCO_GMB 2 /* CONST_VISCO_GMB, forward/constants.h:30 */
+#define CGFD_REF_VISCO_GRAVES_QS 1 /* CONST_VISCO_GRAVES_QS, forward/constants.h:29 */
 
 typedef struct {
   int total_len;

@@ -808,6 +808,41 @@ static void rhs_atten_plane(orc_t *o, const float *w, float *h, int k)
   }
 }
 
+/* Graves Q attenuation after the last stage's combine, physical points of
+ * one k-slab (forward/sv_curv_col_el.c:638-666) */
+static void graves_qs_slab(orc_t *o, float *w, long k0, long k1)
+{
+  const cgfd_problem_t *p = o->p;
+  float coef = -3.14159265358979323846 * p->qs_freq * p->dt;
+  for (int c = 0; c < p->ncmp; c++)
+    for (long k = k0; k < k1; k++)
+      for (int j = p->nj1; j <= p->nj2; j++)
+        for (int i = p->ni1; i <= p->ni2; i++) {
+          size_t q = (size_t)i + j * o->ln + (size_t)k * o->sl;
+          float qatt = expf(coef / p->Qs[q]);
+          w[c * o->vol + q] *= qatt;
+        }
+}
+
+/* exponential sponge after each step (forward/bdry_t.c:841-890): the
+ * points of the enabled blocks times min(Ex[i], Ey[j], Ez[k]) */
+static void ablexp_apply(orc_t *o, float *w)
+{
+  const cgfd_problem_t *p = o->p;
+  for (int c = 0; c < p->ncmp; c++)
+    for (int n = 0; n < 6; n++) {
+      const int *b = p->ablexp_blk[n];
+      if (b[0] != 1) continue;
+      for (int k = b[5]; k <= b[6]; k++)
+        for (int j = b[3]; j <= b[4]; j++)
+          for (int i = b[1]; i <= b[2]; i++) {
+            float mask = (p->ablexp_Ex[i] < p->ablexp_Ey[j]) ? p->ablexp_Ex[i] : p->ablexp_Ey[j];
+            if (mask > p->ablexp_Ez[k]) mask = p->ablexp_Ez[k];
+            w[c * o->vol + (size_t)i + j * o->ln + (size_t)k * o->sl] *= mask;
+          }
+    }
+}
+
 /* visco-elastic free surface after the last stage: rotate the surface
  * stress into the local frame, drop the traction components, rotate back
  * (forward/sv_curv_col_vis_iso.c:509-623) */
@@ -1162,6 +1197,10 @@ static void *worker(void *arg)
       } else {
         float cb = RK_B[is] * p->dt;
         for (long e = e0; e < e1; e++) end[e] += cb * rhs[e];
+        if (p->graves_qs) {      /* drv_rk_curv_col.c:414-416 */
+          pthread_barrier_wait(&o->bar);
+          graves_qs_slab(o, end, k0, k1);
+        }
         for (int d = 0; d < 3; d++)
           for (int s = 0; s < 2; s++) {
             if (!p->pml[d][s].enabled) continue;
@@ -1179,6 +1218,7 @@ static void *worker(void *arg)
       pthread_barrier_wait(&o->bar);
     }
     if (tid == 0) {
+      if (p->ablexp) ablexp_apply(o, end);      /* drv_rk_curv_col.c:484-486 */
       if (o->pg) pg_calcu(o, end, pre, o->pg, o->dis);
       keep_recv(o, end, it);
     }

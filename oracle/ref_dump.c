@@ -89,6 +89,7 @@ static void perturb(gd_t *gd, md_t *md, bdry_t *bdry, wav_t *wav, float amp_v)
     fields[nf++] = md->c11; fields[nf++] = md->c13; fields[nf++] = md->c33;
     fields[nf++] = md->c55; fields[nf++] = md->c66;
   }
+  if (md->visco_type == CONST_VISCO_GRAVES_QS) fields[nf++] = md->Qs;
   for (int f = 0; f < nf; f++)
     for (size_t p = 0; p < n; p++) fields[f][p] *= 1.0f + 0.1f * urand();
 
@@ -201,12 +202,29 @@ static void dump_inputs(fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md,
     }
   }
 
+  if (md->visco_type == CONST_VISCO_GRAVES_QS) {
+    put("md.Qs", 'f', md->Qs, n);
+    put_f("md.visco_Qs_freq", md->visco_Qs_freq);
+  }
+
   /* boundaries */
   put("bdry.is_sides_pml", 'i', bdry->is_sides_pml, 6);
   put("bdry.is_sides_free", 'i', bdry->is_sides_free, 6);
   put_i("bdry.is_enable_pml", bdry->is_enable_pml);
   put_i("bdry.is_enable_free", bdry->is_enable_free);
   put_i("bdry.is_enable_ablexp", bdry->is_enable_ablexp);
+  if (bdry->is_enable_ablexp == 1) {
+    int blk[6][7];
+    for (int b = 0; b < 6; b++) {
+      bdry_block_t *D = &bdry->bdry_blk[b];
+      int v[7] = {D->enable, D->ni1, D->ni2, D->nj1, D->nj2, D->nk1, D->nk2};
+      memcpy(blk[b], v, sizeof v);
+    }
+    put("bdry.ablexp_blk", 'i', blk, 42);
+    put("bdry.ablexp_Ex", 'f', bdry->ablexp_Ex, gd->nx);
+    put("bdry.ablexp_Ey", 'f', bdry->ablexp_Ey, gd->ny);
+    put("bdry.ablexp_Ez", 'f', bdry->ablexp_Ez, gd->nz);
+  }
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {
       if (bdry->is_sides_pml[d][s] != 1) continue;

@@ -122,6 +122,41 @@ CASES = {
         stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
         lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
     ),
+    # Graves Q attenuation (visco_config graves_Qs) of an elastic medium on
+    # the topography, Qs perturbed +-10 % around the reference's test value
+    "iso_topo_graves": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_iso",
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        visco=dict(type="graves_Qs", Qs_freq=2.0),
+        free=True, seed=4242, steps=9, dt=0.004,
+        src=dict(kind="moment", loc=(8.3, 7.6, 4.0), spatial="gauss",
+                 m=(1e16, 2e16, -1e16, 0.5e16, -0.3e16, 0.2e16), fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
+    # exponential sponge (ablexp) on five faces instead of CFS-PML, flat
+    # free surface, noise state
+    "iso_flat_ablexp": dict(
+        ni=24, nj=20, nk=16, dh=100.0, topo=False, medium="elastic_iso",
+        pml={}, ablexp=dict(x_left=5, x_right=6, y_front=4, y_back=5, z_bottom=6),
+        free=True, seed=99, steps=10, dt=0.005,
+        src=dict(kind="moment", loc=(12.0, 10.0, 6.0), spatial="gauss",
+                 m=(1e16, 1e16, 1e16, 0.0, 0.0, 0.0), fc=8.0, t0=0.05),
+        stations=[(4.0 + 2 * n, 10.0, 0.0, 1) for n in range(6)],
+        lines=[],
+    ),
+    # VTI medium on the topography with the sponge and Graves Q together
+    "vti_topo_ablexp_graves": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_vti",
+        pml={}, ablexp=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        visco=dict(type="graves_Qs", Qs_freq=1.5),
+        free=True, seed=8642, steps=9, dt=0.004,
+        src=dict(kind="force+moment", loc=(8.3, 7.6, 4.0), spatial="gauss",
+                 f=(1e15, -2e15, 3e15), m=(1e16, 2e16, -1e16, 0.5e16, -0.3e16, 0.2e16),
+                 fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
+        lines=[],
+    ),
     # no free surface: PML on all six faces (z2 face included), noise state
     "iso_box_pml6": dict(
         ni=16, nj=14, nk=12, dh=100.0, topo=False, medium="elastic_iso",
@@ -179,6 +214,8 @@ def write_par(path, c, work):
         par[faces[key]] = {"cfspml": {"number_of_layers": nlay,
                                       "alpha_max": 3.14, "beta_max": 2.0,
                                       "ref_vel": 6000.0}}
+    for key, nlay in c.get("ablexp", {}).items():
+        par[faces[key]] = {"ablexp": {"number_of_layers": nlay, "ref_vel": 6000.0}}
     if c["free"]:
         par["boundary_z_top"] = {"free": "timg"}
     if c["topo"]:

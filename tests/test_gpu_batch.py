@@ -124,3 +124,26 @@ def test_batch_rejects_mixed_media(base):
                           c55=shots[1].media["mu"], c66=shots[1].media["mu"])
     with pytest.raises(_lib.CgfdError):
         solver.Batch(shots)
+
+
+def test_batch_graves_q(base):
+    """Graves Q attenuation (the last stage's factor) in a batch equals the
+    single-shot runs; the exponential sponge is refused in batches."""
+    from cgfd3d_gb300 import _lib, solver
+    shots = _shots(base, 2, 9, 61)
+    rng = np.random.default_rng(3)
+    for p in shots:
+        p.graves_qs = dict(Qs=rng.uniform(15, 25, p.vol).astype(np.float32), freq=2.0)
+    singles = [p.copy() for p in shots]
+    with solver.Batch(shots) as b:
+        b.run(shots[0].nt_total)
+        b.fetch()
+    for p, q in zip(shots, singles):
+        solver.drv_rk_curv_col_allstep(q)
+        lev = p.final_level()
+        _same(p.level(lev), q.level(lev), "graves wavefield")
+    bad = _shots(base, 2, 3, 71)
+    bad[1].ablexp = dict(Ex=np.ones(bad[1].nx, np.float32), Ey=np.ones(bad[1].ny, np.float32),
+                         Ez=np.ones(bad[1].nz, np.float32), blk=np.zeros((6, 7), np.int32))
+    with pytest.raises(_lib.CgfdError):
+        solver.Batch(bad)
