@@ -181,6 +181,79 @@ def add_pml(p, X, Y, Z, nlay, faces, vref, alpha_max, beta_max=2.0):
 # media
 # ---------------------------------------------------------------------------
 
+def _abl_mask(i, vel, dt, nlay, dh):
+    """bdry_ablexp_cal_mask (forward/bdry_t.c:822-839) in float arithmetic."""
+    f32 = np.float32
+    length = f32(nlay) * f32(dh)
+    nstep = int(f32(f32(length / f32(vel)) / f32(dt)))
+    total = f32(0.0)
+    for n in range(nstep):
+        x = f32(f32(f32(n) * f32(dt)) * f32(vel)) / length
+        total = f32(total + x * x)
+    alpha = f32(0.6 / float(total))
+    r = f32(f32(i) / f32(nlay))
+    return f32(np.exp(f32(-alpha * (r * r))))
+
+
+def _abl_dh(X, Y, Z, box, axis):
+    """Mean grid spacing along `axis` over a block (bdry_cal_abl_len_dh,
+    forward/bdry_t.c:372-506): segment lengths in double, averaged."""
+    i1, i2, j1, j2, k1, k2 = box
+    sl = (slice(k1, k2 + 1), slice(j1, j2 + 1), slice(i1, i2 + 1))
+    x, y, z = [np.asarray(A, np.float64)[sl] for A in (X, Y, Z)]
+    ax = {0: 2, 1: 1, 2: 0}[axis]
+    d = np.sqrt(np.diff(x, axis=ax) ** 2 + np.diff(y, axis=ax) ** 2 + np.diff(z, axis=ax) ** 2)
+    return np.float32(d.sum() / d.size)
+
+
+def add_ablexp(p, layers, vel=6000.0, coords=None, dh=None):
+    """Exponential sponge on the faces in `layers` (x_left, x_right,
+    y_front, y_back, z_bottom, z_top -> number of layers), as
+    bdry_ablexp_set builds it (forward/bdry_t.c:513-820): six disjoint
+    blocks (x layers over the whole j, k range; y layers between them;
+    z layers inside both) and per-index masks, the outermost layer damped
+    most.  The grid spacing per block is the mean along the face normal of
+    the curvilinear grid `coords` = (X, Y, Z) (padded (nz, ny, nx)), or `dh`
+    for a Cartesian grid.  vel: reference velocity (scalar or per face)."""
+    names = ["x_left", "x_right", "y_front", "y_back", "z_bottom", "z_top"]
+    nl = {n: int(layers.get(n, 0)) for n in names}
+    v = {n: float(vel[n] if isinstance(vel, dict) else vel) for n in names}
+    Ex, Ey, Ez = (np.ones(m, np.float32) for m in (p.nx, p.ny, p.nz))
+    ix1, ix2 = p.ni1 + nl["x_left"], p.ni2 - nl["x_right"]
+    jy1, jy2 = p.nj1 + nl["y_front"], p.nj2 - nl["y_back"]
+    boxes = [(p.ni1, p.ni1 + nl["x_left"] - 1, p.nj1, p.nj2, p.nk1, p.nk2),
+             (p.ni2 - nl["x_right"] + 1, p.ni2, p.nj1, p.nj2, p.nk1, p.nk2),
+             (ix1, ix2, p.nj1, p.nj1 + nl["y_front"] - 1, p.nk1, p.nk2),
+             (ix1, ix2, p.nj2 - nl["y_back"] + 1, p.nj2, p.nk1, p.nk2),
+             (ix1, ix2, jy1, jy2, p.nk1, p.nk1 + nl["z_bottom"] - 1),
+             (ix1, ix2, jy1, jy2, p.nk2 - nl["z_top"] + 1, p.nk2)]
+    blk = np.zeros((6, 7), np.int32)
+    for n, name in enumerate(names):
+        b = boxes[n]
+        blk[n, 1:] = b
+        if b[1] < b[0] or b[3] < b[2] or b[5] < b[4] or nl[name] == 0:
+            continue
+        blk[n, 0] = 1
+        axis = n // 2
+        h = dh if coords is None else _abl_dh(*coords, b, axis)
+        lo, hi = b[2 * axis], b[2 * axis + 1]
+        cnt = hi - lo + 1
+        E = (Ex, Ey, Ez)[axis]
+        for a in range(lo, hi + 1):
+            depth = cnt - (a - lo) if n % 2 == 0 else a - lo + 1
+            E[a] = _abl_mask(depth, v[name], p.dt, cnt, h)
+    p.ablexp = dict(Ex=Ex, Ey=Ey, Ez=Ez, blk=blk)
+    return p
+
+
+def add_graves_qs(p, Qs, freq):
+    """Graves Q attenuation of an elastic medium (visco_config graves_Qs):
+    Qs per point (nx*ny*nz, or a scalar), reference frequency `freq`."""
+    q = np.broadcast_to(np.asarray(Qs, np.float32), (p.vol,)).copy()
+    p.graves_qs = dict(Qs=q, freq=float(freq))
+    return p
+
+
 def set_iso_media(p, vp, vs, rho):
     vp, vs, rho = [np.broadcast_to(np.asarray(a, np.float32), (p.nz, p.ny, p.nx))
                    for a in (vp, vs, rho)]
