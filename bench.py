@@ -41,12 +41,13 @@ UNIT = "pt-stage/s"
 # components (stage 0: pre r, tmp w, end w; stages 1-2: cur, pre, end r, tmp,
 # end w; stage 3: cur, end r, end w) plus the per-point coefficients (9
 # metrics + media), float32.  iso 36+12, vti 36+15, visco 108+18 floats.
-BYTES_PER_PT_STAGE = {"topo": 192, "flat": 192, "vti": 204, "visco": 504}
+BYTES_PER_PT_STAGE = {"topo": 192, "flat": 192, "vti": 204, "visco": 504, "aniso": 268}
 WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "slices": dict(ni=400, nj=400, nk=200),
              "locate": dict(ni=400, nj=400, nk=200),
              "batch": dict(ni=400, nj=400, nk=200),
              "vti": dict(ni=300, nj=300, nk=150),
+             "aniso": dict(ni=300, nj=300, nk=150),
              "visco": dict(ni=300, nj=300, nk=150),
              "flat": dict(ni=100, nj=100, nk=60)}
 SAMPLE_NK = 24                 # CPU sample: same model, 24 planes deep
@@ -189,7 +190,7 @@ def build_model(args, steps, nk=None):
     nk = nk or args.nk
     if args.workload == "flat":
         return models.flat_model(ni=args.ni, nj=args.nj, nk=nk, steps=steps)
-    if args.workload in ("vti", "visco"):
+    if args.workload in ("vti", "visco", "aniso"):
         return models.topo_media_model(args.workload, ni=args.ni, nj=args.nj,
                                        nk=nk, steps=steps, dt=0.005, nrecv=400)
     return models.topo_model(ni=args.ni, nj=args.nj, nk=nk, steps=steps,
@@ -203,6 +204,9 @@ def workload_name(args):
                    "CFS-PML 12, timg free surface, DC source, 400 receivers",
             "visco": "topography visco-elastic GMB 3 bodies %dx%dx%d (Qp 200, Qs "
                      "100), CFS-PML 12, timg free surface, DC source, 400 receivers",
+            "aniso": "topography tilted TI %dx%dx%d (21 constants; VTI of the vti "
+                     "workload tilted 30+-10 deg), CFS-PML 12, timg free surface, DC "
+                     "source, 400 receivers",
             "flat": "flat iso %dx%dx%d, CFS-PML 10, timg free surface, explosive "
                     "source, 20 receivers"}[
                 "topo" if args.workload == "slices" else args.workload] % (

@@ -6,9 +6,13 @@ tests/test_abi.py checks sizes and offsets against a compiled probe.
 
 import ctypes as C
 
-CGFD_ABI_VERSION = 4
+CGFD_ABI_VERSION = 5
 CGFD_MEDIUM_ELASTIC_ISO = 2
 CGFD_MEDIUM_ELASTIC_VTI = 3
+CGFD_MEDIUM_ELASTIC_ANISO = 4
+ANISO_NAMES = ["c11", "c12", "c13", "c14", "c15", "c16", "c22", "c23", "c24", "c25",
+               "c26", "c33", "c34", "c35", "c36", "c44", "c45", "c46", "c55", "c56", "c66"]
+ANISO_EXTRA = [n for n in ANISO_NAMES if n not in ("c11", "c13", "c33", "c55", "c66")]
 CGFD_MEDIUM_VISCOELASTIC_ISO = 5
 CGFD_MAX_MAXWELL = 8
 CGFD_SRC_POINT = 1
@@ -78,6 +82,7 @@ class Problem(C.Structure):
            ("ablexp", C.c_int),
            ("ablexp_Ex", PF), ("ablexp_Ey", PF), ("ablexp_Ez", PF),
            ("ablexp_blk", (C.c_int * 7) * 6)]
+        + [(n, PF) for n in ANISO_EXTRA]
     )
 
 

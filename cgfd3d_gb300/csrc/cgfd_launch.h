@@ -1,6 +1,6 @@
 /*
  * Launchers of the per-stage kernels, one set per medium.  Each medium's
- * kernels live in their own translation unit (cgfd_launch_{iso,vti,vis}.cu,
+ * kernels live in their own translation unit (cgfd_launch_{iso,vti,vis,ani}.cu,
  * all expanding cgfd_launch.cuh) so that the library's build compiles them
  * in parallel; cgfd_solver.cu only sees these declarations.
  */
@@ -32,6 +32,8 @@ void cgfd_launch_stage_vti(int code, int kind, dim3 grid, cudaStream_t st,
                            const StageArgs &a, const StageMaps &m);
 void cgfd_launch_stage_vis(int code, int kind, dim3 grid, cudaStream_t st,
                            const StageArgs &a, const StageMaps &m);
+void cgfd_launch_stage_ani(int code, int kind, dim3 grid, cudaStream_t st,
+                           const StageArgs &a, const StageMaps &m);
 
 /* the stage of a batch of shots in one launch of `nctas` CTAs (per-shot
  * arguments and tensor maps in device memory); isotropic and VTI media.
@@ -51,14 +53,18 @@ void cgfd_launch_pml_vti(int dim, int b, int kind, int f, long long n,
                          cudaStream_t st, const StageArgs &a);
 void cgfd_launch_pml_vis(int dim, int b, int kind, int f, long long n,
                          cudaStream_t st, const StageArgs &a);
+void cgfd_launch_pml_ani(int dim, int b, int kind, int f, long long n,
+                         cudaStream_t st, const StageArgs &a);
 
 /* tile rows (consumer warps) and dynamic shared memory of each medium's
  * stage kernel */
 int cgfd_stage_rows_iso(void);
 int cgfd_stage_rows_vti(void);
 int cgfd_stage_rows_vis(void);
+int cgfd_stage_rows_ani(void);
 int cgfd_stage_smem_iso(void);
 int cgfd_stage_smem_vti(void);
 int cgfd_stage_smem_vis(void);
+int cgfd_stage_smem_ani(void);
 
 #endif

@@ -6,11 +6,14 @@
  * MED_VIS  GMB visco-elastic isotropic: the isotropic elastic operators
  *          plus 6 memory variables per Maxwell body
  *          (forward/sv_curv_col_vis_iso.c)
+ * MED_ANI  fully anisotropic elastic, 21 constants
+ *          (forward/sv_curv_col_el_aniso.c)
  *
  * Device media block (one padded volume per component, stride g.vol):
  *   iso  slw, lambda, mu
  *   vti  slw, c11, c13, c33, c55, c66
  *   vis  slw, lambda, mu, Ylam[0..nmw-1], Ymu[0..nmw-1]
+ *   ani  slw, c11, c12, .., c16, c22, .., c26, c33, .., c66 (21)
  * slw is 1/rho, as the reference holds it (forward/md_t.c:601-623).
  */
 #ifndef CGFD_MEDIA_CUH
@@ -18,12 +21,12 @@
 
 #include "cgfd_common.h"
 
-enum { MED_ISO = 0, MED_VTI = 1, MED_VIS = 2 };
+enum { MED_ISO = 0, MED_VTI = 1, MED_VIS = 2, MED_ANI = 3 };
 
 /* media components of the device block for a medium */
 __host__ __device__ constexpr int med_ncomp(int med, int nmw)
 {
-  return med == MED_VTI ? 6 : (med == MED_VIS ? 3 + 2 * nmw : 3);
+  return med == MED_VTI ? 6 : med == MED_VIS ? 3 + 2 * nmw : med == MED_ANI ? 22 : 3;
 }
 
 /* elastic constants of one point */
@@ -31,7 +34,37 @@ struct MedPt {
   float slw;
   float lam, mu, l2m;                    /* iso, vis */
   float c11, c12, c13, c33, c55, c66;    /* vti */
+  float c[21];                           /* ani: c11 c12 .. c16 c22 .. c66 */
 };
+
+/* C_IJ (Voigt indices 1..6, compile-time) of the packed anisotropic set */
+template <int I, int J>
+__device__ __forceinline__ float cij(const MedPt &m)
+{
+  constexpr int a = I < J ? I : J, b = I < J ? J : I;
+  constexpr int off = a == 1 ? 0 : a == 2 ? 6 : a == 3 ? 11 : a == 4 ? 15 : a == 5 ? 18 : 20;
+  return m.c[off + b - a];
+}
+
+/* anisotropic stress rates from the six strain-rate sums: exx, eyy, ezz
+ * and the engineering shears gyz, gxz, gxy (rows Txx Tyy Tzz Tyz Txz Txy =
+ * Voigt 1..6); algebraically the reference's expanded expression,
+ * forward/sv_curv_col_el_aniso.c:453-470 */
+__device__ __forceinline__ void ani_hooke(const MedPt &m, float exx, float eyy,
+                                          float ezz, float gyz, float gxz,
+                                          float gxy, float *r)
+{
+#define ANI_ROW(R)                                                              \
+  (cij<R, 1>(m) * exx + cij<R, 2>(m) * eyy + cij<R, 3>(m) * ezz +              \
+   cij<R, 4>(m) * gyz + cij<R, 5>(m) * gxz + cij<R, 6>(m) * gxy)
+  r[C_TXX] = ANI_ROW(1);
+  r[C_TYY] = ANI_ROW(2);
+  r[C_TZZ] = ANI_ROW(3);
+  r[C_TYZ] = ANI_ROW(4);
+  r[C_TXZ] = ANI_ROW(5);
+  r[C_TXY] = ANI_ROW(6);
+#undef ANI_ROW
+}
 
 /* constants at p (component stride s); c12 = c11 - 2 c66
  * (forward/sv_curv_col_el_vti.c:351) */
@@ -41,7 +74,12 @@ __device__ __forceinline__ MedPt med_from(const float *p, long long s)
   MedPt m;
   auto ld = [&](long long o) { return GLOBAL ? __ldg(p + o) : p[o]; };
   m.slw = ld(0);
-  if (MED == MED_VTI) {
+  if (MED == MED_ANI) {
+#pragma unroll
+    for (int n = 0; n < 21; n++) m.c[n] = ld((n + 1) * s);
+    m.lam = m.mu = m.l2m = 0.f;
+    m.c11 = m.c12 = m.c13 = m.c33 = m.c55 = m.c66 = 0.f;
+  } else if (MED == MED_VTI) {
     m.c11 = ld(s); m.c13 = ld(2 * s); m.c33 = ld(3 * s);
     m.c55 = ld(4 * s); m.c66 = ld(5 * s);
     m.c12 = m.c11 - 2.0f * m.c66;
@@ -65,7 +103,18 @@ __device__ __forceinline__ void hooke9(const MedPt &m, float xix, float xiy,
                                        float DyVz, float DzVx, float DzVy,
                                        float DzVz, float *r)
 {
-  if (MED != MED_VTI) {
+  if (MED == MED_ANI) {
+    const float exx = xix * DxVx + etx * DyVx + ztx * DzVx;
+    const float eyy = xiy * DxVy + ety * DyVy + zty * DzVy;
+    const float ezz = xiz * DxVz + etz * DyVz + ztz * DzVz;
+    const float gyz = xiz * DxVy + xiy * DxVz + etz * DyVy + ety * DyVz +
+                      ztz * DzVy + zty * DzVz;
+    const float gxz = xiz * DxVx + xix * DxVz + etz * DyVx + etx * DyVz +
+                      ztz * DzVx + ztx * DzVz;
+    const float gxy = xiy * DxVx + xix * DxVy + ety * DyVx + etx * DyVy +
+                      zty * DzVx + ztx * DzVy;
+    ani_hooke(m, exx, eyy, ezz, gyz, gxz, gxy, r);
+  } else if (MED != MED_VTI) {
     const float lam = m.lam, mu = m.mu, l2m = m.l2m;
     r[C_TXX] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
                lam * (xiy * DxVy + ety * DyVy + zty * DzVy + xiz * DxVz +
@@ -109,7 +158,10 @@ __device__ __forceinline__ void hooke1(const MedPt &m, float e1, float e2,
                                        float e3, float DVx, float DVy,
                                        float DVz, float *s)
 {
-  if (MED != MED_VTI) {
+  if (MED == MED_ANI) {
+    ani_hooke(m, e1 * DVx, e2 * DVy, e3 * DVz, e3 * DVy + e2 * DVz,
+              e3 * DVx + e1 * DVz, e2 * DVx + e1 * DVy, s);
+  } else if (MED != MED_VTI) {
     const float lam = m.lam, mu = m.mu, l2m = m.l2m;
     s[C_TXX] = l2m * e1 * DVx + lam * e2 * DVy + lam * e3 * DVz;
     s[C_TYY] = lam * e1 * DVx + l2m * e2 * DVy + lam * e3 * DVz;

@@ -263,6 +263,57 @@ __global__ void k_dvh2dvz_vti(DevGrid g, const float *__restrict__ M,
     }
 }
 
+/* anisotropic free-surface matrices (forward/sv_curv_col_el_aniso.c:
+ * 1267-1423): matVx2Vz = -A^-1 B, matVy2Vz = -A^-1 C with
+ * K(a, b)[r][c] = sum over n, m of C(V(r,n), V(c,m)) b_m a_n, the traction
+ * on the plane of normal a from the gradient along b (A = K(zt, zt),
+ * B = K(zt, xi), C = K(zt, et)) */
+__global__ void k_dvh2dvz_ani(DevGrid g, const float *__restrict__ M,
+                              const float *__restrict__ med, float *mVx, float *mVy)
+{
+  int i = g.ni1 + blockIdx.x * blockDim.x + threadIdx.x;
+  int j = g.nj1 + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i > g.ni2 || j > g.nj2) return;
+  long long q = (i + g.xoff) + (long long)j * g.px + (long long)g.nk2 * g.sl;
+  const long long v = g.vol;
+  float xi[3] = {M[v + q], M[2 * v + q], M[3 * v + q]};
+  float et[3] = {M[4 * v + q], M[5 * v + q], M[6 * v + q]};
+  float zt[3] = {M[7 * v + q], M[8 * v + q], M[9 * v + q]};
+  float c[21];
+  for (int n = 0; n < 21; n++) c[n] = med[(n + 1) * v + q];
+  const int vg[3][3] = {{1, 6, 5}, {6, 2, 4}, {5, 4, 3}};
+  const int off[7] = {0, 0, 6, 11, 15, 18, 20};
+  auto C = [&](int I, int J) {
+    int a = I < J ? I : J, b = I < J ? J : I;
+    return c[off[a] + b - a];
+  };
+  auto K = [&](const float *a, const float *b, float out[3][3]) {
+    for (int r = 0; r < 3; r++)
+      for (int cc = 0; cc < 3; cc++) {
+        float s = 0.f;
+        for (int n = 0; n < 3; n++)
+          for (int m = 0; m < 3; m++) s += C(vg[r][n], vg[cc][m]) * b[m] * a[n];
+        out[r][cc] = s;
+      }
+  };
+  float A[3][3], B[3][3], Cm[3][3];
+  K(zt, zt, A);
+  K(zt, xi, B);
+  K(zt, et, Cm);
+  inv3_dev(A);
+  long long ij = (i + (long long)j * g.nx) * 9;
+  for (int r = 0; r < 3; r++)
+    for (int cc = 0; cc < 3; cc++) {
+      float ab = 0.f, ac = 0.f;
+      for (int k = 0; k < 3; k++) {
+        ab += A[r][k] * B[k][cc];
+        ac += A[r][k] * Cm[k][cc];
+      }
+      mVx[ij + r * 3 + cc] = -ab;
+      mVy[ij + r * 3 + cc] = -ac;
+    }
+}
+
 /* visco-elastic free-surface matrices (forward/sv_curv_col_vis_iso.c:
  * 416-503): the isotropic A^-1 B, A^-1 C and the rotation matrix D of the
  * local surface frame (rows: the in-plane direction normal to the eta
@@ -775,7 +826,7 @@ struct cgfd_solver {
   const cgfd_problem_t *p;
   DevGrid g;
   cudaStream_t stream;
-  int med;                      /* MED_ISO / MED_VTI / MED_VIS */
+  int med;                      /* MED_ISO / MED_VTI / MED_VIS / MED_ANI */
   int ncmp;                     /* wavefield components per level */
   int nmed;                     /* media components */
   float *wav;                   /* 4 levels x ncmp x vol */
@@ -829,7 +880,8 @@ static size_t level_floats(const cgfd_solver_t *s) { return (size_t)s->ncmp * s-
 
 static int medium_of(int medium_type)
 {
-  return medium_type == CGFD_MEDIUM_ELASTIC_VTI ? MED_VTI
+  return medium_type == CGFD_MEDIUM_ELASTIC_ANISO ? MED_ANI
+       : medium_type == CGFD_MEDIUM_ELASTIC_VTI ? MED_VTI
        : medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO ? MED_VIS : MED_ISO;
 }
 
@@ -859,9 +911,17 @@ static int validate(const cgfd_problem_t *p)
 {
   if (p->medium_type != CGFD_MEDIUM_ELASTIC_ISO &&
       p->medium_type != CGFD_MEDIUM_ELASTIC_VTI &&
+      p->medium_type != CGFD_MEDIUM_ELASTIC_ANISO &&
       p->medium_type != CGFD_MEDIUM_VISCOELASTIC_ISO)
     return set_err(CGFD_EINVAL, "medium_type %d not supported (elastic_iso 2, "
-                   "elastic_vti 3, viscoelastic_iso 5)", p->medium_type);
+                   "elastic_vti 3, elastic_aniso 4, viscoelastic_iso 5)", p->medium_type);
+  if (p->medium_type == CGFD_MEDIUM_ELASTIC_ANISO) {
+    const float *c[21] = {p->c11, p->c12, p->c13, p->c14, p->c15, p->c16, p->c22,
+                          p->c23, p->c24, p->c25, p->c26, p->c33, p->c34, p->c35,
+                          p->c36, p->c44, p->c45, p->c46, p->c55, p->c56, p->c66};
+    for (int n = 0; n < 21; n++)
+      if (!c[n]) return set_err(CGFD_EINVAL, "anisotropic medium: constant %d missing", n);
+  }
   int ncmp_want = 9;
   if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO) {
     if (p->nmaxwell < 1 || p->nmaxwell > CGFD_VIS_NMW_MAX)
@@ -908,7 +968,8 @@ static int validate(const cgfd_problem_t *p)
   } else if (!p->x3d || !p->y3d || !p->z3d) {
     return set_err(CGFD_EINVAL, "neither metrics nor grid coordinates given");
   }
-  if (p->medium_type != CGFD_MEDIUM_ELASTIC_VTI && (!p->lambda || !p->mu))
+  if (p->medium_type != CGFD_MEDIUM_ELASTIC_VTI &&
+      p->medium_type != CGFD_MEDIUM_ELASTIC_ANISO && (!p->lambda || !p->mu))
     return set_err(CGFD_EINVAL, "missing lambda/mu");
   for (int d = 0; d < 3; d++)
     for (int s = 0; s < 2; s++) {
@@ -1189,7 +1250,8 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   s->ncmp = p->ncmp;
   s->nmed = med_ncomp(s->med, s->med == MED_VIS ? p->nmaxwell : 0);
   s->ty = s->med == MED_VTI ? cgfd_stage_rows_vti()
-        : s->med == MED_VIS ? cgfd_stage_rows_vis() : cgfd_stage_rows_iso();
+        : s->med == MED_VIS ? cgfd_stage_rows_vis()
+        : s->med == MED_ANI ? cgfd_stage_rows_ani() : cgfd_stage_rows_iso();
   DevGrid &g = s->g;
   g.ni = p->ni; g.nj = p->nj; g.nk = p->nk;
   g.nx = p->nx; g.ny = p->ny; g.nz = p->nz;
@@ -1239,10 +1301,15 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
   TRY(dalloc(s, &s->media, (size_t)s->nmed * vol));
   TRYC(cudaMemsetAsync(s->media, 0, (size_t)s->nmed * vol * sizeof(float), st));
   {
-    const float *md[3 + 2 * CGFD_VIS_NMW_MAX];
+    const float *md[22 + 2 * CGFD_VIS_NMW_MAX];
     int nm = 0;
     md[nm++] = p->slw;
-    if (s->med == MED_VTI) {
+    if (s->med == MED_ANI) {
+      const float *c[21] = {p->c11, p->c12, p->c13, p->c14, p->c15, p->c16, p->c22,
+                            p->c23, p->c24, p->c25, p->c26, p->c33, p->c34, p->c35,
+                            p->c36, p->c44, p->c45, p->c46, p->c55, p->c56, p->c66};
+      for (int n = 0; n < 21; n++) md[nm++] = c[n];
+    } else if (s->med == MED_VTI) {
       md[nm++] = p->c11; md[nm++] = p->c13; md[nm++] = p->c33;
       md[nm++] = p->c55; md[nm++] = p->c66;
     } else {
@@ -1343,6 +1410,8 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
                                       s->mats, s->mats + n2, s->mats + 2 * n2);
     } else if (s->med == MED_VTI) {
       k_dvh2dvz_vti<<<gr, b, 0, st>>>(g, M, s->media, s->mats, s->mats + n2);
+    } else if (s->med == MED_ANI) {
+      k_dvh2dvz_ani<<<gr, b, 0, st>>>(g, M, s->media, s->mats, s->mats + n2);
     } else {
       /* the surface plane of the grid coordinates (rows j-3..j+3 are read) */
       size_t s2n = (size_t)g.nx * g.ny;
@@ -1559,6 +1628,7 @@ static void launch_stage(cgfd_solver_t *s, int code, int kind, cudaStream_t st,
           (s->g.nk + s->kchunk - 1) / s->kchunk);
   if (s->med == MED_VTI) cgfd_launch_stage_vti(code, kind, gr, st, a, s->maps);
   else if (s->med == MED_VIS) cgfd_launch_stage_vis(code, kind, gr, st, a, s->maps);
+  else if (s->med == MED_ANI) cgfd_launch_stage_ani(code, kind, gr, st, a, s->maps);
   else cgfd_launch_stage_iso(code, kind, gr, st, a, s->maps);
 }
 
@@ -1572,6 +1642,7 @@ static void launch_pml_faces(cgfd_solver_t *s, int kind, int bx, int by, int bz,
     int dim = F.dim, b = dim == 0 ? bx : (dim == 1 ? by : bz);
     if (s->med == MED_VTI) cgfd_launch_pml_vti(dim, b, kind, f, F.avol, st, a);
     else if (s->med == MED_VIS) cgfd_launch_pml_vis(dim, b, kind, f, F.avol, st, a);
+    else if (s->med == MED_ANI) cgfd_launch_pml_ani(dim, b, kind, f, F.avol, st, a);
     else cgfd_launch_pml_iso(dim, b, kind, f, F.avol, st, a);
   }
 }
@@ -2345,8 +2416,9 @@ extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
     if (!p) return set_err(CGFD_EINVAL, "shot %d: null problem", k);
     if (p->medium_type != shots[0]->medium_type)
       return set_err(CGFD_EINVAL, "shot %d: every shot of a batch has the same medium", k);
-    if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO)
-      return set_err(CGFD_EINVAL, "batched shots: elastic media (iso, VTI) only");
+    if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO ||
+        p->medium_type == CGFD_MEDIUM_ELASTIC_ANISO)
+      return set_err(CGFD_EINVAL, "batched shots: isotropic and VTI elastic media only");
     if (p->src_n > 0 && p->src_n_surface_force > 0)
       return set_err(CGFD_EINVAL, "shot %d: surface force sources are not batched", k);
     if (p->ablexp)

@@ -66,7 +66,8 @@ constexpr int PTS = TX * TY;
 template <int MED>
 struct Slot {
   static constexpr int NMED = MED == MED_VTI ? 6
-                            : (MED == MED_VIS ? 3 + 2 * CGFD_VIS_NMW_MAX : 3);
+                            : MED == MED_VIS ? 3 + 2 * CGFD_VIS_NMW_MAX
+                            : MED == MED_ANI ? 22 : 3;
   static constexpr int NJ = MED == MED_VIS ? 6 * CGFD_VIS_NMW_MAX : 0;
   static constexpr int S_MET = 0;
   static constexpr int S_MED = 9 * PTS;
@@ -443,7 +444,7 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
                    LDG(Bm + 3) * DyVx + LDG(Bm + 4) * DyVy + LDG(Bm + 5) * DyVz;
             DzVz = LDG(A + 6) * DxVx + LDG(A + 7) * DxVy + LDG(A + 8) * DxVz +
                    LDG(Bm + 6) * DyVx + LDG(Bm + 7) * DyVy + LDG(Bm + 8) * DyVz;
-            if (MED != MED_VTI && a.VS) {
+            if (MED != MED_VTI && MED != MED_ANI && a.VS) {
               /* surface force: matF2Vz (VxSrc, VySrc, VzSrc)
                * (forward/sv_curv_col_el_iso.c:583-592) */
               const long long n2 = (long long)g.nx * g.ny, i2 = i + (long long)j * g.nx;

@@ -28,7 +28,7 @@
  *
  * Errors print the library's message and call MPI_Abort when MPI is linked
  * (exit(1) otherwise), as the reference does.  Unsupported configurations
- * (dd sources, full anisotropy)
+ * (dd sources)
  * are reported the same way instead of being ignored.
  */
 #include <stdio.h>
@@ -174,6 +174,7 @@ void drv_rk_curv_col_allstep(
     unsupported("an operator set other than MacCormack DRP with RK4");
   if (md->medium_type != CGFD_MEDIUM_ELASTIC_ISO &&
       md->medium_type != CGFD_MEDIUM_ELASTIC_VTI &&
+      md->medium_type != CGFD_MEDIUM_ELASTIC_ANISO &&
       md->medium_type != CGFD_MEDIUM_VISCOELASTIC_ISO)
     unsupported("this medium type");
   if (md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO &&
@@ -197,6 +198,12 @@ void drv_rk_curv_col_allstep(
   p.mu = md->mu;
   p.c11 = md->c11; p.c13 = md->c13; p.c33 = md->c33;
   p.c55 = md->c55; p.c66 = md->c66;
+  if (md->medium_type == CGFD_MEDIUM_ELASTIC_ANISO) {
+    p.c12 = md->c12; p.c14 = md->c14; p.c15 = md->c15; p.c16 = md->c16;
+    p.c22 = md->c22; p.c23 = md->c23; p.c24 = md->c24; p.c25 = md->c25;
+    p.c26 = md->c26; p.c34 = md->c34; p.c35 = md->c35; p.c36 = md->c36;
+    p.c44 = md->c44; p.c45 = md->c45; p.c46 = md->c46; p.c56 = md->c56;
+  }
   if (md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO) {
     if (md->nmaxwell > CGFD_MAX_MAXWELL) unsupported("more than 8 Maxwell bodies");
     p.nmaxwell = md->nmaxwell;

@@ -463,6 +463,56 @@ def thomsen_to_vti(vp, vs, rho, eps, delta, gamma):
             for c in (c11, c13, c33, c55, c66)]
 
 
+def bond_matrix(R):
+    """6x6 Bond transformation of a stiffness in Voigt order (xx, yy, zz, yz,
+    xz, xy) for the rotation R (..., 3, 3): C' = M C M^T (Auld)."""
+    a = np.asarray(R, np.float64)
+    M = np.empty(a.shape[:-2] + (6, 6))
+    pairs = [(1, 2), (2, 0), (0, 1)]          # columns 4, 5, 6: yz, zx, xy
+    for r in range(3):
+        for c in range(3):
+            M[..., r, c] = a[..., r, c] ** 2
+        for n, (u, v) in enumerate(pairs):
+            M[..., r, 3 + n] = 2.0 * a[..., r, u] * a[..., r, v]
+    rows = [(1, 2), (2, 0), (0, 1)]           # rows 4, 5, 6
+    for n, (u, v) in enumerate(rows):
+        for c in range(3):
+            M[..., 3 + n, c] = a[..., u, c] * a[..., v, c]
+        for m, (s_, t) in enumerate(pairs):
+            M[..., 3 + n, 3 + m] = a[..., u, s_] * a[..., v, t] + a[..., u, t] * a[..., v, s_]
+    return M
+
+
+def tti_stiffness(c11, c13, c33, c55, c66, tilt, azimuth):
+    """The 21 constants of a tilted transversely isotropic medium: the VTI
+    stiffness (c12 = c11 - 2 c66) with its symmetry axis rotated by `tilt`
+    from the vertical towards azimuth `azimuth` (radians, per point or
+    scalar).  Returns a dict c11..c66 of float32 arrays."""
+    c11, c13, c33, c55, c66 = [np.asarray(v, np.float64) for v in (c11, c13, c33, c55, c66)]
+    n = c11.size
+    C = np.zeros((n, 6, 6))
+    C[:, 0, 0] = C[:, 1, 1] = c11
+    C[:, 2, 2] = c33
+    C[:, 0, 1] = C[:, 1, 0] = c11 - 2.0 * c66
+    C[:, 0, 2] = C[:, 2, 0] = C[:, 1, 2] = C[:, 2, 1] = c13
+    C[:, 3, 3] = C[:, 4, 4] = c55
+    C[:, 5, 5] = c66
+    th = np.broadcast_to(np.asarray(tilt, np.float64), (n,))
+    ph = np.broadcast_to(np.asarray(azimuth, np.float64), (n,))
+    ct, st, cp, sp = np.cos(th), np.sin(th), np.cos(ph), np.sin(ph)
+    R = np.zeros((n, 3, 3))                   # Rz(azimuth) @ Ry(tilt)
+    R[:, 0, 0], R[:, 0, 1], R[:, 0, 2] = cp * ct, -sp, cp * st
+    R[:, 1, 0], R[:, 1, 1], R[:, 1, 2] = sp * ct, cp, sp * st
+    R[:, 2, 0], R[:, 2, 1], R[:, 2, 2] = -st, 0.0, ct
+    M = bond_matrix(R)
+    Cr = np.einsum("nij,njk,nlk->nil", M, C, M)
+    out = {}
+    for I in range(6):
+        for J in range(I, 6):
+            out["c%d%d" % (I + 1, J + 1)] = np.ascontiguousarray(Cr[:, I, J].astype(np.float32))
+    return out
+
+
 def gmb_coefficients(Qp, Qs, nmaxwell, fmin, fmax, fr):
     """GMB relaxation frequencies and weights for constant Qp, Qs, and the
     relaxed-to-unrelaxed modulus factors, restating the least-squares fit of
@@ -493,13 +543,15 @@ def gmb_coefficients(Qp, Qs, nmaxwell, fmin, fmax, fr):
 
 def topo_media_model(kind, ni=300, nj=300, nk=150, steps=1500, dt=None,
                      npml=12, seed=2025, nrecv=400, nmaxwell=3):
-    """The topography model with a VTI (kind "vti") or GMB visco-elastic
-    (kind "visco") medium.
+    """The topography model with a VTI (kind "vti"), tilted TI (kind
+    "aniso", all 21 constants) or GMB visco-elastic (kind "visco") medium.
 
     vti:   the three layers perturbed by 5 % with a seeded Gaussian random
            field of 2 km correlation; Thomsen epsilon, delta ~ U[0, 0.2] and
            gamma ~ U[0, 0.1] per point (independent seeded fields mapped
            through the normal CDF); converted to c11, c13, c33, c55, c66.
+    aniso: the vti medium with its symmetry axis tilted 30 degrees +- 10
+           (seeded Gaussian random field) towards azimuth 40 degrees.
     visco: the three layers, Qp = 200, Qs = 100, `nmaxwell` Maxwell bodies
            fitted over 0.5-5 Hz with reference frequency 1.58 Hz.
     """
@@ -511,7 +563,7 @@ def topo_media_model(kind, ni=300, nj=300, nk=150, steps=1500, dt=None,
     vs = np.sqrt(mu / rho)
     vp = np.sqrt((lam + 2 * mu) / rho)
     shape = (p.nz, p.ny, p.nx)
-    if kind == "vti":
+    if kind in ("vti", "aniso"):
         pert = 1.0 + 0.05 * gaussian_field_3d(shape, 100.0, 2000.0, seed + 1).ravel()
         vp, vs, rho = vp * pert, vs * pert, rho * pert
         u = [normal_cdf(gaussian_field_3d(shape, 100.0, 2000.0, seed + s).ravel())
@@ -521,6 +573,12 @@ def topo_media_model(kind, ni=300, nj=300, nk=150, steps=1500, dt=None,
         p.medium_type = abi.CGFD_MEDIUM_ELASTIC_VTI
         p.media = {"slw": np.ascontiguousarray((1.0 / rho).astype(np.float32)),
                    "c11": c11, "c13": c13, "c33": c33, "c55": c55, "c66": c66}
+        if kind == "aniso":
+            tilt = np.radians(30.0 + 10.0 * gaussian_field_3d(shape, 100.0, 2000.0,
+                                                              seed + 5).ravel())
+            p.medium_type = abi.CGFD_MEDIUM_ELASTIC_ANISO
+            p.media = dict(slw=p.media["slw"],
+                           **tti_stiffness(c11, c13, c33, c55, c66, tilt, np.radians(40.0)))
     elif kind == "visco":
         wl, YP, YS, fac_p, fac_s = gmb_coefficients(200.0, 100.0, nmaxwell,
                                                     0.5, 5.0, 1.58)

@@ -115,7 +115,7 @@ class Problem:
         s.slw = P(self.media.get("slw"))
         s.lambda_ = P(self.media.get("lambda"))
         s.mu = P(self.media.get("mu"))
-        for n in ("c11", "c13", "c33", "c55", "c66"):
+        for n in abi.ANISO_NAMES:
             setattr(s, n, P(self.media.get(n)))
         s.nmaxwell = self.nmaxwell
         s.wl = P(self.wl)
@@ -219,7 +219,7 @@ def from_golden(path_or_npz):
             p.coords[n] = _f32(d["gd." + n])
     p.medium_type = int(d["md.medium_type"][0])
     p.media["slw"] = _f32(d["md.slw"])
-    for n in ("lambda", "mu", "c11", "c13", "c33", "c55", "c66"):
+    for n in ["lambda", "mu"] + abi.ANISO_NAMES:
         if "md." + n in d:
             p.media[n] = _f32(d["md." + n])
     if "md.nmaxwell" in d:

@@ -12,6 +12,8 @@ import ctypes as C
 
 import numpy as np
 
+from . import abi
+
 PF = C.POINTER(C.c_float)
 PPF = C.POINTER(PF)
 PI = C.POINTER(C.c_int)
@@ -253,7 +255,7 @@ def build_reference_structs(p):
     if "lambda" in p.media:
         md.lambda_ = _fp(p.media["lambda"])
         md.mu = _fp(p.media["mu"])
-    for n in ("c11", "c13", "c33", "c55", "c66"):
+    for n in abi.ANISO_NAMES:
         if n in p.media:
             setattr(md, n, _fp(p.media[n]))
     if p.nmaxwell > 0:

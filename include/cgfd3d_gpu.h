@@ -33,11 +33,12 @@
 extern "C" {
 #endif
 
-#define CGFD_ABI_VERSION 4
+#define CGFD_ABI_VERSION 5
 
 /* medium types, same codes as forward/constants.h:24-29 */
 #define CGFD_MEDIUM_ELASTIC_ISO 2
 #define CGFD_MEDIUM_ELASTIC_VTI 3
+#define CGFD_MEDIUM_ELASTIC_ANISO 4
 #define CGFD_MEDIUM_VISCOELASTIC_ISO 5
 #define CGFD_MAX_MAXWELL 8
 
@@ -151,6 +152,12 @@ typedef struct {
   int ablexp;
   const float *ablexp_Ex, *ablexp_Ey, *ablexp_Ez;
   int ablexp_blk[6][7];
+
+  /* fully anisotropic elastic medium (medium_type 4, md_t c11..c66,
+   * forward/md_t.h): the 16 constants below together with c11, c13, c33,
+   * c55, c66 above, nx*ny*nz each (forward/sv_curv_col_el_aniso.c) */
+  const float *c12, *c14, *c15, *c16, *c22, *c23, *c24, *c25, *c26;
+  const float *c34, *c35, *c36, *c44, *c45, *c46, *c56;
 } cgfd_problem_t;
 
 /* Opaque device-resident solver. */

@@ -7,7 +7,7 @@
  *
  * It restates, for the flat problem description of include/cgfd3d_gpu.h,
  * what the reference's drv_rk_curv_col_allstep does for isotropic elastic,
- * VTI elastic and GMB visco-elastic isotropic media (the float arithmetic
+ * VTI elastic, fully anisotropic elastic and GMB visco-elastic isotropic media (the float arithmetic
  * is ordered as in the reference so that the results are bit-identical to
  * the reference's own CPU build, which is checked against the golden
  * fixtures under tests/golden/):
@@ -31,6 +31,9 @@
  *   VTI media            forward/sv_curv_col_el_vti.c:200-397 (interior),
  *                        :407-590 (vlow), :592-1075 (CFS-PML),
  *                        :1085-1206 (free-surface matrices)
+ *   anisotropic media    forward/sv_curv_col_el_aniso.c:234-503 (interior),
+ *                        :507-716 (vlow), :718-1265 (CFS-PML),
+ *                        :1267-1423 (free-surface matrices)
  *   GMB visco-elastic    forward/sv_curv_col_vis_iso.c:22-245 (stage order),
  *                        :250-347 (attenuation), :353-507 (free-surface
  *                        matrices), :509-623 (surface stress rotation, after
@@ -140,14 +143,50 @@ static inline float lam2mu_of(float lam, float mu)
  * c12 = c11 - 2 c66 evaluated in double as the reference's `2.0 *` does,
  * c13, c33, c55, c66; forward/sv_curv_col_el_vti.c:345-351) */
 typedef struct {
-  int vti;
+  int vti, aniso;
   float lam, mu, l2m;
   float c11, c12, c13, c33, c55, c66;
+  float c[21];      /* anisotropic: c11 c12 .. c16 c22 .. c26 c33 .. c66 */
 } med_t;
+
+/* C_IJ (Voigt indices 1..6) of the packed anisotropic constants */
+static inline float cij(const med_t *m, int I, int J)
+{
+  static const int off[7] = {0, 0, 6, 11, 15, 18, 20};
+  if (I > J) { int t = I; I = J; J = t; }
+  return m->c[off[I] + J - I];
+}
+
+/* Voigt index of the strain component (a, b), a, b in x, y, z = 0, 1, 2 */
+static inline int voigt(int a, int b)
+{
+  static const int v[3][3] = {{1, 6, 5}, {6, 2, 4}, {5, 4, 3}};
+  return v[a][b];
+}
+
+/* the reference's factor of output row R and velocity component v for a
+ * metric direction (m0, m1, m2): C(R,V(v,x))*m0 + C(R,V(v,y))*m1 +
+ * C(R,V(v,z))*m2 (forward/sv_curv_col_el_aniso.c:453-470) */
+static inline float ani_f(const med_t *m, int R, int v, float m0, float m1, float m2)
+{
+  return cij(m, R, voigt(v, 0)) * m0 + cij(m, R, voigt(v, 1)) * m1 +
+         cij(m, R, voigt(v, 2)) * m2;
+}
+
+/* output rows in the reference's order hTxx hTyy hTzz hTyz hTxz hTxy */
+static const int ANI_ROW_COMP[6] = {TXX, TYY, TZZ, TYZ, TXZ, TXY};
 
 static inline void med_at(const cgfd_problem_t *p, size_t q, med_t *m)
 {
   memset(m, 0, sizeof(*m));
+  if (p->medium_type == CGFD_MEDIUM_ELASTIC_ANISO) {
+    const float *c[21] = {p->c11, p->c12, p->c13, p->c14, p->c15, p->c16, p->c22,
+                          p->c23, p->c24, p->c25, p->c26, p->c33, p->c34, p->c35,
+                          p->c36, p->c44, p->c45, p->c46, p->c55, p->c56, p->c66};
+    m->aniso = 1;
+    for (int n = 0; n < 21; n++) m->c[n] = c[n][q];
+    return;
+  }
   if (p->medium_type == CGFD_MEDIUM_ELASTIC_VTI) {
     m->vti = 1;
     m->c11 = p->c11[q]; m->c13 = p->c13[q]; m->c33 = p->c33[q];
@@ -171,6 +210,21 @@ static inline void hooke9(const med_t *m, float xix, float xiy, float xiz,
                           float DzVx, float DzVy, float DzVz, float *h,
                           size_t V, size_t q)
 {
+  if (m->aniso) {
+    /* forward/sv_curv_col_el_aniso.c:453-470: nine terms, xi / eta / zeta
+     * gradients in turn, x y z velocity in each */
+    const float mt[3][3] = {{xix, xiy, xiz}, {etx, ety, etz}, {ztx, zty, ztz}};
+    const float D[3][3] = {{DxVx, DxVy, DxVz}, {DyVx, DyVy, DyVz}, {DzVx, DzVy, DzVz}};
+    for (int r = 0; r < 6; r++) {
+      float acc = ani_f(m, r + 1, 0, mt[0][0], mt[0][1], mt[0][2]) * D[0][0];
+      for (int t = 1; t < 9; t++) {
+        int d = t / 3, v = t % 3;
+        acc = acc + ani_f(m, r + 1, v, mt[d][0], mt[d][1], mt[d][2]) * D[d][v];
+      }
+      h[ANI_ROW_COMP[r] * V + q] = acc;
+    }
+    return;
+  }
   if (!m->vti) {
     float lam = m->lam, mu = m->mu, l2m = m->l2m;
     h[TXX * V + q] = l2m * (xix * DxVx + etx * DyVx + ztx * DzVx) +
@@ -219,6 +273,14 @@ static inline void hooke9(const med_t *m, float xix, float xiy, float xiz,
 static inline void hooke1(const med_t *m, float e1, float e2, float e3,
                           float DVx, float DVy, float DVz, float *r)
 {
+  if (m->aniso) {
+    /* forward/sv_curv_col_el_aniso.c:824-829 */
+    for (int w = 0; w < 6; w++)
+      r[ANI_ROW_COMP[w]] = ani_f(m, w + 1, 0, e1, e2, e3) * DVx +
+                           ani_f(m, w + 1, 1, e1, e2, e3) * DVy +
+                           ani_f(m, w + 1, 2, e1, e2, e3) * DVz;
+    return;
+  }
   if (!m->vti) {
     float lam = m->lam, mu = m->mu, l2m = m->l2m;
     r[TXX] = l2m * e1 * DVx + lam * e2 * DVy + lam * e3 * DVz;
@@ -246,6 +308,10 @@ static inline void hooke1(const med_t *m, float e1, float e2, float e3,
 static inline void hooke_surf(const med_t *m, float ztx, float zty, float ztz,
                               float DzVx, float DzVy, float DzVz, float *s)
 {
+  if (m->aniso) {   /* forward/sv_curv_col_el_aniso.c:875-880 */
+    hooke1(m, ztx, zty, ztz, DzVx, DzVy, DzVz, s);
+    return;
+  }
   if (!m->vti) {
     float lam = m->lam, mu = m->mu, l2m = m->l2m;
     s[TXX] = l2m * (ztx * DzVx) + lam * (zty * DzVy + ztz * DzVz);
@@ -393,6 +459,51 @@ int oracle_dvh2dvz_vti(const cgfd_problem_t *p, float *mVx, float *mVy)
       C[2][2] = (c55 * etx) * ztx + (c55 * ety) * zty + (c33 * etz) * ztz;
       mul3(A, B, AB);
       mul3(A, C, AC);
+      size_t ij = (j * ln + i) * 9;
+      for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+          mVx[ij + r * 3 + c] = -1.0f * AB[r][c];
+          mVy[ij + r * 3 + c] = -1.0f * AC[r][c];
+        }
+    }
+  return 0;
+}
+
+/* anisotropic: matVx2Vz = -A^-1 B, matVy2Vz = -A^-1 C at k = nk2
+ * (forward/sv_curv_col_el_aniso.c:1267-1423), with
+ * M[a][b] = sum over n of (sum over m of C(V(a,n),V(b,m)) g_m) zeta_n for the
+ * metric g = zeta (A), xi (B), eta (C); matF2Vz is left untouched */
+int oracle_dvh2dvz_aniso(const cgfd_problem_t *p, float *mVx, float *mVy)
+{
+  size_t ln = p->nx, sl = (size_t)p->nx * p->ny;
+  int k = p->nk2;
+  for (int j = p->nj1; j <= p->nj2; j++)
+    for (int i = p->ni1; i <= p->ni2; i++) {
+      size_t q = i + j * ln + k * sl;
+      const float g[3][3] = {{p->xi_x[q], p->xi_y[q], p->xi_z[q]},
+                             {p->eta_x[q], p->eta_y[q], p->eta_z[q]},
+                             {p->zeta_x[q], p->zeta_y[q], p->zeta_z[q]}};
+      const float *zt = g[2];
+      med_t m;
+      med_at(p, q, &m);
+      float M[3][3][3];     /* [A, B, C] */
+      const int gsel[3] = {2, 0, 1};
+      for (int w = 0; w < 3; w++) {
+        const float *gm = g[gsel[w]];
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) {
+            float t[3];
+            for (int n = 0; n < 3; n++)
+              t[n] = cij(&m, voigt(a, n), voigt(b, 0)) * gm[0] +
+                     cij(&m, voigt(a, n), voigt(b, 1)) * gm[1] +
+                     cij(&m, voigt(a, n), voigt(b, 2)) * gm[2];
+            M[w][a][b] = t[0] * zt[0] + t[1] * zt[1] + t[2] * zt[2];
+          }
+      }
+      float AB[3][3], AC[3][3];
+      inv3(M[0]);
+      mul3(M[0], M[1], AB);
+      mul3(M[0], M[2], AC);
       size_t ij = (j * ln + i) * 9;
       for (int r = 0; r < 3; r++)
         for (int c = 0; c < 3; c++) {
@@ -642,7 +753,7 @@ static void rhs_vlow_row(orc_t *o, const float *w, float *h, int j, int zbias,
                b[7] * DyVy + b[8] * DyVz;
         /* + matF2Vz * (VxSrc,VySrc,VzSrc): zero without surface forces;
            the VTI routine has no such term (sv_curv_col_el_vti.c:525-547) */
-        if (!m.vti) {
+        if (!m.vti && !m.aniso) {
           const float *f = o->mF + ij;
           size_t i2 = i + j * ln;
           float vx = 0.0f, vy = 0.0f, vz = 0.0f;
@@ -1256,7 +1367,7 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
 {
   int med = p->medium_type;
   if (med != CGFD_MEDIUM_ELASTIC_ISO && med != CGFD_MEDIUM_ELASTIC_VTI &&
-      med != CGFD_MEDIUM_VISCOELASTIC_ISO)
+      med != CGFD_MEDIUM_ELASTIC_ANISO && med != CGFD_MEDIUM_VISCOELASTIC_ISO)
     return CGFD_EINVAL;
   if (p->src_n_surface_force > 0 &&
       (!p->src_force || !p->src_force_rate_indx || !p->Fx_rate || !p->Fy_rate ||
@@ -1300,6 +1411,8 @@ int oracle_allstep_pg(const cgfd_problem_t *p, int timg_mode, int nthreads,
     }
     if (med == CGFD_MEDIUM_ELASTIC_VTI) {
       oracle_dvh2dvz_vti(p, mVx, mVy);
+    } else if (med == CGFD_MEDIUM_ELASTIC_ANISO) {
+      oracle_dvh2dvz_aniso(p, mVx, mVy);
     } else if (med == CGFD_MEDIUM_VISCOELASTIC_ISO) {
       o.mD = calloc(n2, sizeof(float));
       oracle_dvh2dvz_vis(p, mVx, mVy, o.mD);

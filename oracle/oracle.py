@@ -95,6 +95,10 @@ def surface_matrices(problem):
     ptr = {k: v.ctypes.data for k, v in out.items()}
     if problem.medium_type == 3:
         lib().oracle_dvh2dvz_vti(C.addressof(cs), ptr["matVx2Vz2"], ptr["matVy2Vz2"])
+    elif problem.medium_type == 4:
+        L = lib()
+        L.oracle_dvh2dvz_aniso.argtypes = [C.c_void_p] * 3
+        L.oracle_dvh2dvz_aniso(C.addressof(cs), ptr["matVx2Vz2"], ptr["matVy2Vz2"])
     elif problem.medium_type == 5:
         out["matD"] = np.zeros(n2, np.float32)
         lib().oracle_dvh2dvz_vis(C.addressof(cs), ptr["matVx2Vz2"],

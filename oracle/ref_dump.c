@@ -74,6 +74,35 @@ static int is_phys(gd_t *gd, int i, int j, int k)
          k >= gd->nk1 && k <= gd->nk2;
 }
 
+/* the 21 constants of an anisotropic medium, c11 c12 .. c16 c22 .. c66 */
+static float **aniso_fields(md_t *md)
+{
+  static float *c[21];
+  float *v[21] = {md->c11, md->c12, md->c13, md->c14, md->c15, md->c16, md->c22,
+                  md->c23, md->c24, md->c25, md->c26, md->c33, md->c34, md->c35,
+                  md->c36, md->c44, md->c45, md->c46, md->c55, md->c56, md->c66};
+  memcpy(c, v, sizeof v);
+  return c;
+}
+
+/* The reference's anisotropic test medium (forward/md_t.c:539-590) leaves
+ * c12, c22, c44 and the off-diagonal terms zero, which is not a stable
+ * medium.  With CGFD_DUMP_SEED set, an anisotropic model gets instead a
+ * transversely isotropic stiffness (c11 = c22 = 25.2 GPa, c33 = 18,
+ * c13 = c23 = 10.962, c44 = c55 = 5.12, c66 = 7.168, c12 = c11 - 2 c66)
+ * plus every one of the 21 constants offset by up to +-0.4 GPa (seeded),
+ * before the pointwise +-10 % of perturb(). */
+static void aniso_base(gd_t *gd, md_t *md)
+{
+  const float base[21] = {25.2e9f, 10.864e9f, 10.962e9f, 0, 0, 0, 25.2e9f, 10.962e9f,
+                          0, 0, 0, 18.0e9f, 0, 0, 0, 5.12e9f, 0, 0, 5.12e9f, 0, 7.168e9f};
+  float off[21];
+  for (int n = 0; n < 21; n++) off[n] = 0.4e9f * urand();
+  float **c = aniso_fields(md);
+  for (size_t p = 0; p < gd->siz_icmp; p++)
+    for (int n = 0; n < 21; n++) c[n][p] = base[n] + off[n];
+}
+
 static void perturb(gd_t *gd, md_t *md, bdry_t *bdry, wav_t *wav, float amp_v)
 {
   size_t n = gd->siz_icmp;
@@ -88,6 +117,9 @@ static void perturb(gd_t *gd, md_t *md, bdry_t *bdry, wav_t *wav, float amp_v)
   } else if (md->medium_type == CONST_MEDIUM_ELASTIC_VTI) {
     fields[nf++] = md->c11; fields[nf++] = md->c13; fields[nf++] = md->c33;
     fields[nf++] = md->c55; fields[nf++] = md->c66;
+  } else if (md->medium_type == CONST_MEDIUM_ELASTIC_ANISO) {
+    float **c = aniso_fields(md);
+    for (int n = 0; n < 21; n++) fields[nf++] = c[n];
   }
   if (md->visco_type == CONST_VISCO_GRAVES_QS) fields[nf++] = md->Qs;
   for (int f = 0; f < nf; f++)
@@ -202,6 +234,17 @@ static void dump_inputs(fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md,
     }
   }
 
+  if (md->medium_type == CONST_MEDIUM_ELASTIC_ANISO) {
+    static const char *nm[21] = {"c11", "c12", "c13", "c14", "c15", "c16", "c22",
+                                 "c23", "c24", "c25", "c26", "c33", "c34", "c35",
+                                 "c36", "c44", "c45", "c46", "c55", "c56", "c66"};
+    float **c = aniso_fields(md);
+    for (int m = 0; m < 21; m++) {
+      char key[48];
+      snprintf(key, 48, "md.%s", nm[m]);
+      put(key, 'f', c[m], n);
+    }
+  }
   if (md->visco_type == CONST_VISCO_GRAVES_QS) {
     put("md.Qs", 'f', md->Qs, n);
     put_f("md.visco_Qs_freq", md->visco_Qs_freq);
@@ -380,6 +423,7 @@ void __wrap_drv_rk_curv_col_allstep(
     if (seed) {
       g_rng = (uint32_t)strtoul(seed, NULL, 10);
       if (g_rng == 0) g_rng = 1;
+      if (md->medium_type == CONST_MEDIUM_ELASTIC_ANISO) aniso_base(gd, md);
       perturb(gd, md, bdry, wav, amp ? (float)atof(amp) : 1e-2f);
     }
     dump_inputs(fd, gd, metric, md, src, bdry, wav, iorecv, ioline, dt,

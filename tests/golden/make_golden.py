@@ -157,6 +157,19 @@ CASES = {
         stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
         lines=[],
     ),
+    # fully anisotropic medium (21 constants; a stable transversely
+    # isotropic stiffness with every constant offset, see oracle/ref_dump.c)
+    # on the topography, seeded noise state, every boundary branch
+    "aniso_topo_noise": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_aniso",
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        free=True, seed=97531, steps=9, dt=0.004,
+        src=dict(kind="force+moment", loc=(8.3, 7.6, 4.0), spatial="gauss",
+                 f=(1e15, -2e15, 3e15), m=(1e16, 2e16, -1e16, 0.5e16, -0.3e16, 0.2e16),
+                 fc=8.0, t0=0.05),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1), (12.0, 6.0, 3.4, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
     # no free surface: PML on all six faces (z2 face included), noise state
     "iso_box_pml6": dict(
         ni=16, nj=14, nk=12, dh=100.0, topo=False, medium="elastic_iso",

@@ -65,7 +65,7 @@ def pml_mode(request, monkeypatch):
     return request.param
 
 
-@pytest.mark.parametrize("kind", ["iso", "vti", "visco"])
+@pytest.mark.parametrize("kind", ["iso", "vti", "visco", "aniso"])
 @pytest.mark.parametrize("shape", [(96, 80, 48), (70, 45, 37)])
 def test_media_model_noise_state(kind, shape, pml_mode):
     from cgfd3d_gb300 import models, solver
@@ -82,7 +82,7 @@ def test_media_model_noise_state(kind, shape, pml_mode):
     _compare(p, q, "%s %s" % (kind, shape))
 
 
-@pytest.mark.parametrize("kind", ["vti", "visco"])
+@pytest.mark.parametrize("kind", ["vti", "visco", "aniso"])
 def test_media_surface_matrices(kind):
     """Free-surface matrices computed on the device against the oracle's
     (and, for visco, the surface rotation matrices)."""
