@@ -398,13 +398,18 @@ def run_ours(args):
                                                      dt=0.01, nrecv=4))
     if world > 1:
         torch.distributed.barrier()
-    t0 = time.perf_counter()
-    se = solver.Solver(q)
-    se.run(q.nt_total)
-    se.fetch()
-    h2d, d2h = se.transfer_bytes()
-    se.close()
-    t_e2e = time.perf_counter() - t0
+    # three end-to-end runs of the same problem (each from host buffers to
+    # host buffers), the median reported: host-side copies vary from run to run
+    reps = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        se = solver.Solver(q)
+        se.run(q.nt_total)
+        se.fetch()
+        h2d, d2h = se.transfer_bytes()
+        se.close()
+        reps.append(time.perf_counter() - t0)
+    t_e2e = sorted(reps)[1]
     if world > 1:
         tt = torch.tensor([t_e2e], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -439,7 +444,8 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": h2d / q.nt_total,
                 "d2h_bytes_per_step": d2h / q.nt_total,
-                "steps": q.nt_total},
+                "steps": q.nt_total, "runs_ms": [1e3 * t for t in reps],
+                "reported": "median of 3 runs"},
         "gpu_launches": n_all,
         "clocks": clocks,
     }

@@ -143,6 +143,10 @@ void CGFD_CAT(cgfd_launch_stage_batch_, CGFD_MED_NAME)(int code, int kind, int n
 {
   launch_batch_med<CGFD_MED>(code, kind, nctas, st, args, geo, nshot);
 }
+
+/* tile rows the batched kernel was compiled with: must equal the single
+ * kernel's, whose tensor maps the batch reuses */
+int CGFD_CAT(cgfd_stage_rows_batch_, CGFD_MED_NAME)(void) { return s2::TY; }
 #endif
 
 #if CGFD_SINGLE

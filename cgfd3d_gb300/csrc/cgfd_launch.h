@@ -62,6 +62,8 @@ int cgfd_stage_rows_iso(void);
 int cgfd_stage_rows_vti(void);
 int cgfd_stage_rows_vis(void);
 int cgfd_stage_rows_ani(void);
+int cgfd_stage_rows_batch_iso(void);
+int cgfd_stage_rows_batch_vti(void);
 int cgfd_stage_smem_iso(void);
 int cgfd_stage_smem_vti(void);
 int cgfd_stage_smem_vis(void);

@@ -1,5 +1,5 @@
 /* Stage and CFS-PML kernels of the vti medium (see cgfd_launch.cuh). */
-#define CGFD_TILE_ROWS 10
+#define CGFD_TILE_ROWS 11
 #include "cgfd_media.cuh"
 #define CGFD_MED MED_VTI
 #define CGFD_MED_NAME vti

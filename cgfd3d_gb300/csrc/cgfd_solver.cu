@@ -2427,6 +2427,17 @@ extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
     if (p->nt_total != shots[0]->nt_total || p->dt != shots[0]->dt)
       return set_err(CGFD_EINVAL, "shot %d: every shot steps with the same dt and nt_total", k);
   }
+  {
+    /* the batched kernel reuses each shot's tensor maps: its tile rows must
+     * be the single kernel's */
+    const int med = medium_of(shots[0]->medium_type);
+    const int rows_single = med == MED_VTI ? cgfd_stage_rows_vti() : cgfd_stage_rows_iso();
+    const int rows_batch = med == MED_VTI ? cgfd_stage_rows_batch_vti()
+                                          : cgfd_stage_rows_batch_iso();
+    if (rows_single != rows_batch)
+      return set_err(CGFD_EINVAL, "batched stage kernel built with %d tile rows, the "
+                     "single-shot kernel with %d", rows_batch, rows_single);
+  }
   cgfd_batch_t *b = new cgfd_batch_t();
   b->n = nshot;
   b->nt_total = shots[0]->nt_total;
