@@ -6,7 +6,7 @@ tests/test_abi.py checks sizes and offsets against a compiled probe.
 
 import ctypes as C
 
-CGFD_ABI_VERSION = 5
+CGFD_ABI_VERSION = 6
 CGFD_MEDIUM_ELASTIC_ISO = 2
 CGFD_MEDIUM_ELASTIC_VTI = 3
 CGFD_MEDIUM_ELASTIC_ANISO = 4
@@ -83,6 +83,8 @@ class Problem(C.Structure):
            ("ablexp_Ex", PF), ("ablexp_Ey", PF), ("ablexp_Ez", PF),
            ("ablexp_blk", (C.c_int * 7) * 6)]
         + [(n, PF) for n in ANISO_EXTRA]
+        + [("dd_n", C.c_int), ("dd_max_nt", C.c_int),
+           ("dd_si", PI), ("dd_sj", PI), ("dd_sk", PI), ("dd_vi", PF), ("dd_mij", PF)]
     )
 
 

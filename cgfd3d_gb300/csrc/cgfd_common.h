@@ -117,6 +117,12 @@ struct StageArgs {
   /* Graves Q attenuation factors expf(-PI f dt / Qs) per point (pitched
    * volume), applied to `end` by the last stage; null when off */
   const float *qatt;
+  /* distributed sources: per-column entries (is = dd point), tables
+   * [step][stage][point][3 | 6] */
+  int dd_n, dd_max_nt;
+  const int *dd_col;
+  const SrcEntry *dd_ent;
+  const float *dd_vi, *dd_mij;
 };
 
 /* StageArgs is copied word by word into shared memory by the batched stage

@@ -866,6 +866,9 @@ struct cgfd_solver {
   float *staging;               /* upload staging volume (set-up only) */
   OutSlot out[CGFD_OUT_SLOTS + 1];   /* output boxes; the last: blocking calls */
   float *qatt;                  /* Graves Q factors (pitched volume), or null */
+  int *dd_col;                  /* dd sources: per-column entry offsets */
+  SrcEntry *dd_ent;
+  float *dd_tab;                /* dd_vi then dd_mij */
   float *abl;                   /* sponge masks Ex | Ey | Ez, or null */
   AblexpBlocks abx;             /* sponge blocks */
   StageMaps maps;               /* tensor maps of the stage kernel */
@@ -995,6 +998,15 @@ static int validate(const cgfd_problem_t *p)
         }
       }
     }
+  if (p->dd_n > 0) {
+    if (!p->dd_si || !p->dd_sj || !p->dd_sk || p->dd_max_nt < 0 ||
+        (!p->dd_vi && !p->dd_mij))
+      return set_err(CGFD_EINVAL, "dd sources: indices or tables missing");
+    for (int n = 0; n < p->dd_n; n++)
+      if (p->dd_si[n] < p->ni1 || p->dd_si[n] > p->ni2 || p->dd_sj[n] < p->nj1 ||
+          p->dd_sj[n] > p->nj2 || p->dd_sk[n] < p->nk1 || p->dd_sk[n] > p->nk2)
+        return set_err(CGFD_EINVAL, "dd source %d outside the physical points", n);
+  }
   if (p->graves_qs) {
     if (!p->Qs) return set_err(CGFD_EINVAL, "Graves Q: Qs missing");
     if (p->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO)
@@ -1214,7 +1226,8 @@ extern "C" void cgfd_solver_destroy(cgfd_solver_t *s)
                   s->src_it_begin, s->src_it_end, s->src_ent, s->stf,
                   s->recv_dijk, s->recv_seismo, s->line_seismo, s->recv_idx,
                   s->line_iptr, s->d_it, s->d_flag, s->d_err, s->pg, s->dis,
-                  s->sf, s->sf_w, s->frate, s->surf, s->staging, s->qatt, s->abl};
+                  s->sf, s->sf_w, s->frate, s->surf, s->staging, s->qatt, s->abl,
+                  s->dd_col, s->dd_ent, s->dd_tab};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   for (OutSlot &o : s->out) {
@@ -1508,6 +1521,47 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
       cudaStreamSynchronize(st);       /* host vectors go out of scope */
     }
   }
+  if (p->dd_n > 0) {
+    /* distributed sources: point entries per column, sorted by k then point
+     * (added in point order, as sv_curv_col_el_rhs_srcdd loops them) */
+    size_t ln = p->nx, sl = (size_t)p->nx * p->ny;
+    std::vector<HostEntry> all(p->dd_n);
+    for (int n = 0; n < p->dd_n; n++) {
+      HostEntry &h = all[n];
+      h.col = (p->dd_si[n] - p->ni1) + (p->dd_sj[n] - p->nj1) * p->ni;
+      h.e.k = p->dd_sk[n];
+      h.e.is = n;
+      h.e.coef = 1.0f;
+      h.e.q = dev_index(g, p->dd_si[n] + p->dd_sj[n] * ln + (size_t)p->dd_sk[n] * sl);
+      h.e.vf = h.e.rjac = 0.f;
+      h.e.force_on = 1;
+    }
+    std::stable_sort(all.begin(), all.end(), [](const HostEntry &x, const HostEntry &y) {
+      if (x.col != y.col) return x.col < y.col;
+      if (x.e.k != y.e.k) return x.e.k < y.e.k;
+      return x.e.is < y.e.is;
+    });
+    std::vector<int> col((size_t)p->ni * p->nj + 1, 0);
+    std::vector<SrcEntry> ent;
+    for (auto &h : all) { col[h.col + 1]++; ent.push_back(h.e); }
+    for (size_t c = 1; c < col.size(); c++) col[c] += col[c - 1];
+    TRY(dalloc(s, &s->dd_col, col.size()));
+    TRY(dalloc(s, &s->dd_ent, ent.size()));
+    TRYC(cudaMemcpyAsync(s->dd_col, col.data(), col.size() * 4, cudaMemcpyHostToDevice, st));
+    TRYC(cudaMemcpyAsync(s->dd_ent, ent.data(), ent.size() * sizeof(SrcEntry),
+                         cudaMemcpyHostToDevice, st));
+    k_src_weights<<<(unsigned)((ent.size() + 127) / 128), 128, 0, st>>>(
+        g, s->dd_ent, (int)ent.size(), s->media, s->metric);
+    TRYC(cudaGetLastError());
+    size_t nt = (size_t)p->dd_max_nt * 4 * p->dd_n;
+    TRY(dalloc(s, &s->dd_tab, 9 * nt + 1));
+    if (p->dd_vi && nt)
+      TRYC(cudaMemcpyAsync(s->dd_tab, p->dd_vi, 3 * nt * 4, cudaMemcpyHostToDevice, st));
+    if (p->dd_mij && nt)
+      TRYC(cudaMemcpyAsync(s->dd_tab + 3 * nt, p->dd_mij, 6 * nt * 4, cudaMemcpyHostToDevice,
+                           st));
+    s->h2d_bytes += 9 * nt * 4;
+  }
   tr.mark("sources");
   /* receivers and lines */
   if (p->recv_n > 0) {
@@ -1713,6 +1767,15 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
     a.Fx = s->stf; a.Fy = s->stf + nstf; a.Fz = s->stf + 2 * nstf;
     a.Mxx = s->stf + 3 * nstf; a.Myy = s->stf + 4 * nstf; a.Mzz = s->stf + 5 * nstf;
     a.Mxz = s->stf + 6 * nstf; a.Myz = s->stf + 7 * nstf; a.Mxy = s->stf + 8 * nstf;
+  }
+  if (p->dd_n > 0) {
+    a.dd_n = p->dd_n;
+    a.dd_max_nt = p->dd_max_nt;
+    a.dd_col = s->dd_col;
+    a.dd_ent = s->dd_ent;
+    size_t nt = (size_t)p->dd_max_nt * 4 * p->dd_n;
+    a.dd_vi = p->dd_vi ? s->dd_tab : nullptr;
+    a.dd_mij = p->dd_mij ? s->dd_tab + 3 * nt : nullptr;
   }
   a.d_it = s->d_it;
   a.istage = istage;
@@ -2424,6 +2487,8 @@ extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
     if (p->ablexp)
       return set_err(CGFD_EINVAL, "shot %d: the exponential sponge is not batched "
                      "(CFS-PML is)", k);
+    if (p->dd_n > 0)
+      return set_err(CGFD_EINVAL, "shot %d: distributed sources are not batched", k);
     if (p->nt_total != shots[0]->nt_total || p->dt != shots[0]->dt)
       return set_err(CGFD_EINVAL, "shot %d: every shot steps with the same dt and nt_total", k);
   }

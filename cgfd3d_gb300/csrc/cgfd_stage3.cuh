@@ -344,11 +344,16 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
   const int sp = ty * TX + tx;        /* point index inside a stream slot */
 
   /* per-thread constants of the k loop */
-  int src_e0 = 0, src_e1 = 0;
+  int src_e0 = 0, src_e1 = 0, dd_e0 = 0, dd_e1 = 0;
   if (a.src_n > 0 && valid) {
     long long colidx = (long long)(i - g.ni1) + (long long)(j - g.nj1) * g.ni;
     src_e0 = a.src_col[colidx];
     src_e1 = a.src_col[colidx + 1];
+  }
+  if (a.dd_n > 0 && valid) {
+    long long colidx = (long long)(i - g.ni1) + (long long)(j - g.nj1) * g.ni;
+    dd_e0 = a.dd_col[colidx];
+    dd_e1 = a.dd_col[colidx + 1];
   }
 
   /* faces whose (i, j) range holds this column (x/y faces), and the k
@@ -576,6 +581,32 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
             r[C_TXZ] -= a.Mxz[t] * s.rjac;
             r[C_TYZ] -= a.Myz[t] * s.rjac;
             r[C_TXY] -= a.Mxy[t] * s.rjac;
+          }
+        }
+      }
+      if (dd_e0 < dd_e1) {
+        /* distributed sources after the others (forward/sv_curv_col_el.c:
+         * 487-590), while the step is below dd_max_nt */
+        const int itg = *a.d_it;
+        if (itg < a.dd_max_nt) {
+          const long long t0 = ((long long)itg * 4 + a.istage) * a.dd_n;
+          for (int e = dd_e0; e < dd_e1; e++) {
+            SrcEntry s = a.dd_ent[e];
+            if (s.k != k) continue;
+            const long long t = t0 + s.is;
+            if (a.dd_vi) {
+              r[C_VX] += a.dd_vi[3 * t + 0] * s.vf;
+              r[C_VY] += a.dd_vi[3 * t + 1] * s.vf;
+              r[C_VZ] += a.dd_vi[3 * t + 2] * s.vf;
+            }
+            if (a.dd_mij) {
+              r[C_TXX] -= a.dd_mij[6 * t + 0] * s.rjac;
+              r[C_TYY] -= a.dd_mij[6 * t + 1] * s.rjac;
+              r[C_TZZ] -= a.dd_mij[6 * t + 2] * s.rjac;
+              r[C_TYZ] -= a.dd_mij[6 * t + 3] * s.rjac;
+              r[C_TXZ] -= a.dd_mij[6 * t + 4] * s.rjac;
+              r[C_TXY] -= a.dd_mij[6 * t + 5] * s.rjac;
+            }
           }
         }
       }

@@ -28,7 +28,7 @@
  *
  * Errors print the library's message and call MPI_Abort when MPI is linked
  * (exit(1) otherwise), as the reference does.  Unsupported configurations
- * (dd sources)
+ * (dd sources spread over several points)
  * are reported the same way instead of being ignored.
  */
 #include <stdio.h>
@@ -154,6 +154,13 @@ static void write_step(const out_ctx_t *o, int it)
 }
 #endif
 
+static void fatal(const char *what)
+{
+  fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s\n", what);
+  fflush(stderr);
+  CGFD_ABORT();
+}
+
 static void unsupported(const char *what)
 {
   fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s is not supported\n", what);
@@ -180,7 +187,8 @@ void drv_rk_curv_col_allstep(
   if (md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO &&
       md->visco_type != CGFD_REF_VISCO_GMB)
     unsupported("a visco-elastic model other than GMB");
-  if (src->dd_is_valid == 1) unsupported("a distributed (dd) source");
+  if (src->dd_is_valid == 1 && src->dd_is_add_at_point != 1)
+    unsupported("a distributed (dd) source spread over several points");
 
   cgfd_problem_t p;
   memset(&p, 0, sizeof(p));
@@ -231,6 +239,31 @@ void drv_rk_curv_col_allstep(
       int v[7] = {D->enable, D->ni1, D->ni2, D->nj1, D->nj2, D->nk1, D->nk2};
       memcpy(p.ablexp_blk[n], v, sizeof v);
     }
+  }
+  /* distributed sources: the reference streams their per-step values from
+   * the files its set-up wrote (forward/src_t.c:1929-2000); here the whole
+   * files are read once and handed to the device */
+  float *dd_vi = NULL, *dd_mij = NULL;
+  if (src->dd_is_valid == 1 && src->dd_total_number > 0) {
+    size_t nt = (size_t)src->dd_max_nt * src->max_stage * src->dd_total_number;
+    if (src->max_stage != 4) unsupported("dd sources with other than 4 stages");
+    if (src->dd_vi_actived == 1) {
+      dd_vi = (float *)malloc(3 * nt * sizeof(float));
+      if (!dd_vi || fseek(src->fp_vi, 0, SEEK_SET) != 0 ||
+          fread(dd_vi, sizeof(float), 3 * nt, src->fp_vi) != 3 * nt)
+        fatal("cannot read the dd force-rate file");
+    }
+    if (src->dd_mij_actived == 1) {
+      dd_mij = (float *)malloc(6 * nt * sizeof(float));
+      if (!dd_mij || fseek(src->fp_mij, 0, SEEK_SET) != 0 ||
+          fread(dd_mij, sizeof(float), 6 * nt, src->fp_mij) != 6 * nt)
+        fatal("cannot read the dd moment-rate file");
+    }
+    p.dd_n = src->dd_total_number;
+    p.dd_max_nt = src->dd_max_nt;
+    p.dd_si = src->dd_si; p.dd_sj = src->dd_sj; p.dd_sk = src->dd_sk;
+    p.dd_vi = dd_vi;
+    p.dd_mij = dd_mij;
   }
   p.free_top = bdry->is_sides_free[2][1] == 1;
   for (int d = 0; d < 3; d++)
@@ -447,4 +480,5 @@ void drv_rk_curv_col_allstep(
     n += ioline->line_nr[l];
   }
   free(rdijk); free(ridx); free(rseis); free(liptr); free(lseis);
+  free(dd_vi); free(dd_mij);
 }

@@ -246,6 +246,23 @@ def add_ablexp(p, layers, vel=6000.0, coords=None, dh=None):
     return p
 
 
+def add_dd_sources(p, ijk, vi=None, mij=None, max_nt=None):
+    """Distributed (dd) sources at grid points: `ijk` (n, 3) local indices
+    (ghosts included); vi (max_nt, 4, n, 3) force rates and/or mij
+    (max_nt, 4, n, 6) moment rates (Mxx Myy Mzz Myz Mxz Mxy) per step and RK
+    stage, as the reference's set-up leaves them in its dd files."""
+    ijk = np.asarray(ijk, np.int32).reshape(-1, 3)
+    tabs = [t for t in (vi, mij) if t is not None]
+    if not tabs:
+        raise ValueError("dd sources need vi or mij")
+    nt = tabs[0].shape[0] if max_nt is None else int(max_nt)
+    p.dd = dict(si=np.ascontiguousarray(ijk[:, 0]), sj=np.ascontiguousarray(ijk[:, 1]),
+                sk=np.ascontiguousarray(ijk[:, 2]), max_nt=nt,
+                vi=None if vi is None else np.ascontiguousarray(vi, np.float32).ravel(),
+                mij=None if mij is None else np.ascontiguousarray(mij, np.float32).ravel())
+    return p
+
+
 def add_graves_qs(p, Qs, freq):
     """Graves Q attenuation of an elastic medium (visco_config graves_Qs):
     Qs per point (nx*ny*nz, or a scalar), reference frequency `freq`."""

@@ -56,6 +56,7 @@ class Problem:
         self.free_top = 0
         self.graves_qs = None     # dict(Qs=volume, freq=Hz): Graves Q attenuation
         self.ablexp = None        # dict(Ex, Ey, Ez, blk (6, 7)): exponential sponge
+        self.dd = None            # dict(si, sj, sk, max_nt, vi, mij): dd sources
         self.pml = [[None, None] for _ in range(3)]
         self.src = None
         self.recv = None
@@ -177,6 +178,11 @@ class Problem:
             s.graves_qs = 1
             s.qs_freq = float(self.graves_qs["freq"])
             s.Qs = P(self.graves_qs["Qs"])
+        if self.dd is not None:
+            d = self.dd
+            s.dd_n, s.dd_max_nt = len(d["si"]), int(d["max_nt"])
+            s.dd_si, s.dd_sj, s.dd_sk = [P(d[k], C.c_int) for k in ("si", "sj", "sk")]
+            s.dd_vi, s.dd_mij = P(d.get("vi")), P(d.get("mij"))
         if self.ablexp is not None:
             s.ablexp = 1
             s.ablexp_Ex, s.ablexp_Ey, s.ablexp_Ez = [P(self.ablexp[k]) for k in ("Ex", "Ey", "Ez")]

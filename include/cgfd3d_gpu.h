@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define CGFD_ABI_VERSION 5
+#define CGFD_ABI_VERSION 6
 
 /* medium types, same codes as forward/constants.h:24-29 */
 #define CGFD_MEDIUM_ELASTIC_ISO 2
@@ -158,6 +158,18 @@ typedef struct {
    * c55, c66 above, nx*ny*nz each (forward/sv_curv_col_el_aniso.c) */
   const float *c12, *c14, *c15, *c16, *c22, *c23, *c24, *c25, *c26;
   const float *c34, *c35, *c36, *c44, *c45, *c46, *c56;
+
+  /* distributed (dd) sources added at grid points (src_t dd_*,
+   * forward/src_t.c:1182-1930, injected after the other sources by
+   * sv_curv_col_el_rhs_srcdd, forward/sv_curv_col_el.c:487-590): dd_n points
+   * at local indices (ghosts included) dd_si/sj/sk; per step and RK stage
+   * dd_vi[dd_max_nt][4][dd_n][3] (added to the velocity rates times
+   * slw/jac) and dd_mij[dd_max_nt][4][dd_n][6] (Mxx Myy Mzz Myz Mxz Mxy,
+   * subtracted from the stress rates times 1/jac), either may be NULL; the
+   * sources act while the step index is below dd_max_nt. */
+  int dd_n, dd_max_nt;
+  const int *dd_si, *dd_sj, *dd_sk;
+  const float *dd_vi, *dd_mij;
 } cgfd_problem_t;
 
 /* Opaque device-resident solver. */

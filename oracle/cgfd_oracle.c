@@ -20,6 +20,7 @@
  *   velocity "vlow"      forward/sv_curv_col_el_iso.c:451-634
  *   ADE CFS-PML          forward/sv_curv_col_el_iso.c:644-1146
  *   source injection     forward/sv_curv_col_el.c:311-479, src_t.c:2111-2151
+ *   distributed sources  forward/sv_curv_col_el.c:487-590
  *   surface force layers forward/src_t.c:153-314 (traction and velocity-rate
  *                        layers of the forces whose spread reaches the
  *                        surface, used by the traction image and vlow)
@@ -919,6 +920,38 @@ static void rhs_atten_plane(orc_t *o, const float *w, float *h, int k)
   }
 }
 
+/* distributed sources at grid points after the other sources
+ * (forward/sv_curv_col_el.c:487-590): force rates times slw/jac, moment
+ * rates times 1/jac (evaluated in double as the reference's 1.0 / jac) */
+static void rhs_srcdd(orc_t *o, float *h, int it, int is)
+{
+  const cgfd_problem_t *p = o->p;
+  const size_t V = o->vol;
+  if (p->dd_vi) {
+    const float *vi = p->dd_vi + ((size_t)it * 4 + is) * p->dd_n * 3;
+    for (int n = 0; n < p->dd_n; n++, vi += 3) {
+      size_t q = p->dd_si[n] + p->dd_sj[n] * o->ln + (size_t)p->dd_sk[n] * o->sl;
+      float v = p->slw[q] / p->jac[q];
+      h[VX * V + q] += vi[0] * v;
+      h[VY * V + q] += vi[1] * v;
+      h[VZ * V + q] += vi[2] * v;
+    }
+  }
+  if (p->dd_mij) {
+    const float *m = p->dd_mij + ((size_t)it * 4 + is) * p->dd_n * 6;
+    for (int n = 0; n < p->dd_n; n++, m += 6) {
+      size_t q = p->dd_si[n] + p->dd_sj[n] * o->ln + (size_t)p->dd_sk[n] * o->sl;
+      float rjac = 1.0 / p->jac[q];
+      h[TXX * V + q] -= m[0] * rjac;
+      h[TYY * V + q] -= m[1] * rjac;
+      h[TZZ * V + q] -= m[2] * rjac;
+      h[TYZ * V + q] -= m[3] * rjac;
+      h[TXZ * V + q] -= m[4] * rjac;
+      h[TXY * V + q] -= m[5] * rjac;
+    }
+  }
+}
+
 /* Graves Q attenuation after the last stage's combine, physical points of
  * one k-slab (forward/sv_curv_col_el.c:638-666) */
 static void graves_qs_slab(orc_t *o, float *w, long k0, long k1)
@@ -1276,6 +1309,7 @@ static void *worker(void *arg)
       }
       /* 5. sources */
       if (tid == 0 && p->src_n > 0) rhs_src(o, rhs, it, is);
+      if (tid == 0 && p->dd_n > 0 && it < p->dd_max_nt) rhs_srcdd(o, rhs, it, is);
       pthread_barrier_wait(&o->bar);
       /* RK combine over the whole padded volume (drv_rk_curv_col.c:292-446) */
       if (is < 3) {
