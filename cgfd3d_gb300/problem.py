@@ -237,6 +237,13 @@ def from_golden(path_or_npz):
     p.free_top = int(free[2, 1])
     if "md.Qs" in d:
         p.graves_qs = dict(Qs=_f32(d["md.Qs"]), freq=float(d["md.visco_Qs_freq"][0]))
+    if "src.dd_total_number" in d and int(d["src.dd_is_valid"][0]) == 1:
+        nd = int(d["src.dd_total_number"][0])
+        p.dd = dict(si=_i32(d["src.dd_si"]), sj=_i32(d["src.dd_sj"]), sk=_i32(d["src.dd_sk"]),
+                    max_nt=int(d["src.dd_max_nt"][0]),
+                    vi=_f32(d["src.dd_vi"]) if "src.dd_vi" in d else None,
+                    mij=_f32(d["src.dd_mij"]) if "src.dd_mij" in d else None)
+        assert len(p.dd["si"]) == nd
     if "bdry.ablexp_Ex" in d:
         p.ablexp = dict(Ex=_f32(d["bdry.ablexp_Ex"]), Ey=_f32(d["bdry.ablexp_Ey"]),
                         Ez=_f32(d["bdry.ablexp_Ez"]), blk=_i32(d["bdry.ablexp_blk"]))

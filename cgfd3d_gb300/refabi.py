@@ -288,6 +288,29 @@ def build_reference_structs(p):
                 setattr(src, n, _fp(s[n]))
         if s.get("force_rate_indx") is not None:
             src.force_rate_indx = s["force_rate_indx"].ctypes.data_as(PI)
+    if p.dd is not None:
+        # distributed sources: the reference hands its time loop files of
+        # per-step tables (forward/src_t.c:1640-1835); write them and open
+        # them with the C library, as the reference's set-up leaves them
+        import tempfile
+        libc = C.CDLL(None)
+        libc.fopen.restype = C.c_void_p
+        libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+        d = p.dd
+        src.dd_is_valid, src.dd_is_add_at_point = 1, 1
+        src.dd_total_number, src.dd_max_nt = len(d["si"]), int(d["max_nt"])
+        src.max_stage = 4
+        for n in ("si", "sj", "sk"):
+            setattr(src, "dd_" + n, d[n].ctypes.data_as(PI))
+        for key, act, fp in (("vi", "dd_vi_actived", "fp_vi"), ("mij", "dd_mij_actived", "fp_mij")):
+            if d.get(key) is None:
+                continue
+            tmp = tempfile.NamedTemporaryFile(suffix=".bin", delete=False)
+            tmp.write(np.ascontiguousarray(d[key], np.float32).tobytes())
+            tmp.close()
+            keep.setdefault("dd_files", []).append(tmp.name)
+            setattr(src, act, 1)
+            setattr(src, fp, libc.fopen(tmp.name.encode(), b"rb"))
     bd = Bdry()
     bd.is_sides_free[2][1] = int(p.free_top)
     bd.is_enable_free = int(p.free_top)

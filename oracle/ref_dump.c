@@ -296,6 +296,32 @@ static void dump_inputs(fd_t *fd, gd_t *gd, gdcurv_metric_t *metric, md_t *md,
   put_i("src.is_surface_force_strict", src->is_surface_force_strict);
   put_i("src.total_number_surface_force", src->total_number_surface_force);
   put_i("src.dd_is_valid", src->dd_is_valid);
+  if (src->dd_is_valid == 1) {
+    /* distributed sources: indices and the whole per-step tables, read from
+     * the files the set-up wrote (position restored for the time loop) */
+    int nd = src->dd_total_number;
+    put_i("src.dd_total_number", nd);
+    put_i("src.dd_max_nt", src->dd_max_nt);
+    put_i("src.dd_is_add_at_point", src->dd_is_add_at_point);
+    put("src.dd_si", 'i', src->dd_si, nd);
+    put("src.dd_sj", 'i', src->dd_sj, nd);
+    put("src.dd_sk", 'i', src->dd_sk, nd);
+    FILE *fps[2] = {src->dd_vi_actived == 1 ? src->fp_vi : NULL,
+                    src->dd_mij_actived == 1 ? src->fp_mij : NULL};
+    const char *names[2] = {"src.dd_vi", "src.dd_mij"};
+    const int ncmp[2] = {3, 6};
+    for (int t = 0; t < 2; t++) {
+      if (!fps[t]) continue;
+      size_t n = (size_t)src->dd_max_nt * src->max_stage * nd * ncmp[t];
+      float *buf = malloc(n * sizeof(float));
+      long pos = ftell(fps[t]);
+      fseek(fps[t], 0, SEEK_SET);
+      if (fread(buf, sizeof(float), n, fps[t]) != n) exit(3);
+      fseek(fps[t], pos, SEEK_SET);
+      put(names[t], 'f', buf, n);
+      free(buf);
+    }
+  }
   int ns = src->total_number;
   if (ns > 0) {
     size_t nstf = (size_t)ns * src->max_nt * src->max_stage;

@@ -170,6 +170,24 @@ CASES = {
         stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1), (12.0, 6.0, 3.4, 1)],
         lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
     ),
+    # distributed (dd) sources at grid points next to an ordinary moment
+    # source: force and moment rates of 12 points (interior, PML, free
+    # surface, one column) read by the reference from a raw container
+    # (oracle/shim/netcdf_null.c), three steps per read, input ending before
+    # the last steps
+    "iso_topo_dd": dict(
+        ni=18, nj=16, nk=14, dh=100.0, topo=True, medium="elastic_iso",
+        pml=dict(x_left=4, x_right=4, y_front=4, y_back=4, z_bottom=4),
+        free=True, seed=1122, steps=9, dt=0.004,
+        src=dict(kind="moment", loc=(8.3, 7.6, 4.0), spatial="point",
+                 m=(1e16, 2e16, -1e16, 0.5e16, -0.3e16, 0.2e16), fc=8.0, t0=0.05),
+        dd=dict(points=[(8, 7, 5), (8, 7, 9), (8, 7, 11), (2, 5, 6), (15, 12, 3),
+                        (5, 13, 13), (12, 3, 13), (10, 10, 1), (6, 9, 12), (14, 6, 8),
+                        (3, 3, 2), (9, 11, 13)],
+                nt_per_read=3, dt_in=0.002, t_end=0.03, seed=77),
+        stations=[(3.25, 4.5, 0.0, 1), (10.7, 9.1, 0.0, 1)],
+        lines=[dict(start=(2, 8, 13), incre=(2, 0, 0), count=6)],
+    ),
     # no free surface: PML on all six faces (z2 face included), noise state
     "iso_box_pml6": dict(
         ni=16, nj=14, nk=12, dh=100.0, topo=False, medium="elastic_iso",
@@ -255,6 +273,9 @@ def write_par(path, c, work):
         "is_export_source": 0,
         "source_export_dir": work,
         "source_spatial_distribution_type": c["src"]["spatial"],
+        **({"in_ddsource_file": os.path.join(work, "dd.raw"),
+            "ddsource_add_at_point": 1,
+            "ddsource_nt_per_read": c["dd"]["nt_per_read"]} if "dd" in c else {}),
         "output_dir": os.path.join(work, "out"),
         "tmp_dir": os.path.join(work, "tmp"),
         "in_station_file": os.path.join(work, "case.station"),
@@ -285,6 +306,42 @@ def write_src(path, c):
     lines.append(" ".join("%g" % v for v in vals))
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
+
+
+def write_dd(path, c):
+    """Distributed-source input in the raw container of the NetCDF shim
+    (oracle/shim/netcdf_null.c): grid-index locations, per-point force and
+    moment rates sampled every dt_in from 0 to t_end (smooth random pulses)."""
+    d = c["dd"]
+    rng = np.random.default_rng(d["seed"])
+    pts = np.array(d["points"], np.float32)
+    n = len(pts)
+    t = np.arange(0.0, d["t_end"] + 0.5 * d["dt_in"], d["dt_in"]).astype(np.float32)
+    t[0] = 0.0
+    pulses = {}
+    for name in ("Fx", "Fy", "Fz", "Mxx_rate", "Myy_rate", "Mzz_rate", "Myz_rate",
+                 "Mxz_rate", "Mxy_rate"):
+        amp = (1e15 if name.startswith("F") else 1e17) * rng.standard_normal((n, 1))
+        tc = rng.uniform(0.005, 0.02, (n, 1))
+        w = rng.uniform(0.004, 0.01, (n, 1))
+        pulses[name] = (amp * np.exp(-((t[None, :] - tc) / w) ** 2)).astype(np.float32)
+    b = b"CGNCRAW1"
+    atts = [("location_is_axis", 0), ("z_is_depth", 0)]
+    b += struct.pack("<i", len(atts))
+    for nm, v in atts:
+        b += nm.encode().ljust(32, b"\0") + struct.pack("<i", v)
+    dims = [("time", len(t)), ("number", n)]
+    b += struct.pack("<i", len(dims))
+    for nm, ln in dims:
+        b += nm.encode().ljust(32, b"\0") + struct.pack("<q", ln)
+    vars_ = [("time", [0], t), ("x", [1], pts[:, 0]), ("y", [1], pts[:, 1]),
+             ("z", [1], pts[:, 2])] + [(nm, [1, 0], v) for nm, v in pulses.items()]
+    b += struct.pack("<i", len(vars_))
+    for nm, dd, data in vars_:
+        b += nm.encode().ljust(32, b"\0") + struct.pack("<i4i", len(dd), *(dd + [0] * (4 - len(dd))))
+        b += np.ascontiguousarray(data, "<f4").tobytes()
+    with open(path, "wb") as f:
+        f.write(b)
 
 
 def write_station(path, c):
@@ -344,6 +401,8 @@ def run_case(name, c, ref_bin):
         write_par(os.path.join(work, "par.json"), c, work)
         write_src(os.path.join(work, "case.src"), c)
         write_station(os.path.join(work, "case.station"), c)
+        if "dd" in c:
+            write_dd(os.path.join(work, "dd.raw"), c)
         env = dict(os.environ)
         env["CGFD_DUMP_FILE"] = os.path.join(work, "dump.bin")
         if c.get("seed") is not None:
