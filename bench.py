@@ -45,6 +45,7 @@ BYTES_PER_PT_STAGE = {"topo": 192, "flat": 192, "vti": 204, "visco": 504, "aniso
 WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "slices": dict(ni=400, nj=400, nk=200),
              "locate": dict(ni=400, nj=400, nk=200),
+             "media": dict(ni=400, nj=400, nk=200),
              "batch": dict(ni=400, nj=400, nk=200),
              "vti": dict(ni=300, nj=300, nk=150),
              "aniso": dict(ni=300, nj=300, nk=150),
@@ -309,6 +310,8 @@ def run_reference(args):
         return run_reference_batch(args)
     if args.workload == "locate":
         return run_locate(args, reference=True)
+    if args.workload == "media":
+        return run_media(args, reference=True)
     threads = os.cpu_count() or 1
     # warm-up sample, then the timed samples (one RK4 step each)
     cpu_rate(args, 1, threads)
@@ -747,6 +750,94 @@ def run_locate(args, reference=False):
     return 0
 
 
+def layered_model(X, Y, nlayer=4, seed=13):
+    """A layered elastic isotropic model over the grid's area: undulating
+    interfaces from 500 m above sea level down to -15 km, velocities and
+    densities increasing with depth, gradients with power laws."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    NX, NY = 81, 81
+    minx, miny = float(X.min()) - 100.0, float(Y.min()) - 100.0
+    dx = (float(X.max()) + 100.0 - minx) / (NX - 1)
+    dy = (float(Y.max()) + 100.0 - miny) / (NY - 1)
+    xs, ys = minx + dx * np.arange(NX), miny + dy * np.arange(NY)
+    XX, YY = np.meshgrid(xs, ys)
+    tops = [3000.0, -3000.0, -9000.0, -15000.0][:nlayer]
+    recs = []
+    for n, t in enumerate(tops):
+        e = t + 300.0 * np.sin(XX / 7000.0 + n) * np.cos(YY / 5000.0)
+        rho, vp, vs = 2300 + 200 * n, 4000 + 800 * n, 2300 + 450 * n
+        r = lambda a: a * (1 + 0.02 * rng.uniform(-1, 1, XX.shape))
+        recs.append(np.stack([e, r(rho), np.full_like(XX, 0.02), np.full_like(XX, 1.0),
+                              r(vp), np.full_like(XX, 0.05), np.full_like(XX, 1.0),
+                              r(vs), np.full_like(XX, 0.03), np.full_like(XX, 0.9)], -1))
+    return dict(NI=len(tops), NX=NX, NY=NY, MINX=minx, MINY=miny, DX=dx, DY=dy,
+                rec=np.stack(recs).astype(np.float32))
+
+
+def run_media(args, reference=False):
+    """Media discretisation: a 4-interface layered elastic isotropic model
+    onto the topography grid with the "loc" method, grid points per second
+    (host coordinates in, host lambda/mu/rho out)."""
+    import numpy as np
+    from types import SimpleNamespace
+    from cgfd3d_gb300 import models
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    shp = (args.nk + 6, args.nj + 6, args.ni + 6)
+    X, Y, Z = [a.reshape(shp) for a in
+               models._coords_of(SimpleNamespace(ni=args.ni, nj=args.nj, nk=args.nk), 2024)]
+    m = layered_model(X, Y)
+    npts = X.size
+    line = {"metric": "grid points discretised/s", "unit": "points/s", "n_gpus": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": "layered elastic isotropic model (4 interfaces, "
+                       "81x81 mesh) onto the topography grid %dx%dx%d (padded), "
+                       "method loc" % (args.ni, args.nj, args.nk),
+                       "parallelism": "single"}}
+    if reference or not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+        kk = 4                                 # a slab of 4 k-planes
+        t0 = time.perf_counter()
+        oracle.layer_el_iso_loc(m, X[:kk], Y[:kk], Z[:kk])
+        tc = time.perf_counter() - t0
+        cpu = {"value": X[:kk].size / tc, "unit": "points/s", "cores": 1, "kind": "port",
+               "sample": "%d k-planes (%d points), C oracle port, 1 thread, %.2f s"
+                         % (kk, X[:kk].size, tc)}
+    if reference:
+        line.update({"impl": "reference", "value": cpu["value"], "steps": 1, "warmup": 0,
+                     "ms_per_step": 1e3 * npts / cpu["value"], "cpu_baseline": cpu,
+                     "e2e": {"value": cpu["value"], "unit": "points/s",
+                             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        print(json.dumps(line), flush=True)
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    from cgfd3d_gb300 import media
+    K, W = args.steps, max(args.warmup, 0)
+    for _ in range(W):
+        media.layer_el_iso(m, X, Y, Z)
+    ts = []
+    for _ in range(K):
+        t0 = time.perf_counter()
+        media.layer_el_iso(m, X, Y, Z)
+        ts.append(time.perf_counter() - t0)
+    t = sorted(ts)[len(ts) // 2]
+    line.update({"value": npts / t, "steps": K, "warmup": W, "ms_per_step": 1e3 * t,
+                 "e2e": {"value": npts / t, "unit": "points/s",
+                         "h2d_bytes_per_step": 3 * npts * 4 + m["rec"].nbytes,
+                         "d2h_bytes_per_step": 3 * npts * 4,
+                         "how": "host coordinates to host media, median of K calls"},
+                 "gpu_launches": K})
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -757,6 +848,8 @@ def main():
         return run_slices(args)
     if args.workload == "locate":
         return run_locate(args)
+    if args.workload == "media":
+        return run_media(args)
     return run_ours(args)
 
 

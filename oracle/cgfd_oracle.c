@@ -43,6 +43,7 @@
  * Multi-threaded with pthreads (one slab of k-planes per thread) so that it
  * can serve as the host-core baseline.
  */
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -1878,4 +1879,125 @@ int oracle_locate(int nx, int ny, int nz, const float *x3d, const float *y3d,
     zout[q] = sz;
   }
   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* layered media: elastic isotropic model discretised with the "loc" method  */
+/* ------------------------------------------------------------------------ */
+
+/* Restates media_layer2model_el_iso with "loc" (media/media_layer2model.cpp:
+ * 140-190, 422-560, 1334-1384) and its helpers (media/media_utility.cpp:
+ * 53-55, 88-140, 173-209).  rec: [NI][NY][NX][10] = elevation, rho,
+ * rho_grad, rho_pow, vp, vp_grad, vp_pow, vs, vs_grad, vs_pow.  Returns 1
+ * when a point lies outside the interface mesh or vp <= sqrt(2) vs (where
+ * the reference exits), else 0. */
+
+static float lay_bilinear(const float *xv, int NX, const float *yv, int NY,
+                          const float *v, int stride, float xq, float yq)
+{
+  int ix = (xq - xv[0]) / (xv[1] - xv[0]);
+  int iy = (yq - yv[0]) / (yv[1] - yv[0]);
+  if (ix < 0 || iy < 0) return FLT_MAX;
+  int indx = iy * NX + ix;
+  if (ix == NX - 1 || iy == NY - 1) return v[indx * stride];
+  float area = (xv[ix + 1] - xv[ix]) * (yv[iy + 1] - yv[iy]);
+  float vq = v[indx * stride] * (xv[ix + 1] - xq) * (yv[iy + 1] - yq) +
+             v[(indx + 1) * stride] * (xq - xv[ix]) * (yv[iy + 1] - yq) +
+             v[(indx + NX) * stride] * (xv[ix + 1] - xq) * (yq - yv[iy]) +
+             v[(indx + 1 + NX) * stride] * (xq - xv[ix]) * (yq - yv[iy]);
+  vq /= area;
+  return vq;
+}
+
+static int lay_last_ge(float value, const float *x, int n)
+{
+  if (value > x[0]) return -1;
+  float dist = FLT_MAX;
+  int indx = -1;
+  for (int i = 0; i < n; i++) {
+    if (x[i] == -FLT_MAX) continue;
+    float d = x[i] - value;
+    if (d < 0) break;
+    if (d >= 0 && d <= dist) { dist = d; indx = i; }
+  }
+  return indx;
+}
+
+static int lay_first_ge(float value, const float *x, int n)
+{
+  float dist = FLT_MAX;
+  int idx = -1;
+  for (int i = 0; i < n; i++) {
+    if (x[i] == -FLT_MAX) continue;
+    float d = x[i] - value;
+    if (d >= 0 && d <= dist) {
+      if (d <= 1e-6) return i;
+      dist = d;
+      idx = i;
+    }
+  }
+  return idx;
+}
+
+/* value + pow(dz, power) * grad of one property of layer mi at (x, y) */
+static float lay_value(const float *xv, int NX, const float *yv, int NY, const float *rec,
+                       size_t slice, int mi, int c, float dz, float x, float y)
+{
+  float v = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + c, 10, x, y);
+  float g = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + c + 1, 10, x, y);
+  float pw = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + c + 2, 10, x, y);
+  return v + pow(dz, pw) * g;
+}
+
+int oracle_layer_el_iso_loc(int NI, int NX, int NY, float MINX, float MINY, float DX,
+                            float DY, const float *rec, int nx, int ny, int nz,
+                            const float *x3d, const float *y3d, const float *z3d,
+                            float *lam, float *mu, float *rho)
+{
+  float *xv = malloc(NX * sizeof(float)), *yv = malloc(NY * sizeof(float));
+  float *elev = malloc(NI * sizeof(float));
+  for (int i = 0; i < NX; i++) xv[i] = MINX + DX * i;
+  for (int j = 0; j < NY; j++) yv[j] = MINY + DY * j;
+  const float maxx = MINX + (NX - 1) * DX, maxy = MINY + (NY - 1) * DY;
+  const size_t slice = (size_t)NX * NY;
+  int bad = 0;
+  size_t vol = (size_t)nx * ny * nz;
+  for (size_t q = 0; q < vol && !bad; q++) {
+    float x = x3d[q], y = y3d[q], z = z3d[q];
+    if (x < MINX || x > maxx || y < MINY || y > maxy) { bad = 1; break; }
+    for (int n = 0; n < NI; n++)
+      elev[n] = lay_bilinear(xv, NX, yv, NY, rec + n * slice * 10, 10, x, y);
+    int mi = lay_last_ge(z, elev, NI);
+    float var[3];          /* rho, vp, vs */
+    if (mi == -1) {
+      mi = lay_last_ge(elev[0], elev, NI);
+      var[0] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 1, 10, x, y);
+      var[1] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 4, 10, x, y);
+      var[2] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 7, 10, x, y);
+    } else {
+      float dz = elev[mi] - z;
+      var[1] = lay_value(xv, NX, yv, NY, rec, slice, mi, 4, dz, x, y);
+      var[2] = lay_value(xv, NX, yv, NY, rec, slice, mi, 7, dz, x, y);
+      var[0] = lay_value(xv, NX, yv, NY, rec, slice, mi, 1, dz, x, y);
+      if (var[1] <= var[2] * sqrt(2)) { bad = 1; break; }
+      if (fabsf(dz - 0.0f) < FLT_EPSILON) {
+        int m2 = lay_first_ge(z, elev, NI) - 1;
+        if (m2 >= 0) {
+          float dz2 = elev[m2] - z;
+          float vp_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 4, dz2, x, y);
+          float vs_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 7, dz2, x, y);
+          float rho_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 1, dz2, x, y);
+          var[0] = (var[0] + rho_top) / 2.0;
+          var[1] = (var[1] + vp_top) / 2.0;
+          var[2] = (var[2] + vs_top) / 2.0;
+        }
+      }
+    }
+    float vp = var[1], vs = var[2], r = var[0];
+    mu[q] = vs * vs * r;
+    lam[q] = vp * vp * r - 2.0 * mu[q];
+    rho[q] = r;
+  }
+  free(xv); free(yv); free(elev);
+  return bad;
 }

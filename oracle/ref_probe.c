@@ -26,12 +26,29 @@
  *                 n x { float x, y, z; int is_depth; }
  *       <output>: n x { int is_here, si, sj, sk; float sx_inc, sy_inc,
  *                       sz_inc, z; }   (z after the depth conversion)
+ *
+ *   ref_probe layer <md3lay> <grid> <method> <output>
+ *       an elastic isotropic layered model discretised on a curvilinear
+ *       grid by media_layer2model_el_iso (media/media_layer2model.cpp:
+ *       140-190) with the equivalent-medium method <method> (loc, har, ari).
+ *       <grid>:   int nx, ny, nz; float x3d, y3d, z3d [nz][ny][nx]
+ *       <output>: float lambda, mu, rho [nz][ny][nx]
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "io_funcs.h"
+
+/* the reference's layered-model discretisation (C linkage,
+ * media/media_layer2model.hpp:63-76); grid type 3 is GRID_CURV
+ * (media/media_utility.hpp:50) */
+int media_layer2model_el_iso(float *lam3d, float *mu3d, float *rho3d,
+                             const float *x3d, const float *y3d, const float *z3d,
+                             size_t nx, size_t ny, size_t nz, int grid_type,
+                             const char *in_3lay_file,
+                             const char *equivalent_medium_method, int myid);
+#define PROBE_GRID_CURV 3
 
 static void rd(void *p, size_t n, FILE *fp)
 {
@@ -178,10 +195,38 @@ static int probe_locate(const char *in, const char *out)
   return 0;
 }
 
+static int probe_layer(const char *lay, const char *grid, const char *method,
+                       const char *out)
+{
+  FILE *fp = fopen(grid, "rb");
+  if (!fp) return 2;
+  int d[3];
+  rd(d, sizeof d, fp);
+  size_t vol = (size_t)d[0] * d[1] * d[2];
+  float *x = malloc(vol * 4), *y = malloc(vol * 4), *z = malloc(vol * 4);
+  rd(x, vol * 4, fp);
+  rd(y, vol * 4, fp);
+  rd(z, vol * 4, fp);
+  fclose(fp);
+  float *lam = calloc(vol, 4), *mu = calloc(vol, 4), *rho = calloc(vol, 4);
+  media_layer2model_el_iso(lam, mu, rho, x, y, z, d[0], d[1], d[2], PROBE_GRID_CURV, lay,
+                           method, 0);
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  fwrite(lam, 4, vol, fo);
+  fwrite(mu, 4, vol, fo);
+  fwrite(rho, 4, vol, fo);
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
   if (argc == 4 && strcmp(argv[1], "locate") == 0) return probe_locate(argv[2], argv[3]);
-  fprintf(stderr, "usage: ref_probe sac|locate <input> <output>\n");
+  if (argc == 6 && strcmp(argv[1], "layer") == 0)
+    return probe_layer(argv[2], argv[3], argv[4], argv[5]);
+  fprintf(stderr, "usage: ref_probe sac|locate <input> <output> | "
+                  "layer <md3lay> <grid> <method> <output>\n");
   return 2;
 }
