@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--media-method", default="har", choices=["loc", "har", "ari"],
+                    help="equivalent-medium method of --workload media")
     ap.add_argument("--workload", default="topo", choices=sorted(WORKLOADS))
     ap.add_argument("--nshot", type=int, default=64,
                     help="batch workload: shots per GPU")
@@ -752,8 +754,10 @@ def run_locate(args, reference=False):
 
 def layered_model(X, Y, nlayer=4, seed=13):
     """A layered elastic isotropic model over the grid's area: undulating
-    interfaces from 500 m above sea level down to -15 km, velocities and
-    densities increasing with depth, gradients with power laws."""
+    interfaces from 3 km above sea level down to -15 km, velocities and
+    densities increasing with depth, perturbed by 2 % per mesh point; linear
+    vp and rho gradients, as the reference's example layered models have
+    (example/prep_medium/gen_eliso_lay.m: powers 1, no vs gradient)."""
     import numpy as np
     rng = np.random.default_rng(seed)
     NX, NY = 81, 81
@@ -770,15 +774,16 @@ def layered_model(X, Y, nlayer=4, seed=13):
         r = lambda a: a * (1 + 0.02 * rng.uniform(-1, 1, XX.shape))
         recs.append(np.stack([e, r(rho), np.full_like(XX, 0.02), np.full_like(XX, 1.0),
                               r(vp), np.full_like(XX, 0.05), np.full_like(XX, 1.0),
-                              r(vs), np.full_like(XX, 0.03), np.full_like(XX, 0.9)], -1))
+                              r(vs), np.full_like(XX, 0.0), np.full_like(XX, 1.0)], -1))
     return dict(NI=len(tops), NX=NX, NY=NY, MINX=minx, MINY=miny, DX=dx, DY=dy,
                 rec=np.stack(recs).astype(np.float32))
 
 
 def run_media(args, reference=False):
     """Media discretisation: a 4-interface layered elastic isotropic model
-    onto the topography grid with the "loc" method, grid points per second
-    (host coordinates in, host lambda/mu/rho out)."""
+    onto the topography grid with the equivalent-medium method
+    --media-method, grid points per second (host coordinates in, host
+    lambda/mu/rho out)."""
     import numpy as np
     from types import SimpleNamespace
     from cgfd3d_gb300 import models
@@ -795,18 +800,19 @@ def run_media(args, reference=False):
             "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": "layered elastic isotropic model (4 interfaces, "
                        "81x81 mesh) onto the topography grid %dx%dx%d (padded), "
-                       "method loc" % (args.ni, args.nj, args.nk),
+                       "method %s" % (args.ni, args.nj, args.nk, args.media_method),
                        "parallelism": "single"}}
     if reference or not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle
-        kk = 4                                 # a slab of 4 k-planes
+        cw = 96                                # a block of 96 x 96 full-depth columns
+        sx, sy, sz = [np.ascontiguousarray(a[:, :cw, :cw]) for a in (X, Y, Z)]
         t0 = time.perf_counter()
-        oracle.layer_el_iso_loc(m, X[:kk], Y[:kk], Z[:kk])
+        oracle.layer_el_iso(m, sx, sy, sz, args.media_method)
         tc = time.perf_counter() - t0
-        cpu = {"value": X[:kk].size / tc, "unit": "points/s", "cores": 1, "kind": "port",
-               "sample": "%d k-planes (%d points), C oracle port, 1 thread, %.2f s"
-                         % (kk, X[:kk].size, tc)}
+        cpu = {"value": sx.size / tc, "unit": "points/s", "cores": 1, "kind": "port",
+               "sample": "%dx%d full-depth columns (%d points), C oracle port, 1 thread, "
+                         "%.2f s" % (cw, cw, sx.size, tc)}
     if reference:
         line.update({"impl": "reference", "value": cpu["value"], "steps": 1, "warmup": 0,
                      "ms_per_step": 1e3 * npts / cpu["value"], "cpu_baseline": cpu,
@@ -819,11 +825,11 @@ def run_media(args, reference=False):
     from cgfd3d_gb300 import media
     K, W = args.steps, max(args.warmup, 0)
     for _ in range(W):
-        media.layer_el_iso(m, X, Y, Z)
+        media.layer_el_iso(m, X, Y, Z, args.media_method)
     ts = []
     for _ in range(K):
         t0 = time.perf_counter()
-        media.layer_el_iso(m, X, Y, Z)
+        media.layer_el_iso(m, X, Y, Z, args.media_method)
         ts.append(time.perf_counter() - t0)
     t = sorted(ts)[len(ts) // 2]
     line.update({"value": npts / t, "steps": K, "warmup": W, "ms_per_step": 1e3 * t,
@@ -831,7 +837,7 @@ def run_media(args, reference=False):
                          "h2d_bytes_per_step": 3 * npts * 4 + m["rec"].nbytes,
                          "d2h_bytes_per_step": 3 * npts * 4,
                          "how": "host coordinates to host media, median of K calls"},
-                 "gpu_launches": K})
+                 "gpu_launches": K * (1 if args.media_method == "loc" else 4)})
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

@@ -12,6 +12,18 @@
  * above for points on an interface (:119-140), then mu = vs^2 rho and
  * lambda = vp^2 rho - 2 mu.  Here one thread does one point in the same
  * float/double order; the file is compiled with --fmad=false.
+ *
+ * The "har" and "ari" methods (media/media_layer2model.cpp:1984-2190) start
+ * from "loc" and recompute each interior point whose cell -- the hexahedron
+ * of the eight half-grid points (cell centres, media/media_utility.cpp:
+ * 656-760) around it -- touches more than one layer: the cell is sampled at
+ * 9^3 points (media/media_utility.cpp:627-654) and rho is averaged
+ * arithmetically, kappa and mu harmonically ("har") or lambda and mu
+ * arithmetically ("ari").  Here k_layer_mark gives every half-grid point its
+ * layer, k_layer_mixed lists the points whose eight cell vertices disagree,
+ * and k_layer_avg gives each listed point to one thread, which adds its
+ * samples into the running sums in the reference's sample order, so the
+ * float sums round as the reference's do.
  */
 #include <cuda_runtime.h>
 
@@ -19,6 +31,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 
 #include "../../include/cgfd3d_gpu.h"
 
@@ -42,26 +55,48 @@ struct LayerMesh {
   const float *rec;     /* [NI][NY][NX][10] */
 };
 
-__device__ float lay_bilinear(const LayerMesh &L, int col, int layer, float xq, float yq)
+/* Bilinear interpolation on the interfaces' mesh (BilinearInterpolation,
+ * media/media_utility.cpp:173-209), split in two: the cell and the weight
+ * differences of a point, computed once, then the interpolation of any
+ * column of any layer there -- the reference computes the same cell and
+ * differences for every column, so the values are the same bits. */
+struct LayW {
+  int indx, edge, ok;
+  float wxb, wxa, wyb, wya, area;
+};
+
+__device__ LayW lay_weights(const LayerMesh &L, float xq, float yq)
 {
+  LayW w;
   const float x0 = L.MINX, x1 = L.MINX + L.DX, y0 = L.MINY, y1 = L.MINY + L.DY;
   int ix = (int)((xq - x0) / (x1 - x0));
   int iy = (int)((yq - y0) / (y1 - y0));
-  if (ix < 0 || iy < 0) return FLT_MAX;
+  w.ok = !(ix < 0 || iy < 0);
   /* the caller keeps (xq, yq) inside the mesh; an index rounded past its
    * last point is held there (the reference would read past its arrays) */
-  ix = ix > L.NX - 1 ? L.NX - 1 : ix;
-  iy = iy > L.NY - 1 ? L.NY - 1 : iy;
-  const float *v = L.rec + (size_t)layer * L.NX * L.NY * 10 + col;
-  const int indx = iy * L.NX + ix;
-  if (ix == L.NX - 1 || iy == L.NY - 1) return v[indx * 10];
+  ix = ix < 0 ? 0 : ix > L.NX - 1 ? L.NX - 1 : ix;
+  iy = iy < 0 ? 0 : iy > L.NY - 1 ? L.NY - 1 : iy;
+  w.indx = iy * L.NX + ix;
+  w.edge = ix == L.NX - 1 || iy == L.NY - 1;
   const float xa = L.MINX + L.DX * ix, xb = L.MINX + L.DX * (ix + 1);
   const float ya = L.MINY + L.DY * iy, yb = L.MINY + L.DY * (iy + 1);
-  const float area = (xb - xa) * (yb - ya);
-  float vq = v[indx * 10] * (xb - xq) * (yb - yq) + v[(indx + 1) * 10] * (xq - xa) * (yb - yq) +
-             v[(indx + L.NX) * 10] * (xb - xq) * (yq - ya) +
-             v[(indx + 1 + L.NX) * 10] * (xq - xa) * (yq - ya);
-  vq /= area;
+  w.wxb = xb - xq;
+  w.wxa = xq - xa;
+  w.wyb = yb - yq;
+  w.wya = yq - ya;
+  w.area = (xb - xa) * (yb - ya);
+  return w;
+}
+
+__device__ float lay_interp(const LayerMesh &L, const LayW &w, int col, int layer)
+{
+  if (!w.ok) return FLT_MAX;
+  const float *v = L.rec + (size_t)layer * L.NX * L.NY * 10 + col;
+  const int indx = w.indx;
+  if (w.edge) return v[indx * 10];
+  float vq = v[indx * 10] * w.wxb * w.wyb + v[(indx + 1) * 10] * w.wxa * w.wyb +
+             v[(indx + L.NX) * 10] * w.wxb * w.wya + v[(indx + 1 + L.NX) * 10] * w.wxa * w.wya;
+  vq /= w.area;
   return vq;
 }
 
@@ -95,13 +130,83 @@ __device__ int lay_first_ge(float value, const float *x, int n)
   return idx;
 }
 
-/* value + pow(dz, power) * gradient of property column c of a layer */
-__device__ float lay_value(const LayerMesh &L, int layer, int c, float dz, float x, float y)
+/* value + pow(dz, power) * gradient of property column c of a layer, in
+ * double as the reference's std::pow(float, float) promotes.  Two cases skip
+ * the double pow and give the same bits: pow(dz, 1) is dz, and dz * g of two
+ * floats is exact in double, so one double fma rounds v + dz g as the
+ * reference's multiply-then-add does; a zero gradient with a power in [0, 8]
+ * (pow finite for any float dz >= 0) adds a zero of the gradient's sign,
+ * which the float add v + g gives exactly. */
+__device__ float lay_value(const LayerMesh &L, const LayW &w, int layer, int c, float dz)
 {
-  const float v = lay_bilinear(L, c, layer, x, y);
-  const float g = lay_bilinear(L, c + 1, layer, x, y);
-  const float pw = lay_bilinear(L, c + 2, layer, x, y);
+  const float v = lay_interp(L, w, c, layer);
+  const float g = lay_interp(L, w, c + 1, layer);
+  const float pw = lay_interp(L, w, c + 2, layer);
+  if (pw == 1.0f) return (float)fma((double)dz, (double)g, (double)v);
+  if (g == 0.0f && pw >= 0.0f && pw <= 8.0f) return v + g;
   return (float)((double)v + pow((double)dz, (double)pw) * (double)g);
+}
+
+/* vp <= sqrt(2) vs, compared in double as the reference does; a float
+ * product within 2^-20 of the double one decides all but the points within
+ * that margin, which take the double comparison. */
+__device__ bool lay_vp_low(float vp, float vs)
+{
+  const float t = vs * 1.41421356f, mg = fabsf(t) * 0x1p-20f;
+  if (vp > t + mg) return false;
+  if (vp < t - mg) return true;
+  return (double)vp <= (double)vs * sqrt(2.0);
+}
+
+/* lambda = vp vp rho - 2.0 mu as the reference rounds it (the float product
+ * minus 2 mu in double, then to float).  The double difference of two floats
+ * is exact, or the smaller is below 2^-28 of the larger and both roundings
+ * give the larger: the float subtraction gives the same bits while 2 mu is
+ * finite in float. */
+__device__ float lay_lambda(float vp, float r, float m)
+{
+  const float a = vp * vp * r;
+  if (fabsf(m) < 1e37f) return a - 2.0f * m;
+  return (float)((double)a - 2.0 * (double)m);
+}
+
+/* rho, vp, vs of one point (AssignLayerMediaPara2Point with
+ * CalPointValue_layer, media/media_layer2model.cpp:422-560); 0, or 1 outside
+ * the mesh, 2 where vp <= sqrt(2) vs (the reference exits on both). */
+__device__ int lay_point(const LayerMesh &L, float x, float y, float z, float *elev, float &r,
+                         float &vp, float &vs)
+{
+  const float maxx = L.MINX + (L.NX - 1) * L.DX, maxy = L.MINY + (L.NY - 1) * L.DY;
+  if (x < L.MINX || x > maxx || y < L.MINY || y > maxy) return 1;
+  const LayW w = lay_weights(L, x, y);
+  for (int n = 0; n < L.NI; n++) elev[n] = lay_interp(L, w, 0, n);
+  int mi = lay_last_ge(z, elev, L.NI);
+  if (mi == -1) {
+    mi = lay_last_ge(elev[0], elev, L.NI);
+    if (mi < 0) return 1;   /* only a NaN elevation or coordinate gets here */
+    r = lay_interp(L, w, 1, mi);
+    vp = lay_interp(L, w, 4, mi);
+    vs = lay_interp(L, w, 7, mi);
+    return 0;
+  }
+  const float dz = elev[mi] - z;
+  vp = lay_value(L, w, mi, 4, dz);
+  vs = lay_value(L, w, mi, 7, dz);
+  r = lay_value(L, w, mi, 1, dz);
+  if (lay_vp_low(vp, vs)) return 2;
+  if (fabsf(dz - 0.0f) < FLT_EPSILON) {
+    const int m2 = lay_first_ge(z, elev, L.NI) - 1;
+    if (m2 >= 0) {
+      const float dz2 = elev[m2] - z;
+      const float vp_top = lay_value(L, w, m2, 4, dz2);
+      const float vs_top = lay_value(L, w, m2, 7, dz2);
+      const float rho_top = lay_value(L, w, m2, 1, dz2);
+      r = (float)((double)(r + rho_top) / 2.0);
+      vp = (float)((double)(vp + vp_top) / 2.0);
+      vs = (float)((double)(vs + vs_top) / 2.0);
+    }
+  }
+  return 0;
 }
 
 __global__ void k_layer_el_iso_loc(LayerMesh L, long long vol, const float *__restrict__ x3d,
@@ -109,80 +214,211 @@ __global__ void k_layer_el_iso_loc(LayerMesh L, long long vol, const float *__re
                                    const float *__restrict__ z3d, float *lam, float *mu,
                                    float *rho, int *bad)
 {
-  const float maxx = L.MINX + (L.NX - 1) * L.DX, maxy = L.MINY + (L.NY - 1) * L.DY;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
        q += (long long)gridDim.x * blockDim.x) {
-    const float x = x3d[q], y = y3d[q], z = z3d[q];
-    if (x < L.MINX || x > maxx || y < L.MINY || y > maxy) {
-      atomicOr(bad, 1);
+    float elev[LAY_MAX], r, vp, vs;
+    const int st = lay_point(L, x3d[q], y3d[q], z3d[q], elev, r, vp, vs);
+    if (st) {
+      atomicOr(bad, st);
       continue;
-    }
-    float elev[LAY_MAX];
-    for (int n = 0; n < L.NI; n++) elev[n] = lay_bilinear(L, 0, n, x, y);
-    int mi = lay_last_ge(z, elev, L.NI);
-    float r, vp, vs;
-    if (mi == -1) {
-      mi = lay_last_ge(elev[0], elev, L.NI);
-      r = lay_bilinear(L, 1, mi, x, y);
-      vp = lay_bilinear(L, 4, mi, x, y);
-      vs = lay_bilinear(L, 7, mi, x, y);
-    } else {
-      const float dz = elev[mi] - z;
-      vp = lay_value(L, mi, 4, dz, x, y);
-      vs = lay_value(L, mi, 7, dz, x, y);
-      r = lay_value(L, mi, 1, dz, x, y);
-      if ((double)vp <= (double)vs * sqrt(2.0)) {
-        atomicOr(bad, 2);
-        continue;
-      }
-      if (fabsf(dz - 0.0f) < FLT_EPSILON) {
-        const int m2 = lay_first_ge(z, elev, L.NI) - 1;
-        if (m2 >= 0) {
-          const float dz2 = elev[m2] - z;
-          const float vp_top = lay_value(L, m2, 4, dz2, x, y);
-          const float vs_top = lay_value(L, m2, 7, dz2, x, y);
-          const float rho_top = lay_value(L, m2, 1, dz2, x, y);
-          r = (float)((double)(r + rho_top) / 2.0);
-          vp = (float)((double)(vp + vp_top) / 2.0);
-          vs = (float)((double)(vs + vs_top) / 2.0);
-        }
-      }
     }
     const float m = vs * vs * r;
     mu[q] = m;
-    lam[q] = (float)((double)(vp * vp * r) - 2.0 * (double)m);
+    lam[q] = lay_lambda(vp, r, m);
     rho[q] = r;
+  }
+}
+
+/* half-grid coordinate at q (i, j, k): the mean of the cell's eight corners
+ * above q, or the grid point itself on the last index of an axis */
+__device__ float lay_half(const float *__restrict__ G, long long q, int i, int j, int k, int nx,
+                          int ny, int nz)
+{
+  if (i >= nx - 1 || j >= ny - 1 || k >= nz - 1) return G[q];
+  const long long line = nx, sl = (long long)nx * ny;
+  const float s = G[q] + G[q + 1] + G[q + line + 1] + G[q + line] + G[q + sl] + G[q + sl + 1] +
+                  G[q + sl + line + 1] + G[q + line + sl];
+  return (float)((double)s / 8.0);
+}
+
+/* layer number of every half-grid point (MarkInterfaceNumber,
+ * media/media_layer2model.cpp:1515-1598) */
+__global__ void k_layer_mark(LayerMesh L, int nx, int ny, int nz, const float *__restrict__ x3d,
+                             const float *__restrict__ y3d, const float *__restrict__ z3d,
+                             signed char *mat)
+{
+  const long long vol = (long long)nx * ny * nz;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % nx), j = (int)((q / nx) % ny), k = (int)(q / ((long long)nx * ny));
+    const float hx = lay_half(x3d, q, i, j, k, nx, ny, nz);
+    const float hy = lay_half(y3d, q, i, j, k, nx, ny, nz);
+    const float hz = lay_half(z3d, q, i, j, k, nx, ny, nz);
+    float elev[LAY_MAX];
+    const LayW w = lay_weights(L, hx, hy);
+    for (int n = 0; n < L.NI; n++) elev[n] = lay_interp(L, w, 0, n);
+    int mi = lay_last_ge(hz, elev, L.NI);
+    if (mi == -1) mi = lay_last_ge(elev[0], elev, L.NI);
+    mat[q] = (signed char)mi;
+  }
+}
+
+/* interior points whose eight cell vertices hold more than one layer (and
+ * none -1: NumOfValues, media/media_utility.cpp:610-624) */
+__global__ void k_layer_mixed(int nx, int ny, int nz, const signed char *__restrict__ mat,
+                              long long *list, unsigned long long *count)
+{
+  const long long vol = (long long)nx * ny * nz, line = nx, sl = (long long)nx * ny;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q % nx), j = (int)((q / nx) % ny), k = (int)(q / sl);
+    if (i < 1 || i > nx - 2 || j < 1 || j > ny - 2 || k < 1 || k > nz - 2) continue;
+    const int v[8] = {mat[q - 1 - line - sl], mat[q - line - sl], mat[q - sl], mat[q - 1 - sl],
+                      mat[q - 1 - line], mat[q - line], mat[q], mat[q - 1]};
+    unsigned long long seen = 0ull;   /* layer numbers are below LAY_MAX = 64 */
+    int num = 0, neg = 0;
+    for (int n = 0; n < 8; n++) {
+      if (v[n] < 0) { neg = 1; break; }
+      const unsigned long long bit = 1ull << v[n];
+      if (!(seen & bit)) { seen |= bit; num++; }
+    }
+    if (!neg && num > 1) list[atomicAdd(count, 1ull)] = q;
+  }
+}
+
+#define LAY_NG 8
+#define LAY_NSG ((LAY_NG + 1) * (LAY_NG + 1) * (LAY_NG + 1))
+
+/* a point's equivalent medium from 9^3 samples of its cell, one thread per
+ * listed point (every thread runs the same 729 samples, so a warp stays
+ * converged but for the layer lookups).  method 1: har, 2: ari
+ * (media/media_layer2model.cpp:1984-2190). */
+__global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int nx, int ny,
+                                                   int nz, const float *__restrict__ x3d,
+                                                   const float *__restrict__ y3d,
+                                                   const float *__restrict__ z3d,
+                                                   const long long *__restrict__ list,
+                                                   const unsigned long long *count, float *lam,
+                                                   float *mu, float *rho, int *bad)
+{
+  const long long nlist = (long long)*count, line = nx, sl = (long long)nx * ny;
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nlist;
+       w += (long long)gridDim.x * blockDim.x) {
+    const long long q = list[w];
+    /* the cell's eight half-grid vertices, in the reference's order */
+    const long long c[8] = {q - 1 - line - sl, q - 1 - sl, q - sl, q - line - sl,
+                            q - 1 - line, q - 1, q, q - line};
+    float vx[8], vy[8], vz[8];
+#pragma unroll
+    for (int n = 0; n < 8; n++) {
+      const long long p = c[n];
+      const int i = (int)(p % nx), j = (int)((p / nx) % ny), k = (int)(p / sl);
+      vx[n] = lay_half(x3d, p, i, j, k, nx, ny, nz);
+      vy[n] = lay_half(y3d, p, i, j, k, nx, ny, nz);
+      vz[n] = lay_half(z3d, p, i, j, k, nx, ny, nz);
+    }
+    float s_rho = 0.0f, s_a = 0.0f, s_b = 0.0f;   /* rho; kappa or lambda; mu */
+    int st = 0;
+    const float ng = (float)LAY_NG;
+    for (int kk = 0; kk <= LAY_NG; kk++)
+      for (int jj = 0; jj <= LAY_NG; jj++)
+        for (int ii = 0; ii <= LAY_NG; ii++) {
+          const float fi = (float)ii, fj = (float)jj, fk = (float)kk;
+          float pt[3];
+#pragma unroll
+          for (int d = 0; d < 3; d++) {
+            const float *v = d == 0 ? vx : d == 1 ? vy : vz;
+            const float ly00 = v[0] + (v[1] - v[0]) / ng * fj;
+            const float ly10 = v[3] + (v[2] - v[3]) / ng * fj;
+            const float ly01 = v[4] + (v[5] - v[4]) / ng * fj;
+            const float ly11 = v[7] + (v[6] - v[7]) / ng * fj;
+            const float lxy0 = ly00 + (ly10 - ly00) / ng * fi;
+            const float lxy1 = ly01 + (ly11 - ly01) / ng * fi;
+            pt[d] = lxy0 + (lxy1 - lxy0) / ng * fk;
+          }
+          float elev[LAY_MAX], r = 1.f, vp = 1.f, vs = 1.f;
+          st |= lay_point(L, pt[0], pt[1], pt[2], elev, r, vp, vs);
+          const float m = vs * vs * r;
+          const float lambda = lay_lambda(vp, r, m);
+          s_rho = s_rho + r;
+          if (method == 1) {
+            s_a = (float)((double)s_a + 1.0 / ((double)lambda + 2.0 / 3.0 * (double)m));
+            s_b = (float)((double)s_b + 1.0 / (double)m);
+          } else {
+            s_a = s_a + lambda;
+            s_b = s_b + m;
+          }
+        }
+    if (st) {
+      atomicOr(bad, st);
+    } else if (method == 1) {
+      const float hm = (float)((double)LAY_NSG / (double)s_b);
+      const float hk = (float)((double)LAY_NSG / (double)s_a);
+      lam[q] = (float)((double)hk - 2.0 / 3.0 * (double)hm);
+      mu[q] = hm;
+      rho[q] = (float)((double)s_rho / (double)LAY_NSG);
+    } else {
+      lam[q] = (float)((double)s_a / (double)LAY_NSG);
+      mu[q] = (float)((double)s_b / (double)LAY_NSG);
+      rho[q] = (float)((double)s_rho / (double)LAY_NSG);
+    }
   }
 }
 
 extern "C" int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY,
                                        float DX, float DY, const float *rec, int nx, int ny,
                                        int nz, const float *x3d, const float *y3d,
-                                       const float *z3d, float *lam, float *mu, float *rho)
+                                       const float *z3d, const char *method, float *lam,
+                                       float *mu, float *rho)
 {
+  int meth = -1;
+  if (method && strcmp(method, "loc") == 0) meth = 0;
+  if (method && strcmp(method, "har") == 0) meth = 1;
+  if (method && strcmp(method, "ari") == 0) meth = 2;
+  if (meth < 0)
+    return lay_err(CGFD_EINVAL, "layered model: equivalent medium method %s (loc, har or ari)",
+                   method ? method : "(null)");
   if (NI < 1 || NI > LAY_MAX || NX < 2 || NY < 2 || !(DX > 0) || !(DY > 0))
     return lay_err(CGFD_EINVAL, "layered model: %d interfaces on a %dx%d mesh (1..%d "
                    "interfaces, at least 2x2 points, positive spacing)", NI, NX, NY, LAY_MAX);
   if (!rec || !x3d || !y3d || !z3d || !lam || !mu || !rho || nx < 1 || ny < 1 || nz < 1)
     return lay_err(CGFD_EINVAL, "layered model: missing array or empty grid");
   const size_t vol = (size_t)nx * ny * nz, nrec = (size_t)NI * NX * NY * 10;
-  float *d = nullptr;
+  /* device buffer: x, y, z, lambda, mu, rho, the model; then for har/ari the
+   * layer numbers (bytes) and the list of points to average */
+  const size_t fl = 6 * vol + nrec, extra = meth ? vol * sizeof(long long) + vol + 16 : 0;
+  char *d = nullptr;
   int *d_bad = nullptr, bad = 0;
   cudaStream_t st = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d, (6 * vol + nrec) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d, fl * sizeof(float) + extra);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int));
-  float *dx = d, *dy = d + vol, *dz = d + 2 * vol, *dl = d + 3 * vol, *dm = d + 4 * vol,
-        *dr = d + 5 * vol, *drec = d + 6 * vol;
+  float *df = (float *)d;
+  float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *dl = df + 3 * vol, *dm = df + 4 * vol,
+        *dr = df + 5 * vol, *drec = df + 6 * vol;
+  /* the list (8-byte aligned: fl * 4 rounded up), its counter, the layer numbers */
+  const size_t off = (fl * sizeof(float) + 7) & ~(size_t)7;
+  long long *dlist = meth ? (long long *)(d + off) : nullptr;
+  unsigned long long *dcount = meth ? (unsigned long long *)(d + off + vol * 8) : nullptr;
+  signed char *dmat = meth ? (signed char *)(d + off + vol * 8 + 8) : nullptr;
+  if (meth && off + vol * 8 + 8 + vol > fl * sizeof(float) + extra) e = cudaErrorInvalidValue;
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+  if (e == cudaSuccess && meth) e = cudaMemsetAsync(dcount, 0, 8, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(drec, rec, nrec * 4, cudaMemcpyHostToDevice, st);
+  const LayerMesh L = {NI, NX, NY, MINX, MINY, DX, DY, drec};
   if (e == cudaSuccess) {
-    LayerMesh L = {NI, NX, NY, MINX, MINY, DX, DY, drec};
     k_layer_el_iso_loc<<<152 * 8, 256, 0, st>>>(L, (long long)vol, dx, dy, dz, dl, dm, dr,
                                                  d_bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && meth) {
+    k_layer_mark<<<152 * 8, 256, 0, st>>>(L, nx, ny, nz, dx, dy, dz, dmat);
+    k_layer_mixed<<<152 * 8, 256, 0, st>>>(nx, ny, nz, dmat, dlist, dcount);
+    k_layer_avg<<<152 * 16, 128, 0, st>>>(L, meth, nx, ny, nz, dx, dy, dz, dlist, dcount, dl,
+                                         dm, dr, d_bad);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);

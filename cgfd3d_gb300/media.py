@@ -2,13 +2,15 @@
 
 ``read_md3lay`` parses the reference's layered-model text format (.md3lay,
 media/media_read_file.cpp:22-240) for elastic isotropic models;
-``layer_el_iso`` discretises such a model on a curvilinear grid with the
-reference's "loc" method (media_layer2model_el_iso,
-media/media_layer2model.cpp:140-190, 422-560, 1334-1384) on the device
-(``cgfd_media_layer_el_iso``): per grid point the interfaces' elevations
+``layer_el_iso`` discretises such a model on a curvilinear grid on the
+device (``cgfd_media_layer_el_iso``) as the reference's
+media_layer2model_el_iso does (media/media_layer2model.cpp:140-190, 422-560,
+1334-1384, 1984-2190).  "loc": per grid point the interfaces' elevations
 interpolated at (x, y), the layer below the point, each property's value
 plus its gradient times depth-below-interface to its power, the mean of the
-two layers for points on an interface, then lambda, mu, rho.
+two layers for points on an interface, then lambda, mu, rho.  "har" / "ari":
+points whose cell touches more than one layer are recomputed from 9^3
+samples of the cell, averaged harmonically (kappa, mu) or arithmetically.
 """
 
 import ctypes as C
@@ -47,9 +49,10 @@ def read_md3lay(text):
                 DY=float(DY), rec=vals.reshape(NI, NY, NX, 10))
 
 
-def layer_el_iso(model, x3d, y3d, z3d):
+def layer_el_iso(model, x3d, y3d, z3d, method="loc"):
     """lambda, mu, rho of the model on the grid (arrays shaped like x3d),
-    computed on the device with the "loc" method."""
+    computed on the device with the equivalent-medium method "loc", "har"
+    or "ari"."""
     shape = np.shape(x3d)
     nz, ny, nx = shape
     x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
@@ -59,5 +62,5 @@ def layer_el_iso(model, x3d, y3d, z3d):
         int(model["NI"]), int(model["NX"]), int(model["NY"]), C.c_float(model["MINX"]),
         C.c_float(model["MINY"]), C.c_float(model["DX"]), C.c_float(model["DY"]),
         rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
-        *[o.ctypes.data for o in out]))
+        method.encode(), *[o.ctypes.data for o in out]))
     return tuple(out)

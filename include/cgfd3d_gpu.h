@@ -329,18 +329,23 @@ int cgfd_locator_locate(cgfd_locator_t *loc, int n, const float *x, const float 
 
 void cgfd_locator_destroy(cgfd_locator_t *loc);
 
-/* An elastic isotropic layered model discretised on a curvilinear grid
- * with the "loc" method, as media_layer2model_el_iso does
- * (media/media_layer2model.cpp:140-190, 422-560, 1334-1384): NI interfaces
- * on a uniform NX x NY mesh from (MINX, MINY) with spacing DX, DY; rec holds
+/* An elastic isotropic layered model discretised on a curvilinear grid,
+ * as media_layer2model_el_iso does (media/media_layer2model.cpp:140-190,
+ * 422-560, 1334-1384, 1984-2190; called at
+ * forward/main_curv_col_el_3d.c:328-334): NI interfaces on a uniform
+ * NX x NY mesh from (MINX, MINY) with spacing DX, DY; rec holds
  * [NI][NY][NX][10] = elevation, rho, rho_grad, rho_pow, vp, vp_grad,
- * vp_pow, vs, vs_grad, vs_pow (the .md3lay record).  Writes lam, mu, rho
- * (host, nx*ny*nz each).  A point outside the mesh or with vp <= sqrt(2) vs
- * is CGFD_EINVAL (the reference exits there). */
+ * vp_pow, vs, vs_grad, vs_pow (the .md3lay record).  method is the
+ * reference's equivalent_medium_method: "loc" (the value at each point),
+ * "har" (harmonic kappa and mu, arithmetic rho over each cell that touches
+ * two layers) or "ari" (arithmetic lambda, mu, rho there).  Writes lam, mu,
+ * rho (host, nx*ny*nz each).  A point outside the mesh or with
+ * vp <= sqrt(2) vs is CGFD_EINVAL (the reference exits there), and so is
+ * another method. */
 int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY, float DX,
                             float DY, const float *rec, int nx, int ny, int nz,
                             const float *x3d, const float *y3d, const float *z3d,
-                            float *lam, float *mu, float *rho);
+                            const char *method, float *lam, float *mu, float *rho);
 
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);

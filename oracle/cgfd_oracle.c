@@ -1892,6 +1892,8 @@ int oracle_locate(int nx, int ny, int nz, const float *x3d, const float *y3d,
  * when a point lies outside the interface mesh or vp <= sqrt(2) vs (where
  * the reference exits), else 0. */
 
+#define LAY_MAXI 64
+
 static float lay_bilinear(const float *xv, int NX, const float *yv, int NY,
                           const float *v, int stride, float xq, float yq)
 {
@@ -1949,55 +1951,213 @@ static float lay_value(const float *xv, int NX, const float *yv, int NY, const f
   return v + pow(dz, pw) * g;
 }
 
-int oracle_layer_el_iso_loc(int NI, int NX, int NY, float MINX, float MINY, float DX,
-                            float DY, const float *rec, int nx, int ny, int nz,
-                            const float *x3d, const float *y3d, const float *z3d,
-                            float *lam, float *mu, float *rho)
+typedef struct {
+  int NI, NX, NY;
+  const float *xv, *yv, *rec;
+  size_t slice;
+  float minx, maxx, miny, maxy;
+  float *elev;
+} lay_model_t;
+
+/* rho, vp, vs of one point: AssignLayerMediaPara2Point with
+ * CalPointValue_layer for ELASTIC_ISOTROPIC (media/media_layer2model.cpp:
+ * 422-560).  Returns 1 where the reference exits (outside the mesh, or
+ * vp <= sqrt(2) vs), else 0. */
+static int lay_point(const lay_model_t *m, float x, float y, float z, float *var)
 {
+  const int NI = m->NI, NX = m->NX, NY = m->NY;
+  const float *xv = m->xv, *yv = m->yv, *rec = m->rec;
+  const size_t slice = m->slice;
+  float *elev = m->elev;
+  if (x < m->minx || x > m->maxx || y < m->miny || y > m->maxy) return 1;
+  for (int n = 0; n < NI; n++)
+    elev[n] = lay_bilinear(xv, NX, yv, NY, rec + n * slice * 10, 10, x, y);
+  int mi = lay_last_ge(z, elev, NI);
+  if (mi == -1) {
+    mi = lay_last_ge(elev[0], elev, NI);
+    var[0] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 1, 10, x, y);
+    var[1] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 4, 10, x, y);
+    var[2] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 7, 10, x, y);
+    return 0;
+  }
+  float dz = elev[mi] - z;
+  var[1] = lay_value(xv, NX, yv, NY, rec, slice, mi, 4, dz, x, y);
+  var[2] = lay_value(xv, NX, yv, NY, rec, slice, mi, 7, dz, x, y);
+  var[0] = lay_value(xv, NX, yv, NY, rec, slice, mi, 1, dz, x, y);
+  if (var[1] <= var[2] * sqrt(2)) return 1;
+  if (fabsf(dz - 0.0f) < FLT_EPSILON) {
+    int m2 = lay_first_ge(z, elev, NI) - 1;
+    if (m2 >= 0) {
+      float dz2 = elev[m2] - z;
+      float vp_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 4, dz2, x, y);
+      float vs_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 7, dz2, x, y);
+      float rho_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 1, dz2, x, y);
+      var[0] = (var[0] + rho_top) / 2.0;
+      var[1] = (var[1] + vp_top) / 2.0;
+      var[2] = (var[2] + vs_top) / 2.0;
+    }
+  }
+  return 0;
+}
+
+/* the half grid of a curvilinear grid: each point but the last along an
+ * axis moved to the centre of the cell above it (media/media_utility.cpp:
+ * 656-760, GRID_CURV) */
+static void lay_half_grid(int nx, int ny, int nz, const float *G, float *H)
+{
+  const size_t line = nx, sl = (size_t)nx * ny, vol = sl * nz;
+  memcpy(H, G, vol * sizeof(float));
+  for (int k = 0; k < nz - 1; k++)
+    for (int j = 0; j < ny - 1; j++)
+      for (int i = 0; i < nx - 1; i++) {
+        size_t q = i + j * line + k * sl;
+        H[q] = (G[q] + G[q + 1] + G[q + line + 1] + G[q + line] + G[q + sl] + G[q + sl + 1] +
+                G[q + sl + line + 1] + G[q + line + sl]) / 8.0;
+      }
+}
+
+/* the layer number of each half-grid point (MarkInterfaceNumber,
+ * media/media_layer2model.cpp:1515-1598, GRID_CURV) */
+static void lay_mark(const lay_model_t *m, size_t vol, const float *Hx, const float *Hy,
+                     const float *Hz, int *mat)
+{
+  for (size_t q = 0; q < vol; q++) {
+    for (int n = 0; n < m->NI; n++)
+      m->elev[n] = lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + n * m->slice * 10, 10,
+                                Hx[q], Hy[q]);
+    int mi = lay_last_ge(Hz[q], m->elev, m->NI);
+    if (mi == -1) mi = lay_last_ge(m->elev[0], m->elev, m->NI);
+    mat[q] = mi;
+  }
+}
+
+/* distinct values among 8 layer numbers, 0 when one is -1
+ * (NumOfValues, media/media_utility.cpp:610-624) */
+static int lay_num_values(const int *v, int NI)
+{
+  int tab[LAY_MAXI] = {0}, num = 0;
+  (void)NI;
+  for (int i = 0; i < 8; i++) {
+    if (v[i] == -1) return 0;
+    if (tab[v[i]] == 0) num++;
+    tab[v[i]]++;
+  }
+  return num;
+}
+
+#define LAY_NG 8
+
+/* sample isg of the (NG+1)^3 points spanning a cell of 8 vertices
+ * (MeshSubdivide, media/media_utility.cpp:627-654) */
+static void lay_subpoint(const float (*v)[3], int i, int j, int k, float *p)
+{
+  const float ng = LAY_NG;
+  for (int d = 0; d < 3; d++) {
+    float ly00 = v[0][d] + (v[1][d] - v[0][d]) / ng * j;
+    float ly10 = v[3][d] + (v[2][d] - v[3][d]) / ng * j;
+    float ly01 = v[4][d] + (v[5][d] - v[4][d]) / ng * j;
+    float ly11 = v[7][d] + (v[6][d] - v[7][d]) / ng * j;
+    float lxy0 = ly00 + (ly10 - ly00) / ng * i;
+    float lxy1 = ly01 + (ly11 - ly01) / ng * i;
+    p[d] = lxy0 + (lxy1 - lxy0) / ng * k;
+  }
+}
+
+/* method 0: loc; 1: har (harmonic kappa and mu, arithmetic rho over the
+ * subdivided cell, media/media_layer2model.cpp:1984-2095); 2: ari
+ * (arithmetic lambda, mu, rho, :2098-2190).  har and ari start from loc
+ * and recompute the points whose cell (between the half-grid points
+ * around them) touches more than one layer. */
+int oracle_layer_el_iso(int method, int NI, int NX, int NY, float MINX, float MINY, float DX,
+                        float DY, const float *rec, int nx, int ny, int nz, const float *x3d,
+                        const float *y3d, const float *z3d, float *lam, float *mu, float *rho)
+{
+  if (NI < 1 || NI > LAY_MAXI) return 1;
   float *xv = malloc(NX * sizeof(float)), *yv = malloc(NY * sizeof(float));
   float *elev = malloc(NI * sizeof(float));
   for (int i = 0; i < NX; i++) xv[i] = MINX + DX * i;
   for (int j = 0; j < NY; j++) yv[j] = MINY + DY * j;
-  const float maxx = MINX + (NX - 1) * DX, maxy = MINY + (NY - 1) * DY;
-  const size_t slice = (size_t)NX * NY;
+  lay_model_t m = {NI, NX, NY, xv, yv, rec, (size_t)NX * NY, MINX, MINX + (NX - 1) * DX,
+                   MINY, MINY + (NY - 1) * DY, elev};
   int bad = 0;
-  size_t vol = (size_t)nx * ny * nz;
+  const size_t line = nx, sl = (size_t)nx * ny, vol = sl * nz;
   for (size_t q = 0; q < vol && !bad; q++) {
-    float x = x3d[q], y = y3d[q], z = z3d[q];
-    if (x < MINX || x > maxx || y < MINY || y > maxy) { bad = 1; break; }
-    for (int n = 0; n < NI; n++)
-      elev[n] = lay_bilinear(xv, NX, yv, NY, rec + n * slice * 10, 10, x, y);
-    int mi = lay_last_ge(z, elev, NI);
     float var[3];          /* rho, vp, vs */
-    if (mi == -1) {
-      mi = lay_last_ge(elev[0], elev, NI);
-      var[0] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 1, 10, x, y);
-      var[1] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 4, 10, x, y);
-      var[2] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 7, 10, x, y);
-    } else {
-      float dz = elev[mi] - z;
-      var[1] = lay_value(xv, NX, yv, NY, rec, slice, mi, 4, dz, x, y);
-      var[2] = lay_value(xv, NX, yv, NY, rec, slice, mi, 7, dz, x, y);
-      var[0] = lay_value(xv, NX, yv, NY, rec, slice, mi, 1, dz, x, y);
-      if (var[1] <= var[2] * sqrt(2)) { bad = 1; break; }
-      if (fabsf(dz - 0.0f) < FLT_EPSILON) {
-        int m2 = lay_first_ge(z, elev, NI) - 1;
-        if (m2 >= 0) {
-          float dz2 = elev[m2] - z;
-          float vp_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 4, dz2, x, y);
-          float vs_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 7, dz2, x, y);
-          float rho_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 1, dz2, x, y);
-          var[0] = (var[0] + rho_top) / 2.0;
-          var[1] = (var[1] + vp_top) / 2.0;
-          var[2] = (var[2] + vs_top) / 2.0;
-        }
-      }
-    }
+    if (lay_point(&m, x3d[q], y3d[q], z3d[q], var)) { bad = 1; break; }
     float vp = var[1], vs = var[2], r = var[0];
     mu[q] = vs * vs * r;
     lam[q] = vp * vp * r - 2.0 * mu[q];
     rho[q] = r;
   }
+  if (method != 0 && !bad) {
+    float *Hx = malloc(vol * sizeof(float)), *Hy = malloc(vol * sizeof(float));
+    float *Hz = malloc(vol * sizeof(float));
+    int *mat = malloc(vol * sizeof(int));
+    lay_half_grid(nx, ny, nz, x3d, Hx);
+    lay_half_grid(nx, ny, nz, y3d, Hy);
+    lay_half_grid(nx, ny, nz, z3d, Hz);
+    lay_mark(&m, vol, Hx, Hy, Hz, mat);
+    const int nsg = (LAY_NG + 1) * (LAY_NG + 1) * (LAY_NG + 1);
+    for (int j = 1; j < ny - 1 && !bad; j++)
+      for (int k = 1; k < nz - 1 && !bad; k++)
+        for (int i = 1; i < nx - 1 && !bad; i++) {
+          size_t q = i + j * line + k * sl;
+          /* the cell's vertices, in the reference's order */
+          const size_t c[8] = {q - 1 - line - sl, q - 1 - sl, q - sl, q - line - sl,
+                               q - 1 - line, q - 1, q, q - line};
+          const int v[8] = {mat[c[0]], mat[c[3]], mat[c[2]], mat[c[1]],
+                            mat[c[4]], mat[c[7]], mat[c[6]], mat[c[5]]};
+          if (lay_num_values(v, NI) <= 1) continue;
+          float vert[8][3];
+          for (int n = 0; n < 8; n++) {
+            vert[n][0] = Hx[c[n]];
+            vert[n][1] = Hy[c[n]];
+            vert[n][2] = Hz[c[n]];
+          }
+          float s_rho = 0.0, s_a = 0.0, s_b = 0.0;   /* rho; kappa or lambda; mu */
+          for (int kk = 0; kk <= LAY_NG && !bad; kk++)
+            for (int jj = 0; jj <= LAY_NG && !bad; jj++)
+              for (int ii = 0; ii <= LAY_NG; ii++) {
+                float p[3], var[3];
+                lay_subpoint((const float (*)[3])vert, ii, jj, kk, p);
+                if (lay_point(&m, p[0], p[1], p[2], var)) { bad = 1; break; }
+                float vp = var[1], vs = var[2], r = var[0];
+                float mu_ = vs * vs * r;
+                float lambda = vp * vp * r - 2.0 * mu_;
+                s_rho += r;
+                if (method == 1) {
+                  s_a += (1.0 / (lambda + 2.0 / 3.0 * mu_));
+                  s_b += (1.0 / mu_);
+                } else {
+                  s_a += lambda;
+                  s_b += mu_;
+                }
+              }
+          if (bad) break;
+          if (method == 1) {
+            s_b = nsg * 1.0 / s_b;
+            s_a = nsg * 1.0 / s_a;
+            s_rho = s_rho / (nsg * 1.0);
+            lam[q] = s_a - 2.0 / 3.0 * s_b;
+            mu[q] = s_b;
+            rho[q] = s_rho;
+          } else {
+            lam[q] = s_a / (nsg * 1.0);
+            mu[q] = s_b / (nsg * 1.0);
+            rho[q] = s_rho / (nsg * 1.0);
+          }
+        }
+    free(Hx); free(Hy); free(Hz); free(mat);
+  }
   free(xv); free(yv); free(elev);
   return bad;
+}
+
+int oracle_layer_el_iso_loc(int NI, int NX, int NY, float MINX, float MINY, float DX,
+                            float DY, const float *rec, int nx, int ny, int nz,
+                            const float *x3d, const float *y3d, const float *z3d,
+                            float *lam, float *mu, float *rho)
+{
+  return oracle_layer_el_iso(0, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d,
+                             z3d, lam, mu, rho);
 }

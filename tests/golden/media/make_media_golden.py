@@ -5,7 +5,7 @@ Runs ``oracle/_ref/ref_probe layer`` (the reference's
 media_layer2model_el_iso, media/media_layer2model.cpp:140-190, built by
 ``make -C oracle``) on a seeded elastic isotropic layered model (.md3lay
 text, media/media_read_file.cpp:22-240) and a curvilinear grid, with the
-equivalent-medium method "loc": four interfaces, one of them flat and lying
+equivalent-medium methods "loc", "har" and "ari": four interfaces, one of them flat and lying
 exactly on a grid level (the points on it take the mean of the two layers),
 velocity and density gradients with power laws, and grid points above the
 top interface.  Stores the model, the grid and the reference's lambda, mu
@@ -105,12 +105,19 @@ def main():
             f.write(struct.pack("<3i", nx, ny, nz))
             for A in (X, Y, Z):
                 f.write(A.astype("<f4").tobytes())
-        subprocess.run([PROBE, "layer", lay, gpath, "loc", opath], check=True)
-        out = np.fromfile(opath, "<f4").reshape(3, nz, ny, nx)
+        res = {}
+        for meth in ("loc", "har", "ari"):
+            subprocess.run([PROBE, "layer", lay, gpath, meth, opath], check=True,
+                           stdout=subprocess.DEVNULL)
+            o = np.fromfile(opath, "<f4").reshape(3, nz, ny, nx)
+            sfx = "" if meth == "loc" else "_" + meth
+            res.update({"lam" + sfx: o[0], "mu" + sfx: o[1], "rho" + sfx: o[2]})
+        out = (res["lam"], res["mu"], res["rho"])
         md3lay = open(lay).read()
     np.savez_compressed(os.path.join(HERE, "layer_el_iso.npz"), x3d=X, y3d=Y, z3d=Z,
-                        md3lay=np.frombuffer(md3lay.encode(), np.uint8),
-                        lam=out[0], mu=out[1], rho=out[2])
+                        md3lay=np.frombuffer(md3lay.encode(), np.uint8), **res)
+    print("points changed from loc: har %d, ari %d"
+          % ((res["lam_har"] != res["lam"]).sum(), (res["lam_ari"] != res["lam"]).sum()))
     on = int(np.isclose(Z, -800.0).sum())
     print("grid %s, %d points on the flat interface, rho range %.1f-%.1f"
           % (X.shape, on, out[2].min(), out[2].max()))

@@ -1,6 +1,6 @@
-"""Layered-media discretisation ("loc" method) against the reference's own
-media_layer2model_el_iso: the oracle bit for bit (CPU), the device within
-float rounding (GPU)."""
+"""Layered-media discretisation (equivalent-medium methods "loc", "har",
+"ari") against the reference's own media_layer2model_el_iso: the oracle bit
+for bit (CPU), the device within float rounding (GPU)."""
 
 import os
 import sys
@@ -24,16 +24,30 @@ def test_md3lay_parser():
     assert np.all(m["rec"][2, :, :, 0] == -800.0)       # the flat interface
 
 
-def test_oracle_matches_reference_bitwise():
+METHODS = [("loc", ""), ("har", "_har"), ("ari", "_ari")]
+
+
+@pytest.mark.parametrize("method,sfx", METHODS)
+def test_oracle_matches_reference_bitwise(method, sfx):
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     z, m = _fixture()
-    got = oracle.layer_el_iso_loc(m, z["x3d"], z["y3d"], z["z3d"])
-    for g, w in zip(got, (z["lam"], z["mu"], z["rho"])):
-        np.testing.assert_array_equal(g.view(np.int32), w.view(np.int32))
+    got = oracle.layer_el_iso(m, z["x3d"], z["y3d"], z["z3d"], method)
+    for g, n in zip(got, ("lam", "mu", "rho")):
+        np.testing.assert_array_equal(g.view(np.int32), z[n + sfx].view(np.int32))
     # points on the flat interface take the mean of the two layers
     on = np.isclose(z["z3d"], -800.0)
     assert on.sum() > 100
+    if method != "loc":
+        # the averaged points are those whose cells straddle an interface
+        changed = z["lam" + sfx] != z["lam"]
+        assert 500 < changed.sum() < 0.3 * changed.size
+
+
+def test_har_and_ari_differ():
+    z, _ = _fixture()
+    d = z["lam_har"] != z["lam_ari"]
+    assert d.sum() > 500
 
 
 def test_oracle_refuses_points_outside_the_mesh():
@@ -46,13 +60,68 @@ def test_oracle_refuses_points_outside_the_mesh():
 
 
 @pytest.mark.gpu
-def test_device_matches_reference():
+@pytest.mark.parametrize("method,sfx", METHODS)
+def test_device_matches_reference(method, sfx):
+    """Within 2e-6 relative: the device's double pow may differ from the
+    host libm's in its last bit, which can move a float rounding."""
     from cgfd3d_gb300 import _lib, media
     z, m = _fixture()
-    got = media.layer_el_iso(m, z["x3d"], z["y3d"], z["z3d"])
-    for g, w in zip(got, (z["lam"], z["mu"], z["rho"])):
-        np.testing.assert_allclose(g, w, rtol=2e-6, atol=0)
+    got = media.layer_el_iso(m, z["x3d"], z["y3d"], z["z3d"], method)
+    for g, n in zip(got, ("lam", "mu", "rho")):
+        np.testing.assert_allclose(g, z[n + sfx], rtol=2e-6, atol=0)
     x = z["x3d"].copy()
     x[0, 0, 0] = m["MINX"] - 10.0
     with pytest.raises(_lib.CgfdError):
-        media.layer_el_iso(m, x, z["y3d"], z["z3d"])
+        media.layer_el_iso(m, x, z["y3d"], z["z3d"], method)
+
+
+@pytest.mark.gpu
+def test_device_refuses_unknown_method():
+    from cgfd3d_gb300 import _lib, media
+    z, m = _fixture()
+    with pytest.raises(_lib.CgfdError):
+        media.layer_el_iso(m, z["x3d"], z["y3d"], z["z3d"], "vol")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["har", "ari"])
+def test_device_matches_oracle_larger(method):
+    """A larger grid (bench model generator, 64 x 56 x 40 cells) against the
+    oracle: the same points averaged, values within float rounding."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    from types import SimpleNamespace
+    from cgfd3d_gb300 import media, models
+    ni, nj, nk = 64, 56, 40
+    shp = (nk + 6, nj + 6, ni + 6)
+    X, Y, Z = [a.reshape(shp) for a in
+               models._coords_of(SimpleNamespace(ni=ni, nj=nj, nk=nk), 2024)]
+    m = _bench_model(X, Y, Z)
+    want = oracle.layer_el_iso(m, X, Y, Z, method)
+    loc = oracle.layer_el_iso(m, X, Y, Z, "loc")
+    got = media.layer_el_iso(m, X, Y, Z, method)
+    assert (want[0] != loc[0]).sum() > 1000
+    for g, w in zip(got, want):
+        np.testing.assert_allclose(g, w, rtol=2e-6, atol=0)
+
+
+def _bench_model(X, Y, Z):
+    """Four interfaces spread over the grid's depth, gradients with powers."""
+    rng = np.random.default_rng(3)
+    NX, NY = 30, 24
+    minx, miny = float(X.min()) - 10.0, float(Y.min()) - 10.0
+    dx = (float(X.max()) + 10.0 - minx) / (NX - 1)
+    dy = (float(Y.max()) + 10.0 - miny) / (NY - 1)
+    XX, YY = np.meshgrid(minx + dx * np.arange(NX), miny + dy * np.arange(NY))
+    zmin, zmax = float(Z.min()), float(Z.max())
+    recs = []
+    for n in range(4):
+        t = zmax - (0.1 + 0.25 * n) * (zmax - zmin)
+        e = t + 0.03 * (zmax - zmin) * np.sin(XX / (0.3 * (dx * NX)) + n)
+        r = lambda a: a * (1 + 0.02 * rng.uniform(-1, 1, XX.shape))
+        recs.append(np.stack([e, r(2300 + 150 * n), np.full_like(XX, 0.01), np.full_like(XX, 1.0),
+                              r(4000 + 700 * n), np.full_like(XX, 0.04), np.full_like(XX, 0.9),
+                              r(2300 + 400 * n), np.full_like(XX, 0.0), np.full_like(XX, 1.0)],
+                             -1))
+    return dict(NI=4, NX=NX, NY=NY, MINX=minx, MINY=miny, DX=dx, DY=dy,
+                rec=np.stack(recs).astype(np.float32))
