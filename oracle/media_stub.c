@@ -1,0 +1,40 @@
+/*
+ * media_stub.c -- TEST INFRASTRUCTURE ONLY.  Stands in for the CUDA
+ * library's cgfd_media_layer_el_iso (include/cgfd3d_gpu.h) in a CPU-only
+ * link of the reference with the media drop-in adapter
+ * (cgfd3d_gb300/csrc/dropin/media_layer2model_gpu.cpp), so a test can run
+ * the adapter inside the reference's own process and check what it hands
+ * over: the values come from the oracle's restatement, which equals the
+ * reference bit for bit.  Linked only into oracle/_ref/ref_probe_media
+ * (oracle/Makefile); nothing of the product links it.
+ */
+#include <string.h>
+
+#include "cgfd3d_gpu.h"
+
+int oracle_layer_el_iso(int method, int NI, int NX, int NY, float MINX, float MINY, float DX,
+                        float DY, const float *rec, int nx, int ny, int nz, const float *x3d,
+                        const float *y3d, const float *z3d, float *lam, float *mu, float *rho);
+
+static const char *stub_msg = "";
+
+int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY, float DX,
+                            float DY, const float *rec, int nx, int ny, int nz,
+                            const float *x3d, const float *y3d, const float *z3d,
+                            const char *method, float *lam, float *mu, float *rho)
+{
+  int m = !method ? -1 : !strcmp(method, "loc") ? 0 : !strcmp(method, "har") ? 1
+        : !strcmp(method, "ari") ? 2 : -1;
+  if (m < 0) {
+    stub_msg = "layered model: unknown equivalent medium method";
+    return CGFD_EINVAL;
+  }
+  if (oracle_layer_el_iso(m, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
+                          lam, mu, rho)) {
+    stub_msg = "layered model: a point outside the mesh or vp <= sqrt(2) vs";
+    return CGFD_EINVAL;
+  }
+  return 0;
+}
+
+const char *cgfd_last_error(void) { return stub_msg; }

@@ -1,4 +1,5 @@
-"""The reference solver links with its time loop replaced by the GPU library.
+"""The reference solver links with its time loop and its layered-media
+discretisation replaced by the GPU library.
 
 Where the reference tree is present, oracle/Makefile builds the reference's
 main with the drop-in adapter compiled against the reference's own headers in
@@ -28,3 +29,6 @@ def test_reference_main_links_against_gpu_library():
     assert " T drv_rk_curv_col_allstep" in syms
     assert " U cgfd_solver_create" in syms
     assert " T sv_curv_col_el_iso_onestage" in syms  # the rest of the reference
+    # the layered-media discretisation: main's call is wrapped by the adapter
+    assert " T __wrap_media_layer2model_el_iso" in syms
+    assert " U cgfd_media_layer_el_iso" in syms

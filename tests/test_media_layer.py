@@ -75,6 +75,45 @@ def test_device_matches_reference(method, sfx):
         media.layer_el_iso(m, x, z["y3d"], z["z3d"], method)
 
 
+REF = "/root/reference"
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("method,sfx", METHODS)
+def test_dropin_adapter_inside_reference(method, sfx, tmp_path):
+    """The media drop-in adapter runs inside the reference's process: the
+    reference's media_layer2model_el_iso call is wrapped, the adapter reads
+    the .md3lay with the reference's reader and hands its arrays to
+    cgfd_media_layer_el_iso, answered here by the oracle (oracle/media_stub.c).
+    The result must equal the reference's own bit for bit."""
+    import struct
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe_media"], check=True, capture_output=True)
+    z, _ = _fixture()
+    lay = tmp_path / "model.md3lay"
+    lay.write_bytes(bytes(z["md3lay"]))
+    nz, ny, nx = z["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(struct.pack("<3i", nx, ny, nz))
+        for a in (z["x3d"], z["y3d"], z["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    out = tmp_path / "out.bin"
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_probe_media")
+    r = subprocess.run([exe, "layer", str(lay), str(grid), method, str(out)],
+                       capture_output=True, text=True, check=True)
+    assert "discretising the layered model on the GPU (method %s)" % method in r.stdout
+    got = np.fromfile(out, "<f4").reshape(3, nz, ny, nx)
+    for g, n in zip(got, ("lam", "mu", "rho")):
+        np.testing.assert_array_equal(g.view(np.int32), z[n + sfx].view(np.int32))
+    # another method goes to the reference's routine, which rejects it
+    r = subprocess.run([exe, "layer", str(lay), str(grid), "tti", str(out)],
+                       capture_output=True, text=True)
+    assert r.returncode == 1 and "Wrong parametrization method" in r.stderr
+
+
 @pytest.mark.gpu
 def test_device_refuses_unknown_method():
     from cgfd3d_gb300 import _lib, media
