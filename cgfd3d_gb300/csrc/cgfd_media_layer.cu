@@ -1,29 +1,33 @@
 /*
- * cgfd_media_layer.cu -- an elastic isotropic layered model discretised on
- * a curvilinear grid on the device, with the reference's "loc" method.
+ * cgfd_media_layer.cu -- layered models (elastic isotropic and the three
+ * elastic VTI parametrisations) discretised on a curvilinear grid on the
+ * device, with the reference's equivalent-medium methods "loc", "har" and
+ * "ari".
  *
  * The reference evaluates every grid point on the host
- * (media_layer2model_el_iso, media/media_layer2model.cpp:140-190, 422-560,
- * 1334-1384): the elevation of each interface interpolated bilinearly at the
- * point's (x, y) on the interfaces' uniform mesh
+ * (media_layer2model_el_iso / _el_vti, media/media_layer2model.cpp:140-247,
+ * 422-830, 1334-1438): the elevation of each interface interpolated
+ * bilinearly at the point's (x, y) on the interfaces' uniform mesh
  * (media/media_utility.cpp:173-209), the layer whose top interface is the
  * lowest one at or above the point (:88-110), each property's value plus
  * gradient x (depth below that interface)^power, the mean with the layer
- * above for points on an interface (:119-140), then mu = vs^2 rho and
- * lambda = vp^2 rho - 2 mu.  Here one thread does one point in the same
- * float/double order; the file is compiled with --fmad=false.
+ * above for points on an interface (:119-140), then the medium: mu = vs^2
+ * rho and lambda = vp^2 rho - 2 mu (isotropic) or the VTI stiffness of the
+ * parametrisation (para2vti, media/media_utility.cpp:827-882).  Here one
+ * thread does one point in the same float/double order; the file is
+ * compiled with --fmad=false.
  *
- * The "har" and "ari" methods (media/media_layer2model.cpp:1984-2190) start
+ * The "har" and "ari" methods (media/media_layer2model.cpp:1984-2436) start
  * from "loc" and recompute each interior point whose cell -- the hexahedron
  * of the eight half-grid points (cell centres, media/media_utility.cpp:
  * 656-760) around it -- touches more than one layer: the cell is sampled at
  * 9^3 points (media/media_utility.cpp:627-654) and rho is averaged
- * arithmetically, kappa and mu harmonically ("har") or lambda and mu
- * arithmetically ("ari").  Here k_layer_mark gives every half-grid point its
- * layer, k_layer_mixed lists the points whose eight cell vertices disagree,
- * and k_layer_avg gives each listed point to one thread, which adds its
- * samples into the running sums in the reference's sample order, so the
- * float sums round as the reference's do.
+ * arithmetically, the moduli harmonically ("har": kappa and mu, or c11 c13
+ * c33 c55 c66) or arithmetically ("ari").  Here k_layer_mark gives every
+ * half-grid point its layer, k_layer_mixed lists the points whose eight cell
+ * vertices disagree, and k_layer_avg gives each listed point to one thread,
+ * which adds its samples into the running sums in the reference's sample
+ * order, so the float sums round as the reference's do.
  */
 #include <cuda_runtime.h>
 
@@ -49,10 +53,25 @@ static int lay_err(int code, const char *fmt, ...)
   return cgfd_set_error_msg(code, buf);
 }
 
+/* media kinds, with the reference's numbers (media/media_utility.hpp:40-43) */
+#define LAY_ISO 21          /* rho vp vs */
+#define LAY_VTI_PREM 22     /* rho vph vpv vsh vsv eta */
+#define LAY_VTI_THOMSEN 23  /* rho vp0 vs0 epsilon delta gamma */
+#define LAY_VTI_CIJ 24      /* rho c11 c33 c55 c66 c13 */
+
+template <int KIND> struct LayKind {
+  static constexpr int np = KIND == LAY_ISO ? 3 : 6;   /* properties per point */
+  static constexpr int nout = np;                      /* output volumes */
+};
+
 struct LayerMesh {
-  int NI, NX, NY;
+  int NI, NX, NY, nc;   /* nc: record width, 1 + 3 x properties */
   float MINX, MINY, DX, DY;
-  const float *rec;     /* [NI][NY][NX][10] */
+  const float *rec;     /* [NI][NY][NX][nc] */
+};
+
+struct LayOut {
+  float *v[6];          /* lambda mu rho, or c11 c33 c55 c66 c13 rho */
 };
 
 /* Bilinear interpolation on the interfaces' mesh (BilinearInterpolation,
@@ -91,11 +110,12 @@ __device__ LayW lay_weights(const LayerMesh &L, float xq, float yq)
 __device__ float lay_interp(const LayerMesh &L, const LayW &w, int col, int layer)
 {
   if (!w.ok) return FLT_MAX;
-  const float *v = L.rec + (size_t)layer * L.NX * L.NY * 10 + col;
+  const int nc = L.nc;
+  const float *v = L.rec + (size_t)layer * L.NX * L.NY * nc + col;
   const int indx = w.indx;
-  if (w.edge) return v[indx * 10];
-  float vq = v[indx * 10] * w.wxb * w.wyb + v[(indx + 1) * 10] * w.wxa * w.wyb +
-             v[(indx + L.NX) * 10] * w.wxb * w.wya + v[(indx + 1 + L.NX) * 10] * w.wxa * w.wya;
+  if (w.edge) return v[indx * nc];
+  float vq = v[indx * nc] * w.wxb * w.wyb + v[(indx + 1) * nc] * w.wxa * w.wyb +
+             v[(indx + L.NX) * nc] * w.wxb * w.wya + v[(indx + 1 + L.NX) * nc] * w.wxa * w.wya;
   vq /= w.area;
   return vq;
 }
@@ -130,15 +150,16 @@ __device__ int lay_first_ge(float value, const float *x, int n)
   return idx;
 }
 
-/* value + pow(dz, power) * gradient of property column c of a layer, in
+/* value + pow(dz, power) * gradient of property p of a layer, in
  * double as the reference's std::pow(float, float) promotes.  Two cases skip
  * the double pow and give the same bits: pow(dz, 1) is dz, and dz * g of two
  * floats is exact in double, so one double fma rounds v + dz g as the
  * reference's multiply-then-add does; a zero gradient with a power in [0, 8]
  * (pow finite for any float dz >= 0) adds a zero of the gradient's sign,
  * which the float add v + g gives exactly. */
-__device__ float lay_value(const LayerMesh &L, const LayW &w, int layer, int c, float dz)
+__device__ float lay_value(const LayerMesh &L, const LayW &w, int layer, int p, float dz)
 {
+  const int c = 1 + 3 * p;
   const float v = lay_interp(L, w, c, layer);
   const float g = lay_interp(L, w, c + 1, layer);
   const float pw = lay_interp(L, w, c + 2, layer);
@@ -170,12 +191,14 @@ __device__ float lay_lambda(float vp, float r, float m)
   return (float)((double)a - 2.0 * (double)m);
 }
 
-/* rho, vp, vs of one point (AssignLayerMediaPara2Point with
- * CalPointValue_layer, media/media_layer2model.cpp:422-560); 0, or 1 outside
- * the mesh, 2 where vp <= sqrt(2) vs (the reference exits on both). */
-__device__ int lay_point(const LayerMesh &L, float x, float y, float z, float *elev, float &r,
-                         float &vp, float &vs)
+/* the properties of one point (AssignLayerMediaPara2Point with
+ * CalPointValue_layer, media/media_layer2model.cpp:422-830): var[0..np-1]
+ * in the record's order; 0, or 1 outside the mesh, 2 where an isotropic
+ * point has vp <= sqrt(2) vs (the reference exits on both). */
+template <int KIND>
+__device__ int lay_point(const LayerMesh &L, float x, float y, float z, float *elev, float *var)
 {
+  constexpr int NP = LayKind<KIND>::np;
   const float maxx = L.MINX + (L.NX - 1) * L.DX, maxy = L.MINY + (L.NY - 1) * L.DY;
   if (x < L.MINX || x > maxx || y < L.MINY || y > maxy) return 1;
   const LayW w = lay_weights(L, x, y);
@@ -184,48 +207,91 @@ __device__ int lay_point(const LayerMesh &L, float x, float y, float z, float *e
   if (mi == -1) {
     mi = lay_last_ge(elev[0], elev, L.NI);
     if (mi < 0) return 1;   /* only a NaN elevation or coordinate gets here */
-    r = lay_interp(L, w, 1, mi);
-    vp = lay_interp(L, w, 4, mi);
-    vs = lay_interp(L, w, 7, mi);
+#pragma unroll
+    for (int p = 0; p < NP; p++) var[p] = lay_interp(L, w, 1 + 3 * p, mi);
     return 0;
   }
   const float dz = elev[mi] - z;
-  vp = lay_value(L, w, mi, 4, dz);
-  vs = lay_value(L, w, mi, 7, dz);
-  r = lay_value(L, w, mi, 1, dz);
-  if (lay_vp_low(vp, vs)) return 2;
+#pragma unroll
+  for (int p = 0; p < NP; p++) var[p] = lay_value(L, w, mi, p, dz);
+  if (KIND == LAY_ISO && lay_vp_low(var[1], var[2])) return 2;
   if (fabsf(dz - 0.0f) < FLT_EPSILON) {
     const int m2 = lay_first_ge(z, elev, L.NI) - 1;
     if (m2 >= 0) {
-      const float dz2 = elev[m2] - z;
-      const float vp_top = lay_value(L, w, m2, 4, dz2);
-      const float vs_top = lay_value(L, w, m2, 7, dz2);
-      const float rho_top = lay_value(L, w, m2, 1, dz2);
-      r = (float)((double)(r + rho_top) / 2.0);
-      vp = (float)((double)(vp + vp_top) / 2.0);
-      vs = (float)((double)(vs + vs_top) / 2.0);
+      /* the layer above at its own interface's depth, except for
+       * elastic_vti_cij models, whose branch of the reference keeps the
+       * point's dz (media/media_layer2model.cpp:742-774; the others
+       * recompute it, :617, :690) */
+      const float dz2 = KIND == LAY_VTI_CIJ ? dz : elev[m2] - z;
+#pragma unroll
+      for (int p = 0; p < NP; p++) {
+        const float top = lay_value(L, w, m2, p, dz2);
+        var[p] = (float)((double)(var[p] + top) / 2.0);
+      }
     }
   }
   return 0;
 }
 
-__global__ void k_layer_el_iso_loc(LayerMesh L, long long vol, const float *__restrict__ x3d,
-                                   const float *__restrict__ y3d,
-                                   const float *__restrict__ z3d, float *lam, float *mu,
-                                   float *rho, int *bad)
+/* VTI stiffness c11 c33 c55 c66 c13 rho of a point's parameters (para2vti,
+ * media/media_utility.cpp:827-882), in the reference's float/double order */
+template <int KIND> __device__ void lay_para2vti(const float *var, float *c)
+{
+  if (KIND == LAY_VTI_PREM) {
+    const float vph = var[1], vpv = var[2], vsh = var[3], vsv = var[4], rho = var[0];
+    const float eta = var[5];
+    c[0] = vph * vph * rho;
+    c[1] = vpv * vpv * rho;
+    c[3] = vsh * vsh * rho;
+    c[2] = vsv * vsv * rho;
+    c[5] = rho;
+    c[4] = (float)((double)eta * ((double)c[0] - 2.0 * (double)c[2]));
+  } else if (KIND == LAY_VTI_THOMSEN) {
+    const float rho = var[0], vp0 = var[1], vs0 = var[2], epsil = var[3], delta = var[4];
+    const float gamma = var[5];
+    const float c33 = vp0 * vp0 * rho, c55 = vs0 * vs0 * rho;
+    const float d = c33 - c55;
+    c[5] = rho;
+    c[1] = c33;
+    c[2] = c55;
+    c[3] = (float)(2.0 * (double)gamma * (double)c55 + (double)c55);
+    c[0] = (float)(2.0 * (double)epsil * (double)c33 + (double)c33);
+    c[4] = (float)(sqrt(2.0 * (double)delta * (double)c33 * (double)d + (double)(d * d)) -
+                   (double)c55);
+  } else {
+    c[0] = var[1];
+    c[1] = var[2];
+    c[2] = var[3];
+    c[3] = var[4];
+    c[4] = var[5];
+    c[5] = var[0];
+  }
+}
+
+template <int KIND>
+__global__ void k_layer_loc(LayerMesh L, long long vol, const float *__restrict__ x3d,
+                            const float *__restrict__ y3d, const float *__restrict__ z3d,
+                            LayOut out, int *bad)
 {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
        q += (long long)gridDim.x * blockDim.x) {
-    float elev[LAY_MAX], r, vp, vs;
-    const int st = lay_point(L, x3d[q], y3d[q], z3d[q], elev, r, vp, vs);
+    float elev[LAY_MAX], var[6];
+    const int st = lay_point<KIND>(L, x3d[q], y3d[q], z3d[q], elev, var);
     if (st) {
       atomicOr(bad, st);
       continue;
     }
-    const float m = vs * vs * r;
-    mu[q] = m;
-    lam[q] = lay_lambda(vp, r, m);
-    rho[q] = r;
+    if (KIND == LAY_ISO) {
+      const float m = var[2] * var[2] * var[0];
+      out.v[1][q] = m;
+      out.v[0][q] = lay_lambda(var[1], var[0], m);
+      out.v[2][q] = var[0];
+    } else {
+      float c[6];
+      lay_para2vti<KIND>(var, c);
+#pragma unroll
+      for (int n = 0; n < 6; n++) out.v[n][q] = c[n];
+    }
   }
 }
 
@@ -292,14 +358,15 @@ __global__ void k_layer_mixed(int nx, int ny, int nz, const signed char *__restr
 /* a point's equivalent medium from 9^3 samples of its cell, one thread per
  * listed point (every thread runs the same 729 samples, so a warp stays
  * converged but for the layer lookups).  method 1: har, 2: ari
- * (media/media_layer2model.cpp:1984-2190). */
+ * (media/media_layer2model.cpp:1984-2436). */
+template <int KIND>
 __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int nx, int ny,
                                                    int nz, const float *__restrict__ x3d,
                                                    const float *__restrict__ y3d,
                                                    const float *__restrict__ z3d,
                                                    const long long *__restrict__ list,
-                                                   const unsigned long long *count, float *lam,
-                                                   float *mu, float *rho, int *bad)
+                                                   const unsigned long long *count, LayOut out,
+                                                   int *bad)
 {
   const long long nlist = (long long)*count, line = nx, sl = (long long)nx * ny;
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nlist;
@@ -317,7 +384,9 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
       vy[n] = lay_half(y3d, p, i, j, k, nx, ny, nz);
       vz[n] = lay_half(z3d, p, i, j, k, nx, ny, nz);
     }
-    float s_rho = 0.0f, s_a = 0.0f, s_b = 0.0f;   /* rho; kappa or lambda; mu */
+    /* isotropic: s[0] rho, s[1] kappa or lambda, s[2] mu;
+     * VTI: s[0..4] c11 c33 c55 c66 c13, s[5] rho */
+    float s[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int st = 0;
     const float ng = (float)LAY_NG;
     for (int kk = 0; kk <= LAY_NG; kk++)
@@ -336,40 +405,74 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
             const float lxy1 = ly01 + (ly11 - ly01) / ng * fi;
             pt[d] = lxy0 + (lxy1 - lxy0) / ng * fk;
           }
-          float elev[LAY_MAX], r = 1.f, vp = 1.f, vs = 1.f;
-          st |= lay_point(L, pt[0], pt[1], pt[2], elev, r, vp, vs);
-          const float m = vs * vs * r;
-          const float lambda = lay_lambda(vp, r, m);
-          s_rho = s_rho + r;
-          if (method == 1) {
-            s_a = (float)((double)s_a + 1.0 / ((double)lambda + 2.0 / 3.0 * (double)m));
-            s_b = (float)((double)s_b + 1.0 / (double)m);
+          float elev[LAY_MAX], var[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+          st |= lay_point<KIND>(L, pt[0], pt[1], pt[2], elev, var);
+          if (KIND == LAY_ISO) {
+            const float m = var[2] * var[2] * var[0];
+            const float lambda = lay_lambda(var[1], var[0], m);
+            s[0] = s[0] + var[0];
+            if (method == 1) {
+              s[1] = (float)((double)s[1] + 1.0 / ((double)lambda + 2.0 / 3.0 * (double)m));
+              s[2] = (float)((double)s[2] + 1.0 / (double)m);
+            } else {
+              s[1] = s[1] + lambda;
+              s[2] = s[2] + m;
+            }
           } else {
-            s_a = s_a + lambda;
-            s_b = s_b + m;
+            float cp[6];
+            lay_para2vti<KIND>(var, cp);
+            if (method == 1) {
+#pragma unroll
+              for (int n = 0; n < 5; n++) s[n] = (float)((double)s[n] + 1.0 / (double)cp[n]);
+            } else {
+#pragma unroll
+              for (int n = 0; n < 5; n++) s[n] = s[n] + cp[n];
+            }
+            s[5] = s[5] + cp[5];
           }
         }
     if (st) {
       atomicOr(bad, st);
-    } else if (method == 1) {
-      const float hm = (float)((double)LAY_NSG / (double)s_b);
-      const float hk = (float)((double)LAY_NSG / (double)s_a);
-      lam[q] = (float)((double)hk - 2.0 / 3.0 * (double)hm);
-      mu[q] = hm;
-      rho[q] = (float)((double)s_rho / (double)LAY_NSG);
+    } else if (KIND == LAY_ISO && method == 1) {
+      const float hm = (float)((double)LAY_NSG / (double)s[2]);
+      const float hk = (float)((double)LAY_NSG / (double)s[1]);
+      out.v[0][q] = (float)((double)hk - 2.0 / 3.0 * (double)hm);
+      out.v[1][q] = hm;
+      out.v[2][q] = (float)((double)s[0] / (double)LAY_NSG);
+    } else if (KIND == LAY_ISO) {
+      out.v[0][q] = (float)((double)s[1] / (double)LAY_NSG);
+      out.v[1][q] = (float)((double)s[2] / (double)LAY_NSG);
+      out.v[2][q] = (float)((double)s[0] / (double)LAY_NSG);
     } else {
-      lam[q] = (float)((double)s_a / (double)LAY_NSG);
-      mu[q] = (float)((double)s_b / (double)LAY_NSG);
-      rho[q] = (float)((double)s_rho / (double)LAY_NSG);
+      /* the VTI branches divide the float sums by the int count in float */
+#pragma unroll
+      for (int n = 0; n < 5; n++)
+        out.v[n][q] = method == 1 ? (float)((double)LAY_NSG / (double)s[n])
+                                  : s[n] / (float)LAY_NSG;
+      out.v[5][q] = s[5] / (float)LAY_NSG;
     }
   }
 }
 
-extern "C" int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY,
-                                       float DX, float DY, const float *rec, int nx, int ny,
-                                       int nz, const float *x3d, const float *y3d,
-                                       const float *z3d, const char *method, float *lam,
-                                       float *mu, float *rho)
+template <int KIND>
+static void lay_launch(const LayerMesh &L, int meth, int nx, int ny, int nz, size_t vol,
+                       const float *dx, const float *dy, const float *dz, const LayOut &o,
+                       signed char *dmat, long long *dlist, unsigned long long *dcount,
+                       int *d_bad, cudaStream_t st)
+{
+  k_layer_loc<KIND><<<152 * 8, 256, 0, st>>>(L, (long long)vol, dx, dy, dz, o, d_bad);
+  if (meth) {
+    k_layer_mark<<<152 * 8, 256, 0, st>>>(L, nx, ny, nz, dx, dy, dz, dmat);
+    k_layer_mixed<<<152 * 8, 256, 0, st>>>(nx, ny, nz, dmat, dlist, dcount);
+    k_layer_avg<KIND><<<152 * 16, 128, 0, st>>>(L, meth, nx, ny, nz, dx, dy, dz, dlist, dcount,
+                                                 o, d_bad);
+  }
+}
+
+/* one call: upload, discretise, download; out holds nout host volumes */
+static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, float DX, float DY,
+                   const float *rec, int nx, int ny, int nz, const float *x3d,
+                   const float *y3d, const float *z3d, const char *method, float **out)
 {
   int meth = -1;
   if (method && strcmp(method, "loc") == 0) meth = 0;
@@ -381,12 +484,15 @@ extern "C" int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float
   if (NI < 1 || NI > LAY_MAX || NX < 2 || NY < 2 || !(DX > 0) || !(DY > 0))
     return lay_err(CGFD_EINVAL, "layered model: %d interfaces on a %dx%d mesh (1..%d "
                    "interfaces, at least 2x2 points, positive spacing)", NI, NX, NY, LAY_MAX);
-  if (!rec || !x3d || !y3d || !z3d || !lam || !mu || !rho || nx < 1 || ny < 1 || nz < 1)
+  const int nout = kind == LAY_ISO ? 3 : 6, nc = 1 + 3 * nout;
+  bool have_out = true;
+  for (int n = 0; n < nout; n++) have_out = have_out && out[n];
+  if (!rec || !x3d || !y3d || !z3d || !have_out || nx < 1 || ny < 1 || nz < 1)
     return lay_err(CGFD_EINVAL, "layered model: missing array or empty grid");
-  const size_t vol = (size_t)nx * ny * nz, nrec = (size_t)NI * NX * NY * 10;
-  /* device buffer: x, y, z, lambda, mu, rho, the model; then for har/ari the
-   * layer numbers (bytes) and the list of points to average */
-  const size_t fl = 6 * vol + nrec, extra = meth ? vol * sizeof(long long) + vol + 16 : 0;
+  const size_t vol = (size_t)nx * ny * nz, nrec = (size_t)NI * NX * NY * nc;
+  /* device buffer: x, y, z, the outputs, the model; then for har/ari the
+   * list of points to average, its counter and the layer numbers (bytes) */
+  const size_t fl = (3 + nout) * vol + nrec, extra = meth ? vol * 8 + 8 + vol + 8 : 0;
   char *d = nullptr;
   int *d_bad = nullptr, bad = 0;
   cudaStream_t st = nullptr;
@@ -394,37 +500,43 @@ extern "C" int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float
   if (e == cudaSuccess) e = cudaMalloc((void **)&d, fl * sizeof(float) + extra);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int));
   float *df = (float *)d;
-  float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *dl = df + 3 * vol, *dm = df + 4 * vol,
-        *dr = df + 5 * vol, *drec = df + 6 * vol;
-  /* the list (8-byte aligned: fl * 4 rounded up), its counter, the layer numbers */
+  float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *drec = df + (3 + nout) * vol;
+  LayOut o = {};
+  for (int n = 0; n < nout; n++) o.v[n] = df + (3 + n) * vol;
+  /* 8-byte aligned start of the list: fl floats rounded up */
   const size_t off = (fl * sizeof(float) + 7) & ~(size_t)7;
   long long *dlist = meth ? (long long *)(d + off) : nullptr;
   unsigned long long *dcount = meth ? (unsigned long long *)(d + off + vol * 8) : nullptr;
   signed char *dmat = meth ? (signed char *)(d + off + vol * 8 + 8) : nullptr;
-  if (meth && off + vol * 8 + 8 + vol > fl * sizeof(float) + extra) e = cudaErrorInvalidValue;
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
   if (e == cudaSuccess && meth) e = cudaMemsetAsync(dcount, 0, 8, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(drec, rec, nrec * 4, cudaMemcpyHostToDevice, st);
-  const LayerMesh L = {NI, NX, NY, MINX, MINY, DX, DY, drec};
+  const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
   if (e == cudaSuccess) {
-    k_layer_el_iso_loc<<<152 * 8, 256, 0, st>>>(L, (long long)vol, dx, dy, dz, dl, dm, dr,
-                                                 d_bad);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess && meth) {
-    k_layer_mark<<<152 * 8, 256, 0, st>>>(L, nx, ny, nz, dx, dy, dz, dmat);
-    k_layer_mixed<<<152 * 8, 256, 0, st>>>(nx, ny, nz, dmat, dlist, dcount);
-    k_layer_avg<<<152 * 16, 128, 0, st>>>(L, meth, nx, ny, nz, dx, dy, dz, dlist, dcount, dl,
-                                         dm, dr, d_bad);
+    switch (kind) {
+      case LAY_ISO:
+        lay_launch<LAY_ISO>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount, d_bad, st);
+        break;
+      case LAY_VTI_PREM:
+        lay_launch<LAY_VTI_PREM>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount,
+                                 d_bad, st);
+        break;
+      case LAY_VTI_THOMSEN:
+        lay_launch<LAY_VTI_THOMSEN>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount,
+                                    d_bad, st);
+        break;
+      default:
+        lay_launch<LAY_VTI_CIJ>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount,
+                                d_bad, st);
+    }
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(lam, dl, vol * 4, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(mu, dm, vol * 4, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(rho, dr, vol * 4, cudaMemcpyDeviceToHost, st);
+  for (int n = 0; n < nout && e == cudaSuccess; n++)
+    e = cudaMemcpyAsync(out[n], o.v[n], vol * 4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (d) cudaFree(d);
   if (d_bad) cudaFree(d_bad);
@@ -435,4 +547,30 @@ extern "C" int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float
                               "interfaces' mesh");
   if (bad & 2) return lay_err(CGFD_EINVAL, "layered model: vp <= sqrt(2) vs at a grid point");
   return 0;
+}
+
+extern "C" int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY,
+                                       float DX, float DY, const float *rec, int nx, int ny,
+                                       int nz, const float *x3d, const float *y3d,
+                                       const float *z3d, const char *method, float *lam,
+                                       float *mu, float *rho)
+{
+  float *out[3] = {lam, mu, rho};
+  return lay_run(LAY_ISO, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
+                 method, out);
+}
+
+extern "C" int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, float MINX,
+                                       float MINY, float DX, float DY, const float *rec, int nx,
+                                       int ny, int nz, const float *x3d, const float *y3d,
+                                       const float *z3d, const char *method, float *c11,
+                                       float *c33, float *c55, float *c66, float *c13,
+                                       float *rho)
+{
+  if (media_type != LAY_VTI_PREM && media_type != LAY_VTI_THOMSEN && media_type != LAY_VTI_CIJ)
+    return lay_err(CGFD_EINVAL, "layered model: VTI media type %d (22 prem, 23 thomsen, "
+                   "24 cij)", media_type);
+  float *out[6] = {c11, c33, c55, c66, c13, rho};
+  return lay_run(media_type, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
+                 method, out);
 }

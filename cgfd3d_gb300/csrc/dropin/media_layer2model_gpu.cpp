@@ -1,19 +1,19 @@
 /*
  * media_layer2model_gpu.cpp -- drop-in for CGFD3D's discretisation of
- * elastic isotropic layered models on a curvilinear grid.
+ * elastic isotropic and elastic VTI layered models on a curvilinear grid.
  *
  * Built inside the reference tree (its media headers: inter_t,
- * read_interface_file) and linked with -Wl,--wrap=media_layer2model_el_iso,
- * so the reference's main (forward/main_curv_col_el_3d.c:328-334) calls
- * __wrap_media_layer2model_el_iso below with its unchanged arguments.  The
+ * read_interface_file) and linked with -Wl,--wrap=media_layer2model_el_iso
+ * and -Wl,--wrap=media_layer2model_el_vti, so the reference's main
+ * (forward/main_curv_col_el_3d.c:328-345) calls the __wrap_ functions below
+ * with its unchanged arguments.  The
  * .md3lay file is read by the reference's own reader
  * (media/media_read_file.cpp:22-240), its arrays are interleaved into the
- * record layout of cgfd_media_layer_el_iso (include/cgfd3d_gpu.h) and the
- * device computes lambda, mu, rho with the requested equivalent-medium
+ * record layout of cgfd_media_layer_el_iso / _el_vti (include/cgfd3d_gpu.h)
+ * and the device computes the medium with the requested equivalent-medium
  * method.  Grids other than curvilinear, methods other than loc/har/ari and
- * media other than elastic isotropic go to the reference's routine
- * (__real_media_layer2model_el_iso), which handles or rejects them as it
- * always did.  Errors print the library's message and exit(1), as the
+ * other media types go to the reference's routine (__real_...), which
+ * handles or rejects them as it always did.  Errors print the library's message and exit(1), as the
  * reference does on bad input.
  */
 #include <cfloat>
@@ -39,6 +39,41 @@ extern "C" int __real_media_layer2model_el_iso(float *lam3d, float *mu3d, float 
                                                const char *equivalent_medium_method,
                                                int myid);
 
+extern "C" int __real_media_layer2model_el_vti(float *rho, float *c11, float *c33,
+                                               float *c55, float *c66, float *c13,
+                                               const float *x3d, const float *y3d,
+                                               const float *z3d, size_t nx, size_t ny,
+                                               size_t nz, int grid_type,
+                                               const char *in_3lay_file,
+                                               const char *equivalent_medium_method,
+                                               int myid);
+
+/* the grid and method this library takes */
+static bool lay_ours(int grid_type, const char *m, size_t nx, size_t ny, size_t nz)
+{
+  return grid_type == GRID_CURV && m &&
+         (strcmp(m, "loc") == 0 || strcmp(m, "har") == 0 || strcmp(m, "ari") == 0) &&
+         nx <= INT_MAX && ny <= INT_MAX && nz <= INT_MAX;
+}
+
+/* [interface][y][x][ncol]: the reader's arrays ([interface][y][x] each)
+ * interleaved */
+static std::vector<float> lay_interleave(const inter_t &it, const float *const *cols, int ncol)
+{
+  const size_t n = it.NI * it.NX * it.NY;
+  std::vector<float> rec(n * ncol);
+  for (size_t q = 0; q < n; q++)
+    for (int c = 0; c < ncol; c++) rec[q * ncol + c] = cols[c][q];
+  return rec;
+}
+
+static void lay_fail(const char *file)
+{
+  fprintf(stderr, "Error: %s (layered model %s)\n", cgfd_last_error(), file);
+  fflush(stderr);
+  exit(1);
+}
+
 extern "C" int __wrap_media_layer2model_el_iso(float *lam3d, float *mu3d, float *rho3d,
                                                const float *x3d, const float *y3d,
                                                const float *z3d, size_t nx, size_t ny,
@@ -48,10 +83,7 @@ extern "C" int __wrap_media_layer2model_el_iso(float *lam3d, float *mu3d, float 
                                                int myid)
 {
   const char *m = equivalent_medium_method;
-  const bool ours = grid_type == GRID_CURV && m &&
-                    (strcmp(m, "loc") == 0 || strcmp(m, "har") == 0 || strcmp(m, "ari") == 0) &&
-                    nx <= INT_MAX && ny <= INT_MAX && nz <= INT_MAX;
-  if (!ours)
+  if (!lay_ours(grid_type, m, nx, ny, nz))
     return __real_media_layer2model_el_iso(lam3d, mu3d, rho3d, x3d, y3d, z3d, nx, ny, nz,
                                            grid_type, in_3lay_file, m, myid);
   inter_t it;
@@ -59,23 +91,66 @@ extern "C" int __wrap_media_layer2model_el_iso(float *lam3d, float *mu3d, float 
   if (it.media_type != ELASTIC_ISOTROPIC)
     return __real_media_layer2model_el_iso(lam3d, mu3d, rho3d, x3d, y3d, z3d, nx, ny, nz,
                                            grid_type, in_3lay_file, m, myid);
-  /* [interface][y][x][10]: elevation, then value, gradient and power of rho,
-   * vp and vs (the reader's arrays are [interface][y][x] each) */
-  const size_t n = it.NI * it.NX * it.NY;
+  /* elevation, then value, gradient and power of rho, vp and vs */
   const float *cols[10] = {it.elevation, it.rho, it.rho_grad, it.rho_pow, it.vp,
                            it.vp_grad,   it.vp_pow, it.vs,     it.vs_grad, it.vs_pow};
-  std::vector<float> rec(n * 10);
-  for (size_t q = 0; q < n; q++)
-    for (int c = 0; c < 10; c++) rec[q * 10 + c] = cols[c][q];
+  const std::vector<float> rec = lay_interleave(it, cols, 10);
   if (myid == 0)
     fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
   const int rc = cgfd_media_layer_el_iso((int)it.NI, (int)it.NX, (int)it.NY, it.MINX, it.MINY,
                                          it.DX, it.DY, rec.data(), (int)nx, (int)ny, (int)nz,
                                          x3d, y3d, z3d, m, lam3d, mu3d, rho3d);
-  if (rc != 0) {
-    fprintf(stderr, "Error: %s (layered model %s)\n", cgfd_last_error(), in_3lay_file);
-    fflush(stderr);
-    exit(1);
+  if (rc != 0) lay_fail(in_3lay_file);
+  return 0;
+}
+
+extern "C" int __wrap_media_layer2model_el_vti(float *rho, float *c11, float *c33, float *c55,
+                                               float *c66, float *c13, const float *x3d,
+                                               const float *y3d, const float *z3d, size_t nx,
+                                               size_t ny, size_t nz, int grid_type,
+                                               const char *in_3lay_file,
+                                               const char *equivalent_medium_method,
+                                               int myid)
+{
+  const char *m = equivalent_medium_method;
+  if (!lay_ours(grid_type, m, nx, ny, nz))
+    return __real_media_layer2model_el_vti(rho, c11, c33, c55, c66, c13, x3d, y3d, z3d, nx, ny,
+                                           nz, grid_type, in_3lay_file, m, myid);
+  inter_t it;
+  read_interface_file(in_3lay_file, &it);
+  /* elevation, then value, gradient and power of the six parameters */
+  const float *cols[19];
+  cols[0] = it.elevation;
+  const float *p[18];
+  if (it.media_type == ELASTIC_VTI_PREM) {
+    const float *q[18] = {it.rho, it.rho_grad, it.rho_pow, it.vph, it.vph_grad, it.vph_pow,
+                          it.vpv, it.vpv_grad, it.vpv_pow, it.vsh, it.vsh_grad, it.vsh_pow,
+                          it.vsv, it.vsv_grad, it.vsv_pow, it.eta, it.eta_grad, it.eta_pow};
+    memcpy(p, q, sizeof p);
+  } else if (it.media_type == ELASTIC_VTI_THOMSEN) {
+    const float *q[18] = {it.rho,     it.rho_grad,     it.rho_pow,     it.vp0,
+                          it.vp0_grad, it.vp0_pow,     it.vs0,         it.vs0_grad,
+                          it.vs0_pow, it.epsilon,      it.epsilon_grad, it.epsilon_pow,
+                          it.delta,   it.delta_grad,   it.delta_pow,   it.gamma,
+                          it.gamma_grad, it.gamma_pow};
+    memcpy(p, q, sizeof p);
+  } else if (it.media_type == ELASTIC_VTI_CIJ) {
+    const float *q[18] = {it.rho, it.rho_grad, it.rho_pow, it.c11, it.c11_grad, it.c11_pow,
+                          it.c33, it.c33_grad, it.c33_pow, it.c55, it.c55_grad, it.c55_pow,
+                          it.c66, it.c66_grad, it.c66_pow, it.c13, it.c13_grad, it.c13_pow};
+    memcpy(p, q, sizeof p);
+  } else {
+    return __real_media_layer2model_el_vti(rho, c11, c33, c55, c66, c13, x3d, y3d, z3d, nx, ny,
+                                           nz, grid_type, in_3lay_file, m, myid);
   }
+  for (int c = 0; c < 18; c++) cols[1 + c] = p[c];
+  const std::vector<float> rec = lay_interleave(it, cols, 19);
+  if (myid == 0)
+    fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
+  const int rc = cgfd_media_layer_el_vti(it.media_type, (int)it.NI, (int)it.NX, (int)it.NY,
+                                         it.MINX, it.MINY, it.DX, it.DY, rec.data(), (int)nx,
+                                         (int)ny, (int)nz, x3d, y3d, z3d, m, c11, c33, c55, c66,
+                                         c13, rho);
+  if (rc != 0) lay_fail(in_3lay_file);
   return 0;
 }

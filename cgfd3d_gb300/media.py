@@ -19,16 +19,28 @@ import numpy as np
 
 from . import _lib
 
-# columns of a layer record: elevation, then (value, gradient, power) of
-# rho, vp, vs
+# columns of a layer record: elevation, then (value, gradient, power) of each
+# property of the media type, in the .md3lay file's order
+# (media/media_read_file.cpp:150-400)
+MD3LAY_PROPERTIES = {
+    "elastic_isotropic": ["rho", "vp", "vs"],
+    "elastic_vti_prem": ["rho", "vph", "vpv", "vsh", "vsv", "eta"],
+    "elastic_vti_thomsen": ["rho", "vp0", "vs0", "epsilon", "delta", "gamma"],
+    "elastic_vti_cij": ["rho", "c11", "c33", "c55", "c66", "c13"],
+}
+# the media-type numbers of the reference (media/media_utility.hpp:40-43),
+# also those of cgfd_media_layer_el_vti's media_type argument
+MEDIA_TYPE_CODES = {"elastic_isotropic": 21, "elastic_vti_prem": 22,
+                    "elastic_vti_thomsen": 23, "elastic_vti_cij": 24}
 MD3LAY_COLUMNS = ["elevation", "rho", "rho_grad", "rho_pow", "vp", "vp_grad", "vp_pow",
                   "vs", "vs_grad", "vs_pow"]
 
 
 def read_md3lay(text):
-    """An elastic isotropic .md3lay model (text or path) as a dict: NI, NX,
-    NY, MINX, MINY, DX, DY and rec (NI, NY, NX, 10) float32; lines starting
-    with '#' and empty lines are skipped, as the reference's reader does."""
+    """A .md3lay model (text or path) of an elastic isotropic or VTI medium
+    as a dict: media_type, NI, NX, NY, MINX, MINY, DX, DY and rec
+    (NI, NY, NX, 1 + 3 * properties) float32; lines starting with '#' and
+    empty lines are skipped, as the reference's reader does."""
     if "\n" not in text:
         with open(text) as f:
             text = f.read()
@@ -37,22 +49,26 @@ def read_md3lay(text):
         if line.startswith("#") or line == "\n":
             continue
         words += line.split()
-    if not words or words[0] != "elastic_isotropic":
-        raise ValueError("only elastic_isotropic layered models are read")
+    if not words or words[0] not in MD3LAY_PROPERTIES:
+        raise ValueError("layered models of %s are read" % ", ".join(MD3LAY_PROPERTIES))
+    kind = words[0]
+    nc = 1 + 3 * len(MD3LAY_PROPERTIES[kind])
     NI = int(words[1])
     NX, NY = int(words[2]), int(words[3])
     MINX, MINY, DX, DY = [np.float32(w) for w in words[4:8]]
-    vals = np.array([np.float32(w) for w in words[8:8 + NI * NY * NX * 10]], np.float32)
-    if vals.size != NI * NY * NX * 10 or NI < 1 or NX < 2 or NY < 2:
+    vals = np.array([np.float32(w) for w in words[8:8 + NI * NY * NX * nc]], np.float32)
+    if vals.size != NI * NY * NX * nc or NI < 1 or NX < 2 or NY < 2:
         raise ValueError("incomplete layered model")
-    return dict(NI=NI, NX=NX, NY=NY, MINX=float(MINX), MINY=float(MINY), DX=float(DX),
-                DY=float(DY), rec=vals.reshape(NI, NY, NX, 10))
+    return dict(media_type=kind, NI=NI, NX=NX, NY=NY, MINX=float(MINX), MINY=float(MINY),
+                DX=float(DX), DY=float(DY), rec=vals.reshape(NI, NY, NX, nc))
 
 
 def layer_el_iso(model, x3d, y3d, z3d, method="loc"):
-    """lambda, mu, rho of the model on the grid (arrays shaped like x3d),
-    computed on the device with the equivalent-medium method "loc", "har"
-    or "ari"."""
+    """lambda, mu, rho of an elastic isotropic model on the grid (arrays
+    shaped like x3d), computed on the device with the equivalent-medium
+    method "loc", "har" or "ari"."""
+    if model.get("media_type", "elastic_isotropic") != "elastic_isotropic":
+        raise ValueError("layer_el_iso takes elastic_isotropic models")
     shape = np.shape(x3d)
     nz, ny, nx = shape
     x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
@@ -64,3 +80,31 @@ def layer_el_iso(model, x3d, y3d, z3d, method="loc"):
         rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
         method.encode(), *[o.ctypes.data for o in out]))
     return tuple(out)
+
+
+def layer_el_vti(model, x3d, y3d, z3d, method="loc"):
+    """c11, c33, c55, c66, c13, rho of an elastic VTI model
+    (elastic_vti_prem, _thomsen or _cij) on the grid, computed on the device
+    (cgfd_media_layer_el_vti)."""
+    kind = model.get("media_type")
+    if kind not in ("elastic_vti_prem", "elastic_vti_thomsen", "elastic_vti_cij"):
+        raise ValueError("layer_el_vti takes elastic_vti_* models")
+    shape = np.shape(x3d)
+    nz, ny, nx = shape
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    rec = np.ascontiguousarray(model["rec"], np.float32)
+    out = [np.empty(shape, np.float32) for _ in range(6)]
+    _lib.check(_lib.lib().cgfd_media_layer_el_vti(
+        MEDIA_TYPE_CODES[kind], int(model["NI"]), int(model["NX"]), int(model["NY"]),
+        C.c_float(model["MINX"]), C.c_float(model["MINY"]), C.c_float(model["DX"]),
+        C.c_float(model["DY"]), rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data,
+        z.ctypes.data, method.encode(), *[o.ctypes.data for o in out]))
+    return tuple(out)
+
+
+def layer(model, x3d, y3d, z3d, method="loc"):
+    """The model's medium on the grid: (lambda, mu, rho) for elastic
+    isotropic models, (c11, c33, c55, c66, c13, rho) for VTI ones."""
+    if model.get("media_type", "elastic_isotropic") == "elastic_isotropic":
+        return layer_el_iso(model, x3d, y3d, z3d, method)
+    return layer_el_vti(model, x3d, y3d, z3d, method)

@@ -347,6 +347,27 @@ int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY, floa
                             const float *x3d, const float *y3d, const float *z3d,
                             const char *method, float *lam, float *mu, float *rho);
 
+/* Media types of cgfd_media_layer_el_vti, numbered as the reference numbers
+ * them (media/media_utility.hpp:41-43). */
+#define CGFD_LAYER_VTI_PREM 22     /* rho vph vpv vsh vsv eta */
+#define CGFD_LAYER_VTI_THOMSEN 23  /* rho vp0 vs0 epsilon delta gamma */
+#define CGFD_LAYER_VTI_CIJ 24      /* rho c11 c33 c55 c66 c13 */
+
+/* An elastic VTI layered model discretised on a curvilinear grid, as
+ * media_layer2model_el_vti does (media/media_layer2model.cpp:192-247,
+ * 560-780, 1386-1438, 2197-2436; called at forward/main_curv_col_el_3d.c:
+ * 336-345): as cgfd_media_layer_el_iso, with rec [NI][NY][NX][19] =
+ * elevation, then value, gradient and power of the six parameters of
+ * media_type in the .md3lay order; the parameters become c11 c33 c55 c66 c13
+ * rho as para2vti converts them (media/media_utility.cpp:827-882).  "har"
+ * averages c11 c13 c33 c55 c66 harmonically and rho arithmetically, "ari"
+ * all arithmetically.  Writes the six host volumes (nx*ny*nz each). */
+int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, float MINX, float MINY,
+                            float DX, float DY, const float *rec, int nx, int ny, int nz,
+                            const float *x3d, const float *y3d, const float *z3d,
+                            const char *method, float *c11, float *c33, float *c55,
+                            float *c66, float *c13, float *rho);
+
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);
 

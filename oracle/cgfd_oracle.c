@@ -1941,17 +1941,17 @@ static int lay_first_ge(float value, const float *x, int n)
   return idx;
 }
 
-/* value + pow(dz, power) * grad of one property of layer mi at (x, y) */
-static float lay_value(const float *xv, int NX, const float *yv, int NY, const float *rec,
-                       size_t slice, int mi, int c, float dz, float x, float y)
-{
-  float v = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + c, 10, x, y);
-  float g = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + c + 1, 10, x, y);
-  float pw = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + c + 2, 10, x, y);
-  return v + pow(dz, pw) * g;
-}
+/* media kinds of a layered model, with the reference's numbers
+ * (media/media_utility.hpp:40-43): elastic isotropic (rho vp vs) and the
+ * three VTI parametrisations (rho vph vpv vsh vsv eta / rho vp0 vs0 epsilon
+ * delta gamma / rho c11 c33 c55 c66 c13) */
+#define LAY_ISO 21
+#define LAY_VTI_PREM 22
+#define LAY_VTI_THOMSEN 23
+#define LAY_VTI_CIJ 24
 
 typedef struct {
+  int kind, np, nc;          /* properties per point; record width 1 + 3 np */
   int NI, NX, NY;
   const float *xv, *yv, *rec;
   size_t slice;
@@ -1959,45 +1959,86 @@ typedef struct {
   float *elev;
 } lay_model_t;
 
-/* rho, vp, vs of one point: AssignLayerMediaPara2Point with
- * CalPointValue_layer for ELASTIC_ISOTROPIC (media/media_layer2model.cpp:
- * 422-560).  Returns 1 where the reference exits (outside the mesh, or
- * vp <= sqrt(2) vs), else 0. */
+/* value + pow(dz, power) * grad of property p of layer mi at (x, y) */
+static float lay_value(const lay_model_t *m, int mi, int p, float dz, float x, float y)
+{
+  const float *r = m->rec + mi * m->slice * m->nc + 1 + 3 * p;
+  float v = lay_bilinear(m->xv, m->NX, m->yv, m->NY, r, m->nc, x, y);
+  float g = lay_bilinear(m->xv, m->NX, m->yv, m->NY, r + 1, m->nc, x, y);
+  float pw = lay_bilinear(m->xv, m->NX, m->yv, m->NY, r + 2, m->nc, x, y);
+  return v + pow(dz, pw) * g;
+}
+
+/* the properties of one point: AssignLayerMediaPara2Point with
+ * CalPointValue_layer (media/media_layer2model.cpp:422-830).  Returns 1
+ * where the reference exits (outside the mesh; for elastic isotropic media
+ * also vp <= sqrt(2) vs), else 0. */
 static int lay_point(const lay_model_t *m, float x, float y, float z, float *var)
 {
-  const int NI = m->NI, NX = m->NX, NY = m->NY;
-  const float *xv = m->xv, *yv = m->yv, *rec = m->rec;
-  const size_t slice = m->slice;
+  const int NI = m->NI;
   float *elev = m->elev;
   if (x < m->minx || x > m->maxx || y < m->miny || y > m->maxy) return 1;
   for (int n = 0; n < NI; n++)
-    elev[n] = lay_bilinear(xv, NX, yv, NY, rec + n * slice * 10, 10, x, y);
+    elev[n] = lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + n * m->slice * m->nc, m->nc,
+                           x, y);
   int mi = lay_last_ge(z, elev, NI);
   if (mi == -1) {
     mi = lay_last_ge(elev[0], elev, NI);
-    var[0] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 1, 10, x, y);
-    var[1] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 4, 10, x, y);
-    var[2] = lay_bilinear(xv, NX, yv, NY, rec + mi * slice * 10 + 7, 10, x, y);
+    for (int p = 0; p < m->np; p++)
+      var[p] = lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + mi * m->slice * m->nc + 1 + 3 * p,
+                            m->nc, x, y);
     return 0;
   }
   float dz = elev[mi] - z;
-  var[1] = lay_value(xv, NX, yv, NY, rec, slice, mi, 4, dz, x, y);
-  var[2] = lay_value(xv, NX, yv, NY, rec, slice, mi, 7, dz, x, y);
-  var[0] = lay_value(xv, NX, yv, NY, rec, slice, mi, 1, dz, x, y);
-  if (var[1] <= var[2] * sqrt(2)) return 1;
+  for (int p = 0; p < m->np; p++) var[p] = lay_value(m, mi, p, dz, x, y);
+  if (m->kind == LAY_ISO && var[1] <= var[2] * sqrt(2)) return 1;
   if (fabsf(dz - 0.0f) < FLT_EPSILON) {
     int m2 = lay_first_ge(z, elev, NI) - 1;
     if (m2 >= 0) {
-      float dz2 = elev[m2] - z;
-      float vp_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 4, dz2, x, y);
-      float vs_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 7, dz2, x, y);
-      float rho_top = lay_value(xv, NX, yv, NY, rec, slice, m2, 1, dz2, x, y);
-      var[0] = (var[0] + rho_top) / 2.0;
-      var[1] = (var[1] + vp_top) / 2.0;
-      var[2] = (var[2] + vs_top) / 2.0;
+      /* the layer above is taken at its own interface's depth, except for
+       * elastic_vti_cij models: that branch of the reference keeps the
+       * point's dz (media/media_layer2model.cpp:742-774; the others
+       * recompute it, :617, :690) */
+      float dz2 = m->kind == LAY_VTI_CIJ ? dz : elev[m2] - z;
+      for (int p = 0; p < m->np; p++) {
+        float top = lay_value(m, m2, p, dz2, x, y);
+        var[p] = (var[p] + top) / 2.0;
+      }
     }
   }
   return 0;
+}
+
+/* VTI stiffness from the point's parameters (para2vti,
+ * media/media_utility.cpp:827-882): c = c11 c33 c55 c66 c13 rho */
+static void lay_para2vti(int kind, const float *var, float *c)
+{
+  if (kind == LAY_VTI_PREM) {
+    float vph = var[1], vpv = var[2], vsh = var[3], vsv = var[4], rho = var[0], eta = var[5];
+    c[0] = vph * vph * rho;
+    c[1] = vpv * vpv * rho;
+    c[3] = vsh * vsh * rho;
+    c[2] = vsv * vsv * rho;
+    c[5] = rho;
+    c[4] = eta * (c[0] - 2.0 * c[2]);
+  } else if (kind == LAY_VTI_THOMSEN) {
+    float rho = var[0], vp0 = var[1], vs0 = var[2], epsil = var[3], delta = var[4];
+    float gamma = var[5];
+    float c33 = vp0 * vp0 * rho, c55 = vs0 * vs0 * rho;
+    c[5] = rho;
+    c[1] = c33;
+    c[2] = c55;
+    c[3] = 2.0 * gamma * c55 + c55;
+    c[0] = 2.0 * epsil * c33 + c33;
+    c[4] = sqrt(2.0 * delta * c33 * (c33 - c55) + (c33 - c55) * (c33 - c55)) - c55;
+  } else {
+    c[0] = var[1];
+    c[1] = var[2];
+    c[2] = var[3];
+    c[3] = var[4];
+    c[4] = var[5];
+    c[5] = var[0];
+  }
 }
 
 /* the half grid of a curvilinear grid: each point but the last along an
@@ -2023,8 +2064,8 @@ static void lay_mark(const lay_model_t *m, size_t vol, const float *Hx, const fl
 {
   for (size_t q = 0; q < vol; q++) {
     for (int n = 0; n < m->NI; n++)
-      m->elev[n] = lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + n * m->slice * 10, 10,
-                                Hx[q], Hy[q]);
+      m->elev[n] = lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + n * m->slice * m->nc,
+                                m->nc, Hx[q], Hy[q]);
     int mi = lay_last_ge(Hz[q], m->elev, m->NI);
     if (mi == -1) mi = lay_last_ge(m->elev[0], m->elev, m->NI);
     mat[q] = mi;
@@ -2033,10 +2074,9 @@ static void lay_mark(const lay_model_t *m, size_t vol, const float *Hx, const fl
 
 /* distinct values among 8 layer numbers, 0 when one is -1
  * (NumOfValues, media/media_utility.cpp:610-624) */
-static int lay_num_values(const int *v, int NI)
+static int lay_num_values(const int *v)
 {
   int tab[LAY_MAXI] = {0}, num = 0;
-  (void)NI;
   for (int i = 0; i < 8; i++) {
     if (v[i] == -1) return 0;
     if (tab[v[i]] == 0) num++;
@@ -2047,7 +2087,7 @@ static int lay_num_values(const int *v, int NI)
 
 #define LAY_NG 8
 
-/* sample isg of the (NG+1)^3 points spanning a cell of 8 vertices
+/* sample (i, j, k) of the (NG+1)^3 points spanning a cell of 8 vertices
  * (MeshSubdivide, media/media_utility.cpp:627-654) */
 static void lay_subpoint(const float (*v)[3], int i, int j, int k, float *p)
 {
@@ -2063,31 +2103,51 @@ static void lay_subpoint(const float (*v)[3], int i, int j, int k, float *p)
   }
 }
 
-/* method 0: loc; 1: har (harmonic kappa and mu, arithmetic rho over the
- * subdivided cell, media/media_layer2model.cpp:1984-2095); 2: ari
- * (arithmetic lambda, mu, rho, :2098-2190).  har and ari start from loc
- * and recompute the points whose cell (between the half-grid points
- * around them) touches more than one layer. */
-int oracle_layer_el_iso(int method, int NI, int NX, int NY, float MINX, float MINY, float DX,
-                        float DY, const float *rec, int nx, int ny, int nz, const float *x3d,
-                        const float *y3d, const float *z3d, float *lam, float *mu, float *rho)
+/* The output of one point from its properties: lambda, mu, rho (elastic
+ * isotropic; media/media_layer2model.cpp:1375-1380) or c11 c33 c55 c66 c13
+ * rho (VTI). */
+static void lay_store(int kind, const float *var, float **out, size_t q)
+{
+  if (kind == LAY_ISO) {
+    float vp = var[1], vs = var[2], r = var[0];
+    out[1][q] = vs * vs * r;
+    out[0][q] = vp * vp * r - 2.0 * out[1][q];
+    out[2][q] = r;
+  } else {
+    float c[6];
+    lay_para2vti(kind, var, c);
+    for (int n = 0; n < 6; n++) out[n][q] = c[n];
+  }
+}
+
+/* kind: LAY_ISO or LAY_VTI_*; method 0: loc; 1: har; 2: ari.  har and ari
+ * start from loc and recompute the points whose cell (between the half-grid
+ * points around them) touches more than one layer from its 9^3 samples:
+ * elastic isotropic har: harmonic kappa and mu, arithmetic rho
+ * (media/media_layer2model.cpp:1984-2095); ari: arithmetic lambda, mu, rho
+ * (:2098-2190); VTI har: harmonic c11 c13 c33 c55 c66, arithmetic rho
+ * (:2197-2314); ari: all arithmetic (:2317-2436).  out: 3 (isotropic:
+ * lambda, mu, rho) or 6 (VTI: c11 c33 c55 c66 c13 rho) arrays. */
+int oracle_layer(int kind, int method, int NI, int NX, int NY, float MINX, float MINY,
+                 float DX, float DY, const float *rec, int nx, int ny, int nz,
+                 const float *x3d, const float *y3d, const float *z3d, float **out)
 {
   if (NI < 1 || NI > LAY_MAXI) return 1;
+  if (kind != LAY_ISO && kind != LAY_VTI_PREM && kind != LAY_VTI_THOMSEN && kind != LAY_VTI_CIJ)
+    return 1;
+  const int np = kind == LAY_ISO ? 3 : 6;
   float *xv = malloc(NX * sizeof(float)), *yv = malloc(NY * sizeof(float));
   float *elev = malloc(NI * sizeof(float));
   for (int i = 0; i < NX; i++) xv[i] = MINX + DX * i;
   for (int j = 0; j < NY; j++) yv[j] = MINY + DY * j;
-  lay_model_t m = {NI, NX, NY, xv, yv, rec, (size_t)NX * NY, MINX, MINX + (NX - 1) * DX,
-                   MINY, MINY + (NY - 1) * DY, elev};
+  lay_model_t m = {kind, np, 1 + 3 * np, NI, NX, NY, xv, yv, rec, (size_t)NX * NY, MINX,
+                   MINX + (NX - 1) * DX, MINY, MINY + (NY - 1) * DY, elev};
   int bad = 0;
   const size_t line = nx, sl = (size_t)nx * ny, vol = sl * nz;
   for (size_t q = 0; q < vol && !bad; q++) {
-    float var[3];          /* rho, vp, vs */
+    float var[6];
     if (lay_point(&m, x3d[q], y3d[q], z3d[q], var)) { bad = 1; break; }
-    float vp = var[1], vs = var[2], r = var[0];
-    mu[q] = vs * vs * r;
-    lam[q] = vp * vp * r - 2.0 * mu[q];
-    rho[q] = r;
+    lay_store(kind, var, out, q);
   }
   if (method != 0 && !bad) {
     float *Hx = malloc(vol * sizeof(float)), *Hy = malloc(vol * sizeof(float));
@@ -2105,52 +2165,79 @@ int oracle_layer_el_iso(int method, int NI, int NX, int NY, float MINX, float MI
           /* the cell's vertices, in the reference's order */
           const size_t c[8] = {q - 1 - line - sl, q - 1 - sl, q - sl, q - line - sl,
                                q - 1 - line, q - 1, q, q - line};
-          const int v[8] = {mat[c[0]], mat[c[3]], mat[c[2]], mat[c[1]],
-                            mat[c[4]], mat[c[7]], mat[c[6]], mat[c[5]]};
-          if (lay_num_values(v, NI) <= 1) continue;
+          int v[8];
+          for (int n = 0; n < 8; n++) v[n] = mat[c[n]];
+          if (lay_num_values(v) <= 1) continue;
           float vert[8][3];
           for (int n = 0; n < 8; n++) {
             vert[n][0] = Hx[c[n]];
             vert[n][1] = Hy[c[n]];
             vert[n][2] = Hz[c[n]];
           }
-          float s_rho = 0.0, s_a = 0.0, s_b = 0.0;   /* rho; kappa or lambda; mu */
+          /* isotropic: s[0] rho, s[1] kappa or lambda, s[2] mu;
+           * VTI: s[0..4] c11 c33 c55 c66 c13, s[5] rho */
+          float s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
           for (int kk = 0; kk <= LAY_NG && !bad; kk++)
             for (int jj = 0; jj <= LAY_NG && !bad; jj++)
               for (int ii = 0; ii <= LAY_NG; ii++) {
-                float p[3], var[3];
+                float p[3], var[6];
                 lay_subpoint((const float (*)[3])vert, ii, jj, kk, p);
                 if (lay_point(&m, p[0], p[1], p[2], var)) { bad = 1; break; }
-                float vp = var[1], vs = var[2], r = var[0];
-                float mu_ = vs * vs * r;
-                float lambda = vp * vp * r - 2.0 * mu_;
-                s_rho += r;
-                if (method == 1) {
-                  s_a += (1.0 / (lambda + 2.0 / 3.0 * mu_));
-                  s_b += (1.0 / mu_);
+                if (kind == LAY_ISO) {
+                  float vp = var[1], vs = var[2], r = var[0];
+                  float mu_ = vs * vs * r;
+                  float lambda = vp * vp * r - 2.0 * mu_;
+                  s[0] += r;
+                  if (method == 1) {
+                    s[1] += (1.0 / (lambda + 2.0 / 3.0 * mu_));
+                    s[2] += (1.0 / mu_);
+                  } else {
+                    s[1] += lambda;
+                    s[2] += mu_;
+                  }
                 } else {
-                  s_a += lambda;
-                  s_b += mu_;
+                  float cp[6];
+                  lay_para2vti(kind, var, cp);
+                  for (int n = 0; n < 5; n++) {
+                    if (method == 1)
+                      s[n] += (1.0 / cp[n]);
+                    else
+                      s[n] += cp[n];
+                  }
+                  s[5] += cp[5];
                 }
               }
           if (bad) break;
-          if (method == 1) {
-            s_b = nsg * 1.0 / s_b;
-            s_a = nsg * 1.0 / s_a;
-            s_rho = s_rho / (nsg * 1.0);
-            lam[q] = s_a - 2.0 / 3.0 * s_b;
-            mu[q] = s_b;
-            rho[q] = s_rho;
+          if (kind == LAY_ISO && method == 1) {
+            s[2] = nsg * 1.0 / s[2];
+            s[1] = nsg * 1.0 / s[1];
+            s[0] = s[0] / (nsg * 1.0);
+            out[0][q] = s[1] - 2.0 / 3.0 * s[2];
+            out[1][q] = s[2];
+            out[2][q] = s[0];
+          } else if (kind == LAY_ISO) {
+            out[0][q] = s[1] / (nsg * 1.0);
+            out[1][q] = s[2] / (nsg * 1.0);
+            out[2][q] = s[0] / (nsg * 1.0);
           } else {
-            lam[q] = s_a / (nsg * 1.0);
-            mu[q] = s_b / (nsg * 1.0);
-            rho[q] = s_rho / (nsg * 1.0);
+            for (int n = 0; n < 5; n++)
+              out[n][q] = method == 1 ? (float)(1.0 * nsg / s[n]) : s[n] / nsg;
+            out[5][q] = s[5] / nsg;
           }
         }
     free(Hx); free(Hy); free(Hz); free(mat);
   }
   free(xv); free(yv); free(elev);
   return bad;
+}
+
+int oracle_layer_el_iso(int method, int NI, int NX, int NY, float MINX, float MINY, float DX,
+                        float DY, const float *rec, int nx, int ny, int nz, const float *x3d,
+                        const float *y3d, const float *z3d, float *lam, float *mu, float *rho)
+{
+  float *out[3] = {lam, mu, rho};
+  return oracle_layer(LAY_ISO, method, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d,
+                      y3d, z3d, out);
 }
 
 int oracle_layer_el_iso_loc(int NI, int NX, int NY, float MINX, float MINY, float DX,

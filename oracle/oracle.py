@@ -149,28 +149,38 @@ def locate(x3d, y3d, z3d, points, is_depth=None):
 
 
 LAYER_METHODS = {"loc": 0, "har": 1, "ari": 2}
+LAYER_KINDS = {"elastic_isotropic": 21, "elastic_vti_prem": 22, "elastic_vti_thomsen": 23,
+               "elastic_vti_cij": 24}
 
 
-def layer_el_iso(model, x3d, y3d, z3d, method="loc"):
-    """lambda, mu, rho of an elastic isotropic layered model (dict of
-    cgfd3d_gb300.media.read_md3lay) on a grid, as the reference's
-    media_layer2model_el_iso computes them with the equivalent-medium method
-    "loc", "har" or "ari"; None where the reference would exit (point outside
-    the interface mesh or vp <= sqrt(2) vs)."""
+def layer(model, x3d, y3d, z3d, method="loc"):
+    """A layered model (dict of cgfd3d_gb300.media.read_md3lay) discretised
+    on a grid as the reference's media_layer2model_el_iso / _el_vti do with
+    the equivalent-medium method "loc", "har" or "ari": (lambda, mu, rho) for
+    elastic isotropic models, (c11, c33, c55, c66, c13, rho) for VTI ones;
+    None where the reference would exit (point outside the interface mesh or,
+    isotropic, vp <= sqrt(2) vs)."""
     import numpy as np
     L = lib()
-    L.oracle_layer_el_iso.restype = C.c_int
-    L.oracle_layer_el_iso.argtypes = ([C.c_int] * 4 + [C.c_float] * 4 + [C.c_void_p] +
-                                      [C.c_int] * 3 + [C.c_void_p] * 6)
+    L.oracle_layer.restype = C.c_int
+    L.oracle_layer.argtypes = ([C.c_int] * 5 + [C.c_float] * 4 + [C.c_void_p] +
+                               [C.c_int] * 3 + [C.c_void_p] * 4)
+    kind = LAYER_KINDS[model.get("media_type", "elastic_isotropic")]
     nz, ny, nx = np.shape(x3d)
     x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
     rec = np.ascontiguousarray(model["rec"], np.float32)
-    out = [np.zeros((nz, ny, nx), np.float32) for _ in range(3)]
-    bad = L.oracle_layer_el_iso(LAYER_METHODS[method], model["NI"], model["NX"], model["NY"],
-                                model["MINX"], model["MINY"], model["DX"], model["DY"],
-                                rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data,
-                                z.ctypes.data, *[o.ctypes.data for o in out])
+    out = [np.zeros((nz, ny, nx), np.float32) for _ in range(3 if kind == 21 else 6)]
+    ptrs = (C.c_void_p * len(out))(*[o.ctypes.data for o in out])
+    bad = L.oracle_layer(kind, LAYER_METHODS[method], model["NI"], model["NX"], model["NY"],
+                         model["MINX"], model["MINY"], model["DX"], model["DY"],
+                         rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data,
+                         z.ctypes.data, C.cast(ptrs, C.c_void_p))
     return None if bad else tuple(out)
+
+
+def layer_el_iso(model, x3d, y3d, z3d, method="loc"):
+    """lambda, mu, rho of an elastic isotropic layered model (see layer)."""
+    return layer(model, x3d, y3d, z3d, method)
 
 
 def layer_el_iso_loc(model, x3d, y3d, z3d):

@@ -33,6 +33,11 @@
  *       140-190) with the equivalent-medium method <method> (loc, har, ari).
  *       <grid>:   int nx, ny, nz; float x3d, y3d, z3d [nz][ny][nx]
  *       <output>: float lambda, mu, rho [nz][ny][nx]
+ *
+ *   ref_probe layer_vti <md3lay> <grid> <method> <output>
+ *       an elastic VTI layered model (elastic_vti_prem, _thomsen or _cij)
+ *       discretised by media_layer2model_el_vti (media/media_layer2model.cpp:
+ *       192-247); <output>: float c11, c33, c55, c66, c13, rho [nz][ny][nx]
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -47,6 +52,11 @@ int media_layer2model_el_iso(float *lam3d, float *mu3d, float *rho3d,
                              const float *x3d, const float *y3d, const float *z3d,
                              size_t nx, size_t ny, size_t nz, int grid_type,
                              const char *in_3lay_file,
+                             const char *equivalent_medium_method, int myid);
+int media_layer2model_el_vti(float *rho, float *c11, float *c33, float *c55, float *c66,
+                             float *c13, const float *x3d, const float *y3d,
+                             const float *z3d, size_t nx, size_t ny, size_t nz,
+                             int grid_type, const char *in_3lay_file,
                              const char *equivalent_medium_method, int myid);
 #define PROBE_GRID_CURV 3
 
@@ -220,13 +230,39 @@ static int probe_layer(const char *lay, const char *grid, const char *method,
   return 0;
 }
 
+static int probe_layer_vti(const char *lay, const char *grid, const char *method,
+                           const char *out)
+{
+  FILE *fp = fopen(grid, "rb");
+  if (!fp) return 2;
+  int d[3];
+  rd(d, sizeof d, fp);
+  size_t vol = (size_t)d[0] * d[1] * d[2];
+  float *x = malloc(vol * 4), *y = malloc(vol * 4), *z = malloc(vol * 4);
+  rd(x, vol * 4, fp);
+  rd(y, vol * 4, fp);
+  rd(z, vol * 4, fp);
+  fclose(fp);
+  float *c[6];   /* c11 c33 c55 c66 c13 rho */
+  for (int n = 0; n < 6; n++) c[n] = calloc(vol, 4);
+  media_layer2model_el_vti(c[5], c[0], c[1], c[2], c[3], c[4], x, y, z, d[0], d[1], d[2],
+                           PROBE_GRID_CURV, lay, method, 0);
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  for (int n = 0; n < 6; n++) fwrite(c[n], 4, vol, fo);
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
   if (argc == 4 && strcmp(argv[1], "locate") == 0) return probe_locate(argv[2], argv[3]);
   if (argc == 6 && strcmp(argv[1], "layer") == 0)
     return probe_layer(argv[2], argv[3], argv[4], argv[5]);
+  if (argc == 6 && strcmp(argv[1], "layer_vti") == 0)
+    return probe_layer_vti(argv[2], argv[3], argv[4], argv[5]);
   fprintf(stderr, "usage: ref_probe sac|locate <input> <output> | "
-                  "layer <md3lay> <grid> <method> <output>\n");
+                  "layer|layer_vti <md3lay> <grid> <method> <output>\n");
   return 2;
 }

@@ -11,8 +11,14 @@ velocity and density gradients with power laws, and grid points above the
 top interface.  Stores the model, the grid and the reference's lambda, mu
 and rho.
 
+It also writes layer_el_vti.npz: three elastic VTI layered models
+(elastic_vti_prem, elastic_vti_thomsen, elastic_vti_cij) on a smaller grid,
+discretised by media_layer2model_el_vti (media/media_layer2model.cpp:192-247)
+with every method for the Thomsen model and one or two for the others; keys
+<type>_<method>_<c11|c33|c55|c66|c13|rho> and <type>_md3lay.
+
 This script needs the reference build and runs only where it exists; the
-fixture it writes is committed and is all the tests need elsewhere.
+fixtures it writes are committed and are all the tests need elsewhere.
 
     python tests/golden/media/make_media_golden.py
 """
@@ -79,11 +85,57 @@ def layers(X, Y, seed=5):
                 rec=np.stack(recs).astype(np.float32))
 
 
-def write_md3lay(path, L):
+VTI_TYPES = {
+    # per property: base value per layer (4 layers), gradient, power
+    "elastic_vti_prem": [((2300, 2450, 2600, 2750), 0.05, 1.0),     # rho
+                         ((4000, 4600, 5300, 6100), 0.3, 1.0),      # vph
+                         ((3800, 4450, 5200, 6000), 0.2, 0.8),      # vpv
+                         ((2200, 2600, 3000, 3500), 0.0, 1.0),      # vsh
+                         ((2100, 2550, 2950, 3450), 0.1, 1.0),      # vsv
+                         ((0.95, 0.92, 0.97, 1.0), 0.0, 1.0)],      # eta
+    "elastic_vti_thomsen": [((2300, 2450, 2600, 2750), 0.05, 1.0),  # rho
+                            ((3800, 4500, 5200, 6000), 0.3, 1.0),   # vp0
+                            ((2100, 2550, 2950, 3450), 0.2, 0.9),   # vs0
+                            ((0.15, 0.10, 0.08, 0.05), 0.0, 1.0),   # epsilon
+                            ((0.08, 0.05, 0.04, 0.02), 1e-5, 1.0),  # delta
+                            ((0.10, 0.07, 0.05, 0.03), 0.0, 1.0)],  # gamma
+    "elastic_vti_cij": [((2300, 2450, 2600, 2750), 0.05, 1.0),      # rho
+                        ((3.9e10, 5.2e10, 7.3e10, 1.0e11), 2e6, 1.0),   # c11
+                        ((3.3e10, 4.8e10, 7.0e10, 9.9e10), 1e6, 0.7),   # c33
+                        ((1.0e10, 1.6e10, 2.3e10, 3.3e10), 0.0, 1.0),   # c55
+                        ((1.2e10, 1.8e10, 2.5e10, 3.5e10), 5e5, 1.0),   # c66
+                        ((1.2e10, 1.6e10, 2.4e10, 3.2e10), 0.0, 1.0)],  # c13
+}
+
+VTI_CASES = [("elastic_vti_prem", "loc"), ("elastic_vti_prem", "ari"),
+             ("elastic_vti_thomsen", "loc"), ("elastic_vti_thomsen", "har"),
+             ("elastic_vti_thomsen", "ari"),
+             ("elastic_vti_cij", "loc"), ("elastic_vti_cij", "har")]
+
+
+def vti_layers(X, Y, kind, seed=7):
+    """Four interfaces (as layers()) with the six properties of a VTI
+    parametrisation: elevation, then (value, gradient, power) each."""
+    rng = np.random.default_rng(seed)
+    base = layers(X, Y)
+    XX_shape = base["rec"].shape[1:3]
+    recs = []
+    for n in range(4):
+        cols = [base["rec"][n, :, :, 0]]
+        for vals, grad, pw in VTI_TYPES[kind]:
+            cols += [vals[n] * (1.0 + 0.02 * rng.uniform(-1, 1, XX_shape)),
+                     np.full(XX_shape, grad), np.full(XX_shape, pw if n % 2 == 0 else 1.0)]
+        recs.append(np.stack(cols, -1))
+    out = dict(base)
+    out["rec"] = np.stack(recs).astype(np.float32)
+    return out
+
+
+def write_md3lay(path, L, kind="elastic_isotropic"):
     rec = L["rec"]
     with open(path, "w") as f:
-        f.write("# layered elastic isotropic model\n")
-        f.write("elastic_isotropic\n%d\n" % rec.shape[0])
+        f.write("# layered %s model\n" % kind.replace("_", " "))
+        f.write("%s\n%d\n" % (kind, rec.shape[0]))
         f.write("%d %d %.9g %.9g %.9g %.9g\n" % (L["NX"], L["NY"], L["MINX"], L["MINY"],
                                                  L["DX"], L["DY"]))
         for n in range(rec.shape[0]):
@@ -118,9 +170,35 @@ def main():
                         md3lay=np.frombuffer(md3lay.encode(), np.uint8), **res)
     print("points changed from loc: har %d, ari %d"
           % ((res["lam_har"] != res["lam"]).sum(), (res["lam_ari"] != res["lam"]).sum()))
+    vti_main()
     on = int(np.isclose(Z, -800.0).sum())
     print("grid %s, %d points on the flat interface, rho range %.1f-%.1f"
           % (X.shape, on, out[2].min(), out[2].max()))
+
+
+def vti_main():
+    X, Y, Z = grid(ni=16, nj=14, nk=16)
+    nz, ny, nx = X.shape
+    res = dict(x3d=X, y3d=Y, z3d=Z)
+    with tempfile.TemporaryDirectory() as tmp:
+        gpath, opath = os.path.join(tmp, "grid.bin"), os.path.join(tmp, "out.bin")
+        with open(gpath, "wb") as f:
+            f.write(struct.pack("<3i", nx, ny, nz))
+            for A in (X, Y, Z):
+                f.write(A.astype("<f4").tobytes())
+        for kind in VTI_TYPES:
+            lay = os.path.join(tmp, kind + ".md3lay")
+            write_md3lay(lay, vti_layers(X, Y, kind), kind)
+            res[kind + "_md3lay"] = np.frombuffer(open(lay).read().encode(), np.uint8)
+        for kind, meth in VTI_CASES:
+            lay = os.path.join(tmp, kind + ".md3lay")
+            subprocess.run([PROBE, "layer_vti", lay, gpath, meth, opath], check=True,
+                           stdout=subprocess.DEVNULL)
+            o = np.fromfile(opath, "<f4").reshape(6, nz, ny, nx)
+            for c, name in enumerate(("c11", "c33", "c55", "c66", "c13", "rho")):
+                res["%s_%s_%s" % (kind, meth, name)] = o[c]
+    np.savez_compressed(os.path.join(HERE, "layer_el_vti.npz"), **res)
+    print("vti: grid %s, %d cases" % (X.shape, len(VTI_CASES)))
 
 
 if __name__ == "__main__":

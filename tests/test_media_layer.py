@@ -1,6 +1,7 @@
 """Layered-media discretisation (equivalent-medium methods "loc", "har",
-"ari") against the reference's own media_layer2model_el_iso: the oracle bit
-for bit (CPU), the device within float rounding (GPU)."""
+"ari") against the reference's own media_layer2model_el_iso and
+media_layer2model_el_vti: the oracle bit for bit (CPU), the device within
+float rounding (GPU), the drop-in adapter inside the reference's process."""
 
 import os
 import sys
@@ -10,12 +11,24 @@ import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FIX = os.path.join(REPO, "tests", "golden", "media", "layer_el_iso.npz")
+FIX_VTI = os.path.join(REPO, "tests", "golden", "media", "layer_el_vti.npz")
+VTI_OUT = ("c11", "c33", "c55", "c66", "c13", "rho")
+VTI_CASES = [("elastic_vti_prem", "loc"), ("elastic_vti_prem", "ari"),
+             ("elastic_vti_thomsen", "loc"), ("elastic_vti_thomsen", "har"),
+             ("elastic_vti_thomsen", "ari"),
+             ("elastic_vti_cij", "loc"), ("elastic_vti_cij", "har")]
 
 
 def _fixture():
     from cgfd3d_gb300 import media
     z = np.load(FIX)
     return z, media.read_md3lay(bytes(z["md3lay"]).decode())
+
+
+def _vti(kind):
+    from cgfd3d_gb300 import media
+    z = np.load(FIX_VTI)
+    return z, media.read_md3lay(bytes(z[kind + "_md3lay"]).decode())
 
 
 def test_md3lay_parser():
@@ -42,6 +55,21 @@ def test_oracle_matches_reference_bitwise(method, sfx):
         # the averaged points are those whose cells straddle an interface
         changed = z["lam" + sfx] != z["lam"]
         assert 500 < changed.sum() < 0.3 * changed.size
+
+
+@pytest.mark.parametrize("kind,method", VTI_CASES)
+def test_oracle_vti_matches_reference_bitwise(kind, method):
+    """Bit for bit, including the elastic_vti_cij branch's evaluation of the
+    layer above an interface point with the point's own dz (a restatement
+    that recomputes dz there differs at 264 points of the loc case)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    z, m = _vti(kind)
+    assert m["media_type"] == kind and m["rec"].shape[-1] == 19
+    got = oracle.layer(m, z["x3d"], z["y3d"], z["z3d"], method)
+    for g, n in zip(got, VTI_OUT):
+        np.testing.assert_array_equal(g.view(np.int32), z["%s_%s_%s" % (kind, method, n)]
+                                      .view(np.int32))
 
 
 def test_har_and_ari_differ():
@@ -112,6 +140,46 @@ def test_dropin_adapter_inside_reference(method, sfx, tmp_path):
     r = subprocess.run([exe, "layer", str(lay), str(grid), "tti", str(out)],
                        capture_output=True, text=True)
     assert r.returncode == 1 and "Wrong parametrization method" in r.stderr
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("kind,method", VTI_CASES)
+def test_dropin_adapter_vti_inside_reference(kind, method, tmp_path):
+    """As test_dropin_adapter_inside_reference, for media_layer2model_el_vti."""
+    import struct
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe_media"], check=True, capture_output=True)
+    z, _ = _vti(kind)
+    lay = tmp_path / "model.md3lay"
+    lay.write_bytes(bytes(z[kind + "_md3lay"]))
+    nz, ny, nx = z["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(struct.pack("<3i", nx, ny, nz))
+        for a in (z["x3d"], z["y3d"], z["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    out = tmp_path / "out.bin"
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_probe_media")
+    r = subprocess.run([exe, "layer_vti", str(lay), str(grid), method, str(out)],
+                       capture_output=True, text=True, check=True)
+    assert "discretising the layered model on the GPU (method %s)" % method in r.stdout
+    got = np.fromfile(out, "<f4").reshape(6, nz, ny, nx)
+    for g, n in zip(got, VTI_OUT):
+        np.testing.assert_array_equal(g.view(np.int32), z["%s_%s_%s" % (kind, method, n)]
+                                      .view(np.int32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,method", VTI_CASES)
+def test_device_vti_matches_reference(kind, method):
+    """Within 2e-6 relative (the device's double pow and the reference's)."""
+    from cgfd3d_gb300 import media
+    z, m = _vti(kind)
+    got = media.layer_el_vti(m, z["x3d"], z["y3d"], z["z3d"], method)
+    for g, n in zip(got, VTI_OUT):
+        np.testing.assert_allclose(g, z["%s_%s_%s" % (kind, method, n)], rtol=2e-6, atol=0)
 
 
 @pytest.mark.gpu
