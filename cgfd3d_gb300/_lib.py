@@ -65,6 +65,8 @@ def lib():
                                           [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp] * 3)
     L.cgfd_media_layer_el_vti.argtypes = ([C.c_int] * 4 + [C.c_float] * 4 + [vp] +
                                           [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp] * 6)
+    L.cgfd_media_layer_onecmp.argtypes = ([C.c_int] * 3 + [C.c_float] * 4 + [vp] +
+                                          [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp])
     L.cgfd_locator_destroy.restype = None
     L.cgfd_batch_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
     L.cgfd_batch_run.argtypes = [vp, C.c_int]

@@ -1,11 +1,11 @@
 /*
- * cgfd_media_layer.cu -- layered models (elastic isotropic and the three
- * elastic VTI parametrisations) discretised on a curvilinear grid on the
+ * cgfd_media_layer.cu -- layered models (one component, elastic isotropic
+ * and the three elastic VTI parametrisations) discretised on a curvilinear grid on the
  * device, with the reference's equivalent-medium methods "loc", "har" and
  * "ari".
  *
  * The reference evaluates every grid point on the host
- * (media_layer2model_el_iso / _el_vti, media/media_layer2model.cpp:140-247,
+ * (media_layer2model_onecmp / _el_iso / _el_vti, media/media_layer2model.cpp:47-247,
  * 422-830, 1334-1438): the elevation of each interface interpolated
  * bilinearly at the point's (x, y) on the interfaces' uniform mesh
  * (media/media_utility.cpp:173-209), the layer whose top interface is the
@@ -53,14 +53,15 @@ static int lay_err(int code, const char *fmt, ...)
   return cgfd_set_error_msg(code, buf);
 }
 
-/* media kinds, with the reference's numbers (media/media_utility.hpp:40-43) */
+/* media kinds, with the reference's numbers (media/media_utility.hpp:38-43) */
+#define LAY_ONE 0           /* one component (Qp, Qs, ...) */
 #define LAY_ISO 21          /* rho vp vs */
 #define LAY_VTI_PREM 22     /* rho vph vpv vsh vsv eta */
 #define LAY_VTI_THOMSEN 23  /* rho vp0 vs0 epsilon delta gamma */
 #define LAY_VTI_CIJ 24      /* rho c11 c33 c55 c66 c13 */
 
 template <int KIND> struct LayKind {
-  static constexpr int np = KIND == LAY_ISO ? 3 : 6;   /* properties per point */
+  static constexpr int np = KIND == LAY_ONE ? 1 : KIND == LAY_ISO ? 3 : 6;   /* per point */
   static constexpr int nout = np;                      /* output volumes */
 };
 
@@ -71,7 +72,7 @@ struct LayerMesh {
 };
 
 struct LayOut {
-  float *v[6];          /* lambda mu rho, or c11 c33 c55 c66 c13 rho */
+  float *v[6];          /* var; lambda mu rho; or c11 c33 c55 c66 c13 rho */
 };
 
 /* Bilinear interpolation on the interfaces' mesh (BilinearInterpolation,
@@ -281,7 +282,9 @@ __global__ void k_layer_loc(LayerMesh L, long long vol, const float *__restrict_
       atomicOr(bad, st);
       continue;
     }
-    if (KIND == LAY_ISO) {
+    if (KIND == LAY_ONE) {
+      out.v[0][q] = var[0];
+    } else if (KIND == LAY_ISO) {
       const float m = var[2] * var[2] * var[0];
       out.v[1][q] = m;
       out.v[0][q] = lay_lambda(var[1], var[0], m);
@@ -407,7 +410,9 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
           }
           float elev[LAY_MAX], var[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
           st |= lay_point<KIND>(L, pt[0], pt[1], pt[2], elev, var);
-          if (KIND == LAY_ISO) {
+          if (KIND == LAY_ONE) {
+            s[0] = method == 1 ? (float)((double)s[0] + 1.0 / (double)var[0]) : s[0] + var[0];
+          } else if (KIND == LAY_ISO) {
             const float m = var[2] * var[2] * var[0];
             const float lambda = lay_lambda(var[1], var[0], m);
             s[0] = s[0] + var[0];
@@ -433,6 +438,9 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
         }
     if (st) {
       atomicOr(bad, st);
+    } else if (KIND == LAY_ONE) {
+      out.v[0][q] = method == 1 ? (float)((double)LAY_NSG / (double)s[0])
+                                : (float)((double)s[0] / (double)LAY_NSG);
     } else if (KIND == LAY_ISO && method == 1) {
       const float hm = (float)((double)LAY_NSG / (double)s[2]);
       const float hk = (float)((double)LAY_NSG / (double)s[1]);
@@ -484,7 +492,7 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   if (NI < 1 || NI > LAY_MAX || NX < 2 || NY < 2 || !(DX > 0) || !(DY > 0))
     return lay_err(CGFD_EINVAL, "layered model: %d interfaces on a %dx%d mesh (1..%d "
                    "interfaces, at least 2x2 points, positive spacing)", NI, NX, NY, LAY_MAX);
-  const int nout = kind == LAY_ISO ? 3 : 6, nc = 1 + 3 * nout;
+  const int nout = kind == LAY_ONE ? 1 : kind == LAY_ISO ? 3 : 6, nc = 1 + 3 * nout;
   bool have_out = true;
   for (int n = 0; n < nout; n++) have_out = have_out && out[n];
   if (!rec || !x3d || !y3d || !z3d || !have_out || nx < 1 || ny < 1 || nz < 1)
@@ -517,6 +525,9 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
   if (e == cudaSuccess) {
     switch (kind) {
+      case LAY_ONE:
+        lay_launch<LAY_ONE>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount, d_bad, st);
+        break;
       case LAY_ISO:
         lay_launch<LAY_ISO>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount, d_bad, st);
         break;
@@ -572,5 +583,15 @@ extern "C" int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, f
                    "24 cij)", media_type);
   float *out[6] = {c11, c33, c55, c66, c13, rho};
   return lay_run(media_type, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
+                 method, out);
+}
+
+extern "C" int cgfd_media_layer_onecmp(int NI, int NX, int NY, float MINX, float MINY, float DX,
+                                       float DY, const float *rec, int nx, int ny, int nz,
+                                       const float *x3d, const float *y3d, const float *z3d,
+                                       const char *method, float *var)
+{
+  float *out[1] = {var};
+  return lay_run(LAY_ONE, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
                  method, out);
 }

@@ -1,11 +1,12 @@
 /*
  * media_layer2model_gpu.cpp -- drop-in for CGFD3D's discretisation of
- * elastic isotropic and elastic VTI layered models on a curvilinear grid.
+ * elastic isotropic, elastic VTI and one-component (Qp, Qs) layered models
+ * on a curvilinear grid.
  *
  * Built inside the reference tree (its media headers: inter_t,
- * read_interface_file) and linked with -Wl,--wrap=media_layer2model_el_iso
- * and -Wl,--wrap=media_layer2model_el_vti, so the reference's main
- * (forward/main_curv_col_el_3d.c:328-345) calls the __wrap_ functions below
+ * read_interface_file) and linked with -Wl,--wrap=media_layer2model_el_iso,
+ * _el_vti and _onecmp, so the reference's main
+ * (forward/main_curv_col_el_3d.c:328-382) calls the __wrap_ functions below
  * with its unchanged arguments.  The
  * .md3lay file is read by the reference's own reader
  * (media/media_read_file.cpp:22-240), its arrays are interleaved into the
@@ -152,5 +153,35 @@ extern "C" int __wrap_media_layer2model_el_vti(float *rho, float *c11, float *c3
                                          (int)ny, (int)nz, x3d, y3d, z3d, m, c11, c33, c55, c66,
                                          c13, rho);
   if (rc != 0) lay_fail(in_3lay_file);
+  return 0;
+}
+
+extern "C" int __real_media_layer2model_onecmp(float *var3d, const float *x3d, const float *y3d,
+                                               const float *z3d, size_t nx, size_t ny,
+                                               size_t nz, int grid_type, const char *in_var_file,
+                                               const char *average_method, int myid);
+
+extern "C" int __wrap_media_layer2model_onecmp(float *var3d, const float *x3d, const float *y3d,
+                                               const float *z3d, size_t nx, size_t ny,
+                                               size_t nz, int grid_type, const char *in_var_file,
+                                               const char *average_method, int myid)
+{
+  const char *m = average_method;
+  if (!lay_ours(grid_type, m, nx, ny, nz))
+    return __real_media_layer2model_onecmp(var3d, x3d, y3d, z3d, nx, ny, nz, grid_type,
+                                           in_var_file, m, myid);
+  inter_t it;
+  read_interface_file(in_var_file, &it);
+  if (it.media_type != ONE_COMPONENT)
+    return __real_media_layer2model_onecmp(var3d, x3d, y3d, z3d, nx, ny, nz, grid_type,
+                                           in_var_file, m, myid);
+  const float *cols[4] = {it.elevation, it.var, it.var_grad, it.var_pow};
+  const std::vector<float> rec = lay_interleave(it, cols, 4);
+  if (myid == 0)
+    fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
+  const int rc = cgfd_media_layer_onecmp((int)it.NI, (int)it.NX, (int)it.NY, it.MINX, it.MINY,
+                                         it.DX, it.DY, rec.data(), (int)nx, (int)ny, (int)nz,
+                                         x3d, y3d, z3d, m, var3d);
+  if (rc != 0) lay_fail(in_var_file);
   return 0;
 }

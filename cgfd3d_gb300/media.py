@@ -23,6 +23,7 @@ from . import _lib
 # property of the media type, in the .md3lay file's order
 # (media/media_read_file.cpp:150-400)
 MD3LAY_PROPERTIES = {
+    "one_component": ["var"],
     "elastic_isotropic": ["rho", "vp", "vs"],
     "elastic_vti_prem": ["rho", "vph", "vpv", "vsh", "vsv", "eta"],
     "elastic_vti_thomsen": ["rho", "vp0", "vs0", "epsilon", "delta", "gamma"],
@@ -30,14 +31,15 @@ MD3LAY_PROPERTIES = {
 }
 # the media-type numbers of the reference (media/media_utility.hpp:40-43),
 # also those of cgfd_media_layer_el_vti's media_type argument
-MEDIA_TYPE_CODES = {"elastic_isotropic": 21, "elastic_vti_prem": 22,
+MEDIA_TYPE_CODES = {"one_component": 0, "elastic_isotropic": 21, "elastic_vti_prem": 22,
                     "elastic_vti_thomsen": 23, "elastic_vti_cij": 24}
 MD3LAY_COLUMNS = ["elevation", "rho", "rho_grad", "rho_pow", "vp", "vp_grad", "vp_pow",
                   "vs", "vs_grad", "vs_pow"]
 
 
 def read_md3lay(text):
-    """A .md3lay model (text or path) of an elastic isotropic or VTI medium
+    """A .md3lay model (text or path) of one component or an elastic
+    isotropic or VTI medium
     as a dict: media_type, NI, NX, NY, MINX, MINY, DX, DY and rec
     (NI, NY, NX, 1 + 3 * properties) float32; lines starting with '#' and
     empty lines are skipped, as the reference's reader does."""
@@ -102,9 +104,31 @@ def layer_el_vti(model, x3d, y3d, z3d, method="loc"):
     return tuple(out)
 
 
+def layer_onecmp(model, x3d, y3d, z3d, method="loc"):
+    """One component (Qp, Qs, ...) of a one_component model on the grid,
+    computed on the device (cgfd_media_layer_onecmp)."""
+    if model.get("media_type") != "one_component":
+        raise ValueError("layer_onecmp takes one_component models")
+    shape = np.shape(x3d)
+    nz, ny, nx = shape
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    rec = np.ascontiguousarray(model["rec"], np.float32)
+    out = np.empty(shape, np.float32)
+    _lib.check(_lib.lib().cgfd_media_layer_onecmp(
+        int(model["NI"]), int(model["NX"]), int(model["NY"]), C.c_float(model["MINX"]),
+        C.c_float(model["MINY"]), C.c_float(model["DX"]), C.c_float(model["DY"]),
+        rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
+        method.encode(), out.ctypes.data))
+    return (out,)
+
+
 def layer(model, x3d, y3d, z3d, method="loc"):
-    """The model's medium on the grid: (lambda, mu, rho) for elastic
-    isotropic models, (c11, c33, c55, c66, c13, rho) for VTI ones."""
-    if model.get("media_type", "elastic_isotropic") == "elastic_isotropic":
+    """The model's medium on the grid: (var,) for one-component models,
+    (lambda, mu, rho) for elastic isotropic models, (c11, c33, c55, c66, c13,
+    rho) for VTI ones."""
+    kind = model.get("media_type", "elastic_isotropic")
+    if kind == "one_component":
+        return layer_onecmp(model, x3d, y3d, z3d, method)
+    if kind == "elastic_isotropic":
         return layer_el_iso(model, x3d, y3d, z3d, method)
     return layer_el_vti(model, x3d, y3d, z3d, method)

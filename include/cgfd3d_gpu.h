@@ -368,6 +368,17 @@ int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, float MINX, 
                             const char *method, float *c11, float *c33, float *c55,
                             float *c66, float *c13, float *rho);
 
+/* One component of a layered model (the Qp and Qs of visco-elastic runs)
+ * discretised on a curvilinear grid, as media_layer2model_onecmp does
+ * (media/media_layer2model.cpp:47-88, 1239-1283, 1603-1782; called at
+ * forward/main_curv_col_el_3d.c:370-382): rec [NI][NY][NX][4] = elevation,
+ * value, gradient, power; "har" averages the value harmonically, "ari"
+ * arithmetically.  Writes var (host, nx*ny*nz). */
+int cgfd_media_layer_onecmp(int NI, int NX, int NY, float MINX, float MINY, float DX, float DY,
+                            const float *rec, int nx, int ny, int nz, const float *x3d,
+                            const float *y3d, const float *z3d, const char *method,
+                            float *var);
+
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);
 

@@ -1942,9 +1942,11 @@ static int lay_first_ge(float value, const float *x, int n)
 }
 
 /* media kinds of a layered model, with the reference's numbers
- * (media/media_utility.hpp:40-43): elastic isotropic (rho vp vs) and the
+ * (media/media_utility.hpp:38-43): one component (Qp, Qs, ...), elastic
+ * isotropic (rho vp vs) and the
  * three VTI parametrisations (rho vph vpv vsh vsv eta / rho vp0 vs0 epsilon
  * delta gamma / rho c11 c33 c55 c66 c13) */
+#define LAY_ONE 0
 #define LAY_ISO 21
 #define LAY_VTI_PREM 22
 #define LAY_VTI_THOMSEN 23
@@ -2108,7 +2110,9 @@ static void lay_subpoint(const float (*v)[3], int i, int j, int k, float *p)
  * rho (VTI). */
 static void lay_store(int kind, const float *var, float **out, size_t q)
 {
-  if (kind == LAY_ISO) {
+  if (kind == LAY_ONE) {
+    out[0][q] = var[0];
+  } else if (kind == LAY_ISO) {
     float vp = var[1], vs = var[2], r = var[0];
     out[1][q] = vs * vs * r;
     out[0][q] = vp * vp * r - 2.0 * out[1][q];
@@ -2120,22 +2124,24 @@ static void lay_store(int kind, const float *var, float **out, size_t q)
   }
 }
 
-/* kind: LAY_ISO or LAY_VTI_*; method 0: loc; 1: har; 2: ari.  har and ari
+/* kind: LAY_ONE, LAY_ISO or LAY_VTI_*; method 0: loc; 1: har; 2: ari.  har and ari
  * start from loc and recompute the points whose cell (between the half-grid
  * points around them) touches more than one layer from its 9^3 samples:
  * elastic isotropic har: harmonic kappa and mu, arithmetic rho
  * (media/media_layer2model.cpp:1984-2095); ari: arithmetic lambda, mu, rho
  * (:2098-2190); VTI har: harmonic c11 c13 c33 c55 c66, arithmetic rho
- * (:2197-2314); ari: all arithmetic (:2317-2436).  out: 3 (isotropic:
- * lambda, mu, rho) or 6 (VTI: c11 c33 c55 c66 c13 rho) arrays. */
+ * (:2197-2314); ari: all arithmetic (:2317-2436); one component: the value
+ * harmonically or arithmetically (:1603-1782).  out: 1 (one component), 3
+ * (isotropic: lambda, mu, rho) or 6 (VTI: c11 c33 c55 c66 c13 rho) arrays. */
 int oracle_layer(int kind, int method, int NI, int NX, int NY, float MINX, float MINY,
                  float DX, float DY, const float *rec, int nx, int ny, int nz,
                  const float *x3d, const float *y3d, const float *z3d, float **out)
 {
   if (NI < 1 || NI > LAY_MAXI) return 1;
-  if (kind != LAY_ISO && kind != LAY_VTI_PREM && kind != LAY_VTI_THOMSEN && kind != LAY_VTI_CIJ)
+  if (kind != LAY_ONE && kind != LAY_ISO && kind != LAY_VTI_PREM && kind != LAY_VTI_THOMSEN &&
+      kind != LAY_VTI_CIJ)
     return 1;
-  const int np = kind == LAY_ISO ? 3 : 6;
+  const int np = kind == LAY_ONE ? 1 : kind == LAY_ISO ? 3 : 6;
   float *xv = malloc(NX * sizeof(float)), *yv = malloc(NY * sizeof(float));
   float *elev = malloc(NI * sizeof(float));
   for (int i = 0; i < NX; i++) xv[i] = MINX + DX * i;
@@ -2183,7 +2189,12 @@ int oracle_layer(int kind, int method, int NI, int NX, int NY, float MINX, float
                 float p[3], var[6];
                 lay_subpoint((const float (*)[3])vert, ii, jj, kk, p);
                 if (lay_point(&m, p[0], p[1], p[2], var)) { bad = 1; break; }
-                if (kind == LAY_ISO) {
+                if (kind == LAY_ONE) {
+                  if (method == 1)
+                    s[0] += (1.0 / var[0]);
+                  else
+                    s[0] += var[0];
+                } else if (kind == LAY_ISO) {
                   float vp = var[1], vs = var[2], r = var[0];
                   float mu_ = vs * vs * r;
                   float lambda = vp * vp * r - 2.0 * mu_;
@@ -2208,7 +2219,10 @@ int oracle_layer(int kind, int method, int NI, int NX, int NY, float MINX, float
                 }
               }
           if (bad) break;
-          if (kind == LAY_ISO && method == 1) {
+          if (kind == LAY_ONE) {
+            /* media/media_layer2model.cpp:1603-1782 (nsg is a size_t there) */
+            out[0][q] = method == 1 ? (float)(nsg * 1.0 / s[0]) : (float)(s[0] / (nsg * 1.0));
+          } else if (kind == LAY_ISO && method == 1) {
             s[2] = nsg * 1.0 / s[2];
             s[1] = nsg * 1.0 / s[1];
             s[0] = s[0] / (nsg * 1.0);

@@ -1,6 +1,6 @@
 /*
  * media_stub.c -- TEST INFRASTRUCTURE ONLY.  Stands in for the CUDA
- * library's cgfd_media_layer_el_iso and cgfd_media_layer_el_vti
+ * library's cgfd_media_layer_el_iso, _el_vti and _onecmp
  * (include/cgfd3d_gpu.h) in a CPU-only
  * link of the reference with the media drop-in adapter
  * (cgfd3d_gb300/csrc/dropin/media_layer2model_gpu.cpp), so a test can run
@@ -64,3 +64,12 @@ int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, float MINX, 
 }
 
 const char *cgfd_last_error(void) { return stub_msg; }
+
+int cgfd_media_layer_onecmp(int NI, int NX, int NY, float MINX, float MINY, float DX, float DY,
+                            const float *rec, int nx, int ny, int nz, const float *x3d,
+                            const float *y3d, const float *z3d, const char *method, float *var)
+{
+  float *out[1] = {var};
+  return stub_run(0, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d, method,
+                  out);
+}

@@ -149,14 +149,15 @@ def locate(x3d, y3d, z3d, points, is_depth=None):
 
 
 LAYER_METHODS = {"loc": 0, "har": 1, "ari": 2}
-LAYER_KINDS = {"elastic_isotropic": 21, "elastic_vti_prem": 22, "elastic_vti_thomsen": 23,
+LAYER_KINDS = {"one_component": 0, "elastic_isotropic": 21, "elastic_vti_prem": 22, "elastic_vti_thomsen": 23,
                "elastic_vti_cij": 24}
 
 
 def layer(model, x3d, y3d, z3d, method="loc"):
     """A layered model (dict of cgfd3d_gb300.media.read_md3lay) discretised
     on a grid as the reference's media_layer2model_el_iso / _el_vti do with
-    the equivalent-medium method "loc", "har" or "ari": (lambda, mu, rho) for
+    the equivalent-medium method "loc", "har" or "ari": (var,) for
+    one-component models (media_layer2model_onecmp), (lambda, mu, rho) for
     elastic isotropic models, (c11, c33, c55, c66, c13, rho) for VTI ones;
     None where the reference would exit (point outside the interface mesh or,
     isotropic, vp <= sqrt(2) vs)."""
@@ -169,7 +170,7 @@ def layer(model, x3d, y3d, z3d, method="loc"):
     nz, ny, nx = np.shape(x3d)
     x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
     rec = np.ascontiguousarray(model["rec"], np.float32)
-    out = [np.zeros((nz, ny, nx), np.float32) for _ in range(3 if kind == 21 else 6)]
+    out = [np.zeros((nz, ny, nx), np.float32) for _ in range({0: 1, 21: 3}.get(kind, 6))]
     ptrs = (C.c_void_p * len(out))(*[o.ctypes.data for o in out])
     bad = L.oracle_layer(kind, LAYER_METHODS[method], model["NI"], model["NX"], model["NY"],
                          model["MINX"], model["MINY"], model["DX"], model["DY"],

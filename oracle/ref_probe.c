@@ -38,6 +38,11 @@
  *       an elastic VTI layered model (elastic_vti_prem, _thomsen or _cij)
  *       discretised by media_layer2model_el_vti (media/media_layer2model.cpp:
  *       192-247); <output>: float c11, c33, c55, c66, c13, rho [nz][ny][nx]
+ *
+ *   ref_probe layer_one <md3lay> <grid> <method> <output>
+ *       a one-component layered model (Qp, Qs, ...) discretised by
+ *       media_layer2model_onecmp (media/media_layer2model.cpp:47-88);
+ *       <output>: float var [nz][ny][nx]
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -58,6 +63,9 @@ int media_layer2model_el_vti(float *rho, float *c11, float *c33, float *c55, flo
                              const float *z3d, size_t nx, size_t ny, size_t nz,
                              int grid_type, const char *in_3lay_file,
                              const char *equivalent_medium_method, int myid);
+int media_layer2model_onecmp(float *var3d, const float *x3d, const float *y3d,
+                             const float *z3d, size_t nx, size_t ny, size_t nz, int grid_type,
+                             const char *in_var_file, const char *average_method, int myid);
 #define PROBE_GRID_CURV 3
 
 static void rd(void *p, size_t n, FILE *fp)
@@ -254,6 +262,28 @@ static int probe_layer_vti(const char *lay, const char *grid, const char *method
   return 0;
 }
 
+static int probe_layer_one(const char *lay, const char *grid, const char *method,
+                           const char *out)
+{
+  FILE *fp = fopen(grid, "rb");
+  if (!fp) return 2;
+  int d[3];
+  rd(d, sizeof d, fp);
+  size_t vol = (size_t)d[0] * d[1] * d[2];
+  float *x = malloc(vol * 4), *y = malloc(vol * 4), *z = malloc(vol * 4);
+  rd(x, vol * 4, fp);
+  rd(y, vol * 4, fp);
+  rd(z, vol * 4, fp);
+  fclose(fp);
+  float *v = calloc(vol, 4);
+  media_layer2model_onecmp(v, x, y, z, d[0], d[1], d[2], PROBE_GRID_CURV, lay, method, 0);
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  fwrite(v, 4, vol, fo);
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
@@ -262,7 +292,9 @@ int main(int argc, char **argv)
     return probe_layer(argv[2], argv[3], argv[4], argv[5]);
   if (argc == 6 && strcmp(argv[1], "layer_vti") == 0)
     return probe_layer_vti(argv[2], argv[3], argv[4], argv[5]);
+  if (argc == 6 && strcmp(argv[1], "layer_one") == 0)
+    return probe_layer_one(argv[2], argv[3], argv[4], argv[5]);
   fprintf(stderr, "usage: ref_probe sac|locate <input> <output> | "
-                  "layer|layer_vti <md3lay> <grid> <method> <output>\n");
+                  "layer|layer_vti|layer_one <md3lay> <grid> <method> <output>\n");
   return 2;
 }

@@ -17,6 +17,11 @@ discretised by media_layer2model_el_vti (media/media_layer2model.cpp:192-247)
 with every method for the Thomsen model and one or two for the others; keys
 <type>_<method>_<c11|c33|c55|c66|c13|rho> and <type>_md3lay.
 
+And layer_onecmp.npz: a one-component layered model (a Qs-like value with
+gradients and powers) on the first grid, discretised by
+media_layer2model_onecmp (media/media_layer2model.cpp:47-88) with each
+method; keys md3lay, var_loc, var_har, var_ari.
+
 This script needs the reference build and runs only where it exists; the
 fixtures it writes are committed and are all the tests need elsewhere.
 
@@ -171,9 +176,41 @@ def main():
     print("points changed from loc: har %d, ari %d"
           % ((res["lam_har"] != res["lam"]).sum(), (res["lam_ari"] != res["lam"]).sum()))
     vti_main()
+    one_main(X, Y, Z)
     on = int(np.isclose(Z, -800.0).sum())
     print("grid %s, %d points on the flat interface, rho range %.1f-%.1f"
           % (X.shape, on, out[2].min(), out[2].max()))
+
+
+def one_main(X, Y, Z):
+    rng = np.random.default_rng(11)
+    base = layers(X, Y)
+    shp = base["rec"].shape[1:3]
+    recs = []
+    for n, (q, g, pw) in enumerate([(60.0, 0.02, 1.0), (90.0, 0.05, 0.8), (140.0, 0.0, 1.0),
+                                    (220.0, 0.01, 1.2)]):
+        recs.append(np.stack([base["rec"][n, :, :, 0],
+                              q * (1.0 + 0.05 * rng.uniform(-1, 1, shp)),
+                              np.full(shp, g), np.full(shp, pw)], -1))
+    L = dict(base)
+    L["rec"] = np.stack(recs).astype(np.float32)
+    nz, ny, nx = X.shape
+    res = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        lay = os.path.join(tmp, "qs.md3lay")
+        write_md3lay(lay, L, "one_component")
+        res["md3lay"] = np.frombuffer(open(lay).read().encode(), np.uint8)
+        gpath, opath = os.path.join(tmp, "grid.bin"), os.path.join(tmp, "out.bin")
+        with open(gpath, "wb") as f:
+            f.write(struct.pack("<3i", nx, ny, nz))
+            for A in (X, Y, Z):
+                f.write(A.astype("<f4").tobytes())
+        for meth in ("loc", "har", "ari"):
+            subprocess.run([PROBE, "layer_one", lay, gpath, meth, opath], check=True,
+                           stdout=subprocess.DEVNULL)
+            res["var_" + meth] = np.fromfile(opath, "<f4").reshape(nz, ny, nx)
+    np.savez_compressed(os.path.join(HERE, "layer_onecmp.npz"), **res)
+    print("onecmp: har changed %d points" % (res["var_har"] != res["var_loc"]).sum())
 
 
 def vti_main():

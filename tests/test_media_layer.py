@@ -12,6 +12,7 @@ import pytest
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FIX = os.path.join(REPO, "tests", "golden", "media", "layer_el_iso.npz")
 FIX_VTI = os.path.join(REPO, "tests", "golden", "media", "layer_el_vti.npz")
+FIX_ONE = os.path.join(REPO, "tests", "golden", "media", "layer_onecmp.npz")
 VTI_OUT = ("c11", "c33", "c55", "c66", "c13", "rho")
 VTI_CASES = [("elastic_vti_prem", "loc"), ("elastic_vti_prem", "ari"),
              ("elastic_vti_thomsen", "loc"), ("elastic_vti_thomsen", "har"),
@@ -70,6 +71,23 @@ def test_oracle_vti_matches_reference_bitwise(kind, method):
     for g, n in zip(got, VTI_OUT):
         np.testing.assert_array_equal(g.view(np.int32), z["%s_%s_%s" % (kind, method, n)]
                                       .view(np.int32))
+
+
+def _one():
+    from cgfd3d_gb300 import media
+    z = np.load(FIX_ONE)
+    g = np.load(FIX)
+    return z, g, media.read_md3lay(bytes(z["md3lay"]).decode())
+
+
+@pytest.mark.parametrize("method", ["loc", "har", "ari"])
+def test_oracle_onecmp_matches_reference_bitwise(method):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    z, g, m = _one()
+    assert m["media_type"] == "one_component" and m["rec"].shape[-1] == 4
+    got = oracle.layer(m, g["x3d"], g["y3d"], g["z3d"], method)[0]
+    np.testing.assert_array_equal(got.view(np.int32), z["var_" + method].view(np.int32))
 
 
 def test_har_and_ari_differ():
@@ -169,6 +187,42 @@ def test_dropin_adapter_vti_inside_reference(kind, method, tmp_path):
     for g, n in zip(got, VTI_OUT):
         np.testing.assert_array_equal(g.view(np.int32), z["%s_%s_%s" % (kind, method, n)]
                                       .view(np.int32))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("method", ["loc", "har", "ari"])
+def test_dropin_adapter_onecmp_inside_reference(method, tmp_path):
+    """As test_dropin_adapter_inside_reference, for media_layer2model_onecmp."""
+    import struct
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe_media"], check=True, capture_output=True)
+    z, g, _ = _one()
+    lay = tmp_path / "qs.md3lay"
+    lay.write_bytes(bytes(z["md3lay"]))
+    nz, ny, nx = g["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(struct.pack("<3i", nx, ny, nz))
+        for a in (g["x3d"], g["y3d"], g["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    out = tmp_path / "out.bin"
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_probe_media")
+    r = subprocess.run([exe, "layer_one", str(lay), str(grid), method, str(out)],
+                       capture_output=True, text=True, check=True)
+    assert "discretising the layered model on the GPU (method %s)" % method in r.stdout
+    got = np.fromfile(out, "<f4").reshape(nz, ny, nx)
+    np.testing.assert_array_equal(got.view(np.int32), z["var_" + method].view(np.int32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["loc", "har", "ari"])
+def test_device_onecmp_matches_reference(method):
+    from cgfd3d_gb300 import media
+    z, g, m = _one()
+    got = media.layer(m, g["x3d"], g["y3d"], g["z3d"], method)[0]
+    np.testing.assert_allclose(got, z["var_" + method], rtol=2e-6, atol=0)
 
 
 @pytest.mark.gpu
