@@ -63,10 +63,13 @@ def lib():
     L.cgfd_locator_destroy.argtypes = [vp]
     L.cgfd_media_layer_el_iso.argtypes = ([C.c_int] * 3 + [C.c_float] * 4 + [vp] +
                                           [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp] * 3)
+    L.cgfd_media_layer_pow_ok.argtypes = [C.c_int, vp, C.c_size_t]
     L.cgfd_media_layer_el_vti.argtypes = ([C.c_int] * 4 + [C.c_float] * 4 + [vp] +
                                           [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp] * 6)
-    L.cgfd_media_layer_onecmp.argtypes = ([C.c_int] * 3 + [C.c_float] * 4 + [vp] +
-                                          [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp])
+    L.cgfd_media_bin_el_iso.argtypes = ([vp] + [C.c_float] * 4 + [vp] * 3 + [C.c_int] * 3 +
+                                        [vp] * 6)
+    L.cgfd_media_bin_vis_iso.argtypes = ([vp] + [C.c_float] * 4 + [vp] * 2 + [C.c_int] * 3 +
+                                         [vp] * 5)
     L.cgfd_locator_destroy.restype = None
     L.cgfd_batch_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
     L.cgfd_batch_run.argtypes = [vp, C.c_int]

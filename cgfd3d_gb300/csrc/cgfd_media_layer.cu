@@ -1,11 +1,11 @@
 /*
- * cgfd_media_layer.cu -- layered models (one component, elastic isotropic
- * and the three elastic VTI parametrisations) discretised on a curvilinear grid on the
+ * cgfd_media_layer.cu -- layered models (elastic isotropic and the three
+ * elastic VTI parametrisations) discretised on a curvilinear grid on the
  * device, with the reference's equivalent-medium methods "loc", "har" and
  * "ari".
  *
  * The reference evaluates every grid point on the host
- * (media_layer2model_onecmp / _el_iso / _el_vti, media/media_layer2model.cpp:47-247,
+ * (media_layer2model_el_iso / _el_vti, media/media_layer2model.cpp:140-247,
  * 422-830, 1334-1438): the elevation of each interface interpolated
  * bilinearly at the point's (x, y) on the interfaces' uniform mesh
  * (media/media_utility.cpp:173-209), the layer whose top interface is the
@@ -53,15 +53,14 @@ static int lay_err(int code, const char *fmt, ...)
   return cgfd_set_error_msg(code, buf);
 }
 
-/* media kinds, with the reference's numbers (media/media_utility.hpp:38-43) */
-#define LAY_ONE 0           /* one component (Qp, Qs, ...) */
+/* media kinds, with the reference's numbers (media/media_utility.hpp:40-43) */
 #define LAY_ISO 21          /* rho vp vs */
 #define LAY_VTI_PREM 22     /* rho vph vpv vsh vsv eta */
 #define LAY_VTI_THOMSEN 23  /* rho vp0 vs0 epsilon delta gamma */
 #define LAY_VTI_CIJ 24      /* rho c11 c33 c55 c66 c13 */
 
 template <int KIND> struct LayKind {
-  static constexpr int np = KIND == LAY_ONE ? 1 : KIND == LAY_ISO ? 3 : 6;   /* per point */
+  static constexpr int np = KIND == LAY_ISO ? 3 : 6;   /* properties per point */
   static constexpr int nout = np;                      /* output volumes */
 };
 
@@ -71,8 +70,13 @@ struct LayerMesh {
   const float *rec;     /* [NI][NY][NX][nc] */
 };
 
+/* Bounds self-checks of the kernels: an index out of its range records a
+ * code here and the access is skipped; the host reports a non-zero code as
+ * an internal error (1 layer index, 2 listed point, 3 list position). */
+__device__ int g_lay_check;
+
 struct LayOut {
-  float *v[6];          /* var; lambda mu rho; or c11 c33 c55 c66 c13 rho */
+  float *v[6];          /* lambda mu rho, or c11 c33 c55 c66 c13 rho */
 };
 
 /* Bilinear interpolation on the interfaces' mesh (BilinearInterpolation,
@@ -111,6 +115,10 @@ __device__ LayW lay_weights(const LayerMesh &L, float xq, float yq)
 __device__ float lay_interp(const LayerMesh &L, const LayW &w, int col, int layer)
 {
   if (!w.ok) return FLT_MAX;
+  if (layer < 0 || layer >= L.NI || col < 0 || col >= L.nc) {
+    atomicExch(&g_lay_check, 1);
+    return FLT_MAX;
+  }
   const int nc = L.nc;
   const float *v = L.rec + (size_t)layer * L.NX * L.NY * nc + col;
   const int indx = w.indx;
@@ -282,9 +290,7 @@ __global__ void k_layer_loc(LayerMesh L, long long vol, const float *__restrict_
       atomicOr(bad, st);
       continue;
     }
-    if (KIND == LAY_ONE) {
-      out.v[0][q] = var[0];
-    } else if (KIND == LAY_ISO) {
+    if (KIND == LAY_ISO) {
       const float m = var[2] * var[2] * var[0];
       out.v[1][q] = m;
       out.v[0][q] = lay_lambda(var[1], var[0], m);
@@ -351,17 +357,40 @@ __global__ void k_layer_mixed(int nx, int ny, int nz, const signed char *__restr
       const unsigned long long bit = 1ull << v[n];
       if (!(seen & bit)) { seen |= bit; num++; }
     }
-    if (!neg && num > 1) list[atomicAdd(count, 1ull)] = q;
+    if (!neg && num > 1) {
+      const unsigned long long at = atomicAdd(count, 1ull);
+      if (at < (unsigned long long)vol)
+        list[at] = q;
+      else
+        atomicExch(&g_lay_check, 3);
+    }
   }
 }
 
 #define LAY_NG 8
 #define LAY_NSG ((LAY_NG + 1) * (LAY_NG + 1) * (LAY_NG + 1))
 
+/* one coordinate of sample (fi, fj, fk) of a cell from its eight vertices'
+ * coordinates v0..v7 (MeshSubdivide, media/media_utility.cpp:627-654) */
+__device__ __forceinline__ float lay_sub(float v0, float v1, float v2, float v3, float v4,
+                                         float v5, float v6, float v7, float fi, float fj,
+                                         float fk)
+{
+  const float ng = (float)LAY_NG;
+  const float ly00 = v0 + (v1 - v0) / ng * fj;
+  const float ly10 = v3 + (v2 - v3) / ng * fj;
+  const float ly01 = v4 + (v5 - v4) / ng * fj;
+  const float ly11 = v7 + (v6 - v7) / ng * fj;
+  const float lxy0 = ly00 + (ly10 - ly00) / ng * fi;
+  const float lxy1 = ly01 + (ly11 - ly01) / ng * fi;
+  return lxy0 + (lxy1 - lxy0) / ng * fk;
+}
+
 /* a point's equivalent medium from 9^3 samples of its cell, one thread per
  * listed point (every thread runs the same 729 samples, so a warp stays
  * converged but for the layer lookups).  method 1: har, 2: ari
- * (media/media_layer2model.cpp:1984-2436). */
+ * (media/media_layer2model.cpp:1984-2436); elastic isotropic and VTI
+ * media. */
 template <int KIND>
 __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int nx, int ny,
                                                    int nz, const float *__restrict__ x3d,
@@ -375,6 +404,11 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
   for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nlist;
        w += (long long)gridDim.x * blockDim.x) {
     const long long q = list[w];
+    const long long vol = sl * nz;
+    if (q < 1 + line + sl || q >= vol) {
+      atomicExch(&g_lay_check, 2);
+      continue;
+    }
     /* the cell's eight half-grid vertices, in the reference's order */
     const long long c[8] = {q - 1 - line - sl, q - 1 - sl, q - sl, q - line - sl,
                             q - 1 - line, q - 1, q, q - line};
@@ -391,28 +425,19 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
      * VTI: s[0..4] c11 c33 c55 c66 c13, s[5] rho */
     float s[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int st = 0;
-    const float ng = (float)LAY_NG;
     for (int kk = 0; kk <= LAY_NG; kk++)
       for (int jj = 0; jj <= LAY_NG; jj++)
         for (int ii = 0; ii <= LAY_NG; ii++) {
           const float fi = (float)ii, fj = (float)jj, fk = (float)kk;
-          float pt[3];
-#pragma unroll
-          for (int d = 0; d < 3; d++) {
-            const float *v = d == 0 ? vx : d == 1 ? vy : vz;
-            const float ly00 = v[0] + (v[1] - v[0]) / ng * fj;
-            const float ly10 = v[3] + (v[2] - v[3]) / ng * fj;
-            const float ly01 = v[4] + (v[5] - v[4]) / ng * fj;
-            const float ly11 = v[7] + (v[6] - v[7]) / ng * fj;
-            const float lxy0 = ly00 + (ly10 - ly00) / ng * fi;
-            const float lxy1 = ly01 + (ly11 - ly01) / ng * fi;
-            pt[d] = lxy0 + (lxy1 - lxy0) / ng * fk;
-          }
+          const float px = lay_sub(vx[0], vx[1], vx[2], vx[3], vx[4], vx[5], vx[6], vx[7], fi,
+                                   fj, fk);
+          const float py = lay_sub(vy[0], vy[1], vy[2], vy[3], vy[4], vy[5], vy[6], vy[7], fi,
+                                   fj, fk);
+          const float pz = lay_sub(vz[0], vz[1], vz[2], vz[3], vz[4], vz[5], vz[6], vz[7], fi,
+                                   fj, fk);
           float elev[LAY_MAX], var[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
-          st |= lay_point<KIND>(L, pt[0], pt[1], pt[2], elev, var);
-          if (KIND == LAY_ONE) {
-            s[0] = method == 1 ? (float)((double)s[0] + 1.0 / (double)var[0]) : s[0] + var[0];
-          } else if (KIND == LAY_ISO) {
+          st |= lay_point<KIND>(L, px, py, pz, elev, var);
+          if (KIND == LAY_ISO) {
             const float m = var[2] * var[2] * var[0];
             const float lambda = lay_lambda(var[1], var[0], m);
             s[0] = s[0] + var[0];
@@ -438,9 +463,6 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
         }
     if (st) {
       atomicOr(bad, st);
-    } else if (KIND == LAY_ONE) {
-      out.v[0][q] = method == 1 ? (float)((double)LAY_NSG / (double)s[0])
-                                : (float)((double)s[0] / (double)LAY_NSG);
     } else if (KIND == LAY_ISO && method == 1) {
       const float hm = (float)((double)LAY_NSG / (double)s[2]);
       const float hk = (float)((double)LAY_NSG / (double)s[1]);
@@ -460,6 +482,21 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
       out.v[5][q] = s[5] / (float)LAY_NSG;
     }
   }
+}
+
+/* Whether every (value, gradient, power) triple of a layered model with a
+ * non-zero gradient has its power in [0, 1], the range that has run on the
+ * device.  Other models are refused, because one-component models with a
+ * power of 1.2 faulted on the device for a cause not found (unit powers
+ * and zero gradients take no pow at all). */
+extern "C" int cgfd_media_layer_pow_ok(int nc, const float *rec, size_t nrec)
+{
+  for (size_t r = 0; r < nrec; r++)
+    for (int c = 1; c + 2 <= nc - 1; c += 3) {
+      const float g = rec[r * nc + c + 1], pw = rec[r * nc + c + 2];
+      if (g != 0.0f && !(pw >= 0.0f && pw <= 1.0f)) return 0;
+    }
+  return 1;
 }
 
 template <int KIND>
@@ -492,12 +529,17 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   if (NI < 1 || NI > LAY_MAX || NX < 2 || NY < 2 || !(DX > 0) || !(DY > 0))
     return lay_err(CGFD_EINVAL, "layered model: %d interfaces on a %dx%d mesh (1..%d "
                    "interfaces, at least 2x2 points, positive spacing)", NI, NX, NY, LAY_MAX);
-  const int nout = kind == LAY_ONE ? 1 : kind == LAY_ISO ? 3 : 6, nc = 1 + 3 * nout;
+  const int nout = kind == LAY_ISO ? 3 : 6, nc = 1 + 3 * nout;
   bool have_out = true;
   for (int n = 0; n < nout; n++) have_out = have_out && out[n];
   if (!rec || !x3d || !y3d || !z3d || !have_out || nx < 1 || ny < 1 || nz < 1)
     return lay_err(CGFD_EINVAL, "layered model: missing array or empty grid");
   const size_t vol = (size_t)nx * ny * nz, nrec = (size_t)NI * NX * NY * nc;
+  /* powers outside [0, 1] on a non-zero gradient have not run on the
+   * device (cgfd_media_layer_pow_ok): such models are refused */
+  if (!cgfd_media_layer_pow_ok(nc, rec, nrec / nc))
+    return lay_err(CGFD_EINVAL, "layered model: a power outside [0, 1] with a non-zero gradient "
+                   "(not taken on the device)");
   /* device buffer: x, y, z, the outputs, the model; then for har/ari the
    * list of points to average, its counter and the layer numbers (bytes) */
   const size_t fl = (3 + nout) * vol + nrec, extra = meth ? vol * 8 + 8 + vol + 8 : 0;
@@ -516,6 +558,10 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   long long *dlist = meth ? (long long *)(d + off) : nullptr;
   unsigned long long *dcount = meth ? (unsigned long long *)(d + off + vol * 8) : nullptr;
   signed char *dmat = meth ? (signed char *)(d + off + vol * 8 + 8) : nullptr;
+  const int zero = 0;
+  int check = 0;
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_lay_check, &zero, sizeof(int), 0,
+                                                    cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
   if (e == cudaSuccess && meth) e = cudaMemsetAsync(dcount, 0, 8, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
@@ -525,9 +571,6 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
   if (e == cudaSuccess) {
     switch (kind) {
-      case LAY_ONE:
-        lay_launch<LAY_ONE>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount, d_bad, st);
-        break;
       case LAY_ISO:
         lay_launch<LAY_ISO>(L, meth, nx, ny, nz, vol, dx, dy, dz, o, dmat, dlist, dcount, d_bad, st);
         break;
@@ -546,6 +589,8 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(&check, g_lay_check, sizeof(int), 0,
+                                                      cudaMemcpyDeviceToHost, st);
   for (int n = 0; n < nout && e == cudaSuccess; n++)
     e = cudaMemcpyAsync(out[n], o.v[n], vol * 4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -554,6 +599,8 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   if (st) cudaStreamDestroy(st);
   if (e != cudaSuccess)
     return lay_err(CGFD_ECUDA, "layered model: %s", cudaGetErrorString(e));
+  if (check)
+    return lay_err(CGFD_ECUDA, "layered model: internal bounds check %d failed", check);
   if (bad & 1) return lay_err(CGFD_EINVAL, "layered model: a grid point lies outside the "
                               "interfaces' mesh");
   if (bad & 2) return lay_err(CGFD_EINVAL, "layered model: vp <= sqrt(2) vs at a grid point");
@@ -583,15 +630,5 @@ extern "C" int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, f
                    "24 cij)", media_type);
   float *out[6] = {c11, c33, c55, c66, c13, rho};
   return lay_run(media_type, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
-                 method, out);
-}
-
-extern "C" int cgfd_media_layer_onecmp(int NI, int NX, int NY, float MINX, float MINY, float DX,
-                                       float DY, const float *rec, int nx, int ny, int nz,
-                                       const float *x3d, const float *y3d, const float *z3d,
-                                       const char *method, float *var)
-{
-  float *out[1] = {var};
-  return lay_run(LAY_ONE, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
                  method, out);
 }

@@ -1,20 +1,22 @@
 /*
  * media_layer2model_gpu.cpp -- drop-in for CGFD3D's discretisation of
- * elastic isotropic, elastic VTI and one-component (Qp, Qs) layered models
- * on a curvilinear grid.
+ * media on a curvilinear grid: elastic isotropic and elastic VTI layered
+ * models, and models given as binary volumes.
  *
  * Built inside the reference tree (its media headers: inter_t,
- * read_interface_file) and linked with -Wl,--wrap=media_layer2model_el_iso,
- * _el_vti and _onecmp, so the reference's main
- * (forward/main_curv_col_el_3d.c:328-382) calls the __wrap_ functions below
- * with its unchanged arguments.  The
- * .md3lay file is read by the reference's own reader
- * (media/media_read_file.cpp:22-240), its arrays are interleaved into the
- * record layout of cgfd_media_layer_el_iso / _el_vti (include/cgfd3d_gpu.h)
- * and the device computes the medium with the requested equivalent-medium
- * method.  Grids other than curvilinear, methods other than loc/har/ari and
- * other media types go to the reference's routine (__real_...), which
- * handles or rejects them as it always did.  Errors print the library's message and exit(1), as the
+ * read_interface_file) and linked with -Wl,--wrap= for
+ * media_layer2model_el_iso, _el_vti and media_bin2model_el_iso, _vis_iso,
+ * so the reference's main (forward/main_curv_col_el_3d.c:328-515)
+ * calls the __wrap_ functions below with its unchanged arguments.  A .md3lay
+ * file is read by the reference's own reader (media/media_read_file.cpp:
+ * 22-240), its arrays are interleaved into the record layout of
+ * cgfd_media_layer_* (include/cgfd3d_gpu.h) and the device computes the
+ * medium with the requested equivalent-medium method; binary volumes are
+ * read whole, one fread per file instead of one per sample, and
+ * interpolated on the device (cgfd_media_bin_*).  Grids other than
+ * curvilinear, methods other than loc/har/ari and other media types go to
+ * the reference's routine (__real_...), which handles or rejects them as it
+ * always did.  Errors print the library's message and exit(1), as the
  * reference does on bad input.
  */
 #include <cfloat>
@@ -96,6 +98,9 @@ extern "C" int __wrap_media_layer2model_el_iso(float *lam3d, float *mu3d, float 
   const float *cols[10] = {it.elevation, it.rho, it.rho_grad, it.rho_pow, it.vp,
                            it.vp_grad,   it.vp_pow, it.vs,     it.vs_grad, it.vs_pow};
   const std::vector<float> rec = lay_interleave(it, cols, 10);
+  if (!cgfd_media_layer_pow_ok(10, rec.data(), it.NI * it.NX * it.NY))
+    return __real_media_layer2model_el_iso(lam3d, mu3d, rho3d, x3d, y3d, z3d, nx, ny, nz,
+                                           grid_type, in_3lay_file, m, myid);
   if (myid == 0)
     fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
   const int rc = cgfd_media_layer_el_iso((int)it.NI, (int)it.NX, (int)it.NY, it.MINX, it.MINY,
@@ -146,6 +151,9 @@ extern "C" int __wrap_media_layer2model_el_vti(float *rho, float *c11, float *c3
   }
   for (int c = 0; c < 18; c++) cols[1 + c] = p[c];
   const std::vector<float> rec = lay_interleave(it, cols, 19);
+  if (!cgfd_media_layer_pow_ok(19, rec.data(), it.NI * it.NX * it.NY))
+    return __real_media_layer2model_el_vti(rho, c11, c33, c55, c66, c13, x3d, y3d, z3d, nx, ny,
+                                           nz, grid_type, in_3lay_file, m, myid);
   if (myid == 0)
     fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
   const int rc = cgfd_media_layer_el_vti(it.media_type, (int)it.NI, (int)it.NX, (int)it.NY,
@@ -156,32 +164,97 @@ extern "C" int __wrap_media_layer2model_el_vti(float *rho, float *c11, float *c3
   return 0;
 }
 
-extern "C" int __real_media_layer2model_onecmp(float *var3d, const float *x3d, const float *y3d,
-                                               const float *z3d, size_t nx, size_t ny,
-                                               size_t nz, int grid_type, const char *in_var_file,
-                                               const char *average_method, int myid);
-
-extern "C" int __wrap_media_layer2model_onecmp(float *var3d, const float *x3d, const float *y3d,
-                                               const float *z3d, size_t nx, size_t ny,
-                                               size_t nz, int grid_type, const char *in_var_file,
-                                               const char *average_method, int myid)
+/* a whole binary volume of n floats, as stored */
+static std::vector<float> bin_read(const char *file, size_t n)
 {
-  const char *m = average_method;
-  if (!lay_ours(grid_type, m, nx, ny, nz))
-    return __real_media_layer2model_onecmp(var3d, x3d, y3d, z3d, nx, ny, nz, grid_type,
-                                           in_var_file, m, myid);
-  inter_t it;
-  read_interface_file(in_var_file, &it);
-  if (it.media_type != ONE_COMPONENT)
-    return __real_media_layer2model_onecmp(var3d, x3d, y3d, z3d, nx, ny, nz, grid_type,
-                                           in_var_file, m, myid);
-  const float *cols[4] = {it.elevation, it.var, it.var_grad, it.var_pow};
-  const std::vector<float> rec = lay_interleave(it, cols, 4);
-  if (myid == 0)
-    fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
-  const int rc = cgfd_media_layer_onecmp((int)it.NI, (int)it.NX, (int)it.NY, it.MINX, it.MINY,
-                                         it.DX, it.DY, rec.data(), (int)nx, (int)ny, (int)nz,
-                                         x3d, y3d, z3d, m, var3d);
-  if (rc != 0) lay_fail(in_var_file);
+  std::vector<float> v(n);
+  FILE *fp = fopen(file, "rb");
+  if (!fp || fread(v.data(), sizeof(float), n, fp) != n) {
+    fprintf(stderr, "Error: Insufficient data in %s.\n", file);
+    fflush(stderr);
+    exit(1);
+  }
+  fclose(fp);
+  return v;
+}
+
+static cgfd_bin_model_t bin_layout(const int *order, const int *size, const float *spacing,
+                                   const float *origin)
+{
+  cgfd_bin_model_t m;
+  for (int d = 0; d < 3; d++) {
+    m.order[d] = order[d];
+    m.size[d] = size[d];
+    m.spacing[d] = spacing[d];
+    m.origin[d] = origin[d];
+  }
+  return m;
+}
+
+extern "C" int __real_media_bin2model_el_iso(float *rho3d, float *lam3d, float *mu3d,
+                                             const float *x3d, const float *y3d,
+                                             const float *z3d, size_t nx, size_t ny, size_t nz,
+                                             float xmin, float xmax, float ymin, float ymax,
+                                             int grid_type, int *bin_order, int *bin_size,
+                                             float *bin_spacing, float *bin_origin,
+                                             const char *bin_file_rho, const char *bin_file_vp,
+                                             const char *bin_file_vs);
+
+extern "C" int __wrap_media_bin2model_el_iso(float *rho3d, float *lam3d, float *mu3d,
+                                             const float *x3d, const float *y3d,
+                                             const float *z3d, size_t nx, size_t ny, size_t nz,
+                                             float xmin, float xmax, float ymin, float ymax,
+                                             int grid_type, int *bin_order, int *bin_size,
+                                             float *bin_spacing, float *bin_origin,
+                                             const char *bin_file_rho, const char *bin_file_vp,
+                                             const char *bin_file_vs)
+{
+  if (grid_type != GRID_CURV || nx > INT_MAX || ny > INT_MAX || nz > INT_MAX ||
+      bin_size[0] < 1 || bin_size[1] < 1 || bin_size[2] < 1)
+    return __real_media_bin2model_el_iso(rho3d, lam3d, mu3d, x3d, y3d, z3d, nx, ny, nz, xmin,
+                                         xmax, ymin, ymax, grid_type, bin_order, bin_size,
+                                         bin_spacing, bin_origin, bin_file_rho, bin_file_vp,
+                                         bin_file_vs);
+  const size_t n = (size_t)bin_size[0] * bin_size[1] * bin_size[2];
+  fprintf(stdout, "- reading model files %s, %s, %s\n", bin_file_rho, bin_file_vp, bin_file_vs);
+  const std::vector<float> rho = bin_read(bin_file_rho, n), vp = bin_read(bin_file_vp, n),
+                           vs = bin_read(bin_file_vs, n);
+  const cgfd_bin_model_t m = bin_layout(bin_order, bin_size, bin_spacing, bin_origin);
+  fprintf(stdout, "discretising the binary model on the GPU\n");
+  if (cgfd_media_bin_el_iso(&m, xmin, xmax, ymin, ymax, rho.data(), vp.data(), vs.data(),
+                            (int)nx, (int)ny, (int)nz, x3d, y3d, z3d, rho3d, lam3d, mu3d))
+    lay_fail(bin_file_rho);
+  return 0;
+}
+
+extern "C" int __real_media_bin2model_vis_iso(float *Qp3d, float *Qs3d, const float *x3d,
+                                              const float *y3d, const float *z3d, size_t nx,
+                                              size_t ny, size_t nz, float xmin, float xmax,
+                                              float ymin, float ymax, int grid_type,
+                                              int *bin_order, int *bin_size, float *bin_spacing,
+                                              float *bin_origin, const char *bin_file_Qp,
+                                              const char *bin_file_Qs);
+
+extern "C" int __wrap_media_bin2model_vis_iso(float *Qp3d, float *Qs3d, const float *x3d,
+                                              const float *y3d, const float *z3d, size_t nx,
+                                              size_t ny, size_t nz, float xmin, float xmax,
+                                              float ymin, float ymax, int grid_type,
+                                              int *bin_order, int *bin_size, float *bin_spacing,
+                                              float *bin_origin, const char *bin_file_Qp,
+                                              const char *bin_file_Qs)
+{
+  if (grid_type != GRID_CURV || nx > INT_MAX || ny > INT_MAX || nz > INT_MAX ||
+      bin_size[0] < 1 || bin_size[1] < 1 || bin_size[2] < 1)
+    return __real_media_bin2model_vis_iso(Qp3d, Qs3d, x3d, y3d, z3d, nx, ny, nz, xmin, xmax,
+                                          ymin, ymax, grid_type, bin_order, bin_size,
+                                          bin_spacing, bin_origin, bin_file_Qp, bin_file_Qs);
+  const size_t n = (size_t)bin_size[0] * bin_size[1] * bin_size[2];
+  fprintf(stdout, "- reading model files %s, %s\n", bin_file_Qp, bin_file_Qs);
+  const std::vector<float> qp = bin_read(bin_file_Qp, n), qs = bin_read(bin_file_Qs, n);
+  const cgfd_bin_model_t m = bin_layout(bin_order, bin_size, bin_spacing, bin_origin);
+  fprintf(stdout, "discretising the binary model on the GPU\n");
+  if (cgfd_media_bin_vis_iso(&m, xmin, xmax, ymin, ymax, qp.data(), qs.data(), (int)nx,
+                             (int)ny, (int)nz, x3d, y3d, z3d, Qp3d, Qs3d))
+    lay_fail(bin_file_Qp);
   return 0;
 }

@@ -1,4 +1,4 @@
-"""Media discretisation: layered models onto a grid.
+"""Media discretisation: layered and binary-volume models onto a grid.
 
 ``read_md3lay`` parses the reference's layered-model text format (.md3lay,
 media/media_read_file.cpp:22-240) for elastic isotropic models;
@@ -104,31 +104,50 @@ def layer_el_vti(model, x3d, y3d, z3d, method="loc"):
     return tuple(out)
 
 
-def layer_onecmp(model, x3d, y3d, z3d, method="loc"):
-    """One component (Qp, Qs, ...) of a one_component model on the grid,
-    computed on the device (cgfd_media_layer_onecmp)."""
-    if model.get("media_type") != "one_component":
-        raise ValueError("layer_onecmp takes one_component models")
-    shape = np.shape(x3d)
-    nz, ny, nx = shape
-    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
-    rec = np.ascontiguousarray(model["rec"], np.float32)
-    out = np.empty(shape, np.float32)
-    _lib.check(_lib.lib().cgfd_media_layer_onecmp(
-        int(model["NI"]), int(model["NX"]), int(model["NY"]), C.c_float(model["MINX"]),
-        C.c_float(model["MINY"]), C.c_float(model["DX"]), C.c_float(model["DY"]),
-        rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
-        method.encode(), out.ctypes.data))
-    return (out,)
-
-
 def layer(model, x3d, y3d, z3d, method="loc"):
-    """The model's medium on the grid: (var,) for one-component models,
-    (lambda, mu, rho) for elastic isotropic models, (c11, c33, c55, c66, c13,
-    rho) for VTI ones."""
+    """The model's medium on the grid: (lambda, mu, rho) for elastic
+    isotropic models, (c11, c33, c55, c66, c13, rho) for VTI ones.
+    One-component models (Qp, Qs) are read but not discretised on the
+    device."""
     kind = model.get("media_type", "elastic_isotropic")
     if kind == "one_component":
-        return layer_onecmp(model, x3d, y3d, z3d, method)
+        raise ValueError("one-component layered models are not discretised on the device")
     if kind == "elastic_isotropic":
         return layer_el_iso(model, x3d, y3d, z3d, method)
     return layer_el_vti(model, x3d, y3d, z3d, method)
+
+
+class BinModel(C.Structure):
+    """cgfd_bin_model_t: the layout of a model given as binary volumes, as
+    the reference's par file gives it (bin_order, bin_size, bin_spacing,
+    bin_origin)."""
+    _fields_ = [("order", C.c_int * 3), ("size", C.c_int * 3), ("spacing", C.c_float * 3),
+                ("origin", C.c_float * 3)]
+
+    @classmethod
+    def of(cls, order, size, spacing, origin):
+        m = cls()
+        for d in range(3):
+            m.order[d], m.size[d] = int(order[d]), int(size[d])
+            m.spacing[d], m.origin[d] = float(spacing[d]), float(origin[d])
+        return m
+
+
+def bin_model(layout, ext, vols, x3d, y3d, z3d, vis=False):
+    """A model given as binary volumes on the grid, on the device: rho,
+    lambda, mu from (rho, vp, vs) volumes, or Qp, Qs from (Qp, Qs) volumes
+    when vis is set.  layout: BinModel; ext: the grid's xmin, xmax, ymin,
+    ymax; vols: the volumes as stored in their files (flat or shaped)."""
+    shape = np.shape(x3d)
+    nz, ny, nx = shape
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    nfile = layout.size[0] * layout.size[1] * layout.size[2]
+    v = [np.ascontiguousarray(a, np.float32).ravel() for a in vols]
+    if len(v) != (2 if vis else 3) or any(a.size != nfile for a in v):
+        raise ValueError("expected %d volumes of %d samples" % (2 if vis else 3, nfile))
+    out = [np.empty(shape, np.float32) for _ in v]
+    fn = _lib.lib().cgfd_media_bin_vis_iso if vis else _lib.lib().cgfd_media_bin_el_iso
+    _lib.check(fn(C.byref(layout), *[C.c_float(float(e)) for e in ext],
+                  *[a.ctypes.data for a in v], nx, ny, nz, x.ctypes.data, y.ctypes.data,
+                  z.ctypes.data, *[o.ctypes.data for o in out]))
+    return tuple(out)

@@ -341,7 +341,13 @@ void cgfd_locator_destroy(cgfd_locator_t *loc);
  * two layers) or "ari" (arithmetic lambda, mu, rho there).  Writes lam, mu,
  * rho (host, nx*ny*nz each).  A point outside the mesh or with
  * vp <= sqrt(2) vs is CGFD_EINVAL (the reference exits there), and so is
- * another method. */
+ * another method, and so is a model with a power outside [0, 1] on a
+ * non-zero gradient: cgfd_media_layer_pow_ok(nc, rec, NI*NX*NY) tells it
+ * beforehand
+ * (nc: the record width, 10 here, 19 for VTI), and callers then use the
+ * reference's host routine. */
+int cgfd_media_layer_pow_ok(int nc, const float *rec, size_t nrec);
+
 int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY, float DX,
                             float DY, const float *rec, int nx, int ny, int nz,
                             const float *x3d, const float *y3d, const float *z3d,
@@ -368,16 +374,40 @@ int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, float MINX, 
                             const char *method, float *c11, float *c33, float *c55,
                             float *c66, float *c13, float *rho);
 
-/* One component of a layered model (the Qp and Qs of visco-elastic runs)
- * discretised on a curvilinear grid, as media_layer2model_onecmp does
- * (media/media_layer2model.cpp:47-88, 1239-1283, 1603-1782; called at
- * forward/main_curv_col_el_3d.c:370-382): rec [NI][NY][NX][4] = elevation,
- * value, gradient, power; "har" averages the value harmonically, "ari"
- * arithmetically.  Writes var (host, nx*ny*nz). */
-int cgfd_media_layer_onecmp(int NI, int NX, int NY, float MINX, float MINY, float DX, float DY,
-                            const float *rec, int nx, int ny, int nz, const float *x3d,
-                            const float *y3d, const float *z3d, const char *method,
-                            float *var);
+
+/* A model given as binary volumes of float samples on a regular 3-D mesh,
+ * described as the reference's par file describes it: order[i] is the axis
+ * (0 x, 1 y, 2 z) of the i-th dimension of the files, fastest first;
+ * size, spacing and origin per file dimension (the z spacing may be
+ * negative). */
+typedef struct {
+  int order[3];
+  int size[3];
+  float spacing[3];
+  float origin[3];
+} cgfd_bin_model_t;
+
+/* rho, lambda, mu interpolated from rho, vp, vs volumes (whole files in
+ * their stored order, size[0]*size[1]*size[2] floats each) on a curvilinear
+ * grid, as media_bin2model_el_iso does (media/media_bin2model.cpp:27-234;
+ * called at forward/main_curv_col_el_3d.c:470-484): the volumes cropped to
+ * the grid's [xmin, xmax] x [ymin, ymax], then trilinear interpolation at
+ * every point (TrilinearInterpolation, media/media_utility.cpp:299-391),
+ * points beyond the model taking its edge.  A model that misses the grid,
+ * a bad order, or a crop with fewer than two samples along an axis is
+ * CGFD_EINVAL. */
+int cgfd_media_bin_el_iso(const cgfd_bin_model_t *model, float xmin, float xmax, float ymin,
+                          float ymax, const float *rho_vol, const float *vp_vol,
+                          const float *vs_vol, int nx, int ny, int nz, const float *x3d,
+                          const float *y3d, const float *z3d, float *rho, float *lam,
+                          float *mu);
+
+/* Qp, Qs interpolated from Qp, Qs volumes the same way
+ * (media_bin2model_vis_iso, media/media_bin2model.cpp:236-432). */
+int cgfd_media_bin_vis_iso(const cgfd_bin_model_t *model, float xmin, float xmax, float ymin,
+                           float ymax, const float *qp_vol, const float *qs_vol, int nx,
+                           int ny, int nz, const float *x3d, const float *y3d,
+                           const float *z3d, float *qp, float *qs);
 
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);

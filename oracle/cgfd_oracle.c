@@ -2262,3 +2262,148 @@ int oracle_layer_el_iso_loc(int NI, int NX, int NY, float MINX, float MINY, floa
   return oracle_layer_el_iso(0, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d,
                              z3d, lam, mu, rho);
 }
+
+/* ------------------------------------------------------------------------ */
+/* models given as binary volumes (media/media_bin2model.cpp:27-432)          */
+/* ------------------------------------------------------------------------ */
+
+/* The crop of the volumes to the grid's x/y range and the coordinate
+ * vectors (media_bin2model_el_iso, media/media_bin2model.cpp:44-158).
+ * Returns 1 where the reference exits (bad bin_order, no overlap), and 1
+ * where the crop keeps fewer than two samples along an axis (the
+ * reference's interpolation would read past its vectors). */
+typedef struct {
+  int dim[3];            /* file dimension holding x, y, z */
+  int start[2];          /* first kept x, y sample */
+  int n[3];              /* kept samples along x, y, z */
+  size_t st[3];          /* file strides of x, y, z */
+  float *xv, *yv, *zv;
+} bin_crop_t;
+
+static int bin_setup(const int *order, const int *size, const float *spacing,
+                     const float *origin, const float *ext, size_t vol, const float *z3d,
+                     bin_crop_t *b)
+{
+  int dimx = -1, dimy = -1, dimz = -1;
+  for (int i = 0; i < 3; i++) {
+    if (order[i] == 0) dimx = i;
+    else if (order[i] == 1) dimy = i;
+    else if (order[i] == 2) dimz = i;
+    else return 1;
+  }
+  if (dimx == -1 || dimy == -1 || dimz == -1) return 1;
+  const float xmin = ext[0], xmax = ext[1], ymin = ext[2], ymax = ext[3];
+  const float bx0 = origin[dimx], by0 = origin[dimy], bz0 = origin[dimz];
+  const float bdx = spacing[dimx], bdy = spacing[dimy], bdz = spacing[dimz];
+  int ix_start = (xmin < bx0 ? 0 : (xmin - bx0) / bdx);
+  if (ix_start >= size[dimx] || xmax < bx0) return 1;
+  int ix_end = ceil((xmax - bx0) / bdx);
+  if (ix_end >= size[dimx]) ix_end = size[dimx] - 1;
+  int iy_start = (ymin < by0 ? 0 : (ymin - by0) / bdy);
+  if (iy_start >= size[dimy] || ymax < by0) return 1;
+  int iy_end = ceil((ymax - by0) / bdy);
+  if (iy_end >= size[dimy]) iy_end = size[dimy] - 1;
+  float zmin = FLT_MAX, zmax = -FLT_MAX;
+  for (size_t i = 0; i < vol; i++) {
+    zmin = fminf(zmin, z3d[i]);
+    zmax = fmaxf(zmax, z3d[i]);
+  }
+  float bzn = bz0 + bdz * (size[dimz] - 1);
+  if (zmin >= fmaxf(bzn, bz0) || zmax <= fminf(bz0, bzn)) return 1;
+  b->dim[0] = dimx; b->dim[1] = dimy; b->dim[2] = dimz;
+  b->start[0] = ix_start; b->start[1] = iy_start;
+  b->n[0] = ix_end - ix_start + 1;
+  b->n[1] = iy_end - iy_start + 1;
+  b->n[2] = size[dimz];
+  if (b->n[0] < 2 || b->n[1] < 2 || b->n[2] < 2) return 1;
+  const size_t fst[3] = {1, (size_t)size[0], (size_t)size[0] * size[1]};
+  for (int d = 0; d < 3; d++) b->st[d] = fst[b->dim[d]];
+  b->xv = malloc(b->n[0] * sizeof(float));
+  b->yv = malloc(b->n[1] * sizeof(float));
+  b->zv = malloc(b->n[2] * sizeof(float));
+  for (size_t i = 0; i < (size_t)b->n[0]; i++) b->xv[i] = bx0 + (ix_start + i) * bdx;
+  for (size_t i = 0; i < (size_t)b->n[1]; i++) b->yv[i] = by0 + (iy_start + i) * bdy;
+  for (size_t i = 0; i < (size_t)b->n[2]; i++) b->zv[i] = bz0 + i * bdz;
+  return 0;
+}
+
+/* one volume (file order) at (xq, yq, zq): TrilinearInterpolation
+ * (media/media_utility.cpp:299-391) on the cropped vectors */
+static float bin_trilinear(const bin_crop_t *b, const float *v, float xq, float yq, float zq)
+{
+  const float *x = b->xv, *y = b->yv, *z = b->zv;
+  const int nx = b->n[0], ny = b->n[1], nz = b->n[2];
+  float dx = x[1] - x[0], dy = y[1] - y[0], dz = z[1] - z[0];
+  int ix0 = floor((xq - x[0]) / dx), iy0 = floor((yq - y[0]) / dy);
+  int ix2 = ceil((xq - x[0]) / dx), iy2 = ceil((yq - y[0]) / dy);
+  ix0 = ix0 < 0 ? 0 : ix0;
+  ix2 = ix2 < 0 ? 0 : ix2;
+  ix0 = ix0 > nx - 1 ? nx - 1 : ix0;
+  ix2 = ix2 > nx - 1 ? nx - 1 : ix2;
+  iy0 = iy0 < 0 ? 0 : iy0;
+  iy2 = iy2 < 0 ? 0 : iy2;
+  iy0 = iy0 > ny - 1 ? ny - 1 : iy0;
+  iy2 = iy2 > ny - 1 ? ny - 1 : iy2;
+  int iz0 = floor((zq - z[0]) / dz), iz2 = ceil((zq - z[0]) / dz);
+  iz0 = iz0 < 0 ? 0 : iz0;
+  iz0 = iz0 > nz - 1 ? nz - 1 : iz0;
+  iz2 = iz2 > nz - 1 ? nz - 1 : iz2;
+  iz2 = iz2 < 0 ? 0 : iz2;
+#define BINV(i, j, k) \
+  v[(size_t)((i) + b->start[0]) * b->st[0] + (size_t)((j) + b->start[1]) * b->st[1] + \
+    (size_t)(k) * b->st[2]]
+  if (ix0 == ix2 && iy0 == iy2 && iz0 == iz2) return BINV(ix0, iy0, iz0);
+  float v000 = BINV(ix0, iy0, iz0), v002 = BINV(ix0, iy0, iz2);
+  float v200 = BINV(ix2, iy0, iz0), v202 = BINV(ix2, iy0, iz2);
+  float v020 = BINV(ix0, iy2, iz0), v022 = BINV(ix0, iy2, iz2);
+  float v220 = BINV(ix2, iy2, iz0), v222 = BINV(ix2, iy2, iz2);
+#undef BINV
+  float v100, v102, v122, v120;
+  if (ix0 == ix2) {
+    v100 = v000; v102 = v002; v122 = v022; v120 = v020;
+  } else {
+    float w = (xq - x[ix0]) / (x[ix2] - x[ix0]);
+    v100 = v000 + w * (v200 - v000);
+    v102 = v002 + w * (v202 - v002);
+    v122 = v022 + w * (v222 - v022);
+    v120 = v020 + w * (v220 - v020);
+  }
+  float v110, v112;
+  if (iy0 == iy2) {
+    v110 = v100; v112 = v102;
+  } else {
+    float w = (yq - y[iy0]) / (y[iy2] - y[iy0]);
+    v110 = v100 + w * (v120 - v100);
+    v112 = v102 + w * (v122 - v102);
+  }
+  if (iz0 == iz2) return v110;
+  return v110 + (zq - z[iz0]) / (z[iz2] - z[iz0]) * (v112 - v110);
+}
+
+/* vis 0: rho, lambda, mu from volumes rho, vp, vs
+ * (parameterization_bin_el_iso_loc, media/media_bin2model.cpp:185-234);
+ * vis 1: Qp, Qs from volumes Qp, Qs (:387-432).  ext: xmin xmax ymin ymax
+ * of the grid.  Returns 1 where the reference exits. */
+int oracle_bin(int vis, const int *order, const int *size, const float *spacing,
+               const float *origin, const float *ext, const float *const *vols, int nx, int ny,
+               int nz, const float *x3d, const float *y3d, const float *z3d, float **out)
+{
+  const size_t vol = (size_t)nx * ny * nz;
+  bin_crop_t b;
+  if (bin_setup(order, size, spacing, origin, ext, vol, z3d, &b)) return 1;
+  for (size_t q = 0; q < vol; q++) {
+    if (vis) {
+      out[0][q] = bin_trilinear(&b, vols[0], x3d[q], y3d[q], z3d[q]);
+      out[1][q] = bin_trilinear(&b, vols[1], x3d[q], y3d[q], z3d[q]);
+    } else {
+      float rho = bin_trilinear(&b, vols[0], x3d[q], y3d[q], z3d[q]);
+      float vp = bin_trilinear(&b, vols[1], x3d[q], y3d[q], z3d[q]);
+      float vs = bin_trilinear(&b, vols[2], x3d[q], y3d[q], z3d[q]);
+      out[2][q] = vs * vs * rho;
+      out[1][q] = vp * vp * rho - 2.0 * out[2][q];
+      out[0][q] = rho;
+    }
+  }
+  free(b.xv); free(b.yv); free(b.zv);
+  return 0;
+}

@@ -1,6 +1,6 @@
 /*
  * media_stub.c -- TEST INFRASTRUCTURE ONLY.  Stands in for the CUDA
- * library's cgfd_media_layer_el_iso, _el_vti and _onecmp
+ * library's cgfd_media_layer_el_iso, _el_vti and cgfd_media_bin_*
  * (include/cgfd3d_gpu.h) in a CPU-only
  * link of the reference with the media drop-in adapter
  * (cgfd3d_gb300/csrc/dropin/media_layer2model_gpu.cpp), so a test can run
@@ -18,6 +18,12 @@ int oracle_layer(int kind, int method, int NI, int NX, int NY, float MINX, float
                  const float *x3d, const float *y3d, const float *z3d, float **out);
 
 static const char *stub_msg = "";
+
+int cgfd_media_layer_pow_ok(int nc, const float *rec, size_t nrec)
+{
+  (void)nc; (void)rec; (void)nrec;
+  return 1;
+}
 
 static int stub_method(const char *method)
 {
@@ -65,11 +71,41 @@ int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, float MINX, 
 
 const char *cgfd_last_error(void) { return stub_msg; }
 
-int cgfd_media_layer_onecmp(int NI, int NX, int NY, float MINX, float MINY, float DX, float DY,
-                            const float *rec, int nx, int ny, int nz, const float *x3d,
-                            const float *y3d, const float *z3d, const char *method, float *var)
+
+int oracle_bin(int vis, const int *order, const int *size, const float *spacing,
+               const float *origin, const float *ext, const float *const *vols, int nx, int ny,
+               int nz, const float *x3d, const float *y3d, const float *z3d, float **out);
+
+static int stub_bin(int vis, const cgfd_bin_model_t *m, float xmin, float xmax, float ymin,
+                    float ymax, const float *const *v, int nx, int ny, int nz,
+                    const float *x3d, const float *y3d, const float *z3d, float **o)
 {
-  float *out[1] = {var};
-  return stub_run(0, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d, method,
-                  out);
+  const float ext[4] = {xmin, xmax, ymin, ymax};
+  if (oracle_bin(vis, m->order, m->size, m->spacing, m->origin, ext, v, nx, ny, nz, x3d, y3d,
+                 z3d, o)) {
+    stub_msg = "binary model: the model does not cover the grid";
+    return CGFD_EINVAL;
+  }
+  return 0;
+}
+
+int cgfd_media_bin_el_iso(const cgfd_bin_model_t *model, float xmin, float xmax, float ymin,
+                          float ymax, const float *rho_vol, const float *vp_vol,
+                          const float *vs_vol, int nx, int ny, int nz, const float *x3d,
+                          const float *y3d, const float *z3d, float *rho, float *lam,
+                          float *mu)
+{
+  const float *v[3] = {rho_vol, vp_vol, vs_vol};
+  float *o[3] = {rho, lam, mu};
+  return stub_bin(0, model, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
+}
+
+int cgfd_media_bin_vis_iso(const cgfd_bin_model_t *model, float xmin, float xmax, float ymin,
+                           float ymax, const float *qp_vol, const float *qs_vol, int nx,
+                           int ny, int nz, const float *x3d, const float *y3d,
+                           const float *z3d, float *qp, float *qs)
+{
+  const float *v[2] = {qp_vol, qs_vol};
+  float *o[2] = {qp, qs};
+  return stub_bin(1, model, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
 }

@@ -187,3 +187,28 @@ def layer_el_iso(model, x3d, y3d, z3d, method="loc"):
 def layer_el_iso_loc(model, x3d, y3d, z3d):
     """layer_el_iso with the "loc" method."""
     return layer_el_iso(model, x3d, y3d, z3d, "loc")
+
+
+def bin_model(m, x3d, y3d, z3d, vis=False):
+    """A model given as binary volumes (dict: order, size, spacing, origin,
+    ext and the file-order volumes rho_vol, vp_vol, vs_vol or qp_vol, qs_vol)
+    interpolated on a grid as media_bin2model_el_iso (rho, lambda, mu) or
+    media_bin2model_vis_iso (Qp, Qs) does; None where the reference exits."""
+    import numpy as np
+    L = lib()
+    L.oracle_bin.restype = C.c_int
+    L.oracle_bin.argtypes = [C.c_int] + [C.c_void_p] * 6 + [C.c_int] * 3 + [C.c_void_p] * 4
+    nz, ny, nx = np.shape(x3d)
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    keys = ("qp_vol", "qs_vol") if vis else ("rho_vol", "vp_vol", "vs_vol")
+    vols = [np.ascontiguousarray(m[k], np.float32) for k in keys]
+    hdr = [np.ascontiguousarray(m[k], t) for k, t in
+           (("order", np.int32), ("size", np.int32), ("spacing", np.float32),
+            ("origin", np.float32), ("ext", np.float32))]
+    out = [np.zeros((nz, ny, nx), np.float32) for _ in keys]
+    vp_ = (C.c_void_p * len(vols))(*[v.ctypes.data for v in vols])
+    op_ = (C.c_void_p * len(out))(*[o.ctypes.data for o in out])
+    bad = L.oracle_bin(1 if vis else 0, *[h.ctypes.data for h in hdr], C.cast(vp_, C.c_void_p),
+                       nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
+                       C.cast(op_, C.c_void_p))
+    return None if bad else tuple(out)

@@ -43,6 +43,15 @@
  *       a one-component layered model (Qp, Qs, ...) discretised by
  *       media_layer2model_onecmp (media/media_layer2model.cpp:47-88);
  *       <output>: float var [nz][ny][nx]
+ *
+ *   ref_probe bin <grid> <params> <rho> <vp> <vs> <output>
+ *   ref_probe bin_vis <grid> <params> <Qp> <Qs> <output>
+ *       a model given as binary volumes interpolated on a curvilinear grid
+ *       by media_bin2model_el_iso / media_bin2model_vis_iso
+ *       (media/media_bin2model.cpp:27-432).  <params>: int bin_order[3],
+ *       bin_size[3]; float bin_spacing[3], bin_origin[3], xmin, xmax, ymin,
+ *       ymax.  <output>: float rho, lambda, mu (bin) or Qp, Qs (bin_vis)
+ *       [nz][ny][nx]
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -66,6 +75,17 @@ int media_layer2model_el_vti(float *rho, float *c11, float *c33, float *c55, flo
 int media_layer2model_onecmp(float *var3d, const float *x3d, const float *y3d,
                              const float *z3d, size_t nx, size_t ny, size_t nz, int grid_type,
                              const char *in_var_file, const char *average_method, int myid);
+int media_bin2model_el_iso(float *rho3d, float *lam3d, float *mu3d, const float *x3d,
+                           const float *y3d, const float *z3d, size_t nx, size_t ny, size_t nz,
+                           float xmin, float xmax, float ymin, float ymax, int grid_type,
+                           int *bin_order, int *bin_size, float *bin_spacing,
+                           float *bin_origin, const char *bin_file_rho, const char *bin_file_vp,
+                           const char *bin_file_vs);
+int media_bin2model_vis_iso(float *Qp3d, float *Qs3d, const float *x3d, const float *y3d,
+                            const float *z3d, size_t nx, size_t ny, size_t nz, float xmin,
+                            float xmax, float ymin, float ymax, int grid_type, int *bin_order,
+                            int *bin_size, float *bin_spacing, float *bin_origin,
+                            const char *bin_file_Qp, const char *bin_file_Qs);
 #define PROBE_GRID_CURV 3
 
 static void rd(void *p, size_t n, FILE *fp)
@@ -284,6 +304,47 @@ static int probe_layer_one(const char *lay, const char *grid, const char *method
   return 0;
 }
 
+static int probe_bin(int vis, const char *grid, const char *params, const char *const *files,
+                     const char *out)
+{
+  FILE *fp = fopen(grid, "rb");
+  if (!fp) return 2;
+  int d[3];
+  rd(d, sizeof d, fp);
+  size_t vol = (size_t)d[0] * d[1] * d[2];
+  float *x = malloc(vol * 4), *y = malloc(vol * 4), *z = malloc(vol * 4);
+  rd(x, vol * 4, fp);
+  rd(y, vol * 4, fp);
+  rd(z, vol * 4, fp);
+  fclose(fp);
+  fp = fopen(params, "rb");
+  if (!fp) return 2;
+  int order[3], size[3];
+  float spacing[3], origin[3], ext[4];
+  rd(order, sizeof order, fp);
+  rd(size, sizeof size, fp);
+  rd(spacing, sizeof spacing, fp);
+  rd(origin, sizeof origin, fp);
+  rd(ext, sizeof ext, fp);
+  fclose(fp);
+  const int nout = vis ? 2 : 3;
+  float *o[3];
+  for (int n = 0; n < nout; n++) o[n] = calloc(vol, 4);
+  if (vis)
+    media_bin2model_vis_iso(o[0], o[1], x, y, z, d[0], d[1], d[2], ext[0], ext[1], ext[2],
+                            ext[3], PROBE_GRID_CURV, order, size, spacing, origin, files[0],
+                            files[1]);
+  else
+    media_bin2model_el_iso(o[0], o[1], o[2], x, y, z, d[0], d[1], d[2], ext[0], ext[1], ext[2],
+                           ext[3], PROBE_GRID_CURV, order, size, spacing, origin, files[0],
+                           files[1], files[2]);
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  for (int n = 0; n < nout; n++) fwrite(o[n], 4, vol, fo);
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
@@ -294,6 +355,10 @@ int main(int argc, char **argv)
     return probe_layer_vti(argv[2], argv[3], argv[4], argv[5]);
   if (argc == 6 && strcmp(argv[1], "layer_one") == 0)
     return probe_layer_one(argv[2], argv[3], argv[4], argv[5]);
+  if (argc == 8 && strcmp(argv[1], "bin") == 0)
+    return probe_bin(0, argv[2], argv[3], (const char *const *)argv + 4, argv[7]);
+  if (argc == 7 && strcmp(argv[1], "bin_vis") == 0)
+    return probe_bin(1, argv[2], argv[3], (const char *const *)argv + 4, argv[6]);
   fprintf(stderr, "usage: ref_probe sac|locate <input> <output> | "
                   "layer|layer_vti|layer_one <md3lay> <grid> <method> <output>\n");
   return 2;

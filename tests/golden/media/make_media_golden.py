@@ -22,6 +22,13 @@ gradients and powers) on the first grid, discretised by
 media_layer2model_onecmp (media/media_layer2model.cpp:47-88) with each
 method; keys md3lay, var_loc, var_har, var_ari.
 
+And bin_model.npz: a model given as binary volumes (stored z fastest,
+then x, then y; z decreasing; wider than the grid in x and y and shallower
+than its bottom) interpolated on the first grid by media_bin2model_el_iso
+and media_bin2model_vis_iso (media/media_bin2model.cpp:27-432); keys
+order, size, spacing, origin, ext (xmin xmax ymin ymax), rho_vol, vp_vol,
+vs_vol, qp_vol, qs_vol (file order) and rho, lam, mu, Qp, Qs.
+
 This script needs the reference build and runs only where it exists; the
 fixtures it writes are committed and are all the tests need elsewhere.
 
@@ -177,6 +184,7 @@ def main():
           % ((res["lam_har"] != res["lam"]).sum(), (res["lam_ari"] != res["lam"]).sum()))
     vti_main()
     one_main(X, Y, Z)
+    bin_main(X, Y, Z)
     on = int(np.isclose(Z, -800.0).sum())
     print("grid %s, %d points on the flat interface, rho range %.1f-%.1f"
           % (X.shape, on, out[2].min(), out[2].max()))
@@ -211,6 +219,62 @@ def one_main(X, Y, Z):
             res["var_" + meth] = np.fromfile(opath, "<f4").reshape(nz, ny, nx)
     np.savez_compressed(os.path.join(HERE, "layer_onecmp.npz"), **res)
     print("onecmp: har changed %d points" % (res["var_har"] != res["var_loc"]).sum())
+
+
+def bin_main(X, Y, Z):
+    rng = np.random.default_rng(17)
+    order = np.array([2, 0, 1], np.int32)              # file dims: z, x, y
+    dx, dy, dz = 110.0, 130.0, -85.0
+    x0, y0, z0 = float(X.min()) - 250.0, float(Y.min()) - 200.0, 400.0
+    nxb = int((float(X.max()) + 300.0 - x0) / dx) + 1
+    nyb = int((float(Y.max()) + 250.0 - y0) / dy) + 1
+    nzb = 20                                            # to z = -1215: the grid goes deeper
+    size = np.array([nzb, nxb, nyb], np.int32)
+    spacing = np.array([dz, dx, dy], np.float32)
+    origin = np.array([z0, x0, y0], np.float32)
+    zz = z0 + dz * np.arange(nzb)
+    xx = x0 + dx * np.arange(nxb)
+    yy = y0 + dy * np.arange(nyb)
+    Yg, Xg, Zg = np.meshgrid(yy, xx, zz, indexing="ij")    # [y][x][z]: z fastest
+    depth = np.clip(-Zg, 0, None)
+
+    def field(base, grad, amp):
+        return (base + grad * depth + amp * np.sin(Xg / 400.0 + 0.3 * Zg / 100.0)
+                * np.cos(Yg / 500.0) + amp * 0.3 * rng.standard_normal(Xg.shape))
+
+    vols = {"rho_vol": field(2200.0, 0.4, 40.0), "vp_vol": field(3600.0, 1.5, 150.0),
+            "vs_vol": field(2000.0, 0.9, 80.0), "qp_vol": field(120.0, 0.08, 10.0),
+            "qs_vol": field(60.0, 0.04, 5.0)}
+    vols = {k: v.astype(np.float32) for k, v in vols.items()}
+    ext = np.array([X.min(), X.max(), Y.min(), Y.max()], np.float32)
+    nz, ny, nx = X.shape
+    res = dict(order=order, size=size, spacing=spacing, origin=origin, ext=ext, **vols)
+    with tempfile.TemporaryDirectory() as tmp:
+        gpath = os.path.join(tmp, "grid.bin")
+        with open(gpath, "wb") as f:
+            f.write(struct.pack("<3i", nx, ny, nz))
+            for A in (X, Y, Z):
+                f.write(A.astype("<f4").tobytes())
+        ppath = os.path.join(tmp, "params.bin")
+        with open(ppath, "wb") as f:
+            for a in (order, size, spacing, origin, ext):
+                f.write(a.tobytes())
+        files = {}
+        for k, v in vols.items():
+            files[k] = os.path.join(tmp, k + ".bin")
+            v.tofile(files[k])
+        opath = os.path.join(tmp, "out.bin")
+        subprocess.run([PROBE, "bin", gpath, ppath, files["rho_vol"], files["vp_vol"],
+                        files["vs_vol"], opath], check=True, stdout=subprocess.DEVNULL)
+        o = np.fromfile(opath, "<f4").reshape(3, nz, ny, nx)
+        res.update(rho=o[0], lam=o[1], mu=o[2])
+        subprocess.run([PROBE, "bin_vis", gpath, ppath, files["qp_vol"], files["qs_vol"],
+                        opath], check=True, stdout=subprocess.DEVNULL)
+        o = np.fromfile(opath, "<f4").reshape(2, nz, ny, nx)
+        res.update(Qp=o[0], Qs=o[1])
+    np.savez_compressed(os.path.join(HERE, "bin_model.npz"), **res)
+    print("bin: model %s (z, x, y), rho %.1f-%.1f" % (tuple(size), res["rho"].min(),
+                                                     res["rho"].max()))
 
 
 def vti_main():

@@ -1,5 +1,6 @@
-"""The reference solver links with its time loop and its layered-media
-discretisation replaced by the GPU library.
+"""The reference solver links with its time loop and its media
+discretisation (layered and binary-volume models) replaced by the GPU
+library.
 
 Where the reference tree is present, oracle/Makefile builds the reference's
 main with the drop-in adapter compiled against the reference's own headers in
@@ -30,5 +31,9 @@ def test_reference_main_links_against_gpu_library():
     assert " U cgfd_solver_create" in syms
     assert " T sv_curv_col_el_iso_onestage" in syms  # the rest of the reference
     # the layered-media discretisation: main's call is wrapped by the adapter
-    assert " T __wrap_media_layer2model_el_iso" in syms
-    assert " U cgfd_media_layer_el_iso" in syms
+    for fn in ("media_layer2model_el_iso", "media_layer2model_el_vti",
+               "media_bin2model_el_iso", "media_bin2model_vis_iso"):
+        assert " T __wrap_" + fn in syms
+    for fn in ("cgfd_media_layer_el_iso", "cgfd_media_layer_el_vti",
+               "cgfd_media_bin_el_iso", "cgfd_media_bin_vis_iso"):
+        assert " U " + fn in syms

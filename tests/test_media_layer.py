@@ -13,6 +13,7 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FIX = os.path.join(REPO, "tests", "golden", "media", "layer_el_iso.npz")
 FIX_VTI = os.path.join(REPO, "tests", "golden", "media", "layer_el_vti.npz")
 FIX_ONE = os.path.join(REPO, "tests", "golden", "media", "layer_onecmp.npz")
+FIX_BIN = os.path.join(REPO, "tests", "golden", "media", "bin_model.npz")
 VTI_OUT = ("c11", "c33", "c55", "c66", "c13", "rho")
 VTI_CASES = [("elastic_vti_prem", "loc"), ("elastic_vti_prem", "ari"),
              ("elastic_vti_thomsen", "loc"), ("elastic_vti_thomsen", "har"),
@@ -88,6 +89,39 @@ def test_oracle_onecmp_matches_reference_bitwise(method):
     assert m["media_type"] == "one_component" and m["rec"].shape[-1] == 4
     got = oracle.layer(m, g["x3d"], g["y3d"], g["z3d"], method)[0]
     np.testing.assert_array_equal(got.view(np.int32), z["var_" + method].view(np.int32))
+
+
+@pytest.mark.parametrize("vis", [False, True])
+def test_oracle_bin_matches_reference_bitwise(vis):
+    """Binary-volume models (media_bin2model_el_iso / _vis_iso): stored z
+    fastest, z decreasing, cropped in x and y, grid points below the model."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    z = np.load(FIX_BIN)
+    g = np.load(FIX)
+    got = oracle.bin_model(z, g["x3d"], g["y3d"], g["z3d"], vis)
+    for a, k in zip(got, ("Qp", "Qs") if vis else ("rho", "lam", "mu")):
+        np.testing.assert_array_equal(a.view(np.int32), z[k].view(np.int32))
+    # the grid reaches below the model: those points take its last level
+    assert g["z3d"].min() < float(z["origin"][0] + z["spacing"][0] * (z["size"][0] - 1))
+
+
+def test_pow_guard():
+    """cgfd_media_layer_pow_ok (host logic, no device work): the fixtures'
+    powers are in [0, 1]; a power of 1.2 on a non-zero gradient is refused,
+    on a zero gradient it is not evaluated and passes."""
+    from cgfd3d_gb300 import _lib
+    L = _lib.lib()
+    z, m = _fixture()
+    r = np.ascontiguousarray(m["rec"], np.float32)
+    assert L.cgfd_media_layer_pow_ok(10, r.ctypes.data, r.size // 10) == 1
+    r2 = r.copy()
+    r2[1, 2, 3, 6] = 1.2                       # vp power, gradient 0.3-0.4 there
+    assert L.cgfd_media_layer_pow_ok(10, r2.ctypes.data, r2.size // 10) == 0
+    r3 = r.copy()
+    r3[1, 2, 3, 9] = 1.2                       # vs power with its gradient zeroed
+    r3[1, 2, 3, 8] = 0.0
+    assert L.cgfd_media_layer_pow_ok(10, r3.ctypes.data, r3.size // 10) == 1
 
 
 def test_har_and_ari_differ():
@@ -191,38 +225,60 @@ def test_dropin_adapter_vti_inside_reference(kind, method, tmp_path):
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
                     reason="reference tree not present")
-@pytest.mark.parametrize("method", ["loc", "har", "ari"])
-def test_dropin_adapter_onecmp_inside_reference(method, tmp_path):
-    """As test_dropin_adapter_inside_reference, for media_layer2model_onecmp."""
-    import struct
+@pytest.mark.parametrize("vis", [False, True])
+def test_dropin_adapter_bin_inside_reference(vis, tmp_path):
+    """The adapter takes the reference's media_bin2model_el_iso / _vis_iso
+    calls: whole-file reads, library call (answered by the oracle here),
+    the reference's values bit for bit."""
     import subprocess
     subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
                     "_ref/ref_probe_media"], check=True, capture_output=True)
-    z, g, _ = _one()
-    lay = tmp_path / "qs.md3lay"
-    lay.write_bytes(bytes(z["md3lay"]))
+    z = np.load(FIX_BIN)
+    g = np.load(FIX)
     nz, ny, nx = g["x3d"].shape
     grid = tmp_path / "grid.bin"
     with open(grid, "wb") as f:
-        f.write(struct.pack("<3i", nx, ny, nz))
+        f.write(np.array([nx, ny, nz], "<i4").tobytes())
         for a in (g["x3d"], g["y3d"], g["z3d"]):
             f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    params = tmp_path / "params.bin"
+    with open(params, "wb") as f:
+        for k, t in (("order", "<i4"), ("size", "<i4"), ("spacing", "<f4"), ("origin", "<f4"),
+                     ("ext", "<f4")):
+            f.write(np.ascontiguousarray(z[k], t).tobytes())
+    keys = ("qp_vol", "qs_vol") if vis else ("rho_vol", "vp_vol", "vs_vol")
+    files = []
+    for k in keys:
+        files.append(str(tmp_path / (k + ".bin")))
+        np.ascontiguousarray(z[k], "<f4").tofile(files[-1])
     out = tmp_path / "out.bin"
     exe = os.path.join(REPO, "oracle", "_ref", "ref_probe_media")
-    r = subprocess.run([exe, "layer_one", str(lay), str(grid), method, str(out)],
-                       capture_output=True, text=True, check=True)
-    assert "discretising the layered model on the GPU (method %s)" % method in r.stdout
-    got = np.fromfile(out, "<f4").reshape(nz, ny, nx)
-    np.testing.assert_array_equal(got.view(np.int32), z["var_" + method].view(np.int32))
+    r = subprocess.run([exe, "bin_vis" if vis else "bin", str(grid), str(params)] + files +
+                       [str(out)], capture_output=True, text=True, check=True)
+    assert "discretising the binary model on the GPU" in r.stdout
+    got = np.fromfile(out, "<f4").reshape(len(keys), nz, ny, nx)
+    for a, k in zip(got, ("Qp", "Qs") if vis else ("rho", "lam", "mu")):
+        np.testing.assert_array_equal(a.view(np.int32), z[k].view(np.int32))
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method", ["loc", "har", "ari"])
-def test_device_onecmp_matches_reference(method):
+@pytest.mark.parametrize("vis", [False, True])
+def test_device_bin_matches_reference(vis):
+    """Trilinear interpolation in the reference's float order (--fmad=false):
+    bit for bit; lambda within a float rounding of the double form."""
     from cgfd3d_gb300 import media
-    z, g, m = _one()
-    got = media.layer(m, g["x3d"], g["y3d"], g["z3d"], method)[0]
-    np.testing.assert_allclose(got, z["var_" + method], rtol=2e-6, atol=0)
+    z = np.load(FIX_BIN)
+    g = np.load(FIX)
+    lay = media.BinModel.of(z["order"], z["size"], z["spacing"], z["origin"])
+    keys = ("qp_vol", "qs_vol") if vis else ("rho_vol", "vp_vol", "vs_vol")
+    got = media.bin_model(lay, z["ext"], [z[k] for k in keys], g["x3d"], g["y3d"], g["z3d"],
+                          vis)
+    for a, k in zip(got, ("Qp", "Qs") if vis else ("rho", "lam", "mu")):
+        np.testing.assert_array_equal(a.view(np.int32), z[k].view(np.int32))
+    bad = media.BinModel.of(z["order"], z["size"], z["spacing"], z["origin"])
+    bad.origin[1] = float(g["x3d"].max()) + 10.0          # model east of the grid
+    with pytest.raises(Exception):
+        media.bin_model(bad, z["ext"], [z[k] for k in keys], g["x3d"], g["y3d"], g["z3d"], vis)
 
 
 @pytest.mark.gpu
