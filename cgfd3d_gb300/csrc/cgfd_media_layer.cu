@@ -484,6 +484,83 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
   }
 }
 
+/* ---- 3-D grid models (.md3grd), elastic isotropic ----------------------
+ * NI grid levels (the "interfaces" of LayerMesh, nc = 4: elevation, rho, vp,
+ * vs) in NL layers; start[l] is the first level of layer l
+ * (media/media_grid2model.cpp:424-556, 1269-1356, 1819-2079). */
+struct GridLayers {
+  int NL;
+  int start[LAY_MAX];
+};
+
+__device__ bool grd_is_start(const GridLayers &G, int mi)
+{
+  for (int l = 1; l < G.NL; l++)
+    if (G.start[l] == mi) return true;
+  return false;
+}
+
+/* rho, vp, vs at a point, linear between the two levels around it
+ * (AssignGridMediaPara2Point with CalPointValue_grid); on: the point lies
+ * on a layer's top level.  0, or 1 outside the mesh, 2 vp <= sqrt(2) vs. */
+__device__ int grd_point(const LayerMesh &L, const GridLayers &G, float x, float y, float z,
+                         float *elev, float &r, float &vp, float &vs, int &on)
+{
+  const float maxx = L.MINX + (L.NX - 1) * L.DX, maxy = L.MINY + (L.NY - 1) * L.DY;
+  on = 0;
+  if (x < L.MINX || x > maxx || y < L.MINY || y > maxy) return 1;
+  const LayW w = lay_weights(L, x, y);
+  const int NI = L.NI;
+  for (int n = 0; n < NI; n++) elev[n] = lay_interp(L, w, 0, n);
+  int mi = lay_last_ge(z, elev, NI);
+  on = mi >= 0 && grd_is_start(G, mi) && fabsf(z - elev[mi]) < FLT_EPSILON;
+  float dis_r = 0.5f;
+  if (mi >= 0 && mi + 1 < NI && (double)fabsf(elev[mi + 1] - elev[mi]) > 1e-6)
+    dis_r = (z - elev[mi]) / (elev[mi + 1] - elev[mi]);
+  if (mi == -1 || mi == NI - 1) {
+    if (mi == -1) mi = lay_last_ge(elev[0], elev, NI);
+    if (mi < 0) return 1;   /* only a NaN elevation or coordinate gets here */
+    r = lay_interp(L, w, 1, mi);
+    vp = lay_interp(L, w, 2, mi);
+    vs = lay_interp(L, w, 3, mi);
+    return 0;
+  }
+  if (mi > 0 && fabsf(elev[mi] - z) < FLT_EPSILON && grd_is_start(G, mi)) {
+    mi--;
+    dis_r = 0.5f;
+  }
+  const float vp0 = lay_interp(L, w, 2, mi), vs0 = lay_interp(L, w, 3, mi);
+  const float rho0 = lay_interp(L, w, 1, mi);
+  const float vp1 = lay_interp(L, w, 2, mi + 1), vs1 = lay_interp(L, w, 3, mi + 1);
+  const float rho1 = lay_interp(L, w, 1, mi + 1);
+  vp = vp0 + (vp1 - vp0) * dis_r;
+  vs = vs0 + (vs1 - vs0) * dis_r;
+  r = rho0 + (rho1 - rho0) * dis_r;
+  if (lay_vp_low(vp, vs)) return 2;
+  return 0;
+}
+
+/* out: rho, lambda, mu (the reference's argument order) */
+__global__ void k_grid_loc(LayerMesh L, GridLayers G, long long vol, const float *__restrict__ x3d,
+                           const float *__restrict__ y3d, const float *__restrict__ z3d,
+                           LayOut out, int *bad)
+{
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
+       q += (long long)gridDim.x * blockDim.x) {
+    float elev[LAY_MAX], r, vp, vs;
+    int on;
+    const int st = grd_point(L, G, x3d[q], y3d[q], z3d[q], elev, r, vp, vs, on);
+    if (st) {
+      atomicOr(bad, st);
+      continue;
+    }
+    const float m = vs * vs * r;
+    out.v[2][q] = m;
+    out.v[1][q] = lay_lambda(vp, r, m);
+    out.v[0][q] = r;
+  }
+}
+
 /* Whether every (value, gradient, power) triple of a layered model with a
  * non-zero gradient has its power in [0, 1], the range that has run on the
  * device.  Other models are refused, because one-component models with a
@@ -631,4 +708,84 @@ extern "C" int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, f
   float *out[6] = {c11, c33, c55, c66, c13, rho};
   return lay_run(media_type, NI, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d, z3d,
                  method, out);
+}
+
+extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                                      float MINY, float DX, float DY, const float *rec, int nx,
+                                      int ny, int nz, const float *x3d, const float *y3d,
+                                      const float *z3d, const char *method, float *rho,
+                                      float *lam, float *mu)
+{
+  int meth = -1;
+  if (method && strcmp(method, "loc") == 0) meth = 0;
+  if (method && strcmp(method, "har") == 0) meth = 1;
+  if (method && strcmp(method, "ari") == 0) meth = 2;
+  if (meth < 0)
+    return lay_err(CGFD_EINVAL, "grid model: equivalent medium method %s (loc, har or ari)",
+                   method ? method : "(null)");
+  /* The cell averaging of grid models gave other values on the device than
+   * the same kernel source built for the host (which equals the reference),
+   * and other ones again with another register allocation; the cause is not
+   * found, so grid models take "loc" on the device only. */
+  if (meth != 0)
+    return lay_err(CGFD_EINVAL, "grid model: the device takes the loc method (har and ari: the "
+                   "reference's host routine)");
+  if (NI < 1 || NI > LAY_MAX || NL < 1 || NL > NI || !ngz || NX < 2 || NY < 2 || !(DX > 0) ||
+      !(DY > 0))
+    return lay_err(CGFD_EINVAL, "grid model: %d levels in %d layers on a %dx%d mesh (1..%d "
+                   "levels, at least 2x2 points, positive spacing)", NI, NL, NX, NY, LAY_MAX);
+  GridLayers G = {};
+  G.NL = NL;
+  int acc = 0;
+  for (int l = 0; l < NL; l++) {
+    if (ngz[l] < 1) return lay_err(CGFD_EINVAL, "grid model: layer %d has %d levels", l, ngz[l]);
+    G.start[l] = acc;
+    acc += ngz[l];
+  }
+  if (acc != NI)
+    return lay_err(CGFD_EINVAL, "grid model: the layers hold %d levels, not %d", acc, NI);
+  if (!rec || !x3d || !y3d || !z3d || !rho || !lam || !mu || nx < 1 || ny < 1 || nz < 1)
+    return lay_err(CGFD_EINVAL, "grid model: missing array or empty grid");
+  const int nc = 4;
+  const size_t vol = (size_t)nx * ny * nz, nrec = (size_t)NI * NX * NY * nc;
+  /* device buffer: x, y, z, rho, lambda, mu, the model */
+  const size_t fl = 6 * vol + nrec;
+  char *d = nullptr;
+  int *d_bad = nullptr, bad = 0, check = 0;
+  const int zero = 0;
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d, fl * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int));
+  float *df = (float *)d;
+  float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *drec = df + 6 * vol;
+  LayOut o = {};
+  for (int n = 0; n < 3; n++) o.v[n] = df + (3 + n) * vol;
+  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_lay_check, &zero, sizeof(int), 0,
+                                                    cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y3d, vol * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z3d, vol * 4, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(drec, rec, nrec * 4, cudaMemcpyHostToDevice, st);
+  const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
+  if (e == cudaSuccess) {
+    k_grid_loc<<<152 * 8, 256, 0, st>>>(L, G, (long long)vol, dx, dy, dz, o, d_bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(&check, g_lay_check, sizeof(int), 0,
+                                                      cudaMemcpyDeviceToHost, st);
+  float *out[3] = {rho, lam, mu};
+  for (int n = 0; n < 3 && e == cudaSuccess; n++)
+    e = cudaMemcpyAsync(out[n], o.v[n], vol * 4, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (d) cudaFree(d);
+  if (d_bad) cudaFree(d_bad);
+  if (st) cudaStreamDestroy(st);
+  if (e != cudaSuccess) return lay_err(CGFD_ECUDA, "grid model: %s", cudaGetErrorString(e));
+  if (check) return lay_err(CGFD_ECUDA, "grid model: internal bounds check %d failed", check);
+  if (bad & 1) return lay_err(CGFD_EINVAL, "grid model: a grid point lies outside the mesh");
+  if (bad & 2) return lay_err(CGFD_EINVAL, "grid model: vp <= sqrt(2) vs at a grid point");
+  return 0;
 }

@@ -1,11 +1,13 @@
 /*
  * media_layer2model_gpu.cpp -- drop-in for CGFD3D's discretisation of
  * media on a curvilinear grid: elastic isotropic and elastic VTI layered
- * models, and models given as binary volumes.
+ * models, elastic isotropic 3-D grid models, and models given as binary
+ * volumes.
  *
  * Built inside the reference tree (its media headers: inter_t,
  * read_interface_file) and linked with -Wl,--wrap= for
- * media_layer2model_el_iso, _el_vti and media_bin2model_el_iso, _vis_iso,
+ * media_layer2model_el_iso, _el_vti, media_grid2model_el_iso and
+ * media_bin2model_el_iso, _vis_iso,
  * so the reference's main (forward/main_curv_col_el_3d.c:328-515)
  * calls the __wrap_ functions below with its unchanged arguments.  A .md3lay
  * file is read by the reference's own reader (media/media_read_file.cpp:
@@ -256,5 +258,44 @@ extern "C" int __wrap_media_bin2model_vis_iso(float *Qp3d, float *Qs3d, const fl
   if (cgfd_media_bin_vis_iso(&m, xmin, xmax, ymin, ymax, qp.data(), qs.data(), (int)nx,
                              (int)ny, (int)nz, x3d, y3d, z3d, Qp3d, Qs3d))
     lay_fail(bin_file_Qp);
+  return 0;
+}
+
+extern "C" int __real_media_grid2model_el_iso(float *rho3d, float *lam3d, float *mu3d,
+                                              const float *x3d, const float *y3d,
+                                              const float *z3d, int nx, int ny, int nz,
+                                              float Xmin, float Xmax, float Ymin, float Ymax,
+                                              int grid_type, const char *in_media_file,
+                                              const char *equivalent_medium_method, int myid);
+
+/* a .md3grd model: read (and cropped to the grid's extent) by the reference's
+ * reader, discretised on the device */
+extern "C" int __wrap_media_grid2model_el_iso(float *rho3d, float *lam3d, float *mu3d,
+                                              const float *x3d, const float *y3d,
+                                              const float *z3d, int nx, int ny, int nz,
+                                              float Xmin, float Xmax, float Ymin, float Ymax,
+                                              int grid_type, const char *in_media_file,
+                                              const char *equivalent_medium_method, int myid)
+{
+  const char *m = equivalent_medium_method;
+  /* the library takes grid models with "loc" only */
+  if (!lay_ours(grid_type, m, nx, ny, nz) || strcmp(m, "loc") != 0)
+    return __real_media_grid2model_el_iso(rho3d, lam3d, mu3d, x3d, y3d, z3d, nx, ny, nz, Xmin,
+                                          Xmax, Ymin, Ymax, grid_type, in_media_file, m, myid);
+  int NL = 0;
+  std::vector<int> NGz;
+  inter_t it;
+  read_grid_file(in_media_file, Xmin, Xmax, Ymin, Ymax, NL, NGz, &it);
+  if (it.media_type != ELASTIC_ISOTROPIC)
+    return __real_media_grid2model_el_iso(rho3d, lam3d, mu3d, x3d, y3d, z3d, nx, ny, nz, Xmin,
+                                          Xmax, Ymin, Ymax, grid_type, in_media_file, m, myid);
+  const float *cols[4] = {it.elevation, it.rho, it.vp, it.vs};
+  const std::vector<float> rec = lay_interleave(it, cols, 4);
+  if (myid == 0)
+    fprintf(stdout, "discretising the grid model on the GPU (method %s)\n", m);
+  if (cgfd_media_grid_el_iso((int)it.NI, NL, NGz.data(), (int)it.NX, (int)it.NY, it.MINX,
+                             it.MINY, it.DX, it.DY, rec.data(), nx, ny, nz, x3d, y3d, z3d, m,
+                             rho3d, lam3d, mu3d))
+    lay_fail(in_media_file);
   return 0;
 }

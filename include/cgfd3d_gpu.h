@@ -348,6 +348,23 @@ void cgfd_locator_destroy(cgfd_locator_t *loc);
  * reference's host routine. */
 int cgfd_media_layer_pow_ok(int nc, const float *rec, size_t nrec);
 
+/* An elastic isotropic 3-D grid model (.md3grd) discretised on a
+ * curvilinear grid, as media_grid2model_el_iso does
+ * (media/media_grid2model.cpp:133-189, 424-556, 1067-1126, 1269-1356,
+ * 1819-2079; called at forward/main_curv_col_el_3d.c:394-403): NI grid
+ * levels in NL layers of ngz[l] levels, on a uniform NX x NY mesh from
+ * (MINX, MINY) with spacing DX, DY, as the reference's reader leaves it
+ * after cropping to the grid's extent; rec [NI][NY][NX][4] = elevation, rho,
+ * vp, vs.  Values are linear between the two levels around a point;
+ * method "loc" ("har" and "ari" are CGFD_EINVAL here: their device kernel is
+ * withdrawn, and callers use the reference's host routine for them).
+ * Writes rho, lambda, mu (host, the reference's argument order).  A point
+ * outside the mesh or with vp <= sqrt(2) vs is CGFD_EINVAL. */
+int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                           float MINY, float DX, float DY, const float *rec, int nx, int ny,
+                           int nz, const float *x3d, const float *y3d, const float *z3d,
+                           const char *method, float *rho, float *lam, float *mu);
+
 int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY, float DX,
                             float DY, const float *rec, int nx, int ny, int nz,
                             const float *x3d, const float *y3d, const float *z3d,

@@ -2407,3 +2407,187 @@ int oracle_bin(int vis, const int *order, const int *size, const float *spacing,
   free(b.xv); free(b.yv); free(b.zv);
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* 3-D grid models (.md3grd), elastic isotropic (media/media_grid2model.cpp)  */
+/* ------------------------------------------------------------------------ */
+
+/* NI grid levels in NL layers of ngz[l] levels each; rec [NI][NY][NX][4] =
+ * elevation, rho, vp, vs as the reference's reader leaves them (after its
+ * crop to the grid's extent, media/media_read_file.cpp read_grid_file). */
+typedef struct {
+  int NI, NX, NY, NL;
+  int start[LAY_MAXI];        /* first level of each layer */
+  const float *xv, *yv, *rec;
+  size_t slice;
+  float minx, maxx, miny, maxy;
+  float *elev, *elev_nl;
+} grd_model_t;
+
+/* whether level mi starts a layer other than the first (the reference's
+ * layer_indx set, media/media_grid2model.cpp:447-452) */
+static int grd_is_start(const grd_model_t *m, int mi)
+{
+  for (int l = 1; l < m->NL; l++)
+    if (m->start[l] == mi) return 1;
+  return 0;
+}
+
+static float grd_val(const grd_model_t *m, int level, int c, float x, float y)
+{
+  return lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + level * m->slice * 4 + c, 4, x, y);
+}
+
+/* rho, vp, vs at a point: AssignGridMediaPara2Point with CalPointValue_grid
+ * for ELASTIC_ISOTROPIC (media/media_grid2model.cpp:424-556).  *on: the
+ * point lies on a layer's top level (isPointOnInter).  Returns 1 where the
+ * reference exits (outside the mesh, vp <= sqrt(2) vs). */
+static int grd_point(const grd_model_t *m, float x, float y, float z, float *var, int *on)
+{
+  const int NI = m->NI;
+  float *elev = m->elev;
+  if (x < m->minx || x > m->maxx || y < m->miny || y > m->maxy) return 1;
+  for (int n = 0; n < NI; n++) elev[n] = grd_val(m, n, 0, x, y);
+  int mi = lay_last_ge(z, elev, NI);
+  *on = mi >= 0 && grd_is_start(m, mi) && fabsf(z - elev[mi]) < FLT_EPSILON;
+  /* the reference computes this before the branches, also where mi is -1
+   * or NI-1 (it reads past its vector there; the value is not used) */
+  float dis_r = 1.0 / 2.0;
+  if (mi >= 0 && mi + 1 < NI && fabs(elev[mi + 1] - elev[mi]) > 1e-6)
+    dis_r = (z - elev[mi]) / (elev[mi + 1] - elev[mi]);
+  if (mi == -1 || mi == NI - 1) {
+    if (mi == -1) mi = lay_last_ge(elev[0], elev, NI);
+    var[0] = grd_val(m, mi, 1, x, y);
+    var[1] = grd_val(m, mi, 2, x, y);
+    var[2] = grd_val(m, mi, 3, x, y);
+    return 0;
+  }
+  if (mi > 0 && fabsf(elev[mi] - z) < FLT_EPSILON && grd_is_start(m, mi)) {
+    mi--;
+    dis_r = 1.0 / 2.0;
+  }
+  float vp0 = grd_val(m, mi, 2, x, y), vs0 = grd_val(m, mi, 3, x, y);
+  float rho0 = grd_val(m, mi, 1, x, y);
+  float vp1 = grd_val(m, mi + 1, 2, x, y), vs1 = grd_val(m, mi + 1, 3, x, y);
+  float rho1 = grd_val(m, mi + 1, 1, x, y);
+  var[1] = vp0 + (vp1 - vp0) * dis_r;
+  var[2] = vs0 + (vs1 - vs0) * dis_r;
+  var[0] = rho0 + (rho1 - rho0) * dis_r;
+  if (var[1] <= sqrt(2) * var[2]) return 1;
+  return 0;
+}
+
+/* the layer of a half-grid point (LayerNumberAtPoint,
+ * media/media_grid2model.cpp:1269-1310) */
+static int grd_layer(const grd_model_t *m, float x, float y, float z)
+{
+  for (int l = 0; l < m->NL; l++) m->elev_nl[l] = grd_val(m, m->start[l], 0, x, y);
+  int mi = lay_last_ge(z, m->elev_nl, m->NL);
+  if (mi == -1) mi = lay_last_ge(m->elev_nl[0], m->elev_nl, m->NL);
+  return mi;
+}
+
+/* method 0 loc, 1 har, 2 ari (parametrization_grid_el_iso_loc / _har /
+ * _ari, media/media_grid2model.cpp:1067-1126, 1819-2079): out = rho, lambda,
+ * mu (the reference's argument order).  har and ari recompute the interior
+ * points whose cell touches two layers from the 9^3 samples not lying on a
+ * layer's top level.  Returns 1 where the reference exits. */
+int oracle_grid_el_iso(int method, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                       float MINY, float DX, float DY, const float *rec, int nx, int ny, int nz,
+                       const float *x3d, const float *y3d, const float *z3d, float **out)
+{
+  if (NI < 1 || NI > LAY_MAXI || NL < 1 || NL > NI) return 1;
+  grd_model_t m;
+  m.NI = NI; m.NX = NX; m.NY = NY; m.NL = NL;
+  int acc = 0;
+  for (int l = 0; l < NL; l++) {
+    m.start[l] = acc;
+    acc += ngz[l];
+  }
+  if (acc != NI) return 1;
+  float *xv = malloc(NX * sizeof(float)), *yv = malloc(NY * sizeof(float));
+  for (int i = 0; i < NX; i++) xv[i] = MINX + DX * i;
+  for (int j = 0; j < NY; j++) yv[j] = MINY + DY * j;
+  m.xv = xv; m.yv = yv; m.rec = rec; m.slice = (size_t)NX * NY;
+  m.minx = MINX; m.maxx = MINX + (NX - 1) * DX;
+  m.miny = MINY; m.maxy = MINY + (NY - 1) * DY;
+  m.elev = malloc(NI * sizeof(float));
+  m.elev_nl = malloc(NL * sizeof(float));
+  int bad = 0;
+  const size_t line = nx, sl = (size_t)nx * ny, vol = sl * nz;
+  for (size_t q = 0; q < vol && !bad; q++) {
+    float var[3];
+    int on;
+    if (grd_point(&m, x3d[q], y3d[q], z3d[q], var, &on)) { bad = 1; break; }
+    float vp = var[1], vs = var[2], r = var[0];
+    out[2][q] = vs * vs * r;
+    out[1][q] = vp * vp * r - 2.0 * out[2][q];
+    out[0][q] = r;
+  }
+  if (method != 0 && !bad) {
+    float *Hx = malloc(vol * sizeof(float)), *Hy = malloc(vol * sizeof(float));
+    float *Hz = malloc(vol * sizeof(float));
+    int *mat = malloc(vol * sizeof(int));
+    lay_half_grid(nx, ny, nz, x3d, Hx);
+    lay_half_grid(nx, ny, nz, y3d, Hy);
+    lay_half_grid(nx, ny, nz, z3d, Hz);
+    for (size_t q = 0; q < vol; q++) mat[q] = grd_layer(&m, Hx[q], Hy[q], Hz[q]);
+    for (int j = 1; j < ny - 1 && !bad; j++)
+      for (int k = 1; k < nz - 1 && !bad; k++)
+        for (int i = 1; i < nx - 1 && !bad; i++) {
+          size_t q = i + j * line + k * sl;
+          const size_t c[8] = {q - 1 - line - sl, q - 1 - sl, q - sl, q - line - sl,
+                               q - 1 - line, q - 1, q, q - line};
+          int v[8];
+          for (int n = 0; n < 8; n++) v[n] = mat[c[n]];
+          if (lay_num_values(v) <= 1) continue;
+          float vert[8][3];
+          for (int n = 0; n < 8; n++) {
+            vert[n][0] = Hx[c[n]];
+            vert[n][1] = Hy[c[n]];
+            vert[n][2] = Hz[c[n]];
+          }
+          float s_rho = 0.0, s_a = 0.0, s_b = 0.0;   /* rho; kappa or lambda; mu */
+          int num_dis = (LAY_NG + 1) * (LAY_NG + 1) * (LAY_NG + 1);
+          for (int kk = 0; kk <= LAY_NG && !bad; kk++)
+            for (int jj = 0; jj <= LAY_NG && !bad; jj++)
+              for (int ii = 0; ii <= LAY_NG; ii++) {
+                float p[3], var[3];
+                int on;
+                lay_subpoint((const float (*)[3])vert, ii, jj, kk, p);
+                if (grd_point(&m, p[0], p[1], p[2], var, &on)) { bad = 1; break; }
+                if (on) {
+                  num_dis--;
+                  continue;
+                }
+                float rho = var[0], vp = var[1], vs = var[2];
+                float mu_ = vs * vs * rho;
+                float lambda = vp * vp * rho - 2.0 * mu_;
+                s_rho += rho;
+                if (method == 1) {
+                  s_a += (1.0 / (lambda + 2.0 / 3.0 * mu_));
+                  s_b += (1.0 / mu_);
+                } else {
+                  s_a += lambda;
+                  s_b += mu_;
+                }
+              }
+          if (bad) break;
+          if (method == 1) {
+            s_b = num_dis * 1.0 / s_b;
+            s_a = num_dis * 1.0 / s_a;
+            s_rho = s_rho / num_dis;
+            out[1][q] = s_a - 2.0 / 3.0 * s_b;
+            out[2][q] = s_b;
+            out[0][q] = s_rho;
+          } else {
+            out[1][q] = s_a / (num_dis * 1.0);
+            out[2][q] = s_b / (num_dis * 1.0);
+            out[0][q] = s_rho / (num_dis * 1.0);
+          }
+        }
+    free(Hx); free(Hy); free(Hz); free(mat);
+  }
+  free(xv); free(yv); free(m.elev); free(m.elev_nl);
+  return bad;
+}

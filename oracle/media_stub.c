@@ -109,3 +109,22 @@ int cgfd_media_bin_vis_iso(const cgfd_bin_model_t *model, float xmin, float xmax
   float *o[2] = {qp, qs};
   return stub_bin(1, model, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
 }
+
+int oracle_grid_el_iso(int method, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                       float MINY, float DX, float DY, const float *rec, int nx, int ny, int nz,
+                       const float *x3d, const float *y3d, const float *z3d, float **out);
+
+int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                           float MINY, float DX, float DY, const float *rec, int nx, int ny,
+                           int nz, const float *x3d, const float *y3d, const float *z3d,
+                           const char *method, float *rho, float *lam, float *mu)
+{
+  int m = stub_method(method);
+  float *o[3] = {rho, lam, mu};
+  if (m < 0 || oracle_grid_el_iso(m, NI, NL, ngz, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz,
+                                  x3d, y3d, z3d, o)) {
+    stub_msg = "grid model: bad method, a point outside the mesh or vp <= sqrt(2) vs";
+    return CGFD_EINVAL;
+  }
+  return 0;
+}

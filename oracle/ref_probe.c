@@ -44,6 +44,12 @@
  *       media_layer2model_onecmp (media/media_layer2model.cpp:47-88);
  *       <output>: float var [nz][ny][nx]
  *
+ *   ref_probe grid <md3grd> <grid> <method> <ext> <output>
+ *       an elastic isotropic 3-D grid model discretised by
+ *       media_grid2model_el_iso (media/media_grid2model.cpp:133-189) with the
+ *       grid's extent <ext> (float xmin, xmax, ymin, ymax);
+ *       <output>: float rho, lambda, mu [nz][ny][nx]
+ *
  *   ref_probe bin <grid> <params> <rho> <vp> <vs> <output>
  *   ref_probe bin_vis <grid> <params> <Qp> <Qs> <output>
  *       a model given as binary volumes interpolated on a curvilinear grid
@@ -86,6 +92,11 @@ int media_bin2model_vis_iso(float *Qp3d, float *Qs3d, const float *x3d, const fl
                             float xmax, float ymin, float ymax, int grid_type, int *bin_order,
                             int *bin_size, float *bin_spacing, float *bin_origin,
                             const char *bin_file_Qp, const char *bin_file_Qs);
+int media_grid2model_el_iso(float *rho3d, float *lam3d, float *mu3d, const float *x3d,
+                            const float *y3d, const float *z3d, int nx, int ny, int nz,
+                            float Xmin, float Xmax, float Ymin, float Ymax, int grid_type,
+                            const char *in_media_file, const char *equivalent_medium_method,
+                            int myid);
 #define PROBE_GRID_CURV 3
 
 static void rd(void *p, size_t n, FILE *fp)
@@ -345,6 +356,35 @@ static int probe_bin(int vis, const char *grid, const char *params, const char *
   return 0;
 }
 
+static int probe_grid(const char *grd, const char *grid, const char *method, const char *extf,
+                      const char *out)
+{
+  FILE *fp = fopen(grid, "rb");
+  if (!fp) return 2;
+  int d[3];
+  rd(d, sizeof d, fp);
+  size_t vol = (size_t)d[0] * d[1] * d[2];
+  float *x = malloc(vol * 4), *y = malloc(vol * 4), *z = malloc(vol * 4);
+  rd(x, vol * 4, fp);
+  rd(y, vol * 4, fp);
+  rd(z, vol * 4, fp);
+  fclose(fp);
+  float ext[4];
+  fp = fopen(extf, "rb");
+  if (!fp) return 2;
+  rd(ext, sizeof ext, fp);
+  fclose(fp);
+  float *o[3];
+  for (int n = 0; n < 3; n++) o[n] = calloc(vol, 4);
+  media_grid2model_el_iso(o[0], o[1], o[2], x, y, z, d[0], d[1], d[2], ext[0], ext[1], ext[2],
+                          ext[3], PROBE_GRID_CURV, grd, method, 0);
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  for (int n = 0; n < 3; n++) fwrite(o[n], 4, vol, fo);
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
@@ -355,6 +395,8 @@ int main(int argc, char **argv)
     return probe_layer_vti(argv[2], argv[3], argv[4], argv[5]);
   if (argc == 6 && strcmp(argv[1], "layer_one") == 0)
     return probe_layer_one(argv[2], argv[3], argv[4], argv[5]);
+  if (argc == 7 && strcmp(argv[1], "grid") == 0)
+    return probe_grid(argv[2], argv[3], argv[4], argv[5], argv[6]);
   if (argc == 8 && strcmp(argv[1], "bin") == 0)
     return probe_bin(0, argv[2], argv[3], (const char *const *)argv + 4, argv[7]);
   if (argc == 7 && strcmp(argv[1], "bin_vis") == 0)

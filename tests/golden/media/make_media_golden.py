@@ -29,6 +29,12 @@ and media_bin2model_vis_iso (media/media_bin2model.cpp:27-432); keys
 order, size, spacing, origin, ext (xmin xmax ymin ymax), rho_vol, vp_vol,
 vs_vol, qp_vol, qs_vol (file order) and rho, lam, mu, Qp, Qs.
 
+And grid_el_iso.npz: an elastic isotropic 3-D grid model (.md3grd: three
+layers of three grid levels, a layer boundary where two levels coincide and
+one on a flat grid level, grid points below the last level) on the first
+grid through media_grid2model_el_iso (media/media_grid2model.cpp:133-189)
+with each method; keys md3grd, ext and rho_<m>, lam_<m>, mu_<m>.
+
 This script needs the reference build and runs only where it exists; the
 fixtures it writes are committed and are all the tests need elsewhere.
 
@@ -185,6 +191,7 @@ def main():
     vti_main()
     one_main(X, Y, Z)
     bin_main(X, Y, Z)
+    grid_main(X, Y, Z)
     on = int(np.isclose(Z, -800.0).sum())
     print("grid %s, %d points on the flat interface, rho range %.1f-%.1f"
           % (X.shape, on, out[2].min(), out[2].max()))
@@ -275,6 +282,59 @@ def bin_main(X, Y, Z):
     np.savez_compressed(os.path.join(HERE, "bin_model.npz"), **res)
     print("bin: model %s (z, x, y), rho %.1f-%.1f" % (tuple(size), res["rho"].min(),
                                                      res["rho"].max()))
+
+
+def grid_main(X, Y, Z):
+    rng = np.random.default_rng(23)
+    ext = np.array([X.min(), X.max(), Y.min(), Y.max()], np.float32)
+    NX, NY = 12, 10
+    # the mesh covers the grid exactly as the reader crops it: (xmin - MINX)
+    # below one DX and ceil((xmax - MINX) / DX) = NX - 1
+    dx = float(ext[1] - ext[0]) / (NX - 1.8)
+    dy = float(ext[3] - ext[2]) / (NY - 1.8)
+    minx, miny = float(ext[0]) - 0.3 * dx, float(ext[2]) - 0.3 * dy
+    XX, YY = np.meshgrid(minx + dx * np.arange(NX), miny + dy * np.arange(NY))
+    l2 = -390.0 + 80.0 * np.sin(XX / 900.0 + 0.5)
+    levels = [60.0 + 20.0 * np.sin(XX / 700.0) * np.cos(YY / 500.0),
+              -150.0 + 30.0 * np.sin(XX / 900.0), l2,
+              l2, -600.0 + 20.0 * np.cos(YY / 600.0), np.full_like(XX, -800.0),
+              np.full_like(XX, -800.0), -1100.0 + 60.0 * np.cos(YY / 600.0),
+              np.full_like(XX, -1400.0)]
+    props = [((2300, 2400), (3800, 4200), (2100, 2300)),
+             ((2450, 2600), (4500, 5000), (2550, 2800)),
+             ((2650, 2800), (5200, 6000), (2950, 3450))]
+    lines = ["elastic_isotropic", "3", "3 3 3",          # (no comments: the reader takes none)
+             "%d %d %.9g %.9g %.9g %.9g" % (NX, NY, minx, miny, dx, dy)]
+    for ni, e in enumerate(levels):
+        layer, t = ni // 3, (ni % 3) / 2.0
+        vals = [lo + (hi - lo) * t for lo, hi in props[layer]]
+        pert = [v * (1.0 + 0.02 * rng.uniform(-1, 1, XX.shape)) for v in vals]
+        for j in range(NY):
+            for i in range(NX):
+                lines.append("%.9g %.9g %.9g %.9g" % (np.float32(e[j, i]), pert[0][j, i],
+                                                       pert[1][j, i], pert[2][j, i]))
+    text = "\n".join(lines) + "\n"
+    nz, ny, nx = X.shape
+    res = dict(md3grd=np.frombuffer(text.encode(), np.uint8), ext=ext)
+    with tempfile.TemporaryDirectory() as tmp:
+        grd = os.path.join(tmp, "model.md3grd")
+        open(grd, "w").write(text)
+        gpath, epath = os.path.join(tmp, "grid.bin"), os.path.join(tmp, "ext.bin")
+        opath = os.path.join(tmp, "out.bin")
+        with open(gpath, "wb") as f:
+            f.write(struct.pack("<3i", nx, ny, nz))
+            for A in (X, Y, Z):
+                f.write(A.astype("<f4").tobytes())
+        ext.tofile(epath)
+        for meth in ("loc", "har", "ari"):
+            subprocess.run([PROBE, "grid", grd, gpath, meth, epath, opath], check=True,
+                           stdout=subprocess.DEVNULL)
+            o = np.fromfile(opath, "<f4").reshape(3, nz, ny, nx)
+            res.update({"rho_" + meth: o[0], "lam_" + meth: o[1], "mu_" + meth: o[2]})
+    np.savez_compressed(os.path.join(HERE, "grid_el_iso.npz"), **res)
+    print("grid: har changed %d points, rho %.1f-%.1f"
+          % ((res["lam_har"] != res["lam_loc"]).sum(), res["rho_loc"].min(),
+             res["rho_loc"].max()))
 
 
 def vti_main():

@@ -124,6 +124,30 @@ def test_pow_guard():
     assert L.cgfd_media_layer_pow_ok(10, r3.ctypes.data, r3.size // 10) == 1
 
 
+FIX_GRID = os.path.join(REPO, "tests", "golden", "media", "grid_el_iso.npz")
+
+
+def _grid():
+    from cgfd3d_gb300 import media
+    z = np.load(FIX_GRID)
+    g = np.load(FIX)
+    return z, g, media.read_md3grd(bytes(z["md3grd"]).decode(), z["ext"])
+
+
+@pytest.mark.parametrize("method", ["loc", "har", "ari"])
+def test_oracle_grid_matches_reference_bitwise(method):
+    """3-D grid models (media_grid2model_el_iso): three layers of three
+    levels, coincident levels at a layer boundary, a boundary on a flat grid
+    level, points below the last level; the reader's crop restated."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    z, g, m = _grid()
+    assert (m["NI"], m["NL"], m["rec"].shape[-1]) == (9, 3, 4)
+    got = oracle.grid_el_iso(m, g["x3d"], g["y3d"], g["z3d"], method)
+    for a, k in zip(got, ("rho", "lam", "mu")):
+        np.testing.assert_array_equal(a.view(np.int32), z[k + "_" + method].view(np.int32))
+
+
 def test_har_and_ari_differ():
     z, _ = _fixture()
     d = z["lam_har"] != z["lam_ari"]
@@ -279,6 +303,52 @@ def test_device_bin_matches_reference(vis):
     bad.origin[1] = float(g["x3d"].max()) + 10.0          # model east of the grid
     with pytest.raises(Exception):
         media.bin_model(bad, z["ext"], [z[k] for k in keys], g["x3d"], g["y3d"], g["z3d"], vis)
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("method", ["loc", "har", "ari"])
+def test_dropin_adapter_grid_inside_reference(method, tmp_path):
+    """The adapter takes media_grid2model_el_iso: the reference's reader and
+    crop, then the library call (answered by the oracle here)."""
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe_media"], check=True, capture_output=True)
+    z, g, _ = _grid()
+    grd = tmp_path / "model.md3grd"
+    grd.write_bytes(bytes(z["md3grd"]))
+    nz, ny, nx = g["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(np.array([nx, ny, nz], "<i4").tobytes())
+        for a in (g["x3d"], g["y3d"], g["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    ext = tmp_path / "ext.bin"
+    np.ascontiguousarray(z["ext"], "<f4").tofile(ext)
+    out = tmp_path / "out.bin"
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_probe_media")
+    r = subprocess.run([exe, "grid", str(grd), str(grid), method, str(ext), str(out)],
+                       capture_output=True, text=True, check=True)
+    # loc goes to the library; har and ari stay with the reference's routine
+    on_gpu = "discretising the grid model on the GPU (method %s)" % method in r.stdout
+    assert on_gpu == (method == "loc")
+    got = np.fromfile(out, "<f4").reshape(3, nz, ny, nx)
+    for a, k in zip(got, ("rho", "lam", "mu")):
+        np.testing.assert_array_equal(a.view(np.int32), z[k + "_" + method].view(np.int32))
+
+
+@pytest.mark.gpu
+def test_device_grid_matches_reference():
+    """loc on the device in the reference's float order (--fmad=false, no
+    pow on this path): bit for bit.  har and ari are refused."""
+    from cgfd3d_gb300 import _lib, media
+    z, g, m = _grid()
+    got = media.grid_el_iso(m, g["x3d"], g["y3d"], g["z3d"], "loc")
+    for a, k in zip(got, ("rho", "lam", "mu")):
+        np.testing.assert_array_equal(a.view(np.int32), z[k + "_loc"].view(np.int32))
+    for method in ("har", "ari"):
+        with pytest.raises(_lib.CgfdError):
+            media.grid_el_iso(m, g["x3d"], g["y3d"], g["z3d"], method)
 
 
 @pytest.mark.gpu
