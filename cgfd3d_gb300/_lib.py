@@ -64,6 +64,9 @@ def lib():
     L.cgfd_media_layer_el_iso.argtypes = ([C.c_int] * 3 + [C.c_float] * 4 + [vp] +
                                           [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] + [vp] * 3)
     L.cgfd_media_layer_pow_ok.argtypes = [C.c_int, vp, C.c_size_t]
+    L.cgfd_media_grid_el_vti.argtypes = ([C.c_int] * 3 + [vp] + [C.c_int] * 2 + [C.c_float] * 4 +
+                                         [vp] + [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] +
+                                         [vp] * 6)
     L.cgfd_media_grid_el_iso.argtypes = ([C.c_int] * 2 + [vp] + [C.c_int] * 2 + [C.c_float] * 4 +
                                          [vp] + [C.c_int] * 3 + [vp] * 3 + [C.c_char_p] +
                                          [vp] * 3)

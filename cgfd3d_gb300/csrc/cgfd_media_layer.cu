@@ -500,12 +500,15 @@ __device__ bool grd_is_start(const GridLayers &G, int mi)
   return false;
 }
 
-/* rho, vp, vs at a point, linear between the two levels around it
- * (AssignGridMediaPara2Point with CalPointValue_grid); on: the point lies
- * on a layer's top level.  0, or 1 outside the mesh, 2 vp <= sqrt(2) vs. */
+/* the parameters at a point (rho vp vs, or the six of a VTI type), linear
+ * between the two levels around it (AssignGridMediaPara2Point with
+ * CalPointValue_grid); on: the point lies on a layer's top level.  0, or 1
+ * outside the mesh, 2 for an isotropic point with vp <= sqrt(2) vs. */
+template <int KIND>
 __device__ int grd_point(const LayerMesh &L, const GridLayers &G, float x, float y, float z,
-                         float *elev, float &r, float &vp, float &vs, int &on)
+                         float *elev, float *var, int &on)
 {
+  constexpr int NP = LayKind<KIND>::np;
   const float maxx = L.MINX + (L.NX - 1) * L.DX, maxy = L.MINY + (L.NY - 1) * L.DY;
   on = 0;
   if (x < L.MINX || x > maxx || y < L.MINY || y > maxy) return 1;
@@ -520,44 +523,50 @@ __device__ int grd_point(const LayerMesh &L, const GridLayers &G, float x, float
   if (mi == -1 || mi == NI - 1) {
     if (mi == -1) mi = lay_last_ge(elev[0], elev, NI);
     if (mi < 0) return 1;   /* only a NaN elevation or coordinate gets here */
-    r = lay_interp(L, w, 1, mi);
-    vp = lay_interp(L, w, 2, mi);
-    vs = lay_interp(L, w, 3, mi);
+#pragma unroll
+    for (int p = 0; p < NP; p++) var[p] = lay_interp(L, w, 1 + p, mi);
     return 0;
   }
   if (mi > 0 && fabsf(elev[mi] - z) < FLT_EPSILON && grd_is_start(G, mi)) {
     mi--;
     dis_r = 0.5f;
   }
-  const float vp0 = lay_interp(L, w, 2, mi), vs0 = lay_interp(L, w, 3, mi);
-  const float rho0 = lay_interp(L, w, 1, mi);
-  const float vp1 = lay_interp(L, w, 2, mi + 1), vs1 = lay_interp(L, w, 3, mi + 1);
-  const float rho1 = lay_interp(L, w, 1, mi + 1);
-  vp = vp0 + (vp1 - vp0) * dis_r;
-  vs = vs0 + (vs1 - vs0) * dis_r;
-  r = rho0 + (rho1 - rho0) * dis_r;
-  if (lay_vp_low(vp, vs)) return 2;
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    const float v0 = lay_interp(L, w, 1 + p, mi), v1 = lay_interp(L, w, 1 + p, mi + 1);
+    var[p] = v0 + (v1 - v0) * dis_r;
+  }
+  if (KIND == LAY_ISO && lay_vp_low(var[1], var[2])) return 2;
   return 0;
 }
 
-/* out: rho, lambda, mu (the reference's argument order) */
+/* out: rho, lambda, mu (isotropic, the reference's argument order) or c11
+ * c33 c55 c66 c13 rho (VTI) */
+template <int KIND>
 __global__ void k_grid_loc(LayerMesh L, GridLayers G, long long vol, const float *__restrict__ x3d,
                            const float *__restrict__ y3d, const float *__restrict__ z3d,
                            LayOut out, int *bad)
 {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
        q += (long long)gridDim.x * blockDim.x) {
-    float elev[LAY_MAX], r, vp, vs;
+    float elev[LAY_MAX], var[6];
     int on;
-    const int st = grd_point(L, G, x3d[q], y3d[q], z3d[q], elev, r, vp, vs, on);
+    const int st = grd_point<KIND>(L, G, x3d[q], y3d[q], z3d[q], elev, var, on);
     if (st) {
       atomicOr(bad, st);
       continue;
     }
-    const float m = vs * vs * r;
-    out.v[2][q] = m;
-    out.v[1][q] = lay_lambda(vp, r, m);
-    out.v[0][q] = r;
+    if (KIND == LAY_ISO) {
+      const float m = var[2] * var[2] * var[0];
+      out.v[2][q] = m;
+      out.v[1][q] = lay_lambda(var[1], var[0], m);
+      out.v[0][q] = var[0];
+    } else {
+      float c[6];
+      lay_para2vti<KIND>(var, c);
+#pragma unroll
+      for (int n = 0; n < 6; n++) out.v[n][q] = c[n];
+    }
   }
 }
 
@@ -710,12 +719,13 @@ extern "C" int cgfd_media_layer_el_vti(int media_type, int NI, int NX, int NY, f
                  method, out);
 }
 
-extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float MINX,
-                                      float MINY, float DX, float DY, const float *rec, int nx,
-                                      int ny, int nz, const float *x3d, const float *y3d,
-                                      const float *z3d, const char *method, float *rho,
-                                      float *lam, float *mu)
+/* one grid-model call; out: 3 (isotropic) or 6 (VTI) host volumes */
+static int grd_run(int kind, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                   float MINY, float DX, float DY, const float *rec, int nx, int ny, int nz,
+                   const float *x3d, const float *y3d, const float *z3d, const char *method,
+                   float *const *out)
 {
+  const int nout = kind == LAY_ISO ? 3 : 6;
   int meth = -1;
   if (method && strcmp(method, "loc") == 0) meth = 0;
   if (method && strcmp(method, "har") == 0) meth = 1;
@@ -744,12 +754,14 @@ extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, in
   }
   if (acc != NI)
     return lay_err(CGFD_EINVAL, "grid model: the layers hold %d levels, not %d", acc, NI);
-  if (!rec || !x3d || !y3d || !z3d || !rho || !lam || !mu || nx < 1 || ny < 1 || nz < 1)
+  bool have_out = true;
+  for (int n = 0; n < nout; n++) have_out = have_out && out[n];
+  if (!rec || !x3d || !y3d || !z3d || !have_out || nx < 1 || ny < 1 || nz < 1)
     return lay_err(CGFD_EINVAL, "grid model: missing array or empty grid");
-  const int nc = 4;
+  const int nc = 1 + nout;
   const size_t vol = (size_t)nx * ny * nz, nrec = (size_t)NI * NX * NY * nc;
-  /* device buffer: x, y, z, rho, lambda, mu, the model */
-  const size_t fl = 6 * vol + nrec;
+  /* device buffer: x, y, z, the outputs, the model */
+  const size_t fl = (3 + nout) * vol + nrec;
   char *d = nullptr;
   int *d_bad = nullptr, bad = 0, check = 0;
   const int zero = 0;
@@ -758,9 +770,9 @@ extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, in
   if (e == cudaSuccess) e = cudaMalloc((void **)&d, fl * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int));
   float *df = (float *)d;
-  float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *drec = df + 6 * vol;
+  float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *drec = df + (3 + nout) * vol;
   LayOut o = {};
-  for (int n = 0; n < 3; n++) o.v[n] = df + (3 + n) * vol;
+  for (int n = 0; n < nout; n++) o.v[n] = df + (3 + n) * vol;
   if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_lay_check, &zero, sizeof(int), 0,
                                                     cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
@@ -770,14 +782,28 @@ extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, in
   if (e == cudaSuccess) e = cudaMemcpyAsync(drec, rec, nrec * 4, cudaMemcpyHostToDevice, st);
   const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
   if (e == cudaSuccess) {
-    k_grid_loc<<<152 * 8, 256, 0, st>>>(L, G, (long long)vol, dx, dy, dz, o, d_bad);
+    switch (kind) {
+      case LAY_ISO:
+        k_grid_loc<LAY_ISO><<<152 * 8, 256, 0, st>>>(L, G, (long long)vol, dx, dy, dz, o, d_bad);
+        break;
+      case LAY_VTI_PREM:
+        k_grid_loc<LAY_VTI_PREM><<<152 * 8, 256, 0, st>>>(L, G, (long long)vol, dx, dy, dz, o,
+                                                           d_bad);
+        break;
+      case LAY_VTI_THOMSEN:
+        k_grid_loc<LAY_VTI_THOMSEN><<<152 * 8, 256, 0, st>>>(L, G, (long long)vol, dx, dy, dz, o,
+                                                              d_bad);
+        break;
+      default:
+        k_grid_loc<LAY_VTI_CIJ><<<152 * 8, 256, 0, st>>>(L, G, (long long)vol, dx, dy, dz, o,
+                                                          d_bad);
+    }
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(&check, g_lay_check, sizeof(int), 0,
                                                       cudaMemcpyDeviceToHost, st);
-  float *out[3] = {rho, lam, mu};
-  for (int n = 0; n < 3 && e == cudaSuccess; n++)
+  for (int n = 0; n < nout && e == cudaSuccess; n++)
     e = cudaMemcpyAsync(out[n], o.v[n], vol * 4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (d) cudaFree(d);
@@ -788,4 +814,30 @@ extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, in
   if (bad & 1) return lay_err(CGFD_EINVAL, "grid model: a grid point lies outside the mesh");
   if (bad & 2) return lay_err(CGFD_EINVAL, "grid model: vp <= sqrt(2) vs at a grid point");
   return 0;
+}
+
+extern "C" int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                                      float MINY, float DX, float DY, const float *rec, int nx,
+                                      int ny, int nz, const float *x3d, const float *y3d,
+                                      const float *z3d, const char *method, float *rho,
+                                      float *lam, float *mu)
+{
+  float *out[3] = {rho, lam, mu};
+  return grd_run(LAY_ISO, NI, NL, ngz, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d,
+                 z3d, method, out);
+}
+
+extern "C" int cgfd_media_grid_el_vti(int media_type, int NI, int NL, const int *ngz, int NX,
+                                      int NY, float MINX, float MINY, float DX, float DY,
+                                      const float *rec, int nx, int ny, int nz,
+                                      const float *x3d, const float *y3d, const float *z3d,
+                                      const char *method, float *c11, float *c33, float *c55,
+                                      float *c66, float *c13, float *rho)
+{
+  if (media_type != LAY_VTI_PREM && media_type != LAY_VTI_THOMSEN && media_type != LAY_VTI_CIJ)
+    return lay_err(CGFD_EINVAL, "grid model: VTI media type %d (22 prem, 23 thomsen, 24 cij)",
+                   media_type);
+  float *out[6] = {c11, c33, c55, c66, c13, rho};
+  return grd_run(media_type, NI, NL, ngz, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz, x3d, y3d,
+                 z3d, method, out);
 }

@@ -299,3 +299,53 @@ extern "C" int __wrap_media_grid2model_el_iso(float *rho3d, float *lam3d, float 
     lay_fail(in_media_file);
   return 0;
 }
+
+extern "C" int __real_media_grid2model_el_vti(float *rho, float *c11, float *c33, float *c55,
+                                              float *c66, float *c13, const float *x3d,
+                                              const float *y3d, const float *z3d, int nx, int ny,
+                                              int nz, float Xmin, float Xmax, float Ymin,
+                                              float Ymax, int grid_type,
+                                              const char *in_media_file,
+                                              const char *equivalent_medium_method, int myid);
+
+extern "C" int __wrap_media_grid2model_el_vti(float *rho, float *c11, float *c33, float *c55,
+                                              float *c66, float *c13, const float *x3d,
+                                              const float *y3d, const float *z3d, int nx, int ny,
+                                              int nz, float Xmin, float Xmax, float Ymin,
+                                              float Ymax, int grid_type,
+                                              const char *in_media_file,
+                                              const char *equivalent_medium_method, int myid)
+{
+  const char *m = equivalent_medium_method;
+  if (!lay_ours(grid_type, m, nx, ny, nz) || strcmp(m, "loc") != 0)
+    return __real_media_grid2model_el_vti(rho, c11, c33, c55, c66, c13, x3d, y3d, z3d, nx, ny,
+                                          nz, Xmin, Xmax, Ymin, Ymax, grid_type, in_media_file,
+                                          m, myid);
+  int NL = 0;
+  std::vector<int> NGz;
+  inter_t it;
+  read_grid_file(in_media_file, Xmin, Xmax, Ymin, Ymax, NL, NGz, &it);
+  const float *cols[7] = {it.elevation};
+  if (it.media_type == ELASTIC_VTI_PREM) {
+    const float *q[6] = {it.rho, it.vph, it.vpv, it.vsh, it.vsv, it.eta};
+    for (int c = 0; c < 6; c++) cols[1 + c] = q[c];
+  } else if (it.media_type == ELASTIC_VTI_THOMSEN) {
+    const float *q[6] = {it.rho, it.vp0, it.vs0, it.epsilon, it.delta, it.gamma};
+    for (int c = 0; c < 6; c++) cols[1 + c] = q[c];
+  } else if (it.media_type == ELASTIC_VTI_CIJ) {
+    const float *q[6] = {it.rho, it.c11, it.c33, it.c55, it.c66, it.c13};
+    for (int c = 0; c < 6; c++) cols[1 + c] = q[c];
+  } else {
+    return __real_media_grid2model_el_vti(rho, c11, c33, c55, c66, c13, x3d, y3d, z3d, nx, ny,
+                                          nz, Xmin, Xmax, Ymin, Ymax, grid_type, in_media_file,
+                                          m, myid);
+  }
+  const std::vector<float> rec = lay_interleave(it, cols, 7);
+  if (myid == 0)
+    fprintf(stdout, "discretising the grid model on the GPU (method %s)\n", m);
+  if (cgfd_media_grid_el_vti(it.media_type, (int)it.NI, NL, NGz.data(), (int)it.NX, (int)it.NY,
+                             it.MINX, it.MINY, it.DX, it.DY, rec.data(), nx, ny, nz, x3d, y3d,
+                             z3d, m, c11, c33, c55, c66, c13, rho))
+    lay_fail(in_media_file);
+  return 0;
+}

@@ -154,31 +154,34 @@ def bin_model(layout, ext, vols, x3d, y3d, z3d, vis=False):
 
 
 def read_md3grd(text, ext):
-    """An elastic isotropic 3-D grid model (.md3grd text or path) as the
+    """An elastic isotropic or VTI 3-D grid model (.md3grd text or path) as the
     reference's reader leaves it for a grid of extent ext = (xmin, xmax,
     ymin, ymax) (read_grid_file, media/media_read_file.cpp): the mesh
     cropped to columns floor((xmin - MINX) / DX) .. ceil((xmax - MINX) / DX)
     and the rows alike.  Returns a dict: media_type, NL, ngz (levels per
-    layer), NI (levels), NX, NY, MINX, MINY, DX, DY and rec (NI, NY, NX, 4) =
-    elevation, rho, vp, vs.  The file has no comment lines (the reference's
-    reader takes none)."""
+    layer), NI (levels), NX, NY, MINX, MINY, DX, DY and rec (NI, NY, NX, 4 or
+    7) = elevation, then rho, vp, vs or the six VTI parameters.  The file has
+    no comment lines (the reference's reader takes none)."""
     if "\n" not in text:
         with open(text) as f:
             text = f.read()
     words = text.split()
-    if not words or words[0] != "elastic_isotropic":
-        raise ValueError("elastic_isotropic grid models are read")
+    ncol = {"elastic_isotropic": 4, "elastic_vti_prem": 7, "elastic_vti_thomsen": 7,
+            "elastic_vti_cij": 7}
+    if not words or words[0] not in ncol:
+        raise ValueError("grid models of %s are read" % ", ".join(ncol))
+    kind, nc = words[0], ncol[words[0]]
     NL = int(words[1])
     ngz = [int(w) for w in words[2:2 + NL]]
     NI = sum(ngz)
     pos = 2 + NL
     NX, NY = int(words[pos]), int(words[pos + 1])
     MINX, MINY, DX, DY = [np.float32(w) for w in words[pos + 2:pos + 6]]
-    vals = np.array([np.float32(w) for w in words[pos + 6:pos + 6 + NI * NY * NX * 4]],
+    vals = np.array([np.float32(w) for w in words[pos + 6:pos + 6 + NI * NY * NX * nc]],
                     np.float32)
-    if NL < 1 or min(ngz) < 1 or NX < 2 or NY < 2 or vals.size != NI * NY * NX * 4:
+    if NL < 1 or min(ngz) < 1 or NX < 2 or NY < 2 or vals.size != NI * NY * NX * nc:
         raise ValueError("incomplete grid model")
-    full = vals.reshape(NI, NY, NX, 4)
+    full = vals.reshape(NI, NY, NX, nc)
     xmin, xmax, ymin, ymax = [np.float32(e) for e in ext]
     q = lambda a, b, d: np.float32(np.float32(a - b) / d)
     ix0, iy0 = q(xmin, MINX, DX), q(ymin, MINY, DY)
@@ -190,7 +193,7 @@ def read_md3grd(text, ext):
         raise ValueError("the grid model does not cover the grid")
     minx = np.float32(np.float32(ix0 * DX) + MINX)
     miny = np.float32(np.float32(iy0 * DY) + MINY)
-    return dict(media_type="elastic_isotropic", NL=NL, ngz=ngz, NI=NI, NX=ix1 - ix0 + 1,
+    return dict(media_type=kind, NL=NL, ngz=ngz, NI=NI, NX=ix1 - ix0 + 1,
                 NY=iy1 - iy0 + 1, MINX=float(minx), MINY=float(miny), DX=float(DX),
                 DY=float(DY), rec=np.ascontiguousarray(full[:, iy0:iy1 + 1, ix0:ix1 + 1]))
 
@@ -210,4 +213,23 @@ def grid_el_iso(model, x3d, y3d, z3d, method="loc"):
         C.c_float(model["MINX"]), C.c_float(model["MINY"]), C.c_float(model["DX"]),
         C.c_float(model["DY"]), rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data,
         z.ctypes.data, method.encode(), *[o.ctypes.data for o in out]))
+    return tuple(out)
+
+
+def grid_el_vti(model, x3d, y3d, z3d, method="loc"):
+    """c11, c33, c55, c66, c13, rho of an elastic VTI 3-D grid model (dict of
+    read_md3grd) on the grid with "loc", computed on the device
+    (cgfd_media_grid_el_vti)."""
+    shape = np.shape(x3d)
+    nz, ny, nx = shape
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    rec = np.ascontiguousarray(model["rec"], np.float32)
+    ngz = np.ascontiguousarray(model["ngz"], np.int32)
+    out = [np.empty(shape, np.float32) for _ in range(6)]
+    _lib.check(_lib.lib().cgfd_media_grid_el_vti(
+        MEDIA_TYPE_CODES[model["media_type"]], int(model["NI"]), int(model["NL"]),
+        ngz.ctypes.data, int(model["NX"]), int(model["NY"]), C.c_float(model["MINX"]),
+        C.c_float(model["MINY"]), C.c_float(model["DX"]), C.c_float(model["DY"]),
+        rec.ctypes.data, nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
+        method.encode(), *[o.ctypes.data for o in out]))
     return tuple(out)

@@ -365,6 +365,18 @@ int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float
                            int nz, const float *x3d, const float *y3d, const float *z3d,
                            const char *method, float *rho, float *lam, float *mu);
 
+/* An elastic VTI 3-D grid model (media_type CGFD_LAYER_VTI_*) with the
+ * "loc" method, as media_grid2model_el_vti does (media/media_grid2model.cpp:
+ * 190-249, 556-700, 1127-1184; called at forward/main_curv_col_el_3d.c:
+ * 406-415): rec [NI][NY][NX][7] = elevation and the six parameters of the
+ * type, linear between levels, then para2vti.  Writes c11 c33 c55 c66 c13
+ * rho (host).  "har" and "ari" are CGFD_EINVAL. */
+int cgfd_media_grid_el_vti(int media_type, int NI, int NL, const int *ngz, int NX, int NY,
+                           float MINX, float MINY, float DX, float DY, const float *rec, int nx,
+                           int ny, int nz, const float *x3d, const float *y3d, const float *z3d,
+                           const char *method, float *c11, float *c33, float *c55, float *c66,
+                           float *c13, float *rho);
+
 int cgfd_media_layer_el_iso(int NI, int NX, int NY, float MINX, float MINY, float DX,
                             float DY, const float *rec, int nx, int ny, int nz,
                             const float *x3d, const float *y3d, const float *z3d,

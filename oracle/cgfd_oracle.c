@@ -2416,6 +2416,7 @@ int oracle_bin(int vis, const int *order, const int *size, const float *spacing,
  * elevation, rho, vp, vs as the reference's reader leaves them (after its
  * crop to the grid's extent, media/media_read_file.cpp read_grid_file). */
 typedef struct {
+  int kind, np, nc;           /* LAY_ISO (rho vp vs) or LAY_VTI_*; nc = 1 + np */
   int NI, NX, NY, NL;
   int start[LAY_MAXI];        /* first level of each layer */
   const float *xv, *yv, *rec;
@@ -2435,13 +2436,16 @@ static int grd_is_start(const grd_model_t *m, int mi)
 
 static float grd_val(const grd_model_t *m, int level, int c, float x, float y)
 {
-  return lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + level * m->slice * 4 + c, 4, x, y);
+  return lay_bilinear(m->xv, m->NX, m->yv, m->NY, m->rec + level * m->slice * m->nc + c, m->nc,
+                      x, y);
 }
 
-/* rho, vp, vs at a point: AssignGridMediaPara2Point with CalPointValue_grid
- * for ELASTIC_ISOTROPIC (media/media_grid2model.cpp:424-556).  *on: the
- * point lies on a layer's top level (isPointOnInter).  Returns 1 where the
- * reference exits (outside the mesh, vp <= sqrt(2) vs). */
+/* the parameters at a point (rho vp vs, or the six of a VTI type):
+ * AssignGridMediaPara2Point with CalPointValue_grid
+ * (media/media_grid2model.cpp:424-700), linear between the two levels
+ * around the point.  *on: the point lies on a layer's top level
+ * (isPointOnInter).  Returns 1 where the reference exits (outside the mesh;
+ * isotropic: vp <= sqrt(2) vs). */
 static int grd_point(const grd_model_t *m, float x, float y, float z, float *var, int *on)
 {
   const int NI = m->NI;
@@ -2457,23 +2461,18 @@ static int grd_point(const grd_model_t *m, float x, float y, float z, float *var
     dis_r = (z - elev[mi]) / (elev[mi + 1] - elev[mi]);
   if (mi == -1 || mi == NI - 1) {
     if (mi == -1) mi = lay_last_ge(elev[0], elev, NI);
-    var[0] = grd_val(m, mi, 1, x, y);
-    var[1] = grd_val(m, mi, 2, x, y);
-    var[2] = grd_val(m, mi, 3, x, y);
+    for (int p = 0; p < m->np; p++) var[p] = grd_val(m, mi, 1 + p, x, y);
     return 0;
   }
   if (mi > 0 && fabsf(elev[mi] - z) < FLT_EPSILON && grd_is_start(m, mi)) {
     mi--;
     dis_r = 1.0 / 2.0;
   }
-  float vp0 = grd_val(m, mi, 2, x, y), vs0 = grd_val(m, mi, 3, x, y);
-  float rho0 = grd_val(m, mi, 1, x, y);
-  float vp1 = grd_val(m, mi + 1, 2, x, y), vs1 = grd_val(m, mi + 1, 3, x, y);
-  float rho1 = grd_val(m, mi + 1, 1, x, y);
-  var[1] = vp0 + (vp1 - vp0) * dis_r;
-  var[2] = vs0 + (vs1 - vs0) * dis_r;
-  var[0] = rho0 + (rho1 - rho0) * dis_r;
-  if (var[1] <= sqrt(2) * var[2]) return 1;
+  for (int p = 0; p < m->np; p++) {
+    float v0 = grd_val(m, mi, 1 + p, x, y), v1 = grd_val(m, mi + 1, 1 + p, x, y);
+    var[p] = v0 + (v1 - v0) * dis_r;
+  }
+  if (m->kind == LAY_ISO && var[1] <= sqrt(2) * var[2]) return 1;
   return 0;
 }
 
@@ -2492,12 +2491,18 @@ static int grd_layer(const grd_model_t *m, float x, float y, float z)
  * mu (the reference's argument order).  har and ari recompute the interior
  * points whose cell touches two layers from the 9^3 samples not lying on a
  * layer's top level.  Returns 1 where the reference exits. */
+static int oracle_grid_vti_loc(int kind, int NI, int NL, const int *ngz, int NX, int NY,
+                               float MINX, float MINY, float DX, float DY, const float *rec,
+                               int nx, int ny, int nz, const float *x3d, const float *y3d,
+                               const float *z3d, float **out);
+
 int oracle_grid_el_iso(int method, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
                        float MINY, float DX, float DY, const float *rec, int nx, int ny, int nz,
                        const float *x3d, const float *y3d, const float *z3d, float **out)
 {
   if (NI < 1 || NI > LAY_MAXI || NL < 1 || NL > NI) return 1;
   grd_model_t m;
+  m.kind = LAY_ISO; m.np = 3; m.nc = 4;
   m.NI = NI; m.NX = NX; m.NY = NY; m.NL = NL;
   int acc = 0;
   for (int l = 0; l < NL; l++) {
@@ -2590,4 +2595,54 @@ int oracle_grid_el_iso(int method, int NI, int NL, const int *ngz, int NX, int N
   }
   free(xv); free(yv); free(m.elev); free(m.elev_nl);
   return bad;
+}
+
+/* An elastic VTI grid model (kind LAY_VTI_*) with "loc": the six parameters
+ * at each point, then para2vti (parametrization_grid_el_vti_loc,
+ * media/media_grid2model.cpp:1127-1184); rec [NI][NY][NX][7]; out = c11 c33
+ * c55 c66 c13 rho.  Returns 1 where the reference exits. */
+static int oracle_grid_vti_loc(int kind, int NI, int NL, const int *ngz, int NX, int NY,
+                               float MINX, float MINY, float DX, float DY, const float *rec,
+                               int nx, int ny, int nz, const float *x3d, const float *y3d,
+                               const float *z3d, float **out)
+{
+  if (NI < 1 || NI > LAY_MAXI || NL < 1 || NL > NI) return 1;
+  grd_model_t m;
+  m.kind = kind; m.np = 6; m.nc = 7;
+  m.NI = NI; m.NX = NX; m.NY = NY; m.NL = NL;
+  int acc = 0;
+  for (int l = 0; l < NL; l++) {
+    m.start[l] = acc;
+    acc += ngz[l];
+  }
+  if (acc != NI) return 1;
+  float *xv = malloc(NX * sizeof(float)), *yv = malloc(NY * sizeof(float));
+  for (int i = 0; i < NX; i++) xv[i] = MINX + DX * i;
+  for (int j = 0; j < NY; j++) yv[j] = MINY + DY * j;
+  m.xv = xv; m.yv = yv; m.rec = rec; m.slice = (size_t)NX * NY;
+  m.minx = MINX; m.maxx = MINX + (NX - 1) * DX;
+  m.miny = MINY; m.maxy = MINY + (NY - 1) * DY;
+  m.elev = malloc(NI * sizeof(float));
+  m.elev_nl = malloc(NL * sizeof(float));
+  int bad = 0;
+  const size_t vol = (size_t)nx * ny * nz;
+  for (size_t q = 0; q < vol && !bad; q++) {
+    float var[6], c[6];
+    int on;
+    if (grd_point(&m, x3d[q], y3d[q], z3d[q], var, &on)) { bad = 1; break; }
+    lay_para2vti(kind, var, c);
+    for (int n = 0; n < 6; n++) out[n][q] = c[n];
+  }
+  free(xv); free(yv); free(m.elev); free(m.elev_nl);
+  return bad;
+}
+
+int oracle_grid_el_vti_loc(int kind, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                           float MINY, float DX, float DY, const float *rec, int nx, int ny,
+                           int nz, const float *x3d, const float *y3d, const float *z3d,
+                           float **out)
+{
+  if (kind != LAY_VTI_PREM && kind != LAY_VTI_THOMSEN && kind != LAY_VTI_CIJ) return 1;
+  return oracle_grid_vti_loc(kind, NI, NL, ngz, NX, NY, MINX, MINY, DX, DY, rec, nx, ny, nz,
+                             x3d, y3d, z3d, out);
 }

@@ -128,3 +128,24 @@ int cgfd_media_grid_el_iso(int NI, int NL, const int *ngz, int NX, int NY, float
   }
   return 0;
 }
+
+int oracle_grid_el_vti_loc(int kind, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
+                           float MINY, float DX, float DY, const float *rec, int nx, int ny,
+                           int nz, const float *x3d, const float *y3d, const float *z3d,
+                           float **out);
+
+int cgfd_media_grid_el_vti(int media_type, int NI, int NL, const int *ngz, int NX, int NY,
+                           float MINX, float MINY, float DX, float DY, const float *rec, int nx,
+                           int ny, int nz, const float *x3d, const float *y3d, const float *z3d,
+                           const char *method, float *c11, float *c33, float *c55, float *c66,
+                           float *c13, float *rho)
+{
+  float *o[6] = {c11, c33, c55, c66, c13, rho};
+  if (stub_method(method) != 0 ||
+      oracle_grid_el_vti_loc(media_type, NI, NL, ngz, NX, NY, MINX, MINY, DX, DY, rec, nx, ny,
+                             nz, x3d, y3d, z3d, o)) {
+    stub_msg = "grid model: bad method or a point outside the mesh";
+    return CGFD_EINVAL;
+  }
+  return 0;
+}

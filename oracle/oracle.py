@@ -237,3 +237,27 @@ def grid_el_iso(model, x3d, y3d, z3d, method="loc"):
                                x.ctypes.data, y.ctypes.data, z.ctypes.data,
                                C.cast(ptrs, C.c_void_p))
     return None if bad else tuple(out)
+
+
+def grid_el_vti_loc(model, x3d, y3d, z3d):
+    """An elastic VTI 3-D grid model (dict of cgfd3d_gb300.media.read_md3grd)
+    with "loc", as media_grid2model_el_vti: (c11, c33, c55, c66, c13, rho);
+    None where the reference would exit."""
+    import numpy as np
+    L = lib()
+    L.oracle_grid_el_vti_loc.restype = C.c_int
+    L.oracle_grid_el_vti_loc.argtypes = ([C.c_int] * 3 + [C.c_void_p] + [C.c_int] * 2 +
+                                         [C.c_float] * 4 + [C.c_void_p] + [C.c_int] * 3 +
+                                         [C.c_void_p] * 4)
+    nz, ny, nx = np.shape(x3d)
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    rec = np.ascontiguousarray(model["rec"], np.float32)
+    ngz = np.ascontiguousarray(model["ngz"], np.int32)
+    out = [np.zeros((nz, ny, nx), np.float32) for _ in range(6)]
+    ptrs = (C.c_void_p * 6)(*[o.ctypes.data for o in out])
+    bad = L.oracle_grid_el_vti_loc(LAYER_KINDS[model["media_type"]], model["NI"], model["NL"],
+                                   ngz.ctypes.data, model["NX"], model["NY"], model["MINX"],
+                                   model["MINY"], model["DX"], model["DY"], rec.ctypes.data,
+                                   nx, ny, nz, x.ctypes.data, y.ctypes.data, z.ctypes.data,
+                                   C.cast(ptrs, C.c_void_p))
+    return None if bad else tuple(out)

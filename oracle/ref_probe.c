@@ -50,6 +50,11 @@
  *       grid's extent <ext> (float xmin, xmax, ymin, ymax);
  *       <output>: float rho, lambda, mu [nz][ny][nx]
  *
+ *   ref_probe grid_vti <md3grd> <grid> <method> <ext> <output>
+ *       an elastic VTI 3-D grid model by media_grid2model_el_vti
+ *       (media/media_grid2model.cpp:190-249); <output>: float c11, c33, c55,
+ *       c66, c13, rho [nz][ny][nx]
+ *
  *   ref_probe bin <grid> <params> <rho> <vp> <vs> <output>
  *   ref_probe bin_vis <grid> <params> <Qp> <Qs> <output>
  *       a model given as binary volumes interpolated on a curvilinear grid
@@ -97,6 +102,11 @@ int media_grid2model_el_iso(float *rho3d, float *lam3d, float *mu3d, const float
                             float Xmin, float Xmax, float Ymin, float Ymax, int grid_type,
                             const char *in_media_file, const char *equivalent_medium_method,
                             int myid);
+int media_grid2model_el_vti(float *rho, float *c11, float *c33, float *c55, float *c66,
+                            float *c13, const float *x3d, const float *y3d, const float *z3d,
+                            int nx, int ny, int nz, float Xmin, float Xmax, float Ymin,
+                            float Ymax, int grid_type, const char *in_media_file,
+                            const char *equivalent_medium_method, int myid);
 #define PROBE_GRID_CURV 3
 
 static void rd(void *p, size_t n, FILE *fp)
@@ -356,8 +366,8 @@ static int probe_bin(int vis, const char *grid, const char *params, const char *
   return 0;
 }
 
-static int probe_grid(const char *grd, const char *grid, const char *method, const char *extf,
-                      const char *out)
+static int probe_grid(int vti, const char *grd, const char *grid, const char *method,
+                      const char *extf, const char *out)
 {
   FILE *fp = fopen(grid, "rb");
   if (!fp) return 2;
@@ -374,13 +384,18 @@ static int probe_grid(const char *grd, const char *grid, const char *method, con
   if (!fp) return 2;
   rd(ext, sizeof ext, fp);
   fclose(fp);
-  float *o[3];
-  for (int n = 0; n < 3; n++) o[n] = calloc(vol, 4);
-  media_grid2model_el_iso(o[0], o[1], o[2], x, y, z, d[0], d[1], d[2], ext[0], ext[1], ext[2],
-                          ext[3], PROBE_GRID_CURV, grd, method, 0);
+  const int nout = vti ? 6 : 3;
+  float *o[6];   /* rho lambda mu, or c11 c33 c55 c66 c13 rho */
+  for (int n = 0; n < nout; n++) o[n] = calloc(vol, 4);
+  if (vti)
+    media_grid2model_el_vti(o[5], o[0], o[1], o[2], o[3], o[4], x, y, z, d[0], d[1], d[2],
+                            ext[0], ext[1], ext[2], ext[3], PROBE_GRID_CURV, grd, method, 0);
+  else
+    media_grid2model_el_iso(o[0], o[1], o[2], x, y, z, d[0], d[1], d[2], ext[0], ext[1],
+                            ext[2], ext[3], PROBE_GRID_CURV, grd, method, 0);
   FILE *fo = fopen(out, "wb");
   if (!fo) return 2;
-  for (int n = 0; n < 3; n++) fwrite(o[n], 4, vol, fo);
+  for (int n = 0; n < nout; n++) fwrite(o[n], 4, vol, fo);
   fclose(fo);
   return 0;
 }
@@ -396,7 +411,9 @@ int main(int argc, char **argv)
   if (argc == 6 && strcmp(argv[1], "layer_one") == 0)
     return probe_layer_one(argv[2], argv[3], argv[4], argv[5]);
   if (argc == 7 && strcmp(argv[1], "grid") == 0)
-    return probe_grid(argv[2], argv[3], argv[4], argv[5], argv[6]);
+    return probe_grid(0, argv[2], argv[3], argv[4], argv[5], argv[6]);
+  if (argc == 7 && strcmp(argv[1], "grid_vti") == 0)
+    return probe_grid(1, argv[2], argv[3], argv[4], argv[5], argv[6]);
   if (argc == 8 && strcmp(argv[1], "bin") == 0)
     return probe_bin(0, argv[2], argv[3], (const char *const *)argv + 4, argv[7]);
   if (argc == 7 && strcmp(argv[1], "bin_vis") == 0)

@@ -35,6 +35,10 @@ one on a flat grid level, grid points below the last level) on the first
 grid through media_grid2model_el_iso (media/media_grid2model.cpp:133-189)
 with each method; keys md3grd, ext and rho_<m>, lam_<m>, mu_<m>.
 
+And grid_el_vti.npz: elastic VTI grid models of the three parametrisations
+(the same levels) through media_grid2model_el_vti with "loc"; keys
+<type>_md3grd and <type>_<c11|c33|c55|c66|c13|rho>.
+
 This script needs the reference build and runs only where it exists; the
 fixtures it writes are committed and are all the tests need elsewhere.
 
@@ -192,6 +196,7 @@ def main():
     one_main(X, Y, Z)
     bin_main(X, Y, Z)
     grid_main(X, Y, Z)
+    grid_vti_main(X, Y, Z)
     on = int(np.isclose(Z, -800.0).sum())
     print("grid %s, %d points on the flat interface, rho range %.1f-%.1f"
           % (X.shape, on, out[2].min(), out[2].max()))
@@ -335,6 +340,66 @@ def grid_main(X, Y, Z):
     print("grid: har changed %d points, rho %.1f-%.1f"
           % ((res["lam_har"] != res["lam_loc"]).sum(), res["rho_loc"].min(),
              res["rho_loc"].max()))
+
+
+GRID_VTI = {
+    # per layer (top value, bottom value) of the six parameters
+    "elastic_vti_prem": [((2300, 2400), (4000, 4400), (3800, 4200), (2200, 2400), (2100, 2300),
+                          (0.95, 0.93))] * 3,
+    "elastic_vti_thomsen": [((2300, 2450), (3800, 4300), (2100, 2400), (0.15, 0.12),
+                             (0.08, 0.06), (0.10, 0.08))] * 3,
+    "elastic_vti_cij": [((2300, 2450), (3.9e10, 4.6e10), (3.3e10, 4.0e10), (1.0e10, 1.3e10),
+                         (1.2e10, 1.5e10), (1.2e10, 1.4e10))] * 3,
+}
+
+
+def grid_vti_main(X, Y, Z):
+    rng = np.random.default_rng(29)
+    ext = np.array([X.min(), X.max(), Y.min(), Y.max()], np.float32)
+    NX, NY = 12, 10
+    dx = float(ext[1] - ext[0]) / (NX - 1.8)
+    dy = float(ext[3] - ext[2]) / (NY - 1.8)
+    minx, miny = float(ext[0]) - 0.3 * dx, float(ext[2]) - 0.3 * dy
+    XX, YY = np.meshgrid(minx + dx * np.arange(NX), miny + dy * np.arange(NY))
+    l2 = -390.0 + 80.0 * np.sin(XX / 900.0 + 0.5)
+    levels = [60.0 + 20.0 * np.sin(XX / 700.0) * np.cos(YY / 500.0),
+              -150.0 + 30.0 * np.sin(XX / 900.0), l2,
+              l2, -600.0 + 20.0 * np.cos(YY / 600.0), np.full_like(XX, -800.0),
+              np.full_like(XX, -800.0), -1100.0 + 60.0 * np.cos(YY / 600.0),
+              np.full_like(XX, -1400.0)]
+    nz, ny, nx = X.shape
+    res = dict(ext=ext)
+    with tempfile.TemporaryDirectory() as tmp:
+        gpath, epath = os.path.join(tmp, "grid.bin"), os.path.join(tmp, "ext.bin")
+        opath = os.path.join(tmp, "out.bin")
+        with open(gpath, "wb") as f:
+            f.write(struct.pack("<3i", nx, ny, nz))
+            for A in (X, Y, Z):
+                f.write(A.astype("<f4").tobytes())
+        ext.tofile(epath)
+        for kind, props in GRID_VTI.items():
+            lines = [kind, "3", "3 3 3", "%d %d %.9g %.9g %.9g %.9g" % (NX, NY, minx, miny, dx, dy)]
+            for ni, e in enumerate(levels):
+                layer, t = ni // 3, (ni % 3) / 2.0
+                scale = 1.0 + 0.08 * layer
+                vals = [(lo + (hi - lo) * t) * (scale if c < 5 or kind != "elastic_vti_thomsen"
+                                               else 1.0) for c, (lo, hi) in enumerate(props[layer])]
+                pert = [v * (1.0 + 0.02 * rng.uniform(-1, 1, XX.shape)) for v in vals]
+                for j in range(NY):
+                    for i in range(NX):
+                        lines.append(" ".join(["%.9g" % np.float32(e[j, i])] +
+                                              ["%.9g" % p_[j, i] for p_ in pert]))
+            text = "\n".join(lines) + "\n"
+            res[kind + "_md3grd"] = np.frombuffer(text.encode(), np.uint8)
+            grd = os.path.join(tmp, kind + ".md3grd")
+            open(grd, "w").write(text)
+            subprocess.run([PROBE, "grid_vti", grd, gpath, "loc", epath, opath], check=True,
+                           stdout=subprocess.DEVNULL)
+            o = np.fromfile(opath, "<f4").reshape(6, nz, ny, nx)
+            for c, name in enumerate(("c11", "c33", "c55", "c66", "c13", "rho")):
+                res[kind + "_" + name] = o[c]
+    np.savez_compressed(os.path.join(HERE, "grid_el_vti.npz"), **res)
+    print("grid vti: %d types" % len(GRID_VTI))
 
 
 def vti_main():

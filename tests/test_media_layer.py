@@ -148,6 +148,28 @@ def test_oracle_grid_matches_reference_bitwise(method):
         np.testing.assert_array_equal(a.view(np.int32), z[k + "_" + method].view(np.int32))
 
 
+FIX_GRID_VTI = os.path.join(REPO, "tests", "golden", "media", "grid_el_vti.npz")
+GRID_VTI_TYPES = ["elastic_vti_prem", "elastic_vti_thomsen", "elastic_vti_cij"]
+
+
+def _grid_vti(kind):
+    from cgfd3d_gb300 import media
+    z = np.load(FIX_GRID_VTI)
+    g = np.load(FIX)
+    return z, g, media.read_md3grd(bytes(z[kind + "_md3grd"]).decode(), z["ext"])
+
+
+@pytest.mark.parametrize("kind", GRID_VTI_TYPES)
+def test_oracle_grid_vti_matches_reference_bitwise(kind):
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    z, g, m = _grid_vti(kind)
+    assert m["media_type"] == kind and m["rec"].shape[-1] == 7
+    got = oracle.grid_el_vti_loc(m, g["x3d"], g["y3d"], g["z3d"])
+    for a, k in zip(got, VTI_OUT):
+        np.testing.assert_array_equal(a.view(np.int32), z[kind + "_" + k].view(np.int32))
+
+
 def test_har_and_ari_differ():
     z, _ = _fixture()
     d = z["lam_har"] != z["lam_ari"]
@@ -335,6 +357,46 @@ def test_dropin_adapter_grid_inside_reference(method, tmp_path):
     got = np.fromfile(out, "<f4").reshape(3, nz, ny, nx)
     for a, k in zip(got, ("rho", "lam", "mu")):
         np.testing.assert_array_equal(a.view(np.int32), z[k + "_" + method].view(np.int32))
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("kind", GRID_VTI_TYPES)
+def test_dropin_adapter_grid_vti_inside_reference(kind, tmp_path):
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe_media"], check=True, capture_output=True)
+    z, g, _ = _grid_vti(kind)
+    grd = tmp_path / "model.md3grd"
+    grd.write_bytes(bytes(z[kind + "_md3grd"]))
+    nz, ny, nx = g["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(np.array([nx, ny, nz], "<i4").tobytes())
+        for a in (g["x3d"], g["y3d"], g["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    ext = tmp_path / "ext.bin"
+    np.ascontiguousarray(z["ext"], "<f4").tofile(ext)
+    out = tmp_path / "out.bin"
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_probe_media")
+    r = subprocess.run([exe, "grid_vti", str(grd), str(grid), "loc", str(ext), str(out)],
+                       capture_output=True, text=True, check=True)
+    assert "discretising the grid model on the GPU (method loc)" in r.stdout
+    got = np.fromfile(out, "<f4").reshape(6, nz, ny, nx)
+    for a, k in zip(got, VTI_OUT):
+        np.testing.assert_array_equal(a.view(np.int32), z[kind + "_" + k].view(np.int32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", GRID_VTI_TYPES)
+def test_device_grid_vti_matches_reference(kind):
+    """VTI grid models with loc on the device: bit for bit (no pow here; the
+    double arithmetic of para2vti is kept)."""
+    from cgfd3d_gb300 import media
+    z, g, m = _grid_vti(kind)
+    got = media.grid_el_vti(m, g["x3d"], g["y3d"], g["z3d"])
+    for a, k in zip(got, VTI_OUT):
+        np.testing.assert_array_equal(a.view(np.int32), z[kind + "_" + k].view(np.int32))
 
 
 @pytest.mark.gpu
