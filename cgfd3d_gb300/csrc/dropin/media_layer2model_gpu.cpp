@@ -349,3 +349,101 @@ extern "C" int __wrap_media_grid2model_el_vti(float *rho, float *c11, float *c33
     lay_fail(in_media_file);
   return 0;
 }
+
+extern "C" int __real_media_layer2model_el_aniso(
+    float *rho, float *c11, float *c12, float *c13, float *c14, float *c15, float *c16,
+    float *c22, float *c23, float *c24, float *c25, float *c26, float *c33, float *c34, float *c35,
+    float *c36, float *c44, float *c45, float *c46, float *c55, float *c56, float *c66,
+    const float *x3d, const float *y3d, const float *z3d, size_t nx, size_t ny, size_t nz,
+    int grid_type, const char *in_3lay_file, const char *equivalent_medium_method, int myid);
+
+/* media_layer2model_el_aniso for elastic isotropic and VTI layered models
+ * (media/media_layer2model.cpp:249-375): the same discretisation on the
+ * device, then the reference's spreading into the 21 constants, in its
+ * float/double order.  TTI and full-anisotropy models and the "tti" method
+ * stay with the reference's routine. */
+extern "C" int __wrap_media_layer2model_el_aniso(
+    float *rho, float *c11, float *c12, float *c13, float *c14, float *c15, float *c16,
+    float *c22, float *c23, float *c24, float *c25, float *c26, float *c33, float *c34, float *c35,
+    float *c36, float *c44, float *c45, float *c46, float *c55, float *c56, float *c66,
+    const float *x3d, const float *y3d, const float *z3d, size_t nx, size_t ny, size_t nz,
+    int grid_type, const char *in_3lay_file, const char *equivalent_medium_method, int myid)
+{
+  const char *m = equivalent_medium_method;
+  if (!lay_ours(grid_type, m, nx, ny, nz))
+    return __real_media_layer2model_el_aniso(rho, c11, c12, c13, c14, c15, c16, c22, c23, c24,
+                                             c25, c26, c33, c34, c35, c36, c44, c45, c46, c55,
+                                             c56, c66, x3d, y3d, z3d, nx, ny, nz, grid_type,
+                                             in_3lay_file, m, myid);
+  inter_t it;
+  read_interface_file(in_3lay_file, &it);
+  const int t = it.media_type;
+  const size_t vol = nx * ny * nz;
+  int rc = -1;
+  if (t == ELASTIC_ISOTROPIC) {
+    const float *cols[10] = {it.elevation, it.rho, it.rho_grad, it.rho_pow, it.vp,
+                             it.vp_grad,   it.vp_pow, it.vs,     it.vs_grad, it.vs_pow};
+    const std::vector<float> rec = lay_interleave(it, cols, 10);
+    if (cgfd_media_layer_pow_ok(10, rec.data(), it.NI * it.NX * it.NY)) {
+      if (myid == 0)
+        fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
+      /* lambda into c13, mu into c44, as the reference's isotropic branch */
+      rc = cgfd_media_layer_el_iso((int)it.NI, (int)it.NX, (int)it.NY, it.MINX, it.MINY, it.DX,
+                                   it.DY, rec.data(), (int)nx, (int)ny, (int)nz, x3d, y3d, z3d,
+                                   m, c13, c44, rho);
+      if (rc != 0) lay_fail(in_3lay_file);
+      for (size_t i = 0; i < vol; ++i) {
+        c11[i] = c13[i] + 2.0 * c44[i];
+        c22[i] = c11[i]; c33[i] = c11[i];
+        c12[i] = c13[i]; c23[i] = c13[i];
+        c55[i] = c44[i]; c66[i] = c44[i];
+      }
+    }
+  } else if (t == ELASTIC_VTI_PREM || t == ELASTIC_VTI_THOMSEN || t == ELASTIC_VTI_CIJ) {
+    const float *cols[19] = {it.elevation};
+    const float *p[18];
+    if (t == ELASTIC_VTI_PREM) {
+      const float *q[18] = {it.rho, it.rho_grad, it.rho_pow, it.vph, it.vph_grad, it.vph_pow,
+                            it.vpv, it.vpv_grad, it.vpv_pow, it.vsh, it.vsh_grad, it.vsh_pow,
+                            it.vsv, it.vsv_grad, it.vsv_pow, it.eta, it.eta_grad, it.eta_pow};
+      memcpy(p, q, sizeof p);
+    } else if (t == ELASTIC_VTI_THOMSEN) {
+      const float *q[18] = {it.rho,     it.rho_grad,     it.rho_pow,     it.vp0,
+                            it.vp0_grad, it.vp0_pow,     it.vs0,         it.vs0_grad,
+                            it.vs0_pow, it.epsilon,      it.epsilon_grad, it.epsilon_pow,
+                            it.delta,   it.delta_grad,   it.delta_pow,   it.gamma,
+                            it.gamma_grad, it.gamma_pow};
+      memcpy(p, q, sizeof p);
+    } else {
+      const float *q[18] = {it.rho, it.rho_grad, it.rho_pow, it.c11, it.c11_grad, it.c11_pow,
+                            it.c33, it.c33_grad, it.c33_pow, it.c55, it.c55_grad, it.c55_pow,
+                            it.c66, it.c66_grad, it.c66_pow, it.c13, it.c13_grad, it.c13_pow};
+      memcpy(p, q, sizeof p);
+    }
+    for (int c = 0; c < 18; c++) cols[1 + c] = p[c];
+    const std::vector<float> rec = lay_interleave(it, cols, 19);
+    if (cgfd_media_layer_pow_ok(19, rec.data(), it.NI * it.NX * it.NY)) {
+      if (myid == 0)
+        fprintf(stdout, "discretising the layered model on the GPU (method %s)\n", m);
+      rc = cgfd_media_layer_el_vti(t, (int)it.NI, (int)it.NX, (int)it.NY, it.MINX, it.MINY,
+                                   it.DX, it.DY, rec.data(), (int)nx, (int)ny, (int)nz, x3d,
+                                   y3d, z3d, m, c11, c33, c55, c66, c13, rho);
+      if (rc != 0) lay_fail(in_3lay_file);
+      for (size_t i = 0; i < vol; i++) {
+        c12[i] = c11[i] - 2.0 * c66[i];
+        c22[i] = c11[i];
+        c23[i] = c13[i];
+        c44[i] = c55[i];
+      }
+    }
+  }
+  if (rc != 0)
+    return __real_media_layer2model_el_aniso(rho, c11, c12, c13, c14, c15, c16, c22, c23, c24,
+                                             c25, c26, c33, c34, c35, c36, c44, c45, c46, c55,
+                                             c56, c66, x3d, y3d, z3d, nx, ny, nz, grid_type,
+                                             in_3lay_file, m, myid);
+  float *zero[12] = {c14, c24, c34, c15, c25, c35, c16, c26, c36, c45, c46, c56};
+  for (int n = 0; n < 12; n++)
+    for (size_t i = 0; i < vol; i++) zero[n][i] = 0.0;
+  return 0;
+}

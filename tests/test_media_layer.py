@@ -399,6 +399,44 @@ def test_device_grid_vti_matches_reference(kind):
         np.testing.assert_array_equal(a.view(np.int32), z[kind + "_" + k].view(np.int32))
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("case", [("iso", "har"), ("iso", "loc"), ("elastic_vti_thomsen", "ari"),
+                                  ("elastic_vti_cij", "loc")])
+def test_dropin_adapter_aniso_inside_reference(case, tmp_path):
+    """media_layer2model_el_aniso for isotropic and VTI layered models: the
+    adapter's build (library call answered by the oracle, then the spreading
+    into the 21 constants) against the unmodified reference, all 22 volumes
+    bit for bit."""
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe", "_ref/ref_probe_media"], check=True, capture_output=True)
+    kind, method = case
+    if kind == "iso":
+        z, _ = _fixture()
+        text, grid_src = bytes(z["md3lay"]), z
+    else:
+        z, _ = _vti(kind)
+        text, grid_src = bytes(z[kind + "_md3lay"]), z
+    lay = tmp_path / "model.md3lay"
+    lay.write_bytes(text)
+    nz, ny, nx = grid_src["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(np.array([nx, ny, nz], "<i4").tobytes())
+        for a in (grid_src["x3d"], grid_src["y3d"], grid_src["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    outs = []
+    for exe in ("ref_probe", "ref_probe_media"):
+        out = tmp_path / (exe + ".bin")
+        r = subprocess.run([os.path.join(REPO, "oracle", "_ref", exe), "layer_aniso", str(lay),
+                            str(grid), method, str(out)], capture_output=True, text=True,
+                           check=True)
+        outs.append(np.fromfile(out, "<f4").reshape(22, nz, ny, nx))
+    assert "discretising the layered model on the GPU (method %s)" % method in r.stdout
+    np.testing.assert_array_equal(outs[1].view(np.int32), outs[0].view(np.int32))
+
+
 @pytest.mark.gpu
 def test_device_grid_matches_reference():
     """loc on the device in the reference's float order (--fmad=false, no
