@@ -447,3 +447,80 @@ extern "C" int __wrap_media_layer2model_el_aniso(
     for (size_t i = 0; i < vol; i++) zero[n][i] = 0.0;
   return 0;
 }
+
+extern "C" int __real_media_grid2model_el_aniso(
+    float *rho, float *c11, float *c12, float *c13, float *c14, float *c15, float *c16,
+    float *c22, float *c23, float *c24, float *c25, float *c26, float *c33, float *c34, float *c35,
+    float *c36, float *c44, float *c45, float *c46, float *c55, float *c56, float *c66,
+    const float *x3d, const float *y3d, const float *z3d, int nx, int ny, int nz, float Xmin,
+    float Xmax, float Ymin, float Ymax, int grid_type, const char *in_media_file,
+    const char *equivalent_medium_method, int myid);
+
+/* media_grid2model_el_aniso for elastic isotropic and VTI grid models with
+ * "loc" (media/media_grid2model.cpp:250-395): the device discretisation,
+ * then the reference's spreading into the 21 constants. */
+extern "C" int __wrap_media_grid2model_el_aniso(
+    float *rho, float *c11, float *c12, float *c13, float *c14, float *c15, float *c16,
+    float *c22, float *c23, float *c24, float *c25, float *c26, float *c33, float *c34, float *c35,
+    float *c36, float *c44, float *c45, float *c46, float *c55, float *c56, float *c66,
+    const float *x3d, const float *y3d, const float *z3d, int nx, int ny, int nz, float Xmin,
+    float Xmax, float Ymin, float Ymax, int grid_type, const char *in_media_file,
+    const char *equivalent_medium_method, int myid)
+{
+  const char *m = equivalent_medium_method;
+  if (!lay_ours(grid_type, m, nx, ny, nz) || strcmp(m, "loc") != 0)
+    return __real_media_grid2model_el_aniso(rho, c11, c12, c13, c14, c15, c16, c22, c23, c24,
+                                            c25, c26, c33, c34, c35, c36, c44, c45, c46, c55,
+                                            c56, c66, x3d, y3d, z3d, nx, ny, nz, Xmin, Xmax,
+                                            Ymin, Ymax, grid_type, in_media_file, m, myid);
+  int NL = 0;
+  std::vector<int> NGz;
+  inter_t it;
+  read_grid_file(in_media_file, Xmin, Xmax, Ymin, Ymax, NL, NGz, &it);
+  const int t = it.media_type;
+  const size_t vol = (size_t)nx * ny * nz;
+  if (t == ELASTIC_ISOTROPIC) {
+    const float *cols[4] = {it.elevation, it.rho, it.vp, it.vs};
+    const std::vector<float> rec = lay_interleave(it, cols, 4);
+    if (myid == 0) fprintf(stdout, "discretising the grid model on the GPU (method %s)\n", m);
+    /* lambda into c13, mu into c44, as the reference's isotropic branch */
+    if (cgfd_media_grid_el_iso((int)it.NI, NL, NGz.data(), (int)it.NX, (int)it.NY, it.MINX,
+                               it.MINY, it.DX, it.DY, rec.data(), nx, ny, nz, x3d, y3d, z3d, m,
+                               rho, c13, c44))
+      lay_fail(in_media_file);
+    for (size_t i = 0; i < vol; ++i) {
+      c11[i] = c13[i] + 2.0 * c44[i];
+      c22[i] = c11[i]; c33[i] = c11[i];
+      c12[i] = c13[i]; c23[i] = c13[i];
+      c55[i] = c44[i]; c66[i] = c44[i];
+    }
+  } else if (t == ELASTIC_VTI_PREM || t == ELASTIC_VTI_THOMSEN || t == ELASTIC_VTI_CIJ) {
+    const float *cols[7] = {it.elevation};
+    const float *q[3][6] = {{it.rho, it.vph, it.vpv, it.vsh, it.vsv, it.eta},
+                            {it.rho, it.vp0, it.vs0, it.epsilon, it.delta, it.gamma},
+                            {it.rho, it.c11, it.c33, it.c55, it.c66, it.c13}};
+    const int k = t == ELASTIC_VTI_PREM ? 0 : t == ELASTIC_VTI_THOMSEN ? 1 : 2;
+    for (int c = 0; c < 6; c++) cols[1 + c] = q[k][c];
+    const std::vector<float> rec = lay_interleave(it, cols, 7);
+    if (myid == 0) fprintf(stdout, "discretising the grid model on the GPU (method %s)\n", m);
+    if (cgfd_media_grid_el_vti(t, (int)it.NI, NL, NGz.data(), (int)it.NX, (int)it.NY, it.MINX,
+                               it.MINY, it.DX, it.DY, rec.data(), nx, ny, nz, x3d, y3d, z3d, m,
+                               c11, c33, c55, c66, c13, rho))
+      lay_fail(in_media_file);
+    for (size_t i = 0; i < vol; i++) {
+      c12[i] = c11[i] - 2.0 * c66[i];
+      c22[i] = c11[i];
+      c23[i] = c13[i];
+      c44[i] = c55[i];
+    }
+  } else {
+    return __real_media_grid2model_el_aniso(rho, c11, c12, c13, c14, c15, c16, c22, c23, c24,
+                                            c25, c26, c33, c34, c35, c36, c44, c45, c46, c55,
+                                            c56, c66, x3d, y3d, z3d, nx, ny, nz, Xmin, Xmax,
+                                            Ymin, Ymax, grid_type, in_media_file, m, myid);
+  }
+  float *zero[12] = {c14, c24, c34, c15, c25, c35, c16, c26, c36, c45, c46, c56};
+  for (int n = 0; n < 12; n++)
+    for (size_t i = 0; i < vol; i++) zero[n][i] = 0.0;
+  return 0;
+}

@@ -60,6 +60,11 @@
  *       (media/media_layer2model.cpp:249-420); <output>: float rho, c11,
  *       c12, ..., c66 (the 21 in the reference's argument order) [nz][ny][nx]
  *
+ *   ref_probe grid_aniso <md3grd> <grid> <method> <ext> <output>
+ *       a 3-D grid model through media_grid2model_el_aniso
+ *       (media/media_grid2model.cpp:250-420); <output>: the 22 volumes as
+ *       layer_aniso
+ *
  *   ref_probe bin <grid> <params> <rho> <vp> <vs> <output>
  *   ref_probe bin_vis <grid> <params> <Qp> <Qs> <output>
  *       a model given as binary volumes interpolated on a curvilinear grid
@@ -120,6 +125,14 @@ int media_layer2model_el_aniso(float *rho, float *c11, float *c12, float *c13, f
                                const float *z3d, size_t nx, size_t ny, size_t nz, int grid_type,
                                const char *in_3lay_file, const char *equivalent_medium_method,
                                int myid);
+int media_grid2model_el_aniso(float *rho, float *c11, float *c12, float *c13, float *c14,
+                              float *c15, float *c16, float *c22, float *c23, float *c24,
+                              float *c25, float *c26, float *c33, float *c34, float *c35,
+                              float *c36, float *c44, float *c45, float *c46, float *c55,
+                              float *c56, float *c66, const float *x3d, const float *y3d,
+                              const float *z3d, int nx, int ny, int nz, float Xmin, float Xmax,
+                              float Ymin, float Ymax, int grid_type, const char *in_media_file,
+                              const char *equivalent_medium_method, int myid);
 #define PROBE_GRID_CURV 3
 
 static void rd(void *p, size_t n, FILE *fp)
@@ -439,6 +452,37 @@ static int probe_layer_aniso(const char *lay, const char *grid, const char *meth
   return 0;
 }
 
+static int probe_grid_aniso(const char *grd, const char *grid, const char *method,
+                            const char *extf, const char *out)
+{
+  FILE *fp = fopen(grid, "rb");
+  if (!fp) return 2;
+  int d[3];
+  rd(d, sizeof d, fp);
+  size_t vol = (size_t)d[0] * d[1] * d[2];
+  float *x = malloc(vol * 4), *y = malloc(vol * 4), *z = malloc(vol * 4);
+  rd(x, vol * 4, fp);
+  rd(y, vol * 4, fp);
+  rd(z, vol * 4, fp);
+  fclose(fp);
+  float ext[4];
+  fp = fopen(extf, "rb");
+  if (!fp) return 2;
+  rd(ext, sizeof ext, fp);
+  fclose(fp);
+  float *c[22];
+  for (int n = 0; n < 22; n++) c[n] = calloc(vol, 4);
+  media_grid2model_el_aniso(c[0], c[1], c[2], c[3], c[4], c[5], c[6], c[7], c[8], c[9], c[10],
+                            c[11], c[12], c[13], c[14], c[15], c[16], c[17], c[18], c[19],
+                            c[20], c[21], x, y, z, d[0], d[1], d[2], ext[0], ext[1], ext[2],
+                            ext[3], PROBE_GRID_CURV, grd, method, 0);
+  FILE *fo = fopen(out, "wb");
+  if (!fo) return 2;
+  for (int n = 0; n < 22; n++) fwrite(c[n], 4, vol, fo);
+  fclose(fo);
+  return 0;
+}
+
 int main(int argc, char **argv)
 {
   if (argc == 4 && strcmp(argv[1], "sac") == 0) return probe_sac(argv[2], argv[3]);
@@ -451,6 +495,8 @@ int main(int argc, char **argv)
     return probe_layer_one(argv[2], argv[3], argv[4], argv[5]);
   if (argc == 6 && strcmp(argv[1], "layer_aniso") == 0)
     return probe_layer_aniso(argv[2], argv[3], argv[4], argv[5]);
+  if (argc == 7 && strcmp(argv[1], "grid_aniso") == 0)
+    return probe_grid_aniso(argv[2], argv[3], argv[4], argv[5], argv[6]);
   if (argc == 7 && strcmp(argv[1], "grid") == 0)
     return probe_grid(0, argv[2], argv[3], argv[4], argv[5], argv[6]);
   if (argc == 7 && strcmp(argv[1], "grid_vti") == 0)

@@ -32,7 +32,8 @@ def test_reference_main_links_against_gpu_library():
     assert " T sv_curv_col_el_iso_onestage" in syms  # the rest of the reference
     # the layered-media discretisation: main's call is wrapped by the adapter
     for fn in ("media_layer2model_el_iso", "media_layer2model_el_vti", "media_layer2model_el_aniso",
-               "media_grid2model_el_iso", "media_grid2model_el_vti", "media_bin2model_el_iso",
+               "media_grid2model_el_iso", "media_grid2model_el_vti", "media_grid2model_el_aniso",
+               "media_bin2model_el_iso",
                "media_bin2model_vis_iso"):
         assert " T __wrap_" + fn in syms
     for fn in ("cgfd_media_layer_el_iso", "cgfd_media_layer_el_vti", "cgfd_media_grid_el_iso",

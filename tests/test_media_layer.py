@@ -437,6 +437,43 @@ def test_dropin_adapter_aniso_inside_reference(case, tmp_path):
     np.testing.assert_array_equal(outs[1].view(np.int32), outs[0].view(np.int32))
 
 
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
+                    reason="reference tree not present")
+@pytest.mark.parametrize("kind", ["elastic_isotropic", "elastic_vti_prem"])
+def test_dropin_adapter_grid_aniso_inside_reference(kind, tmp_path):
+    """media_grid2model_el_aniso for isotropic and VTI grid models with loc:
+    the adapter's build against the unmodified reference, 22 volumes bit for
+    bit."""
+    import subprocess
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8", "REF=" + REF,
+                    "_ref/ref_probe", "_ref/ref_probe_media"], check=True, capture_output=True)
+    if kind == "elastic_isotropic":
+        z, g, _ = _grid()
+        text = bytes(z["md3grd"])
+    else:
+        z, g, _ = _grid_vti(kind)
+        text = bytes(z[kind + "_md3grd"])
+    grd = tmp_path / "model.md3grd"
+    grd.write_bytes(text)
+    nz, ny, nx = g["x3d"].shape
+    grid = tmp_path / "grid.bin"
+    with open(grid, "wb") as f:
+        f.write(np.array([nx, ny, nz], "<i4").tobytes())
+        for a in (g["x3d"], g["y3d"], g["z3d"]):
+            f.write(np.ascontiguousarray(a, "<f4").tobytes())
+    ext = tmp_path / "ext.bin"
+    np.ascontiguousarray(z["ext"], "<f4").tofile(ext)
+    outs = []
+    for exe in ("ref_probe", "ref_probe_media"):
+        out = tmp_path / (exe + ".bin")
+        r = subprocess.run([os.path.join(REPO, "oracle", "_ref", exe), "grid_aniso", str(grd),
+                            str(grid), "loc", str(ext), str(out)], capture_output=True,
+                           text=True, check=True)
+        outs.append(np.fromfile(out, "<f4").reshape(22, nz, ny, nx))
+    assert "discretising the grid model on the GPU (method loc)" in r.stdout
+    np.testing.assert_array_equal(outs[1].view(np.int32), outs[0].view(np.int32))
+
+
 @pytest.mark.gpu
 def test_device_grid_matches_reference():
     """loc on the device in the reference's float order (--fmad=false, no
