@@ -46,6 +46,7 @@ WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "slices": dict(ni=400, nj=400, nk=200),
              "locate": dict(ni=400, nj=400, nk=200),
              "media": dict(ni=400, nj=400, nk=200),
+             "media_bin": dict(ni=400, nj=400, nk=200),
              "batch": dict(ni=400, nj=400, nk=200),
              "vti": dict(ni=300, nj=300, nk=150),
              "aniso": dict(ni=300, nj=300, nk=150),
@@ -314,6 +315,8 @@ def run_reference(args):
         return run_locate(args, reference=True)
     if args.workload == "media":
         return run_media(args, reference=True)
+    if args.workload == "media_bin":
+        return run_media_bin(args, reference=True)
     threads = os.cpu_count() or 1
     # warm-up sample, then the timed samples (one RK4 step each)
     cpu_rate(args, 1, threads)
@@ -844,6 +847,85 @@ def run_media(args, reference=False):
     return 0
 
 
+def run_media_bin(args, reference=False):
+    """A model given as binary volumes (rho, vp, vs; 161 x 161 x 80 samples,
+    stored z fastest, z decreasing) interpolated onto the topography grid,
+    grid points per second (host coordinates and volumes in, host rho,
+    lambda, mu out)."""
+    import numpy as np
+    from types import SimpleNamespace
+    from cgfd3d_gb300 import models
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    shp = (args.nk + 6, args.nj + 6, args.ni + 6)
+    X, Y, Z = [a.reshape(shp) for a in
+               models._coords_of(SimpleNamespace(ni=args.ni, nj=args.nj, nk=args.nk), 2024)]
+    npts = X.size
+    ext = (float(X.min()), float(X.max()), float(Y.min()), float(Y.max()))
+    nxb, nyb, nzb = 161, 161, 80
+    dx = (ext[1] - ext[0] + 400.0) / (nxb - 1)
+    dy = (ext[3] - ext[2] + 400.0) / (nyb - 1)
+    z0, dz = float(Z.max()) + 100.0, -(float(Z.max()) - float(Z.min()) + 200.0) / (nzb - 1)
+    order, size = (2, 0, 1), (nzb, nxb, nyb)
+    spacing, origin = (dz, dx, dy), (z0, ext[0] - 200.0, ext[2] - 200.0)
+    rng = np.random.default_rng(31)
+    depth = np.clip(-(z0 + dz * np.arange(nzb)), 0, None)[None, None, :]
+    base = np.ones((nyb, nxb, 1), np.float32)
+    vols = [(b + g * depth + a * rng.standard_normal((nyb, nxb, nzb))).astype(np.float32)
+            * base for b, g, a in ((2200.0, 0.05, 20.0), (3600.0, 0.12, 60.0),
+                                   (2000.0, 0.07, 30.0))]
+    line = {"metric": "grid points discretised/s", "unit": "points/s", "n_gpus": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": "binary-volume model 161x161x80 (rho, vp, vs) onto the "
+                       "topography grid %dx%dx%d (padded), trilinear"
+                       % (args.ni, args.nj, args.nk), "parallelism": "single"}}
+    if reference or not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+        m = dict(order=np.array(order, np.int32), size=np.array(size, np.int32),
+                 spacing=np.array(spacing, np.float32), origin=np.array(origin, np.float32),
+                 ext=np.array(ext, np.float32), rho_vol=vols[0], vp_vol=vols[1], vs_vol=vols[2])
+        kk = 16                                 # a slab of 16 k-planes
+        t0 = time.perf_counter()
+        oracle.bin_model(m, X[:kk], Y[:kk], Z[:kk])
+        tc = time.perf_counter() - t0
+        cpu = {"value": X[:kk].size / tc, "unit": "points/s", "cores": 1, "kind": "port",
+               "sample": "%d k-planes (%d points), C oracle port, 1 thread, %.2f s"
+                         % (kk, X[:kk].size, tc)}
+    if reference:
+        line.update({"impl": "reference", "value": cpu["value"], "steps": 1, "warmup": 0,
+                     "ms_per_step": 1e3 * npts / cpu["value"], "cpu_baseline": cpu,
+                     "e2e": {"value": cpu["value"], "unit": "points/s",
+                             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        print(json.dumps(line), flush=True)
+        return 0
+    import torch
+    torch.cuda.set_device(local)
+    from cgfd3d_gb300 import media
+    lay = media.BinModel.of(order, size, spacing, origin)
+    for _ in range(max(args.warmup, 0)):
+        media.bin_model(lay, ext, vols, X, Y, Z)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        media.bin_model(lay, ext, vols, X, Y, Z)
+        ts.append(time.perf_counter() - t0)
+    t = sorted(ts)[len(ts) // 2]
+    line.update({"value": npts / t, "steps": args.steps, "warmup": args.warmup,
+                 "ms_per_step": 1e3 * t,
+                 "e2e": {"value": npts / t, "unit": "points/s",
+                         "h2d_bytes_per_step": 3 * npts * 4 + 3 * vols[0].nbytes,
+                         "d2h_bytes_per_step": 3 * npts * 4,
+                         "how": "host coordinates and volumes to host media, median of K calls"},
+                 "gpu_launches": args.steps})
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -856,6 +938,8 @@ def main():
         return run_locate(args)
     if args.workload == "media":
         return run_media(args)
+    if args.workload == "media_bin":
+        return run_media_bin(args)
     return run_ours(args)
 
 
