@@ -74,7 +74,34 @@ __global__ void k_nf_final(const int *part, int nb, int *out)
 }
 
 static std::mutex g_na_mutex;
-static int *g_na_ptr[64];          /* device address of g_nf_scratch per device */
+#define NA_MAX_DEVICES 64
+/* device address of g_nf_scratch per device, with the context it was looked
+ * up in: the module (and so the array) is loaded per context, and a
+ * cudaDeviceReset or another current context on the same device loads it
+ * at a new address, so a cached address is used only while the context it
+ * belongs to is the current one */
+static int *g_na_ptr[NA_MAX_DEVICES];
+static void *g_na_ctx[NA_MAX_DEVICES];
+
+/* the calling thread's current context (a CUcontext), or null */
+static void *na_current_context(void)
+{
+  typedef int (*get_ctx_t)(void **);
+  static get_ctx_t fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (get_ctx_t)p;
+    looked = true;
+  }
+  void *ctx = nullptr;
+  if (fn && fn(&ctx) != 0) ctx = nullptr;
+  return ctx;
+}
 
 extern "C" int cgfd_check_finite_noalloc(const float *d_data, size_t n,
                                          int *nonfinite)
@@ -90,17 +117,26 @@ extern "C" int cgfd_check_finite_noalloc(const float *d_data, size_t n,
                   n, (unsigned long long)CGFD_NOALLOC_MAX_FLOATS, CGFD_NOALLOC_MAX_BLOCKS);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 64)
+  if (e != cudaSuccess)
     return na_err(CGFD_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= NA_MAX_DEVICES)
+    return na_err(CGFD_EINVAL,
+                  "cgfd_check_finite_noalloc: device index %d is beyond the %d devices "
+                  "this entry point keeps scratch addresses for",
+                  dev, NA_MAX_DEVICES);
   int *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_ptr[dev]) {
+    /* the first call in a context (after cudaSetDevice makes it current,
+     * or after a reset) looks the address up; later calls reuse it */
+    void *ctx = na_current_context();
+    if (!g_na_ptr[dev] || !ctx || ctx != g_na_ctx[dev]) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_nf_scratch);
       if (e != cudaSuccess || !p)
         return na_err(CGFD_ECUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
       g_na_ptr[dev] = (int *)p;
+      g_na_ctx[dev] = na_current_context();
     }
     scratch = g_na_ptr[dev];
   }

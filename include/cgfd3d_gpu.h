@@ -12,8 +12,8 @@
  *
  *   1. the drop-in `drv_rk_curv_col_allstep` itself, built from
  *      cgfd3d_gb300/csrc/dropin/drv_rk_curv_col_gpu.c against the reference's
- *      own struct headers; it unpacks the reference
- *      structs into a cgfd_problem_t and calls cgfd_allstep();
+ *      own struct headers; it unpacks the reference structs into a
+ *      cgfd_problem_t and calls cgfd_allstep();
  *   2. the flat C ABI below: plain pointers and sizes, no reference types,
  *      so any FFI (ctypes, cgo, JNI) can bind it.
  *
@@ -492,10 +492,15 @@ void cgfd_batch_destroy(cgfd_batch_t *b);
  * d_data is NaN or Inf, else 0.  Scratch: a file-scope __device__ array of
  * CGFD_NOALLOC_MAX_BLOCKS + 1 ints that every GPU loading this library keeps
  * until exit; n above CGFD_NOALLOC_MAX_FLOATS is rejected (CGFD_EINVAL).
- * The first call on a device looks the scratch address up and should come
- * before any stream capture; calls that overlap on the GPU race on the
- * shared scratch.  Runs on the legacy default stream and returns after the
- * result is on the host. */
+ * The first call in a device's context looks the scratch address up (again
+ * after a cudaDeviceReset or when another context of the device is current)
+ * and should come before any stream capture; calls that overlap on the GPU
+ * race on the shared scratch.  Runs on the legacy default stream and
+ * returns after the result is on the host.  The legacy default stream is
+ * not ordered against the solver's own non-blocking stream: a caller that
+ * checks arrays a solver is still writing (cgfd_solver_run_async) must wait
+ * for that solver's work first (cgfd_solver_fetch_* or a device
+ * synchronisation). */
 #define CGFD_NOALLOC_MAX_BLOCKS 65536
 #define CGFD_NOALLOC_MAX_FLOATS (65536ull * 256ull * 64ull)
 int cgfd_check_finite_noalloc(const float *d_data, size_t n, int *nonfinite);

@@ -83,6 +83,122 @@ def allstep(problem, timg_mode=TIMG_ZERO, nthreads=1, want_mats=False,
     return mats if want_mats else None
 
 
+# ---------------------------------------------------------------------------
+# double-precision build of the same time loop (cgfd_oracle_f64.c)
+# ---------------------------------------------------------------------------
+
+LIB64 = os.path.join(HERE, "_build", "libcgfd_oracle_f64.so")
+
+
+def build64(force=False):
+    """Compile the double-precision instantiation of the oracle."""
+    srcs = [os.path.join(HERE, f) for f in ("cgfd_oracle_f64.c", "cgfd_oracle.c")]
+    if (not force and os.path.exists(LIB64)
+            and os.path.getmtime(LIB64) >= max(os.path.getmtime(s) for s in srcs)):
+        return LIB64
+    os.makedirs(os.path.dirname(LIB64), exist_ok=True)
+    subprocess.run(["gcc", "-O3", "-ffp-contract=off", "-fPIC", "-shared",
+                    "-I" + os.path.join(REPO, "include"), "-I" + HERE, "-o", LIB64,
+                    srcs[0], "-lpthread", "-lm"], check=True)
+    return LIB64
+
+
+_lib64 = None
+_wide = {}
+
+
+def _widen(t):
+    """The ctypes type of `t` with every float (and pointer to float) made
+    double, as cgfd_oracle_f64.c sees the problem description."""
+    if t is C.c_float:
+        return C.c_double
+    if isinstance(t, type) and issubclass(t, C._Pointer) and t._type_ is C.c_float:
+        return C.POINTER(C.c_double)
+    if isinstance(t, type) and issubclass(t, C.Array):
+        return _widen(t._type_) * t._length_
+    if isinstance(t, type) and issubclass(t, C.Structure):
+        if t not in _wide:
+            _wide[t] = type(t.__name__ + "64", (C.Structure,),
+                            {"_fields_": [(n, _widen(ft)) for n, ft in t._fields_]})
+        return _wide[t]
+    return t
+
+
+def _copy_wide(src, dst):
+    for name, ft in type(src)._fields_:
+        v = getattr(src, name)
+        wt = dict(type(dst)._fields_)[name]
+        if isinstance(ft, type) and issubclass(ft, C.Structure):
+            _copy_wide(v, getattr(dst, name))
+        elif isinstance(ft, type) and issubclass(ft, C.Array):
+            _copy_array(v, getattr(dst, name), ft)
+        elif isinstance(ft, type) and issubclass(ft, C._Pointer) and ft._type_ is C.c_float:
+            setattr(dst, name, C.cast(v, wt))
+        else:
+            setattr(dst, name, v)
+
+
+def _copy_array(src, dst, ft):
+    et = ft._type_
+    for n in range(ft._length_):
+        if isinstance(et, type) and issubclass(et, C.Structure):
+            _copy_wide(src[n], dst[n])
+        elif isinstance(et, type) and issubclass(et, C.Array):
+            _copy_array(src[n], dst[n], et)
+        elif isinstance(et, type) and issubclass(et, C._Pointer) and et._type_ is C.c_float:
+            dst[n] = C.cast(src[n], C.POINTER(C.c_double))
+        else:
+            dst[n] = src[n]
+
+
+def _as_f64(obj):
+    """Deep copy of a problem's containers with every float32 array as a
+    float64 array (ints and scalars unchanged)."""
+    import numpy as np
+    if isinstance(obj, np.ndarray):
+        return obj.astype(np.float64) if obj.dtype == np.float32 else obj
+    if isinstance(obj, dict):
+        return {k: _as_f64(v) for k, v in obj.items()}
+    if isinstance(obj, list):
+        return [_as_f64(v) for v in obj]
+    return obj
+
+
+def widen_problem(problem):
+    """A copy of a cgfd3d_gb300.problem.Problem whose float32 arrays are
+    float64 (the inputs as the FP32 runs read them, exactly)."""
+    q = problem.copy()
+    for k, v in list(q.__dict__.items()):
+        q.__dict__[k] = _as_f64(v)
+    return q
+
+
+def allstep64(problem, timg_mode=TIMG_ZERO, nthreads=1):
+    """Run the double-precision oracle on a copy of `problem` (float32
+    inputs widened exactly to float64).  Returns the widened problem, whose
+    wavefield, PML auxiliaries and seismograms then hold the FP64 results
+    (problem.level(problem.final_level()) etc.)."""
+    import numpy as np
+    global _lib64
+    if _lib64 is None:
+        _lib64 = C.CDLL(build64())
+        _lib64.oracle_allstep_pg.restype = C.c_int
+        _lib64.oracle_allstep_pg.argtypes = [C.c_void_p, C.c_int, C.c_int,
+                                             C.c_void_p, C.c_void_p, C.c_void_p,
+                                             C.c_void_p]
+    q = widen_problem(problem)
+    cs = q.to_c()                      # float-typed pointers to double data
+    cw = _widen(type(cs))()
+    _copy_wide(cs, cw)
+    cw._keep = cs._keep
+    mats = [np.zeros(q.nx * q.ny * 9, np.float64) for _ in range(3)] if q.free_top else None
+    ptrs = [m.ctypes.data for m in mats] if mats else [None, None, None]
+    rc = _lib64.oracle_allstep_pg(C.addressof(cw), timg_mode, nthreads, *ptrs, None)
+    if rc != 0:
+        raise RuntimeError("oracle_allstep (double) failed with code %d" % rc)
+    return q
+
+
 def surface_matrices(problem):
     """Free-surface matrices of the problem's medium, as the oracle computes
     them before the time loop: dict of matVx2Vz2, matVy2Vz2, matF2Vz2 and,

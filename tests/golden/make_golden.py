@@ -16,7 +16,9 @@ boundary branch is exercised from the first step.
 This script needs the reference tree and runs only where it exists; the
 fixtures it writes are committed and are all the tests need elsewhere.
 
-    python tests/golden/make_golden.py [--ref /root/reference] [case ...]
+    python tests/golden/make_golden.py [--ref <reference tree>] [case ...]
+
+The reference tree defaults to $CGFD_REF_TREE.
 """
 
 import argparse
@@ -243,8 +245,8 @@ def write_par(path, c, work):
     }
     for key, nlay in c["pml"].items():
         par[faces[key]] = {"cfspml": {"number_of_layers": nlay,
-                                      "alpha_max": 3.14, "beta_max": 2.0,
-                                      "ref_vel": 6000.0}}
+                                      "alpha_max": c.get("pml_alpha_max", 3.14),
+                                      "beta_max": 2.0, "ref_vel": 6000.0}}
     for key, nlay in c.get("ablexp", {}).items():
         par[faces[key]] = {"ablexp": {"number_of_layers": nlay, "ref_vel": 6000.0}}
     if c["free"]:
@@ -424,9 +426,11 @@ def run_case(name, c, ref_bin):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CGFD_REF_TREE", ""))
     ap.add_argument("cases", nargs="*")
     a = ap.parse_args()
+    if not a.ref or not os.path.isdir(a.ref):
+        sys.exit("give the reference tree with --ref or $CGFD_REF_TREE")
     subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "-j8",
                     "REF=" + a.ref], check=True, capture_output=True)
     ref_bin = os.path.join(REPO, "oracle", "_ref", "cgfd3d_ref_dump")

@@ -1,6 +1,24 @@
 """Comparison helpers shared by the parity tests."""
 
+import os
+
 import numpy as np
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def ref_tree():
+    """The reference source tree, for the tests that build or read it:
+    $CGFD_REF_TREE, else the tree the oracle's reference build used
+    (oracle/_ref/ref_tree.txt, written by oracle/Makefile); None when
+    neither names an existing directory."""
+    path = os.environ.get("CGFD_REF_TREE", "")
+    if not path:
+        rec = os.path.join(REPO, "oracle", "_ref", "ref_tree.txt")
+        if os.path.exists(rec):
+            with open(rec) as f:
+                path = f.read().strip()
+    return path if path and os.path.isdir(path) else None
 
 # tolerances of the parity bar: relative L2 and max-abs relative to the peak
 REL_L2 = 1e-5

@@ -14,8 +14,10 @@ import subprocess
 
 import pytest
 
+from helpers import ref_tree
+
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = ref_tree() or ""
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "forward")),

@@ -9,6 +9,8 @@ import sys
 import numpy as np
 import pytest
 
+from helpers import ref_tree
+
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FIX = os.path.join(REPO, "tests", "golden", "media", "layer_el_iso.npz")
 FIX_VTI = os.path.join(REPO, "tests", "golden", "media", "layer_el_vti.npz")
@@ -201,7 +203,7 @@ def test_device_matches_reference(method, sfx):
         media.layer_el_iso(m, x, z["y3d"], z["z3d"], method)
 
 
-REF = "/root/reference"
+REF = ref_tree() or ""
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),

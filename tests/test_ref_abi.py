@@ -15,8 +15,10 @@ import pytest
 
 from cgfd3d_gb300 import refabi
 
+from helpers import ref_tree
+
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = ref_tree() or ""
 
 
 def _fields():
