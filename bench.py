@@ -328,19 +328,28 @@ def run_reference(args):
         rates.append(r)
         tot += t
     rate = args.steps / sum(1.0 / r for r in rates)
+    # the reference itself is single-threaded: the same sample on one thread
+    r1, t1, _ = cpu_rate(args, 1, 1)
+    nk_cut = min(SAMPLE_NK, args.nk)
     sample = ("one RK4 step per timed step of the %s model (same generator, "
               "nk cut to %d), C oracle port, %d threads" %
-              (args.workload, min(SAMPLE_NK, args.nk), threads))
+              (args.workload, nk_cut, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator, no dataset)",
-        "config": {"workload": workload_name(args) + " (CPU sample nk=%d)" %
-                   min(SAMPLE_NK, args.nk)},
+        "config": {"workload": workload_name(args) + (
+            " -- CPU arm: the C port of the reference path (bit-identical to the "
+            "reference build), %d threads, on the model cut to nk=%d (rate per "
+            "point-stage; the reference sources are not on the GPU machine)"
+            % (threads, nk_cut)),
+            "same_config": False},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": sample,
+                         "single_thread": {"value": r1, "unit": UNIT, "cores": 1,
+                                           "seconds": t1}},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }

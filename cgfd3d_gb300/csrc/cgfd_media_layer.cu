@@ -64,16 +64,16 @@ template <int KIND> struct LayKind {
   static constexpr int nout = np;                      /* output volumes */
 };
 
+/* Bounds self-checks of the kernels: an index out of its range records a
+ * code in the call's check word (`chk`, device memory of that call alone)
+ * and the access is skipped; the host reports a non-zero code as an
+ * internal error (1 layer index, 2 listed point, 3 list position). */
 struct LayerMesh {
   int NI, NX, NY, nc;   /* nc: record width, 1 + 3 x properties */
   float MINX, MINY, DX, DY;
   const float *rec;     /* [NI][NY][NX][nc] */
+  int *chk;             /* the call's check word */
 };
-
-/* Bounds self-checks of the kernels: an index out of its range records a
- * code here and the access is skipped; the host reports a non-zero code as
- * an internal error (1 layer index, 2 listed point, 3 list position). */
-__device__ int g_lay_check;
 
 struct LayOut {
   float *v[6];          /* lambda mu rho, or c11 c33 c55 c66 c13 rho */
@@ -116,7 +116,7 @@ __device__ float lay_interp(const LayerMesh &L, const LayW &w, int col, int laye
 {
   if (!w.ok) return FLT_MAX;
   if (layer < 0 || layer >= L.NI || col < 0 || col >= L.nc) {
-    atomicExch(&g_lay_check, 1);
+    atomicExch(L.chk, 1);
     return FLT_MAX;
   }
   const int nc = L.nc;
@@ -341,7 +341,7 @@ __global__ void k_layer_mark(LayerMesh L, int nx, int ny, int nz, const float *_
 /* interior points whose eight cell vertices hold more than one layer (and
  * none -1: NumOfValues, media/media_utility.cpp:610-624) */
 __global__ void k_layer_mixed(int nx, int ny, int nz, const signed char *__restrict__ mat,
-                              long long *list, unsigned long long *count)
+                              long long *list, unsigned long long *count, int *chk)
 {
   const long long vol = (long long)nx * ny * nz, line = nx, sl = (long long)nx * ny;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < vol;
@@ -362,7 +362,7 @@ __global__ void k_layer_mixed(int nx, int ny, int nz, const signed char *__restr
       if (at < (unsigned long long)vol)
         list[at] = q;
       else
-        atomicExch(&g_lay_check, 3);
+        atomicExch(chk, 3);
     }
   }
 }
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(128) k_layer_avg(LayerMesh L, int method, int 
     const long long q = list[w];
     const long long vol = sl * nz;
     if (q < 1 + line + sl || q >= vol) {
-      atomicExch(&g_lay_check, 2);
+      atomicExch(L.chk, 2);
       continue;
     }
     /* the cell's eight half-grid vertices, in the reference's order */
@@ -594,7 +594,7 @@ static void lay_launch(const LayerMesh &L, int meth, int nx, int ny, int nz, siz
   k_layer_loc<KIND><<<152 * 8, 256, 0, st>>>(L, (long long)vol, dx, dy, dz, o, d_bad);
   if (meth) {
     k_layer_mark<<<152 * 8, 256, 0, st>>>(L, nx, ny, nz, dx, dy, dz, dmat);
-    k_layer_mixed<<<152 * 8, 256, 0, st>>>(nx, ny, nz, dmat, dlist, dcount);
+    k_layer_mixed<<<152 * 8, 256, 0, st>>>(nx, ny, nz, dmat, dlist, dcount, L.chk);
     k_layer_avg<KIND><<<152 * 16, 128, 0, st>>>(L, meth, nx, ny, nz, dx, dy, dz, dlist, dcount,
                                                  o, d_bad);
   }
@@ -634,7 +634,9 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   cudaStream_t st = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d, fl * sizeof(float) + extra);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int));
+  /* d_bad[0]: input errors (outside the mesh, vp <= sqrt(2) vs);
+   * d_bad[1]: this call's bounds check word */
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, 2 * sizeof(int));
   float *df = (float *)d;
   float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *drec = df + (3 + nout) * vol;
   LayOut o = {};
@@ -644,17 +646,14 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
   long long *dlist = meth ? (long long *)(d + off) : nullptr;
   unsigned long long *dcount = meth ? (unsigned long long *)(d + off + vol * 8) : nullptr;
   signed char *dmat = meth ? (signed char *)(d + off + vol * 8 + 8) : nullptr;
-  const int zero = 0;
   int check = 0;
-  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_lay_check, &zero, sizeof(int), 0,
-                                                    cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st);
   if (e == cudaSuccess && meth) e = cudaMemsetAsync(dcount, 0, 8, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(drec, rec, nrec * 4, cudaMemcpyHostToDevice, st);
-  const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
+  const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec, d_bad + 1};
   if (e == cudaSuccess) {
     switch (kind) {
       case LAY_ISO:
@@ -675,8 +674,8 @@ static int lay_run(int kind, int NI, int NX, int NY, float MINX, float MINY, flo
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(&check, g_lay_check, sizeof(int), 0,
-                                                      cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&check, d_bad + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   for (int n = 0; n < nout && e == cudaSuccess; n++)
     e = cudaMemcpyAsync(out[n], o.v[n], vol * 4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -764,23 +763,21 @@ static int grd_run(int kind, int NI, int NL, const int *ngz, int NX, int NY, flo
   const size_t fl = (3 + nout) * vol + nrec;
   char *d = nullptr;
   int *d_bad = nullptr, bad = 0, check = 0;
-  const int zero = 0;
   cudaStream_t st = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc((void **)&d, fl * sizeof(float));
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, sizeof(int));
+  /* d_bad[0]: input errors; d_bad[1]: this call's bounds check word */
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_bad, 2 * sizeof(int));
   float *df = (float *)d;
   float *dx = df, *dy = df + vol, *dz = df + 2 * vol, *drec = df + (3 + nout) * vol;
   LayOut o = {};
   for (int n = 0; n < nout; n++) o.v[n] = df + (3 + n) * vol;
-  if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(g_lay_check, &zero, sizeof(int), 0,
-                                                    cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, 2 * sizeof(int), st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(drec, rec, nrec * 4, cudaMemcpyHostToDevice, st);
-  const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec};
+  const LayerMesh L = {NI, NX, NY, nc, MINX, MINY, DX, DY, drec, d_bad + 1};
   if (e == cudaSuccess) {
     switch (kind) {
       case LAY_ISO:
@@ -801,8 +798,8 @@ static int grd_run(int kind, int NI, int NL, const int *ngz, int NX, int NY, flo
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyFromSymbolAsync(&check, g_lay_check, sizeof(int), 0,
-                                                      cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&check, d_bad + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
   for (int n = 0; n < nout && e == cudaSuccess; n++)
     e = cudaMemcpyAsync(out[n], o.v[n], vol * 4, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);

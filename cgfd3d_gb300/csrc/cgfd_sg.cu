@@ -1,0 +1,361 @@
+/*
+ * cgfd_sg.cu -- device kernels of the learned seismogram surrogate around
+ * its matrix products (cgfd_sg_gemm.cu).
+ *
+ * The network (composed in cgfd3d_gb300/surrogate.py) maps a source
+ * position to six sets of receiver Green's functions, one per moment-tensor
+ * component, and contracts them with the moment tensor:
+ *
+ *   features   Fourier features of the normalised position   (k_features)
+ *   encoder    GEMMs with bias + GELU                          (cgfd_sg_gemm)
+ *   decoder    per layer: nearest 2x upsampling and a 5-tap 1-D convolution
+ *              over time, as an im2col gather (k_im2col_up) and a GEMM
+ *   output     G[b, t, k, r] (k: moment component, r: receiver x component)
+ *              u[b, t, r] = sum_k M[b, k] G[b, t, k, r]        (k_contract)
+ *
+ * Training adds the loss and its gradient in the contraction (relative L2
+ * misfit per shot, k_contract_loss), the adjoint of the im2col gather fused
+ * with the GELU derivative (k_col2im_up_gelu), GELU derivative for the
+ * encoder (k_gelu_bwd), column sums for bias gradients, transposes of the
+ * operands of the weight-gradient products, and AdamW on fp32 master
+ * weights with a bf16 copy for the products.  Layouts are row-major,
+ * channels last ([B, T, C]); every kernel is a grid-stride loop.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+
+#include "../../include/cgfd3d_gpu.h"
+
+__attribute__((visibility("hidden"))) int cgfd_set_error_msg(int code, const char *msg);
+
+namespace sg {
+
+typedef __nv_bfloat16 bf16;
+
+static int sg_err(int code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  return cgfd_set_error_msg(code, buf);
+}
+
+static int launched(const char *what)
+{
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return sg_err(CGFD_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+  return 0;
+}
+
+static inline int nblocks(long long n, int threads)
+{
+  long long b = (n + threads - 1) / threads;
+  return (int)(b < 152 * 32 ? (b < 1 ? 1 : b) : 152 * 32);
+}
+
+#define GRID_LOOP(i, n) \
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < (n); \
+       i += (long long)gridDim.x * blockDim.x)
+
+__device__ __forceinline__ float gelu_grad(float x)
+{
+  const float c = 0.7978845608028654f, a = 0.044715f;
+  const float u = c * (x + a * x * x * x);
+  const float t = tanhf(u);
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * c * (1.0f + 3.0f * a * x * x);
+}
+
+/* row b: [x, y, z, sin(pi f x), cos(pi f x) for f = 1..nfreq per coordinate,
+ * zeros] -- nfeat >= 3 + 6 nfreq columns */
+__global__ void k_features(const float *__restrict__ pos, int B, int nfreq, int nfeat,
+                           bf16 *__restrict__ out)
+{
+  GRID_LOOP(i, (long long)B * nfeat)
+  {
+    const int b = (int)(i / nfeat), c = (int)(i % nfeat);
+    float v = 0.0f;
+    if (c < 3) {
+      v = pos[3 * b + c];
+    } else if (c < 3 + 6 * nfreq) {
+      const int r = c - 3, d = r / (2 * nfreq), f = (r % (2 * nfreq)) / 2 + 1;
+      const float a = 3.14159265358979f * (float)f * pos[3 * b + d];
+      v = (r & 1) ? cosf(a) : sinf(a);
+    }
+    out[i] = __float2bfloat16_rn(v);
+  }
+}
+
+/* A[(b, t), (j, c)] = X[b, (t + j - h) / up, c] for 0 <= t + j - h < Tin up,
+ * else 0; h = ks / 2; X [B, Tin, C], A [B Tin up, ks C] */
+__global__ void k_im2col_up(const bf16 *__restrict__ X, int B, int Tin, int C, int up, int ks,
+                            bf16 *__restrict__ A)
+{
+  const int Tout = Tin * up, h = ks / 2;
+  const long long n = (long long)B * Tout * ks * C;
+  GRID_LOOP(i, n)
+  {
+    const int c = (int)(i % C);
+    long long r = i / C;
+    const int j = (int)(r % ks);
+    r /= ks;
+    const int t = (int)(r % Tout), b = (int)(r / Tout);
+    const int tt = t + j - h;
+    A[i] = (tt >= 0 && tt < Tout) ? X[((long long)b * Tin + tt / up) * C + c]
+                                  : __float2bfloat16_rn(0.0f);
+  }
+}
+
+/* adjoint of k_im2col_up, times GELU'(Z): dZ[b, s, c] = GELU'(Z[b, s, c])
+ * sum over (t, j) with (t + j - h) / up = s of dA[(b, t), (j, c)] (Z null:
+ * no GELU factor) */
+__global__ void k_col2im_up_gelu(const bf16 *__restrict__ dA, int B, int Tin, int C, int up,
+                                 int ks, const bf16 *__restrict__ Z, bf16 *__restrict__ dZ)
+{
+  const int Tout = Tin * up, h = ks / 2;
+  GRID_LOOP(i, (long long)B * Tin * C)
+  {
+    const int c = (int)(i % C);
+    const long long r = i / C;
+    const int s = (int)(r % Tin), b = (int)(r / Tin);
+    float acc = 0.0f;
+    for (int tt = s * up; tt < s * up + up; tt++)
+      for (int j = 0; j < ks; j++) {
+        const int t = tt - j + h;
+        if (t < 0 || t >= Tout) continue;
+        acc += __bfloat162float(dA[(((long long)b * Tout + t) * ks + j) * C + c]);
+      }
+    if (Z) acc *= gelu_grad(__bfloat162float(Z[i]));
+    dZ[i] = __float2bfloat16_rn(acc);
+  }
+}
+
+__global__ void k_gelu_bwd(const bf16 *__restrict__ dH, const bf16 *__restrict__ Z, long long n,
+                           bf16 *__restrict__ dZ)
+{
+  GRID_LOOP(i, n)
+  dZ[i] = __float2bfloat16_rn(__bfloat162float(dH[i]) * gelu_grad(__bfloat162float(Z[i])));
+}
+
+/* u[b, t, r] = scale sum_k M[b, k] G[b, t, k, r] for t < T (G holds Tg >= T
+ * steps) */
+__global__ void k_contract(const bf16 *__restrict__ G, const float *__restrict__ M, int B,
+                           int Tg, int T, int R, float scale, float *__restrict__ U)
+{
+  GRID_LOOP(i, (long long)B * T * R)
+  {
+    const int r = (int)(i % R);
+    const long long bt = i / R;
+    const int t = (int)(bt % T), b = (int)(bt / T);
+    const bf16 *g = G + ((long long)b * Tg + t) * 6 * R + r;
+    float u = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) u += M[6 * b + k] * __bfloat162float(g[k * R]);
+    U[i] = scale * u;
+  }
+}
+
+/* Training form of k_contract with the relative L2 misfit: per shot
+ * err[b] += sum (u - Utrue)^2 (err zeroed by the caller), and the gradient of
+ * loss = (1/B) sum_b err_b / norm_b:  dG[b, t, k, r] = M[b, k] scale 2 (u -
+ * Utrue) / (B norm_b), zero for t >= T. */
+__global__ void k_contract_loss(const bf16 *__restrict__ G, const float *__restrict__ M, int B,
+                                int Tg, int T, int R, float scale,
+                                const float *__restrict__ Utrue, const float *__restrict__ norm,
+                                float *__restrict__ err, bf16 *__restrict__ dG)
+{
+  GRID_LOOP(i, (long long)B * Tg * R)
+  {
+    const int r = (int)(i % R);
+    const long long bt = i / R;
+    const int t = (int)(bt % Tg), b = (int)(bt / Tg);
+    const bf16 *g = G + bt * 6 * R + r;
+    bf16 *dg = dG + bt * 6 * R + r;
+    if (t >= T) {
+#pragma unroll
+      for (int k = 0; k < 6; k++) dg[k * R] = __float2bfloat16_rn(0.0f);
+      continue;
+    }
+    float u = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) u += M[6 * b + k] * __bfloat162float(g[k * R]);
+    const float d = scale * u - Utrue[((long long)b * T + t) * R + r];
+    atomicAdd(err + b, d * d);
+    const float du = 2.0f * d * scale / ((float)B * norm[b]);
+#pragma unroll
+    for (int k = 0; k < 6; k++) dg[k * R] = __float2bfloat16_rn(M[6 * b + k] * du);
+  }
+}
+
+/* Y[c, r] = X[r, c] (X rows x cols with row stride ldx; Y row stride ldy) */
+__global__ void k_transpose(const bf16 *__restrict__ X, int rows, int cols, long long ldx,
+                            bf16 *__restrict__ Y, long long ldy)
+{
+  __shared__ bf16 tile[32][33];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    tile[k][threadIdx.x] = (r < rows && c < cols) ? X[(long long)r * ldx + c]
+                                                  : __float2bfloat16_rn(0.0f);
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (c < cols && r < rows) Y[(long long)c * ldy + r] = tile[threadIdx.x][k];
+  }
+}
+
+/* out[c] (+)= sum over rows of X[r, c] (fp32 accumulation) */
+__global__ void k_colsum(const bf16 *__restrict__ X, long long rows, int cols, long long ld,
+                         float *__restrict__ out)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  const long long per = (rows + gridDim.y - 1) / gridDim.y;
+  const long long r0 = blockIdx.y * per, r1 = min(rows, r0 + per);
+  float acc = 0.0f;
+  for (long long r = r0; r < r1; r++) acc += __bfloat162float(X[r * ld + c]);
+  atomicAdd(out + c, acc);
+}
+
+/* AdamW step on fp32 master weights, refreshing their bf16 copy */
+__global__ void k_adamw(float *__restrict__ w, bf16 *__restrict__ w16,
+                        const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                        long long n, float lr, float b1, float b2, float eps, float wd, float c1,
+                        float c2)
+{
+  GRID_LOOP(i, n)
+  {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float upd = (mi / c1) / (sqrtf(vi / c2) + eps);
+    const float wi = w[i] * (1.0f - lr * wd) - lr * upd;
+    w[i] = wi;
+    w16[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+__global__ void k_f32_to_bf16(const float *__restrict__ x, long long n, bf16 *__restrict__ y)
+{
+  GRID_LOOP(i, n) y[i] = __float2bfloat16_rn(x[i]);
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+#define SG_STREAM(s) ((cudaStream_t)(s))
+
+extern "C" int cgfd_sg_features(const float *pos, int B, int nfreq, int nfeat, void *out,
+                                void *stream)
+{
+  if (!pos || !out || B < 1 || nfreq < 0 || nfeat < 3 + 6 * nfreq)
+    return sg_err(CGFD_EINVAL, "sg_features: %d shots, %d frequencies, %d features", B, nfreq,
+                  nfeat);
+  k_features<<<nblocks((long long)B * nfeat, 256), 256, 0, SG_STREAM(stream)>>>(
+      pos, B, nfreq, nfeat, (bf16 *)out);
+  return launched("sg_features");
+}
+
+extern "C" int cgfd_sg_im2col_up(const void *X, int B, int Tin, int C, int up, int ks, void *A,
+                                 void *stream)
+{
+  if (!X || !A || B < 1 || Tin < 1 || C < 1 || up < 1 || ks < 1 || !(ks & 1))
+    return sg_err(CGFD_EINVAL, "sg_im2col_up: B %d T %d C %d up %d ks %d", B, Tin, C, up, ks);
+  const long long n = (long long)B * Tin * up * ks * C;
+  k_im2col_up<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>((const bf16 *)X, B, Tin, C, up,
+                                                               ks, (bf16 *)A);
+  return launched("sg_im2col_up");
+}
+
+extern "C" int cgfd_sg_col2im_up_gelu(const void *dA, int B, int Tin, int C, int up, int ks,
+                                      const void *Z, void *dZ, void *stream)
+{
+  if (!dA || !dZ || B < 1 || Tin < 1 || C < 1 || up < 1 || ks < 1 || !(ks & 1))
+    return sg_err(CGFD_EINVAL, "sg_col2im_up: B %d T %d C %d up %d ks %d", B, Tin, C, up, ks);
+  k_col2im_up_gelu<<<nblocks((long long)B * Tin * C, 256), 256, 0, SG_STREAM(stream)>>>(
+      (const bf16 *)dA, B, Tin, C, up, ks, (const bf16 *)Z, (bf16 *)dZ);
+  return launched("sg_col2im_up");
+}
+
+extern "C" int cgfd_sg_gelu_bwd(const void *dH, const void *Z, long long n, void *dZ,
+                                void *stream)
+{
+  if (!dH || !Z || !dZ || n < 0) return sg_err(CGFD_EINVAL, "sg_gelu_bwd: bad arguments");
+  if (n == 0) return 0;
+  k_gelu_bwd<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>((const bf16 *)dH, (const bf16 *)Z,
+                                                              n, (bf16 *)dZ);
+  return launched("sg_gelu_bwd");
+}
+
+extern "C" int cgfd_sg_contract(const void *G, const float *M, int B, int Tg, int T, int R,
+                                float scale, float *U, void *stream)
+{
+  if (!G || !M || !U || B < 1 || T < 1 || Tg < T || R < 1)
+    return sg_err(CGFD_EINVAL, "sg_contract: B %d Tg %d T %d R %d", B, Tg, T, R);
+  k_contract<<<nblocks((long long)B * T * R, 256), 256, 0, SG_STREAM(stream)>>>(
+      (const bf16 *)G, M, B, Tg, T, R, scale, U);
+  return launched("sg_contract");
+}
+
+extern "C" int cgfd_sg_contract_loss(const void *G, const float *M, int B, int Tg, int T, int R,
+                                     float scale, const float *Utrue, const float *norm,
+                                     float *err, void *dG, void *stream)
+{
+  if (!G || !M || !Utrue || !norm || !err || !dG || B < 1 || T < 1 || Tg < T || R < 1)
+    return sg_err(CGFD_EINVAL, "sg_contract_loss: B %d Tg %d T %d R %d", B, Tg, T, R);
+  k_contract_loss<<<nblocks((long long)B * Tg * R, 256), 256, 0, SG_STREAM(stream)>>>(
+      (const bf16 *)G, M, B, Tg, T, R, scale, Utrue, norm, err, (bf16 *)dG);
+  return launched("sg_contract_loss");
+}
+
+extern "C" int cgfd_sg_transpose(const void *X, int rows, int cols, long long ldx, void *Y,
+                                 long long ldy, void *stream)
+{
+  if (!X || !Y || rows < 1 || cols < 1 || ldx < cols || ldy < rows)
+    return sg_err(CGFD_EINVAL, "sg_transpose: %d x %d (ld %lld, %lld)", rows, cols, ldx, ldy);
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  k_transpose<<<grid, block, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols, ldx,
+                                                     (bf16 *)Y, ldy);
+  return launched("sg_transpose");
+}
+
+extern "C" int cgfd_sg_colsum(const void *X, long long rows, int cols, long long ld, float *out,
+                              void *stream)
+{
+  if (!X || !out || rows < 1 || cols < 1 || ld < cols)
+    return sg_err(CGFD_EINVAL, "sg_colsum: %lld x %d", rows, cols);
+  const int bx = (cols + 127) / 128;
+  long long by = (rows + 511) / 512;
+  if (by > 1024) by = 1024;
+  k_colsum<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols,
+                                                                   ld, out);
+  return launched("sg_colsum");
+}
+
+extern "C" int cgfd_sg_adamw(float *w, void *w16, const float *g, float *m, float *v,
+                             long long n, float lr, float b1, float b2, float eps, float wd,
+                             int step, void *stream)
+{
+  if (!w || !w16 || !g || !m || !v || n < 1 || step < 1)
+    return sg_err(CGFD_EINVAL, "sg_adamw: bad arguments");
+  const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+  k_adamw<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>(w, (bf16 *)w16, g, m, v, n, lr, b1, b2,
+                                                          eps, wd, c1, c2);
+  return launched("sg_adamw");
+}
+
+extern "C" int cgfd_sg_to_bf16(const float *x, long long n, void *y, void *stream)
+{
+  if (!x || !y || n < 0) return sg_err(CGFD_EINVAL, "sg_to_bf16: bad arguments");
+  if (n == 0) return 0;
+  k_f32_to_bf16<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>(x, n, (bf16 *)y);
+  return launched("sg_to_bf16");
+}

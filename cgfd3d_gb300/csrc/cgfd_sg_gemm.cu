@@ -1,0 +1,425 @@
+/*
+ * cgfd_sg_gemm.cu -- BF16 matrix products on the 5th-generation tensor cores
+ * (tcgen05, sm_103a) for the learned seismogram surrogate (cgfd_sg.cu).
+ *
+ *   C[M, N] = alpha * A[M, K] . B[N, K]^T   (+ bias[N], optional GELU)
+ *
+ * A and B are bf16, row-major with K contiguous ("K-major" for both
+ * operands); the product accumulates in FP32 in tensor memory (TMEM).  One
+ * CTA computes one 128 x 128 tile of C (or, split along K, its share of
+ * one), with four warps:
+ *
+ *   warp 0, lane 0   producer: bulk tensor copies (cp.async.bulk.tensor,
+ *                    128-byte swizzle) of the A and B tiles of each 64-wide
+ *                    K block into a 4-stage shared-memory ring;
+ *   warp 1, lane 0   MMA issuer: four tcgen05.mma (M 128, N 128, K 16) per K
+ *                    block, then tcgen05.commit to the stage's `empty`
+ *                    barrier, which frees the stage when those MMAs are done;
+ *   warps 0-3        epilogue: each warp reads its 32 TMEM lanes (rows) with
+ *                    tcgen05.ld, applies alpha, bias and GELU, and stores
+ *                    bf16, fp32, or adds fp32 atomically (split-K partial
+ *                    products of weight gradients).
+ *
+ * Warp 0 allocates the 128 TMEM columns of the accumulator and frees them
+ * at the end.  Every mbarrier wait is bounded: on timeout the thread sets
+ * the error word (a device int the caller reads), the pipeline stops
+ * issuing, and the kernel still drains what it issued, frees TMEM and
+ * returns.  Rows of A or B beyond M, N or K read as zeros (the tensor
+ * maps' out-of-bounds fill); stores are guarded.
+ */
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/cgfd3d_gpu.h"
+
+__attribute__((visibility("hidden"))) int cgfd_set_error_msg(int code, const char *msg);
+
+namespace sgg {
+
+constexpr int BM = 128, BN = 128, BK = 64;   /* BK: one 128-byte swizzle row of bf16 */
+constexpr int STAGES = 4;
+constexpr int TILE_A = BM * BK * 2;          /* 16 KiB */
+constexpr int TILE_B = BN * BK * 2;          /* 16 KiB */
+constexpr int SMEM_BYTES = STAGES * (TILE_A + TILE_B) + 1024;   /* + alignment slack */
+constexpr int NTHREADS = 128;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr int WAIT_LIMIT = 1 << 24;
+
+struct Epi {
+  void *C;
+  long long ldc;
+  __nv_bfloat16 *Z;      /* pre-activation copy (bf16), or null */
+  const float *bias;     /* per column, or null */
+  float alpha;
+  int act;               /* CGFD_SG_ACT_* */
+  int mode;              /* CGFD_SG_OUT_* */
+  int M, N;
+  int *err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t n)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+/* bounded wait: false after `limit` polls (the caller records the error) */
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, int limit)
+{
+  for (int n = 0; n < limit; n++) {
+    if (mbar_try(b, parity)) return true;
+    if (n > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                       uint64_t *bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+/* shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+ * start address (>> 4), leading byte offset 16 B (unused by swizzled
+ * K-major layouts), stride byte offset 1024 B (eight 128-byte rows),
+ * descriptor version 1, layout "128-byte swizzle" (2) */
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
+{
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)(16 >> 4) << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+/* instruction descriptor of kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
+ * (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit
+ * 17, M >> 4 at bit 24 */
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc)
+{
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar)
+{
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+/* 32 consecutive fp32 columns of this warp's 32 TMEM lanes */
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ float gelu(float x)
+{
+  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+  return 0.5f * x * (1.0f + tanhf(u));
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_gemm_tn(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+              Epi e, int K, int kper)
+{
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], accum;
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+  /* 128-byte swizzled tiles sit on 1024-byte boundaries */
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *sA = smem, *sB = smem + STAGES * TILE_A;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kb0 = blockIdx.z * kper;
+  const int kend = min(K, kb0 + kper);
+  const int nkb = kend > kb0 ? (kend - kb0 + BK - 1) / BK : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&accum, 1);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_sh)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_sh;
+
+  if (warp == 0 && lane == 0) {
+    /* producer */
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES) {
+        if (!mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1,
+                       *(volatile int *)&abort_sh ? 64 : WAIT_LIMIT)) {
+          atomicOr(e.err, 1);
+          abort_sh = 1;
+          break;
+        }
+      }
+      if (*(volatile int *)&abort_sh) break;
+      mbar_expect_tx(&full[s], TILE_A + TILE_B);
+      tma_2d(sA + s * TILE_A, &ta, kb0 + kb * BK, m0, &full[s]);
+      tma_2d(sB + s * TILE_B, &tb, kb0 + kb * BK, n0, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    /* MMA issuer: every issued copy is waited for, also after an error */
+    bool ok = true;
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb % STAGES;
+      if (!mbar_wait(&full[s], (kb / STAGES) & 1, ok ? WAIT_LIMIT : 64)) {
+        if (ok) atomicOr(e.err, 2);
+        ok = false;
+        abort_sh = 1;
+        continue;
+      }
+      tc_fence_after();
+      if (ok) {
+        const uint32_t a0 = smem_u32(sA + s * TILE_A), b0 = smem_u32(sB + s * TILE_B);
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; kk++)
+          umma(tmem, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+      }
+      umma_commit(&empty[s]);
+    }
+    umma_commit(&accum);
+  }
+  __syncwarp();
+
+  /* epilogue */
+  bool have = nkb > 0;
+  if (have && !mbar_wait(&accum, 0, WAIT_LIMIT)) {
+    atomicOr(e.err, 4);
+    have = false;
+  }
+  tc_fence_after();
+  __syncwarp();
+  const int row = m0 + warp * 32 + lane;
+  const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+  for (int c0 = 0; c0 < BN; c0 += 32) {
+    uint32_t r[32];
+    tmem_ld32(tl + c0, r);
+    if (!have || row >= e.M) continue;
+    const int col0 = n0 + c0;
+    if (col0 >= e.N) continue;
+    float v[32];
+#pragma unroll
+    for (int t = 0; t < 32; t++) {
+      v[t] = __uint_as_float(r[t]) * e.alpha;
+      if (e.bias && col0 + t < e.N) v[t] += e.bias[col0 + t];
+    }
+    const bool full_row = col0 + 32 <= e.N;
+    if (e.mode == CGFD_SG_OUT_BF16) {
+      __nv_bfloat16 *C = (__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0;
+      __nv_bfloat16 *Z = e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr;
+      __align__(16) __nv_bfloat16 h[32], z[32];
+#pragma unroll
+      for (int t = 0; t < 32; t++) {
+        z[t] = __float2bfloat16_rn(v[t]);
+        h[t] = e.act == CGFD_SG_ACT_GELU ? __float2bfloat16_rn(gelu(v[t])) : z[t];
+      }
+      if (full_row) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          reinterpret_cast<uint4 *>(C)[t] = reinterpret_cast<const uint4 *>(h)[t];
+          if (Z) reinterpret_cast<uint4 *>(Z)[t] = reinterpret_cast<const uint4 *>(z)[t];
+        }
+      } else {
+        for (int t = 0; t < 32 && col0 + t < e.N; t++) {
+          C[t] = h[t];
+          if (Z) Z[t] = z[t];
+        }
+      }
+    } else if (e.mode == CGFD_SG_OUT_F32) {
+      float *C = (float *)e.C + (long long)row * e.ldc + col0;
+      if (full_row) {
+#pragma unroll
+        for (int t = 0; t < 8; t++)
+          reinterpret_cast<float4 *>(C)[t] = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2],
+                                                         v[4 * t + 3]);
+      } else {
+        for (int t = 0; t < 32 && col0 + t < e.N; t++) C[t] = v[t];
+      }
+    } else {
+      float *C = (float *)e.C + (long long)row * e.ldc + col0;
+      for (int t = 0; t < 32 && col0 + t < e.N; t++) atomicAdd(C + t, v[t]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+typedef CUresult (*encode_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                              const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                              const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static encode_fn encoder(void)
+{
+  static encode_fn fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void *p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (encode_fn)p;
+  }
+  return fn;
+}
+
+/* a [rows, K] bf16 operand with row stride ld elements, 64 x 128 boxes */
+static bool operand_map(CUtensorMap *m, const void *p, int rows, int K, long long ld)
+{
+  encode_fn fn = encoder();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {BK, 128};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(p), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static int gemm_err(int code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  return cgfd_set_error_msg(code, buf);
+}
+
+}  // namespace sgg
+
+using namespace sgg;
+
+extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long long ldb, void *C,
+                            long long ldc, int M, int N, int K, float alpha, const float *bias,
+                            int act, int mode, void *Z, int splits, int *d_err, void *stream)
+{
+  if (!A || !B || !C || !d_err || M < 1 || N < 1 || K < 1)
+    return gemm_err(CGFD_EINVAL, "sg_gemm: missing operand or empty product (%d x %d x %d)",
+                    M, N, K);
+  if (K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K || ldc < N ||
+      ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
+    return gemm_err(CGFD_EINVAL, "sg_gemm: K, lda, ldb must be multiples of 8 (16-byte rows) "
+                    "and the operands 16-byte aligned (K %d, lda %lld, ldb %lld)", K, lda, ldb);
+  if (mode != CGFD_SG_OUT_BF16 && mode != CGFD_SG_OUT_F32 && mode != CGFD_SG_OUT_F32_ADD)
+    return gemm_err(CGFD_EINVAL, "sg_gemm: output mode %d", mode);
+  if ((mode == CGFD_SG_OUT_BF16 && (ldc % 8 || ((uintptr_t)C & 15) ||
+                                    (Z && ((uintptr_t)Z & 15)))) ||
+      (mode == CGFD_SG_OUT_F32 && (ldc % 4 || ((uintptr_t)C & 15))))
+    return gemm_err(CGFD_EINVAL, "sg_gemm: output rows must be 16-byte aligned");
+  if (splits < 1) splits = 1;
+  if (splits > 1 && mode != CGFD_SG_OUT_F32_ADD)
+    return gemm_err(CGFD_EINVAL, "sg_gemm: a split product must add into fp32");
+  CUtensorMap ta, tb;
+  if (!operand_map(&ta, A, M, K, lda) || !operand_map(&tb, B, N, K, ldb))
+    return gemm_err(CGFD_ECUDA, "sg_gemm: tensor map encoding failed");
+  const int nkb = (K + BK - 1) / BK;
+  const int kper = ((nkb + splits - 1) / splits) * BK;
+  const int nz = (K + kper - 1) / kper;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             SMEM_BYTES) != cudaSuccess)
+      return gemm_err(CGFD_ECUDA, "sg_gemm: shared memory attribute");
+    attr = true;
+  }
+  Epi e;
+  e.C = C;
+  e.ldc = ldc;
+  e.Z = (__nv_bfloat16 *)Z;
+  e.bias = bias;
+  e.alpha = alpha;
+  e.act = act;
+  e.mode = mode;
+  e.M = M;
+  e.N = N;
+  e.err = d_err;
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nz);
+  k_gemm_tn<<<grid, NTHREADS, SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, kper);
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return gemm_err(CGFD_ECUDA, "sg_gemm launch: %s", cudaGetErrorString(err));
+  return 0;
+}

@@ -483,6 +483,33 @@ cgfd_solver_t *cgfd_batch_shot(cgfd_batch_t *b, int k);
 
 void cgfd_batch_destroy(cgfd_batch_t *b);
 
+/* ------------------------------------------------------------------------
+ * Learned seismogram surrogate (no counterpart in the reference, which runs
+ * the solver for every shot).  Device building blocks of a small network
+ * that predicts receiver seismograms from a source position and moment
+ * tensor, trained on seismograms of the batched solver; the Python layer
+ * (cgfd3d_gb300/surrogate.py) composes them.  All pointers are device
+ * pointers; `stream` is a cudaStream_t (null: the legacy default stream);
+ * d_err is a device int that a bounded wait which ran out sets (non-zero).
+ * ---------------------------------------------------------------------- */
+
+/* output modes and activations of cgfd_sg_gemm */
+#define CGFD_SG_OUT_BF16 0       /* C (and Z) bf16, stored */
+#define CGFD_SG_OUT_F32 1        /* C fp32, stored */
+#define CGFD_SG_OUT_F32_ADD 2    /* C fp32, added atomically (split along K) */
+#define CGFD_SG_ACT_NONE 0
+#define CGFD_SG_ACT_GELU 1       /* tanh-form GELU */
+
+/* C[M, N] = alpha A[M, K] B[N, K]^T (+ bias[N]) on the tcgen05 tensor cores:
+ * A, B bf16 with K contiguous (row strides lda, ldb elements, multiples of
+ * 8, operands 16-byte aligned), FP32 accumulation.  mode CGFD_SG_OUT_BF16
+ * stores act(C) as bf16 and, when Z is not null, the pre-activation C as
+ * bf16 (same ldc); CGFD_SG_OUT_F32 stores fp32; CGFD_SG_OUT_F32_ADD adds
+ * fp32 atomically and may split K over `splits` CTAs. */
+int cgfd_sg_gemm(const void *A, long long lda, const void *B, long long ldb, void *C,
+                 long long ldc, int M, int N, int K, float alpha, const float *bias, int act,
+                 int mode, void *Z, int splits, int *d_err, void *stream);
+
 /* No counterpart in the reference.  NaN/Inf test of a device array the
  * caller owns that allocates no device memory, for callers that cannot call
  * cudaMalloc (a process whose device memory belongs to another framework's

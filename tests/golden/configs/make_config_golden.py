@@ -18,7 +18,11 @@ fixture keeps the inputs (constant volumes compress to almost nothing), the
 line and station seismograms (9 components x 501 samples), and from the
 final wavefield four planes through the source instead of the whole volume:
 the free surface k = nk2, the source plane k = nk2 - 20, and the vertical
-planes j = 53 and i = 53 (padded indices).
+planes j = 53 and i = 53 (padded indices).  A second run of the same case
+with number_of_time_steps = 250 adds the same planes after 251 steps
+(out.t251.plane.*), a snapshot taken while the wavefield still fills the
+model; its seismograms are checked to be the first 251 samples of the long
+run's.
 
 This script needs the reference tree and runs only where it exists:
 
@@ -74,8 +78,9 @@ def planes_of(wav, ncmp, nx, ny, nz):
     return out
 
 
-def run_c0(ref_bin, out_path):
-    c = C0
+def run_reference(c, ref_bin):
+    """One reference run of case c: the trimmed dump (inputs, outputs, the
+    final state as out.wav.final)."""
     work = tempfile.mkdtemp(prefix="cgfd_c0_")
     try:
         os.makedirs(os.path.join(work, "out"))
@@ -91,9 +96,32 @@ def run_c0(ref_bin, out_path):
         if r.returncode != 0:
             sys.stderr.write(r.stdout[-4000:] + r.stderr[-4000:])
             raise RuntimeError("reference run failed")
-        d = make_golden.trim(make_golden.read_dump(os.path.join(work, "dump.bin")))
+        return make_golden.trim(make_golden.read_dump(os.path.join(work, "dump.bin")))
     finally:
         shutil.rmtree(work, ignore_errors=True)
+
+
+def run_c0(ref_bin, out_path):
+    """The 501-step run, plus the planes of a 251-step run of the same case
+    (a snapshot while the wavefield is still strong) as out.t251.plane.*;
+    the shorter run's seismograms must be the prefix of the longer one's."""
+    d = run_reference(C0, ref_bin)
+    mid = run_reference(dict(C0, steps=250), ref_bin)
+    nt = int(mid["nt_total"][0])
+    assert nt == 251
+    g = mid["gd.dims"]
+    nx, ny, nz = int(g[3]), int(g[4]), int(g[5])
+    ncmp = int(mid["wav.ncmp"][0])
+    line = d["out.line.0.seismo"].reshape(-1, ncmp, int(d["line.max_nt"][0]))
+    line_mid = mid["out.line.0.seismo"].reshape(-1, ncmp, nt)
+    assert np.array_equal(line[:, :, :nt], line_mid), "251-step run is not a prefix"
+    for name, v in planes_of(mid["out.wav.final"], ncmp, nx, ny, nz).items():
+        d["out.t251.plane." + name] = v
+    return finish_c0(d, out_path)
+
+
+def finish_c0(d, out_path):
+    c = C0
     g = d["gd.dims"]
     nx, ny, nz = int(g[3]), int(g[4]), int(g[5])
     ncmp = int(d["wav.ncmp"][0])
