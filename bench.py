@@ -51,7 +51,8 @@ WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "vti": dict(ni=300, nj=300, nk=150),
              "aniso": dict(ni=300, nj=300, nk=150),
              "visco": dict(ni=300, nj=300, nk=150),
-             "flat": dict(ni=100, nj=100, nk=60)}
+             "flat": dict(ni=100, nj=100, nk=60),
+             "surrogate": dict(ni=256, nj=256, nk=128)}
 SAMPLE_NK = 24                 # CPU sample: same model, 24 planes deep
 CPU_SAMPLE_S = 24.0            # target seconds of CPU work per baseline sample
 
@@ -68,6 +69,12 @@ def parse():
     ap.add_argument("--workload", default="topo", choices=sorted(WORKLOADS))
     ap.add_argument("--nshot", type=int, default=64,
                     help="batch workload: shots per GPU")
+    ap.add_argument("--sg-train", type=int, default=448,
+                    help="surrogate workload: training shots")
+    ap.add_argument("--sg-test", type=int, default=64,
+                    help="surrogate workload: held-out shots")
+    ap.add_argument("--sg-iters", type=int, default=3000,
+                    help="surrogate workload: training steps (batch 256)")
     ap.add_argument("--ni", type=int, default=None)
     ap.add_argument("--nj", type=int, default=None)
     ap.add_argument("--nk", type=int, default=None)
@@ -935,6 +942,173 @@ def run_media_bin(args, reference=False):
     return 0
 
 
+def measured_peak_bf16():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def run_surrogate(args):
+    """Learned surrogate (config 4).  Shots of the batched solver on the fixed
+    256 x 256 x 128 crop of the topography model (sources uniform in the
+    volume 1-8 km deep, random unit moment tensors, Ricker 2 Hz, 64 surface
+    receivers x 3 components x 1000 samples) train the network; held-out
+    shots score it by relative L2 misfit.  value = surrogate inference
+    shots/s at batch 256 (timed alone, CUDA events); beside it the batched
+    solver's shots/s on the same shots, the held-out misfits, the k-nearest
+    least-squares baseline without the network, and the throughput of the
+    fallback rule (2 solver check shots per 64-shot request, the solver for
+    the whole request when a check misfit exceeds 5 %)."""
+    import numpy as np
+    import torch
+    from cgfd3d_gb300 import models, surrogate as SG
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(0)
+    crop = (args.ni, args.nj, args.nk)
+    t_setup = time.perf_counter()
+    base = models._topo_base(400, 400, 200, 2024)
+    model = SG.crop_model(base, crop)
+    del base
+    ntr, nte = args.sg_train, args.sg_test
+    ijd_tr, M_tr = SG.draw_sources(ntr, crop, seed=41)
+    ijd_te, M_te = SG.draw_sources(nte, crop, seed=43)
+    t_setup = time.perf_counter() - t_setup
+    sampler = ClockSampler(0)
+    sampler.start()
+    U_tr, s_tr = SG.solve_shots(model, ijd_tr, M_tr, steps=1000, batch=64)
+    U_te, s_te = SG.solve_shots(model, ijd_te, M_te, steps=1000, batch=64)
+    solver_rate = (ntr + nte) / (s_tr + s_te)
+    scale = float(np.sqrt((U_tr.astype(np.float64) ** 2).mean()))
+    pos_tr, pos_te = SG.normalise_positions(ijd_tr, crop), SG.normalise_positions(ijd_te, crop)
+    net = SG.Surrogate(nrec=64, nt=1000, seed=1, scale=scale, lr=1e-3, wd=1e-4)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    tp, tM, tU = dev(pos_tr), dev(M_tr), dev(U_tr)
+    tnorm = (tU.double() ** 2).reshape(ntr, -1).sum(1).float()
+    B = min(256, ntr)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    hist = []
+    for it in range(args.sg_iters):
+        idx = torch.randperm(ntr, generator=g, device="cuda")[:B]
+        lr = 1e-5 + 0.5 * (1e-3 - 1e-5) * (1.0 + math.cos(math.pi * it / args.sg_iters))
+        loss_b = net.gradients(tp[idx].contiguous(), tM[idx].contiguous(),
+                               tU[idx].contiguous(), tnorm[idx].contiguous())
+        net.apply(lr)
+        if it % 100 == 0 or it == args.sg_iters - 1:
+            hist.append((it, float(torch.sqrt((loss_b / tnorm[idx]).mean()).item())))
+    e1.record()
+    torch.cuda.synchronize()
+    train_s = e0.elapsed_time(e1) * 1e-3
+    # held-out scoring
+    pred = np.concatenate([net.predict(dev(pos_te[a:a + 256]), dev(M_te[a:a + 256])).cpu().numpy()
+                           for a in range(0, nte, 256)])
+    mis = SG.misfit(pred, U_te)
+    mis_tr = SG.misfit(net.predict(dev(pos_tr[:256]), dev(M_tr[:256])).cpu().numpy(),
+                       U_tr[:256])
+    knn = SG.misfit(SG.knn_green(pos_tr, M_tr, U_tr, pos_te, M_te, k=12), U_te)
+    # inference throughput at batch 256, inputs resident
+    pb = dev(np.resize(pos_te, (256, 3)))
+    mb = dev(np.resize(M_te, (256, 6)))
+    for _ in range(3):
+        net.predict(pb, mb)
+    torch.cuda.synchronize()
+    n0 = net.launches
+    e0.record()
+    reps = max(args.steps, 1)
+    for _ in range(reps):
+        net.predict(pb, mb)
+    e1.record()
+    torch.cuda.synchronize()
+    inf_s = e0.elapsed_time(e1) * 1e-3 / reps
+    launches = (net.launches - n0) // reps
+    rate = 256.0 / inf_s
+    # end to end: host positions and moment tensors in, host seismograms out
+    ph = torch.from_numpy(np.resize(pos_te, (256, 3))).pin_memory()
+    mh = torch.from_numpy(np.resize(M_te, (256, 6))).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = net.predict(ph.cuda(non_blocking=True), mh.cuda(non_blocking=True)).cpu()
+    e2e_s = (time.perf_counter() - t0) / reps
+    # the dominant kernel alone: the last decoder layer's product
+    lay = net.lay
+    d = net._buffers(256, False)
+    o, k = lay.dec[-1]
+    rows = 256 * lay.T
+    for _ in range(2):
+        net._gemm(d["a_d%d" % (len(lay.dec) - 1)], k, net.W(len(lay.layers) - 1), k,
+                  d["h_d%d" % (len(lay.dec) - 1)], o, rows, o, k)
+    e0.record()
+    for _ in range(10):
+        net._gemm(d["a_d%d" % (len(lay.dec) - 1)], k, net.W(len(lay.layers) - 1), k,
+                  d["h_d%d" % (len(lay.dec) - 1)], o, rows, o, k)
+    e1.record()
+    torch.cuda.synchronize()
+    g_ms = e0.elapsed_time(e1) / 10
+    flops = 2.0 * rows * o * k
+    achieved = flops / (g_ms * 1e-3) / 1e12
+    clocks = sampler.stop()
+    peak, peak_kind = measured_peak_bf16()
+    # fallback rule over the held-out shots, 64-shot requests
+    rng = np.random.default_rng(9)
+    per_shot_solver = 1.0 / solver_rate
+    t_rule, n_fb, n_req = 0.0, 0, 0
+    for a in range(0, nte, 64):
+        req = np.arange(a, min(a + 64, nte))
+        chk = rng.choice(req, size=min(2, len(req)), replace=False)
+        t_rule += len(req) / rate + len(chk) * per_shot_solver
+        n_req += 1
+        if mis[chk].max() > 0.05:
+            t_rule += (len(req) - len(chk)) * per_shot_solver
+            n_fb += 1
+    line = {
+        "metric": "surrogate shots/s (batch 256 inference)", "value": rate,
+        "unit": "shots/s", "n_gpus": 1, "steps": reps, "warmup": 3,
+        "ms_per_step": 1e3 * inf_s, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (fp32 accumulation)",
+        "data": "synthetic: shots of the batched solver on the seeded topography model",
+        "config": {"workload": "learned surrogate on the %dx%dx%d crop of the topography "
+                   "model: %d training + %d held-out solver shots, 64 receivers x 3 "
+                   "components x 1000 samples, %d training steps at batch %d"
+                   % (crop + (ntr, nte, args.sg_iters, B)),
+                   "parameters": lay.nparam, "parallelism": "single"},
+        "solver": {"value": solver_rate, "unit": "shots/s",
+                   "how": "batched solver, 64 shots per launch, 1000 steps each",
+                   "seconds": s_tr + s_te},
+        "surrogate_over_solver": rate / solver_rate,
+        "heldout_misfit": {"median": float(np.median(mis)), "mean": float(mis.mean()),
+                           "p90": float(np.percentile(mis, 90)),
+                           "within_5pct": float((mis <= 0.05).mean())},
+        "train_misfit_median": float(np.median(mis_tr)),
+        "knn_baseline_misfit": {"median": float(np.median(knn)), "mean": float(knn.mean()),
+                                "within_5pct": float((knn <= 0.05).mean()),
+                                "how": "12 nearest training shots, least-squares Green's "
+                                       "functions, no network"},
+        "fallback_rule": {"shots_per_s": nte / t_rule, "requests": n_req,
+                          "fell_back": n_fb,
+                          "how": "2 solver check shots per 64-shot request; the solver "
+                                 "for the request when a check misfit exceeds 5 %"},
+        "training": {"seconds": train_s, "steps": args.sg_iters,
+                     "misfit_history": hist},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": None, "kernel": "k_gemm_tn (last decoder layer, "
+                     "%d x %d x %d)" % (rows, o, k), "ms": g_ms},
+        "e2e": {"value": 256.0 / e2e_s, "unit": "shots/s",
+                "h2d_bytes_per_step": 256 * 9 * 4, "d2h_bytes_per_step": int(out.numel()) * 4},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "setup_s": t_setup,
+        "device_error": net.device_error(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -949,6 +1123,8 @@ def main():
         return run_media(args)
     if args.workload == "media_bin":
         return run_media_bin(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
     return run_ours(args)
 
 

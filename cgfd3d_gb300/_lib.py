@@ -40,6 +40,7 @@ def lib():
     L.cgfd_solver_check_finite.argtypes = [vp]
     L.cgfd_solver_kernel_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
     L.cgfd_solver_set_timing.argtypes = [vp, C.c_int]
+    L.cgfd_solver_set_wait_test.argtypes = [vp, C.c_int, C.c_int]
     L.cgfd_solver_transfer_bytes.argtypes = [vp, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     L.cgfd_solver_fetch_pg.argtypes = [vp, vp]
     L.cgfd_solver_fetch_state.argtypes = [vp, vp]
@@ -76,6 +77,11 @@ def lib():
                                         [vp] * 6)
     L.cgfd_media_bin_vis_iso.argtypes = ([vp] + [C.c_float] * 4 + [vp] * 2 + [C.c_int] * 3 +
                                          [vp] * 5)
+    L.cgfd_media_bin_crop.argtypes = [vp] + [C.c_float] * 4 + [C.c_int] * 3 + [vp, vp]
+    L.cgfd_media_bin_el_iso_box.argtypes = ([vp, vp] + [C.c_float] * 4 + [vp] * 3 +
+                                            [C.c_int] * 3 + [vp] * 6)
+    L.cgfd_media_bin_vis_iso_box.argtypes = ([vp, vp] + [C.c_float] * 4 + [vp] * 2 +
+                                             [C.c_int] * 3 + [vp] * 5)
     L.cgfd_locator_destroy.restype = None
     L.cgfd_batch_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
     L.cgfd_batch_run.argtypes = [vp, C.c_int]

@@ -123,6 +123,12 @@ struct StageArgs {
   const int *dd_col;
   const SrcEntry *dd_ent;
   const float *dd_vi, *dd_mij;
+  /* polls of an mbarrier wait before it gives up (records error 1 and the
+   * CTA stops); and, for tests of that path only, a wavefield plane (ring
+   * position of the k march, -1: none) whose copy the first CTA of the grid
+   * does not issue, so that a wait on it runs out */
+  int wait_limit;
+  int test_skip_plane;
 };
 
 /* StageArgs is copied word by word into shared memory by the batched stage

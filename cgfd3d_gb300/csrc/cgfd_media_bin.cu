@@ -8,9 +8,10 @@
  * (media_bin2model_el_iso / media_bin2model_vis_iso,
  * media/media_bin2model.cpp:27-432; TrilinearInterpolation,
  * media/media_utility.cpp:299-391).  Here the host works out the same crop
- * and coordinate vectors, the whole files go to the device as they are
- * stored, and one thread per grid point interpolates each volume through
- * the file's strides, in the reference's float order (--fmad=false);
+ * and coordinate vectors (cgfd_media_bin_crop gives callers the box of the
+ * files it covers, so they can read only that), only the box goes to the
+ * device, and one thread per grid point interpolates each volume through
+ * the box's strides, in the reference's float order (--fmad=false);
  * rho, vp, vs become rho, lambda = vp^2 rho - 2 mu, mu = vs^2 rho.
  */
 #include <cuda_runtime.h>
@@ -20,6 +21,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "../../include/cgfd3d_gpu.h"
@@ -39,9 +41,11 @@ static int bin_err(int code, const char *fmt, ...)
 #define BIN_MAXN 65536   /* samples along an axis of the cropped model */
 
 struct BinCrop {
-  int start[2];          /* first kept x, y sample */
+  int dim[3];            /* file dimension holding x, y, z (host only) */
+  int first[3];          /* first kept x, y, z sample of the files */
+  int start[3];          /* offset of the crop's first sample in the volumes read */
   int n[3];              /* kept samples along x, y, z */
-  long long st[3];       /* file strides of the x, y, z axes */
+  long long st[3];       /* strides of the x, y, z axes in the volumes read */
   const float *xv, *yv, *zv;   /* device coordinate vectors */
 };
 
@@ -73,7 +77,7 @@ __device__ float bin_trilinear(const BinCrop &b, const float *__restrict__ v, fl
   iz2 = iz2 < 0 ? 0 : iz2;
   auto at = [&](int i, int j, int k) {
     return v[(long long)(i + b.start[0]) * b.st[0] + (long long)(j + b.start[1]) * b.st[1] +
-             (long long)k * b.st[2]];
+             (long long)(k + b.start[2]) * b.st[2]];
   };
   if (ix0 == ix2 && iy0 == iy2 && iz0 == iz2) return at(ix0, iy0, iz0);
   const float v000 = at(ix0, iy0, iz0), v002 = at(ix0, iy0, iz2);
@@ -178,8 +182,10 @@ static int bin_setup(const cgfd_bin_model_t *m, float xmin, float xmax, float ym
   const float bzn = bz0 + bdz * (m->size[dim[2]] - 1);
   if (zmin >= std::max(bzn, bz0) || zmax <= std::min(bz0, bzn))
     return bin_err(CGFD_EINVAL, "binary model: the model does not cover the grid in z");
-  b.start[0] = ix_start;
-  b.start[1] = iy_start;
+  for (int d = 0; d < 3; d++) b.dim[d] = dim[d];
+  b.first[0] = ix_start;
+  b.first[1] = iy_start;
+  b.first[2] = 0;
   b.n[0] = ix_end - ix_start + 1;
   b.n[1] = iy_end - iy_start + 1;
   b.n[2] = m->size[dim[2]];
@@ -189,8 +195,6 @@ static int bin_setup(const cgfd_bin_model_t *m, float xmin, float xmax, float ym
     if (b.n[d] < 2 || b.n[d] > BIN_MAXN)
       return bin_err(CGFD_EINVAL, "binary model: %d samples along axis %d after the crop "
                      "(2..%d)", b.n[d], d, BIN_MAXN);
-  const long long fst[3] = {1, (long long)m->size[0], (long long)m->size[0] * m->size[1]};
-  for (int d = 0; d < 3; d++) b.st[d] = fst[dim[d]];
   xv.resize(b.n[0]);
   yv.resize(b.n[1]);
   zv.resize(b.n[2]);
@@ -200,12 +204,27 @@ static int bin_setup(const cgfd_bin_model_t *m, float xmin, float xmax, float ym
   return 0;
 }
 
-static int bin_run(int vis, const cgfd_bin_model_t *m, float xmin, float xmax, float ymin,
-                   float ymax, const float *const *vols, int nx, int ny, int nz,
-                   const float *x3d, const float *y3d, const float *z3d, float *const *out)
+/* the box of the files (per file dimension: first sample, count) that a
+ * crop covers */
+static cgfd_bin_box_t bin_box_of(const BinCrop &b)
+{
+  cgfd_bin_box_t box;
+  for (int d = 0; d < 3; d++) {
+    box.first[b.dim[d]] = b.first[d];
+    box.count[b.dim[d]] = b.n[d];
+  }
+  return box;
+}
+
+/* one call on volumes that hold `box` of the files (count[0] x count[1] x
+ * count[2] floats each, file order): the box must contain the grid's crop */
+static int bin_run_box(int vis, const cgfd_bin_model_t *m, const cgfd_bin_box_t *box,
+                       float xmin, float xmax, float ymin, float ymax, const float *const *vols,
+                       int nx, int ny, int nz, const float *x3d, const float *y3d,
+                       const float *z3d, float *const *out)
 {
   const int nv = vis ? 2 : 3;
-  if (!m || !x3d || !y3d || !z3d || nx < 1 || ny < 1 || nz < 1)
+  if (!m || !box || !x3d || !y3d || !z3d || nx < 1 || ny < 1 || nz < 1)
     return bin_err(CGFD_EINVAL, "binary model: missing argument or empty grid");
   for (int n = 0; n < nv; n++)
     if (!vols[n] || !out[n]) return bin_err(CGFD_EINVAL, "binary model: missing volume");
@@ -214,10 +233,22 @@ static int bin_run(int vis, const cgfd_bin_model_t *m, float xmin, float xmax, f
   std::vector<float> xv, yv, zv;
   const int rc = bin_setup(m, xmin, xmax, ymin, ymax, z3d, vol, b, xv, yv, zv);
   if (rc) return rc;
-  const size_t fvol = (size_t)m->size[0] * m->size[1] * m->size[2];
+  for (int d = 0; d < 3; d++) {
+    const int fd = b.dim[d];
+    if (box->count[fd] < 1 || box->first[fd] < 0 || box->first[fd] > b.first[d] ||
+        box->first[fd] + box->count[fd] < b.first[d] + b.n[d])
+      return bin_err(CGFD_EINVAL, "binary model: the volumes' box (file dimension %d: %d + %d) "
+                     "does not hold the crop (%d + %d)", fd, box->first[fd], box->count[fd],
+                     b.first[d], b.n[d]);
+    b.start[d] = b.first[d] - box->first[fd];
+  }
+  const long long bst[3] = {1, (long long)box->count[0],
+                            (long long)box->count[0] * box->count[1]};
+  for (int d = 0; d < 3; d++) b.st[d] = bst[b.dim[d]];
+  const size_t bvol = (size_t)box->count[0] * box->count[1] * box->count[2];
   const size_t nvec = xv.size() + yv.size() + zv.size();
-  /* device: x, y, z, the outputs, the volumes as stored, the vectors */
-  const size_t nfl = (3 + nv) * vol + nv * fvol + nvec;
+  /* device: x, y, z, the outputs, the volumes' boxes, the vectors */
+  const size_t nfl = (3 + nv) * vol + nv * bvol + nvec;
   float *d = nullptr;
   cudaStream_t st = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
@@ -226,14 +257,14 @@ static int bin_run(int vis, const cgfd_bin_model_t *m, float xmin, float xmax, f
   BinVols bv = {};
   for (int n = 0; n < nv; n++) {
     bv.out[n] = d + (3 + n) * vol;
-    bv.v[n] = d + (3 + nv) * vol + n * fvol;
+    bv.v[n] = d + (3 + nv) * vol + n * bvol;
   }
-  float *dvec = d + (3 + nv) * vol + nv * fvol;
+  float *dvec = d + (3 + nv) * vol + nv * bvol;
   if (e == cudaSuccess) e = cudaMemcpyAsync(dx, x3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dy, y3d, vol * 4, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dz, z3d, vol * 4, cudaMemcpyHostToDevice, st);
   for (int n = 0; n < nv && e == cudaSuccess; n++)
-    e = cudaMemcpyAsync((float *)bv.v[n], vols[n], fvol * 4, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync((float *)bv.v[n], vols[n], bvol * 4, cudaMemcpyHostToDevice, st);
   std::vector<float> vec(xv);
   vec.insert(vec.end(), yv.begin(), yv.end());
   vec.insert(vec.end(), zv.begin(), zv.end());
@@ -252,6 +283,78 @@ static int bin_run(int vis, const cgfd_bin_model_t *m, float xmin, float xmax, f
   if (st) cudaStreamDestroy(st);
   if (e != cudaSuccess) return bin_err(CGFD_ECUDA, "binary model: %s", cudaGetErrorString(e));
   return 0;
+}
+
+/* whole files: the crop's box is gathered on the host (one copy per run of
+ * the files' fastest dimension) and only it goes to the device */
+static int bin_run(int vis, const cgfd_bin_model_t *m, float xmin, float xmax, float ymin,
+                   float ymax, const float *const *vols, int nx, int ny, int nz,
+                   const float *x3d, const float *y3d, const float *z3d, float *const *out)
+{
+  const int nv = vis ? 2 : 3;
+  if (!m || !x3d || !y3d || !z3d || nx < 1 || ny < 1 || nz < 1)
+    return bin_err(CGFD_EINVAL, "binary model: missing argument or empty grid");
+  for (int n = 0; n < nv; n++)
+    if (!vols[n] || !out[n]) return bin_err(CGFD_EINVAL, "binary model: missing volume");
+  BinCrop b;
+  std::vector<float> xv, yv, zv;
+  const int rc = bin_setup(m, xmin, xmax, ymin, ymax, z3d, (size_t)nx * ny * nz, b, xv, yv, zv);
+  if (rc) return rc;
+  const cgfd_bin_box_t box = bin_box_of(b);
+  const size_t run = (size_t)box.count[0];
+  const size_t bvol = run * box.count[1] * box.count[2];
+  std::vector<std::vector<float>> boxes(nv, std::vector<float>(bvol));
+  const float *bp[3] = {nullptr, nullptr, nullptr};
+  for (int n = 0; n < nv; n++) {
+    float *dst = boxes[n].data();
+    for (int c2 = 0; c2 < box.count[2]; c2++)
+      for (int c1 = 0; c1 < box.count[1]; c1++) {
+        const size_t src = ((size_t)(box.first[2] + c2) * m->size[1] + box.first[1] + c1) *
+                               m->size[0] + box.first[0];
+        memcpy(dst + ((size_t)c2 * box.count[1] + c1) * run, vols[n] + src, run * 4);
+      }
+    bp[n] = dst;
+  }
+  return bin_run_box(vis, m, &box, xmin, xmax, ymin, ymax, bp, nx, ny, nz, x3d, y3d, z3d, out);
+}
+
+extern "C" int cgfd_media_bin_crop(const cgfd_bin_model_t *model, float xmin, float xmax,
+                                   float ymin, float ymax, int nx, int ny, int nz,
+                                   const float *z3d, cgfd_bin_box_t *box)
+{
+  if (!model || !z3d || !box || nx < 1 || ny < 1 || nz < 1)
+    return bin_err(CGFD_EINVAL, "binary model: missing argument or empty grid");
+  BinCrop b;
+  std::vector<float> xv, yv, zv;
+  const int rc = bin_setup(model, xmin, xmax, ymin, ymax, z3d, (size_t)nx * ny * nz, b, xv,
+                           yv, zv);
+  if (rc) return rc;
+  *box = bin_box_of(b);
+  return 0;
+}
+
+extern "C" int cgfd_media_bin_el_iso_box(const cgfd_bin_model_t *model, const cgfd_bin_box_t *box,
+                                         float xmin, float xmax, float ymin, float ymax,
+                                         const float *rho_box, const float *vp_box,
+                                         const float *vs_box, int nx, int ny, int nz,
+                                         const float *x3d, const float *y3d, const float *z3d,
+                                         float *rho, float *lam, float *mu)
+{
+  const float *v[3] = {rho_box, vp_box, vs_box};
+  float *o[3] = {rho, lam, mu};
+  return bin_run_box(0, model, box, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
+}
+
+extern "C" int cgfd_media_bin_vis_iso_box(const cgfd_bin_model_t *model,
+                                          const cgfd_bin_box_t *box, float xmin, float xmax,
+                                          float ymin, float ymax, const float *qp_box,
+                                          const float *qs_box, int nx, int ny, int nz,
+                                          const float *x3d, const float *y3d, const float *z3d,
+                                          float *qp, float *qs)
+{
+  const float *v[3] = {qp_box, qs_box, nullptr};
+  float *o[3] = {qp, qs, nullptr};
+  return bin_run_box(1, model, box, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
 }
 
 extern "C" int cgfd_media_bin_el_iso(const cgfd_bin_model_t *model, float xmin, float xmax,

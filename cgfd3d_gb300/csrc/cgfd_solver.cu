@@ -862,6 +862,8 @@ struct cgfd_solver {
   cudaGraphExec_t graph8;
   int graph_pre_lev;
   int *d_err;
+  int wait_limit;               /* stage-kernel wait polls (0: the default) */
+  int test_skip_plane;          /* test hook of cgfd_solver_set_wait_test, -1 off */
   float *pg, *dis;              /* surface peak-motion maps (free top) */
   float *staging;               /* upload staging volume (set-up only) */
   OutSlot out[CGFD_OUT_SLOTS + 1];   /* output boxes; the last: blocking calls */
@@ -1610,6 +1612,8 @@ extern "C" int cgfd_solver_create(const cgfd_problem_t *p, cgfd_solver_t **out)
    * measured on GB300, one plane gains ~1 % for isotropic/VTI media, any
    * prefetch loses for the visco-elastic kernel (8-row tiles, larger slots) */
   s->l2_ahead = s->med == MED_VIS ? 0 : 1;
+  s->wait_limit = 0;
+  s->test_skip_plane = -1;
   if (const char *e = getenv("CGFD_L2_AHEAD")) s->l2_ahead = std::max(0, std::min(8, atoi(e)));
   {
     /* k planes per CTA: chunks of at most 20 planes, split evenly (measured
@@ -1780,6 +1784,8 @@ static void fill_args(cgfd_solver_t *s, StageArgs &a, int istage)
   a.d_it = s->d_it;
   a.istage = istage;
   a.err = s->d_err;
+  a.wait_limit = s->wait_limit;
+  a.test_skip_plane = s->test_skip_plane;
   a.kchunk = s->kchunk;
   a.pml_fused = s->pml_fused;
   a.l2_ahead = s->l2_ahead;
@@ -1920,6 +1926,16 @@ extern "C" int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], in
   out[0] = s->t_stage_ms; out[1] = s->t_total_ms; out[2] = s->t_pml_ms;
   count[0] = s->n_stage; count[1] = s->n_stage + s->n_pml + s->n_other;
   count[2] = s->n_pml;
+  return 0;
+}
+
+extern "C" int cgfd_solver_set_wait_test(cgfd_solver_t *s, int wait_limit, int skip_plane)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  if (wait_limit < 0 || skip_plane < -1)
+    return set_err(CGFD_EINVAL, "wait test: limit %d, plane %d", wait_limit, skip_plane);
+  s->wait_limit = wait_limit;
+  s->test_skip_plane = skip_plane;
   return 0;
 }
 

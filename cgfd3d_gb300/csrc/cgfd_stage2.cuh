@@ -69,11 +69,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
   return ok != 0;
 }
 
-/* bounded wait; returns false (and flags the error) on timeout */
+/* bounded wait; returns false (and flags the error) after `limit` polls */
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
-                                          int *err)
+                                          int *err, int limit = 1 << 22)
 {
-  for (int n = 0; n < (1 << 22); n++) {
+  for (int n = 0; n < limit; n++) {
     if (mbar_try_wait(bar, parity)) return true;
     if (n > 16) __nanosleep(128);
   }

@@ -82,10 +82,10 @@ struct Slot {
   static_assert(SMEM_BYTES <= 232448, "more shared memory than one CTA gets");
 };
 
-/* bounded wait; `err` records a timeout */
-__device__ __forceinline__ void wait_full(uint64_t *bar, uint32_t parity, int *err)
+/* bounded wait; `err` records a timeout, and false is returned */
+__device__ __forceinline__ bool wait_full(uint64_t *bar, uint32_t parity, int *err, int limit)
 {
-  mbar_wait(bar, parity, err);
+  return mbar_wait(bar, parity, err, limit);
 }
 
 /* L2 prefetch of one global address (no register, no completion) */
@@ -233,8 +233,12 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
                 S_PRE = L::S_PRE, S_END = L::S_END, SLOT = L::SLOT;
   extern __shared__ __align__(128) float sm[];
   __shared__ __align__(8) uint64_t full_w[NB], empty_w[NB], full_s[NS], empty_s[NS];
+  /* set by the first wait that runs out: every warp of the CTA then leaves
+   * its loop, and the producer waits for the copies it issued */
+  __shared__ int abort_s;
   float *ring = sm;
   float *slots = sm + NB * PLANE;
+  const int lim = a.wait_limit > 0 ? a.wait_limit : (1 << 22);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const DevGrid &g = a.g;
@@ -251,6 +255,7 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
   if (threadIdx.x == 0) {
     for (int b = 0; b < NB; b++) { mbar_init(&full_w[b], 1); mbar_init(&empty_w[b], NCW); }
     for (int b = 0; b < NS; b++) { mbar_init(&full_s[b], 1); mbar_init(&empty_s[b], NCW); }
+    abort_s = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -277,22 +282,43 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
     const uint32_t slot_bytes =
         (9 + nmed + (MED == MED_VIS ? 6 * a.nmw : 0) + (KIND == 1 ? 9 : 0) +
          (KIND >= 1 ? 9 : 0)) * PTS * 4;
+    /* the latest copy issued into each buffer (ring position), for the
+     * drain after an abort; -1: none */
+    int last_w[NB], last_s[NS];
+#pragma unroll
+    for (int b = 0; b < NB; b++) last_w[b] = -1;
+#pragma unroll
+    for (int b = 0; b < NS; b++) last_s[b] = -1;
+    const bool test_cta = a.test_skip_plane >= 0 && bx == 0 && by == 0 && bz == 0;
+    /* false once the CTA has aborted (a wait ran out here or elsewhere) */
+    auto live = [&]() { return *(volatile int *)&abort_s == 0; };
     auto issue_wav = [&](int rel) {
+      if (!live()) return;
       int b = rel % NB;
       if (rel >= NB) {
-        mbar_wait(&empty_w[b], ((rel / NB) - 1) & 1, a.err);
+        if (!mbar_wait(&empty_w[b], ((rel / NB) - 1) & 1, a.err, lim)) {
+          abort_s = 1;
+          return;
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
+      if (test_cta && rel == a.test_skip_plane) return;   /* never arrives */
       mbar_expect_tx(&full_w[b], PLANE_DATA * 4);
       tma_load_5d(ring + b * PLANE, &tmap, bx0, by0, pbase + rel, 0, a.cur_level,
                   &full_w[b]);
+      last_w[b] = rel;
     };
     auto issue_slot = [&](int it) {
+      if (!live()) return;
       int b = it % NS;
       if (it >= NS) {
-        mbar_wait(&empty_s[b], ((it / NS) - 1) & 1, a.err);
+        if (!mbar_wait(&empty_s[b], ((it / NS) - 1) & 1, a.err, lim)) {
+          abort_s = 1;
+          return;
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
+      last_s[b] = it;
       float *dst = slots + b * SLOT;
       int k = kbeg + it;
       mbar_expect_tx(&full_s[b], slot_bytes);
@@ -325,10 +351,20 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
       if (rp < niter + 4) tma_prefetch_5d(&tmap, bx0, by0, pbase + rp, 0, a.cur_level);
     };
     for (int rel = 0; rel < 5; rel++) issue_wav(rel);
-    for (int it = 0; it < niter; it++) {
+    for (int it = 0; it < niter && live(); it++) {
       if (L2_AHEAD > 0) prefetch_ahead(it);
       issue_slot(it);
       if (it + 5 < niter + 4) issue_wav(it + 5);
+    }
+    if (!live()) {
+      /* aborted: the CTA leaves only after the copies it issued have
+       * landed in its shared memory (each wait bounded again) */
+#pragma unroll
+      for (int b = 0; b < NB; b++)
+        if (last_w[b] >= 0) mbar_wait(&full_w[b], (last_w[b] / NB) & 1, a.err, lim);
+#pragma unroll
+      for (int b = 0; b < NS; b++)
+        if (last_s[b] >= 0) mbar_wait(&full_s[b], (last_s[b] / NS) & 1, a.err, lim);
     }
     return;
   }
@@ -383,14 +419,21 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
     const int pmask = (a.pml_fused && valid) ? pml_mask(k) : 0;
     if (a.pml_fused && valid && it + 1 < niter && pml_mask(k + 1))
       prefetch_aux<KIND>(a, i, j, k + 1, pml_mask(k + 1));
+    /* every lane waits; the warp leaves together when any wait of the CTA
+     * has run out */
+    bool ok = *(volatile int *)&abort_s == 0;
 #pragma unroll
     for (int n = 0; n < 5; n++) {
       /* the window's older planes were waited for in earlier iterations:
        * only the first iteration waits for all five */
       int rel = rtop - 4 + n;
-      if (it == 0 || n == 4) wait_full(&full_w[rel % NB], (rel / NB) & 1, a.err);
+      if (ok && (it == 0 || n == 4)) ok = wait_full(&full_w[rel % NB], (rel / NB) & 1, a.err, lim);
     }
-    wait_full(&full_s[it % NS], (it / NS) & 1, a.err);
+    if (ok) ok = wait_full(&full_s[it % NS], (it / NS) & 1, a.err, lim);
+    if (!__all_sync(0xffffffffu, ok)) {
+      if (lane == 0) abort_s = 1;
+      break;
+    }
     Win w;
     {
       int b = (rtop - 4) % NB;

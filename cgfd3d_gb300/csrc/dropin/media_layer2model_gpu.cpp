@@ -13,9 +13,11 @@
  * file is read by the reference's own reader (media/media_read_file.cpp:
  * 22-240), its arrays are interleaved into the record layout of
  * cgfd_media_layer_* (include/cgfd3d_gpu.h) and the device computes the
- * medium with the requested equivalent-medium method; binary volumes are
- * read whole, one fread per file instead of one per sample, and
- * interpolated on the device (cgfd_media_bin_*).  Grids other than
+ * medium with the requested equivalent-medium method; of binary volumes only
+ * the box the grid needs is read, as the reference reads only its crop
+ * (cgfd_media_bin_crop; one fread per run of the files' fastest dimension
+ * instead of one per sample), and interpolated on the device
+ * (cgfd_media_bin_*_box).  Grids other than
  * curvilinear, methods other than loc/har/ari and other media types go to
  * the reference's routine (__real_...), which handles or rejects them as it
  * always did.  Errors print the library's message and exit(1), as the
@@ -166,12 +168,24 @@ extern "C" int __wrap_media_layer2model_el_vti(float *rho, float *c11, float *c3
   return 0;
 }
 
-/* a whole binary volume of n floats, as stored */
-static std::vector<float> bin_read(const char *file, size_t n)
+/* the box of a binary volume (file order, count[0] x count[1] x count[2]
+ * floats), one read per run of the files' fastest dimension */
+static std::vector<float> bin_read_box(const char *file, const int *size,
+                                       const cgfd_bin_box_t &box)
 {
-  std::vector<float> v(n);
+  const size_t run = (size_t)box.count[0];
+  std::vector<float> v(run * box.count[1] * box.count[2]);
   FILE *fp = fopen(file, "rb");
-  if (!fp || fread(v.data(), sizeof(float), n, fp) != n) {
+  bool ok = fp != nullptr;
+  for (int c2 = 0; ok && c2 < box.count[2]; c2++)
+    for (int c1 = 0; ok && c1 < box.count[1]; c1++) {
+      const long long off = (((long long)(box.first[2] + c2) * size[1] + box.first[1] + c1) *
+                                 size[0] + box.first[0]) * (long long)sizeof(float);
+      ok = fseeko(fp, (off_t)off, SEEK_SET) == 0 &&
+           fread(v.data() + ((size_t)c2 * box.count[1] + c1) * run, sizeof(float), run, fp) ==
+               run;
+    }
+  if (!ok) {
     fprintf(stderr, "Error: Insufficient data in %s.\n", file);
     fflush(stderr);
     exit(1);
@@ -217,14 +231,18 @@ extern "C" int __wrap_media_bin2model_el_iso(float *rho3d, float *lam3d, float *
                                          xmax, ymin, ymax, grid_type, bin_order, bin_size,
                                          bin_spacing, bin_origin, bin_file_rho, bin_file_vp,
                                          bin_file_vs);
-  const size_t n = (size_t)bin_size[0] * bin_size[1] * bin_size[2];
-  fprintf(stdout, "- reading model files %s, %s, %s\n", bin_file_rho, bin_file_vp, bin_file_vs);
-  const std::vector<float> rho = bin_read(bin_file_rho, n), vp = bin_read(bin_file_vp, n),
-                           vs = bin_read(bin_file_vs, n);
   const cgfd_bin_model_t m = bin_layout(bin_order, bin_size, bin_spacing, bin_origin);
+  cgfd_bin_box_t box;
+  if (cgfd_media_bin_crop(&m, xmin, xmax, ymin, ymax, (int)nx, (int)ny, (int)nz, z3d, &box))
+    lay_fail(bin_file_rho);
+  fprintf(stdout, "- reading model files %s, %s, %s\n", bin_file_rho, bin_file_vp, bin_file_vs);
+  const std::vector<float> rho = bin_read_box(bin_file_rho, bin_size, box),
+                           vp = bin_read_box(bin_file_vp, bin_size, box),
+                           vs = bin_read_box(bin_file_vs, bin_size, box);
   fprintf(stdout, "discretising the binary model on the GPU\n");
-  if (cgfd_media_bin_el_iso(&m, xmin, xmax, ymin, ymax, rho.data(), vp.data(), vs.data(),
-                            (int)nx, (int)ny, (int)nz, x3d, y3d, z3d, rho3d, lam3d, mu3d))
+  if (cgfd_media_bin_el_iso_box(&m, &box, xmin, xmax, ymin, ymax, rho.data(), vp.data(),
+                                vs.data(), (int)nx, (int)ny, (int)nz, x3d, y3d, z3d, rho3d,
+                                lam3d, mu3d))
     lay_fail(bin_file_rho);
   return 0;
 }
@@ -250,13 +268,16 @@ extern "C" int __wrap_media_bin2model_vis_iso(float *Qp3d, float *Qs3d, const fl
     return __real_media_bin2model_vis_iso(Qp3d, Qs3d, x3d, y3d, z3d, nx, ny, nz, xmin, xmax,
                                           ymin, ymax, grid_type, bin_order, bin_size,
                                           bin_spacing, bin_origin, bin_file_Qp, bin_file_Qs);
-  const size_t n = (size_t)bin_size[0] * bin_size[1] * bin_size[2];
-  fprintf(stdout, "- reading model files %s, %s\n", bin_file_Qp, bin_file_Qs);
-  const std::vector<float> qp = bin_read(bin_file_Qp, n), qs = bin_read(bin_file_Qs, n);
   const cgfd_bin_model_t m = bin_layout(bin_order, bin_size, bin_spacing, bin_origin);
+  cgfd_bin_box_t box;
+  if (cgfd_media_bin_crop(&m, xmin, xmax, ymin, ymax, (int)nx, (int)ny, (int)nz, z3d, &box))
+    lay_fail(bin_file_Qp);
+  fprintf(stdout, "- reading model files %s, %s\n", bin_file_Qp, bin_file_Qs);
+  const std::vector<float> qp = bin_read_box(bin_file_Qp, bin_size, box),
+                           qs = bin_read_box(bin_file_Qs, bin_size, box);
   fprintf(stdout, "discretising the binary model on the GPU\n");
-  if (cgfd_media_bin_vis_iso(&m, xmin, xmax, ymin, ymax, qp.data(), qs.data(), (int)nx,
-                             (int)ny, (int)nz, x3d, y3d, z3d, Qp3d, Qs3d))
+  if (cgfd_media_bin_vis_iso_box(&m, &box, xmin, xmax, ymin, ymax, qp.data(), qs.data(),
+                                 (int)nx, (int)ny, (int)nz, x3d, y3d, z3d, Qp3d, Qs3d))
     lay_fail(bin_file_Qp);
   return 0;
 }

@@ -153,6 +153,44 @@ def bin_model(layout, ext, vols, x3d, y3d, z3d, vis=False):
     return tuple(out)
 
 
+class BinBox(C.Structure):
+    """cgfd_bin_box_t: first sample and count per file dimension."""
+    _fields_ = [("first", C.c_int * 3), ("count", C.c_int * 3)]
+
+
+def bin_crop(layout, ext, z3d):
+    """The box of the files a grid needs (cgfd_media_bin_crop): (first,
+    count) per file dimension."""
+    nz, ny, nx = np.shape(z3d)
+    z = np.ascontiguousarray(z3d, np.float32)
+    box = BinBox()
+    _lib.check(_lib.lib().cgfd_media_bin_crop(C.byref(layout), *[C.c_float(float(e)) for e in ext],
+                                              nx, ny, nz, z.ctypes.data, C.byref(box)))
+    return tuple(box.first), tuple(box.count)
+
+
+def bin_model_box(layout, ext, box, vols, x3d, y3d, z3d, vis=False):
+    """bin_model on volumes holding only `box` = (first, count) of the files
+    (file order, count[0] fastest), as a caller that read just that box
+    passes them (cgfd_media_bin_el_iso_box / _vis_iso_box)."""
+    shape = np.shape(x3d)
+    nz, ny, nx = shape
+    x, y, z = [np.ascontiguousarray(a, np.float32) for a in (x3d, y3d, z3d)]
+    b = BinBox()
+    for d in range(3):
+        b.first[d], b.count[d] = int(box[0][d]), int(box[1][d])
+    n = b.count[0] * b.count[1] * b.count[2]
+    v = [np.ascontiguousarray(a, np.float32).ravel() for a in vols]
+    if len(v) != (2 if vis else 3) or any(a.size != n for a in v):
+        raise ValueError("expected %d volumes of %d samples" % (2 if vis else 3, n))
+    out = [np.empty(shape, np.float32) for _ in v]
+    fn = _lib.lib().cgfd_media_bin_vis_iso_box if vis else _lib.lib().cgfd_media_bin_el_iso_box
+    _lib.check(fn(C.byref(layout), C.byref(b), *[C.c_float(float(e)) for e in ext],
+                  *[a.ctypes.data for a in v], nx, ny, nz, x.ctypes.data, y.ctypes.data,
+                  z.ctypes.data, *[o.ctypes.data for o in out]))
+    return tuple(out)
+
+
 def read_md3grd(text, ext):
     """An elastic isotropic or VTI 3-D grid model (.md3grd text or path) as the
     reference's reader leaves it for a grid of extent ext = (xmin, xmax,

@@ -53,6 +53,12 @@ class Solver:
     def fetch(self):
         _lib.check(_lib.lib().cgfd_solver_fetch(self._h))
 
+    def set_wait_test(self, wait_limit, skip_plane=-1):
+        """Polls before a stage-kernel wait gives up (0: default) and, for
+        tests, a wavefield plane whose copy the first CTA leaves out."""
+        _lib.check(_lib.lib().cgfd_solver_set_wait_test(self._h, int(wait_limit),
+                                                        int(skip_plane)))
+
     def check_finite(self):
         _lib.check(_lib.lib().cgfd_solver_check_finite(self._h))
 

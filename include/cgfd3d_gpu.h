@@ -281,6 +281,17 @@ int cgfd_solver_kernel_times(const cgfd_solver_t *s, float out[3], int count[3])
 /* Record a CUDA event pair around every stage launch of later runs. */
 int cgfd_solver_set_timing(cgfd_solver_t *s, int on);
 
+/* No counterpart in the reference (its loop has no device waits).  Every
+ * wait of the stage kernel on a bulk copy or a buffer release gives up after
+ * `wait_limit` polls (0: the default, about half a second): it records
+ * device error 1, the whole CTA leaves its loop, the producer waits for the
+ * copies it issued, and the run returns CGFD_ECUDA ("device wait timed
+ * out") with the device still usable.  Test hook: skip_plane >= 0 makes the
+ * first CTA of every stage launch leave out the copy of that wavefield
+ * plane of its k march, so a wait on it runs out (-1: off).  A solver that
+ * has timed out keeps its error; destroy it. */
+int cgfd_solver_set_wait_test(cgfd_solver_t *s, int wait_limit, int skip_plane);
+
 /* Host<->device bytes moved so far (uploads at create, fetches). */
 int cgfd_solver_transfer_bytes(const cgfd_solver_t *s, size_t *h2d, size_t *d2h);
 
@@ -437,6 +448,37 @@ int cgfd_media_bin_vis_iso(const cgfd_bin_model_t *model, float xmin, float xmax
                            float ymax, const float *qp_vol, const float *qs_vol, int nx,
                            int ny, int nz, const float *x3d, const float *y3d,
                            const float *z3d, float *qp, float *qs);
+
+/* A box of the binary files: first sample and sample count per file
+ * dimension (the files' order, fastest first). */
+typedef struct {
+  int first[3];
+  int count[3];
+} cgfd_bin_box_t;
+
+/* The box of the files the grid needs: the x/y crop to [xmin, xmax] x
+ * [ymin, ymax] and every z sample, as media_bin2model reads them
+ * (media/media_bin2model.cpp:44-158, which reads only that crop of each
+ * file).  Errors as cgfd_media_bin_el_iso. */
+int cgfd_media_bin_crop(const cgfd_bin_model_t *model, float xmin, float xmax, float ymin,
+                        float ymax, int nx, int ny, int nz, const float *z3d,
+                        cgfd_bin_box_t *box);
+
+/* cgfd_media_bin_el_iso / _vis_iso on volumes that hold only a box of the
+ * files (count[0] * count[1] * count[2] floats each, file order), for
+ * callers that read just the box cgfd_media_bin_crop gives: host and device
+ * memory then grow with the crop, not with the files.  A box that does not
+ * hold the crop is CGFD_EINVAL. */
+int cgfd_media_bin_el_iso_box(const cgfd_bin_model_t *model, const cgfd_bin_box_t *box,
+                              float xmin, float xmax, float ymin, float ymax,
+                              const float *rho_box, const float *vp_box, const float *vs_box,
+                              int nx, int ny, int nz, const float *x3d, const float *y3d,
+                              const float *z3d, float *rho, float *lam, float *mu);
+int cgfd_media_bin_vis_iso_box(const cgfd_bin_model_t *model, const cgfd_bin_box_t *box,
+                               float xmin, float xmax, float ymin, float ymax,
+                               const float *qp_box, const float *qs_box, int nx, int ny, int nz,
+                               const float *x3d, const float *y3d, const float *z3d, float *qp,
+                               float *qs);
 
 /* Bytes of HBM a solver for `p` allocates (wavefield, media, metrics, aux). */
 size_t cgfd_device_bytes(const cgfd_problem_t *p);

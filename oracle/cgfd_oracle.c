@@ -2380,6 +2380,23 @@ static float bin_trilinear(const bin_crop_t *b, const float *v, float xq, float 
   return v110 + (zq - z[iz0]) / (z[iz2] - z[iz0]) * (v112 - v110);
 }
 
+/* The box of the files the crop covers: first sample and count per file
+ * dimension (the reference reads exactly these samples,
+ * media/media_bin2model.cpp:91-175).  Returns 1 where the reference exits. */
+int oracle_bin_crop(const int *order, const int *size, const float *spacing,
+                    const float *origin, const float *ext, size_t vol, const float *z3d,
+                    int *first, int *count)
+{
+  bin_crop_t b;
+  if (bin_setup(order, size, spacing, origin, ext, vol, z3d, &b)) return 1;
+  for (int d = 0; d < 3; d++) {
+    first[b.dim[d]] = d < 2 ? b.start[d] : 0;
+    count[b.dim[d]] = b.n[d];
+  }
+  free(b.xv); free(b.yv); free(b.zv);
+  return 0;
+}
+
 /* vis 0: rho, lambda, mu from volumes rho, vp, vs
  * (parameterization_bin_el_iso_loc, media/media_bin2model.cpp:185-234);
  * vis 1: Qp, Qs from volumes Qp, Qs (:387-432).  ext: xmin xmax ymin ymax

@@ -110,6 +110,71 @@ int cgfd_media_bin_vis_iso(const cgfd_bin_model_t *model, float xmin, float xmax
   return stub_bin(1, model, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
 }
 
+int oracle_bin_crop(const int *order, const int *size, const float *spacing,
+                    const float *origin, const float *ext, size_t vol, const float *z3d,
+                    int *first, int *count);
+
+int cgfd_media_bin_crop(const cgfd_bin_model_t *model, float xmin, float xmax, float ymin,
+                        float ymax, int nx, int ny, int nz, const float *z3d,
+                        cgfd_bin_box_t *box)
+{
+  const float ext[4] = {xmin, xmax, ymin, ymax};
+  if (oracle_bin_crop(model->order, model->size, model->spacing, model->origin, ext,
+                      (size_t)nx * ny * nz, z3d, box->first, box->count)) {
+    stub_msg = "binary model: the model does not cover the grid";
+    return CGFD_EINVAL;
+  }
+  return 0;
+}
+
+/* box volumes placed in zero-filled whole-file volumes (the crop reads
+ * inside the box only), then the whole-file restatement */
+static int stub_bin_box(int vis, const cgfd_bin_model_t *m, const cgfd_bin_box_t *box,
+                        float xmin, float xmax, float ymin, float ymax, const float *const *bv,
+                        int nx, int ny, int nz, const float *x3d, const float *y3d,
+                        const float *z3d, float **o)
+{
+  const int nv = vis ? 2 : 3;
+  const size_t whole = (size_t)m->size[0] * m->size[1] * m->size[2];
+  float *v[3] = {NULL, NULL, NULL};
+  int rc = 0;
+  for (int n = 0; n < nv; n++) {
+    v[n] = calloc(whole, sizeof(float));
+    for (int c2 = 0; c2 < box->count[2]; c2++)
+      for (int c1 = 0; c1 < box->count[1]; c1++)
+        memcpy(v[n] + ((size_t)(box->first[2] + c2) * m->size[1] + box->first[1] + c1) *
+                          m->size[0] + box->first[0],
+               bv[n] + ((size_t)c2 * box->count[1] + c1) * box->count[0],
+               (size_t)box->count[0] * sizeof(float));
+  }
+  rc = stub_bin(vis, m, xmin, xmax, ymin, ymax, (const float *const *)v, nx, ny, nz, x3d, y3d,
+                z3d, o);
+  for (int n = 0; n < nv; n++) free(v[n]);
+  return rc;
+}
+
+int cgfd_media_bin_el_iso_box(const cgfd_bin_model_t *model, const cgfd_bin_box_t *box,
+                              float xmin, float xmax, float ymin, float ymax,
+                              const float *rho_box, const float *vp_box, const float *vs_box,
+                              int nx, int ny, int nz, const float *x3d, const float *y3d,
+                              const float *z3d, float *rho, float *lam, float *mu)
+{
+  const float *v[3] = {rho_box, vp_box, vs_box};
+  float *o[3] = {rho, lam, mu};
+  return stub_bin_box(0, model, box, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
+}
+
+int cgfd_media_bin_vis_iso_box(const cgfd_bin_model_t *model, const cgfd_bin_box_t *box,
+                               float xmin, float xmax, float ymin, float ymax,
+                               const float *qp_box, const float *qs_box, int nx, int ny, int nz,
+                               const float *x3d, const float *y3d, const float *z3d, float *qp,
+                               float *qs)
+{
+  const float *v[2] = {qp_box, qs_box};
+  float *o[2] = {qp, qs};
+  return stub_bin_box(1, model, box, xmin, xmax, ymin, ymax, v, nx, ny, nz, x3d, y3d, z3d, o);
+}
+
 int oracle_grid_el_iso(int method, int NI, int NL, const int *ngz, int NX, int NY, float MINX,
                        float MINY, float DX, float DY, const float *rec, int nx, int ny, int nz,
                        const float *x3d, const float *y3d, const float *z3d, float **out);

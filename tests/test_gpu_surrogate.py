@@ -1,0 +1,126 @@
+"""The seismogram surrogate on the device: the tcgen05 matrix product
+against torch, the forward pass and every parameter gradient against the
+float64 restatement (oracle/surrogate_ref.py), and training on a teacher
+network's outputs.
+
+Tolerances: the device rounds weights, activations and their gradients to
+bf16 (8 significant bits) and accumulates in fp32, so against float64 a
+forward pass agrees to about 1 % (relative L2) and gradients to a few %,
+with cosine similarity above 0.999 per layer.
+"""
+
+import numpy as np
+import pytest
+
+import surrogate_ref as sr
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from cgfd3d_gb300 import surrogate
+    return surrogate._lib_sg()
+
+
+@pytest.mark.parametrize("M,N,K", [(256, 384, 640), (200, 136, 72), (8, 1152, 640),
+                                   (1024, 128, 1024)])
+def test_gemm_modes_match_torch(M, N, K):
+    import ctypes as C
+    import torch
+    from cgfd3d_gb300 import _lib
+    L = _lib()
+    g = torch.Generator(device="cpu").manual_seed(M * 7 + N)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    bias = torch.randn(N, generator=g).cuda()
+    ref = A.float() @ B.float().T
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    P = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    # fp32 store
+    C32 = torch.zeros(M, N, device="cuda")
+    _lib.check(L.cgfd_sg_gemm(P(A), K, P(B), K, P(C32), N, M, N, K, 1.0, None, 0, 1, None, 1,
+                              P(err), s))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert torch.allclose(C32, ref, rtol=1e-4, atol=1e-3), (C32 - ref).abs().max().item()
+    # bf16 with bias, GELU and the pre-activation copy
+    ldc = (N + 7) // 8 * 8
+    H = torch.zeros(M, ldc, dtype=torch.bfloat16, device="cuda")
+    Z = torch.zeros(M, ldc, dtype=torch.bfloat16, device="cuda")
+    _lib.check(L.cgfd_sg_gemm(P(A), K, P(B), K, P(H), ldc, M, N, K, 1.0, P(bias), 1, 0, P(Z),
+                              1, P(err), s))
+    torch.cuda.synchronize()
+    z = ref + bias
+    h = torch.nn.functional.gelu(z, approximate="tanh")
+    assert torch.allclose(Z[:, :N].float(), z, rtol=1e-2, atol=1e-2)
+    assert torch.allclose(H[:, :N].float(), h, rtol=1e-2, atol=1e-2)
+    # fp32 accumulation split along K (added onto existing values)
+    Cacc = torch.ones(M, N, device="cuda")
+    _lib.check(L.cgfd_sg_gemm(P(A), K, P(B), K, P(Cacc), N, M, N, K, 1.0, None, 0, 2, None, 3,
+                              P(err), s))
+    torch.cuda.synchronize()
+    assert torch.allclose(Cacc, ref + 1.0, rtol=1e-4, atol=1e-3)
+    assert int(err.item()) == 0
+
+
+def _flat_params_f64(net):
+    import torch
+    return net.w16.float().cpu().numpy().astype(np.float64)
+
+
+def test_forward_and_gradients_match_float64():
+    import torch
+    from cgfd3d_gb300 import surrogate
+    nrec, nt, B = 4, 1000, 8
+    net = surrogate.Surrogate(nrec=nrec, nt=nt, seed=3, scale=1.0)
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(-1, 1, (B, 3)).astype(np.float32)
+    M = rng.standard_normal((B, 6)).astype(np.float32)
+    params = _flat_params_f64(net)
+    u_ref = sr.forward(params, pos, M, nrec, nt, 1.0)
+    U = (u_ref * (1.0 + 0.3 * rng.standard_normal(u_ref.shape))).astype(np.float32)
+    tp = torch.from_numpy(pos).cuda()
+    tM = torch.from_numpy(M).cuda()
+    u = net.predict(tp, tM).cpu().numpy().astype(np.float64)
+    rel = np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref)
+    assert rel < 2e-2, rel
+    tU = torch.from_numpy(U).cuda()
+    norm = (tU.double() ** 2).reshape(B, -1).sum(1).float()
+    loss_b = net.gradients(tp, tM, tU, norm)
+    g = net.grad.cpu().numpy().astype(np.float64)
+    loss_ref, g_ref = sr.loss_and_grad(params, pos, M, U, nrec, 1.0)
+    loss = float((loss_b / norm).mean().item())
+    assert abs(loss - loss_ref) < 2e-2 * loss_ref, (loss, loss_ref)
+    assert net.device_error() == 0
+    for n, (a, b) in enumerate(net.lay.offsets):
+        o = net.lay.layers[n][0]
+        for name, sl in (("W", slice(a, b)), ("b", slice(b, b + o))):
+            x, y = g[sl], g_ref[sl]
+            cos = float(x @ y / (np.linalg.norm(x) * np.linalg.norm(y) + 1e-300))
+            rl = float(np.linalg.norm(x - y) / (np.linalg.norm(y) + 1e-300))
+            assert cos > 0.999 and rl < 5e-2, (n, name, cos, rl)
+
+
+def test_training_fits_a_teacher():
+    """A student network trained by the device kernels fits the outputs of a
+    fixed teacher network of the same shape: the misfit falls well below
+    its starting value."""
+    import torch
+    from cgfd3d_gb300 import surrogate
+    nrec, nt, B = 4, 1000, 64
+    teacher = surrogate.Surrogate(nrec=nrec, nt=nt, seed=11, scale=1.0)
+    student = surrogate.Surrogate(nrec=nrec, nt=nt, seed=12, scale=1.0, lr=3e-4)
+    rng = np.random.default_rng(7)
+    pos = torch.from_numpy(rng.uniform(-1, 1, (B, 3)).astype(np.float32)).cuda()
+    M = torch.from_numpy(rng.standard_normal((B, 6)).astype(np.float32)).cuda()
+    U = teacher.predict(pos, M).contiguous()
+    norm = (U.double() ** 2).reshape(B, -1).sum(1).float()
+    first = None
+    for it in range(300):
+        loss_b = student.gradients(pos, M, U, norm)
+        student.apply()
+        val = float((loss_b / norm).mean().item())
+        first = val if first is None else first
+    assert student.device_error() == 0
+    assert np.isfinite(val) and val < 0.2 * first, (first, val)

@@ -329,6 +329,35 @@ def test_device_bin_matches_reference(vis):
         media.bin_model(bad, z["ext"], [z[k] for k in keys], g["x3d"], g["y3d"], g["z3d"], vis)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("vis", [False, True])
+def test_device_bin_box_equals_whole_files(vis):
+    """Volumes holding only the crop's box of the files (what a caller that
+    reads just the box passes) give the whole-file results bit for bit; a
+    box that misses part of the crop is refused."""
+    from cgfd3d_gb300 import media
+    z = np.load(FIX_BIN)
+    g = np.load(FIX)
+    lay = media.BinModel.of(z["order"], z["size"], z["spacing"], z["origin"])
+    keys = ("qp_vol", "qs_vol") if vis else ("rho_vol", "vp_vol", "vs_vol")
+    first, count = media.bin_crop(lay, z["ext"], g["z3d"])
+    size = [int(v) for v in z["size"]]
+    assert any(c < s for c, s in zip(count, size))        # a real crop
+    cut = tuple(slice(f, f + c) for f, c in zip(first[::-1], count[::-1]))
+    boxes = [np.asarray(z[k], np.float32).reshape(size[::-1])[cut] for k in keys]
+    whole = media.bin_model(lay, z["ext"], [z[k] for k in keys], g["x3d"], g["y3d"], g["z3d"],
+                            vis)
+    got = media.bin_model_box(lay, z["ext"], (first, count), boxes, g["x3d"], g["y3d"],
+                              g["z3d"], vis)
+    for a, b in zip(got, whole):
+        np.testing.assert_array_equal(a.view(np.int32), b.view(np.int32))
+    short = (first, tuple(c - 1 if d == 0 else c for d, c in enumerate(count)))
+    cut2 = tuple(slice(f, f + c) for f, c in zip(short[0][::-1], short[1][::-1]))
+    small = [np.asarray(z[k], np.float32).reshape(size[::-1])[cut2] for k in keys]
+    with pytest.raises(Exception):
+        media.bin_model_box(lay, z["ext"], short, small, g["x3d"], g["y3d"], g["z3d"], vis)
+
+
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "media")),
                     reason="reference tree not present")
 @pytest.mark.parametrize("method", ["loc", "har", "ari"])
