@@ -85,6 +85,8 @@ def lib():
     L.cgfd_locator_destroy.restype = None
     L.cgfd_batch_create.argtypes = [vp, C.c_int, C.c_int, C.POINTER(vp)]
     L.cgfd_batch_run.argtypes = [vp, C.c_int]
+    L.cgfd_batch_fetch_seismograms.argtypes = [vp]
+    L.cgfd_solver_fetch_seismograms.argtypes = [vp]
     L.cgfd_batch_times.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
     L.cgfd_batch_fetch.argtypes = [vp]
     L.cgfd_batch_reset.argtypes = [vp]

@@ -1995,6 +1995,24 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
   return 0;
 }
 
+extern "C" int cgfd_solver_fetch_seismograms(cgfd_solver_t *s)
+{
+  if (!s) return set_err(CGFD_EINVAL, "null solver");
+  const cgfd_problem_t *p = s->p;
+  if (p->recv_n > 0) {
+    size_t nb = (size_t)p->recv_n * p->recv_ncmp * p->recv_max_nt * 4;
+    CK(cudaMemcpyAsync(p->recv_seismo, s->recv_seismo, nb, cudaMemcpyDeviceToHost, s->stream));
+    s->d2h_bytes += nb;
+  }
+  if (p->line_n > 0) {
+    size_t nb = (size_t)p->line_n * p->ncmp * p->line_max_nt * 4;
+    CK(cudaMemcpyAsync(p->line_seismo, s->line_seismo, nb, cudaMemcpyDeviceToHost, s->stream));
+    s->d2h_bytes += nb;
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  return 0;
+}
+
 extern "C" int cgfd_solver_fetch_surface_matrices(cgfd_solver_t *s, float *mVx,
                                                   float *mVy, float *mF)
 {
@@ -2653,6 +2671,16 @@ extern "C" int cgfd_batch_fetch(cgfd_batch_t *b)
   if (!b) return set_err(CGFD_EINVAL, "null batch");
   for (cgfd_solver_t *s : b->sv) {
     int rc = cgfd_solver_fetch(s);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+extern "C" int cgfd_batch_fetch_seismograms(cgfd_batch_t *b)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  for (cgfd_solver_t *s : b->sv) {
+    int rc = cgfd_solver_fetch_seismograms(s);
     if (rc) return rc;
   }
   return 0;

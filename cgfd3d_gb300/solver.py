@@ -255,6 +255,10 @@ class Batch:
     def fetch(self):
         _lib.check(_lib.lib().cgfd_batch_fetch(self._h))
 
+    def fetch_seismograms(self):
+        """Receiver and line seismograms of every shot (no wavefield)."""
+        _lib.check(_lib.lib().cgfd_batch_fetch_seismograms(self._h))
+
     def reset(self):
         _lib.check(_lib.lib().cgfd_batch_reset(self._h))
 

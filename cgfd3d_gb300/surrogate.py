@@ -412,7 +412,7 @@ def solve_shots(model, ijd, M, steps=1000, dt=0.01, batch=64, **kw):
         t = time.perf_counter()
         with Batch(probs) as b:
             b.run(probs[0].nt_total)
-            b.fetch()
+            b.fetch_seismograms()
         secs += time.perf_counter() - t
         for q, p in enumerate(probs):
             out[a + q] = seismograms(p, steps)

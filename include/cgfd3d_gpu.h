@@ -197,6 +197,10 @@ int cgfd_solver_run(cgfd_solver_t *s, int nsteps);
  * leaves it), PML aux and seismograms back into the host arrays of `p`. */
 int cgfd_solver_fetch(cgfd_solver_t *s);
 
+/* Only the receiver and line seismograms of cgfd_solver_fetch (callers that
+ * need no wavefield, such as shot gathers). */
+int cgfd_solver_fetch_seismograms(cgfd_solver_t *s);
+
 /* Current step index. */
 int cgfd_solver_step(const cgfd_solver_t *s);
 
@@ -507,6 +511,9 @@ int cgfd_batch_times(const cgfd_batch_t *b, float *ms, int *launches);
 
 /* cgfd_solver_fetch for every shot (results into each shot's problem). */
 int cgfd_batch_fetch(cgfd_batch_t *b);
+
+/* cgfd_solver_fetch_seismograms for every shot. */
+int cgfd_batch_fetch_seismograms(cgfd_batch_t *b);
 
 /* Every shot back at step 0 with its problem's host inputs. */
 int cgfd_batch_reset(cgfd_batch_t *b);

@@ -124,3 +124,42 @@ def test_training_fits_a_teacher():
         first = val if first is None else first
     assert student.device_error() == 0
     assert np.isfinite(val) and val < 0.2 * first, (first, val)
+
+
+def test_pipeline_on_solver_shots():
+    """Shots of the batched solver on a small crop of the topography model
+    feed the network: their seismograms equal single-shot runs of the same
+    problems, training lowers the misfit, and held-out predictions are
+    finite."""
+    import torch
+    from cgfd3d_gb300 import models, solver, surrogate as SG
+    from helpers import assert_parity
+    base = models._topo_base(96, 96, 64, 7)
+    crop = (64, 64, 48)
+    model = SG.crop_model(base, crop)
+    ijd, M = SG.draw_sources(12, crop, seed=3)
+    steps, nrec = 100, 16
+    U, secs = SG.solve_shots(model, ijd, M, steps=steps, dt=0.005, batch=6, nrec=nrec)
+    assert U.shape == (12, steps, 3 * nrec) and secs > 0
+    one = SG.shot_problems(model, ijd[:1], M[:1], steps=steps, dt=0.005, nrec=nrec)[0]
+    solver.drv_rk_curv_col_allstep(one)
+    assert_parity(U[0], SG.seismograms(one, steps), "batched shot vs single run")
+    scale = float(np.sqrt((U[:8].astype(np.float64) ** 2).mean()))
+    net = SG.Surrogate(nrec=nrec, nt=steps, seed=2, scale=scale, lr=1e-3)
+    pos = SG.normalise_positions(ijd, crop)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    tp, tM, tU = dev(pos[:8]), dev(M[:8]), dev(U[:8])
+    norm = (tU.double() ** 2).reshape(8, -1).sum(1).float()
+    first = last = None
+    for it in range(150):
+        loss_b = net.gradients(tp, tM, tU, norm)
+        net.apply()
+        v = float((loss_b / norm).mean().item())
+        first = v if first is None else first
+        last = v
+    assert net.device_error() == 0
+    assert last < 0.5 * first, (first, last)
+    pred = net.predict(dev(pos[8:]), dev(M[8:])).cpu().numpy()
+    assert pred.shape == (4, steps, 3 * nrec) and np.isfinite(pred).all()
+    mis = SG.misfit(pred, U[8:])
+    assert np.isfinite(mis).all()
