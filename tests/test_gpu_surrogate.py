@@ -17,7 +17,7 @@ import surrogate_ref as sr
 pytestmark = pytest.mark.gpu
 
 
-def _lib():
+def _sglib():
     from cgfd3d_gb300 import surrogate
     return surrogate._lib_sg()
 
@@ -28,7 +28,7 @@ def test_gemm_modes_match_torch(M, N, K):
     import ctypes as C
     import torch
     from cgfd3d_gb300 import _lib
-    L = _lib()
+    L = _sglib()
     g = torch.Generator(device="cpu").manual_seed(M * 7 + N)
     A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
     B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
