@@ -168,11 +168,19 @@ __global__ void k_contract_loss(const bf16 *__restrict__ G, const float *__restr
                                 const float *__restrict__ Utrue, const float *__restrict__ norm,
                                 float *__restrict__ err, bf16 *__restrict__ dG)
 {
-  GRID_LOOP(i, (long long)B * Tg * R)
-  {
-    const int r = (int)(i % R);
-    const long long bt = i / R;
-    const int t = (int)(bt % Tg), b = (int)(bt / Tg);
+  /* blockIdx.y: the shot; the block's squared misfits are summed in the
+   * block and added to err[b] once */
+  const int b = blockIdx.y;
+  const long long n = (long long)Tg * R;
+  float mb[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) mb[k] = M[6 * b + k];
+  const float gscale = 2.0f * scale / ((float)B * norm[b]);
+  float acc = 0.0f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % R), t = (int)(i / R);
+    const long long bt = (long long)b * Tg + t;
     const bf16 *g = G + bt * 6 * R + r;
     bf16 *dg = dG + bt * 6 * R + r;
     if (t >= T) {
@@ -182,12 +190,22 @@ __global__ void k_contract_loss(const bf16 *__restrict__ G, const float *__restr
     }
     float u = 0.0f;
 #pragma unroll
-    for (int k = 0; k < 6; k++) u += M[6 * b + k] * __bfloat162float(g[k * R]);
+    for (int k = 0; k < 6; k++) u += mb[k] * __bfloat162float(g[k * R]);
     const float d = scale * u - Utrue[((long long)b * T + t) * R + r];
-    atomicAdd(err + b, d * d);
-    const float du = 2.0f * d * scale / ((float)B * norm[b]);
+    acc += d * d;
+    const float du = d * gscale;
 #pragma unroll
-    for (int k = 0; k < 6; k++) dg[k * R] = __float2bfloat16_rn(M[6 * b + k] * du);
+    for (int k = 0; k < 6; k++) dg[k * R] = __float2bfloat16_rn(mb[k] * du);
+  }
+  __shared__ float part[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) part[warp] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    acc = lane < (int)(blockDim.x >> 5) ? part[lane] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) atomicAdd(err + b, acc);
   }
 }
 
@@ -311,7 +329,12 @@ extern "C" int cgfd_sg_contract_loss(const void *G, const float *M, int B, int T
 {
   if (!G || !M || !Utrue || !norm || !err || !dG || B < 1 || T < 1 || Tg < T || R < 1)
     return sg_err(CGFD_EINVAL, "sg_contract_loss: B %d Tg %d T %d R %d", B, Tg, T, R);
-  k_contract_loss<<<nblocks((long long)B * Tg * R, 256), 256, 0, SG_STREAM(stream)>>>(
+  if (B > 65535) return sg_err(CGFD_EINVAL, "sg_contract_loss: %d shots (65535 at most)", B);
+  const long long per = (long long)Tg * R;
+  int bx = (int)((per + 255) / 256);
+  const int cap = (152 * 16 + B - 1) / B;
+  bx = bx < 1 ? 1 : (bx > cap ? cap : bx);
+  k_contract_loss<<<dim3(bx, B), 256, 0, SG_STREAM(stream)>>>(
       (const bf16 *)G, M, B, Tg, T, R, scale, Utrue, norm, err, (bf16 *)dG);
   return launched("sg_contract_loss");
 }

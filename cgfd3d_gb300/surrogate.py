@@ -119,6 +119,7 @@ class Surrogate:
         self.m = torch.zeros_like(self.w)
         self.v = torch.zeros_like(self.w)
         self.err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.launches = 0          # kernels this object has launched
         L = _lib_sg()
         _check(L.cgfd_sg_to_bf16(_ptr(self.w), self.lay.nparam, _ptr(self.w16), _stream()))
         # transposed bf16 weights (in x out) for the input-gradient products
@@ -126,7 +127,6 @@ class Surrogate:
                    for (o, i) in self.lay.layers]
         self._refresh_transposes()
         self._bufs = {}
-        self.launches = 0
 
     # -- parameters -----------------------------------------------------------
     def W(self, n, which="w16"):
