@@ -2,7 +2,8 @@
 gradients (cgfd3d_gb300/surrogate.py, cgfd_sg.cu, cgfd_sg_gemm.cu).
 
 TEST INFRASTRUCTURE ONLY: tests/ compare the device's bf16/fp32 forward
-pass and parameter gradients with this numpy code; the product never
+pass and parameter gradients with this numpy code -- exact, and with the
+device's bf16 roundings emulated (emulate=True) -- and the product never
 imports it.  The reference has no counterpart of the surrogate (it runs
 the solver for every shot), so this restatement is checked on its own
 against finite differences (tests/test_surrogate_ref.py).
@@ -96,8 +97,12 @@ def col2im_up(dA, Tin, up=UP, ks=KS):
     return dX
 
 
-def forward(params, pos, M, nrec, nt, scale, keep=False):
-    """Seismograms u [B, nt, 3 nrec]; with keep, also the activations."""
+def forward(params, pos, M, nrec, nt, scale, keep=False, emulate=False):
+    """Seismograms u [B, nt, 3 nrec]; with keep, also the activations.  With
+    emulate, every value the device stores in bf16 (activations,
+    pre-activations, the Green's functions) is rounded to bf16 here too;
+    products and sums stay float64."""
+    rd = bf16_round if emulate else (lambda v: v)
     P = split(np.asarray(params, np.float64), nrec)
     enc, dec = layers(nrec)
     B = len(pos)
@@ -107,8 +112,8 @@ def forward(params, pos, M, nrec, nt, scale, keep=False):
     for n in range(len(enc)):
         W, b = P[n]
         z = h @ W.T + b
-        acts["z%d" % n], acts["in%d" % n] = z, h
-        h = gelu(z)
+        acts["z%d" % n], acts["in%d" % n] = rd(z), h
+        h = rd(gelu(z))
     X = h.reshape(B, T0, C0)
     ne = len(enc)
     for l in range(len(dec)):
@@ -116,8 +121,8 @@ def forward(params, pos, M, nrec, nt, scale, keep=False):
         A = im2col_up(X)
         Bt, Tout = A.shape[0], A.shape[1]
         z = A.reshape(Bt * Tout, -1) @ W.T + b
-        acts["A%d" % l], acts["zd%d" % l] = A, z
-        X = z.reshape(B, Tout, -1) if l == len(dec) - 1 else gelu(z).reshape(B, Tout, -1)
+        acts["A%d" % l], acts["zd%d" % l] = A, rd(z)
+        X = rd(z).reshape(B, Tout, -1) if l == len(dec) - 1 else rd(gelu(z)).reshape(B, Tout, -1)
     R = 3 * nrec
     G = X.reshape(B, -1, NMT, R)
     u = scale * np.einsum("bk,btkr->btr", np.asarray(M, np.float64), G[:, :nt])
@@ -127,15 +132,19 @@ def forward(params, pos, M, nrec, nt, scale, keep=False):
     return u
 
 
-def loss_and_grad(params, pos, M, U, nrec, scale):
+def loss_and_grad(params, pos, M, U, nrec, scale, emulate=False):
     """Mean squared relative misfit (1/B) sum_b |u_b - U_b|^2 / |U_b|^2 and
-    its gradient with respect to the flat parameter vector."""
+    its gradient with respect to the flat parameter vector.  With emulate,
+    the gradients are rounded to bf16 where the device stores them (dG, the
+    input gradients of every product, every dZ), as forward does for the
+    activations."""
+    rd = bf16_round if emulate else (lambda v: v)
     params = np.asarray(params, np.float64)
     P = split(params, nrec)
     enc, dec = layers(nrec)
     ne = len(enc)
     B, nt, R = U.shape
-    u, a = forward(params, pos, M, nrec, nt, scale, keep=True)
+    u, a = forward(params, pos, M, nrec, nt, scale, keep=True, emulate=emulate)
     norm = (np.asarray(U, np.float64) ** 2).reshape(B, -1).sum(1)
     d = u - U
     loss = float(((d ** 2).reshape(B, -1).sum(1) / norm).mean())
@@ -144,24 +153,24 @@ def loss_and_grad(params, pos, M, U, nrec, scale):
     dG = np.zeros_like(G)
     dG[:, :nt] = scale * np.einsum("bk,btr->btkr", np.asarray(M, np.float64), du)
     grads = [None] * (ne + len(dec))
-    dz = dG.reshape(B * G.shape[1], -1)
+    dz = rd(dG).reshape(B * G.shape[1], -1)
     for l in range(len(dec) - 1, -1, -1):
         W, _ = P[ne + l]
         A = a["A%d" % l]
         Bt, Tout, ks, C = A.shape
         A2 = A.reshape(Bt * Tout, -1)
         grads[ne + l] = (dz.T @ A2, dz.sum(0))
-        dA = (dz @ W).reshape(Bt, Tout, ks, C)
+        dA = rd(dz @ W).reshape(Bt, Tout, ks, C)
         dX = col2im_up(dA, Tout // UP)
         zprev = a["zd%d" % (l - 1)].reshape(B, Tout // UP, -1) if l > 0 else \
             a["z%d" % (ne - 1)].reshape(B, T0, C0)
-        dz = (dX * gelu_grad(zprev)).reshape(-1, dX.shape[-1])
+        dz = rd(dX * gelu_grad(zprev)).reshape(-1, dX.shape[-1])
     dz = dz.reshape(B, -1)
     for n in range(ne - 1, -1, -1):
         W, _ = P[n]
         grads[n] = (dz.T @ a["in%d" % n], dz.sum(0))
         if n == 0:
             break
-        dz = (dz @ W) * gelu_grad(a["z%d" % (n - 1)])
+        dz = rd(rd(dz @ W) * gelu_grad(a["z%d" % (n - 1)]))
     flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
     return loss, flat

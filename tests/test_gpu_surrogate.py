@@ -4,9 +4,14 @@ float64 restatement (oracle/surrogate_ref.py), and training on a teacher
 network's outputs.
 
 Tolerances: the device rounds weights, activations and their gradients to
-bf16 (8 significant bits) and accumulates in fp32, so against float64 a
-forward pass agrees to about 1 % (relative L2) and gradients to a few %,
-with cosine similarity above 0.999 per layer.
+bf16 (8 significant bits) and accumulates in fp32.  Against float64 a
+forward pass agrees to about 1 % (relative L2).  The gradients of a batch
+whose residual is mostly noise are far more sensitive: storing the
+gradients in bf16 moves them by up to ~13 % (cosine 0.99) from exact
+float64 in the first layer, which the restatement shows by rounding where
+the device rounds (emulate=True).  So the device's gradients are held to
+that emulation within 3 % (cosine 0.999) per layer, and to exact float64
+within the emulation's own error.
 """
 
 import numpy as np
@@ -90,16 +95,27 @@ def test_forward_and_gradients_match_float64():
     loss_b = net.gradients(tp, tM, tU, norm)
     g = net.grad.cpu().numpy().astype(np.float64)
     loss_ref, g_ref = sr.loss_and_grad(params, pos, M, U, nrec, 1.0)
+    _, g_emu = sr.loss_and_grad(params, pos, M, U, nrec, 1.0, emulate=True)
     loss = float((loss_b / norm).mean().item())
     assert abs(loss - loss_ref) < 2e-2 * loss_ref, (loss, loss_ref)
     assert net.device_error() == 0
+
+    def cmp(x, y):
+        cos = float(x @ y / (np.linalg.norm(x) * np.linalg.norm(y) + 1e-300))
+        return cos, float(np.linalg.norm(x - y) / (np.linalg.norm(y) + 1e-300))
+
     for n, (a, b) in enumerate(net.lay.offsets):
         o = net.lay.layers[n][0]
         for name, sl in (("W", slice(a, b)), ("b", slice(b, b + o))):
-            x, y = g[sl], g_ref[sl]
-            cos = float(x @ y / (np.linalg.norm(x) * np.linalg.norm(y) + 1e-300))
-            rl = float(np.linalg.norm(x - y) / (np.linalg.norm(y) + 1e-300))
-            assert cos > 0.999 and rl < 5e-2, (n, name, cos, rl)
+            # the device against the restatement that rounds where it rounds:
+            # agreement up to the rare rounding flips fp32 sums cause
+            cos_e, rl_e = cmp(g[sl], g_emu[sl])
+            assert cos_e > 0.999 and rl_e < 3e-2, (n, name, "emulated", cos_e, rl_e)
+            # against exact float64: the error bf16 storage is designed to
+            # give (the emulation's own), no more
+            cos, rl = cmp(g[sl], g_ref[sl])
+            _, rl_design = cmp(g_emu[sl], g_ref[sl])
+            assert cos > 0.98 and rl <= 1.25 * rl_design + 2e-2, (n, name, cos, rl, rl_design)
 
 
 def test_training_fits_a_teacher():
