@@ -52,7 +52,8 @@ WORKLOADS = {"topo": dict(ni=400, nj=400, nk=200),
              "aniso": dict(ni=300, nj=300, nk=150),
              "visco": dict(ni=300, nj=300, nk=150),
              "flat": dict(ni=100, nj=100, nk=60),
-             "surrogate": dict(ni=256, nj=256, nk=128)}
+             "surrogate": dict(ni=256, nj=256, nk=128),
+             "surrogate_net": dict(ni=256, nj=256, nk=128)}
 SAMPLE_NK = 24                 # CPU sample: same model, 24 planes deep
 CPU_SAMPLE_S = 24.0            # target seconds of CPU work per baseline sample
 
@@ -951,6 +952,80 @@ def measured_peak_bf16():
         return 1900.0, "fallback"
 
 
+def run_surrogate_net(args):
+    """The surrogate network's device work alone (no solver shots): K training
+    steps at batch 256 on seeded synthetic targets, then K inference batches,
+    and the dominant product (the last decoder layer, 262,144 x 1152 x 640)
+    timed alone.  value = training steps/s; small enough to profile."""
+    import numpy as np
+    import torch
+    from cgfd3d_gb300 import surrogate as SG
+    torch.cuda.set_device(0)
+    B, K, W = 256, max(args.steps, 1), max(args.warmup, 0)
+    rng = np.random.default_rng(3)
+    net = SG.Surrogate(nrec=64, nt=1000, seed=1, scale=1.0)
+    pos = torch.from_numpy(rng.uniform(-1, 1, (B, 3)).astype(np.float32)).cuda()
+    M = torch.from_numpy(rng.standard_normal((B, 6)).astype(np.float32)).cuda()
+    U = torch.from_numpy(rng.standard_normal((B, 1000, 192)).astype(np.float32)).cuda()
+    norm = (U.double() ** 2).reshape(B, -1).sum(1).float()
+    for _ in range(W):
+        net.gradients(pos, M, U, norm)
+        net.apply()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = net.launches
+    e0.record()
+    for _ in range(K):
+        net.gradients(pos, M, U, norm)
+        net.apply()
+    e1.record()
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1) / K
+    train_launches = (net.launches - n0) // K
+    for _ in range(W):
+        net.predict(pos, M)
+    e0.record()
+    for _ in range(K):
+        net.predict(pos, M)
+    e1.record()
+    torch.cuda.synchronize()
+    inf_ms = e0.elapsed_time(e1) / K
+    lay = net.lay
+    d = net._buffers(B, False)
+    o, k = lay.dec[-1]
+    rows = B * lay.T
+    last = len(lay.dec) - 1
+    args_g = (d["a_d%d" % last], k, net.W(len(lay.layers) - 1), k, d["h_d%d" % last], o,
+              rows, o, k)
+    for _ in range(2):
+        net._gemm(*args_g)
+    e0.record()
+    for _ in range(10):
+        net._gemm(*args_g)
+    e1.record()
+    torch.cuda.synchronize()
+    g_ms = e0.elapsed_time(e1) / 10
+    achieved = 2.0 * rows * o * k / (g_ms * 1e-3) / 1e12
+    peak, peak_kind = measured_peak_bf16()
+    line = {
+        "metric": "surrogate training steps/s (batch 256)", "value": 1e3 / train_ms,
+        "unit": "steps/s", "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": train_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 (fp32 accumulation)", "data": "synthetic targets (seeded)",
+        "config": {"workload": "surrogate network alone: 5.5 M parameters, 64 receivers x 3 "
+                   "components x 1000 samples, batch 256", "parallelism": "single"},
+        "inference": {"ms_per_batch": inf_ms, "shots_per_s": B / (inf_ms * 1e-3)},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                     "kernel": "k_gemm_tn (last decoder layer, %d x %d x %d)" % (rows, o, k),
+                     "ms": g_ms},
+        "gpu_launches": train_launches,
+        "device_error": net.device_error(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_surrogate(args):
     """Learned surrogate (config 4).  Shots of the batched solver on the fixed
     256 x 256 x 128 crop of the topography model (sources uniform in the
@@ -1125,6 +1200,8 @@ def main():
         return run_media_bin(args)
     if args.workload == "surrogate":
         return run_surrogate(args)
+    if args.workload == "surrogate_net":
+        return run_surrogate_net(args)
     return run_ours(args)
 
 

@@ -11,7 +11,9 @@
  *
  *   warp 0, lane 0   producer: bulk tensor copies (cp.async.bulk.tensor,
  *                    128-byte swizzle) of the A and B tiles of each 64-wide
- *                    K block into a 4-stage shared-memory ring;
+ *                    K block into a 3-stage shared-memory ring (97 KiB, so
+ *                    two CTAs share an SM and one's epilogue overlaps the
+ *                    other's main loop);
  *   warp 1, lane 0   MMA issuer: four tcgen05.mma (M 128, N 128, K 16) per K
  *                    block, then tcgen05.commit to the stage's `empty`
  *                    barrier, which frees the stage when those MMAs are done;
@@ -42,7 +44,7 @@ __attribute__((visibility("hidden"))) int cgfd_set_error_msg(int code, const cha
 namespace sgg {
 
 constexpr int BM = 128, BN = 128, BK = 64;   /* BK: one 128-byte swizzle row of bf16 */
-constexpr int STAGES = 4;
+constexpr int STAGES = 3;
 constexpr int TILE_A = BM * BK * 2;          /* 16 KiB */
 constexpr int TILE_B = BN * BK * 2;          /* 16 KiB */
 constexpr int SMEM_BYTES = STAGES * (TILE_A + TILE_B) + 1024;   /* + alignment slack */
@@ -174,7 +176,7 @@ __device__ __forceinline__ float gelu(float x)
   return 0.5f * x * (1.0f + tanhf(u));
 }
 
-__global__ void __launch_bounds__(NTHREADS, 1)
+__global__ void __launch_bounds__(NTHREADS, 2)
     k_gemm_tn(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
               Epi e, int K, int kper)
 {

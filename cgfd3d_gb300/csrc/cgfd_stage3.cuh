@@ -419,17 +419,6 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
     const int pmask = (a.pml_fused && valid) ? pml_mask(k) : 0;
     if (a.pml_fused && valid && it + 1 < niter && pml_mask(k + 1))
       prefetch_aux<KIND>(a, i, j, k + 1, pml_mask(k + 1));
-    /* the auxiliaries of the point's first face are loaded now, before the
-     * waits and the interior operators, so that their latency overlaps that
-     * work (most face points lie in one face; the others load theirs in the
-     * face loop) */
-    const int f0 = pmask ? __ffs(pmask) - 1 : -1;
-    AuxPt<KIND> pax0;
-    if (f0 >= 0) {
-#pragma unroll
-      for (int f = 0; f < CGFD_NFACE; f++)
-        if (f == f0) load_aux<KIND>(a, f, aux_index<KIND>(a.face[f], i, j, k), pax0);
-    }
     /* every lane waits; the warp leaves together when any wait of the CTA
      * has run out */
     bool ok = *(volatile int *)&abort_s == 0;
@@ -562,8 +551,7 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
           if (!(pmask & (1 << f))) continue;
           const DevFace &F = a.face[f];
           AuxPt<KIND> pax;
-          if (f == f0) pax = pax0;
-          else load_aux<KIND>(a, f, aux_index<KIND>(F, i, j, k), pax);
+          load_aux<KIND>(a, f, aux_index<KIND>(F, i, j, k), pax);
           float d[9];
           if (f < 2) {
 #pragma unroll
