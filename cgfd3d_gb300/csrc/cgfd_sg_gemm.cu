@@ -328,6 +328,205 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   }
 }
 
+/* ---- persistent form for large products ---------------------------------
+ * One CTA per SM walks the output tiles (t = blockIdx.x, + gridDim.x, ...;
+ * the N tiles of a row of A are neighbours, so A is re-read from L2).  Six
+ * warps: warp 0 lane 0 the producer, warp 1 lane 0 the MMA issuer, warps 2-5
+ * the epilogue.  Two accumulators of 128 TMEM columns alternate between
+ * tiles: the MMAs of tile i+1 run while the epilogue reads tile i
+ * (tfull[a]: the MMAs of a tile are done; tempty[a]: its accumulator has
+ * been read).  The smem ring runs on across tiles.  Stores as k_gemm_tn
+ * (bf16 or fp32, no split along K). */
+constexpr int PSTAGES = 4;
+constexpr int P_SMEM_BYTES = PSTAGES * (TILE_A + TILE_B) + 1024;
+constexpr int P_THREADS = 192;
+constexpr uint32_t P_TMEM_COLS = 256;
+
+__global__ void __launch_bounds__(P_THREADS, 1)
+    k_gemm_tn_p(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+                Epi e, int K, int ntn, int ntiles)
+{
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full[PSTAGES], empty[PSTAGES], tfull[2], tempty[2], done;
+  __shared__ uint32_t tmem_sh;
+  __shared__ int abort_sh;
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *sA = smem, *sB = smem + PSTAGES * TILE_A;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nkb = (K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < PSTAGES; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int a = 0; a < 2; a++) {
+      mbar_init(&tfull[a], 1);
+      mbar_init(&tempty[a], 4);
+    }
+    mbar_init(&done, 1);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_sh)),
+                 "r"(P_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_sh;
+  auto live = [&]() { return *(volatile int *)&abort_sh == 0; };
+
+  if (warp == 0 && lane == 0) {
+    /* producer; last[s]: the latest ring position issued into stage s */
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb)) : "memory");
+    int last[PSTAGES];
+#pragma unroll
+    for (int s = 0; s < PSTAGES; s++) last[s] = -1;
+    int g = 0;
+    for (int t = blockIdx.x; t < ntiles && live(); t += gridDim.x) {
+      const int m0 = (t / ntn) * BM, n0 = (t % ntn) * BN;
+      for (int kb = 0; kb < nkb; kb++, g++) {
+        const int s = g % PSTAGES;
+        if (g >= PSTAGES && !mbar_wait(&empty[s], ((g / PSTAGES) - 1) & 1, WAIT_LIMIT)) {
+          atomicOr(e.err, 1);
+          abort_sh = 1;
+        }
+        if (!live()) break;
+        mbar_expect_tx(&full[s], TILE_A + TILE_B);
+        tma_2d(sA + s * TILE_A, &ta, kb * BK, m0, &full[s]);
+        tma_2d(sB + s * TILE_B, &tb, kb * BK, n0, &full[s]);
+        last[s] = g;
+      }
+    }
+    if (!live()) {
+      /* the CTA leaves only after its copies have landed */
+#pragma unroll
+      for (int s = 0; s < PSTAGES; s++)
+        if (last[s] >= 0) mbar_wait(&full[s], (last[s] / PSTAGES) & 1, WAIT_LIMIT);
+    }
+  } else if (warp == 1 && lane == 0) {
+    /* MMA issuer */
+    int g = 0, i = 0;
+    for (int t = blockIdx.x; t < ntiles && live(); t += gridDim.x, i++) {
+      const int acc = i & 1;
+      if (i >= 2 && !mbar_wait(&tempty[acc], ((i / 2) - 1) & 1, WAIT_LIMIT)) {
+        atomicOr(e.err, 2);
+        abort_sh = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t d = tmem + (uint32_t)(acc * BN);
+      bool ok = true;
+      for (int kb = 0; kb < nkb; kb++, g++) {
+        const int s = g % PSTAGES;
+        if (!mbar_wait(&full[s], (g / PSTAGES) & 1, WAIT_LIMIT)) {
+          atomicOr(e.err, 2);
+          abort_sh = 1;
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(sA + s * TILE_A), b0 = smem_u32(sB + s * TILE_B);
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; kk++)
+          umma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+        umma_commit(&empty[s]);
+      }
+      if (!ok) break;
+      umma_commit(&tfull[acc]);
+    }
+    /* every MMA issued has finished before TMEM is freed */
+    umma_commit(&done);
+    mbar_wait(&done, 0, WAIT_LIMIT);
+  } else if (warp >= 2) {
+    /* epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 */
+    const int q = warp & 3;
+    int i = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
+      const int acc = i & 1;
+      bool have = live() && mbar_wait(&tfull[acc], (i / 2) & 1, WAIT_LIMIT);
+      have = __all_sync(0xffffffffu, have);
+      if (!have) {
+        if (lane == 0) {
+          atomicOr(e.err, 4);
+          abort_sh = 1;
+        }
+        break;
+      }
+      tc_fence_after();
+      const int m0 = (t / ntn) * BM, n0 = (t % ntn) * BN;
+      const int row = m0 + q * 32 + lane;
+      const uint32_t tl = tmem + (uint32_t)(acc * BN) + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        tmem_ld32(tl + c0, r);
+        const int col0 = n0 + c0;
+        if (row >= e.M || col0 >= e.N) continue;
+        float v[32];
+#pragma unroll
+        for (int u = 0; u < 32; u++) {
+          v[u] = __uint_as_float(r[u]) * e.alpha;
+          if (e.bias && col0 + u < e.N) v[u] += e.bias[col0 + u];
+        }
+        const bool full_row = col0 + 32 <= e.N;
+        if (e.mode == CGFD_SG_OUT_BF16) {
+          __nv_bfloat16 *C = (__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0;
+          __nv_bfloat16 *Z = e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr;
+          __align__(16) __nv_bfloat16 h[32], z[32];
+#pragma unroll
+          for (int u = 0; u < 32; u++) {
+            z[u] = __float2bfloat16_rn(v[u]);
+            h[u] = e.act == CGFD_SG_ACT_GELU ? __float2bfloat16_rn(gelu(v[u])) : z[u];
+          }
+          if (full_row) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              reinterpret_cast<uint4 *>(C)[u] = reinterpret_cast<const uint4 *>(h)[u];
+              if (Z) reinterpret_cast<uint4 *>(Z)[u] = reinterpret_cast<const uint4 *>(z)[u];
+            }
+          } else {
+            for (int u = 0; u < 32 && col0 + u < e.N; u++) {
+              C[u] = h[u];
+              if (Z) Z[u] = z[u];
+            }
+          }
+        } else {
+          float *C = (float *)e.C + (long long)row * e.ldc + col0;
+          if (full_row) {
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+              reinterpret_cast<float4 *>(C)[u] =
+                  make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+          } else {
+            for (int u = 0; u < 32 && col0 + u < e.N; u++) C[u] = v[u];
+          }
+        }
+      }
+      /* this warp's lanes of the accumulator are read: hand it back */
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(
+                                      smem_u32(&tempty[acc]))
+                                  : "memory");
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(P_TMEM_COLS)
+                 : "memory");
+  }
+}
+
 typedef CUresult (*encode_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                               const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
                               const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -402,10 +601,16 @@ extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long lo
   const int kper = ((nkb + splits - 1) / splits) * BK;
   const int nz = (K + kper - 1) / kper;
   static bool attr = false;
+  static int nsm = 0;
   if (!attr) {
+    int dev = 0;
     if (cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             SMEM_BYTES) != cudaSuccess)
-      return gemm_err(CGFD_ECUDA, "sg_gemm: shared memory attribute");
+                             SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(k_gemm_tn_p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             P_SMEM_BYTES) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return gemm_err(CGFD_ECUDA, "sg_gemm: kernel attributes");
     attr = true;
   }
   Epi e;
@@ -419,8 +624,16 @@ extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long lo
   e.M = M;
   e.N = N;
   e.err = d_err;
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, nz);
-  k_gemm_tn<<<grid, NTHREADS, SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, kper);
+  const int ntn = (N + BN - 1) / BN, ntm = (M + BM - 1) / BM;
+  const long long ntiles = (long long)ntn * ntm;
+  if (nz == 1 && mode != CGFD_SG_OUT_F32_ADD && ntiles >= 2LL * nsm && ntiles < (1LL << 31)) {
+    /* large products: one persistent CTA per SM, epilogue overlapped */
+    k_gemm_tn_p<<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, ntn,
+                                                                        (int)ntiles);
+  } else {
+    dim3 grid(ntn, ntm, nz);
+    k_gemm_tn<<<grid, NTHREADS, SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, kper);
+  }
   const cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return gemm_err(CGFD_ECUDA, "sg_gemm launch: %s", cudaGetErrorString(err));
   return 0;

@@ -28,7 +28,10 @@ def _sglib():
 
 
 @pytest.mark.parametrize("M,N,K", [(256, 384, 640), (200, 136, 72), (8, 1152, 640),
-                                   (1024, 128, 1024)])
+                                   (1024, 128, 1024),
+                                   # at least two output tiles per SM: the
+                                   # persistent form (not for the split-K mode)
+                                   (32768, 1152, 640), (40000, 200, 136)])
 def test_gemm_modes_match_torch(M, N, K):
     import ctypes as C
     import torch
