@@ -330,16 +330,19 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 
 /* ---- persistent form for large products ---------------------------------
  * One CTA per SM walks the output tiles (t = blockIdx.x, + gridDim.x, ...;
- * the N tiles of a row of A are neighbours, so A is re-read from L2).  Six
- * warps: warp 0 lane 0 the producer, warp 1 lane 0 the MMA issuer, warps 2-5
- * the epilogue.  Two accumulators of 128 TMEM columns alternate between
+ * the N tiles of a row of A are neighbours, so A is re-read from L2).  Ten
+ * warps: warp 0 lane 0 the producer, warp 1 lane 0 the MMA issuer, warps 2-9
+ * the epilogue (two per TMEM lane quarter, each taking half of the tile's
+ * columns, since one tile's epilogue outlasts the next tile's MMAs).  Two
+ * accumulators of 128 TMEM columns alternate between
  * tiles: the MMAs of tile i+1 run while the epilogue reads tile i
  * (tfull[a]: the MMAs of a tile are done; tempty[a]: its accumulator has
  * been read).  The smem ring runs on across tiles.  Stores as k_gemm_tn
  * (bf16 or fp32, no split along K). */
 constexpr int PSTAGES = 4;
 constexpr int P_SMEM_BYTES = PSTAGES * (TILE_A + TILE_B) + 1024;
-constexpr int P_THREADS = 192;
+constexpr int P_THREADS = 320;
+constexpr int P_EPI_WARPS = 8;
 constexpr uint32_t P_TMEM_COLS = 256;
 
 __global__ void __launch_bounds__(P_THREADS, 1)
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     }
     for (int a = 0; a < 2; a++) {
       mbar_init(&tfull[a], 1);
-      mbar_init(&tempty[a], 4);
+      mbar_init(&tempty[a], P_EPI_WARPS);
     }
     mbar_init(&done, 1);
     abort_sh = 0;
@@ -445,8 +448,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     umma_commit(&done);
     mbar_wait(&done, 0, WAIT_LIMIT);
   } else if (warp >= 2) {
-    /* epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 */
-    const int q = warp & 3;
+    /* epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns
+     * half * 64 .. + 63 */
+    const int q = warp & 3, half = (warp - 2) >> 2;
     int i = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
       const int acc = i & 1;
@@ -464,7 +468,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       const int row = m0 + q * 32 + lane;
       const uint32_t tl = tmem + (uint32_t)(acc * BN) + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
         uint32_t r[32];
         tmem_ld32(tl + c0, r);
         const int col0 = n0 + c0;
