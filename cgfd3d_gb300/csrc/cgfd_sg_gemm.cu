@@ -5,9 +5,11 @@
  *   C[M, N] = alpha * A[M, K] . B[N, K]^T   (+ bias[N], optional GELU)
  *
  * A and B are bf16, row-major with K contiguous ("K-major" for both
- * operands); the product accumulates in FP32 in tensor memory (TMEM).  One
- * CTA computes one 128 x 128 tile of C (or, split along K, its share of
- * one), with four warps:
+ * operands); the product accumulates in FP32 in tensor memory (TMEM).
+ * Products with at least two 128 x 128 output tiles per SM (and no split
+ * along K) run in the persistent form k_gemm_tn_p further down; the others
+ * in k_gemm_tn, where one CTA computes one 128 x 128 tile of C (or, split
+ * along K, its share of one), with four warps:
  *
  *   warp 0, lane 0   producer: bulk tensor copies (cp.async.bulk.tensor,
  *                    128-byte swizzle) of the A and B tiles of each 64-wide
@@ -333,17 +335,21 @@ __global__ void __launch_bounds__(NTHREADS, 2)
  * the N tiles of a row of A are neighbours, so A is re-read from L2).  Ten
  * warps: warp 0 lane 0 the producer, warp 1 lane 0 the MMA issuer, warps 2-9
  * the epilogue (two per TMEM lane quarter, each taking half of the tile's
- * columns, since one tile's epilogue outlasts the next tile's MMAs).  Two
+ * columns, since one tile's epilogue outlasts the next tile's MMAs).  A tile
+ * is 256 x 128: two M-128 MMAs per K step share the B tile, so each B tile
+ * fetched from L2 serves twice the output of k_gemm_tn.  Two
  * accumulators of 128 TMEM columns alternate between
  * tiles: the MMAs of tile i+1 run while the epilogue reads tile i
  * (tfull[a]: the MMAs of a tile are done; tempty[a]: its accumulator has
  * been read).  The smem ring runs on across tiles.  Stores as k_gemm_tn
  * (bf16 or fp32, no split along K). */
 constexpr int PSTAGES = 4;
-constexpr int P_SMEM_BYTES = PSTAGES * (TILE_A + TILE_B) + 1024;
+constexpr int PBM = 2 * BM;                  /* 256-row tiles: two M-128 MMAs share B */
+constexpr int P_STAGE = 2 * TILE_A + TILE_B; /* 48 KiB */
+constexpr int P_SMEM_BYTES = PSTAGES * P_STAGE + 1024;
 constexpr int P_THREADS = 320;
 constexpr int P_EPI_WARPS = 8;
-constexpr uint32_t P_TMEM_COLS = 256;
+constexpr uint32_t P_TMEM_COLS = 512;   /* 2 accumulators x 2 halves x 128 */
 
 __global__ void __launch_bounds__(P_THREADS, 1)
     k_gemm_tn_p(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
@@ -354,7 +360,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  uint8_t *sA = smem, *sB = smem + PSTAGES * TILE_A;
+  /* stage s: A rows 0-127, A rows 128-255, B, each a 128 x 64 tile */
+  auto stA = [&](int s, int h) { return smem + s * P_STAGE + h * TILE_A; };
+  auto stB = [&](int s) { return smem + s * P_STAGE + 2 * TILE_A; };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nkb = (K + BK - 1) / BK;
 
@@ -393,7 +401,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     for (int s = 0; s < PSTAGES; s++) last[s] = -1;
     int g = 0;
     for (int t = blockIdx.x; t < ntiles && live(); t += gridDim.x) {
-      const int m0 = (t / ntn) * BM, n0 = (t % ntn) * BN;
+      const int m0 = (t / ntn) * PBM, n0 = (t % ntn) * BN;
       for (int kb = 0; kb < nkb; kb++, g++) {
         const int s = g % PSTAGES;
         if (g >= PSTAGES && !mbar_wait(&empty[s], ((g / PSTAGES) - 1) & 1, WAIT_LIMIT)) {
@@ -401,9 +409,10 @@ __global__ void __launch_bounds__(P_THREADS, 1)
           abort_sh = 1;
         }
         if (!live()) break;
-        mbar_expect_tx(&full[s], TILE_A + TILE_B);
-        tma_2d(sA + s * TILE_A, &ta, kb * BK, m0, &full[s]);
-        tma_2d(sB + s * TILE_B, &tb, kb * BK, n0, &full[s]);
+        mbar_expect_tx(&full[s], P_STAGE);
+        tma_2d(stA(s, 0), &ta, kb * BK, m0, &full[s]);
+        tma_2d(stA(s, 1), &ta, kb * BK, m0 + BM, &full[s]);
+        tma_2d(stB(s), &tb, kb * BK, n0, &full[s]);
         last[s] = g;
       }
     }
@@ -424,7 +433,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         break;
       }
       tc_fence_after();
-      const uint32_t d = tmem + (uint32_t)(acc * BN);
+      const uint32_t d = tmem + (uint32_t)(acc * 2 * BN);
       bool ok = true;
       for (int kb = 0; kb < nkb; kb++, g++) {
         const int s = g % PSTAGES;
@@ -435,10 +444,13 @@ __global__ void __launch_bounds__(P_THREADS, 1)
           break;
         }
         tc_fence_after();
-        const uint32_t a0 = smem_u32(sA + s * TILE_A), b0 = smem_u32(sB + s * TILE_B);
+        const uint32_t a0 = smem_u32(stA(s, 0)), a1 = smem_u32(stA(s, 1));
+        const uint32_t b0 = smem_u32(stB(s));
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; kk++)
+        for (int kk = 0; kk < BK / 16; kk++) {
           umma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+          umma(d + BN, sdesc(a1 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+        }
         umma_commit(&empty[s]);
       }
       if (!ok) break;
@@ -448,8 +460,8 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     umma_commit(&done);
     mbar_wait(&done, 0, WAIT_LIMIT);
   } else if (warp >= 2) {
-    /* epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, columns
-     * half * 64 .. + 63 */
+    /* epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 of the
+     * accumulator half h = (w - 2) / 4, i.e. rows h 128 + 32 (w % 4) .. */
     const int q = warp & 3, half = (warp - 2) >> 2;
     int i = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
@@ -464,11 +476,11 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         break;
       }
       tc_fence_after();
-      const int m0 = (t / ntn) * BM, n0 = (t % ntn) * BN;
-      const int row = m0 + q * 32 + lane;
-      const uint32_t tl = tmem + (uint32_t)(acc * BN) + ((uint32_t)(q * 32) << 16);
+      const int m0 = (t / ntn) * PBM, n0 = (t % ntn) * BN;
+      const int row = m0 + half * BM + q * 32 + lane;
+      const uint32_t tl = tmem + (uint32_t)(acc * 2 * BN + half * BN) + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
+      for (int c0 = 0; c0 < BN; c0 += 32) {
         uint32_t r[32];
         tmem_ld32(tl + c0, r);
         const int col0 = n0 + c0;
@@ -629,11 +641,12 @@ extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long lo
   e.N = N;
   e.err = d_err;
   const int ntn = (N + BN - 1) / BN, ntm = (M + BM - 1) / BM;
-  const long long ntiles = (long long)ntn * ntm;
-  if (nz == 1 && mode != CGFD_SG_OUT_F32_ADD && ntiles >= 2LL * nsm && ntiles < (1LL << 31)) {
-    /* large products: one persistent CTA per SM, epilogue overlapped */
+  const long long ptiles = (long long)ntn * ((M + PBM - 1) / PBM);
+  if (nz == 1 && mode != CGFD_SG_OUT_F32_ADD && ptiles >= 2LL * nsm && ptiles < (1LL << 31)) {
+    /* large products: one persistent CTA per SM, 256-row tiles, epilogue
+     * overlapped */
     k_gemm_tn_p<<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, ntn,
-                                                                        (int)ntiles);
+                                                                        (int)ptiles);
   } else {
     dim3 grid(ntn, ntm, nz);
     k_gemm_tn<<<grid, NTHREADS, SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, kper);
