@@ -425,16 +425,22 @@ def run_ours(args):
         torch.distributed.barrier()
     # three end-to-end runs of the same problem (each from host buffers to
     # host buffers), the median reported: host-side copies vary from run to run
-    reps = []
+    reps, phases = [], []
     for _ in range(3):
         t0 = time.perf_counter()
         se = solver.Solver(q)
+        t1 = time.perf_counter()
         se.run(q.nt_total)
+        t2 = time.perf_counter()
         se.fetch()
+        t3 = time.perf_counter()
         h2d, d2h = se.transfer_bytes()
         se.close()
-        reps.append(time.perf_counter() - t0)
+        t4 = time.perf_counter()
+        reps.append(t4 - t0)
+        phases.append({"create": t1 - t0, "run": t2 - t1, "fetch": t3 - t2, "close": t4 - t3})
     t_e2e = sorted(reps)[1]
+    mid = phases[reps.index(t_e2e)]
     if world > 1:
         tt = torch.tensor([t_e2e], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -470,7 +476,8 @@ def run_ours(args):
                 "h2d_bytes_per_step": h2d / q.nt_total,
                 "d2h_bytes_per_step": d2h / q.nt_total,
                 "steps": q.nt_total, "runs_ms": [1e3 * t for t in reps],
-                "reported": "median of 3 runs"},
+                "reported": "median of 3 runs",
+                "phases_ms": {k: 1e3 * v for k, v in mid.items()}},
         "gpu_launches": n_all,
         "clocks": clocks,
     }
@@ -1017,7 +1024,8 @@ def run_surrogate_net(args):
         "inference": {"ms_per_batch": inf_ms, "shots_per_s": B / (inf_ms * 1e-3)},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "kernel": "k_gemm_tn (last decoder layer, %d x %d x %d)" % (rows, o, k),
+                     "kernel": "k_gemm_tn_p (persistent form, 256 x 128 tiles; last decoder "
+                               "layer, %d x %d x %d)" % (rows, o, k),
                      "ms": g_ms},
         "gpu_launches": train_launches,
         "device_error": net.device_error(),

@@ -6,7 +6,7 @@
  *
  * A and B are bf16, row-major with K contiguous ("K-major" for both
  * operands); the product accumulates in FP32 in tensor memory (TMEM).
- * Products with at least two 128 x 128 output tiles per SM (and no split
+ * Products with at least two 256 x 128 output tiles per SM (and no split
  * along K) run in the persistent form k_gemm_tn_p further down; the others
  * in k_gemm_tn, where one CTA computes one 128 x 128 tile of C (or, split
  * along K, its share of one), with four warps:
@@ -334,11 +334,11 @@ __global__ void __launch_bounds__(NTHREADS, 2)
  * One CTA per SM walks the output tiles (t = blockIdx.x, + gridDim.x, ...;
  * the N tiles of a row of A are neighbours, so A is re-read from L2).  Ten
  * warps: warp 0 lane 0 the producer, warp 1 lane 0 the MMA issuer, warps 2-9
- * the epilogue (two per TMEM lane quarter, each taking half of the tile's
- * columns, since one tile's epilogue outlasts the next tile's MMAs).  A tile
- * is 256 x 128: two M-128 MMAs per K step share the B tile, so each B tile
- * fetched from L2 serves twice the output of k_gemm_tn.  Two
- * accumulators of 128 TMEM columns alternate between
+ * the epilogue (warp w reads TMEM lane quarter w & 3 of the 128-row half
+ * (w - 2) >> 2 of the tile).  A tile is 256 x 128: two M-128 MMAs per K
+ * step share the B tile, so each B tile fetched from L2 serves twice the
+ * output of k_gemm_tn.  Two accumulators of 256 TMEM columns (128 per
+ * half) alternate between
  * tiles: the MMAs of tile i+1 run while the epilogue reads tile i
  * (tfull[a]: the MMAs of a tile are done; tempty[a]: its accumulator has
  * been read).  The smem ring runs on across tiles.  Stores as k_gemm_tn

@@ -75,7 +75,7 @@ struct SetupTrace {
     if (!on) return;
     cudaStreamSynchronize(st);
     double t = now();
-    fprintf(stderr, "cgfd setup: %-28s %8.2f ms\n", what, 1e3 * (t - t0));
+    fprintf(stderr, "cgfd trace: %-28s %8.2f ms\n", what, 1e3 * (t - t0));
     t0 = t;
   }
 };
@@ -1961,9 +1961,12 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
   size_t L = level_floats(s);
   int host_lev = (s->step % 2 == 1) ? 3 : 0;
   size_t hvol = (size_t)p->nx * p->ny * p->nz;
+  SetupTrace tr;
+  tr.start(s->stream);
   for (int c = 0; c < s->ncmp; c++)
     CK(download_volume(s, p->wav + (size_t)host_lev * s->ncmp * hvol + c * hvol,
                        s->wav + s->pre_lev * L + c * s->g.vol));
+  tr.mark("fetch wavefield");
   for (int d = 0; d < 3; d++)
     for (int sd = 0; sd < 2; sd++) {
       int f = d * 2 + sd;
@@ -1992,6 +1995,7 @@ extern "C" int cgfd_solver_fetch(cgfd_solver_t *s)
     s->d2h_bytes += nb;
   }
   CK(cudaStreamSynchronize(s->stream));
+  tr.mark("fetch PML, seismograms");
   return 0;
 }
 
