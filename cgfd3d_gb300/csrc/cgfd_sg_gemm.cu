@@ -6,8 +6,9 @@
  *
  * A and B are bf16, row-major with K contiguous ("K-major" for both
  * operands); the product accumulates in FP32 in tensor memory (TMEM).
- * Products with at least two 256 x 128 output tiles per SM (and no split
- * along K) run in the persistent form k_gemm_tn_p further down; the others
+ * Products with at least two 32768-output tiles (128 x 256 or 256 x 128)
+ * per SM (and no split along K) run in the persistent form k_gemm_tn_p
+ * further down; the others
  * in k_gemm_tn, where one CTA computes one 128 x 128 tile of C (or, split
  * along K, its share of one), with four warps:
  *
@@ -132,15 +133,21 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr)
 /* instruction descriptor of kind::f16: D fp32 (bits 4-5 = 1), A and B bf16
  * (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit
  * 17, M >> 4 at bit 24 */
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t idesc_mn(int m, int n)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+constexpr uint32_t IDESC = idesc_mn(BM, BN);           /* M 128, N 128 */
+constexpr uint32_t IDESC_N256 = idesc_mn(BM, 2 * BN);  /* M 128, N 256 */
 
-__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc)
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc,
+                                     uint32_t idesc = IDESC)
 {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
 
@@ -176,6 +183,43 @@ __device__ __forceinline__ float gelu(float x)
 {
   const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
   return 0.5f * x * (1.0f + tanhf(u));
+}
+
+/* two floats as a bf16 pair in one register (a at the lower address) */
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+  __nv_bfloat162 t = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t *>(&t);
+}
+
+/* 32 consecutive outputs of one row as bf16: C = act(v), Z = v (Z may be
+ * null); `n` of them lie inside the product (32: one full, aligned run) */
+__device__ __forceinline__ void store_bf16_32(__nv_bfloat16 *C, __nv_bfloat16 *Z,
+                                              const float *v, int act, int n)
+{
+  if (n >= 32) {
+    uint32_t hp[16], zp[16];
+#pragma unroll
+    for (int u = 0; u < 16; u++) {
+      zp[u] = pack_bf16(v[2 * u], v[2 * u + 1]);
+      hp[u] = act == CGFD_SG_ACT_GELU ? pack_bf16(gelu(v[2 * u]), gelu(v[2 * u + 1])) : zp[u];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      reinterpret_cast<uint4 *>(C)[u] = make_uint4(hp[4 * u], hp[4 * u + 1], hp[4 * u + 2],
+                                                   hp[4 * u + 3]);
+      if (Z)
+        reinterpret_cast<uint4 *>(Z)[u] = make_uint4(zp[4 * u], zp[4 * u + 1], zp[4 * u + 2],
+                                                     zp[4 * u + 3]);
+    }
+  } else {
+#pragma unroll
+    for (int u = 0; u < 32; u++) {
+      if (u >= n) continue;
+      C[u] = __float2bfloat16_rn(act == CGFD_SG_ACT_GELU ? gelu(v[u]) : v[u]);
+      if (Z) Z[u] = __float2bfloat16_rn(v[u]);
+    }
+  }
 }
 
 __global__ void __launch_bounds__(NTHREADS, 2)
@@ -285,26 +329,8 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     }
     const bool full_row = col0 + 32 <= e.N;
     if (e.mode == CGFD_SG_OUT_BF16) {
-      __nv_bfloat16 *C = (__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0;
-      __nv_bfloat16 *Z = e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr;
-      __align__(16) __nv_bfloat16 h[32], z[32];
-#pragma unroll
-      for (int t = 0; t < 32; t++) {
-        z[t] = __float2bfloat16_rn(v[t]);
-        h[t] = e.act == CGFD_SG_ACT_GELU ? __float2bfloat16_rn(gelu(v[t])) : z[t];
-      }
-      if (full_row) {
-#pragma unroll
-        for (int t = 0; t < 4; t++) {
-          reinterpret_cast<uint4 *>(C)[t] = reinterpret_cast<const uint4 *>(h)[t];
-          if (Z) reinterpret_cast<uint4 *>(Z)[t] = reinterpret_cast<const uint4 *>(z)[t];
-        }
-      } else {
-        for (int t = 0; t < 32 && col0 + t < e.N; t++) {
-          C[t] = h[t];
-          if (Z) Z[t] = z[t];
-        }
-      }
+      store_bf16_32((__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0,
+                    e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr, v, e.act, e.N - col0);
     } else if (e.mode == CGFD_SG_OUT_F32) {
       float *C = (float *)e.C + (long long)row * e.ldc + col0;
       if (full_row) {
@@ -313,11 +339,15 @@ __global__ void __launch_bounds__(NTHREADS, 2)
           reinterpret_cast<float4 *>(C)[t] = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2],
                                                          v[4 * t + 3]);
       } else {
-        for (int t = 0; t < 32 && col0 + t < e.N; t++) C[t] = v[t];
+#pragma unroll
+        for (int t = 0; t < 32; t++)
+          if (col0 + t < e.N) C[t] = v[t];
       }
     } else {
       float *C = (float *)e.C + (long long)row * e.ldc + col0;
-      for (int t = 0; t < 32 && col0 + t < e.N; t++) atomicAdd(C + t, v[t]);
+#pragma unroll
+      for (int t = 0; t < 32; t++)
+        if (col0 + t < e.N) atomicAdd(C + t, v[t]);
     }
   }
   tc_fence_before();
@@ -334,35 +364,45 @@ __global__ void __launch_bounds__(NTHREADS, 2)
  * One CTA per SM walks the output tiles (t = blockIdx.x, + gridDim.x, ...;
  * the N tiles of a row of A are neighbours, so A is re-read from L2).  Ten
  * warps: warp 0 lane 0 the producer, warp 1 lane 0 the MMA issuer, warps 2-9
- * the epilogue (warp w reads TMEM lane quarter w & 3 of the 128-row half
- * (w - 2) >> 2 of the tile).  A tile is 256 x 128: two M-128 MMAs per K
- * step share the B tile, so each B tile fetched from L2 serves twice the
- * output of k_gemm_tn.  Two accumulators of 256 TMEM columns (128 per
- * half) alternate between
+ * the epilogue.  Two tile forms, each 32768 outputs and 48 KiB of operands
+ * per K block:
+ *   WIDE (N > 128)   128 x 256: one M 128 x N 256 MMA per K step (the
+ *                    tensor pipe does twice the work per cycle at N 256
+ *                    than at N 128); a last tile of at most 128 columns
+ *                    loads one B box and issues N 128;
+ *   narrow (N <= 128) 256 x 128: two M-128 MMAs per K step share the B tile.
+ * Epilogue warp w reads TMEM lane quarter w & 3 of the 128-column (WIDE) or
+ * 128-row (narrow) half (w - 2) >> 2 of the tile.  Two accumulators of 256
+ * TMEM columns alternate between
  * tiles: the MMAs of tile i+1 run while the epilogue reads tile i
  * (tfull[a]: the MMAs of a tile are done; tempty[a]: its accumulator has
  * been read).  The smem ring runs on across tiles.  Stores as k_gemm_tn
  * (bf16 or fp32, no split along K). */
 constexpr int PSTAGES = 4;
-constexpr int PBM = 2 * BM;                  /* 256-row tiles: two M-128 MMAs share B */
-constexpr int P_STAGE = 2 * TILE_A + TILE_B; /* 48 KiB */
+constexpr int P_STAGE = 2 * TILE_A + TILE_B; /* 48 KiB (TILE_A == TILE_B) */
 constexpr int P_SMEM_BYTES = PSTAGES * P_STAGE + 1024;
 constexpr int P_THREADS = 320;
 constexpr int P_EPI_WARPS = 8;
 constexpr uint32_t P_TMEM_COLS = 512;   /* 2 accumulators x 2 halves x 128 */
 
+template <bool WIDE>
 __global__ void __launch_bounds__(P_THREADS, 1)
     k_gemm_tn_p(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
                 Epi e, int K, int ntn, int ntiles)
 {
+  constexpr int TM = WIDE ? BM : 2 * BM, TN = WIDE ? 2 * BN : BN;
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full[PSTAGES], empty[PSTAGES], tfull[2], tempty[2], done;
   __shared__ uint32_t tmem_sh;
   __shared__ int abort_sh;
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  /* stage s: A rows 0-127, A rows 128-255, B, each a 128 x 64 tile */
+  /* stage s, each a 128 x 64 tile: narrow A rows 0-127, A rows 128-255, B;
+   * WIDE A, B rows 0-127, B rows 128-255 (one 256-row K-major operand) */
   auto stA = [&](int s, int h) { return smem + s * P_STAGE + h * TILE_A; };
-  auto stB = [&](int s) { return smem + s * P_STAGE + 2 * TILE_A; };
+  auto stB = [&](int s) { return smem + s * P_STAGE + (WIDE ? TILE_A : 2 * TILE_A); };
+  /* B boxes of the tile at column n0: a WIDE tile's second box only where
+   * columns beyond n0 + 128 exist */
+  auto nbox = [&](int n0) { return WIDE && e.N - n0 > BN ? 2 : 1; };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nkb = (K + BK - 1) / BK;
 
@@ -401,7 +441,8 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     for (int s = 0; s < PSTAGES; s++) last[s] = -1;
     int g = 0;
     for (int t = blockIdx.x; t < ntiles && live(); t += gridDim.x) {
-      const int m0 = (t / ntn) * PBM, n0 = (t % ntn) * BN;
+      const int m0 = (t / ntn) * TM, n0 = (t % ntn) * TN;
+      const int nb = nbox(n0);
       for (int kb = 0; kb < nkb; kb++, g++) {
         const int s = g % PSTAGES;
         if (g >= PSTAGES && !mbar_wait(&empty[s], ((g / PSTAGES) - 1) & 1, WAIT_LIMIT)) {
@@ -409,10 +450,17 @@ __global__ void __launch_bounds__(P_THREADS, 1)
           abort_sh = 1;
         }
         if (!live()) break;
-        mbar_expect_tx(&full[s], P_STAGE);
-        tma_2d(stA(s, 0), &ta, kb * BK, m0, &full[s]);
-        tma_2d(stA(s, 1), &ta, kb * BK, m0 + BM, &full[s]);
-        tma_2d(stB(s), &tb, kb * BK, n0, &full[s]);
+        if (WIDE) {
+          mbar_expect_tx(&full[s], TILE_A + nb * TILE_B);
+          tma_2d(stA(s, 0), &ta, kb * BK, m0, &full[s]);
+          tma_2d(stB(s), &tb, kb * BK, n0, &full[s]);
+          if (nb == 2) tma_2d(stB(s) + TILE_B, &tb, kb * BK, n0 + BN, &full[s]);
+        } else {
+          mbar_expect_tx(&full[s], P_STAGE);
+          tma_2d(stA(s, 0), &ta, kb * BK, m0, &full[s]);
+          tma_2d(stA(s, 1), &ta, kb * BK, m0 + BM, &full[s]);
+          tma_2d(stB(s), &tb, kb * BK, n0, &full[s]);
+        }
         last[s] = g;
       }
     }
@@ -434,6 +482,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       }
       tc_fence_after();
       const uint32_t d = tmem + (uint32_t)(acc * 2 * BN);
+      const uint32_t idesc = nbox((t % ntn) * TN) == 2 ? IDESC_N256 : IDESC;
       bool ok = true;
       for (int kb = 0; kb < nkb; kb++, g++) {
         const int s = g % PSTAGES;
@@ -448,8 +497,12 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         const uint32_t b0 = smem_u32(stB(s));
 #pragma unroll
         for (int kk = 0; kk < BK / 16; kk++) {
-          umma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
-          umma(d + BN, sdesc(a1 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+          if (WIDE) {
+            umma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0, idesc);
+          } else {
+            umma(d, sdesc(a0 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+            umma(d + BN, sdesc(a1 + kk * 32), sdesc(b0 + kk * 32), (kb | kk) != 0);
+          }
         }
         umma_commit(&empty[s]);
       }
@@ -461,7 +514,8 @@ __global__ void __launch_bounds__(P_THREADS, 1)
     mbar_wait(&done, 0, WAIT_LIMIT);
   } else if (warp >= 2) {
     /* epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 of the
-     * accumulator half h = (w - 2) / 4, i.e. rows h 128 + 32 (w % 4) .. */
+     * accumulator half h = (w - 2) / 4: rows 32 (w % 4) .. of columns
+     * h 128 .. (WIDE), rows h 128 + 32 (w % 4) .. (narrow) */
     const int q = warp & 3, half = (warp - 2) >> 2;
     int i = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
@@ -476,15 +530,17 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         break;
       }
       tc_fence_after();
-      const int m0 = (t / ntn) * PBM, n0 = (t % ntn) * BN;
-      const int row = m0 + half * BM + q * 32 + lane;
+      const int m0 = (t / ntn) * TM + (WIDE ? 0 : half * BM);
+      const int n0 = (t % ntn) * TN + (WIDE ? half * BN : 0);
+      const int row = m0 + q * 32 + lane;
       const uint32_t tl = tmem + (uint32_t)(acc * 2 * BN + half * BN) + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
+        const int col0 = n0 + c0;
+        if (col0 >= e.N) break;            /* warp-uniform: nothing left of this half */
         uint32_t r[32];
         tmem_ld32(tl + c0, r);
-        const int col0 = n0 + c0;
-        if (row >= e.M || col0 >= e.N) continue;
+        if (row >= e.M) continue;
         float v[32];
 #pragma unroll
         for (int u = 0; u < 32; u++) {
@@ -493,26 +549,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         }
         const bool full_row = col0 + 32 <= e.N;
         if (e.mode == CGFD_SG_OUT_BF16) {
-          __nv_bfloat16 *C = (__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0;
-          __nv_bfloat16 *Z = e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr;
-          __align__(16) __nv_bfloat16 h[32], z[32];
-#pragma unroll
-          for (int u = 0; u < 32; u++) {
-            z[u] = __float2bfloat16_rn(v[u]);
-            h[u] = e.act == CGFD_SG_ACT_GELU ? __float2bfloat16_rn(gelu(v[u])) : z[u];
-          }
-          if (full_row) {
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-              reinterpret_cast<uint4 *>(C)[u] = reinterpret_cast<const uint4 *>(h)[u];
-              if (Z) reinterpret_cast<uint4 *>(Z)[u] = reinterpret_cast<const uint4 *>(z)[u];
-            }
-          } else {
-            for (int u = 0; u < 32 && col0 + u < e.N; u++) {
-              C[u] = h[u];
-              if (Z) Z[u] = z[u];
-            }
-          }
+          store_bf16_32((__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0,
+                        e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr, v, e.act,
+                        e.N - col0);
         } else {
           float *C = (float *)e.C + (long long)row * e.ldc + col0;
           if (full_row) {
@@ -521,7 +560,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
               reinterpret_cast<float4 *>(C)[u] =
                   make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
           } else {
-            for (int u = 0; u < 32 && col0 + u < e.N; u++) C[u] = v[u];
+#pragma unroll
+            for (int u = 0; u < 32; u++)
+              if (col0 + u < e.N) C[u] = v[u];
           }
         }
       }
@@ -622,7 +663,9 @@ extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long lo
     int dev = 0;
     if (cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              SMEM_BYTES) != cudaSuccess ||
-        cudaFuncSetAttribute(k_gemm_tn_p, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_gemm_tn_p<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             P_SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(k_gemm_tn_p<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              P_SMEM_BYTES) != cudaSuccess ||
         cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -641,12 +684,18 @@ extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long lo
   e.N = N;
   e.err = d_err;
   const int ntn = (N + BN - 1) / BN, ntm = (M + BM - 1) / BM;
-  const long long ptiles = (long long)ntn * ((M + PBM - 1) / PBM);
+  const bool wide = N > BN;
+  const int ptn = wide ? (N + 2 * BN - 1) / (2 * BN) : ntn;
+  const long long ptiles = (long long)ptn * (wide ? ntm : (M + 2 * BM - 1) / (2 * BM));
   if (nz == 1 && mode != CGFD_SG_OUT_F32_ADD && ptiles >= 2LL * nsm && ptiles < (1LL << 31)) {
-    /* large products: one persistent CTA per SM, 256-row tiles, epilogue
-     * overlapped */
-    k_gemm_tn_p<<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, ntn,
-                                                                        (int)ptiles);
+    /* large products: one persistent CTA per SM, 32768-output tiles,
+     * epilogue overlapped */
+    if (wide)
+      k_gemm_tn_p<true><<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(
+          ta, tb, e, K, ptn, (int)ptiles);
+    else
+      k_gemm_tn_p<false><<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(
+          ta, tb, e, K, ptn, (int)ptiles);
   } else {
     dim3 grid(ntn, ntm, nz);
     k_gemm_tn<<<grid, NTHREADS, SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, kper);

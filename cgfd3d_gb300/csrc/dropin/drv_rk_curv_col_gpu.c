@@ -5,7 +5,8 @@
  * (forward/drv_rk_curv_col.h:17-37), reading the reference's structs
  * unchanged, and runs the whole loop through the flat C ABI of
  * include/cgfd3d_gpu.h on the GPU.  Link it instead of
- * forward/drv_rk_curv_col.o; see INTEGRATION.md.
+ * forward/drv_rk_curv_col.o, together with libcgfd3d_gpu.so and the CUDA
+ * runtime (-lcudart).
  *
  * What the reference's loop leaves behind is left behind here too:
  *   wav->v5d         final state in level 0 (nt_total even) or 3 (odd)

@@ -30,8 +30,11 @@ def _sglib():
 @pytest.mark.parametrize("M,N,K", [(256, 384, 640), (200, 136, 72), (8, 1152, 640),
                                    (1024, 128, 1024),
                                    # at least two output tiles per SM: the
-                                   # persistent form (not for the split-K mode)
-                                   (32768, 1152, 640), (40000, 200, 136)])
+                                   # persistent form (not for the split-K mode),
+                                   # 128 x 256 tiles (N > 128; a last tile of
+                                   # 128 or fewer columns) and 256 x 128 tiles
+                                   (32768, 1152, 640), (40000, 200, 136),
+                                   (80000, 120, 72)])
 def test_gemm_modes_match_torch(M, N, K):
     import ctypes as C
     import torch
