@@ -316,17 +316,17 @@ __global__ void __launch_bounds__(NTHREADS, 2)
   const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll 1
   for (int c0 = 0; c0 < BN; c0 += 32) {
+    const int col0 = n0 + c0;
+    if (col0 >= e.N) break;                /* warp-uniform */
     uint32_t r[32];
     tmem_ld32(tl + c0, r);
-    if (!have || row >= e.M) continue;
-    const int col0 = n0 + c0;
-    if (col0 >= e.N) continue;
+    /* bias: one coalesced load per warp, lane t's value broadcast */
+    const float bv = e.bias && col0 + lane < e.N ? e.bias[col0 + lane] : 0.0f;
     float v[32];
 #pragma unroll
-    for (int t = 0; t < 32; t++) {
-      v[t] = __uint_as_float(r[t]) * e.alpha;
-      if (e.bias && col0 + t < e.N) v[t] += e.bias[col0 + t];
-    }
+    for (int t = 0; t < 32; t++)
+      v[t] = __uint_as_float(r[t]) * e.alpha + __shfl_sync(0xffffffffu, bv, t);
+    if (!have || row >= e.M) continue;
     const bool full_row = col0 + 32 <= e.N;
     if (e.mode == CGFD_SG_OUT_BF16) {
       store_bf16_32((__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0,
@@ -380,9 +380,12 @@ __global__ void __launch_bounds__(NTHREADS, 2)
  * (bf16 or fp32, no split along K). */
 constexpr int PSTAGES = 4;
 constexpr int P_STAGE = 2 * TILE_A + TILE_B; /* 48 KiB (TILE_A == TILE_B) */
-constexpr int P_SMEM_BYTES = PSTAGES * P_STAGE + 1024;
+/* epilogue staging, per epilogue warp: 32 rows x 64 B of C and of Z */
+constexpr int P_EPI_BUF = 32 * 64;
 constexpr int P_THREADS = 320;
 constexpr int P_EPI_WARPS = 8;
+constexpr int P_SMEM_BYTES = PSTAGES * P_STAGE + 1024 + P_EPI_WARPS * 2 * P_EPI_BUF;
+static_assert(P_SMEM_BYTES <= 232448, "more shared memory than one CTA gets");
 constexpr uint32_t P_TMEM_COLS = 512;   /* 2 accumulators x 2 halves x 128 */
 
 template <bool WIDE>
@@ -517,6 +520,7 @@ __global__ void __launch_bounds__(P_THREADS, 1)
      * accumulator half h = (w - 2) / 4: rows 32 (w % 4) .. of columns
      * h 128 .. (WIDE), rows h 128 + 32 (w % 4) .. (narrow) */
     const int q = warp & 3, half = (warp - 2) >> 2;
+    uint8_t *ebuf = smem + PSTAGES * P_STAGE + (warp - 2) * 2 * P_EPI_BUF;
     int i = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, i++) {
       const int acc = i & 1;
@@ -540,21 +544,59 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         if (col0 >= e.N) break;            /* warp-uniform: nothing left of this half */
         uint32_t r[32];
         tmem_ld32(tl + c0, r);
-        if (row >= e.M) continue;
+        /* bias: one coalesced load per warp, lane u's value broadcast */
+        const float bv = e.bias && col0 + lane < e.N ? e.bias[col0 + lane] : 0.0f;
         float v[32];
 #pragma unroll
-        for (int u = 0; u < 32; u++) {
-          v[u] = __uint_as_float(r[u]) * e.alpha;
-          if (e.bias && col0 + u < e.N) v[u] += e.bias[col0 + u];
+        for (int u = 0; u < 32; u++)
+          v[u] = __uint_as_float(r[u]) * e.alpha + __shfl_sync(0xffffffffu, bv, u);
+        if (e.mode == CGFD_SG_OUT_BF16 && col0 + 32 <= e.N) {
+          /* the warp's 32 x 32 block through shared memory: lane = row on
+           * the way in, 8 rows of 64 contiguous bytes per store on the way
+           * out (16-byte chunk c of row r sits at c ^ ((r >> 1) & 3), so
+           * neither side has bank conflicts) */
+          uint32_t hp[16], zp[16];
+#pragma unroll
+          for (int u = 0; u < 16; u++) {
+            zp[u] = pack_bf16(v[2 * u], v[2 * u + 1]);
+            hp[u] = e.act == CGFD_SG_ACT_GELU ? pack_bf16(gelu(v[2 * u]), gelu(v[2 * u + 1]))
+                                              : zp[u];
+          }
+          const int sw = (lane >> 1) & 3;
+#pragma unroll
+          for (int c = 0; c < 4; c++) {
+            *reinterpret_cast<uint4 *>(ebuf + lane * 64 + ((c ^ sw) << 4)) =
+                make_uint4(hp[4 * c], hp[4 * c + 1], hp[4 * c + 2], hp[4 * c + 3]);
+            if (e.Z)
+              *reinterpret_cast<uint4 *>(ebuf + P_EPI_BUF + lane * 64 + ((c ^ sw) << 4)) =
+                  make_uint4(zp[4 * c], zp[4 * c + 1], zp[4 * c + 2], zp[4 * c + 3]);
+          }
+          __syncwarp();
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const int rr = j * 8 + (lane >> 2), b = lane & 3;
+            const int off = rr * 64 + ((b ^ ((rr >> 1) & 3)) << 4);
+            const int grow = m0 + q * 32 + rr;
+            if (grow < e.M) {
+              const long long o = (long long)grow * e.ldc + col0 + b * 8;
+              *reinterpret_cast<uint4 *>((__nv_bfloat16 *)e.C + o) =
+                  *reinterpret_cast<const uint4 *>(ebuf + off);
+              if (e.Z)
+                *reinterpret_cast<uint4 *>(e.Z + o) =
+                    *reinterpret_cast<const uint4 *>(ebuf + P_EPI_BUF + off);
+            }
+          }
+          __syncwarp();                    /* the buffer is free for the next block */
+          continue;
         }
-        const bool full_row = col0 + 32 <= e.N;
+        if (row >= e.M) continue;
         if (e.mode == CGFD_SG_OUT_BF16) {
           store_bf16_32((__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0,
                         e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr, v, e.act,
                         e.N - col0);
         } else {
           float *C = (float *)e.C + (long long)row * e.ldc + col0;
-          if (full_row) {
+          if (col0 + 32 <= e.N) {
 #pragma unroll
             for (int u = 0; u < 8; u++)
               reinterpret_cast<float4 *>(C)[u] =
