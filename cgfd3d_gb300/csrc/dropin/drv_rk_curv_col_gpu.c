@@ -36,6 +36,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "../../../include/cgfd3d_dropin.h"
 #include "../../../include/cgfd3d_gpu.h"
 
 #ifdef CGFD_DROPIN_REFERENCE_HEADERS
@@ -52,12 +53,27 @@
 #define CGFD_ABORT() exit(1)
 #endif
 
+/* CGFD_* code of the failure that ended the time loop (0: none so far);
+ * read by cgfd_gpu_last_error(), e.g. from an atexit handler, since the
+ * failure itself ends the process as the reference's errors do */
+static int g_gpu_code = 0;
+
+int cgfd_gpu_last_error(void) { return g_gpu_code; }
+
 static void fail(const char *what)
 {
   fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s: %s\n", what,
           cgfd_last_error());
   fflush(stderr);
   CGFD_ABORT();
+}
+
+/* a library call's status: non-zero is recorded and ends the run */
+static void check(int rc, const char *what)
+{
+  if (rc == 0) return;
+  g_gpu_code = rc;
+  fail(what);
 }
 
 /* Boxes of the slices io_slice_nc_put writes (forward/io_funcs.c:992-1111):
@@ -157,6 +173,7 @@ static void write_step(const out_ctx_t *o, int it)
 
 static void fatal(const char *what)
 {
+  g_gpu_code = CGFD_EINVAL;
   fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s\n", what);
   fflush(stderr);
   CGFD_ABORT();
@@ -164,6 +181,7 @@ static void fatal(const char *what)
 
 static void unsupported(const char *what)
 {
+  g_gpu_code = CGFD_EINVAL;
   fprintf(stderr, "drv_rk_curv_col_allstep (GPU): %s is not supported\n", what);
   fflush(stderr);
   CGFD_ABORT();
@@ -177,6 +195,7 @@ void drv_rk_curv_col_allstep(
     int qc_check_nan_num_of_step, const int output_all, const int verbose)
 {
   (void)mympi; (void)output_fname_part; (void)output_dir;
+  g_gpu_code = 0;
 
   if (fd->num_rk_stages != 4 || fd->num_of_pairs != 8)
     unsupported("an operator set other than MacCormack DRP with RK4");
@@ -394,7 +413,7 @@ void drv_rk_curv_col_allstep(
 #endif
   if (verbose > 0) fprintf(stdout, "GPU time loop: %d steps ...\n", nt_total);
   cgfd_solver_t *s = NULL;
-  if (cgfd_solver_create(&p, &s) != 0) fail("solver setup");
+  check(cgfd_solver_create(&p, &s), "solver setup");
   /* Steps are queued without waiting; the boxes of a step that writes are
    * packed behind it into one of two output slots, and written while the
    * device runs the next step. */
@@ -409,7 +428,7 @@ void drv_rk_curv_col_allstep(
       int next = nslice > 0 || output_every ? done : next_snapshot(iosnap, nt_total, done);
       if (next - done + 1 < n) n = next - done + 1;
     }
-    if (cgfd_solver_run_async(s, n) != 0) fail("time loop");
+    check(cgfd_solver_run_async(s, n), "time loop");
     done += n;
     const int it = done - 1;
     int nbox = 0, due = 0;
@@ -419,44 +438,41 @@ void drv_rk_curv_col_allstep(
         if (snapshot_due(iosnap, m, nt_total, it)) nbox += snapshot_box(iosnap, m, box + nbox);
       due = nbox > 0 || output_every;
     }
-    if (due && !output_every &&
-        cgfd_solver_pack_boxes_async(s, box, nbox, slot) != 0)
-      fail("slices/snapshots");
+    if (due && !output_every)
+      check(cgfd_solver_pack_boxes_async(s, box, nbox, slot), "slices/snapshots");
     if (pend_it >= 0) {
-      if (cgfd_solver_collect_boxes(s, pend_slot, w_host, NULL) != 0) fail("slices/snapshots");
+      check(cgfd_solver_collect_boxes(s, pend_slot, w_host, NULL), "slices/snapshots");
       write_output(pend_it);
       pend_it = -1;
     }
     if (due && output_every) {
-      if (cgfd_solver_fetch_state(s, w_host) != 0) fail("state for output");
+      check(cgfd_solver_fetch_state(s, w_host), "state for output");
       write_output(it);
     } else if (due) {
       pend_it = it;
       pend_slot = slot;
       slot ^= 1;
     }
-    if (qc_check_nan_num_of_step > 0 && done % qc_check_nan_num_of_step == 0 &&
-        cgfd_solver_check_finite(s) != 0)
-      fail("wavefield check");
+    if (qc_check_nan_num_of_step > 0 && done % qc_check_nan_num_of_step == 0)
+      check(cgfd_solver_check_finite(s), "wavefield check");
   }
   if (pend_it >= 0) {
-    if (cgfd_solver_collect_boxes(s, pend_slot, w_host, NULL) != 0) fail("slices/snapshots");
+    check(cgfd_solver_collect_boxes(s, pend_slot, w_host, NULL), "slices/snapshots");
     write_output(pend_it);
   }
-  if (cgfd_solver_run(s, 0) != 0) fail("time loop");   /* waits, reads device errors */
-  if (cgfd_solver_fetch(s) != 0) fail("fetch");
-  if (p.free_top && bdry->matVx2Vz2 &&
-      cgfd_solver_fetch_surface_matrices(s, bdry->matVx2Vz2, bdry->matVy2Vz2,
-                                          bdry->matF2Vz2) != 0)
-    fail("free-surface matrices");
-  if (p.free_top && md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO && bdry->matD &&
-      cgfd_solver_fetch_surface_rotation(s, bdry->matD) != 0)
-    fail("free-surface rotation matrices");
+  check(cgfd_solver_run(s, 0), "time loop");   /* waits, reads device errors */
+  check(cgfd_solver_fetch(s), "fetch");
+  if (p.free_top && bdry->matVx2Vz2)
+    check(cgfd_solver_fetch_surface_matrices(s, bdry->matVx2Vz2, bdry->matVy2Vz2,
+                                             bdry->matF2Vz2),
+          "free-surface matrices");
+  if (p.free_top && md->medium_type == CGFD_MEDIUM_VISCOELASTIC_ISO && bdry->matD)
+    check(cgfd_solver_fetch_surface_rotation(s, bdry->matD), "free-surface rotation matrices");
 #ifdef CGFD_DROPIN_REFERENCE_HEADERS
   if (p.free_top) {
     float *PG = (float *)calloc((size_t)15 * gd->nx * gd->ny, sizeof(float));
     if (!PG) unsupported("host memory for the peak-motion maps");
-    if (cgfd_solver_fetch_pg(s, PG) != 0) fail("peak-motion maps");
+    check(cgfd_solver_fetch_pg(s, PG), "peak-motion maps");
     PG_slice_output(PG, gd, output_dir, output_fname_part, mympi->topoid);
     free(PG);
   }

@@ -39,6 +39,55 @@ def test_every_declared_function_is_exported():
     assert not missing, missing
 
 
+def test_dropin_header_functions_are_exported():
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(REPO, "include", "cgfd3d_dropin.h")).read(),
+                  flags=re.S)
+    names = sorted(set(re.findall(r"\b(cgfd_[a-z0-9_]+)\s*\(", text)))
+    assert names == ["cgfd_gpu_last_error"]
+    syms = exported(os.path.join(BUILD, "libcgfd3d_dropin.so"))
+    assert "drv_rk_curv_col_allstep" in syms
+    assert not [n for n in names if n not in syms]
+
+
+def test_dropin_failure_code_is_kept_for_exit_handlers():
+    """An unsupported configuration (an RK scheme other than RK4) ends the
+    process with status 1, as the reference's errors do, before any device
+    call; cgfd_gpu_last_error() then reports CGFD_EINVAL to an atexit
+    handler."""
+    prog = r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "cgfd3d_ref_abi.h"
+#include "cgfd3d_dropin.h"
+#include "cgfd3d_gpu.h"
+static void report(void) { printf("code %d\n", cgfd_gpu_last_error()); fflush(stdout); }
+int main(void)
+{
+  fd_t fd = {0};
+  fd.num_rk_stages = 3;
+  fd.num_of_pairs = 8;
+  printf("before %d\n", cgfd_gpu_last_error());
+  atexit(report);
+  drv_rk_curv_col_allstep(&fd, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL, NULL,
+                          NULL, 0.01f, 1, 0.0f, NULL, NULL, 0, 0, 0);
+  printf("returned\n");
+  return 0;
+}
+"""
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        with open(src, "w") as f:
+            f.write(prog)
+        subprocess.run(["gcc", "-O1", "-I" + os.path.join(REPO, "include"), "-o", exe, src,
+                        "-L" + BUILD, "-lcgfd3d_dropin", "-Wl,-rpath," + BUILD], check=True)
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1, (r.returncode, r.stdout, r.stderr)
+    assert "before 0" in r.stdout and "returned" not in r.stdout
+    assert "code %d" % 1 in r.stdout      # CGFD_EINVAL
+    assert "is not supported" in r.stderr
+
+
 def test_library_loads_without_gpu():
     lib = ctypes.CDLL(os.path.join(BUILD, "libcgfd3d_gpu.so"))
     lib.cgfd_abi_version.restype = ctypes.c_int
