@@ -91,6 +91,12 @@ def _lib_sg():
     L.cgfd_sg_colsum.argtypes = [vp, ll, i, ll, vp, vp]
     L.cgfd_sg_adamw.argtypes = [vp, vp, vp, vp, vp, ll, f, f, f, f, f, i, vp]
     L.cgfd_sg_to_bf16.argtypes = [vp, ll, vp, vp]
+    L.cgfd_sg_net_nparam.argtypes = [i, i]
+    L.cgfd_sg_net_nparam.restype = ll
+    L.cgfd_sg_net_create.argtypes = [i, i, vp, ll, f, C.POINTER(vp)]
+    L.cgfd_sg_net_predict.argtypes = [vp, i, vp, vp, vp]
+    L.cgfd_sg_net_destroy.argtypes = [vp]
+    L.cgfd_sg_net_destroy.restype = None
     L._sg_ready = True
     return L
 
@@ -310,6 +316,58 @@ class Surrogate:
 
     def device_error(self):
         return int(self.err.item())
+
+    def parameters(self):
+        """The flat fp32 parameter vector (host copy): per layer W (out x
+        in), then its bias."""
+        return self.w.cpu().numpy()
+
+
+def nparam(nrec=64, nt=1000):
+    """Parameters of the layout as the C library counts them (no GPU)."""
+    return int(_lib_sg().cgfd_sg_net_nparam(int(nrec), int(nt)))
+
+
+class Net:
+    """A trained network as the library's C object (cgfd_sg_net_*): host
+    positions and moment tensors in, host seismograms out, no torch on the
+    way.  Chunks of CGFD_SG_NET_CHUNK (256) shots, each bit-identical to
+    Surrogate.predict of the same shots as one batch."""
+
+    CHUNK = 256
+
+    def __init__(self, params, nrec=64, nt=1000, scale=1.0):
+        w = np.ascontiguousarray(params, dtype=np.float32)
+        self.nrec, self.nt = int(nrec), int(nt)
+        self._h = C.c_void_p()
+        _check(_lib_sg().cgfd_sg_net_create(self.nrec, self.nt, w.ctypes.data, w.size,
+                                            float(scale), C.byref(self._h)))
+
+    @classmethod
+    def of(cls, sur):
+        return cls(sur.parameters(), sur.lay.R // 3, sur.lay.nt, sur.scale)
+
+    def predict(self, pos, M):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        M = np.ascontiguousarray(M, dtype=np.float32)
+        n = pos.shape[0]
+        if pos.shape != (n, 3) or M.shape != (n, 6):
+            raise ValueError("positions [n, 3] and moment tensors [n, 6]")
+        u = np.empty((n, self.nt, 3 * self.nrec), np.float32)
+        _check(_lib_sg().cgfd_sg_net_predict(self._h, n, pos.ctypes.data, M.ctypes.data,
+                                             u.ctypes.data))
+        return u
+
+    def close(self):
+        if self._h:
+            _lib_sg().cgfd_sg_net_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

@@ -559,6 +559,62 @@ int cgfd_sg_gemm(const void *A, long long lda, const void *B, long long ldb, voi
                  long long ldc, int M, int N, int K, float alpha, const float *bias, int act,
                  int mode, void *Z, int splits, int *d_err, void *stream);
 
+/* The other building blocks (bf16 arrays unless stated, row-major):
+ *   features      pos [B][3] fp32 -> out [B][nfeat]: the 3 coordinates, then
+ *                 per coordinate d and f = 1..nfreq sin and cos of pi f x_d,
+ *                 zeros up to nfeat
+ *   im2col_up     X [B][Tin][C] -> A [B][Tin up][ks C]: nearest up-sampling
+ *                 by `up` and the ks-tap window over time (zero outside)
+ *   col2im_up_gelu  adjoint of im2col_up, times GELU'(Z): dZ [B][Tin][C]
+ *                 (Z null: no GELU factor)
+ *   gelu_bwd      dZ = dH GELU'(Z) for n values
+ *   contract      U [B][T][R] fp32 = scale sum_k M[b][k] G[b][t][k][R] for t < T
+ *                 (G [B][Tg][6][R], M [B][6] fp32)
+ *   contract_loss as contract against Utrue, err[b] += sum (U - Utrue)^2 and
+ *                 dG of the loss (1/B) sum_b err[b] / norm[b]
+ *   transpose     Y [cols][rows] (ld ldy) = X^T (ld ldx)
+ *   colsum        out[c] += sum over rows of X[r][c] (fp32 out)
+ *   adamw         one AdamW step on fp32 w (and its bf16 copy w16) with
+ *                 gradient g and moments m, v, bias corrections of `step`
+ *   to_bf16       y = bf16(x) for n fp32 values */
+int cgfd_sg_features(const float *pos, int B, int nfreq, int nfeat, void *out, void *stream);
+int cgfd_sg_im2col_up(const void *X, int B, int Tin, int C, int up, int ks, void *A,
+                      void *stream);
+int cgfd_sg_col2im_up_gelu(const void *dA, int B, int Tin, int C, int up, int ks,
+                           const void *Z, void *dZ, void *stream);
+int cgfd_sg_gelu_bwd(const void *dH, const void *Z, long long n, void *dZ, void *stream);
+int cgfd_sg_contract(const void *G, const float *M, int B, int Tg, int T, int R, float scale,
+                     float *U, void *stream);
+int cgfd_sg_contract_loss(const void *G, const float *M, int B, int Tg, int T, int R,
+                          float scale, const float *Utrue, const float *norm, float *err,
+                          void *dG, void *stream);
+int cgfd_sg_transpose(const void *X, int rows, int cols, long long ldx, void *Y,
+                      long long ldy, void *stream);
+int cgfd_sg_colsum(const void *X, long long rows, int cols, long long ld, float *out,
+                   void *stream);
+int cgfd_sg_adamw(float *w, void *w16, const float *g, float *m, float *v, long long n,
+                  float lr, float b1, float b2, float eps, float wd, int step, void *stream);
+int cgfd_sg_to_bf16(const float *x, long long n, void *y, void *stream);
+
+/* A trained surrogate as one object, for callers without Python: shots
+ * given as arrays of per-shot descriptors on the host (normalised source
+ * position pos [n][3] in [-1, 1], moment tensor mt [n][6] in the network's
+ * units, order Mxx Myy Mzz Myz Mxz Mxy as the training data), seismograms
+ * u [n][nt][3 nrec] fp32 back on the host.  params: the flat fp32
+ * parameter vector of cgfd3d_gb300/surrogate.py (per layer W (out x in),
+ * then its bias; cgfd_sg_net_nparam values), scale: the seismograms'
+ * amplitude in the network's units.  Requests run in chunks of
+ * CGFD_SG_NET_CHUNK shots, each chunk bit-identical to the Python layer's
+ * prediction of the same shots as one batch. */
+#define CGFD_SG_NET_CHUNK 256
+typedef struct cgfd_sg_net cgfd_sg_net_t;
+long long cgfd_sg_net_nparam(int nrec, int nt);   /* -1: no such layout */
+int cgfd_sg_net_create(int nrec, int nt, const float *params, long long nparam, float scale,
+                       cgfd_sg_net_t **out);
+int cgfd_sg_net_predict(cgfd_sg_net_t *net, int nshot, const float *pos, const float *mt,
+                        float *u);
+void cgfd_sg_net_destroy(cgfd_sg_net_t *net);
+
 /* No counterpart in the reference.  NaN/Inf test of a device array the
  * caller owns that allocates no device memory, for callers that cannot call
  * cudaMalloc (a process whose device memory belongs to another framework's

@@ -185,3 +185,30 @@ def test_pipeline_on_solver_shots():
     assert pred.shape == (4, steps, 3 * nrec) and np.isfinite(pred).all()
     mis = SG.misfit(pred, U[8:])
     assert np.isfinite(mis).all()
+
+
+def test_c_object_predicts_as_the_python_layer():
+    """cgfd_sg_net_* (host descriptors in, host seismograms out) gives the
+    Python layer's predictions bit for bit: one chunk of 40 shots, and 300
+    shots in chunks of 256 + 44 against the two batches predicted apart."""
+    import torch
+    from cgfd3d_gb300 import surrogate as SG
+    nrec, nt = 4, 1000
+    sur = SG.Surrogate(nrec=nrec, nt=nt, seed=9, scale=0.37)
+    net = SG.Net.of(sur)
+    rng = np.random.default_rng(21)
+    pos = rng.uniform(-1, 1, (300, 3)).astype(np.float32)
+    M = rng.standard_normal((300, 6)).astype(np.float32)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    u40 = net.predict(pos[:40], M[:40])
+    ref40 = sur.predict(dev(pos[:40]), dev(M[:40])).cpu().numpy()
+    assert u40.shape == (40, nt, 3 * nrec)
+    assert np.array_equal(u40, ref40)
+    u = net.predict(pos, M)
+    ref = np.concatenate([sur.predict(dev(pos[:256]), dev(M[:256])).cpu().numpy(),
+                          sur.predict(dev(pos[256:]), dev(M[256:])).cpu().numpy()])
+    assert np.array_equal(u, ref)
+    assert np.isfinite(u).all() and np.abs(u).max() > 0
+    with pytest.raises(Exception):
+        SG.Net(sur.parameters()[:-1], nrec, nt, 1.0)     # wrong parameter count
+    net.close()

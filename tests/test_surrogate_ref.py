@@ -74,3 +74,12 @@ def test_knn_green_recovers_linear_data():
     pred = surrogate.knn_green(pos, M.astype(np.float32), U, q, Mq, k=12)
     true = np.einsum("nk,ktr->ntr", Mq, G)
     assert surrogate.misfit(pred, true).max() < 1e-5
+
+
+def test_c_layout_matches_the_python_layout():
+    """The C object's parameter count (cgfd_sg_net_nparam) is the training
+    layout's, for several receiver counts; impossible layouts are refused."""
+    from cgfd3d_gb300 import surrogate as SG
+    for nrec, nt in ((64, 1000), (4, 1000), (16, 100), (1, 1024)):
+        assert SG.nparam(nrec, nt) == SG.Layout(nrec, nt).nparam
+    assert SG.nparam(64, 1025) == -1 and SG.nparam(0, 10) == -1
