@@ -120,6 +120,9 @@ extern "C" int cgfd_sg_net_create(int nrec, int nt, const float *params, long lo
   if (want < 0)
     return net_err(CGFD_EINVAL, "sg_net_create: %d receivers, %d samples (1..%d samples)",
                    nrec, nt, T0 * (1 << NDEC));
+  if (nrec % 4)
+    return net_err(CGFD_EINVAL, "sg_net_create: %d receivers (a multiple of 4: the last "
+                   "layer's 18 nrec outputs are stored in 16-byte rows)", nrec);
   if (!params || nparam != want)
     return net_err(CGFD_EINVAL, "sg_net_create: %lld parameters given, the layout has %lld",
                    nparam, want);

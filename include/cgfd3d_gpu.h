@@ -603,7 +603,7 @@ int cgfd_sg_to_bf16(const float *x, long long n, void *y, void *stream);
  * u [n][nt][3 nrec] fp32 back on the host.  params: the flat fp32
  * parameter vector of cgfd3d_gb300/surrogate.py (per layer W (out x in),
  * then its bias; cgfd_sg_net_nparam values), scale: the seismograms'
- * amplitude in the network's units.  Requests run in chunks of
+ * amplitude in the network's units; nrec a multiple of 4.  Requests run in chunks of
  * CGFD_SG_NET_CHUNK shots, each chunk bit-identical to the Python layer's
  * prediction of the same shots as one batch. */
 #define CGFD_SG_NET_CHUNK 256
