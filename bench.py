@@ -1023,6 +1023,16 @@ def run_surrogate_net(args):
     e1.record()
     torch.cuda.synchronize()
     inf_ms = e0.elapsed_time(e1) / K
+    # the same inference through the C object: host descriptors in, host
+    # seismograms out (cgfd_sg_net_predict)
+    cnet = SG.Net.of(net)
+    pos_h, M_h = pos.cpu().numpy(), M.cpu().numpy()
+    cnet.predict(pos_h, M_h)
+    t0 = time.perf_counter()
+    for _ in range(K):
+        cnet.predict(pos_h, M_h)
+    c_s = (time.perf_counter() - t0) / K
+    cnet.close()
     lay = net.lay
     d = net._buffers(B, False)
     o, k = lay.dec[-1]
@@ -1048,7 +1058,10 @@ def run_surrogate_net(args):
         "dtype": "bf16 (fp32 accumulation)", "data": "synthetic targets (seeded)",
         "config": {"workload": "surrogate network alone: 5.5 M parameters, 64 receivers x 3 "
                    "components x 1000 samples, batch 256", "parallelism": "single"},
-        "inference": {"ms_per_batch": inf_ms, "shots_per_s": B / (inf_ms * 1e-3)},
+        "inference": {"ms_per_batch": inf_ms, "shots_per_s": B / (inf_ms * 1e-3),
+                      "host_to_host_c_object": {
+                          "ms_per_batch": 1e3 * c_s, "shots_per_s": B / c_s,
+                          "h2d_bytes": B * 9 * 4, "d2h_bytes": B * 1000 * 192 * 4}},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                      "kernel": "k_gemm_tn_p (persistent form, 128 x 256 tiles; last decoder "
