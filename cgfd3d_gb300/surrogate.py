@@ -317,10 +317,35 @@ class Surrogate:
     def device_error(self):
         return int(self.err.item())
 
+    def sync_gradients(self, loss=None, group=None):
+        """Data-parallel training over the ranks of `group`: every rank ran
+        gradients() on its own share of the batch (shares of equal size);
+        the mean over ranks of the gradients (and of `loss`, when given) is
+        the whole batch's.  One all-reduce each; a no-op on one rank."""
+        allreduce_mean(self.grad, group)
+        if loss is not None:
+            allreduce_mean(loss, group)
+        return loss
+
     def parameters(self):
         """The flat fp32 parameter vector (host copy): per layer W (out x
         in), then its bias."""
         return self.w.cpu().numpy()
+
+
+def allreduce_mean(t, group=None):
+    """In place: t becomes the mean of t over the ranks of the initialised
+    process group (NCCL for device tensors, gloo for host tensors); a no-op
+    without a group or with one rank.  The only collective of data-parallel
+    surrogate training."""
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized():
+        return t
+    world = dist.get_world_size(group)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        t.div_(world)
+    return t
 
 
 def nparam(nrec=64, nt=1000):
