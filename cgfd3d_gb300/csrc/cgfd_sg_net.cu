@@ -219,12 +219,19 @@ extern "C" int cgfd_sg_net_predict(cgfd_sg_net_t *n, int nshot, const float *pos
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(n->mt, mt + (size_t)b0 * NMT, (size_t)nb * NMT * 4,
                           cudaMemcpyHostToDevice, n->st);
-    if (e != cudaSuccess) return net_err(CGFD_ECUDA, "sg_net_predict: %s", cudaGetErrorString(e));
-    const int rc = net_forward(n, nb);
-    if (rc) return rc;
-    e = cudaMemcpyAsync(u + (size_t)b0 * per, n->U, (size_t)nb * per * 4, cudaMemcpyDeviceToHost,
-                        n->st);
-    if (e != cudaSuccess) return net_err(CGFD_ECUDA, "sg_net_predict: %s", cudaGetErrorString(e));
+    int rc = e == cudaSuccess ? net_forward(n, nb)
+                              : net_err(CGFD_ECUDA, "sg_net_predict: %s", cudaGetErrorString(e));
+    if (rc == 0) {
+      e = cudaMemcpyAsync(u + (size_t)b0 * per, n->U, (size_t)nb * per * 4,
+                          cudaMemcpyDeviceToHost, n->st);
+      if (e != cudaSuccess)
+        rc = net_err(CGFD_ECUDA, "sg_net_predict: %s", cudaGetErrorString(e));
+    }
+    if (rc) {
+      /* nothing queued may still write into the caller's arrays */
+      cudaStreamSynchronize(n->st);
+      return rc;
+    }
   }
   int herr = 0;
   cudaError_t e = cudaMemcpyAsync(&herr, n->d_err, 4, cudaMemcpyDeviceToHost, n->st);
