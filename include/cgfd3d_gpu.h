@@ -606,7 +606,7 @@ int cgfd_sg_to_bf16(const float *x, long long n, void *y, void *stream);
  * amplitude in the network's units; nrec a multiple of 4.  Requests run in chunks of
  * CGFD_SG_NET_CHUNK shots, each chunk bit-identical to the Python layer's
  * prediction of the same shots as one batch.  An object holds its own
- * stream and work buffers (about 1.3 GB for 64 receivers): one call at a
+ * stream and work buffers (about 1.6 GB for 64 receivers): one call at a
  * time per object; predict returns when u is written. */
 #define CGFD_SG_NET_CHUNK 256
 typedef struct cgfd_sg_net cgfd_sg_net_t;
