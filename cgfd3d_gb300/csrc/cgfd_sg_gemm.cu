@@ -39,6 +39,7 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 
 #include "../../include/cgfd3d_gpu.h"
 
@@ -113,6 +114,18 @@ __device__ __forceinline__ void tma_2d(void *dst, const CUtensorMap *map, int c0
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+/* bulk tensor store of one box from shared memory (bulk-group completion;
+ * rows and columns outside the tensor are not written) */
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, const void *src, int c0,
+                                             int c1)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(c0), "r"(c1), "r"(smem_u32(src))
       : "memory");
 }
 
@@ -391,6 +404,7 @@ constexpr uint32_t P_TMEM_COLS = 512;   /* 2 accumulators x 2 halves x 128 */
 template <bool WIDE>
 __global__ void __launch_bounds__(P_THREADS, 1)
     k_gemm_tn_p(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+                const __grid_constant__ CUtensorMap tc, const __grid_constant__ CUtensorMap tz,
                 Epi e, int K, int ntn, int ntiles)
 {
   constexpr int TM = WIDE ? BM : 2 * BM, TN = WIDE ? 2 * BN : BN;
@@ -551,10 +565,11 @@ __global__ void __launch_bounds__(P_THREADS, 1)
         for (int u = 0; u < 32; u++)
           v[u] = __uint_as_float(r[u]) * e.alpha + __shfl_sync(0xffffffffu, bv, u);
         if (e.mode == CGFD_SG_OUT_BF16 && col0 + 32 <= e.N) {
-          /* the warp's 32 x 32 block through shared memory: lane = row on
-           * the way in, 8 rows of 64 contiguous bytes per store on the way
-           * out (16-byte chunk c of row r sits at c ^ ((r >> 1) & 3), so
-           * neither side has bank conflicts) */
+          /* the warp's 32 x 32 block goes out through shared memory as one
+           * bulk tensor store per output: lane = row writes its 64 bytes,
+           * 16-byte chunk c of row r at c ^ ((r >> 1) & 3), the layout of
+           * the stores' 64-byte swizzle (bank-conflict free as well); rows
+           * beyond M are clipped by the store */
           uint32_t hp[16], zp[16];
 #pragma unroll
           for (int u = 0; u < 16; u++) {
@@ -562,6 +577,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
             hp[u] = e.act == CGFD_SG_ACT_GELU ? pack_bf16(gelu(v[2 * u]), gelu(v[2 * u + 1]))
                                               : zp[u];
           }
+          /* the previous block's stores have read the buffer */
+          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          __syncwarp();
           const int sw = (lane >> 1) & 3;
 #pragma unroll
           for (int c = 0; c < 4; c++) {
@@ -571,22 +589,13 @@ __global__ void __launch_bounds__(P_THREADS, 1)
               *reinterpret_cast<uint4 *>(ebuf + P_EPI_BUF + lane * 64 + ((c ^ sw) << 4)) =
                   make_uint4(zp[4 * c], zp[4 * c + 1], zp[4 * c + 2], zp[4 * c + 3]);
           }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            const int rr = j * 8 + (lane >> 2), b = lane & 3;
-            const int off = rr * 64 + ((b ^ ((rr >> 1) & 3)) << 4);
-            const int grow = m0 + q * 32 + rr;
-            if (grow < e.M) {
-              const long long o = (long long)grow * e.ldc + col0 + b * 8;
-              *reinterpret_cast<uint4 *>((__nv_bfloat16 *)e.C + o) =
-                  *reinterpret_cast<const uint4 *>(ebuf + off);
-              if (e.Z)
-                *reinterpret_cast<uint4 *>(e.Z + o) =
-                    *reinterpret_cast<const uint4 *>(ebuf + P_EPI_BUF + off);
-            }
+          if (lane == 0) {
+            tma_store_2d(&tc, ebuf, col0, m0 + q * 32);
+            if (e.Z) tma_store_2d(&tz, ebuf + P_EPI_BUF, col0, m0 + q * 32);
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
           }
-          __syncwarp();                    /* the buffer is free for the next block */
           continue;
         }
         if (row >= e.M) continue;
@@ -615,6 +624,9 @@ __global__ void __launch_bounds__(P_THREADS, 1)
                                       smem_u32(&tempty[acc]))
                                   : "memory");
     }
+    /* the warp's bulk stores are complete before the CTA leaves */
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    __syncwarp();
   }
   tc_fence_before();
   __syncthreads();
@@ -657,6 +669,21 @@ static bool operand_map(CUtensorMap *m, const void *p, int rows, int K, long lon
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(p), dims, strides, box,
             es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+/* a bf16 [rows, N] output with row stride ld elements, 32 x 32 boxes in the
+ * 64-byte swizzle the persistent epilogue stages its blocks in */
+static bool output_map(CUtensorMap *m, void *p, int rows, int N, long long ld)
+{
+  encode_fn fn = encoder();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)N, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {32, 32};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, p, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 static int gemm_err(int code, const char *fmt, ...)
@@ -731,13 +758,19 @@ extern "C" int cgfd_sg_gemm(const void *A, long long lda, const void *B, long lo
   const long long ptiles = (long long)ptn * (wide ? ntm : (M + 2 * BM - 1) / (2 * BM));
   if (nz == 1 && mode != CGFD_SG_OUT_F32_ADD && ptiles >= 2LL * nsm && ptiles < (1LL << 31)) {
     /* large products: one persistent CTA per SM, 32768-output tiles,
-     * epilogue overlapped */
+     * epilogue overlapped; bf16 outputs leave by bulk tensor stores */
+    CUtensorMap tc, tz;
+    memset(&tc, 0, sizeof(tc));
+    memset(&tz, 0, sizeof(tz));
+    if (mode == CGFD_SG_OUT_BF16 &&
+        (!output_map(&tc, C, M, N, ldc) || (Z && !output_map(&tz, Z, M, N, ldc))))
+      return gemm_err(CGFD_ECUDA, "sg_gemm: output tensor map encoding failed");
     if (wide)
       k_gemm_tn_p<true><<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(
-          ta, tb, e, K, ptn, (int)ptiles);
+          ta, tb, tc, tz, e, K, ptn, (int)ptiles);
     else
       k_gemm_tn_p<false><<<nsm, P_THREADS, P_SMEM_BYTES, (cudaStream_t)stream>>>(
-          ta, tb, e, K, ptn, (int)ptiles);
+          ta, tb, tc, tz, e, K, ptn, (int)ptiles);
   } else {
     dim3 grid(ntn, ntm, nz);
     k_gemm_tn<<<grid, NTHREADS, SMEM_BYTES, (cudaStream_t)stream>>>(ta, tb, e, K, kper);
