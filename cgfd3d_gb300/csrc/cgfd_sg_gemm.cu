@@ -192,6 +192,30 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t *r)
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+/* 64 consecutive fp32 columns of this warp's 32 TMEM lanes (one wait) */
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t *r)
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, "
+      "%45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, "
+      "%62, %63}, [%64];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]),
+        "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]),
+        "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]),
+        "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]),
+        "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]),
+        "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ float gelu(float x)
 {
   const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
@@ -552,68 +576,75 @@ __global__ void __launch_bounds__(P_THREADS, 1)
       const int n0 = (t % ntn) * TN + (WIDE ? half * BN : 0);
       const int row = m0 + q * 32 + lane;
       const uint32_t tl = tmem + (uint32_t)(acc * 2 * BN + half * BN) + ((uint32_t)(q * 32) << 16);
+      /* 64 columns per TMEM load, then two 32-column blocks from registers */
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        const int col0 = n0 + c0;
-        if (col0 >= e.N) break;            /* warp-uniform: nothing left of this half */
-        uint32_t r[32];
-        tmem_ld32(tl + c0, r);
-        /* bias: one coalesced load per warp, lane u's value broadcast */
-        const float bv = e.bias && col0 + lane < e.N ? e.bias[col0 + lane] : 0.0f;
-        float v[32];
+      for (int c64 = 0; c64 < BN; c64 += 64) {
+        if (n0 + c64 >= e.N) break;        /* warp-uniform: nothing left of this half */
+        uint32_t r64[64];
+        tmem_ld64(tl + c64, r64);
 #pragma unroll
-        for (int u = 0; u < 32; u++)
-          v[u] = __uint_as_float(r[u]) * e.alpha + __shfl_sync(0xffffffffu, bv, u);
-        if (e.mode == CGFD_SG_OUT_BF16 && col0 + 32 <= e.N) {
-          /* the warp's 32 x 32 block goes out through shared memory as one
-           * bulk tensor store per output: lane = row writes its 64 bytes,
-           * 16-byte chunk c of row r at c ^ ((r >> 1) & 3), the layout of
-           * the stores' 64-byte swizzle (bank-conflict free as well); rows
-           * beyond M are clipped by the store */
-          uint32_t hp[16], zp[16];
-#pragma unroll
-          for (int u = 0; u < 16; u++) {
-            zp[u] = pack_bf16(v[2 * u], v[2 * u + 1]);
-            hp[u] = e.act == CGFD_SG_ACT_GELU ? pack_bf16(gelu(v[2 * u]), gelu(v[2 * u + 1]))
-                                              : zp[u];
+        for (int sub = 0; sub < 2; sub++) {
+          const int c0 = c64 + 32 * sub;
+          const int col0 = n0 + c0;
+          if (col0 >= e.N) break;
+          const uint32_t *r = r64 + 32 * sub;
+          /* bias: one coalesced load per warp, lane u's value broadcast */
+          const float bv = e.bias && col0 + lane < e.N ? e.bias[col0 + lane] : 0.0f;
+          float v[32];
+  #pragma unroll
+          for (int u = 0; u < 32; u++)
+            v[u] = __uint_as_float(r[u]) * e.alpha + __shfl_sync(0xffffffffu, bv, u);
+          if (e.mode == CGFD_SG_OUT_BF16 && col0 + 32 <= e.N) {
+            /* the warp's 32 x 32 block goes out through shared memory as one
+             * bulk tensor store per output: lane = row writes its 64 bytes,
+             * 16-byte chunk c of row r at c ^ ((r >> 1) & 3), the layout of
+             * the stores' 64-byte swizzle (bank-conflict free as well); rows
+             * beyond M are clipped by the store */
+            uint32_t hp[16], zp[16];
+  #pragma unroll
+            for (int u = 0; u < 16; u++) {
+              zp[u] = pack_bf16(v[2 * u], v[2 * u + 1]);
+              hp[u] = e.act == CGFD_SG_ACT_GELU ? pack_bf16(gelu(v[2 * u]), gelu(v[2 * u + 1]))
+                                                : zp[u];
+            }
+            /* the previous block's stores have read the buffer */
+            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            __syncwarp();
+            const int sw = (lane >> 1) & 3;
+  #pragma unroll
+            for (int c = 0; c < 4; c++) {
+              *reinterpret_cast<uint4 *>(ebuf + lane * 64 + ((c ^ sw) << 4)) =
+                  make_uint4(hp[4 * c], hp[4 * c + 1], hp[4 * c + 2], hp[4 * c + 3]);
+              if (e.Z)
+                *reinterpret_cast<uint4 *>(ebuf + P_EPI_BUF + lane * 64 + ((c ^ sw) << 4)) =
+                    make_uint4(zp[4 * c], zp[4 * c + 1], zp[4 * c + 2], zp[4 * c + 3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+              tma_store_2d(&tc, ebuf, col0, m0 + q * 32);
+              if (e.Z) tma_store_2d(&tz, ebuf + P_EPI_BUF, col0, m0 + q * 32);
+              asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            }
+            continue;
           }
-          /* the previous block's stores have read the buffer */
-          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          __syncwarp();
-          const int sw = (lane >> 1) & 3;
-#pragma unroll
-          for (int c = 0; c < 4; c++) {
-            *reinterpret_cast<uint4 *>(ebuf + lane * 64 + ((c ^ sw) << 4)) =
-                make_uint4(hp[4 * c], hp[4 * c + 1], hp[4 * c + 2], hp[4 * c + 3]);
-            if (e.Z)
-              *reinterpret_cast<uint4 *>(ebuf + P_EPI_BUF + lane * 64 + ((c ^ sw) << 4)) =
-                  make_uint4(zp[4 * c], zp[4 * c + 1], zp[4 * c + 2], zp[4 * c + 3]);
-          }
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncwarp();
-          if (lane == 0) {
-            tma_store_2d(&tc, ebuf, col0, m0 + q * 32);
-            if (e.Z) tma_store_2d(&tz, ebuf + P_EPI_BUF, col0, m0 + q * 32);
-            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-          }
-          continue;
-        }
-        if (row >= e.M) continue;
-        if (e.mode == CGFD_SG_OUT_BF16) {
-          store_bf16_32((__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0,
-                        e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr, v, e.act,
-                        e.N - col0);
-        } else {
-          float *C = (float *)e.C + (long long)row * e.ldc + col0;
-          if (col0 + 32 <= e.N) {
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-              reinterpret_cast<float4 *>(C)[u] =
-                  make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+          if (row >= e.M) continue;
+          if (e.mode == CGFD_SG_OUT_BF16) {
+            store_bf16_32((__nv_bfloat16 *)e.C + (long long)row * e.ldc + col0,
+                          e.Z ? e.Z + (long long)row * e.ldc + col0 : nullptr, v, e.act,
+                          e.N - col0);
           } else {
-#pragma unroll
-            for (int u = 0; u < 32; u++)
-              if (col0 + u < e.N) C[u] = v[u];
+            float *C = (float *)e.C + (long long)row * e.ldc + col0;
+            if (col0 + 32 <= e.N) {
+  #pragma unroll
+              for (int u = 0; u < 8; u++)
+                reinterpret_cast<float4 *>(C)[u] =
+                    make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+            } else {
+  #pragma unroll
+              for (int u = 0; u < 32; u++)
+                if (col0 + u < e.N) C[u] = v[u];
+            }
           }
         }
       }
