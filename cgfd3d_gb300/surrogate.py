@@ -3,7 +3,7 @@
 No counterpart in the reference, which runs the solver once per shot
 (forward/main_curv_col_el_3d.c:849-858).  For a fixed model and receiver
 set, a small network predicts the receivers' velocity seismograms of a shot
-from its source position and moment tensor; the solver stays the judge and
+from its source position and moment tensor; the solver checks it and stays
 the fallback.
 
 Network (device work in cgfd_sg.cu and cgfd_sg_gemm.cu; this module
