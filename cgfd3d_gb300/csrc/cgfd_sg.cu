@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 
 #include "../../include/cgfd3d_gpu.h"
@@ -107,6 +108,72 @@ __global__ void k_im2col_up(const bf16 *__restrict__ X, int B, int Tin, int C, i
     const int tt = t + j - h;
     A[i] = (tt >= 0 && tt < Tout) ? X[((long long)b * Tin + tt / up) * C + c]
                                   : __float2bfloat16_rn(0.0f);
+  }
+}
+
+/* k_im2col_up with 8 channels (16 bytes) per thread, 32-bit index math:
+ * C % 8 == 0, 16-byte aligned X and A, fewer than 2^31 output vectors */
+__global__ void k_im2col_up_v(const uint4 *__restrict__ X, int B, int Tin, int C8, int up,
+                              int ks, uint4 *__restrict__ A)
+{
+  const int Tout = Tin * up, h = ks / 2;
+  const unsigned segs = (unsigned)(ks * C8);
+  const unsigned n = (unsigned)B * (unsigned)Tout * segs;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned row = i / segs, sg = i - row * segs;
+    const int j = (int)(sg / (unsigned)C8), c8 = (int)(sg - (unsigned)j * C8);
+    const int b = (int)(row / (unsigned)Tout), t = (int)(row - (unsigned)b * Tout);
+    const int tt = t + j - h;
+    A[i] = (tt >= 0 && tt < Tout) ? X[((size_t)b * Tin + tt / up) * C8 + c8]
+                                  : make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+__device__ __forceinline__ void acc_bf16x8(float *acc, const uint4 v)
+{
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    acc[2 * u] += __uint_as_float(w[u] << 16);
+    acc[2 * u + 1] += __uint_as_float(w[u] & 0xffff0000u);
+  }
+}
+
+/* k_col2im_up_gelu with 8 channels (16 bytes) per thread, the same
+ * summation order per channel (bit-identical): C % 8 == 0, 16-byte aligned
+ * arrays, fewer than 2^31 output vectors */
+__global__ void k_col2im_up_gelu_v(const uint4 *__restrict__ dA, int B, int Tin, int C8, int up,
+                                   int ks, const uint4 *__restrict__ Z, uint4 *__restrict__ dZ)
+{
+  const int Tout = Tin * up, h = ks / 2;
+  const unsigned n = (unsigned)B * (unsigned)Tin * (unsigned)C8;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned r = i / (unsigned)C8;
+    const int c8 = (int)(i - r * (unsigned)C8);
+    const int b = (int)(r / (unsigned)Tin), s = (int)(r - (unsigned)b * Tin);
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int tt = s * up; tt < s * up + up; tt++)
+      for (int j = 0; j < ks; j++) {
+        const int t = tt - j + h;
+        if (t < 0 || t >= Tout) continue;
+        acc_bf16x8(acc, dA[(((size_t)b * Tout + t) * ks + j) * C8 + c8]);
+      }
+    if (Z) {
+      const uint4 z = Z[i];
+      const uint32_t w[4] = {z.x, z.y, z.z, z.w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        acc[2 * u] *= gelu_grad(__uint_as_float(w[u] << 16));
+        acc[2 * u + 1] *= gelu_grad(__uint_as_float(w[u] & 0xffff0000u));
+      }
+    }
+    uint32_t o[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      __nv_bfloat162 p2 = __floats2bfloat162_rn(acc[2 * u], acc[2 * u + 1]);
+      o[u] = *reinterpret_cast<uint32_t *>(&p2);
+    }
+    dZ[i] = make_uint4(o[0], o[1], o[2], o[3]);
   }
 }
 
@@ -227,6 +294,35 @@ __global__ void k_transpose(const bf16 *__restrict__ X, int rows, int cols, long
   }
 }
 
+/* k_transpose for whole 64 x 64 tiles with 16-byte loads and stores (rows
+ * and cols multiples of 64, ldx and ldy multiples of 8, 16-byte aligned):
+ * a warp reads 32 rows' 16-byte chunks into shared memory, then each lane
+ * gathers one output row's 8 values from a tile column (consecutive lanes,
+ * consecutive columns: no bank conflicts) and stores them as 16 bytes */
+__global__ void __launch_bounds__(256) k_transpose64(const bf16 *__restrict__ X, long long ldx,
+                                                     bf16 *__restrict__ Y, long long ldy)
+{
+  __shared__ __align__(16) unsigned short tile[64][72];
+  const int c0 = blockIdx.x * 64, r0 = blockIdx.y * 64, t = threadIdx.x;
+#pragma unroll
+  for (int p = 0; p < 2; p++) {
+    const int rr = (t >> 3) + 32 * p, q = t & 7;
+    *reinterpret_cast<uint4 *>(&tile[rr][8 * q]) =
+        *reinterpret_cast<const uint4 *>(X + (long long)(r0 + rr) * ldx + c0 + 8 * q);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int p = 0; p < 2; p++) {
+    const int cc = (t & 31) + 32 * p, q = t >> 5;   /* output row c0 + cc, rows r0 + 8q .. */
+    uint32_t w[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      w[u] = (uint32_t)tile[8 * q + 2 * u][cc] | ((uint32_t)tile[8 * q + 2 * u + 1][cc] << 16);
+    *reinterpret_cast<uint4 *>(Y + (long long)(c0 + cc) * ldy + r0 + 8 * q) =
+        make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
 /* out[c] (+)= sum over rows of X[r, c] (fp32 accumulation) */
 __global__ void k_colsum(const bf16 *__restrict__ X, long long rows, int cols, long long ld,
                          float *__restrict__ out)
@@ -288,8 +384,12 @@ extern "C" int cgfd_sg_im2col_up(const void *X, int B, int Tin, int C, int up, i
   if (!X || !A || B < 1 || Tin < 1 || C < 1 || up < 1 || ks < 1 || !(ks & 1))
     return sg_err(CGFD_EINVAL, "sg_im2col_up: B %d T %d C %d up %d ks %d", B, Tin, C, up, ks);
   const long long n = (long long)B * Tin * up * ks * C;
-  k_im2col_up<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>((const bf16 *)X, B, Tin, C, up,
-                                                               ks, (bf16 *)A);
+  if (C % 8 == 0 && !((uintptr_t)X & 15) && !((uintptr_t)A & 15) && n / 8 < (1LL << 31))
+    k_im2col_up_v<<<nblocks(n / 8, 256), 256, 0, SG_STREAM(stream)>>>(
+        (const uint4 *)X, B, Tin, C / 8, up, ks, (uint4 *)A);
+  else
+    k_im2col_up<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>((const bf16 *)X, B, Tin, C, up,
+                                                                 ks, (bf16 *)A);
   return launched("sg_im2col_up");
 }
 
@@ -298,8 +398,14 @@ extern "C" int cgfd_sg_col2im_up_gelu(const void *dA, int B, int Tin, int C, int
 {
   if (!dA || !dZ || B < 1 || Tin < 1 || C < 1 || up < 1 || ks < 1 || !(ks & 1))
     return sg_err(CGFD_EINVAL, "sg_col2im_up: B %d T %d C %d up %d ks %d", B, Tin, C, up, ks);
-  k_col2im_up_gelu<<<nblocks((long long)B * Tin * C, 256), 256, 0, SG_STREAM(stream)>>>(
-      (const bf16 *)dA, B, Tin, C, up, ks, (const bf16 *)Z, (bf16 *)dZ);
+  const long long n = (long long)B * Tin * C;
+  if (C % 8 == 0 && !((uintptr_t)dA & 15) && !((uintptr_t)dZ & 15) && !((uintptr_t)Z & 15) &&
+      n / 8 < (1LL << 31))
+    k_col2im_up_gelu_v<<<nblocks(n / 8, 256), 256, 0, SG_STREAM(stream)>>>(
+        (const uint4 *)dA, B, Tin, C / 8, up, ks, (const uint4 *)Z, (uint4 *)dZ);
+  else
+    k_col2im_up_gelu<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>(
+        (const bf16 *)dA, B, Tin, C, up, ks, (const bf16 *)Z, (bf16 *)dZ);
   return launched("sg_col2im_up");
 }
 
@@ -344,9 +450,15 @@ extern "C" int cgfd_sg_transpose(const void *X, int rows, int cols, long long ld
 {
   if (!X || !Y || rows < 1 || cols < 1 || ldx < cols || ldy < rows)
     return sg_err(CGFD_EINVAL, "sg_transpose: %d x %d (ld %lld, %lld)", rows, cols, ldx, ldy);
-  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
-  k_transpose<<<grid, block, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols, ldx,
-                                                     (bf16 *)Y, ldy);
+  if (rows % 64 == 0 && cols % 64 == 0 && ldx % 8 == 0 && ldy % 8 == 0 &&
+      !((uintptr_t)X & 15) && !((uintptr_t)Y & 15) && cols / 64 < 65536 && rows / 64 < 65536) {
+    k_transpose64<<<dim3(cols / 64, rows / 64), 256, 0, SG_STREAM(stream)>>>((const bf16 *)X, ldx,
+                                                                           (bf16 *)Y, ldy);
+  } else {
+    dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+    k_transpose<<<grid, block, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols, ldx,
+                                                       (bf16 *)Y, ldy);
+  }
   return launched("sg_transpose");
 }
 

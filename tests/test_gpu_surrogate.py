@@ -212,3 +212,57 @@ def test_c_object_predicts_as_the_python_layer():
     with pytest.raises(Exception):
         SG.Net(sur.parameters()[:-1], nrec, nt, 1.0)     # wrong parameter count
     net.close()
+
+
+@pytest.mark.parametrize("B,Tin,C", [(4, 16, 128), (2, 9, 12)])
+def test_gather_kernels_match_torch(B, Tin, C):
+    """im2col with up-sampling, its adjoint with GELU', and the transpose
+    against torch, for a shape that takes the 16-byte paths (C % 8 == 0) and
+    one that takes the scalar ones."""
+    import ctypes as C_
+    import torch
+    L = _sglib()
+    up, ks = 2, 5
+    h, Tout = ks // 2, Tin * up
+    g = torch.Generator(device="cpu").manual_seed(B * 100 + C)
+    X = torch.randn(B, Tin, C, generator=g).to(torch.bfloat16).cuda()
+    A = torch.empty(B * Tout, ks * C, dtype=torch.bfloat16, device="cuda")
+    s = C_.c_void_p(torch.cuda.current_stream().cuda_stream)
+    P = lambda t: C_.c_void_p(t.data_ptr())  # noqa: E731
+    from cgfd3d_gb300 import _lib
+    _lib.check(L.cgfd_sg_im2col_up(P(X), B, Tin, C, up, ks, P(A), s))
+    t = torch.arange(Tout, device="cuda")
+    ref = torch.zeros(B, Tout, ks, C, dtype=torch.bfloat16, device="cuda")
+    for j in range(ks):
+        tt = t + j - h
+        ok = (tt >= 0) & (tt < Tout)
+        ref[:, ok, j, :] = X[:, (tt[ok] // up), :]
+    torch.cuda.synchronize()
+    assert torch.equal(A.view(B, Tout, ks, C), ref)
+    # adjoint: <im2col(x), y> = <x, col2im(y)> (no GELU factor), and GELU'
+    dA = torch.randn(B * Tout, ks * C, generator=g).to(torch.bfloat16).cuda()
+    dZ = torch.empty(B, Tin, C, dtype=torch.bfloat16, device="cuda")
+    _lib.check(L.cgfd_sg_col2im_up_gelu(P(dA), B, Tin, C, up, ks, None, P(dZ), s))
+    ref_dz = torch.zeros(B, Tin, C, dtype=torch.float64, device="cuda")
+    d4 = dA.view(B, Tout, ks, C).double()
+    for j in range(ks):
+        tt = t + j - h
+        ok = (tt >= 0) & (tt < Tout)
+        ref_dz.index_add_(1, tt[ok] // up, d4[:, ok, j, :])
+    torch.cuda.synchronize()
+    assert torch.allclose(dZ.double(), ref_dz, rtol=1e-2, atol=1e-2)
+    Z = torch.randn(B, Tin, C, generator=g).to(torch.bfloat16).cuda()
+    dZg = torch.empty_like(dZ)
+    _lib.check(L.cgfd_sg_col2im_up_gelu(P(dA), B, Tin, C, up, ks, P(Z), P(dZg), s))
+    z = Z.double()
+    c_, a_ = 0.7978845608028654, 0.044715
+    th = torch.tanh(c_ * (z + a_ * z ** 3))
+    gp = 0.5 * (1 + th) + 0.5 * z * (1 - th * th) * c_ * (1 + 3 * a_ * z * z)
+    torch.cuda.synchronize()
+    assert torch.allclose(dZg.double(), dZ.double() * gp, rtol=2e-2, atol=2e-2)
+    # transpose of the im2col matrix (64-multiple shapes take the tiled path)
+    rows, cols = A.shape
+    Y = torch.empty(cols, rows, dtype=torch.bfloat16, device="cuda")
+    _lib.check(L.cgfd_sg_transpose(P(A), rows, cols, cols, P(Y), rows, s))
+    torch.cuda.synchronize()
+    assert torch.equal(Y, A.t())
