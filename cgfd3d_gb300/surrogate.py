@@ -372,13 +372,22 @@ class Net:
     def of(cls, sur):
         return cls(sur.parameters(), sur.lay.R // 3, sur.lay.nt, sur.scale)
 
-    def predict(self, pos, M):
+    def predict(self, pos, M, out=None):
+        """Seismograms [n, nt, 3 nrec] (into `out` when given: C-contiguous
+        float32 of that shape, e.g. pinned for a fast copy back)."""
         pos = np.ascontiguousarray(pos, dtype=np.float32)
         M = np.ascontiguousarray(M, dtype=np.float32)
         n = pos.shape[0]
         if pos.shape != (n, 3) or M.shape != (n, 6):
             raise ValueError("positions [n, 3] and moment tensors [n, 6]")
-        u = np.empty((n, self.nt, 3 * self.nrec), np.float32)
+        shape = (n, self.nt, 3 * self.nrec)
+        if out is None:
+            u = np.empty(shape, np.float32)
+        elif (not isinstance(out, np.ndarray) or out.shape != shape or out.dtype != np.float32
+              or not out.flags.c_contiguous):
+            raise ValueError("out: C-contiguous float32 array of shape %s" % (shape,))
+        else:
+            u = out
         _check(_lib_sg().cgfd_sg_net_predict(self._h, n, pos.ctypes.data, M.ctypes.data,
                                              u.ctypes.data))
         return u
