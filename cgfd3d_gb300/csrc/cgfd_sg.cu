@@ -226,6 +226,35 @@ __global__ void k_contract(const bf16 *__restrict__ G, const float *__restrict__
   }
 }
 
+/* k_contract for 8 consecutive traces per thread (16-byte loads of G, two
+ * 16-byte stores of U), the same sum per value: R % 8 == 0, aligned
+ * arrays, fewer than 2^31 output vectors */
+__global__ void k_contract_v(const uint4 *__restrict__ G, const float *__restrict__ M, int B,
+                             int Tg, int T, int R8, float scale, float4 *__restrict__ U)
+{
+  const unsigned n = (unsigned)B * (unsigned)T * (unsigned)R8;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned bt = i / (unsigned)R8;
+    const int r8 = (int)(i - bt * (unsigned)R8);
+    const int b = (int)(bt / (unsigned)T), t = (int)(bt - (unsigned)b * T);
+    const uint4 *g = G + ((size_t)b * Tg + t) * 6 * R8 + r8;
+    float u[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      const float mk = M[6 * b + k];
+      const uint4 v = g[k * R8];
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        u[2 * e] += mk * __uint_as_float(w[e] << 16);
+        u[2 * e + 1] += mk * __uint_as_float(w[e] & 0xffff0000u);
+      }
+    }
+    U[2 * (size_t)i] = make_float4(scale * u[0], scale * u[1], scale * u[2], scale * u[3]);
+    U[2 * (size_t)i + 1] = make_float4(scale * u[4], scale * u[5], scale * u[6], scale * u[7]);
+  }
+}
+
 /* Training form of k_contract with the relative L2 misfit: per shot
  * err[b] += sum (u - Utrue)^2 (err zeroed by the caller), and the gradient of
  * loss = (1/B) sum_b err_b / norm_b:  dG[b, t, k, r] = M[b, k] scale 2 (u -
@@ -336,6 +365,30 @@ __global__ void k_colsum(const bf16 *__restrict__ X, long long rows, int cols, l
   atomicAdd(out + c, acc);
 }
 
+/* k_colsum for 8 columns per thread (16-byte loads), the same row chunks
+ * and order per column: cols % 8 == 0, ld % 8 == 0, aligned X */
+__global__ void k_colsum_v(const uint4 *__restrict__ X, long long rows, int cols8, long long ld8,
+                           float *__restrict__ out)
+{
+  const int c8 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c8 >= cols8) return;
+  const long long per = (rows + gridDim.y - 1) / gridDim.y;
+  const long long r0 = blockIdx.y * per, r1 = min(rows, r0 + per);
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (long long r = r0; r < r1; r++) {
+    const uint4 v = X[r * ld8 + c8];
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      acc[2 * e] += __uint_as_float(w[e] << 16);
+      acc[2 * e + 1] += __uint_as_float(w[e] & 0xffff0000u);
+    }
+  }
+  if (r1 > r0)
+#pragma unroll
+    for (int e = 0; e < 8; e++) atomicAdd(out + 8 * c8 + e, acc[e]);
+}
+
 /* AdamW step on fp32 master weights, refreshing their bf16 copy */
 __global__ void k_adamw(float *__restrict__ w, bf16 *__restrict__ w16,
                         const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
@@ -424,8 +477,13 @@ extern "C" int cgfd_sg_contract(const void *G, const float *M, int B, int Tg, in
 {
   if (!G || !M || !U || B < 1 || T < 1 || Tg < T || R < 1)
     return sg_err(CGFD_EINVAL, "sg_contract: B %d Tg %d T %d R %d", B, Tg, T, R);
-  k_contract<<<nblocks((long long)B * T * R, 256), 256, 0, SG_STREAM(stream)>>>(
-      (const bf16 *)G, M, B, Tg, T, R, scale, U);
+  const long long n = (long long)B * T * R;
+  if (R % 8 == 0 && !((uintptr_t)G & 15) && !((uintptr_t)U & 15) && n / 8 < (1LL << 31))
+    k_contract_v<<<nblocks(n / 8, 256), 256, 0, SG_STREAM(stream)>>>(
+        (const uint4 *)G, M, B, Tg, T, R / 8, scale, (float4 *)U);
+  else
+    k_contract<<<nblocks(n, 256), 256, 0, SG_STREAM(stream)>>>((const bf16 *)G, M, B, Tg, T, R,
+                                                                scale, U);
   return launched("sg_contract");
 }
 
@@ -467,11 +525,17 @@ extern "C" int cgfd_sg_colsum(const void *X, long long rows, int cols, long long
 {
   if (!X || !out || rows < 1 || cols < 1 || ld < cols)
     return sg_err(CGFD_EINVAL, "sg_colsum: %lld x %d", rows, cols);
-  const int bx = (cols + 127) / 128;
   long long by = (rows + 511) / 512;
   if (by > 1024) by = 1024;
-  k_colsum<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols,
-                                                                   ld, out);
+  if (cols % 8 == 0 && ld % 8 == 0 && !((uintptr_t)X & 15)) {
+    const int bx = (cols / 8 + 127) / 128;
+    k_colsum_v<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const uint4 *)X, rows,
+                                                                       cols / 8, ld / 8, out);
+  } else {
+    const int bx = (cols + 127) / 128;
+    k_colsum<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols,
+                                                                     ld, out);
+  }
   return launched("sg_colsum");
 }
 
