@@ -365,30 +365,6 @@ __global__ void k_colsum(const bf16 *__restrict__ X, long long rows, int cols, l
   atomicAdd(out + c, acc);
 }
 
-/* k_colsum for 8 columns per thread (16-byte loads), the same row chunks
- * and order per column: cols % 8 == 0, ld % 8 == 0, aligned X */
-__global__ void k_colsum_v(const uint4 *__restrict__ X, long long rows, int cols8, long long ld8,
-                           float *__restrict__ out)
-{
-  const int c8 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c8 >= cols8) return;
-  const long long per = (rows + gridDim.y - 1) / gridDim.y;
-  const long long r0 = blockIdx.y * per, r1 = min(rows, r0 + per);
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  for (long long r = r0; r < r1; r++) {
-    const uint4 v = X[r * ld8 + c8];
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-    for (int e = 0; e < 4; e++) {
-      acc[2 * e] += __uint_as_float(w[e] << 16);
-      acc[2 * e + 1] += __uint_as_float(w[e] & 0xffff0000u);
-    }
-  }
-  if (r1 > r0)
-#pragma unroll
-    for (int e = 0; e < 8; e++) atomicAdd(out + 8 * c8 + e, acc[e]);
-}
-
 /* AdamW step on fp32 master weights, refreshing their bf16 copy */
 __global__ void k_adamw(float *__restrict__ w, bf16 *__restrict__ w16,
                         const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
@@ -525,17 +501,11 @@ extern "C" int cgfd_sg_colsum(const void *X, long long rows, int cols, long long
 {
   if (!X || !out || rows < 1 || cols < 1 || ld < cols)
     return sg_err(CGFD_EINVAL, "sg_colsum: %lld x %d", rows, cols);
+  const int bx = (cols + 127) / 128;
   long long by = (rows + 511) / 512;
   if (by > 1024) by = 1024;
-  if (cols % 8 == 0 && ld % 8 == 0 && !((uintptr_t)X & 15)) {
-    const int bx = (cols / 8 + 127) / 128;
-    k_colsum_v<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const uint4 *)X, rows,
-                                                                       cols / 8, ld / 8, out);
-  } else {
-    const int bx = (cols + 127) / 128;
-    k_colsum<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols,
-                                                                     ld, out);
-  }
+  k_colsum<<<dim3(bx, (unsigned)by), 128, 0, SG_STREAM(stream)>>>((const bf16 *)X, rows, cols,
+                                                                   ld, out);
   return launched("sg_colsum");
 }
 
