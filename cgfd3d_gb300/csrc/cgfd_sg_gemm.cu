@@ -413,8 +413,10 @@ __global__ void __launch_bounds__(NTHREADS, 2)
  * TMEM columns alternate between
  * tiles: the MMAs of tile i+1 run while the epilogue reads tile i
  * (tfull[a]: the MMAs of a tile are done; tempty[a]: its accumulator has
- * been read).  The smem ring runs on across tiles.  Stores as k_gemm_tn
- * (bf16 or fp32, no split along K). */
+ * been read).  The smem ring runs on across tiles.  Outputs: bf16 blocks of
+ * 32 x 32 leave through shared memory by bulk tensor stores (tc, tz; rows
+ * past M clipped), ragged bf16 blocks and fp32 outputs by the threads' own
+ * stores; no split along K. */
 constexpr int PSTAGES = 4;
 constexpr int P_STAGE = 2 * TILE_A + TILE_B; /* 48 KiB (TILE_A == TILE_B) */
 /* epilogue staging, per epilogue warp: 32 rows x 64 B of C and of Z */
