@@ -584,6 +584,7 @@ def run_batch(args):
                             base_model=base, seed=3000 + 1009 * rank)
     t0 = time.perf_counter()
     be = solver.Batch(q, kchunk=tune["kchunk"])
+    be.set_schedule(tune.get("persistent", 0))
     be.run(K)
     be.fetch()
     be.close()
@@ -609,7 +610,10 @@ def run_batch(args):
                    "moment tensors, Ricker 2 Hz, 64 receivers each"
                    % (args.nshot, args.ni, args.nj, args.nk),
                    "points_per_gpu": pts, "kchunk": tune["kchunk"],
+                   "schedule": "persistent CTAs, items largest first"
+                               if tune.get("persistent", 0) else "one CTA per item",
                    "autotune_ms": tune["ms"],
+                   "autotune_ms_persistent": tune.get("ms_persistent"),
                    "parallelism": "shots sharded" if world > 1 else "single",
                    "l2": "inputs far larger than L2, no flush"},
         "sequential": {"value": seq_shots_per_s, "unit": "shots/s",

@@ -93,6 +93,11 @@ def lib():
     L.cgfd_batch_set_kchunk.argtypes = [vp, C.c_int]
     L.cgfd_batch_autotune.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.c_int,
                                       C.POINTER(C.c_float), C.POINTER(C.c_int)]
+    L.cgfd_batch_set_schedule.argtypes = [vp, C.c_int]
+    L.cgfd_batch_schedule.argtypes = [vp]
+    L.cgfd_batch_autotune_schedule.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.c_int,
+                                               C.POINTER(C.c_float), C.POINTER(C.c_int),
+                                               C.POINTER(C.c_int)]
     L.cgfd_batch_shot.argtypes = [vp, C.c_int]
     L.cgfd_batch_shot.restype = vp
     L.cgfd_batch_destroy.argtypes = [vp]

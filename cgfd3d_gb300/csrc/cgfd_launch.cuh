@@ -61,41 +61,42 @@ static void launch_stage_med(int code, int kind, dim3 grid, cudaStream_t st,
 
 #if CGFD_BATCH
 template <int BX, int BY, int BZ, int KIND, int MED>
-static void launch_batch_t(int nctas, cudaStream_t st, const StageArgs *args,
-                           const s3::ShotGeo *geo, int nshot)
+static void launch_batch_t(int grid, cudaStream_t st, const StageArgs *args,
+                           const s3::ShotGeo *geo, int nshot, const BatchSched &w)
 {
   constexpr int smem = s3::Slot<MED>::SMEM_BYTES;
-  if (nctas <= 0) {   /* preparation only: set the shared-memory attribute */
+  if (grid <= 0) {   /* preparation only: set the shared-memory attribute */
     cudaFuncSetAttribute(s3::k_stage3_batch<BX, BY, BZ, KIND, MED>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     return;
   }
-  s3::k_stage3_batch<BX, BY, BZ, KIND, MED><<<nctas, s3::NTHREADS, smem, st>>>(
-      args, geo, nshot);
+  s3::k_stage3_batch<BX, BY, BZ, KIND, MED><<<grid, s3::NTHREADS, smem, st>>>(
+      args, geo, nshot, w.order, w.nitems, w.next);
 }
 
 template <int BX, int BY, int BZ, int MED>
-static void launch_batch_k(int kind, int nctas, cudaStream_t st, const StageArgs *args,
-                           const s3::ShotGeo *geo, int nshot)
+static void launch_batch_k(int kind, int grid, cudaStream_t st, const StageArgs *args,
+                           const s3::ShotGeo *geo, int nshot, const BatchSched &w)
 {
-  if (kind == 0) launch_batch_t<BX, BY, BZ, 0, MED>(nctas, st, args, geo, nshot);
-  else if (kind == 1) launch_batch_t<BX, BY, BZ, 1, MED>(nctas, st, args, geo, nshot);
-  else launch_batch_t<BX, BY, BZ, 2, MED>(nctas, st, args, geo, nshot);
+  if (kind == 0) launch_batch_t<BX, BY, BZ, 0, MED>(grid, st, args, geo, nshot, w);
+  else if (kind == 1) launch_batch_t<BX, BY, BZ, 1, MED>(grid, st, args, geo, nshot, w);
+  else launch_batch_t<BX, BY, BZ, 2, MED>(grid, st, args, geo, nshot, w);
 }
 
 template <int MED>
-static void launch_batch_med(int code, int kind, int nctas, cudaStream_t st,
-                             const StageArgs *args, const s3::ShotGeo *geo, int nshot)
+static void launch_batch_med(int code, int kind, int grid, cudaStream_t st,
+                             const StageArgs *args, const s3::ShotGeo *geo, int nshot,
+                             const BatchSched &w)
 {
   switch (code) {
-    case 0: launch_batch_k<0, 0, 0, MED>(kind, nctas, st, args, geo, nshot); break;
-    case 1: launch_batch_k<0, 0, 1, MED>(kind, nctas, st, args, geo, nshot); break;
-    case 2: launch_batch_k<0, 1, 0, MED>(kind, nctas, st, args, geo, nshot); break;
-    case 3: launch_batch_k<0, 1, 1, MED>(kind, nctas, st, args, geo, nshot); break;
-    case 4: launch_batch_k<1, 0, 0, MED>(kind, nctas, st, args, geo, nshot); break;
-    case 5: launch_batch_k<1, 0, 1, MED>(kind, nctas, st, args, geo, nshot); break;
-    case 6: launch_batch_k<1, 1, 0, MED>(kind, nctas, st, args, geo, nshot); break;
-    default: launch_batch_k<1, 1, 1, MED>(kind, nctas, st, args, geo, nshot); break;
+    case 0: launch_batch_k<0, 0, 0, MED>(kind, grid, st, args, geo, nshot, w); break;
+    case 1: launch_batch_k<0, 0, 1, MED>(kind, grid, st, args, geo, nshot, w); break;
+    case 2: launch_batch_k<0, 1, 0, MED>(kind, grid, st, args, geo, nshot, w); break;
+    case 3: launch_batch_k<0, 1, 1, MED>(kind, grid, st, args, geo, nshot, w); break;
+    case 4: launch_batch_k<1, 0, 0, MED>(kind, grid, st, args, geo, nshot, w); break;
+    case 5: launch_batch_k<1, 0, 1, MED>(kind, grid, st, args, geo, nshot, w); break;
+    case 6: launch_batch_k<1, 1, 0, MED>(kind, grid, st, args, geo, nshot, w); break;
+    default: launch_batch_k<1, 1, 1, MED>(kind, grid, st, args, geo, nshot, w); break;
   }
 }
 #endif
@@ -136,12 +137,13 @@ void CGFD_CAT(cgfd_launch_stage_, CGFD_MED_NAME)(int code, int kind, dim3 grid,
 #endif
 
 #if CGFD_BATCH
-void CGFD_CAT(cgfd_launch_stage_batch_, CGFD_MED_NAME)(int code, int kind, int nctas,
+void CGFD_CAT(cgfd_launch_stage_batch_, CGFD_MED_NAME)(int code, int kind, int grid,
                                                        cudaStream_t st,
                                                        const StageArgs *args,
-                                                       const s3::ShotGeo *geo, int nshot)
+                                                       const s3::ShotGeo *geo, int nshot,
+                                                       const BatchSched &w)
 {
-  launch_batch_med<CGFD_MED>(code, kind, nctas, st, args, geo, nshot);
+  launch_batch_med<CGFD_MED>(code, kind, grid, st, args, geo, nshot, w);
 }
 
 /* tile rows the batched kernel was compiled with: must equal the single

@@ -35,16 +35,26 @@ void cgfd_launch_stage_vis(int code, int kind, dim3 grid, cudaStream_t st,
 void cgfd_launch_stage_ani(int code, int kind, dim3 grid, cudaStream_t st,
                            const StageArgs &a, const StageMaps &m);
 
-/* the stage of a batch of shots in one launch of `nctas` CTAs (per-shot
+/* work items of a batched stage launch: nitems (shot, tile, k chunk)
+ * items; next == null: one CTA per item; otherwise persistent CTAs take
+ * items in the order of order[] from the counter *next (zeroed before the
+ * launch) */
+struct BatchSched {
+  const int *order;
+  int nitems;
+  int *next;
+};
+
+/* the stage of a batch of shots in one launch of `grid` CTAs (per-shot
  * arguments and tensor maps in device memory); isotropic and VTI media.
- * nctas <= 0 only sets the kernel's shared-memory attribute (done for every
+ * grid <= 0 only sets the kernel's shared-memory attribute (done for every
  * form before a CUDA graph is captured). */
-void cgfd_launch_stage_batch_iso(int code, int kind, int nctas, cudaStream_t st,
+void cgfd_launch_stage_batch_iso(int code, int kind, int grid, cudaStream_t st,
                                  const StageArgs *args, const s3::ShotGeo *geo,
-                                 int nshot);
-void cgfd_launch_stage_batch_vti(int code, int kind, int nctas, cudaStream_t st,
+                                 int nshot, const BatchSched &w);
+void cgfd_launch_stage_batch_vti(int code, int kind, int grid, cudaStream_t st,
                                  const StageArgs *args, const s3::ShotGeo *geo,
-                                 int nshot);
+                                 int nshot, const BatchSched &w);
 
 /* CFS-PML face kernel of face f (normal dim, operator bias b), n points */
 void cgfd_launch_pml_iso(int dim, int b, int kind, int f, long long n,

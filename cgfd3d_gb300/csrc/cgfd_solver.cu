@@ -2420,6 +2420,11 @@ struct cgfd_batch {
   RecvJob *d_recv = nullptr;      /* [parity][shot] */
   PgJob *d_pg = nullptr;          /* [parity][shot] */
   int nctas = 0, pg_any = 0, max_ni = 0, max_nj = 0;
+  /* schedule of the stage launches: 0 one CTA per (shot, tile, k chunk)
+   * item, 1 persistent CTAs (one per SM) taking the items largest first */
+  int persistent = 0, pgrid = 0;
+  int *d_order = nullptr;         /* items, largest first */
+  int *d_next = nullptr;          /* the persistent launches' item counter */
   cudaGraphExec_t graph = nullptr;
   int graph_par = -1;
   int use_graph = 1;
@@ -2430,10 +2435,11 @@ struct cgfd_batch {
 
 static void batch_free_tables(cgfd_batch_t *b)
 {
-  void *ptrs[] = {b->d_args, b->d_geo, b->d_recv, b->d_pg};
+  void *ptrs[] = {b->d_args, b->d_geo, b->d_recv, b->d_pg, b->d_order, b->d_next};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   b->d_args = nullptr; b->d_geo = nullptr; b->d_recv = nullptr; b->d_pg = nullptr;
+  b->d_order = nullptr; b->d_next = nullptr;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
   b->graph_par = -1;
@@ -2485,6 +2491,29 @@ static int batch_tables(cgfd_batch_t *b)
     b->max_nj = std::max(b->max_nj, s->g.nj);
   }
   b->nctas = cta;
+  /* the persistent schedule's item order: most points x planes first, so
+   * that the short edge tiles and chunks fill the end of the launch */
+  std::vector<int> order(cta);
+  std::vector<long long> cost(cta);
+  for (int k = 0; k < n; k++) {
+    const cgfd_solver_t *s = b->sv[k];
+    const s3::ShotGeo &G = geo[k];
+    const int nitem = G.tiles_x * G.tiles_y * G.nchunk;
+    for (int c = 0; c < nitem; c++) {
+      const int bx = c % G.tiles_x, by = (c / G.tiles_x) % G.tiles_y,
+                bz = c / (G.tiles_x * G.tiles_y);
+      const long long wi = std::min(s2::TX, s->g.ni - bx * s2::TX);
+      const long long wj = std::min(s->ty, s->g.nj - by * s->ty);
+      const long long wk = std::min(b->kchunk, s->g.nk - bz * b->kchunk);
+      cost[G.cta0 + c] = wi * wj * wk;
+    }
+  }
+  for (int c = 0; c < cta; c++) order[c] = c;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return cost[x] > cost[y]; });
+  CK(cudaMalloc((void **)&b->d_order, (size_t)cta * sizeof(int)));
+  CK(cudaMalloc((void **)&b->d_next, sizeof(int)));
+  CK(cudaMemcpy(b->d_order, order.data(), (size_t)cta * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMalloc((void **)&b->d_args, args.size() * sizeof(StageArgs)));
   CK(cudaMalloc((void **)&b->d_geo, geo.size() * sizeof(s3::ShotGeo)));
   CK(cudaMalloc((void **)&b->d_recv, rj.size() * sizeof(RecvJob)));
@@ -2566,11 +2595,21 @@ extern "C" int cgfd_batch_create(const cgfd_problem_t *const *shots, int nshot,
   }
   /* shared-memory attribute of every batched stage form (graph capture
    * must not be the first use) */
+  const BatchSched none = {nullptr, 0, nullptr};
   for (int code = 0; code < 8; code++)
     for (int kind = 0; kind < 3; kind++) {
-      if (b->med == MED_VTI) cgfd_launch_stage_batch_vti(code, kind, 0, b->stream, nullptr, nullptr, 0);
-      else cgfd_launch_stage_batch_iso(code, kind, 0, b->stream, nullptr, nullptr, 0);
+      if (b->med == MED_VTI) cgfd_launch_stage_batch_vti(code, kind, 0, b->stream, nullptr, nullptr, 0, none);
+      else cgfd_launch_stage_batch_iso(code, kind, 0, b->stream, nullptr, nullptr, 0, none);
     }
+  {
+    /* one persistent CTA per SM (the stage kernel's shared memory allows no
+     * more); CGFD_BATCH_PERSISTENT=1 makes it the schedule from the start */
+    int dev = 0, nsm = 0;
+    BTRYC(cudaGetDevice(&dev));
+    BTRYC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    b->pgrid = nsm;
+    if (const char *e = getenv("CGFD_BATCH_PERSISTENT")) b->persistent = atoi(e) != 0;
+  }
   BTRYC(cudaGetLastError());
   BTRY(batch_tables(b));
   *out = b;
@@ -2589,10 +2628,18 @@ static void batch_enqueue_step(cgfd_batch_t *b, int it)
     int kind = is == 0 ? 0 : (is < 3 ? 1 : 2);
     int code = bx * 4 + by * 2 + bz;
     const StageArgs *args = b->d_args + (size_t)(par * 4 + is) * n;
+    int grid = b->nctas;
+    BatchSched w = {nullptr, b->nctas, nullptr};
+    if (b->persistent) {
+      cudaMemsetAsync(b->d_next, 0, sizeof(int), b->stream);
+      grid = std::min(b->pgrid, b->nctas);
+      w.order = b->d_order;
+      w.next = b->d_next;
+    }
     if (b->med == MED_VTI)
-      cgfd_launch_stage_batch_vti(code, kind, b->nctas, b->stream, args, b->d_geo, n);
+      cgfd_launch_stage_batch_vti(code, kind, grid, b->stream, args, b->d_geo, n, w);
     else
-      cgfd_launch_stage_batch_iso(code, kind, b->nctas, b->stream, args, b->d_geo, n);
+      cgfd_launch_stage_batch_iso(code, kind, grid, b->stream, args, b->d_geo, n, w);
   }
   if (b->pg_any) {
     dim3 bl(32, 8), gr((b->max_ni + 31) / 32, (b->max_nj + 7) / 8, n);
@@ -2708,6 +2755,47 @@ extern "C" int cgfd_batch_set_kchunk(cgfd_batch_t *b, int kchunk)
   if (kchunk < 4 || kchunk > 4096) return set_err(CGFD_EINVAL, "kchunk %d out of 4..4096", kchunk);
   b->kchunk = kchunk;
   return batch_tables(b);
+}
+
+extern "C" int cgfd_batch_set_schedule(cgfd_batch_t *b, int persistent)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  b->persistent = persistent ? 1 : 0;
+  if (b->graph) cudaGraphExecDestroy(b->graph);   /* captured with the old schedule */
+  b->graph = nullptr;
+  b->graph_par = -1;
+  return 0;
+}
+
+extern "C" int cgfd_batch_schedule(const cgfd_batch_t *b) { return b ? b->persistent : -1; }
+
+extern "C" int cgfd_batch_autotune_schedule(cgfd_batch_t *b, const int *cand, int ncand,
+                                            int steps, float *ms_out, int *best_kchunk,
+                                            int *best_persistent)
+{
+  if (!b) return set_err(CGFD_EINVAL, "null batch");
+  if (!cand || ncand < 1 || steps < 1 || steps > b->nt_total || !best_kchunk ||
+      !best_persistent)
+    return set_err(CGFD_EINVAL, "autotune: bad candidates or steps");
+  float tbest = 0.f;
+  int kbest = b->kchunk, pbest = b->persistent, first = 1;
+  for (int sch = 0; sch < 2; sch++)
+    for (int c = 0; c < ncand; c++) {
+      int rc = cgfd_batch_set_schedule(b, sch);
+      if (!rc) rc = cgfd_batch_set_kchunk(b, cand[c]);
+      if (!rc) rc = cgfd_batch_run(b, 1);         /* warm-up step */
+      if (!rc) rc = cgfd_batch_run(b, steps < b->nt_total ? steps : b->nt_total - 1);
+      if (rc) return rc;
+      const float t = b->t_ms;
+      if (ms_out) ms_out[sch * ncand + c] = t;
+      if (first || t < tbest) { tbest = t; kbest = cand[c]; pbest = sch; first = 0; }
+      rc = cgfd_batch_reset(b);
+      if (rc) return rc;
+    }
+  *best_kchunk = kbest;
+  *best_persistent = pbest;
+  int rc = cgfd_batch_set_schedule(b, pbest);
+  return rc ? rc : cgfd_batch_set_kchunk(b, kbest);
 }
 
 extern "C" int cgfd_batch_autotune(cgfd_batch_t *b, const int *cand, int ncand, int steps,

@@ -48,6 +48,12 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
                : "memory");
 }
 
+/* the barrier's memory may be initialised again (after every use has ended) */
+__device__ __forceinline__ void mbar_inval(uint64_t *bar)
+{
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
 {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(

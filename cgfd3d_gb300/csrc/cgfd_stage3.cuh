@@ -226,7 +226,8 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
                                             const CUtensorMap &tmap_med,
                                             const CUtensorMap &tmap_pt,
                                             const CUtensorMap &tmap_j,
-                                            int bx, int by, int bz, bool gmem_maps)
+                                            int bx, int by, int bz, bool gmem_maps,
+                                            bool again = false)
 {
   using L = Slot<MED>;
   constexpr int S_MET = L::S_MET, S_MED = L::S_MED, S_JC = L::S_JC,
@@ -253,6 +254,12 @@ __device__ __forceinline__ void stage3_body(const StageArgs &a,
   const int pbase = kbeg + ZS0;       /* plane of ring index 0 */
 
   if (threadIdx.x == 0) {
+    if (again) {
+      /* a persistent CTA's next item: the previous one's barriers have no
+       * operation left (the caller synchronised after it) */
+      for (int b = 0; b < NB; b++) { mbar_inval(&full_w[b]); mbar_inval(&empty_w[b]); }
+      for (int b = 0; b < NS; b++) { mbar_inval(&full_s[b]); mbar_inval(&empty_s[b]); }
+    }
     for (int b = 0; b < NB; b++) { mbar_init(&full_w[b], 1); mbar_init(&empty_w[b], NCW); }
     for (int b = 0; b < NS; b++) { mbar_init(&full_s[b], 1); mbar_init(&empty_s[b], NCW); }
     abort_s = 0;
@@ -730,45 +737,72 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 }
 
 /* The same stage for a batch of independent shots in one launch: a 1-D
- * grid over every shot's CTAs, shot s owning [geo[s].cta0, geo[s+1].cta0);
- * each CTA reads its shot's arguments and tensor maps from global memory.
- * All shots share the step's operator biases and RK stage. */
+ * index space over every shot's CTAs, shot s owning [geo[s].cta0,
+ * geo[s+1].cta0); each item reads its shot's arguments and tensor maps from
+ * global memory.  All shots share the step's operator biases and RK stage.
+ *
+ * Two schedules.  next == null: one CTA per item (grid = nitems), item =
+ * blockIdx.x.  next != null: persistent -- a CTA per SM takes items from
+ * the global counter *next (zeroed before the launch) in the order of
+ * order[] (largest first), runs the stage body on each, re-initialising its
+ * barriers between items, and stops after its shot's error word is set. */
 template <int BX, int BY, int BZ, int KIND, int MED>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_stage3_batch(const StageArgs *__restrict__ args,
-                   const ShotGeo *__restrict__ geo, int nshot)
+                   const ShotGeo *__restrict__ geo, int nshot,
+                   const int *__restrict__ order, int nitems, int *next)
 {
-  int lo = 0, hi = nshot - 1;
-  const int cta = (int)blockIdx.x;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (geo[mid].cta0 <= cta) lo = mid; else hi = mid - 1;
-  }
-  const ShotGeo &G = geo[lo];
-  int c = cta - G.cta0;
-  const int bx = c % G.tiles_x;
-  c /= G.tiles_x;
-  const int by = c % G.tiles_y;
-  const int bz = c / G.tiles_y;
   /* the shot's arguments in shared memory where the CTA's 227 KB allow
    * it: the stage reads them all through its loops, and shared loads are
    * cheaper than re-reading global memory.  The body reads the tile
    * geometry from them before its own first barrier, so the copy
-   * completes here. */
+   * completes first. */
   constexpr bool kArgsInSmem =
       Slot<MED>::SMEM_BYTES + (int)sizeof(StageArgs) + 256 <= 232448;
-  if constexpr (kArgsInSmem) {
-    __shared__ __align__(16) StageArgs sa;
-    const int n4 = (int)(sizeof(StageArgs) / 4);
-    const uint32_t *src = reinterpret_cast<const uint32_t *>(args + lo);
-    uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
-    for (int t = threadIdx.x; t < n4; t += blockDim.x) dst[t] = src[t];
+  __shared__ int item_s;
+  int shot_cur = -1;
+  for (int round = 0;; round++) {
+    if (next) {
+      if (threadIdx.x == 0) {
+        const bool stop = round > 0 && *(volatile const int *)args[shot_cur].err != 0;
+        item_s = stop ? nitems : atomicAdd(next, 1);
+      }
+      __syncthreads();
+    } else if (round > 0) {
+      break;
+    }
+    const int w = next ? item_s : (int)blockIdx.x;
+    if (w >= nitems) break;
+    const int cta = order ? order[w] : w;
+    int lo = 0, hi = nshot - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (geo[mid].cta0 <= cta) lo = mid; else hi = mid - 1;
+    }
+    const ShotGeo &G = geo[lo];
+    int c = cta - G.cta0;
+    const int bx = c % G.tiles_x;
+    c /= G.tiles_x;
+    const int by = c % G.tiles_y;
+    const int bz = c / G.tiles_y;
+    if constexpr (kArgsInSmem) {
+      __shared__ __align__(16) StageArgs sa;
+      if (lo != shot_cur) {
+        const int n4 = (int)(sizeof(StageArgs) / 4);
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(args + lo);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
+        for (int t = threadIdx.x; t < n4; t += blockDim.x) dst[t] = src[t];
+      }
+      __syncthreads();
+      stage3_body<BX, BY, BZ, KIND, MED>(sa, G.wav, G.met, G.med, G.pt, G.j, bx, by,
+                                         bz, true, round > 0);
+    } else {
+      stage3_body<BX, BY, BZ, KIND, MED>(args[lo], G.wav, G.met, G.med, G.pt, G.j,
+                                         bx, by, bz, true, round > 0);
+    }
+    shot_cur = lo;
+    /* every thread is done with the item, its barriers and its arguments */
     __syncthreads();
-    stage3_body<BX, BY, BZ, KIND, MED>(sa, G.wav, G.met, G.med, G.pt, G.j, bx, by,
-                                       bz, true);
-  } else {
-    stage3_body<BX, BY, BZ, KIND, MED>(args[lo], G.wav, G.met, G.med, G.pt, G.j,
-                                       bx, by, bz, true);
   }
 }
 

@@ -265,9 +265,18 @@ class Batch:
     def set_kchunk(self, kchunk):
         _lib.check(_lib.lib().cgfd_batch_set_kchunk(self._h, int(kchunk)))
 
-    def autotune(self, candidates=(8, 12, 16, 24, 32), steps=2, cache=None, key=None):
-        """Pick k planes per CTA by timing `steps` steps per candidate; with
-        `cache` (a JSON file path) and `key`, reuse or record the choice."""
+    def set_schedule(self, persistent):
+        """0: one CTA per (shot, tile, k chunk) item; 1: persistent CTAs."""
+        _lib.check(_lib.lib().cgfd_batch_set_schedule(self._h, int(bool(persistent))))
+
+    def schedule(self):
+        return int(_lib.lib().cgfd_batch_schedule(self._h))
+
+    def autotune(self, candidates=(8, 12, 16, 24, 32), steps=2, cache=None, key=None,
+                 schedules=True):
+        """Pick k planes per CTA (and, with `schedules`, the launch schedule)
+        by timing `steps` steps per candidate; with `cache` (a JSON file
+        path) and `key`, reuse or record the choice."""
         import json
         import os
         if cache and key and os.path.exists(cache):
@@ -276,16 +285,28 @@ class Batch:
                     got = json.load(f).get(key)
                 if got:
                     self.set_kchunk(got["kchunk"])
+                    self.set_schedule(got.get("persistent", 0))
                     return got
             except (OSError, ValueError):
                 pass
         cand = (C.c_int * len(candidates))(*candidates)
-        ms = (C.c_float * len(candidates))()
         best = C.c_int()
-        _lib.check(_lib.lib().cgfd_batch_autotune(self._h, cand, len(candidates),
-                                                   int(steps), ms, C.byref(best)))
-        res = {"kchunk": best.value, "candidates": list(candidates),
-               "ms": [float(v) for v in ms], "steps": int(steps)}
+        if schedules:
+            ms = (C.c_float * (2 * len(candidates)))()
+            pbest = C.c_int()
+            _lib.check(_lib.lib().cgfd_batch_autotune_schedule(
+                self._h, cand, len(candidates), int(steps), ms, C.byref(best), C.byref(pbest)))
+            n = len(candidates)
+            res = {"kchunk": best.value, "persistent": pbest.value,
+                   "candidates": list(candidates), "ms": [float(v) for v in ms[:n]],
+                   "ms_persistent": [float(v) for v in ms[n:]], "steps": int(steps)}
+        else:
+            ms = (C.c_float * len(candidates))()
+            _lib.check(_lib.lib().cgfd_batch_autotune(self._h, cand, len(candidates),
+                                                       int(steps), ms, C.byref(best)))
+            res = {"kchunk": best.value, "persistent": self.schedule(),
+                   "candidates": list(candidates), "ms": [float(v) for v in ms],
+                   "steps": int(steps)}
         if cache and key:
             data = {}
             try:

@@ -527,6 +527,18 @@ int cgfd_batch_set_kchunk(cgfd_batch_t *b, int kchunk);
 int cgfd_batch_autotune(cgfd_batch_t *b, const int *cand, int ncand, int steps,
                         float *ms, int *best);
 
+/* Schedule of the batched stage launches: 0 (default) one CTA per (shot,
+ * tile, k chunk) item; 1 persistent, one CTA per SM taking the items
+ * largest first (most points x planes) from a device counter, re-using its
+ * shared memory and barriers from item to item.  Results are the same. */
+int cgfd_batch_set_schedule(cgfd_batch_t *b, int persistent);
+int cgfd_batch_schedule(const cgfd_batch_t *b);   /* -1 for a null batch */
+
+/* cgfd_batch_autotune over both schedules: ms[s * ncand + c] the time of
+ * candidate c under schedule s; the fastest (kchunk, schedule) is kept. */
+int cgfd_batch_autotune_schedule(cgfd_batch_t *b, const int *cand, int ncand, int steps,
+                                 float *ms, int *best_kchunk, int *best_persistent);
+
 /* The solver of shot k (for cgfd_solver_fetch_* on one shot), or NULL. */
 cgfd_solver_t *cgfd_batch_shot(cgfd_batch_t *b, int k);
 

@@ -45,15 +45,18 @@ def _same(a, b, what):
     np.testing.assert_array_equal(a, b, err_msg=what)
 
 
-@pytest.mark.parametrize("graph", ["1", "0"])
-def test_batch_equals_single_shots(base, graph, monkeypatch):
+@pytest.mark.parametrize("graph,persistent", [("1", 0), ("0", 0), ("1", 1), ("0", 1)])
+def test_batch_equals_single_shots(base, graph, persistent, monkeypatch):
     """Three windows of different sizes, 19 steps (two graph cycles and an
-    eager tail, or all eager): each shot equals its single-shot run."""
+    eager tail, or all eager), one CTA per item or persistent CTAs taking
+    the items largest first: each shot equals its single-shot run."""
     from cgfd3d_gb300 import solver
     monkeypatch.setenv("CGFD_BATCH_GRAPH", graph)
     shots = _shots(base, 3, 18, 21)
     singles = [p.copy() for p in shots]
     with solver.Batch(shots, kchunk=12) as b:
+        b.set_schedule(persistent)
+        assert b.schedule() == persistent
         b.run(3)
         b.run(16)
         b.fetch()
@@ -81,10 +84,13 @@ def test_batch_autotune_resets_state(base, tmp_path):
     with solver.Batch(shots) as b:
         res = b.autotune(candidates=(8, 16, 24), steps=2, cache=cache, key="k")
         assert res["kchunk"] in (8, 16, 24) and len(res["ms"]) == 3
+        assert res["persistent"] in (0, 1) and len(res["ms_persistent"]) == 3
+        assert b.schedule() == res["persistent"]
         b.run(shots[0].nt_total)
         b.fetch()
     with solver.Batch([p.copy() for p in singles]) as b2:
-        assert b2.autotune(cache=cache, key="k")["kchunk"] == res["kchunk"]
+        got = b2.autotune(cache=cache, key="k")
+        assert got["kchunk"] == res["kchunk"] and b2.schedule() == res["persistent"]
     for p, q in zip(shots, singles):
         solver.drv_rk_curv_col_allstep(q)
         lev = p.final_level()
