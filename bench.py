@@ -545,7 +545,8 @@ def run_batch(args):
     b = solver.Batch(probs)
     cache = os.path.join(REPO, "cgfd3d_gb300", "_build", "batch_tune.json")
     key = "iso:%d:%d" % (args.nshot, pts)
-    tune = b.autotune(candidates=(16, 24, 32, 48, 64), steps=2, cache=cache, key=key)
+    tune = b.autotune(candidates=(16, 24, 32, 48, 64, 96, 160), steps=2, cache=cache,
+                     key=key)
     b.run(W)
     sampler = ClockSampler(local)
     sampler.start()
