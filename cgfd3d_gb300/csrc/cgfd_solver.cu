@@ -2425,6 +2425,7 @@ struct cgfd_batch {
   int persistent = 0, pgrid = 0;
   int *d_order = nullptr;         /* items, largest first */
   int *d_next = nullptr;          /* the persistent launches' item counter */
+  cudaError_t enq_err = cudaSuccess;   /* first error of an enqueue call */
   cudaGraphExec_t graph = nullptr;
   int graph_par = -1;
   int use_graph = 1;
@@ -2631,7 +2632,8 @@ static void batch_enqueue_step(cgfd_batch_t *b, int it)
     int grid = b->nctas;
     BatchSched w = {nullptr, b->nctas, nullptr};
     if (b->persistent) {
-      cudaMemsetAsync(b->d_next, 0, sizeof(int), b->stream);
+      const cudaError_t e = cudaMemsetAsync(b->d_next, 0, sizeof(int), b->stream);
+      if (e != cudaSuccess && b->enq_err == cudaSuccess) b->enq_err = e;
       grid = std::min(b->pgrid, b->nctas);
       w.order = b->d_order;
       w.next = b->d_next;
@@ -2695,6 +2697,11 @@ extern "C" int cgfd_batch_run(cgfd_batch_t *b, int nsteps)
     launches += 8 * per_step;
   }
   CK(cudaGetLastError());
+  {
+    const cudaError_t e = b->enq_err;
+    b->enq_err = cudaSuccess;
+    CK(e);
+  }
   CK(cudaEventRecord(b->ev1, b->stream));
   CK(cudaEventSynchronize(b->ev1));
   CK(cudaEventElapsedTime(&b->t_ms, b->ev0, b->ev1));
