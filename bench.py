@@ -527,7 +527,7 @@ def run_batch(args):
     K timed steps of the whole batch against the same shots run one at a
     time.  Ranks shard shots (disjoint seeds), no collective until the end."""
     import torch
-    from cgfd3d_gb300 import _lib, models, shots as S, solver
+    from cgfd3d_gb300 import _lib, models, solver
     import ctypes as C
     rank, world, local = dist_env()
     if not torch.cuda.is_available():

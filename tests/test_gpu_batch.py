@@ -6,8 +6,6 @@ per-point arithmetic is the single-shot kernel's, so every shot's wavefield,
 PML auxiliaries and seismograms must equal its single-shot run exactly.
 """
 
-import os
-
 import numpy as np
 import pytest
 
